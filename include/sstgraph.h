@@ -1,0 +1,174 @@
+/*
+ * sstgraph.h -- C ABI of the GB300 dynamic-graph library (libsstgraph_gb300.so).
+ *
+ * One handle = one graph resident in one GPU's HBM: per-vertex sorted uint32
+ * neighbour sets kept as packed memory arrays, updated by batches and
+ * traversed by device kernels.  The reference's graph type on this path is
+ * SSTGraph::SparseMatrixV<true> (binary CSR, el_t = uint32_t), a header-only
+ * C++ template with no ABI; each entry point below names the reference
+ * member or call site it stands in for (paths inside the reference project).
+ *
+ * Conventions
+ *  - Every call returns an sst_status (0 = SST_OK, negative = error).  On
+ *    error, sst_last_error_message() describes it.
+ *  - `pairs` arrays are interleaved (row, col) uint32 pairs, n pairs long.
+ *  - Pointer arguments are host memory unless SST_DEVICE_PTR is set in
+ *    `flags`, in which case all array arguments of that call are device
+ *    memory of the graph's GPU.  Calls on host memory return after the work
+ *    and the copies are done; calls on device memory are ordered on the
+ *    graph's stream (sst_set_stream) and may return before the GPU finishes.
+ *  - The library never writes the caller's input arrays (the reference's
+ *    insert_batch/remove_batch sort the caller's buffer in place,
+ *    SparseMatrix.hpp:578,664; here the sort happens in device scratch).
+ *  - There is no CPU fallback: without a usable GPU the calls return
+ *    SST_EDEVICE.
+ *  - One writer at a time per handle; calls on one handle are not
+ *    thread-safe (the reference has no locks either, SparseMatrix.hpp).
+ */
+#ifndef SSTGRAPH_H
+#define SSTGRAPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t sst_status;
+#define SST_OK 0
+#define SST_EINVAL (-1)    /* bad argument (null handle, id out of range) */
+#define SST_ENOMEM (-2)    /* device allocation failed */
+#define SST_EBUDGET (-3)   /* the operation would exceed the HBM budget */
+#define SST_ETIMEDOUT (-4) /* a bounded device wait ran out */
+#define SST_EDEVICE (-5)   /* CUDA error or no usable device */
+#define SST_ESTATE (-6)    /* call not valid in the handle's state */
+
+#define SST_HOST_PTR 0u
+#define SST_DEVICE_PTR 1u
+/* accepted for source compatibility with the reference's semi_sorted
+ * argument (SparseMatrix.hpp:167-168); the device always sorts */
+#define SST_SEMI_SORTED 2u
+
+typedef struct sst_graph sst_graph;
+
+typedef struct sst_config {
+  int device;                  /* CUDA device ordinal (default 0) */
+  uint64_t hbm_budget_bytes;   /* 0 = no budget */
+  uint64_t initial_slots;      /* slab slots to reserve up front (0 = auto) */
+  float upper_root;            /* PMA root upper density (0 = default .85) */
+  float lower_root;            /* PMA root lower density (0 = default .20) */
+  float grow_fill;             /* density after a resize (0 = default .70) */
+} sst_config;
+
+/* ---- lifetime ------------------------------------------------------- */
+/* SparseMatrixV(el_t height, el_t width)  SparseMatrix.hpp:73-87
+ * rows = height (CSR lines), cols = width; cfg may be NULL */
+sst_status sst_graph_create(uint32_t height, uint32_t width,
+                            const sst_config *cfg, sst_graph **out);
+/* ~SparseMatrixV  SparseMatrix.hpp:141-146 */
+sst_status sst_graph_destroy(sst_graph *g);
+/* copy constructor SparseMatrixV(const SparseMatrixV&)  SparseMatrix.hpp:88-96
+ * (deep copy on the device) */
+sst_status sst_graph_clone(const sst_graph *g, sst_graph **out);
+/* order the graph's work on a caller stream (a cudaStream_t); NULL = the
+ * library's own stream */
+sst_status sst_set_stream(sst_graph *g, void *stream);
+sst_status sst_sync(sst_graph *g);
+const char *sst_last_error_message(void);
+const char *sst_status_string(sst_status s);
+
+/* ---- updates -------------------------------------------------------- */
+/* insert_batch(tuple<el_t,el_t>*, uint64_t, bool)  SparseMatrix.hpp:556-643
+ * set union per row; self-loops are skipped (:570,602); pairs with an id
+ * out of range are skipped and reported through *n_invalid (may be NULL) */
+sst_status sst_insert_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
+                            uint32_t flags, uint64_t *n_invalid);
+/* remove_batch  SparseMatrix.hpp:645-718; absent edges are no-ops */
+sst_status sst_remove_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
+                            uint32_t flags, uint64_t *n_invalid);
+/* insert(el_t, el_t) / remove(el_t, el_t)  SparseMatrix.hpp:164-166 */
+sst_status sst_insert(sst_graph *g, uint32_t row, uint32_t col);
+sst_status sst_remove(sst_graph *g, uint32_t row, uint32_t col);
+/* rebuild from a CSR whose rows are sorted and duplicate-free
+ * (the reference loads files then inserts in batches, internal/test.hpp:427-450) */
+sst_status sst_build_from_csr(sst_graph *g, const uint64_t *offsets,
+                              const uint32_t *cols, uint32_t flags);
+
+/* ---- queries -------------------------------------------------------- */
+/* has(el_t, el_t)  SparseMatrix.hpp:162,721-727 ; out[i] = 0/1 */
+sst_status sst_has_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
+                         uint8_t *out, uint32_t flags);
+sst_status sst_has(sst_graph *g, uint32_t row, uint32_t col, int *out);
+/* num_nodes / get_rows / get_cols  SparseMatrix.hpp:56,150-161 */
+sst_status sst_num_nodes(const sst_graph *g, uint64_t *out);
+sst_status sst_get_rows(const sst_graph *g, uint32_t *out);
+sst_status sst_get_cols(const sst_graph *g, uint32_t *out);
+/* M()  SparseMatrix.hpp:518-525 */
+sst_status sst_M(sst_graph *g, uint64_t *out);
+/* getDegree  SparseMatrix.hpp:57-59 (all rows, or one) */
+sst_status sst_degrees(sst_graph *g, uint32_t *out, uint32_t flags);
+sst_status sst_get_degree(sst_graph *g, uint32_t v, uint32_t *out);
+/* map_neighbors copy-out  SparseMatrix.hpp:218-253: the neighbours of v in
+ * ascending order; writes min(deg, cap) ids, *deg = full degree */
+sst_status sst_neighbors(sst_graph *g, uint32_t v, uint32_t *out,
+                         uint64_t cap, uint64_t *deg);
+/* map_range over all rows  SparseMatrix.hpp:255-315: the whole graph as a
+ * CSR (offsets[rows+1], cols[M]) */
+sst_status sst_to_csr(sst_graph *g, uint64_t *offsets, uint32_t *cols,
+                      uint32_t flags);
+/* common_neighbors(u, v, early_end)  SparseMatrix.hpp:61-71, per pair */
+sst_status sst_common_neighbors_batch(sst_graph *g, const uint32_t *pairs,
+                                      uint64_t n, int early_end,
+                                      uint64_t *out, uint32_t flags);
+/* touch_all_sum  SparseMatrix.hpp:436-454 */
+sst_status sst_touch_all_sum(sst_graph *g, uint64_t *out);
+/* get_memory_size  SparseMatrix.hpp:317,528-535: device bytes held */
+sst_status sst_memory_size(sst_graph *g, uint64_t *out);
+/* uniform samples of existing edges: edge of rank
+ * floor(draw(seed, first+i) * M / 2^64) in (row, col) order */
+sst_status sst_sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
+                            uint64_t count, uint32_t *pairs, uint32_t flags);
+
+/* ---- traversal (EdgeMap/VertexMap algorithms; the algorithm library
+ *      EdgeMapVertexMap is absent from the reference tree, so the entry
+ *      points follow its call sites in internal/test.hpp:476-618) ------- */
+/* BFS(g, src)  test.hpp:486: parents (parent[src] = src, -1 unreached)
+ * and/or depths (-1 unreached); either pointer may be NULL */
+sst_status sst_bfs(sst_graph *g, uint32_t src, int32_t *parents,
+                   int32_t *depths, uint32_t flags);
+/* PR_S<double>(g, iters)  test.hpp:527 */
+sst_status sst_pagerank(sst_graph *g, uint32_t iters, double damping,
+                        double *out, uint32_t flags);
+/* CC(g)  test.hpp:571: label = smallest vertex id of the component */
+sst_status sst_cc(sst_graph *g, uint32_t *labels, uint32_t flags);
+/* BC(g, src)  test.hpp:547: single-source dependency scores */
+sst_status sst_bc(sst_graph *g, uint32_t src, double *out, uint32_t flags);
+/* TC(g)  test.hpp:606: triangles (each once); per_vertex may be NULL */
+sst_status sst_tc(sst_graph *g, uint64_t *total, uint64_t *per_vertex,
+                  uint32_t flags);
+/* TouchAll(g)  test.hpp:476 */
+sst_status sst_touch_all(sst_graph *g, uint64_t *out);
+
+/* ---- generators (device; same streams as the CPU oracle) ------------ */
+/* RMAT edges first..first+count-1 of stream `seed`, 2^scale vertices */
+sst_status sst_gen_rmat(uint32_t scale, double a, double b, double c,
+                        uint64_t seed, uint64_t first, uint64_t count,
+                        uint32_t *pairs, uint32_t flags);
+/* uniform pairs over n vertices */
+sst_status sst_gen_er(uint32_t n, uint64_t seed, uint64_t first,
+                      uint64_t count, uint32_t *pairs, uint32_t flags);
+/* the reference update-benchmark stream rMat<uint32_t>(nn, hash64(0), a, b, c)
+ * internal/rmat_util.h:82-131, internal/test.hpp:645-654 */
+sst_status sst_gen_ref_rmat(uint32_t nn, double a, double b, double c,
+                            uint64_t first, uint64_t count, uint32_t *pairs,
+                            uint32_t flags);
+
+/* ---- instrumentation -------------------------------------------------- */
+/* number of kernel launches this library issued since load */
+uint64_t sst_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SSTGRAPH_H */

@@ -1,0 +1,103 @@
+// Host-side graph object shared by the C ABI, the update path and the
+// traversal path.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/sstgraph.h"
+#include "common.cuh"
+#include "primitives.cuh"
+
+namespace sst {
+
+// Summary of a planned batch, copied to the host once per batch: it sizes
+// the apply launches, the window scratch and the slab allocation.
+struct PlanSummary {
+  uint32_t n_items;      // unique valid keys that change the graph
+  uint32_t n_groups;     // (row, leaf) groups among them
+  uint32_t n_merge;      // leaf-local merge tasks
+  uint32_t n_tasks;      // window / resize tasks
+  uint64_t task_elems;   // elements staged by window / resize tasks
+  uint64_t src_leaves;   // leaves read by those tasks
+  uint64_t dst_leaves;   // leaves written by those tasks
+  uint64_t invalid;      // pairs with an id out of range
+  uint32_t class_cnt[kNumClasses];  // new segments per capacity class
+};
+
+// Flattened list of all leaves in vertex order: the iteration space of the
+// copy-out, sampling and traversal kernels.  Rebuilt when the graph version
+// changes.
+struct LeafDir {
+  uint64_t version = ~0ull;
+  uint64_t nleaves = 0;
+  uint64_t cap = 0;
+  uint32_t *owner = nullptr;  // vertex of each leaf
+  uint64_t *slot = nullptr;   // first slot of each leaf
+  uint32_t *cnt = nullptr;    // elements in each leaf
+  uint64_t *pre = nullptr;    // exclusive prefix of cnt = CSR position
+  uint64_t *vleaf = nullptr;  // per vertex: index of its first leaf (n+1)
+  void release();
+};
+
+}  // namespace sst
+
+struct sst_graph {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  uint32_t n = 0, width = 0;
+  int rbits = 0, dbits = 0;
+  sst::PmaParams params;
+  uint64_t budget = 0;
+
+  uint64_t *d_base = nullptr;
+  uint32_t *d_cap = nullptr;
+  uint32_t *d_deg = nullptr;
+  uint32_t *d_slots = nullptr;
+  uint8_t *d_lcnt = nullptr;
+  uint64_t nslots = 0;
+  uint64_t bump = 0;
+  uint64_t m = 0;
+  uint64_t version = 0;
+
+  sst::Arena arena;  // per-operation scratch
+  sst::Arena work;   // window / resize staging
+  sst::PlanSummary *h_plan = nullptr;  // pinned
+  sst::PlanSummary *d_plan = nullptr;
+  sst::LeafDir dir;
+  void *h_pinned = nullptr;  // pinned staging for host-pointer calls
+  size_t h_pinned_cap = 0;
+
+  sst::DGraph view() const {
+    return sst::DGraph{n, width, d_base, d_cap, d_deg, d_slots, d_lcnt};
+  }
+};
+
+namespace sst {
+
+sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
+                      const sst_config *cfg);
+void graph_release(sst_graph *g);
+sst_status graph_clone(const sst_graph *src, sst_graph *dst);
+uint64_t graph_device_bytes(const sst_graph *g);
+
+// pairs are device pointers here; the C ABI stages host buffers
+sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,
+                        bool insert, uint64_t *n_invalid);
+sst_status build_from_csr(sst_graph *g, const uint64_t *d_off,
+                          const uint32_t *d_cols);
+sst_status has_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,
+                     uint8_t *d_out);
+sst_status ensure_leaf_dir(sst_graph *g);
+sst_status to_csr(sst_graph *g, uint64_t *d_off, uint32_t *d_cols);
+sst_status neighbors(sst_graph *g, uint32_t v, uint32_t *d_out, uint64_t cap,
+                     uint64_t *deg);
+sst_status sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
+                        uint64_t count, uint32_t *d_pairs);
+sst_status touch_all_sum(sst_graph *g, uint64_t *out);
+sst_status repack(sst_graph *g, uint64_t extra_slots);
+
+// host staging buffer (pinned) of at least `bytes`
+void *pinned(sst_graph *g, size_t bytes);
+
+}  // namespace sst

@@ -1,0 +1,172 @@
+// Stable LSD radix sort of 64-bit keys (8-bit digits) and the launch
+// counter.  Each pass: per-tile digit histograms, one exclusive scan over
+// (digit, tile), then a stable scatter that ranks equal digits with
+// warp match_any + per-warp prefix counts in shared memory.
+#include <atomic>
+
+#include "primitives.cuh"
+
+namespace sst {
+
+static std::atomic<uint64_t> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+uint64_t launches() { return g_launches.load(std::memory_order_relaxed); }
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr int kTile = kThreads * kItems;  // 4096
+constexpr int kRadix = 256;
+
+// Stable ranking of one iteration's 256 keys (one per thread, in index
+// order).  run[d] holds the next output position for digit d and is
+// advanced.  Returns the output position of this thread's key.
+__device__ __forceinline__ uint32_t rank_iteration(uint32_t d, bool valid,
+                                                   uint32_t (*wcnt)[kRadix],
+                                                   uint32_t *run) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) wcnt[w][threadIdx.x] = 0;
+  __syncthreads();
+  uint32_t key = valid ? d : 0xffffffffu;
+  uint32_t peers = __match_any_sync(0xffffffffu, key);
+  uint32_t lt = peers & ((1u << lane) - 1u);
+  if (valid && lt == 0) wcnt[warp][d] = __popc(peers);
+  __syncthreads();
+  {
+    uint32_t s = run[threadIdx.x];
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) {
+      uint32_t c = wcnt[w][threadIdx.x];
+      wcnt[w][threadIdx.x] = s;
+      s += c;
+    }
+    run[threadIdx.x] = s;
+  }
+  uint32_t pos = valid ? wcnt[warp][d] + __popc(lt) : 0;
+  __syncthreads();
+  return pos;
+}
+
+__global__ void k_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
+                       uint32_t *__restrict__ hist, uint32_t nblocks) {
+  __shared__ uint32_t h[kRadix];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  uint64_t t0 = (uint64_t)blockIdx.x * kTile;
+#pragma unroll 4
+  for (int it = 0; it < kItems; it++) {
+    uint64_t i = t0 + (uint64_t)it * kThreads + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xff], 1u);
+  }
+  __syncthreads();
+  hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void k_scatter(const uint64_t *__restrict__ in,
+                          uint64_t *__restrict__ out, uint64_t n, int shift,
+                          const uint32_t *__restrict__ hist, uint32_t nblocks) {
+  __shared__ uint32_t wcnt[kWarps][kRadix];
+  __shared__ uint32_t run[kRadix];
+  run[threadIdx.x] = hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x];
+  __syncthreads();
+  uint64_t t0 = (uint64_t)blockIdx.x * kTile;
+  for (int it = 0; it < kItems; it++) {
+    uint64_t i = t0 + (uint64_t)it * kThreads + threadIdx.x;
+    bool valid = i < n;
+    uint64_t k = valid ? in[i] : 0;
+    uint32_t d = (uint32_t)(k >> shift) & 0xff;
+    uint32_t pos = rank_iteration(d, valid, wcnt, run);
+    if (valid) out[pos] = k;
+  }
+}
+
+// whole sort in one CTA for n <= kSmallSort: keys staged in shared memory
+__global__ void k_sort_small(uint64_t *__restrict__ keys, uint64_t n, int bits) {
+  __shared__ uint64_t buf[2][kSmallSort];
+  __shared__ uint32_t wcnt[kWarps][kRadix];
+  __shared__ uint32_t run[kRadix];
+  __shared__ uint32_t h[kRadix];
+  for (uint64_t i = threadIdx.x; i < n; i += kThreads) buf[0][i] = keys[i];
+  int cur = 0;
+  for (int shift = 0; shift < bits; shift += 8) {
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint64_t i = threadIdx.x; i < n; i += kThreads)
+      atomicAdd(&h[(buf[cur][i] >> shift) & 0xff], 1u);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      // exclusive scan of 256 bins by one warp, 8 bins per lane
+      uint32_t loc[8], s = 0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        loc[j] = s;
+        s += h[threadIdx.x * 8 + j];
+      }
+      uint32_t inc = s;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        uint32_t o = __shfl_up_sync(0xffffffffu, inc, d);
+        if ((int)threadIdx.x >= d) inc += o;
+      }
+      uint32_t excl = inc - s;
+#pragma unroll
+      for (int j = 0; j < 8; j++) run[threadIdx.x * 8 + j] = excl + loc[j];
+    }
+    __syncthreads();
+    int iters = (int)((n + kThreads - 1) / kThreads);
+    for (int it = 0; it < iters; it++) {
+      uint64_t i = (uint64_t)it * kThreads + threadIdx.x;
+      bool valid = i < n;
+      uint64_t k = valid ? buf[cur][i] : 0;
+      uint32_t d = (uint32_t)(k >> shift) & 0xff;
+      uint32_t pos = rank_iteration(d, valid, wcnt, run);
+      if (valid) buf[cur ^ 1][pos] = k;
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
+  for (uint64_t i = threadIdx.x; i < n; i += kThreads) keys[i] = buf[cur][i];
+}
+
+}  // namespace
+
+size_t radix_sort_scratch_bytes(uint64_t n) {
+  uint64_t nblocks = (n + kTile - 1) / kTile;
+  uint64_t hn = nblocks * kRadix;
+  return ((hn * 4 + 255) & ~size_t(255)) + scan_scratch_bytes(hn, 4) + 512;
+}
+
+cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
+                           Arena &arena, cudaStream_t s, uint64_t **result) {
+  *result = keys;
+  if (n < 2 || bits <= 0) return cudaSuccess;
+  if (n <= (uint64_t)kSmallSort) {
+    SST_LAUNCH(k_sort_small, 1, kThreads, 0, s, keys, n, bits);
+    return cudaGetLastError();
+  }
+  uint32_t nblocks = (uint32_t)((n + kTile - 1) / kTile);
+  uint64_t hn = (uint64_t)nblocks * kRadix;
+  uint32_t *hist = arena.take<uint32_t>(hn);
+  if (!hist) return cudaErrorMemoryAllocation;
+  uint64_t *src = keys, *dst = tmp;
+  for (int shift = 0; shift < bits; shift += 8) {
+    SST_LAUNCH(k_hist, nblocks, kThreads, 0, s, src, n, shift, hist, nblocks);
+    size_t mark = arena.used;
+    cudaError_t e = scan<uint32_t, OpAdd>(hist, hist, hn, 0u, OpAdd{}, true,
+                                          false, nullptr, arena, s);
+    arena.used = mark;
+    if (e != cudaSuccess) return e;
+    SST_LAUNCH(k_scatter, nblocks, kThreads, 0, s, src, dst, n, shift, hist,
+               nblocks);
+    uint64_t *t = src;
+    src = dst;
+    dst = t;
+  }
+  *result = src;
+  return cudaGetLastError();
+}
+
+}  // namespace sst

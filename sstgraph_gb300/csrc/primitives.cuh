@@ -1,0 +1,216 @@
+// Device primitives shared by the update and traversal paths: a scratch
+// arena, block/grid scans (any associative operator, forward or reverse),
+// and a stable LSD radix sort of 64-bit keys.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace sst {
+
+void note_launch();
+uint64_t launches();
+
+#define SST_LAUNCH(kernel, grid, block, smem, stream, ...)                    \
+  do {                                                                        \
+    kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);               \
+    ::sst::note_launch();                                                     \
+  } while (0)
+
+// ----------------------------------------------------------------- arena
+// Bump allocator over one device buffer; reset at the start of each
+// operation.  Growing it frees and reallocates (callers grow before use).
+struct Arena {
+  char *base = nullptr;
+  size_t cap = 0;
+  size_t used = 0;
+  size_t peak = 0;
+
+  cudaError_t reserve(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (base) {
+      cudaError_t e = cudaFree(base);
+      if (e != cudaSuccess) return e;
+      base = nullptr;
+      cap = 0;
+    }
+    size_t want = bytes + bytes / 4 + (1u << 20);
+    cudaError_t e = cudaMalloc(&base, want);
+    if (e != cudaSuccess) {
+      base = nullptr;
+      return e;
+    }
+    cap = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (base) cudaFree(base);
+    base = nullptr;
+    cap = used = 0;
+  }
+  void reset() { used = 0; }
+  template <typename T> T *take(size_t count) {
+    size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+    if (bytes == 0) bytes = 256;
+    if (used + bytes > cap) return nullptr;
+    T *p = reinterpret_cast<T *>(base + used);
+    used += bytes;
+    if (used > peak) peak = used;
+    return p;
+  }
+};
+
+// ---------------------------------------------------------------- scans
+struct OpAdd {
+  template <typename T> __device__ __forceinline__ T operator()(T a, T b) const {
+    return a + b;
+  }
+};
+struct OpMax {
+  template <typename T> __device__ __forceinline__ T operator()(T a, T b) const {
+    return a > b ? a : b;
+  }
+};
+struct OpMin {
+  template <typename T> __device__ __forceinline__ T operator()(T a, T b) const {
+    return a < b ? a : b;
+  }
+};
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+template <typename T, typename Op>
+__device__ __forceinline__ T warp_inclusive(T v, Op op) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    T o = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane >= d) v = op(o, v);
+  }
+  return v;
+}
+
+// exclusive scan of one value per thread across the block; returns the
+// block total through *total
+template <typename T, typename Op>
+__device__ __forceinline__ T block_exclusive(T v, T identity, Op op, T *total) {
+  __shared__ T warp_tot[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T inc = warp_inclusive(v, op);
+  if (lane == 31) warp_tot[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < kScanThreads / 32 ? warp_tot[lane] : identity;
+    T wi = warp_inclusive(w, op);
+    if (lane < kScanThreads / 32) warp_tot[lane] = wi;
+  }
+  __syncthreads();
+  T prefix = warp == 0 ? identity : warp_tot[warp - 1];
+  T excl_in_warp = __shfl_up_sync(0xffffffffu, inc, 1);
+  if (lane == 0) excl_in_warp = identity;
+  T res = warp == 0 ? excl_in_warp : (lane == 0 ? prefix : op(prefix, excl_in_warp));
+  *total = warp_tot[kScanThreads / 32 - 1];
+  __syncthreads();
+  return res;
+}
+
+template <typename T, typename Op>
+__global__ void k_scan_reduce(const T *__restrict__ in, uint64_t n, T identity,
+                              Op op, bool reverse, T *__restrict__ block_sums) {
+  uint64_t tile0 = (uint64_t)blockIdx.x * kScanTile;
+  T acc = identity;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    uint64_t i = tile0 + (uint64_t)threadIdx.x * kScanItems + k;
+    if (i < n) acc = op(acc, in[reverse ? n - 1 - i : i]);
+  }
+  T total;
+  block_exclusive(acc, identity, op, &total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+template <typename T, typename Op>
+__global__ void k_scan_apply(const T *__restrict__ in, T *__restrict__ out,
+                             uint64_t n, T identity, Op op, bool reverse,
+                             bool exclusive, const T *__restrict__ block_prefix,
+                             T *__restrict__ total_out) {
+  uint64_t tile0 = (uint64_t)blockIdx.x * kScanTile;
+  T vals[kScanItems];
+  T acc = identity;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    uint64_t i = tile0 + (uint64_t)threadIdx.x * kScanItems + k;
+    vals[k] = i < n ? in[reverse ? n - 1 - i : i] : identity;
+    acc = op(acc, vals[k]);
+  }
+  T total;
+  T run = block_exclusive(acc, identity, op, &total);
+  if (block_prefix) run = op(block_prefix[blockIdx.x], run);
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    uint64_t i = tile0 + (uint64_t)threadIdx.x * kScanItems + k;
+    T nxt = op(run, vals[k]);
+    if (i < n) out[reverse ? n - 1 - i : i] = exclusive ? run : nxt;
+    run = nxt;
+  }
+  if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+    T t = block_prefix ? op(block_prefix[blockIdx.x], total) : total;
+    *total_out = t;
+  }
+}
+
+// Scan of n elements (in may equal out).  total_out (device, may be null)
+// receives the reduction of all n elements.
+template <typename T, typename Op>
+cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
+                 bool exclusive, bool reverse, T *total_out, Arena &arena,
+                 cudaStream_t s) {
+  if (n == 0) {
+    if (total_out) return cudaMemcpyAsync(total_out, &identity, sizeof(T),
+                                          cudaMemcpyHostToDevice, s);
+    return cudaSuccess;
+  }
+  uint64_t blocks = (n + kScanTile - 1) / kScanTile;
+  if (blocks == 1) {
+    SST_LAUNCH((k_scan_apply<T, Op>), 1, kScanThreads, 0, s, in, out, n,
+               identity, op, reverse, exclusive, (const T *)nullptr, total_out);
+    return cudaGetLastError();
+  }
+  T *sums = arena.take<T>(blocks);
+  if (!sums) return cudaErrorMemoryAllocation;
+  SST_LAUNCH((k_scan_reduce<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
+             n, identity, op, reverse, sums);
+  // block prefixes in block order (reverse handled inside the tiles)
+  cudaError_t e = scan<T, Op>(sums, sums, blocks, identity, op, true, false,
+                              (T *)nullptr, arena, s);
+  if (e != cudaSuccess) return e;
+  SST_LAUNCH((k_scan_apply<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
+             out, n, identity, op, reverse, exclusive, (const T *)sums,
+             total_out);
+  return cudaGetLastError();
+}
+
+// scratch bytes a scan of n elements of T takes from the arena
+inline size_t scan_scratch_bytes(uint64_t n, size_t elem) {
+  size_t bytes = 0;
+  uint64_t blocks = (n + kScanTile - 1) / kScanTile;
+  while (blocks > 1) {
+    bytes += ((blocks * elem + 255) & ~size_t(255));
+    blocks = (blocks + kScanTile - 1) / kScanTile;
+  }
+  return bytes + 256;
+}
+
+// ----------------------------------------------------------- radix sort
+// Stable LSD radix sort of 64-bit keys on their low `bits` bits, 8-bit
+// digits.  keys and tmp are both n long; *result points at whichever holds
+// the sorted keys.  Batches up to kSmallSort keys sort in one CTA.
+constexpr int kSmallSort = 2048;
+cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
+                           Arena &arena, cudaStream_t s, uint64_t **result);
+size_t radix_sort_scratch_bytes(uint64_t n);
+
+}  // namespace sst
