@@ -35,6 +35,13 @@
 extern "C" {
 #endif
 
+/* symbols the shared library exports */
+#if defined(__GNUC__)
+#define SST_API __attribute__((visibility("default")))
+#else
+#define SST_API
+#endif
+
 typedef int32_t sst_status;
 #define SST_OK 0
 #define SST_EINVAL (-1)    /* bad argument (null handle, id out of range) */
@@ -64,70 +71,70 @@ typedef struct sst_config {
 /* ---- lifetime ------------------------------------------------------- */
 /* SparseMatrixV(el_t height, el_t width)  SparseMatrix.hpp:73-87
  * rows = height (CSR lines), cols = width; cfg may be NULL */
-sst_status sst_graph_create(uint32_t height, uint32_t width,
+SST_API sst_status sst_graph_create(uint32_t height, uint32_t width,
                             const sst_config *cfg, sst_graph **out);
 /* ~SparseMatrixV  SparseMatrix.hpp:141-146 */
-sst_status sst_graph_destroy(sst_graph *g);
+SST_API sst_status sst_graph_destroy(sst_graph *g);
 /* copy constructor SparseMatrixV(const SparseMatrixV&)  SparseMatrix.hpp:88-96
  * (deep copy on the device) */
-sst_status sst_graph_clone(const sst_graph *g, sst_graph **out);
+SST_API sst_status sst_graph_clone(const sst_graph *g, sst_graph **out);
 /* order the graph's work on a caller stream (a cudaStream_t); NULL = the
  * library's own stream */
-sst_status sst_set_stream(sst_graph *g, void *stream);
-sst_status sst_sync(sst_graph *g);
-const char *sst_last_error_message(void);
-const char *sst_status_string(sst_status s);
+SST_API sst_status sst_set_stream(sst_graph *g, void *stream);
+SST_API sst_status sst_sync(sst_graph *g);
+SST_API const char *sst_last_error_message(void);
+SST_API const char *sst_status_string(sst_status s);
 
 /* ---- updates -------------------------------------------------------- */
 /* insert_batch(tuple<el_t,el_t>*, uint64_t, bool)  SparseMatrix.hpp:556-643
  * set union per row; self-loops are skipped (:570,602); pairs with an id
  * out of range are skipped and reported through *n_invalid (may be NULL) */
-sst_status sst_insert_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
+SST_API sst_status sst_insert_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
                             uint32_t flags, uint64_t *n_invalid);
 /* remove_batch  SparseMatrix.hpp:645-718; absent edges are no-ops */
-sst_status sst_remove_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
+SST_API sst_status sst_remove_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
                             uint32_t flags, uint64_t *n_invalid);
 /* insert(el_t, el_t) / remove(el_t, el_t)  SparseMatrix.hpp:164-166 */
-sst_status sst_insert(sst_graph *g, uint32_t row, uint32_t col);
-sst_status sst_remove(sst_graph *g, uint32_t row, uint32_t col);
+SST_API sst_status sst_insert(sst_graph *g, uint32_t row, uint32_t col);
+SST_API sst_status sst_remove(sst_graph *g, uint32_t row, uint32_t col);
 /* rebuild from a CSR whose rows are sorted and duplicate-free
  * (the reference loads files then inserts in batches, internal/test.hpp:427-450) */
-sst_status sst_build_from_csr(sst_graph *g, const uint64_t *offsets,
+SST_API sst_status sst_build_from_csr(sst_graph *g, const uint64_t *offsets,
                               const uint32_t *cols, uint32_t flags);
 
 /* ---- queries -------------------------------------------------------- */
 /* has(el_t, el_t)  SparseMatrix.hpp:162,721-727 ; out[i] = 0/1 */
-sst_status sst_has_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
+SST_API sst_status sst_has_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
                          uint8_t *out, uint32_t flags);
-sst_status sst_has(sst_graph *g, uint32_t row, uint32_t col, int *out);
+SST_API sst_status sst_has(sst_graph *g, uint32_t row, uint32_t col, int *out);
 /* num_nodes / get_rows / get_cols  SparseMatrix.hpp:56,150-161 */
-sst_status sst_num_nodes(const sst_graph *g, uint64_t *out);
-sst_status sst_get_rows(const sst_graph *g, uint32_t *out);
-sst_status sst_get_cols(const sst_graph *g, uint32_t *out);
+SST_API sst_status sst_num_nodes(const sst_graph *g, uint64_t *out);
+SST_API sst_status sst_get_rows(const sst_graph *g, uint32_t *out);
+SST_API sst_status sst_get_cols(const sst_graph *g, uint32_t *out);
 /* M()  SparseMatrix.hpp:518-525 */
-sst_status sst_M(sst_graph *g, uint64_t *out);
+SST_API sst_status sst_M(sst_graph *g, uint64_t *out);
 /* getDegree  SparseMatrix.hpp:57-59 (all rows, or one) */
-sst_status sst_degrees(sst_graph *g, uint32_t *out, uint32_t flags);
-sst_status sst_get_degree(sst_graph *g, uint32_t v, uint32_t *out);
+SST_API sst_status sst_degrees(sst_graph *g, uint32_t *out, uint32_t flags);
+SST_API sst_status sst_get_degree(sst_graph *g, uint32_t v, uint32_t *out);
 /* map_neighbors copy-out  SparseMatrix.hpp:218-253: the neighbours of v in
  * ascending order; writes min(deg, cap) ids, *deg = full degree */
-sst_status sst_neighbors(sst_graph *g, uint32_t v, uint32_t *out,
+SST_API sst_status sst_neighbors(sst_graph *g, uint32_t v, uint32_t *out,
                          uint64_t cap, uint64_t *deg);
 /* map_range over all rows  SparseMatrix.hpp:255-315: the whole graph as a
  * CSR (offsets[rows+1], cols[M]) */
-sst_status sst_to_csr(sst_graph *g, uint64_t *offsets, uint32_t *cols,
+SST_API sst_status sst_to_csr(sst_graph *g, uint64_t *offsets, uint32_t *cols,
                       uint32_t flags);
 /* common_neighbors(u, v, early_end)  SparseMatrix.hpp:61-71, per pair */
-sst_status sst_common_neighbors_batch(sst_graph *g, const uint32_t *pairs,
+SST_API sst_status sst_common_neighbors_batch(sst_graph *g, const uint32_t *pairs,
                                       uint64_t n, int early_end,
                                       uint64_t *out, uint32_t flags);
 /* touch_all_sum  SparseMatrix.hpp:436-454 */
-sst_status sst_touch_all_sum(sst_graph *g, uint64_t *out);
+SST_API sst_status sst_touch_all_sum(sst_graph *g, uint64_t *out);
 /* get_memory_size  SparseMatrix.hpp:317,528-535: device bytes held */
-sst_status sst_memory_size(sst_graph *g, uint64_t *out);
+SST_API sst_status sst_memory_size(sst_graph *g, uint64_t *out);
 /* uniform samples of existing edges: edge of rank
  * floor(draw(seed, first+i) * M / 2^64) in (row, col) order */
-sst_status sst_sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
+SST_API sst_status sst_sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
                             uint64_t count, uint32_t *pairs, uint32_t flags);
 
 /* ---- traversal (EdgeMap/VertexMap algorithms; the algorithm library
@@ -135,38 +142,38 @@ sst_status sst_sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
  *      points follow its call sites in internal/test.hpp:476-618) ------- */
 /* BFS(g, src)  test.hpp:486: parents (parent[src] = src, -1 unreached)
  * and/or depths (-1 unreached); either pointer may be NULL */
-sst_status sst_bfs(sst_graph *g, uint32_t src, int32_t *parents,
+SST_API sst_status sst_bfs(sst_graph *g, uint32_t src, int32_t *parents,
                    int32_t *depths, uint32_t flags);
 /* PR_S<double>(g, iters)  test.hpp:527 */
-sst_status sst_pagerank(sst_graph *g, uint32_t iters, double damping,
+SST_API sst_status sst_pagerank(sst_graph *g, uint32_t iters, double damping,
                         double *out, uint32_t flags);
 /* CC(g)  test.hpp:571: label = smallest vertex id of the component */
-sst_status sst_cc(sst_graph *g, uint32_t *labels, uint32_t flags);
+SST_API sst_status sst_cc(sst_graph *g, uint32_t *labels, uint32_t flags);
 /* BC(g, src)  test.hpp:547: single-source dependency scores */
-sst_status sst_bc(sst_graph *g, uint32_t src, double *out, uint32_t flags);
+SST_API sst_status sst_bc(sst_graph *g, uint32_t src, double *out, uint32_t flags);
 /* TC(g)  test.hpp:606: triangles (each once); per_vertex may be NULL */
-sst_status sst_tc(sst_graph *g, uint64_t *total, uint64_t *per_vertex,
+SST_API sst_status sst_tc(sst_graph *g, uint64_t *total, uint64_t *per_vertex,
                   uint32_t flags);
 /* TouchAll(g)  test.hpp:476 */
-sst_status sst_touch_all(sst_graph *g, uint64_t *out);
+SST_API sst_status sst_touch_all(sst_graph *g, uint64_t *out);
 
 /* ---- generators (device; same streams as the CPU oracle) ------------ */
 /* RMAT edges first..first+count-1 of stream `seed`, 2^scale vertices */
-sst_status sst_gen_rmat(uint32_t scale, double a, double b, double c,
+SST_API sst_status sst_gen_rmat(uint32_t scale, double a, double b, double c,
                         uint64_t seed, uint64_t first, uint64_t count,
                         uint32_t *pairs, uint32_t flags);
 /* uniform pairs over n vertices */
-sst_status sst_gen_er(uint32_t n, uint64_t seed, uint64_t first,
+SST_API sst_status sst_gen_er(uint32_t n, uint64_t seed, uint64_t first,
                       uint64_t count, uint32_t *pairs, uint32_t flags);
 /* the reference update-benchmark stream rMat<uint32_t>(nn, hash64(0), a, b, c)
  * internal/rmat_util.h:82-131, internal/test.hpp:645-654 */
-sst_status sst_gen_ref_rmat(uint32_t nn, double a, double b, double c,
+SST_API sst_status sst_gen_ref_rmat(uint32_t nn, double a, double b, double c,
                             uint64_t first, uint64_t count, uint32_t *pairs,
                             uint32_t flags);
 
 /* ---- instrumentation -------------------------------------------------- */
 /* number of kernel launches this library issued since load */
-uint64_t sst_kernel_launches(void);
+SST_API uint64_t sst_kernel_launches(void);
 
 #ifdef __cplusplus
 }

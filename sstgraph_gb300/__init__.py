@@ -1,0 +1,407 @@
+"""sstgraph_gb300 -- GB300-native dynamic graph (SSTGraph's hot path).
+
+Python mirror of the reference's graph interface over the C ABI in
+include/sstgraph.h (libsstgraph_gb300.so, built in-tree by build.py).  Names
+follow the reference: ``SparseMatrixV`` (include/SSTGraph/SparseMatrix.hpp)
+with ``insert_batch`` / ``remove_batch`` / ``has`` / ``getDegree`` / ``M`` /
+``map_neighbors`` / ``common_neighbors`` / ``touch_all_sum``, and the
+EdgeMapVertexMap entry points the reference drivers call (``BFS``, ``PR_S``,
+``CC``, ``BC``, ``TC``, ``TouchAll``; internal/test.hpp:476-618).
+
+Every call runs on the GPU.  There is no CPU fallback: if the library is
+missing or no GPU is usable, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libsstgraph_gb300.so")
+
+HOST_PTR = 0
+DEVICE_PTR = 1
+SEMI_SORTED = 2
+
+_STATUS = {0: "ok", -1: "invalid argument", -2: "out of device memory",
+           -3: "HBM budget exceeded", -4: "device wait timed out",
+           -5: "CUDA device error", -6: "invalid state"}
+
+
+class SSTError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{_STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class sst_config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int),
+                ("hbm_budget_bytes", ctypes.c_uint64),
+                ("initial_slots", ctypes.c_uint64),
+                ("upper_root", ctypes.c_float),
+                ("lower_root", ctypes.c_float),
+                ("grow_fill", ctypes.c_float)]
+
+
+# name -> (restype, argtypes); mirrors include/sstgraph.h
+_vp, _u32, _u64, _i32, _dbl = (ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64,
+                               ctypes.c_int32, ctypes.c_double)
+SIGNATURES = {
+    "sst_graph_create": (_i32, [_u32, _u32, ctypes.POINTER(sst_config), ctypes.POINTER(_vp)]),
+    "sst_graph_destroy": (_i32, [_vp]),
+    "sst_graph_clone": (_i32, [_vp, ctypes.POINTER(_vp)]),
+    "sst_set_stream": (_i32, [_vp, _vp]),
+    "sst_sync": (_i32, [_vp]),
+    "sst_last_error_message": (ctypes.c_char_p, []),
+    "sst_status_string": (ctypes.c_char_p, [_i32]),
+    "sst_insert_batch": (_i32, [_vp, _vp, _u64, _u32, ctypes.POINTER(_u64)]),
+    "sst_remove_batch": (_i32, [_vp, _vp, _u64, _u32, ctypes.POINTER(_u64)]),
+    "sst_insert": (_i32, [_vp, _u32, _u32]),
+    "sst_remove": (_i32, [_vp, _u32, _u32]),
+    "sst_build_from_csr": (_i32, [_vp, _vp, _vp, _u32]),
+    "sst_has_batch": (_i32, [_vp, _vp, _u64, _vp, _u32]),
+    "sst_has": (_i32, [_vp, _u32, _u32, ctypes.POINTER(ctypes.c_int)]),
+    "sst_num_nodes": (_i32, [_vp, ctypes.POINTER(_u64)]),
+    "sst_get_rows": (_i32, [_vp, ctypes.POINTER(_u32)]),
+    "sst_get_cols": (_i32, [_vp, ctypes.POINTER(_u32)]),
+    "sst_M": (_i32, [_vp, ctypes.POINTER(_u64)]),
+    "sst_degrees": (_i32, [_vp, _vp, _u32]),
+    "sst_get_degree": (_i32, [_vp, _u32, ctypes.POINTER(_u32)]),
+    "sst_neighbors": (_i32, [_vp, _u32, _vp, _u64, ctypes.POINTER(_u64)]),
+    "sst_to_csr": (_i32, [_vp, _vp, _vp, _u32]),
+    "sst_common_neighbors_batch": (_i32, [_vp, _vp, _u64, ctypes.c_int, _vp, _u32]),
+    "sst_touch_all_sum": (_i32, [_vp, ctypes.POINTER(_u64)]),
+    "sst_memory_size": (_i32, [_vp, ctypes.POINTER(_u64)]),
+    "sst_sample_edges": (_i32, [_vp, _u64, _u64, _u64, _vp, _u32]),
+    "sst_bfs": (_i32, [_vp, _u32, _vp, _vp, _u32]),
+    "sst_pagerank": (_i32, [_vp, _u32, _dbl, _vp, _u32]),
+    "sst_cc": (_i32, [_vp, _vp, _u32]),
+    "sst_bc": (_i32, [_vp, _u32, _vp, _u32]),
+    "sst_tc": (_i32, [_vp, ctypes.POINTER(_u64), _vp, _u32]),
+    "sst_touch_all": (_i32, [_vp, ctypes.POINTER(_u64)]),
+    "sst_gen_rmat": (_i32, [_u32, _dbl, _dbl, _dbl, _u64, _u64, _u64, _vp, _u32]),
+    "sst_gen_er": (_i32, [_u32, _u64, _u64, _u64, _vp, _u32]),
+    "sst_gen_ref_rmat": (_i32, [_u32, _dbl, _dbl, _dbl, _u64, _u64, _vp, _u32]),
+    "sst_kernel_launches": (_u64, []),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != 0:
+        raise SSTError(status, lib().sst_last_error_message().decode())
+
+
+def _ptr(a):
+    """ctypes pointer of a numpy array or a torch tensor (host or device)."""
+    if isinstance(a, np.ndarray):
+        return ctypes.c_void_p(a.ctypes.data), HOST_PTR
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr()), (DEVICE_PTR if a.is_cuda else HOST_PTR)
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def _pairs(edges):
+    if hasattr(edges, "data_ptr"):
+        assert edges.is_contiguous()
+        return edges, edges.numel() // 2
+    e = np.ascontiguousarray(np.asarray(edges, dtype=np.uint32).reshape(-1, 2))
+    return e, e.shape[0]
+
+
+def kernel_launches() -> int:
+    return int(lib().sst_kernel_launches())
+
+
+class SparseMatrixV:
+    """Device-resident SparseMatrixV<true> (binary CSR, uint32 ids).
+
+    Reference: include/SSTGraph/SparseMatrix.hpp.  Arrays may be numpy (host)
+    or torch CUDA tensors (device); results come back in the same place.
+    """
+
+    def __init__(self, height: int, width: int | None = None, *, device: int = 0,
+                 hbm_budget_bytes: int = 0, initial_slots: int = 0,
+                 upper_root: float = 0.0, lower_root: float = 0.0,
+                 grow_fill: float = 0.0, _handle=None):
+        self._h = None
+        if _handle is not None:
+            self._h = _handle
+        else:
+            cfg = sst_config(device, hbm_budget_bytes, initial_slots,
+                             upper_root, lower_root, grow_fill)
+            h = ctypes.c_void_p()
+            _check(lib().sst_graph_create(height, height if width is None else width,
+                                          ctypes.byref(cfg), ctypes.byref(h)))
+            self._h = h
+        r = ctypes.c_uint32()
+        _check(lib().sst_get_rows(self._h, ctypes.byref(r)))
+        self.rows = r.value
+        _check(lib().sst_get_cols(self._h, ctypes.byref(r)))
+        self.cols = r.value
+
+    def close(self):
+        if self._h:
+            lib().sst_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def copy(self) -> "SparseMatrixV":
+        h = ctypes.c_void_p()
+        _check(lib().sst_graph_clone(self._h, ctypes.byref(h)))
+        return SparseMatrixV(0, _handle=h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr: int | None):
+        _check(lib().sst_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def sync(self):
+        _check(lib().sst_sync(self._h))
+
+    # -- updates ------------------------------------------------------------
+    def insert_batch(self, edges, semi_sorted: bool = False) -> int:
+        """Insert (row, col) pairs; returns the count of pairs out of range."""
+        e, n = _pairs(edges)
+        p, flags = _ptr(e)
+        bad = ctypes.c_uint64()
+        _check(lib().sst_insert_batch(self._h, p, n, flags | (SEMI_SORTED if semi_sorted else 0),
+                                      ctypes.byref(bad)))
+        return bad.value
+
+    def remove_batch(self, edges, semi_sorted: bool = False) -> int:
+        e, n = _pairs(edges)
+        p, flags = _ptr(e)
+        bad = ctypes.c_uint64()
+        _check(lib().sst_remove_batch(self._h, p, n, flags | (SEMI_SORTED if semi_sorted else 0),
+                                      ctypes.byref(bad)))
+        return bad.value
+
+    def insert(self, row: int, col: int):
+        _check(lib().sst_insert(self._h, row, col))
+
+    def remove(self, row: int, col: int):
+        _check(lib().sst_remove(self._h, row, col))
+
+    def build_from_csr(self, offsets, cols):
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64) if isinstance(offsets, np.ndarray) else offsets
+        cols = np.ascontiguousarray(cols, dtype=np.uint32) if isinstance(cols, np.ndarray) else cols
+        po, flags = _ptr(offsets)
+        pc, _ = _ptr(cols)
+        _check(lib().sst_build_from_csr(self._h, po, pc, flags))
+
+    # -- queries ------------------------------------------------------------
+    def has(self, row: int, col: int) -> bool:
+        r = ctypes.c_int()
+        _check(lib().sst_has(self._h, row, col, ctypes.byref(r)))
+        return bool(r.value)
+
+    def has_batch(self, edges, out=None):
+        e, n = _pairs(edges)
+        p, flags = _ptr(e)
+        if out is None:
+            if flags == DEVICE_PTR:
+                import torch
+                out = torch.empty(n, dtype=torch.uint8, device=e.device)
+            else:
+                out = np.empty(n, np.uint8)
+        po, _ = _ptr(out)
+        _check(lib().sst_has_batch(self._h, p, n, po, flags))
+        return out
+
+    def num_nodes(self) -> int:
+        return self.rows
+
+    def get_rows(self) -> int:
+        return self.rows
+
+    def get_cols(self) -> int:
+        return self.cols
+
+    def M(self) -> int:
+        r = ctypes.c_uint64()
+        _check(lib().sst_M(self._h, ctypes.byref(r)))
+        return r.value
+
+    def getDegree(self, v: int) -> int:
+        r = ctypes.c_uint32()
+        _check(lib().sst_get_degree(self._h, v, ctypes.byref(r)))
+        return r.value
+
+    def degrees(self, out=None):
+        if out is None:
+            out = np.empty(self.rows, np.uint32)
+        p, flags = _ptr(out)
+        _check(lib().sst_degrees(self._h, p, flags))
+        return out
+
+    def neighbors(self, v: int) -> np.ndarray:
+        d = self.getDegree(v)
+        out = np.empty(max(d, 1), np.uint32)
+        full = ctypes.c_uint64()
+        _check(lib().sst_neighbors(self._h, v, ctypes.c_void_p(out.ctypes.data), d,
+                                   ctypes.byref(full)))
+        return out[:d]
+
+    def map_neighbors(self, v: int, f):
+        """Host-callback map over v's neighbours in ascending order
+        (SparseMatrix.hpp:218-253): f(src, dst) returning True stops early."""
+        for x in self.neighbors(v):
+            if f(v, int(x)):
+                return
+
+    def csr(self):
+        m = self.M()
+        off = np.empty(self.rows + 1, np.uint64)
+        cols = np.empty(max(m, 1), np.uint32)
+        _check(lib().sst_to_csr(self._h, ctypes.c_void_p(off.ctypes.data),
+                                ctypes.c_void_p(cols.ctypes.data), HOST_PTR))
+        return off, cols[:m]
+
+    def common_neighbors(self, a: int, b: int, early_end: bool = False) -> int:
+        return int(self.common_neighbors_batch(np.array([[a, b]], np.uint32), early_end)[0])
+
+    def common_neighbors_batch(self, pairs, early_end: bool = False):
+        e, n = _pairs(pairs)
+        p, flags = _ptr(e)
+        if flags == DEVICE_PTR:
+            import torch
+            out = torch.empty(n, dtype=torch.int64, device=e.device)
+        else:
+            out = np.empty(n, np.uint64)
+        po, _ = _ptr(out)
+        _check(lib().sst_common_neighbors_batch(self._h, p, n, int(early_end), po, flags))
+        return out
+
+    def touch_all_sum(self) -> int:
+        r = ctypes.c_uint64()
+        _check(lib().sst_touch_all_sum(self._h, ctypes.byref(r)))
+        return r.value
+
+    def get_memory_size(self) -> int:
+        r = ctypes.c_uint64()
+        _check(lib().sst_memory_size(self._h, ctypes.byref(r)))
+        return r.value
+
+    def sample_edges(self, count: int, seed: int, first: int = 0, out=None):
+        if out is None:
+            out = np.empty((count, 2), np.uint32)
+        p, flags = _ptr(out)
+        _check(lib().sst_sample_edges(self._h, seed, first, count, p, flags))
+        return out
+
+
+# ---- EdgeMapVertexMap entry points (internal/test.hpp:476-618) ------------
+def _out(g, dtype, out, torch_dtype=None):
+    if out is None:
+        return np.empty(g.rows, dtype)
+    return out
+
+
+def BFS(g: SparseMatrixV, src: int, depths: bool = False, parents=None, out=None):
+    """Parents (parent[src] = src, -1 unreached) as the reference returns;
+    with depths=True the BFS depths instead (-1 unreached)."""
+    buf = _out(g, np.int32, out)
+    p, flags = _ptr(buf)
+    if depths:
+        _check(lib().sst_bfs(g.handle, src, None, p, flags))
+    else:
+        _check(lib().sst_bfs(g.handle, src, p, None, flags))
+    return buf
+
+
+def BFS_both(g: SparseMatrixV, src: int):
+    par = np.empty(g.rows, np.int32)
+    dep = np.empty(g.rows, np.int32)
+    _check(lib().sst_bfs(g.handle, src, ctypes.c_void_p(par.ctypes.data),
+                         ctypes.c_void_p(dep.ctypes.data), HOST_PTR))
+    return par, dep
+
+
+def PR_S(g: SparseMatrixV, iters: int = 10, damping: float = 0.85, out=None):
+    buf = _out(g, np.float64, out)
+    p, flags = _ptr(buf)
+    _check(lib().sst_pagerank(g.handle, iters, damping, p, flags))
+    return buf
+
+
+def CC(g: SparseMatrixV, out=None):
+    buf = _out(g, np.uint32, out)
+    p, flags = _ptr(buf)
+    _check(lib().sst_cc(g.handle, p, flags))
+    return buf
+
+
+def BC(g: SparseMatrixV, src: int, out=None):
+    buf = _out(g, np.float64, out)
+    p, flags = _ptr(buf)
+    _check(lib().sst_bc(g.handle, src, p, flags))
+    return buf
+
+
+def TC(g: SparseMatrixV, per_vertex: bool = False):
+    total = ctypes.c_uint64()
+    if per_vertex:
+        pv = np.empty(g.rows, np.uint64)
+        _check(lib().sst_tc(g.handle, ctypes.byref(total), ctypes.c_void_p(pv.ctypes.data), HOST_PTR))
+        return total.value, pv
+    _check(lib().sst_tc(g.handle, ctypes.byref(total), None, HOST_PTR))
+    return total.value
+
+
+def TouchAll(g: SparseMatrixV) -> int:
+    r = ctypes.c_uint64()
+    _check(lib().sst_touch_all(g.handle, ctypes.byref(r)))
+    return r.value
+
+
+# ---- device generators ------------------------------------------------------
+def gen_rmat(scale, count, a=0.57, b=0.19, c=0.19, seed=1, first=0, out=None):
+    if out is None:
+        out = np.empty((count, 2), np.uint32)
+    p, flags = _ptr(out)
+    _check(lib().sst_gen_rmat(scale, a, b, c, seed, first, count, p, flags))
+    return out
+
+
+def gen_er(n, count, seed=4, first=0, out=None):
+    if out is None:
+        out = np.empty((count, 2), np.uint32)
+    p, flags = _ptr(out)
+    _check(lib().sst_gen_er(n, seed, first, count, p, flags))
+    return out
+
+
+def gen_ref_rmat(nn, count, a=0.5, b=0.1, c=0.1, first=0, out=None):
+    if out is None:
+        out = np.empty((count, 2), np.uint32)
+    p, flags = _ptr(out)
+    _check(lib().sst_gen_ref_rmat(nn, a, b, c, first, count, p, flags))
+    return out

@@ -1,0 +1,1441 @@
+// Graph lifetime, slab allocation and the batch update pipeline.
+//
+// A batch (insert or remove) runs as:
+//   1. keys      (row << dbits | col) per pair; self-loops (insert) and ids
+//                out of range become a sentinel that sorts last
+//   2. sort      stable LSD radix sort of the keys (primitives.cu)
+//   3. locate    per unique key: the leaf of its row's PMA where it belongs
+//                (binary search over leaf heads) and whether it is present
+//   4. pack      keys that change the graph, as (row, leaf) + col, in order
+//   5. group     one group per (row, leaf)
+//   6. classify  insert: a group fits its leaf (leaf merge) or climbs to the
+//                smallest aligned window of 2^t leaves whose count stays
+//                under the upper density bound, or the whole segment is
+//                resized.  remove: deletions are applied leaf-locally first,
+//                then leaves under the lower bound climb the same way.
+//   7. dominance aligned windows nest, so a forward max-scan and a backward
+//                min-scan over the groups find, for each group, the largest
+//                window of its row that covers it; covered groups drop out
+//   8. plan      window/resize tasks are sized and the summary is read back
+//                (the one host synchronisation of a batch): it sizes the
+//                staging buffer and the slab allocation
+//   9. apply     leaf merges (one warp per leaf, shuffle-ranked), then each
+//                task gathers old + new elements at their merged rank into
+//                staging (parallel over leaves and items) and scatters them
+//                evenly over the destination leaves (one warp per leaf)
+// Reference counterparts: SparseMatrix.hpp:556-718 (batch split by row),
+// PMA.hpp:1028-1082 (place: window climb + redistribute),
+// PMA.hpp:612-702 (redistribute / double_list / half_list),
+// PMA.hpp:1185-1222 (take: lower-bound climb).
+#include <algorithm>
+#include <cstdarg>
+#include <cstring>
+#include <vector>
+
+#include "graph.cuh"
+
+namespace sst {
+
+namespace {
+
+enum : uint8_t { kNone = 0, kMerge = 1, kWindow = 2, kResize = 3 };
+
+constexpr int kTB = 256;  // threads per block for element-wise kernels
+
+inline unsigned blocks_for(uint64_t n, int per_block = kTB) {
+  uint64_t b = (n + per_block - 1) / per_block;
+  return (unsigned)(b == 0 ? 1 : b);
+}
+inline unsigned warp_blocks(uint64_t nwarps) {
+  return blocks_for(nwarps * 32);
+}
+
+int bits_for(uint64_t x) {
+  int b = 0;
+  while (b < 64 && (x >> b) != 0) b++;
+  return b;
+}
+
+__device__ __forceinline__ uint32_t lb_u64(const uint64_t *a, uint32_t n,
+                                           uint64_t x) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < x)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// index of the last element <= x in a sorted array (n >= 1, a[0] <= x)
+__device__ __forceinline__ uint64_t last_le_u64(const uint64_t *a, uint64_t n,
+                                                uint64_t x) {
+  uint64_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    uint64_t mid = (lo + hi) >> 1;
+    if (a[mid] <= x)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ uint32_t count_less(const uint32_t *a, uint32_t lo,
+                                               uint32_t hi, uint32_t x) {
+  uint32_t b = lo;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < x)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo - b;
+}
+
+__device__ __forceinline__ uint32_t warp_sum_lcnt(const uint8_t *lc,
+                                                  uint64_t lo, uint64_t hi) {
+  const int lane = threadIdx.x & 31;
+  uint32_t s = 0;
+  for (uint64_t i = lo + lane; i < hi; i += 32) s += lc[i];
+  return __reduce_add_sync(0xffffffffu, s);
+}
+
+// ---------------------------------------------------------------- steps 1-5
+__global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
+                            uint32_t n, uint32_t width, int dbits, bool insert,
+                            uint64_t *__restrict__ keys,
+                            unsigned long long *__restrict__ invalid) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b) return;
+  uint32_t r = pairs[2 * i], c = pairs[2 * i + 1];
+  const uint64_t sent = (uint64_t)n << dbits;
+  bool ok = r < n && c < width && c != kEmpty;
+  if (!ok) atomicAdd(invalid, 1ull);
+  keys[i] = (!ok || (insert && r == c)) ? sent : (((uint64_t)r << dbits) | c);
+}
+
+__global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
+                         int dbits, DGraph g, bool insert,
+                         uint32_t *__restrict__ flag,
+                         uint32_t *__restrict__ leaf_out) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b) return;
+  const uint64_t sent = (uint64_t)g.n << dbits;
+  uint64_t k = keys[i];
+  if (k >= sent || (i > 0 && keys[i - 1] == k)) {
+    flag[i] = 0;
+    leaf_out[i] = 0;
+    return;
+  }
+  uint32_t u = (uint32_t)(k >> dbits);
+  uint32_t x = (uint32_t)(k & ((1ull << dbits) - 1));
+  uint64_t base = g.base[u];
+  uint32_t cap = g.cap[u], deg = g.deg[u];
+  bool present = false;
+  uint32_t l = 0;
+  if (cap > 0) {
+    l = find_leaf(g.slots, base, cap, x);
+    uint32_t c = leaf_count(g, base, cap, deg, l);
+    const uint32_t *p = g.slots + base + ((uint64_t)l << kLeafLog);
+    uint32_t pos = leaf_lower_bound(p, c, x);
+    present = pos < c && p[pos] == x;
+  }
+  flag[i] = insert ? !present : present;
+  leaf_out[i] = l;
+}
+
+__global__ void k_pack(const uint64_t *__restrict__ keys,
+                       const uint32_t *__restrict__ flag,
+                       const uint32_t *__restrict__ pos,
+                       const uint32_t *__restrict__ leaf, uint64_t b, int dbits,
+                       uint64_t *__restrict__ p_ul, uint32_t *__restrict__ p_x) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b || !flag[i]) return;
+  uint64_t k = keys[i];
+  uint32_t j = pos[i];
+  p_ul[j] = ((k >> dbits) << 32) | leaf[i];
+  p_x[j] = (uint32_t)(k & ((1ull << dbits) - 1));
+}
+
+__global__ void k_group_flags(const uint64_t *__restrict__ p_ul,
+                              const uint32_t *__restrict__ d_nitems, uint64_t b,
+                              uint32_t *__restrict__ gflag) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= b) return;
+  uint32_t n = *d_nitems;
+  gflag[j] = (j < n && (j == 0 || p_ul[j] != p_ul[j - 1])) ? 1u : 0u;
+}
+
+__global__ void k_group_start(const uint32_t *__restrict__ gflag,
+                              const uint32_t *__restrict__ gpos,
+                              const uint32_t *__restrict__ d_nitems,
+                              const uint32_t *__restrict__ d_ngroups,
+                              uint64_t b, uint32_t *__restrict__ g_start) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= b) return;
+  if (gflag[j]) g_start[gpos[j]] = (uint32_t)j;
+  if (j == 0) g_start[*d_ngroups] = *d_nitems;
+}
+
+// ---------------------------------------------------------------- step 6
+// insert: warp per group
+__global__ void k_classify_insert(DGraph g, PmaParams p,
+                                  const uint64_t *__restrict__ p_ul,
+                                  const uint32_t *__restrict__ g_start,
+                                  const uint32_t *__restrict__ d_ngroups,
+                                  const uint32_t *__restrict__ d_nitems,
+                                  uint8_t *__restrict__ gtype,
+                                  uint8_t *__restrict__ glev,
+                                  uint32_t *__restrict__ gw0,
+                                  uint32_t *__restrict__ gw1) {
+  uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gid >= *d_ngroups) return;
+  const uint32_t nitems = *d_nitems;
+  uint32_t j0 = g_start[gid], j1 = g_start[gid + 1];
+  uint32_t k = j1 - j0;
+  uint64_t key = p_ul[j0];
+  uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
+  uint64_t base = g.base[u];
+  uint32_t cap = g.cap[u], deg = g.deg[u];
+  uint8_t type;
+  uint32_t lev = 0, w0 = leaf, w1 = leaf + 1;
+  if (cap <= kLeaf) {
+    if (deg + k <= cap) {
+      type = kMerge;
+    } else {
+      type = kResize;
+      lev = 31;
+      w0 = 0;
+      w1 = 1;
+    }
+  } else {
+    uint64_t lbase = base >> kLeafLog;
+    uint32_t c = g.lcnt[lbase + leaf];
+    if (c + k <= kLeaf) {
+      type = kMerge;
+    } else {
+      uint32_t H = log2_floor(cap >> kLeafLog);
+      uint64_t old = c;
+      uint32_t size = 1;
+      type = kResize;
+      for (uint32_t t = 1; t <= H; t++) {
+        uint32_t nw0 = (leaf >> t) << t;
+        if (nw0 == w0)
+          old += warp_sum_lcnt(g.lcnt, lbase + w0 + size, lbase + w0 + 2 * size);
+        else
+          old += warp_sum_lcnt(g.lcnt, lbase + nw0, lbase + w0);
+        w0 = nw0;
+        size <<= 1;
+        w1 = w0 + size;
+        uint64_t kk = (uint64_t)u << 32;
+        uint32_t newc = lb_u64(p_ul, nitems, kk | w1) - lb_u64(p_ul, nitems, kk | w0);
+        if (old + newc <= window_upper(p, t, H)) {
+          type = kWindow;
+          lev = t;
+          break;
+        }
+      }
+      if (type == kResize) {
+        lev = 31;
+        w0 = 0;
+        w1 = cap >> kLeafLog;
+      }
+    }
+  }
+  if (lane == 0) {
+    gtype[gid] = type;
+    glev[gid] = (uint8_t)lev;
+    gw0[gid] = w0;
+    gw1[gid] = w1;
+  }
+}
+
+// remove, first pass: delete inside each touched leaf (warp per group) and
+// take the count off the row's degree
+__global__ void k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
+                              const uint32_t *__restrict__ p_x,
+                              const uint32_t *__restrict__ g_start,
+                              const uint32_t *__restrict__ d_ngroups) {
+  uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gid >= *d_ngroups) return;
+  uint32_t j0 = g_start[gid], j1 = g_start[gid + 1];
+  uint32_t k = j1 - j0;
+  uint64_t key = p_ul[j0];
+  uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
+  uint64_t base = g.base[u];
+  uint32_t cap = g.cap[u], deg = g.deg[u];
+  uint32_t c = leaf_count(g, base, cap, deg, leaf);
+  uint64_t S = base + ((uint64_t)leaf << kLeafLog);
+  uint32_t a = lane < c ? g.slots[S + lane] : kEmpty;
+  uint32_t d = lane < k ? p_x[j0 + lane] : kEmpty;
+  bool del = false;
+  for (uint32_t j = 0; j < k; j++) del |= (__shfl_sync(0xffffffffu, d, j) == a);
+  bool keep = lane < c && !del;
+  uint32_t mask = __ballot_sync(0xffffffffu, keep);
+  uint32_t pos = __popc(mask & ((1u << lane) - 1u));
+  __syncwarp();
+  if (keep) g.slots[S + pos] = a;
+  if (lane >= c - k && lane < c) g.slots[S + lane] = kEmpty;
+  if (lane == 0) {
+    if (cap > kLeaf) g.lcnt[(base >> kLeafLog) + leaf] = (uint8_t)(c - k);
+    atomicSub(&g.deg[u], k);
+  }
+}
+
+// remove, second pass: leaves under the lower bound climb to a window or
+// resize the segment (warp per group)
+__global__ void k_classify_remove(DGraph g, PmaParams p,
+                                  const uint64_t *__restrict__ p_ul,
+                                  const uint32_t *__restrict__ g_start,
+                                  const uint32_t *__restrict__ d_ngroups,
+                                  uint8_t *__restrict__ gtype,
+                                  uint8_t *__restrict__ glev,
+                                  uint32_t *__restrict__ gw0,
+                                  uint32_t *__restrict__ gw1) {
+  uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gid >= *d_ngroups) return;
+  uint64_t key = p_ul[g_start[gid]];
+  uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
+  uint64_t base = g.base[u];
+  uint32_t cap = g.cap[u], deg = g.deg[u];  // deg is already reduced
+  uint8_t type = kNone;
+  uint32_t lev = 0, w0 = leaf, w1 = leaf + 1;
+  if (cap <= kLeaf) {
+    if (deg == 0 || (cap > 1 && 4 * deg <= cap)) {
+      type = kResize;
+      lev = 31;
+      w0 = 0;
+      w1 = 1;
+    }
+  } else {
+    uint64_t lbase = base >> kLeafLog;
+    uint32_t H = log2_floor(cap >> kLeafLog);
+    uint64_t cur = g.lcnt[lbase + leaf];
+    if (cur < window_lower(p, 0, H)) {
+      uint32_t size = 1;
+      type = kResize;
+      for (uint32_t t = 1; t <= H; t++) {
+        uint32_t nw0 = (leaf >> t) << t;
+        if (nw0 == w0)
+          cur += warp_sum_lcnt(g.lcnt, lbase + w0 + size, lbase + w0 + 2 * size);
+        else
+          cur += warp_sum_lcnt(g.lcnt, lbase + nw0, lbase + w0);
+        w0 = nw0;
+        size <<= 1;
+        w1 = w0 + size;
+        if (cur >= window_lower(p, t, H)) {
+          type = kWindow;
+          lev = t;
+          break;
+        }
+      }
+      if (type == kResize) {
+        lev = 31;
+        w0 = 0;
+        w1 = cap >> kLeafLog;
+      }
+    }
+  }
+  if (lane == 0) {
+    gtype[gid] = type;
+    glev[gid] = (uint8_t)lev;
+    gw0[gid] = w0;
+    gw1[gid] = w1;
+  }
+}
+
+// ---------------------------------------------------------------- step 7
+constexpr uint64_t kWinMask = (1ull << 27) - 1;
+
+__global__ void k_dom_keys(const uint64_t *__restrict__ p_ul,
+                           const uint32_t *__restrict__ g_start,
+                           const uint8_t *__restrict__ gtype,
+                           const uint8_t *__restrict__ glev,
+                           const uint32_t *__restrict__ gw0,
+                           const uint32_t *__restrict__ gw1,
+                           const uint32_t *__restrict__ d_ngroups, uint64_t gmax,
+                           uint64_t *__restrict__ fkey,
+                           uint64_t *__restrict__ bkey) {
+  uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= gmax) return;
+  uint64_t f = 0, bk = ~0ull;
+  if (gid < *d_ngroups && gtype[gid] >= kWindow) {
+    uint64_t u = p_ul[g_start[gid]] >> 32;
+    uint64_t lev = glev[gid];
+    f = (u << 32) | ((uint64_t)gw1[gid] << 5) | lev;
+    bk = (u << 32) | ((uint64_t)gw0[gid] << 5) | (31 - lev);
+  }
+  fkey[gid] = f;
+  bkey[gid] = bk;
+}
+
+// fscan[g] = max of fkey over groups before g, bscan[g] = min of bkey over
+// groups after g.  A group is covered when a window of the same row from
+// either side contains its leaf and is larger (or equal and earlier).
+__global__ void k_dom_classify(const uint64_t *__restrict__ p_ul,
+                               const uint32_t *__restrict__ g_start,
+                               const uint8_t *__restrict__ gtype,
+                               const uint8_t *__restrict__ glev,
+                               const uint64_t *__restrict__ fscan,
+                               const uint64_t *__restrict__ bscan,
+                               const uint32_t *__restrict__ d_ngroups,
+                               uint64_t gmax, uint32_t *__restrict__ mflag,
+                               uint32_t *__restrict__ tflag) {
+  uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= gmax) return;
+  uint32_t mf = 0, tf = 0;
+  if (gid < *d_ngroups && gtype[gid] != kNone) {
+    uint64_t key = p_ul[g_start[gid]];
+    uint64_t u = key >> 32;
+    uint32_t leaf = (uint32_t)key;
+    uint64_t L = fscan[gid], R = bscan[gid];
+    bool lcov = L != 0 && (L >> 32) == u && ((L >> 5) & kWinMask) > leaf;
+    bool rcov = R != ~0ull && (R >> 32) == u && ((R >> 5) & kWinMask) <= leaf;
+    uint32_t lt = (uint32_t)(L & 31), rt = 31u - (uint32_t)(R & 31);
+    if (gtype[gid] == kMerge) {
+      mf = !(lcov || rcov);
+    } else {
+      uint32_t lev = glev[gid];
+      bool dom = (lcov && lt >= lev) || (rcov && rt > lev);
+      tf = !dom;
+    }
+  }
+  mflag[gid] = mf;
+  tflag[gid] = tf;
+}
+
+__global__ void k_emit(const uint32_t *__restrict__ mflag,
+                       const uint32_t *__restrict__ mpos,
+                       const uint32_t *__restrict__ tflag,
+                       const uint32_t *__restrict__ tpos, uint64_t gmax,
+                       uint32_t *__restrict__ merge_list,
+                       uint32_t *__restrict__ task_group) {
+  uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= gmax) return;
+  if (mflag[gid]) merge_list[mpos[gid]] = (uint32_t)gid;
+  if (tflag[gid]) task_group[tpos[gid]] = (uint32_t)gid;
+}
+
+// ---------------------------------------------------------------- step 8
+struct Tasks {
+  uint32_t *u;
+  uint32_t *w0;      // first source/destination leaf (0 for a resize)
+  uint64_t *key;     // (u << 32) | w0, ascending
+  uint64_t *nsrc;    // leaves read
+  uint64_t *ndst;    // leaves written
+  uint32_t *newbeg;  // range of packed items merged in (insert)
+  uint32_t *newend;
+  uint64_t *total;   // elements after the task
+  uint64_t *capn;    // new capacity (resize), else 0
+  uint32_t *rank;    // rank within the capacity class (resize)
+  uint8_t *type;
+  uint64_t *out;     // exclusive prefix of total: staging offset
+  uint64_t *soff;    // exclusive prefix of nsrc
+  uint64_t *doff;    // exclusive prefix of ndst
+  unsigned long long *err;  // count of out-of-range staging ranks
+};
+
+// warp per task slot (all gmax slots, so the prefix scans see zeros beyond
+// the task count)
+__global__ void k_task_setup(DGraph g, PmaParams p, bool insert,
+                             const uint64_t *__restrict__ p_ul,
+                             const uint32_t *__restrict__ g_start,
+                             const uint8_t *__restrict__ gtype,
+                             const uint32_t *__restrict__ gw0,
+                             const uint32_t *__restrict__ gw1,
+                             const uint32_t *__restrict__ task_group,
+                             const uint32_t *__restrict__ d_ntasks,
+                             const uint32_t *__restrict__ d_nitems,
+                             uint64_t gmax, Tasks t,
+                             uint32_t *__restrict__ class_cnt) {
+  uint64_t tid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (tid >= gmax) return;
+  if (tid >= *d_ntasks) {
+    if (lane == 0) {
+      t.total[tid] = 0;
+      t.nsrc[tid] = 0;
+      t.ndst[tid] = 0;
+    }
+    return;
+  }
+  const uint32_t nitems = *d_nitems;
+  uint32_t gid = task_group[tid];
+  uint32_t u = (uint32_t)(p_ul[g_start[gid]] >> 32);
+  uint8_t type = gtype[gid];
+  uint64_t base = g.base[u];
+  uint32_t cap = g.cap[u], deg = g.deg[u];
+  uint64_t kk = (uint64_t)u << 32;
+  uint32_t w0, nsrc, nb = 0, ne = 0;
+  uint64_t old, capn = 0, ndst;
+  uint32_t rank = 0;
+  if (type == kWindow) {
+    w0 = gw0[gid];
+    uint32_t w1 = gw1[gid];
+    nsrc = w1 - w0;
+    old = warp_sum_lcnt(g.lcnt, (base >> kLeafLog) + w0, (base >> kLeafLog) + w1);
+    if (insert) {
+      nb = lb_u64(p_ul, nitems, kk | w0);
+      ne = lb_u64(p_ul, nitems, kk | w1);
+    }
+    ndst = nsrc;
+  } else {
+    w0 = 0;
+    nsrc = cap == 0 ? 0 : nleaves_of(cap);
+    old = deg;
+    if (insert) {
+      nb = lb_u64(p_ul, nitems, kk);
+      ne = lb_u64(p_ul, nitems, kk + (1ull << 32));
+    }
+    capn = cap_for(old + (ne - nb), p.grow_fill);
+    ndst = capn == 0 ? 0 : nleaves_of((uint32_t)capn);
+    if (lane == 0 && capn > 0) rank = atomicAdd(&class_cnt[log2_floor(capn)], 1u);
+  }
+  if (lane == 0) {
+    t.u[tid] = u;
+    t.w0[tid] = w0;
+    t.key[tid] = kk | w0;
+    t.nsrc[tid] = nsrc;
+    t.ndst[tid] = ndst;
+    t.newbeg[tid] = nb;
+    t.newend[tid] = ne;
+    t.total[tid] = old + (ne - nb);
+    t.capn[tid] = capn;
+    t.rank[tid] = rank;
+    t.type[tid] = type;
+  }
+}
+
+// ---------------------------------------------------------------- step 9
+__global__ void k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul,
+                             const uint32_t *__restrict__ p_x,
+                             const uint32_t *__restrict__ g_start,
+                             const uint32_t *__restrict__ merge_list,
+                             uint32_t nmerge) {
+  uint64_t tid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (tid >= nmerge) return;
+  uint32_t gid = merge_list[tid];
+  uint32_t j0 = g_start[gid], j1 = g_start[gid + 1];
+  uint32_t k = j1 - j0;
+  uint64_t key = p_ul[j0];
+  uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
+  uint64_t base = g.base[u];
+  uint32_t cap = g.cap[u], deg = g.deg[u];
+  uint32_t c = leaf_count(g, base, cap, deg, leaf);
+  uint64_t S = base + ((uint64_t)leaf << kLeafLog);
+  uint32_t a = lane < c ? g.slots[S + lane] : kEmpty;
+  uint32_t x = lane < k ? p_x[j0 + lane] : kEmpty;
+  uint32_t pa = lane, px = lane;
+#pragma unroll 8
+  for (int j = 0; j < 32; j++) {
+    uint32_t xj = __shfl_sync(0xffffffffu, x, j);
+    uint32_t aj = __shfl_sync(0xffffffffu, a, j);
+    pa += ((uint32_t)j < k && xj < a);
+    px += ((uint32_t)j < c && aj < x);
+  }
+  __syncwarp();
+  if (lane < c) g.slots[S + pa] = a;
+  if (lane < k) g.slots[S + px] = x;
+  if (lane == 0 && cap > kLeaf) g.lcnt[(base >> kLeafLog) + leaf] = (uint8_t)(c + k);
+}
+
+__device__ __forceinline__ uint64_t task_of(const uint64_t *off, uint32_t ntasks,
+                                            uint64_t idx) {
+  // last task whose offset <= idx (offsets non-decreasing; a task with zero
+  // leaves shares its offset with the next one)
+  uint64_t lo = 0, hi = ntasks;
+  while (hi - lo > 1) {
+    uint64_t mid = (lo + hi) >> 1;
+    if (off[mid] <= idx)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_src_counts(DGraph g, Tasks t, uint32_t ntasks,
+                             uint64_t nsrc_total, uint64_t *__restrict__ scnt) {
+  uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsrc_total) return;
+  uint64_t tau = task_of(t.soff, ntasks, s);
+  uint32_t u = t.u[tau];
+  uint32_t l = t.w0[tau] + (uint32_t)(s - t.soff[tau]);
+  scnt[s] = leaf_count(g, g.base[u], g.cap[u], g.deg[u], l);
+}
+
+// warp per source leaf: old elements to their merged rank
+__global__ void k_gather_old(DGraph g, Tasks t, uint32_t ntasks,
+                             uint64_t nsrc_total,
+                             const uint64_t *__restrict__ spre,
+                             const uint32_t *__restrict__ p_x,
+                             uint32_t *__restrict__ stage) {
+  uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (s >= nsrc_total) return;
+  uint64_t tau = task_of(t.soff, ntasks, s);
+  uint32_t u = t.u[tau];
+  uint32_t l = t.w0[tau] + (uint32_t)(s - t.soff[tau]);
+  uint64_t base = g.base[u];
+  uint32_t c = leaf_count(g, base, g.cap[u], g.deg[u], l);
+  if ((uint32_t)lane >= c) return;
+  uint32_t a = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
+  uint64_t rank = (spre[s] - spre[t.soff[tau]]) + lane +
+                  count_less(p_x, t.newbeg[tau], t.newend[tau], a);
+  if (rank >= t.total[tau]) {
+    atomicAdd(t.err, 1ull);
+    return;
+  }
+  stage[t.out[tau] + rank] = a;
+}
+
+// thread per packed item owned by a task: new elements to their merged rank
+__global__ void k_gather_new(DGraph g, Tasks t, uint32_t ntasks,
+                             const uint64_t *__restrict__ spre,
+                             const uint64_t *__restrict__ p_ul,
+                             const uint32_t *__restrict__ p_x, uint32_t nitems,
+                             uint32_t *__restrict__ stage) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nitems || ntasks == 0) return;
+  uint64_t key = p_ul[j];
+  if (key < t.key[0]) return;
+  uint64_t tau = last_le_u64(t.key, ntasks, key);
+  uint32_t u = (uint32_t)(key >> 32);
+  if (t.u[tau] != u || j < t.newbeg[tau] || j >= t.newend[tau]) return;
+  uint32_t x = p_x[j];
+  uint64_t base = g.base[u];
+  uint32_t cap = g.cap[u], deg = g.deg[u];
+  uint64_t old_less = 0;
+  uint32_t nsrc = (uint32_t)t.nsrc[tau];
+  if (nsrc > 0) {
+    uint32_t w0 = t.w0[tau];
+    uint32_t lo = 0, hi = nsrc;  // last leaf of the window with head <= x
+    while (hi - lo > 1) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (g.slots[base + ((uint64_t)(w0 + mid) << kLeafLog)] <= x)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    uint32_t l = w0 + lo;
+    uint32_t c = leaf_count(g, base, cap, deg, l);
+    uint32_t pos = leaf_lower_bound(g.slots + base + ((uint64_t)l << kLeafLog), c, x);
+    uint64_t s0 = t.soff[tau];
+    old_less = (spre[s0 + lo] - spre[s0]) + pos;
+  }
+  uint64_t rank = (j - t.newbeg[tau]) + old_less;
+  if (rank >= t.total[tau]) {
+    atomicAdd(t.err, 1ull);
+    return;
+  }
+  stage[t.out[tau] + rank] = x;
+}
+
+__device__ __forceinline__ uint64_t task_new_base(const Tasks &t, uint64_t tau,
+                                                  const uint64_t *class_start) {
+  uint64_t capn = t.capn[tau];
+  return class_start[log2_floor(capn)] + (uint64_t)t.rank[tau] * capn;
+}
+
+// warp per destination leaf: even redistribution of the staged elements
+__global__ void k_scatter(DGraph g, Tasks t, uint32_t ntasks,
+                          uint64_t ndst_total,
+                          const uint64_t *__restrict__ class_start,
+                          const uint32_t *__restrict__ stage) {
+  uint64_t d = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (d >= ndst_total) return;
+  uint64_t tau = task_of(t.doff, ntasks, d);
+  uint64_t i = d - t.doff[tau];
+  uint64_t NL = t.ndst[tau], T = t.total[tau];
+  uint64_t per = T / NL, ext = T % NL;
+  uint32_t cnt = (uint32_t)(per + (i < ext));
+  uint64_t start = i * per + (i < ext ? i : ext);
+  uint64_t S;
+  uint32_t leafsize = kLeaf;
+  bool multi = true;
+  if (t.type[tau] == kResize) {
+    uint64_t capn = t.capn[tau];
+    S = task_new_base(t, tau, class_start) + (i << kLeafLog);
+    if (capn <= kLeaf) {
+      leafsize = (uint32_t)capn;
+      multi = false;
+    }
+  } else {
+    S = g.base[t.u[tau]] + ((uint64_t)(t.w0[tau] + i) << kLeafLog);
+  }
+  if ((uint32_t)lane < leafsize)
+    g.slots[S + lane] = (uint32_t)lane < cnt ? stage[t.out[tau] + start + lane] : kEmpty;
+  if (lane == 0 && multi) g.lcnt[S >> kLeafLog] = (uint8_t)cnt;
+}
+
+__global__ void k_finalize(DGraph g, Tasks t, uint32_t ntasks,
+                           const uint64_t *__restrict__ class_start) {
+  uint64_t tau = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tau >= ntasks || t.type[tau] != kResize) return;
+  uint32_t u = t.u[tau];
+  uint64_t capn = t.capn[tau];
+  g.base[u] = capn ? task_new_base(t, tau, class_start) : 0;
+  g.cap[u] = (uint32_t)capn;
+}
+
+__global__ void k_deg_add(DGraph g, const uint64_t *__restrict__ p_ul,
+                          const uint32_t *__restrict__ g_start,
+                          const uint32_t *__restrict__ d_ngroups, uint64_t gmax) {
+  uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= gmax || gid >= *d_ngroups) return;
+  uint32_t u = (uint32_t)(p_ul[g_start[gid]] >> 32);
+  atomicAdd(&g.deg[u], g_start[gid + 1] - g_start[gid]);
+}
+
+// ---------------------------------------------------------------- repack
+__global__ void k_class_count(const uint32_t *__restrict__ cap, uint32_t n,
+                              uint32_t *__restrict__ cnt) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n || cap[v] == 0) return;
+  atomicAdd(&cnt[log2_floor(cap[v])], 1u);
+}
+
+__global__ void k_repack_assign(const uint32_t *__restrict__ cap, uint32_t n,
+                                const uint64_t *__restrict__ class_start,
+                                uint32_t *__restrict__ ctr,
+                                uint64_t *__restrict__ newbase) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  uint32_t c = cap[v];
+  if (c == 0) {
+    newbase[v] = 0;
+    return;
+  }
+  uint32_t cls = log2_floor(c);
+  newbase[v] = class_start[cls] + (uint64_t)atomicAdd(&ctr[cls], 1u) * c;
+}
+
+__global__ void k_repack_copy(const uint32_t *__restrict__ cap, uint32_t n,
+                              const uint64_t *__restrict__ oldbase,
+                              const uint64_t *__restrict__ newbase,
+                              const uint32_t *__restrict__ oslots,
+                              const uint8_t *__restrict__ olcnt,
+                              uint32_t *__restrict__ nslots_,
+                              uint8_t *__restrict__ nlcnt) {
+  uint64_t v = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (v >= n) return;
+  uint32_t c = cap[v];
+  if (c == 0) return;
+  uint64_t ob = oldbase[v], nb = newbase[v];
+  for (uint64_t i = lane; i < c; i += 32) nslots_[nb + i] = oslots[ob + i];
+  if (c > kLeaf)
+    for (uint64_t l = lane; l < (c >> kLeafLog); l += 32)
+      nlcnt[(nb >> kLeafLog) + l] = olcnt[(ob >> kLeafLog) + l];
+}
+
+
+}  // namespace
+
+// ====================================================================== host
+
+static thread_local char g_errmsg[512];
+
+void set_error_message(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_errmsg, sizeof(g_errmsg), fmt, ap);
+  va_end(ap);
+}
+void set_cuda_error(cudaError_t e, const char *what, const char *file,
+                    int line) {
+  set_error_message("CUDA error %s (%s) at %s:%d: %s", cudaGetErrorName(e),
+                    cudaGetErrorString(e), file, line, what);
+}
+const char *error_message() { return g_errmsg; }
+
+void LeafDir::release() {
+  cudaFree(owner);
+  cudaFree(slot);
+  cudaFree(cnt);
+  cudaFree(pre);
+  cudaFree(vleaf);
+  owner = nullptr;
+  slot = nullptr;
+  cnt = nullptr;
+  pre = nullptr;
+  vleaf = nullptr;
+  cap = 0;
+  nleaves = 0;
+  version = ~0ull;
+}
+
+void *pinned(sst_graph *g, size_t bytes) {
+  if (bytes <= g->h_pinned_cap) return g->h_pinned;
+  if (g->h_pinned) cudaFreeHost(g->h_pinned);
+  size_t want = bytes + bytes / 4 + 4096;
+  if (cudaMallocHost(&g->h_pinned, want) != cudaSuccess) {
+    g->h_pinned = nullptr;
+    g->h_pinned_cap = 0;
+    return nullptr;
+  }
+  g->h_pinned_cap = want;
+  return g->h_pinned;
+}
+
+uint64_t graph_device_bytes(const sst_graph *g) {
+  return (uint64_t)g->n * 16 + g->nslots * 4 + g->nslots / kLeaf +
+         g->arena.cap + g->work.cap +
+         g->dir.cap * (4 + 8 + 4 + 8) + (uint64_t)(g->n + 1) * 8;
+}
+
+static sst_status budget_check(sst_graph *g, uint64_t extra) {
+  if (g->budget && graph_device_bytes(g) + extra > g->budget) {
+    set_error_message("HBM budget of %llu bytes exceeded (need %llu more)",
+                      (unsigned long long)g->budget,
+                      (unsigned long long)extra);
+    return SST_EBUDGET;
+  }
+  return SST_OK;
+}
+
+static sst_status alloc_slab(sst_graph *g, uint64_t nslots, uint32_t **slots,
+                             uint8_t **lcnt) {
+  if (cudaMalloc(slots, nslots * 4) != cudaSuccess) {
+    cudaGetLastError();
+    set_error_message("cannot allocate a slab of %llu slots",
+                      (unsigned long long)nslots);
+    return SST_ENOMEM;
+  }
+  if (cudaMalloc(lcnt, nslots / kLeaf + 1) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(*slots);
+    set_error_message("cannot allocate leaf counts");
+    return SST_ENOMEM;
+  }
+  return SST_OK;
+}
+
+sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
+                      const sst_config *cfg) {
+  g->n = height;
+  g->width = width;
+  g->rbits = bits_for(height);
+  g->dbits = std::max(1, bits_for(width ? width - 1 : 0));
+  if (cfg) {
+    g->device = cfg->device;
+    g->budget = cfg->hbm_budget_bytes;
+    if (cfg->upper_root > 0) g->params.upper_root = cfg->upper_root;
+    if (cfg->lower_root > 0) g->params.lower_root = cfg->lower_root;
+    if (cfg->grow_fill > 0) g->params.grow_fill = cfg->grow_fill;
+  }
+  SST_CUDA_TRY(cudaSetDevice(g->device));
+  SST_CUDA_TRY(cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking));
+  g->stream = g->own_stream;
+  uint64_t n = std::max<uint64_t>(height, 1);
+  SST_CUDA_TRY(cudaMalloc(&g->d_base, n * 8));
+  SST_CUDA_TRY(cudaMalloc(&g->d_cap, n * 4));
+  SST_CUDA_TRY(cudaMalloc(&g->d_deg, n * 4));
+  SST_CUDA_TRY(cudaMemsetAsync(g->d_base, 0, n * 8, g->stream));
+  SST_CUDA_TRY(cudaMemsetAsync(g->d_cap, 0, n * 4, g->stream));
+  SST_CUDA_TRY(cudaMemsetAsync(g->d_deg, 0, n * 4, g->stream));
+  uint64_t slots = cfg && cfg->initial_slots ? cfg->initial_slots : (1ull << 20);
+  slots = (slots + kLeaf - 1) & ~uint64_t(kLeaf - 1);
+  sst_status st = budget_check(g, slots * 4 + slots / kLeaf);
+  if (st != SST_OK) return st;
+  st = alloc_slab(g, slots, &g->d_slots, &g->d_lcnt);
+  if (st != SST_OK) return st;
+  g->nslots = slots;
+  g->bump = 0;
+  SST_CUDA_TRY(cudaMallocHost(&g->h_plan, sizeof(PlanSummary)));
+  SST_CUDA_TRY(cudaMalloc(&g->d_plan, sizeof(PlanSummary)));
+  SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
+  return SST_OK;
+}
+
+void graph_release(sst_graph *g) {
+  cudaSetDevice(g->device);
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  cudaFree(g->d_base);
+  cudaFree(g->d_cap);
+  cudaFree(g->d_deg);
+  cudaFree(g->d_slots);
+  cudaFree(g->d_lcnt);
+  cudaFree(g->d_plan);
+  if (g->h_plan) cudaFreeHost(g->h_plan);
+  if (g->h_pinned) cudaFreeHost(g->h_pinned);
+  g->arena.release();
+  g->work.release();
+  g->dir.release();
+  trav_release(g);
+  if (g->own_stream) cudaStreamDestroy(g->own_stream);
+  g->own_stream = nullptr;
+  g->stream = nullptr;
+}
+
+sst_status graph_clone(const sst_graph *src, sst_graph *dst) {
+  sst_config cfg{};
+  cfg.device = src->device;
+  cfg.hbm_budget_bytes = src->budget;
+  cfg.initial_slots = std::max<uint64_t>(src->nslots, kLeaf);
+  cfg.upper_root = src->params.upper_root;
+  cfg.lower_root = src->params.lower_root;
+  cfg.grow_fill = src->params.grow_fill;
+  sst_status st = graph_init(dst, src->n, src->width, &cfg);
+  if (st != SST_OK) return st;
+  SST_CUDA_TRY(cudaStreamSynchronize(src->stream));
+  uint64_t n = std::max<uint64_t>(src->n, 1);
+  SST_CUDA_TRY(cudaMemcpyAsync(dst->d_base, src->d_base, n * 8, cudaMemcpyDeviceToDevice, dst->stream));
+  SST_CUDA_TRY(cudaMemcpyAsync(dst->d_cap, src->d_cap, n * 4, cudaMemcpyDeviceToDevice, dst->stream));
+  SST_CUDA_TRY(cudaMemcpyAsync(dst->d_deg, src->d_deg, n * 4, cudaMemcpyDeviceToDevice, dst->stream));
+  SST_CUDA_TRY(cudaMemcpyAsync(dst->d_slots, src->d_slots, src->bump * 4, cudaMemcpyDeviceToDevice, dst->stream));
+  SST_CUDA_TRY(cudaMemcpyAsync(dst->d_lcnt, src->d_lcnt, src->bump / kLeaf + 1, cudaMemcpyDeviceToDevice, dst->stream));
+  SST_CUDA_TRY(cudaStreamSynchronize(dst->stream));
+  dst->bump = src->bump;
+  dst->m = src->m;
+  dst->version = 1;
+  return SST_OK;
+}
+
+// Move every live segment into a fresh slab, packed by capacity class, with
+// room for `extra` more slots.  Freed segments are reclaimed here.
+sst_status repack(sst_graph *g, uint64_t extra) {
+  cudaStream_t s = g->stream;
+  uint32_t n = g->n;
+  // own temporaries: the arena may hold a batch in flight
+  char *tmp = nullptr;
+  uint64_t tbytes = 512 + (uint64_t)std::max<uint32_t>(n, 1) * 8;
+  SST_CUDA_TRY(cudaMalloc(&tmp, tbytes));
+  uint32_t *cnt = reinterpret_cast<uint32_t *>(tmp);
+  uint64_t *cstart = reinterpret_cast<uint64_t *>(tmp + 256);
+  uint64_t *newbase = reinterpret_cast<uint64_t *>(tmp + 512);
+  SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, kNumClasses * 8, s));
+  if (n) SST_LAUNCH(k_class_count, blocks_for(n), kTB, 0, s, g->d_cap, n, cnt);
+  uint32_t hcnt[kNumClasses];
+  SST_CUDA_TRY(cudaMemcpyAsync(hcnt, cnt, sizeof(hcnt), cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t hstart[kNumClasses];
+  uint64_t off = 0;
+  for (int c = kNumClasses - 1; c >= 0; c--) {
+    hstart[c] = off;
+    off += (uint64_t)hcnt[c] << c;
+  }
+  uint64_t live = off;
+  uint64_t need = live + extra + kLeaf;
+  uint64_t nsl = g->nslots;
+  if (need > nsl / 2 + nsl / 4) nsl = std::max<uint64_t>(2 * need, 1ull << 20);
+  nsl = (nsl + kLeaf - 1) & ~uint64_t(kLeaf - 1);
+  // the new slab coexists with the old one while segments move
+  sst_status st = budget_check(g, nsl * 4 + nsl / kLeaf);
+  if (st != SST_OK) {
+    cudaFree(tmp);
+    return st;
+  }
+  uint32_t *nslots_;
+  uint8_t *nlcnt;
+  st = alloc_slab(g, nsl, &nslots_, &nlcnt);
+  if (st != SST_OK) {
+    cudaFree(tmp);
+    return st;
+  }
+  SST_CUDA_TRY(cudaMemcpyAsync(cstart, hstart, sizeof(hstart), cudaMemcpyHostToDevice, s));
+  if (n) {
+    SST_LAUNCH(k_repack_assign, blocks_for(n), kTB, 0, s, g->d_cap, n, cstart,
+               cnt + kNumClasses, newbase);
+    SST_LAUNCH(k_repack_copy, warp_blocks(n), kTB, 0, s, g->d_cap, n, g->d_base,
+               newbase, g->d_slots, g->d_lcnt, nslots_, nlcnt);
+    SST_CUDA_TRY(cudaMemcpyAsync(g->d_base, newbase, (uint64_t)n * 8, cudaMemcpyDeviceToDevice, s));
+  }
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  SST_CUDA_TRY(cudaGetLastError());
+  cudaFree(g->d_slots);
+  cudaFree(g->d_lcnt);
+  g->d_slots = nslots_;
+  g->d_lcnt = nlcnt;
+  g->nslots = nsl;
+  g->bump = live;
+  cudaFree(tmp);
+  return SST_OK;
+}
+
+// bytes of arena scratch an update batch of b pairs takes
+static size_t update_scratch_bytes(uint64_t b) {
+  size_t per = 8 * 2 + 4 * 4 + 8 + 4 + 4 * 3 + 1 * 2 + 4 * 2 + 8 * 4 + 4 * 6 +
+               8 * 8 + 4 * 4 + 1 + 64;
+  return b * per + radix_sort_scratch_bytes(b) + 8 * scan_scratch_bytes(b, 8) +
+         (1 << 16);
+}
+
+sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t b,
+                        bool insert, uint64_t *n_invalid) {
+  if (n_invalid) *n_invalid = 0;
+  if (b == 0) return SST_OK;
+  if (b > 0xFFFFFFF0ull) {
+    set_error_message("batch of %llu pairs exceeds 2^32", (unsigned long long)b);
+    return SST_EINVAL;
+  }
+  cudaStream_t s = g->stream;
+  size_t need = update_scratch_bytes(b);
+  if (need > g->arena.cap) {
+    sst_status st = budget_check(g, need - g->arena.cap);
+    if (st != SST_OK) return st;
+  }
+  SST_CUDA_TRY(g->arena.reserve(need));
+  Arena &A = g->arena;
+  A.reset();
+  PlanSummary *P = g->d_plan;
+  SST_CUDA_TRY(cudaMemsetAsync(P, 0, sizeof(PlanSummary), s));
+
+  const int dbits = g->dbits;
+  DGraph dg = g->view();
+  uint64_t *keys = A.take<uint64_t>(b), *ktmp = A.take<uint64_t>(b);
+  uint32_t *flag = A.take<uint32_t>(b), *pos = A.take<uint32_t>(b + 1);
+  uint32_t *leaf = A.take<uint32_t>(b);
+  uint64_t *p_ul = A.take<uint64_t>(b);
+  uint32_t *p_x = A.take<uint32_t>(b);
+  uint32_t *gflag = A.take<uint32_t>(b), *gpos = A.take<uint32_t>(b);
+  uint32_t *g_start = A.take<uint32_t>(b + 1);
+  uint8_t *gtype = A.take<uint8_t>(b), *glev = A.take<uint8_t>(b);
+  uint32_t *gw0 = A.take<uint32_t>(b), *gw1 = A.take<uint32_t>(b);
+  uint64_t *fkey = A.take<uint64_t>(b), *bkey = A.take<uint64_t>(b);
+  uint32_t *mflag = A.take<uint32_t>(b), *tflag = A.take<uint32_t>(b);
+  uint32_t *mpos = A.take<uint32_t>(b), *tpos = A.take<uint32_t>(b);
+  uint32_t *merge_list = A.take<uint32_t>(b), *task_group = A.take<uint32_t>(b);
+  Tasks T;
+  T.u = A.take<uint32_t>(b);
+  T.w0 = A.take<uint32_t>(b);
+  T.key = A.take<uint64_t>(b);
+  T.nsrc = A.take<uint64_t>(b);
+  T.ndst = A.take<uint64_t>(b);
+  T.newbeg = A.take<uint32_t>(b);
+  T.newend = A.take<uint32_t>(b);
+  T.total = A.take<uint64_t>(b);
+  T.capn = A.take<uint64_t>(b);
+  T.rank = A.take<uint32_t>(b);
+  T.type = A.take<uint8_t>(b);
+  T.out = A.take<uint64_t>(b);
+  T.soff = A.take<uint64_t>(b);
+  T.doff = A.take<uint64_t>(b);
+  T.err = &P->apply_err;
+  uint64_t *cstart = A.take<uint64_t>(kNumClasses);
+  if (!cstart) {
+    set_error_message("update scratch sizing error");
+    return SST_ENOMEM;
+  }
+
+  // 1-2: keys and sort
+  SST_LAUNCH(k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n, g->width,
+             dbits, insert, keys,
+             reinterpret_cast<unsigned long long *>(&P->invalid));
+  uint64_t *sorted = keys;
+  SST_CUDA_TRY(radix_sort_u64(keys, ktmp, b, g->rbits + dbits, A, s, &sorted));
+  // 3-5: locate, pack, group
+  SST_LAUNCH(k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg, insert,
+             flag, leaf);
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(flag, pos, b, 0u, OpAdd{}, true, false,
+                                      &P->n_items, A, s)));
+  SST_LAUNCH(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,
+             p_ul, p_x);
+  SST_LAUNCH(k_group_flags, blocks_for(b), kTB, 0, s, p_ul, &P->n_items, b, gflag);
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(gflag, gpos, b, 0u, OpAdd{}, true, false,
+                                      &P->n_groups, A, s)));
+  SST_LAUNCH(k_group_start, blocks_for(b), kTB, 0, s, gflag, gpos, &P->n_items,
+             &P->n_groups, b, g_start);
+  // 6: classify
+  if (insert) {
+    SST_LAUNCH(k_classify_insert, warp_blocks(b), kTB, 0, s, dg, g->params, p_ul,
+               g_start, &P->n_groups, &P->n_items, gtype, glev, gw0, gw1);
+  } else {
+    SST_LAUNCH(k_leaf_delete, warp_blocks(b), kTB, 0, s, dg, p_ul, p_x, g_start,
+               &P->n_groups);
+    SST_LAUNCH(k_classify_remove, warp_blocks(b), kTB, 0, s, dg, g->params, p_ul,
+               g_start, &P->n_groups, gtype, glev, gw0, gw1);
+  }
+  // 7: dominance
+  SST_LAUNCH(k_dom_keys, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
+             gw0, gw1, &P->n_groups, b, fkey, bkey);
+  SST_CUDA_TRY((scan<uint64_t, OpMax>(fkey, fkey, b, 0ull, OpMax{}, true, false,
+                                      nullptr, A, s)));
+  SST_CUDA_TRY((scan<uint64_t, OpMin>(bkey, bkey, b, ~0ull, OpMin{}, true, true,
+                                      nullptr, A, s)));
+  SST_LAUNCH(k_dom_classify, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
+             fkey, bkey, &P->n_groups, b, mflag, tflag);
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(mflag, mpos, b, 0u, OpAdd{}, true, false,
+                                      &P->n_merge, A, s)));
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(tflag, tpos, b, 0u, OpAdd{}, true, false,
+                                      &P->n_tasks, A, s)));
+  SST_LAUNCH(k_emit, blocks_for(b), kTB, 0, s, mflag, mpos, tflag, tpos, b,
+             merge_list, task_group);
+  // 8: plan
+  SST_LAUNCH(k_task_setup, warp_blocks(b), kTB, 0, s, dg, g->params, insert, p_ul,
+             g_start, gtype, gw0, gw1, task_group, &P->n_tasks, &P->n_items, b, T,
+             P->class_cnt);
+  SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.total, T.out, b, 0ull, OpAdd{}, true,
+                                      false, &P->task_elems, A, s)));
+  SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.nsrc, T.soff, b, 0ull, OpAdd{}, true,
+                                      false, &P->src_leaves, A, s)));
+  SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.ndst, T.doff, b, 0ull, OpAdd{}, true,
+                                      false, &P->dst_leaves, A, s)));
+  SST_CUDA_TRY(cudaMemcpyAsync(g->h_plan, P, sizeof(PlanSummary),
+                               cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  SST_CUDA_TRY(cudaGetLastError());
+  PlanSummary ps = *g->h_plan;
+  if (n_invalid) *n_invalid = ps.invalid;
+
+  // slab space for resized segments, laid out largest class first so each
+  // segment is aligned to min(cap, 32)
+  uint64_t grow = 0;
+  for (int c = 0; c < kNumClasses; c++) grow += (uint64_t)ps.class_cnt[c] << c;
+  uint64_t start = (g->bump + kLeaf - 1) & ~uint64_t(kLeaf - 1);
+  if (grow > 0 && start + grow > g->nslots) {
+    sst_status st = repack(g, grow);
+    if (st != SST_OK) return st;
+    dg = g->view();
+    start = (g->bump + kLeaf - 1) & ~uint64_t(kLeaf - 1);
+  }
+  uint64_t hstart[kNumClasses];
+  uint64_t off = start;
+  for (int c = kNumClasses - 1; c >= 0; c--) {
+    hstart[c] = off;
+    off += (uint64_t)ps.class_cnt[c] << c;
+  }
+  if (grow > 0) g->bump = off;
+  uint64_t *hs = static_cast<uint64_t *>(pinned(g, sizeof(hstart)));
+  if (!hs) return SST_ENOMEM;
+  memcpy(hs, hstart, sizeof(hstart));
+  SST_CUDA_TRY(cudaMemcpyAsync(cstart, hs, sizeof(hstart), cudaMemcpyHostToDevice, s));
+
+  // staging for window / resize tasks
+  size_t wneed = ps.task_elems * 4 + ps.src_leaves * 16 + scan_scratch_bytes(ps.src_leaves, 8) + 4096;
+  if (wneed > g->work.cap) {
+    sst_status st = budget_check(g, wneed - g->work.cap);
+    if (st != SST_OK) return st;
+  }
+  SST_CUDA_TRY(g->work.reserve(wneed));
+  g->work.reset();
+  uint32_t *stage = g->work.take<uint32_t>(ps.task_elems);
+  uint64_t *scnt = g->work.take<uint64_t>(ps.src_leaves);
+  uint64_t *spre = g->work.take<uint64_t>(ps.src_leaves);
+
+  // 9: apply
+  if (insert && ps.n_merge)
+    SST_LAUNCH(k_leaf_merge, warp_blocks(ps.n_merge), kTB, 0, s, dg, p_ul, p_x,
+               g_start, merge_list, ps.n_merge);
+  if (ps.n_tasks) {
+    if (ps.src_leaves) {
+      SST_LAUNCH(k_src_counts, blocks_for(ps.src_leaves), kTB, 0, s, dg, T,
+                 ps.n_tasks, ps.src_leaves, scnt);
+      SST_CUDA_TRY((scan<uint64_t, OpAdd>(scnt, spre, ps.src_leaves, 0ull,
+                                          OpAdd{}, true, false, nullptr,
+                                          g->work, s)));
+      SST_LAUNCH(k_gather_old, warp_blocks(ps.src_leaves), kTB, 0, s, dg, T,
+                 ps.n_tasks, ps.src_leaves, spre, p_x, stage);
+    }
+    if (insert && ps.n_items)
+      SST_LAUNCH(k_gather_new, blocks_for(ps.n_items), kTB, 0, s, dg, T,
+                 ps.n_tasks, spre, p_ul, p_x, ps.n_items, stage);
+    if (ps.dst_leaves)
+      SST_LAUNCH(k_scatter, warp_blocks(ps.dst_leaves), kTB, 0, s, dg, T,
+                 ps.n_tasks, ps.dst_leaves, cstart, stage);
+    SST_LAUNCH(k_finalize, blocks_for(ps.n_tasks), kTB, 0, s, dg, T, ps.n_tasks,
+               cstart);
+  }
+  if (insert)
+    SST_LAUNCH(k_deg_add, blocks_for(b), kTB, 0, s, dg, p_ul, g_start,
+               &P->n_groups, b);
+  SST_CUDA_TRY(cudaMemcpyAsync(&g->h_plan->apply_err, &P->apply_err, 8,
+                               cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  SST_CUDA_TRY(cudaGetLastError());
+  if (g->h_plan->apply_err) {
+    set_error_message("internal error: %llu staged ranks out of range",
+                      (unsigned long long)g->h_plan->apply_err);
+    return SST_EDEVICE;
+  }
+  if (insert)
+    g->m += ps.n_items;
+  else
+    g->m -= ps.n_items;
+  if (ps.n_items) g->version++;
+  return SST_OK;
+}
+
+// ------------------------------------------------------------ other paths
+namespace {
+__global__ void k_csr_to_pairs(const uint64_t *__restrict__ off,
+                               const uint32_t *__restrict__ cols, uint32_t n,
+                               uint32_t *__restrict__ pairs) {
+  uint64_t v = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (v >= n) return;
+  for (uint64_t i = off[v] + lane; i < off[v + 1]; i += 32) {
+    pairs[2 * i] = (uint32_t)v;
+    pairs[2 * i + 1] = cols[i];
+  }
+}
+
+__global__ void k_has(DGraph g, const uint32_t *__restrict__ pairs, uint64_t n,
+                      uint8_t *__restrict__ out) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t u = pairs[2 * i], x = pairs[2 * i + 1];
+  uint8_t r = 0;
+  if (u < g.n) {
+    uint64_t base = g.base[u];
+    uint32_t cap = g.cap[u];
+    if (cap) {
+      uint32_t l = find_leaf(g.slots, base, cap, x);
+      uint32_t c = leaf_count(g, base, cap, g.deg[u], l);
+      const uint32_t *p = g.slots + base + ((uint64_t)l << kLeafLog);
+      uint32_t pos = leaf_lower_bound(p, c, x);
+      r = pos < c && p[pos] == x;
+    }
+  }
+  out[i] = r;
+}
+
+__global__ void k_vertex_leaves(const uint32_t *__restrict__ cap, uint32_t n,
+                                uint64_t *__restrict__ nl) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  nl[v] = cap[v] ? nleaves_of(cap[v]) : 0;
+}
+
+// warp per vertex: its leaves into the directory
+__global__ void k_dir_fill(DGraph g, const uint64_t *__restrict__ vleaf,
+                           uint32_t *__restrict__ owner,
+                           uint64_t *__restrict__ slot,
+                           uint32_t *__restrict__ cnt) {
+  uint64_t v = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (v >= g.n) return;
+  uint64_t k0 = vleaf[v], k1 = vleaf[v + 1];
+  uint64_t base = g.base[v];
+  uint32_t cap = g.cap[v], deg = g.deg[v];
+  for (uint64_t k = k0 + lane; k < k1; k += 32) {
+    uint32_t l = (uint32_t)(k - k0);
+    owner[k] = (uint32_t)v;
+    slot[k] = base + ((uint64_t)l << kLeafLog);
+    cnt[k] = leaf_count(g, base, cap, deg, l);
+  }
+}
+
+// warp per leaf: copy into CSR position
+__global__ void k_dir_copy(const uint32_t *__restrict__ slots,
+                           const uint64_t *__restrict__ slot,
+                           const uint32_t *__restrict__ cnt,
+                           const uint64_t *__restrict__ pre, uint64_t nleaves,
+                           uint32_t *__restrict__ cols) {
+  uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (k >= nleaves) return;
+  if ((uint32_t)lane < cnt[k]) cols[pre[k] + lane] = slots[slot[k] + lane];
+}
+
+__global__ void k_widen(const uint32_t *__restrict__ in, uint64_t n,
+                        uint64_t *__restrict__ out) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[i];
+}
+
+__global__ void k_sample(const uint32_t *__restrict__ slots,
+                         const uint32_t *__restrict__ owner,
+                         const uint64_t *__restrict__ slot,
+                         const uint64_t *__restrict__ pre, uint64_t nleaves,
+                         uint64_t m, uint64_t seed, uint64_t first,
+                         uint64_t count, uint32_t *__restrict__ pairs) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  if (m == 0) {
+    pairs[2 * i] = pairs[2 * i + 1] = 0;
+    return;
+  }
+  uint64_t rank = __umul64hi(draw(seed, first + i, 0), m);
+  uint64_t k = last_le_u64(pre, nleaves, rank);
+  pairs[2 * i] = owner[k];
+  pairs[2 * i + 1] = slots[slot[k] + (rank - pre[k])];
+}
+
+// warp per leaf; 64-bit sum of its elements added to *out
+__global__ void k_sum_leaves(const uint32_t *__restrict__ slots,
+                             const uint64_t *__restrict__ slot,
+                             const uint32_t *__restrict__ cnt, uint64_t nleaves,
+                             unsigned long long *__restrict__ out) {
+  uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (k >= nleaves) return;
+  uint64_t v = (uint32_t)lane < cnt[k] ? slots[slot[k] + lane] : 0;
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+  if (lane == 0 && v) atomicAdd(out, (unsigned long long)v);
+}
+}  // namespace
+
+sst_status build_from_csr(sst_graph *g, const uint64_t *d_off,
+                          const uint32_t *d_cols) {
+  cudaStream_t s = g->stream;
+  uint64_t m = 0;
+  SST_CUDA_TRY(cudaMemcpyAsync(&m, d_off + g->n, 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t n = std::max<uint64_t>(g->n, 1);
+  SST_CUDA_TRY(cudaMemsetAsync(g->d_cap, 0, n * 4, s));
+  SST_CUDA_TRY(cudaMemsetAsync(g->d_deg, 0, n * 4, s));
+  SST_CUDA_TRY(cudaMemsetAsync(g->d_base, 0, n * 8, s));
+  g->bump = 0;
+  g->m = 0;
+  g->version++;
+  if (m == 0) return SST_OK;
+  uint32_t *pairs = nullptr;
+  SST_CUDA_TRY(cudaMallocAsync(&pairs, m * 8, s));
+  SST_LAUNCH(k_csr_to_pairs, warp_blocks(g->n), kTB, 0, s, d_off, d_cols, g->n, pairs);
+  sst_status st = update_batch(g, pairs, m, true, nullptr);
+  cudaFreeAsync(pairs, s);
+  return st;
+}
+
+sst_status has_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,
+                     uint8_t *d_out) {
+  if (n == 0) return SST_OK;
+  SST_LAUNCH(k_has, blocks_for(n), kTB, 0, g->stream, g->view(), d_pairs, n, d_out);
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+sst_status ensure_leaf_dir(sst_graph *g) {
+  LeafDir &D = g->dir;
+  if (D.version == g->version && D.vleaf) return SST_OK;
+  cudaStream_t s = g->stream;
+  uint32_t n = g->n;
+  if (!D.vleaf) SST_CUDA_TRY(cudaMalloc(&D.vleaf, ((uint64_t)n + 1) * 8));
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes((uint64_t)n + 1, 8) + 4096));
+  uint64_t *total = g->arena.take<uint64_t>(1);
+  if (n) SST_LAUNCH(k_vertex_leaves, blocks_for(n), kTB, 0, s, g->d_cap, n, D.vleaf);
+  SST_CUDA_TRY((scan<uint64_t, OpAdd>(D.vleaf, D.vleaf, n, 0ull, OpAdd{}, true,
+                                      false, total, g->arena, s)));
+  uint64_t nl = 0;
+  SST_CUDA_TRY(cudaMemcpyAsync(&nl, total, 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  SST_CUDA_TRY(cudaMemcpyAsync(D.vleaf + n, &nl, 8, cudaMemcpyHostToDevice, s));
+  if (nl > D.cap) {
+    uint64_t want = nl + nl / 4 + 1024;
+    sst_status st = budget_check(g, (want - D.cap) * 24);
+    if (st != SST_OK) return st;
+    SST_CUDA_TRY(cudaStreamSynchronize(s));
+    cudaFree(D.owner);
+    cudaFree(D.slot);
+    cudaFree(D.cnt);
+    cudaFree(D.pre);
+    D.owner = nullptr;
+    D.slot = nullptr;
+    D.cnt = nullptr;
+    D.pre = nullptr;
+    D.cap = 0;
+    SST_CUDA_TRY(cudaMalloc(&D.owner, want * 4));
+    SST_CUDA_TRY(cudaMalloc(&D.slot, want * 8));
+    SST_CUDA_TRY(cudaMalloc(&D.cnt, want * 4));
+    SST_CUDA_TRY(cudaMalloc(&D.pre, (want + 1) * 8));
+    D.cap = want;
+  }
+  D.nleaves = nl;
+  if (n) SST_LAUNCH(k_dir_fill, warp_blocks(n), kTB, 0, s, g->view(), D.vleaf,
+                    D.owner, D.slot, D.cnt);
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes(nl + 1, 8) + (nl + 1) * 8 + 4096));
+  uint64_t *wide = g->arena.take<uint64_t>(nl + 1);
+  if (nl) SST_LAUNCH(k_widen, blocks_for(nl), kTB, 0, s, D.cnt, nl, wide);
+  SST_CUDA_TRY((scan<uint64_t, OpAdd>(wide, D.pre, nl, 0ull, OpAdd{}, true,
+                                      false, D.pre + nl, g->arena, s)));
+  SST_CUDA_TRY(cudaGetLastError());
+  D.version = g->version;
+  return SST_OK;
+}
+
+sst_status to_csr(sst_graph *g, uint64_t *d_off, uint32_t *d_cols) {
+  sst_status st = ensure_leaf_dir(g);
+  if (st != SST_OK) return st;
+  cudaStream_t s = g->stream;
+  uint32_t n = g->n;
+  LeafDir &D = g->dir;
+  // row offsets: CSR position of each vertex's first leaf
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes((uint64_t)n + 1, 8) + ((uint64_t)n + 1) * 8 + 4096));
+  uint64_t *wide = g->arena.take<uint64_t>((uint64_t)n + 1);
+  if (n) SST_LAUNCH(k_widen, blocks_for(n), kTB, 0, s, g->d_deg, n, wide);
+  SST_CUDA_TRY((scan<uint64_t, OpAdd>(wide, d_off, n, 0ull, OpAdd{}, true, false,
+                                      d_off + n, g->arena, s)));
+  if (D.nleaves)
+    SST_LAUNCH(k_dir_copy, warp_blocks(D.nleaves), kTB, 0, s, g->d_slots, D.slot,
+               D.cnt, D.pre, D.nleaves, d_cols);
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+sst_status neighbors(sst_graph *g, uint32_t v, uint32_t *d_out, uint64_t cap,
+                     uint64_t *deg) {
+  sst_status st = ensure_leaf_dir(g);
+  if (st != SST_OK) return st;
+  cudaStream_t s = g->stream;
+  LeafDir &D = g->dir;
+  uint64_t k[2];
+  SST_CUDA_TRY(cudaMemcpyAsync(k, D.vleaf + v, 16, cudaMemcpyDeviceToHost, s));
+  uint32_t d = 0;
+  SST_CUDA_TRY(cudaMemcpyAsync(&d, g->d_deg + v, 4, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  *deg = d;
+  if (k[1] == k[0] || cap == 0) return SST_OK;
+  uint64_t p0 = 0;
+  SST_CUDA_TRY(cudaMemcpyAsync(&p0, D.pre + k[0], 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  if (cap >= d) {
+    // copy leaves with positions rebased to the vertex's first element
+    SST_LAUNCH(k_dir_copy, warp_blocks(k[1] - k[0]), kTB, 0, s, g->d_slots,
+               D.slot + k[0], D.cnt + k[0], D.pre + k[0], k[1] - k[0],
+               d_out - p0);
+  } else {
+    uint32_t *tmp = nullptr;
+    SST_CUDA_TRY(cudaMallocAsync(&tmp, (uint64_t)d * 4, s));
+    SST_LAUNCH(k_dir_copy, warp_blocks(k[1] - k[0]), kTB, 0, s, g->d_slots,
+               D.slot + k[0], D.cnt + k[0], D.pre + k[0], k[1] - k[0], tmp - p0);
+    SST_CUDA_TRY(cudaMemcpyAsync(d_out, tmp, cap * 4, cudaMemcpyDeviceToDevice, s));
+    cudaFreeAsync(tmp, s);
+  }
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+sst_status sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
+                        uint64_t count, uint32_t *d_pairs) {
+  if (count == 0) return SST_OK;
+  sst_status st = ensure_leaf_dir(g);
+  if (st != SST_OK) return st;
+  LeafDir &D = g->dir;
+  SST_LAUNCH(k_sample, blocks_for(count), kTB, 0, g->stream, g->d_slots, D.owner,
+             D.slot, D.pre, D.nleaves, g->m, seed, first, count, d_pairs);
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+sst_status touch_all_sum(sst_graph *g, uint64_t *out) {
+  sst_status st = ensure_leaf_dir(g);
+  if (st != SST_OK) return st;
+  cudaStream_t s = g->stream;
+  LeafDir &D = g->dir;
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(4096));
+  unsigned long long *acc = g->arena.take<unsigned long long>(1);
+  SST_CUDA_TRY(cudaMemsetAsync(acc, 0, 8, s));
+  if (D.nleaves)
+    SST_LAUNCH(k_sum_leaves, warp_blocks(D.nleaves), kTB, 0, s, g->d_slots,
+               D.slot, D.cnt, D.nleaves, acc);
+  SST_CUDA_TRY(cudaMemcpyAsync(out, acc, 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  return SST_OK;
+}
+
+}  // namespace sst

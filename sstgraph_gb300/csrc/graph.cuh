@@ -22,11 +22,14 @@ struct PlanSummary {
   uint64_t dst_leaves;   // leaves written by those tasks
   uint64_t invalid;      // pairs with an id out of range
   uint32_t class_cnt[kNumClasses];  // new segments per capacity class
+  unsigned long long apply_err;     // staged ranks out of range (must be 0)
 };
 
 // Flattened list of all leaves in vertex order: the iteration space of the
 // copy-out, sampling and traversal kernels.  Rebuilt when the graph version
 // changes.
+struct TravState;
+
 struct LeafDir {
   uint64_t version = ~0ull;
   uint64_t nleaves = 0;
@@ -62,9 +65,11 @@ struct sst_graph {
 
   sst::Arena arena;  // per-operation scratch
   sst::Arena work;   // window / resize staging
+  sst::Arena io;     // device copies of host-pointer arguments
   sst::PlanSummary *h_plan = nullptr;  // pinned
   sst::PlanSummary *d_plan = nullptr;
   sst::LeafDir dir;
+  sst::TravState *trav = nullptr;  // traversal work lists and buffers
   void *h_pinned = nullptr;  // pinned staging for host-pointer calls
   size_t h_pinned_cap = 0;
 
@@ -99,5 +104,6 @@ sst_status repack(sst_graph *g, uint64_t extra_slots);
 
 // host staging buffer (pinned) of at least `bytes`
 void *pinned(sst_graph *g, size_t bytes);
+void trav_release(sst_graph *g);
 
 }  // namespace sst

@@ -1,0 +1,944 @@
+// Traversal kernels over the device PMA (the EdgeMap/VertexMap algorithms the
+// reference drivers call at internal/test.hpp:476-618; the algorithm
+// library itself, EdgeMapVertexMap, is absent from the reference tree).
+//
+// Work decomposition, rebuilt when the graph version changes:
+//  - a vertex whose segment is one leaf (cap <= 32) is handled by one thread
+//    that walks its packed leaf;
+//  - a vertex with a multi-leaf segment is cut into chunks of kChunkLeaves
+//    leaves; one warp walks a chunk leaf by leaf (lane = slot, one 128-byte
+//    line per leaf, only the occupied prefix is read); chunks of one vertex
+//    are combined in chunk order, so sums are deterministic.
+#include <algorithm>
+#include <vector>
+
+#include "traverse.cuh"
+
+namespace sst {
+
+namespace {
+constexpr int kTB = 256;
+constexpr uint32_t kChunkLeaves = 32;
+
+inline unsigned blocks_for(uint64_t n, int per = kTB) {
+  uint64_t b = (n + per - 1) / per;
+  return (unsigned)(b == 0 ? 1 : b);
+}
+inline unsigned warp_blocks(uint64_t nwarps) { return blocks_for(nwarps * 32); }
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+  return v;
+}
+}  // namespace
+
+template <typename T> struct DevBuf {
+  T *p = nullptr;
+  uint64_t cap = 0;
+  cudaError_t ensure(uint64_t n) {
+    if (n <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    uint64_t want = n + n / 8 + 64;
+    cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+struct TravState {
+  uint64_t version = ~0ull;
+  // chunk list of multi-leaf vertices
+  uint64_t nchunks = 0, nmulti = 0, nbig = 0;
+  DevBuf<uint64_t> choff;   // per vertex: first chunk (n+1)
+  DevBuf<uint32_t> cv, cl0; // per chunk: vertex, first leaf
+  DevBuf<uint32_t> multi;   // vertices with more than one chunk
+  DevBuf<uint32_t> big;     // vertices with a multi-leaf segment
+  DevBuf<uint32_t> flag, pos;
+  // pagerank
+  DevBuf<double> inv_deg, ca, cb, partial;
+  // bfs
+  DevBuf<uint32_t> qa, qb, fbits;
+  DevBuf<int32_t> depth_tmp, parent_tmp;
+  // bc
+  DevBuf<double> sigma, ratio;
+  DevBuf<uint32_t> lvl_list, lvl_cnt;
+  // cc
+  DevBuf<uint32_t> par;
+  // tc
+  DevBuf<uint64_t> toff, tlpre, tlcnt;
+  DevBuf<uint32_t> tadj;
+  uint64_t *h_small = nullptr;  // pinned readback slots
+  unsigned long long *d_small = nullptr;
+};
+
+void trav_release(sst_graph *g) {
+  TravState *t = g->trav;
+  if (!t) return;
+  t->choff.release();
+  t->cv.release();
+  t->cl0.release();
+  t->multi.release();
+  t->big.release();
+  t->flag.release();
+  t->pos.release();
+  t->inv_deg.release();
+  t->ca.release();
+  t->cb.release();
+  t->partial.release();
+  t->qa.release();
+  t->qb.release();
+  t->fbits.release();
+  t->depth_tmp.release();
+  t->parent_tmp.release();
+  t->sigma.release();
+  t->ratio.release();
+  t->lvl_list.release();
+  t->lvl_cnt.release();
+  t->par.release();
+  t->toff.release();
+  t->tlpre.release();
+  t->tlcnt.release();
+  t->tadj.release();
+  if (t->h_small) cudaFreeHost(t->h_small);
+  if (t->d_small) cudaFree(t->d_small);
+  delete t;
+  g->trav = nullptr;
+}
+
+namespace {
+
+// ------------------------------------------------------------- work lists
+__global__ void k_chunk_counts(const uint32_t *__restrict__ cap, uint32_t n,
+                               uint64_t *__restrict__ nch,
+                               uint32_t *__restrict__ bigf,
+                               uint32_t *__restrict__ multif) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  uint32_t c = cap[v];
+  uint64_t k = c > kLeaf ? ((c >> kLeafLog) + kChunkLeaves - 1) / kChunkLeaves : 0;
+  nch[v] = k;
+  bigf[v] = c > kLeaf;
+  multif[v] = k > 1;
+}
+
+__global__ void k_chunk_fill(const uint32_t *__restrict__ cap, uint32_t n,
+                             const uint64_t *__restrict__ choff,
+                             uint32_t *__restrict__ cv,
+                             uint32_t *__restrict__ cl0) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  uint64_t c0 = choff[v], c1 = choff[v + 1];
+  for (uint64_t c = c0; c < c1; c++) {
+    cv[c] = v;
+    cl0[c] = (uint32_t)((c - c0) * kChunkLeaves);
+  }
+}
+
+__global__ void k_compact_ids(const uint32_t *__restrict__ flag,
+                              const uint32_t *__restrict__ pos, uint32_t n,
+                              uint32_t *__restrict__ out) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n && flag[v]) out[pos[v]] = v;
+}
+
+// ------------------------------------------------------------- pagerank
+__global__ void k_pr_init(const uint32_t *__restrict__ deg, uint32_t n,
+                          double r0, double *__restrict__ inv_deg,
+                          double *__restrict__ contrib) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  uint32_t d = deg[v];
+  double inv = d ? 1.0 / (double)d : 0.0;
+  inv_deg[v] = inv;
+  contrib[v] = r0 * inv;
+}
+
+// thread per vertex with a one-leaf segment: pull in ascending order
+__global__ void k_pr_small(DGraph g, const double *__restrict__ cin,
+                           double *__restrict__ rank, double *__restrict__ cout,
+                           const double *__restrict__ inv_deg, double base,
+                           double damp) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= g.n) return;
+  uint32_t cap = g.cap[v];
+  if (cap > kLeaf) return;
+  uint32_t d = g.deg[v];
+  const uint32_t *p = g.slots + g.base[v];
+  double s = 0.0;
+  for (uint32_t i = 0; i < d; i++) s += cin[p[i]];
+  double r = base + damp * s;
+  rank[v] = r;
+  cout[v] = r * inv_deg[v];
+}
+
+// warp per chunk of a multi-leaf segment
+__global__ void k_pr_chunks(DGraph g, const uint32_t *__restrict__ cv,
+                            const uint32_t *__restrict__ cl0, uint64_t nchunks,
+                            const double *__restrict__ cin,
+                            double *__restrict__ rank, double *__restrict__ cout,
+                            const double *__restrict__ inv_deg,
+                            double *__restrict__ partial, double base,
+                            double damp) {
+  uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= nchunks) return;
+  uint32_t v = cv[c];
+  uint32_t nl = g.cap[v] >> kLeafLog;
+  uint32_t l0 = cl0[c], l1 = min(l0 + kChunkLeaves, nl);
+  uint64_t sb = g.base[v];
+  const uint8_t *lc = g.lcnt + (sb >> kLeafLog);
+  double acc = 0.0;
+  for (uint32_t l = l0; l < l1; l++) {
+    uint32_t cnt = lc[l];
+    if ((uint32_t)lane < cnt) acc += cin[g.slots[sb + ((uint64_t)l << kLeafLog) + lane]];
+  }
+  double s = warp_sum_d(acc);
+  if (lane == 0) {
+    if (nl <= kChunkLeaves) {
+      double r = base + damp * s;
+      rank[v] = r;
+      cout[v] = r * inv_deg[v];
+    } else {
+      partial[c] = s;
+    }
+  }
+}
+
+__global__ void k_pr_fix(const uint32_t *__restrict__ multi, uint64_t nmulti,
+                         const uint64_t *__restrict__ choff,
+                         const double *__restrict__ partial,
+                         double *__restrict__ rank, double *__restrict__ cout,
+                         const double *__restrict__ inv_deg, double base,
+                         double damp) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nmulti) return;
+  uint32_t v = multi[i];
+  double s = 0.0;
+  for (uint64_t c = choff[v]; c < choff[v + 1]; c++) s += partial[c];
+  double r = base + damp * s;
+  rank[v] = r;
+  cout[v] = r * inv_deg[v];
+}
+
+// ------------------------------------------------------------- bfs
+__global__ void k_bfs_init(int32_t *__restrict__ depth, int32_t *__restrict__ parent,
+                           uint32_t n, uint32_t src) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  depth[v] = v == src ? 0 : -1;
+  parent[v] = v == src ? (int32_t)src : -1;
+}
+
+// warp-aggregated append of `mine` to the next queue
+__device__ __forceinline__ void enqueue(bool mine, uint32_t w, uint32_t wdeg,
+                                        uint32_t *q, unsigned long long *qlen_deg) {
+  const int lane = threadIdx.x & 31;
+  uint32_t m = __ballot_sync(0xffffffffu, mine);
+  if (!m) return;
+  uint32_t dsum = __reduce_add_sync(0xffffffffu, mine ? wdeg : 0u);
+  int leader = __ffs(m) - 1;
+  unsigned long long base = 0;
+  // low 32 bits: queue length, high 32 bits ignored; degree sum separate
+  if (lane == leader) {
+    base = atomicAdd(&qlen_deg[0], (unsigned long long)__popc(m));
+    atomicAdd(&qlen_deg[1], (unsigned long long)dsum);
+  }
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (mine) q[base + __popc(m & ((1u << lane) - 1u))] = w;
+}
+
+// push: warp per frontier vertex, lanes over the slots of each leaf
+__global__ void k_bfs_push(DGraph g, const uint32_t *__restrict__ q, uint32_t qn,
+                           int32_t *__restrict__ depth,
+                           int32_t *__restrict__ parent,
+                           uint32_t *__restrict__ nq,
+                           unsigned long long *__restrict__ cnt, int lvl) {
+  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= qn) return;
+  uint32_t u = q[i];
+  uint64_t base = g.base[u];
+  uint32_t cap = g.cap[u], deg = g.deg[u];
+  uint32_t nl = cap ? nleaves_of(cap) : 0;
+  for (uint32_t l = 0; l < nl; l++) {
+    uint32_t c = leaf_count(g, base, cap, deg, l);
+    bool mine = false;
+    uint32_t w = 0, wd = 0;
+    if ((uint32_t)lane < c) {
+      w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
+      if (depth[w] < 0 && atomicCAS(&depth[w], -1, lvl + 1) == -1) {
+        parent[w] = (int32_t)u;
+        mine = true;
+        wd = g.deg[w];
+      }
+    }
+    enqueue(mine, w, wd, nq, cnt);
+  }
+}
+
+__global__ void k_q2bits(const uint32_t *__restrict__ q, uint32_t qn,
+                         uint32_t *__restrict__ bits) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= qn) return;
+  uint32_t u = q[i];
+  atomicOr(&bits[u >> 5], 1u << (u & 31));
+}
+
+__device__ __forceinline__ bool in_front(const uint32_t *bits, uint32_t u) {
+  return (bits[u >> 5] >> (u & 31)) & 1u;
+}
+
+// pull, one-leaf vertices: thread per vertex, first frontier neighbour wins
+__global__ void k_bfs_pull_small(DGraph g, const uint32_t *__restrict__ fbits,
+                                 int32_t *__restrict__ depth,
+                                 int32_t *__restrict__ parent,
+                                 uint32_t *__restrict__ nq,
+                                 unsigned long long *__restrict__ cnt, int lvl) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  bool mine = false;
+  uint32_t d = 0;
+  if (v < g.n && depth[v] < 0 && g.cap[v] <= kLeaf) {
+    d = g.deg[v];
+    const uint32_t *p = g.slots + g.base[v];
+    for (uint32_t i = 0; i < d; i++) {
+      uint32_t u = p[i];
+      if (in_front(fbits, u)) {
+        depth[v] = lvl + 1;
+        parent[v] = (int32_t)u;
+        mine = true;
+        break;
+      }
+    }
+  }
+  enqueue(mine, v, d, nq, cnt);
+}
+
+// pull, multi-leaf vertices: warp per vertex, leaf by leaf, early exit
+__global__ void k_bfs_pull_big(DGraph g, const uint32_t *__restrict__ big,
+                               uint64_t nbig, const uint32_t *__restrict__ fbits,
+                               int32_t *__restrict__ depth,
+                               int32_t *__restrict__ parent,
+                               uint32_t *__restrict__ nq,
+                               unsigned long long *__restrict__ cnt, int lvl) {
+  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= nbig) return;
+  uint32_t v = big[i];
+  if (depth[v] >= 0) return;
+  uint64_t base = g.base[v];
+  uint32_t nl = g.cap[v] >> kLeafLog;
+  const uint8_t *lc = g.lcnt + (base >> kLeafLog);
+  bool found = false;
+  for (uint32_t l = 0; l < nl && !found; l++) {
+    uint32_t c = lc[l];
+    uint32_t u = (uint32_t)lane < c ? g.slots[base + ((uint64_t)l << kLeafLog) + lane] : 0;
+    uint32_t m = __ballot_sync(0xffffffffu, (uint32_t)lane < c && in_front(fbits, u));
+    if (m) {
+      int first = __ffs(m) - 1;
+      uint32_t pu = __shfl_sync(0xffffffffu, u, first);
+      if (lane == 0) {
+        depth[v] = lvl + 1;
+        parent[v] = (int32_t)pu;
+      }
+      found = true;
+    }
+  }
+  enqueue(found && lane == 0, v, g.deg[v], nq, cnt);
+}
+
+// ------------------------------------------------------------- cc
+__device__ __forceinline__ uint32_t cc_root(const uint32_t *par, uint32_t x) {
+  uint32_t p;
+  while ((p = __ldcg(par + x)) != x) x = p;
+  return x;
+}
+
+__global__ void k_iota(uint32_t *__restrict__ p, uint32_t n) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n) p[v] = v;
+}
+
+// warp per leaf: hook the two roots of every edge (w < u) smaller-to-larger
+__global__ void k_cc_hook(const uint32_t *__restrict__ slots,
+                          const uint32_t *__restrict__ owner,
+                          const uint64_t *__restrict__ slot,
+                          const uint32_t *__restrict__ cnt, uint64_t nleaves,
+                          uint32_t *__restrict__ par,
+                          unsigned long long *__restrict__ changed) {
+  uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (k >= nleaves) return;
+  uint32_t u = owner[k];
+  bool ch = false;
+  if ((uint32_t)lane < cnt[k]) {
+    uint32_t w = slots[slot[k] + lane];
+    if (w < u) {
+      uint32_t ru = cc_root(par, u), rw = cc_root(par, w);
+      if (ru != rw) {
+        uint32_t hi = max(ru, rw), lo = min(ru, rw);
+        atomicMin(&par[hi], lo);
+        ch = true;
+      }
+    }
+  }
+  if (__any_sync(0xffffffffu, ch) && lane == 0) atomicAdd(changed, 1ull);
+}
+
+__global__ void k_cc_compress(uint32_t *__restrict__ par, uint32_t n) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  par[v] = cc_root(par, v);
+}
+
+// ------------------------------------------------------------- bc
+__global__ void k_max_depth(const int32_t *__restrict__ depth, uint32_t n,
+                            unsigned long long *__restrict__ out) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  int32_t d = v < n ? depth[v] : -1;
+  for (int o = 16; o > 0; o >>= 1) d = max(d, __shfl_down_sync(0xffffffffu, d, o));
+  if ((threadIdx.x & 31) == 0 && d >= 0) atomicMax(out, (unsigned long long)d);
+}
+
+__global__ void k_level_count(const int32_t *__restrict__ depth, uint32_t n,
+                              uint32_t *__restrict__ cnt) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n && depth[v] >= 0) atomicAdd(&cnt[depth[v]], 1u);
+}
+
+__global__ void k_level_scatter(const int32_t *__restrict__ depth, uint32_t n,
+                                const uint32_t *__restrict__ off,
+                                uint32_t *__restrict__ ctr,
+                                uint32_t *__restrict__ list) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n || depth[v] < 0) return;
+  int32_t d = depth[v];
+  list[off[d] + atomicAdd(&ctr[d], 1u)] = v;
+}
+
+__global__ void k_bc_init(double *__restrict__ sigma, double *__restrict__ ratio,
+                          double *__restrict__ dep, uint32_t n, uint32_t src) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  sigma[v] = v == src ? 1.0 : 0.0;
+  ratio[v] = 0.0;
+  dep[v] = 0.0;
+}
+
+// sigma(v) = sum of sigma over neighbours one level up (thread per vertex)
+__global__ void k_sigma_small(DGraph g, const uint32_t *__restrict__ list,
+                              uint32_t cnt, const int32_t *__restrict__ depth,
+                              double *__restrict__ sigma, int32_t d) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  uint32_t v = list[i];
+  if (g.cap[v] > kLeaf) return;
+  const uint32_t *p = g.slots + g.base[v];
+  uint32_t dg = g.deg[v];
+  double s = 0.0;
+  for (uint32_t k = 0; k < dg; k++) {
+    uint32_t u = p[k];
+    if (depth[u] == d - 1) s += sigma[u];
+  }
+  sigma[v] = s;
+}
+
+__global__ void k_sigma_big(DGraph g, const uint32_t *__restrict__ list,
+                            uint32_t cnt, const int32_t *__restrict__ depth,
+                            double *__restrict__ sigma, int32_t d) {
+  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= cnt) return;
+  uint32_t v = list[i];
+  uint32_t cap = g.cap[v];
+  if (cap <= kLeaf) return;
+  uint64_t base = g.base[v];
+  const uint8_t *lc = g.lcnt + (base >> kLeafLog);
+  double acc = 0.0;
+  for (uint32_t l = 0; l < (cap >> kLeafLog); l++) {
+    if ((uint32_t)lane < lc[l]) {
+      uint32_t u = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
+      if (depth[u] == d - 1) acc += sigma[u];
+    }
+  }
+  double s = warp_sum_d(acc);
+  if (lane == 0) sigma[v] = s;
+}
+
+// dep(v) = sigma(v) * sum over neighbours one level down of (1+dep(w))/sigma(w)
+__global__ void k_delta_small(DGraph g, const uint32_t *__restrict__ list,
+                              uint32_t cnt, const int32_t *__restrict__ depth,
+                              const double *__restrict__ sigma,
+                              double *__restrict__ ratio,
+                              double *__restrict__ dep, int32_t d) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  uint32_t v = list[i];
+  if (g.cap[v] > kLeaf) return;
+  const uint32_t *p = g.slots + g.base[v];
+  uint32_t dg = g.deg[v];
+  double s = 0.0;
+  for (uint32_t k = 0; k < dg; k++) {
+    uint32_t w = p[k];
+    if (depth[w] == d + 1) s += ratio[w];
+  }
+  double dv = sigma[v] * s;
+  dep[v] = dv;
+  ratio[v] = (1.0 + dv) / sigma[v];
+}
+
+__global__ void k_delta_big(DGraph g, const uint32_t *__restrict__ list,
+                            uint32_t cnt, const int32_t *__restrict__ depth,
+                            const double *__restrict__ sigma,
+                            double *__restrict__ ratio, double *__restrict__ dep,
+                            int32_t d) {
+  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= cnt) return;
+  uint32_t v = list[i];
+  uint32_t cap = g.cap[v];
+  if (cap <= kLeaf) return;
+  uint64_t base = g.base[v];
+  const uint8_t *lc = g.lcnt + (base >> kLeafLog);
+  double acc = 0.0;
+  for (uint32_t l = 0; l < (cap >> kLeafLog); l++) {
+    if ((uint32_t)lane < lc[l]) {
+      uint32_t w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
+      if (depth[w] == d + 1) acc += ratio[w];
+    }
+  }
+  double s = warp_sum_d(acc);
+  if (lane == 0) {
+    double dv = sigma[v] * s;
+    dep[v] = dv;
+    ratio[v] = (1.0 + dv) / sigma[v];
+  }
+}
+
+// ------------------------------------------------------------- tc
+// rank order used to orient each undirected edge once: (degree, id)
+__device__ __forceinline__ bool rank_less(const uint32_t *deg, uint32_t a,
+                                          uint32_t b) {
+  uint32_t da = deg[a], db = deg[b];
+  return da < db || (da == db && a < b);
+}
+
+__global__ void k_tc_leafcount(const uint32_t *__restrict__ slots,
+                               const uint32_t *__restrict__ owner,
+                               const uint64_t *__restrict__ slot,
+                               const uint32_t *__restrict__ cnt,
+                               uint64_t nleaves, const uint32_t *__restrict__ deg,
+                               uint64_t *__restrict__ out) {
+  uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (k >= nleaves) return;
+  uint32_t u = owner[k];
+  bool keep = false;
+  if ((uint32_t)lane < cnt[k]) keep = rank_less(deg, slots[slot[k] + lane], u);
+  uint32_t m = __ballot_sync(0xffffffffu, keep);
+  if (lane == 0) out[k] = __popc(m);
+}
+
+__global__ void k_tc_fill(const uint32_t *__restrict__ slots,
+                          const uint32_t *__restrict__ owner,
+                          const uint64_t *__restrict__ slot,
+                          const uint32_t *__restrict__ cnt, uint64_t nleaves,
+                          const uint32_t *__restrict__ deg,
+                          const uint64_t *__restrict__ lpre,
+                          uint32_t *__restrict__ adj) {
+  uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (k >= nleaves) return;
+  uint32_t u = owner[k];
+  uint32_t w = 0;
+  bool keep = false;
+  if ((uint32_t)lane < cnt[k]) {
+    w = slots[slot[k] + lane];
+    keep = rank_less(deg, w, u);
+  }
+  uint32_t m = __ballot_sync(0xffffffffu, keep);
+  if (keep) adj[lpre[k] + __popc(m & ((1u << lane) - 1u))] = w;
+}
+
+__global__ void k_tc_off(const uint64_t *__restrict__ vleaf,
+                         const uint64_t *__restrict__ lpre, uint32_t n,
+                         uint64_t *__restrict__ off) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v <= n) off[v] = lpre[vleaf[v]];
+}
+
+__device__ __forceinline__ bool sorted_has(const uint32_t *a, uint64_t n,
+                                           uint32_t x) {
+  uint64_t lo = 0, hi = n;
+  while (lo < hi) {
+    uint64_t mid = (lo + hi) >> 1;
+    if (a[mid] < x)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo < n && a[lo] == x;
+}
+
+// warp per vertex u: for v in N+(u) (lane-strided), w in N+(v): w in N+(u)?
+__global__ void k_tc_count(const uint64_t *__restrict__ off,
+                           const uint32_t *__restrict__ adj, uint32_t n,
+                           unsigned long long *__restrict__ total,
+                           unsigned long long *__restrict__ pv) {
+  uint64_t u = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (u >= n) return;
+  uint64_t a0 = off[u], a1 = off[u + 1];
+  const uint32_t *A = adj + a0;
+  uint64_t na = a1 - a0;
+  unsigned long long local = 0;
+  for (uint64_t i = lane; i < na; i += 32) {
+    uint32_t v = A[i];
+    uint64_t b0 = off[v], b1 = off[v + 1];
+    unsigned long long cv = 0;
+    for (uint64_t j = b0; j < b1; j++) {
+      uint32_t w = adj[j];
+      if (sorted_has(A, na, w)) {
+        cv++;
+        if (pv) atomicAdd(&pv[w], 1ull);
+      }
+    }
+    if (pv && cv) atomicAdd(&pv[v], cv);
+    local += cv;
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) local += __shfl_down_sync(0xffffffffu, local, d);
+  if (lane == 0 && local) {
+    atomicAdd(total, local);
+    if (pv) atomicAdd(&pv[u], local);
+  }
+}
+
+// ------------------------------------------------------------- pairs
+__device__ __forceinline__ bool pma_has(const DGraph &g, uint32_t u, uint32_t x) {
+  uint32_t cap = g.cap[u];
+  if (!cap) return false;
+  uint64_t base = g.base[u];
+  uint32_t l = find_leaf(g.slots, base, cap, x);
+  uint32_t c = leaf_count(g, base, cap, g.deg[u], l);
+  const uint32_t *p = g.slots + base + ((uint64_t)l << kLeafLog);
+  uint32_t pos = leaf_lower_bound(p, c, x);
+  return pos < c && p[pos] == x;
+}
+
+// thread per pair: walk the smaller set in order, probe the other
+__global__ void k_common(DGraph g, const uint32_t *__restrict__ pairs, uint64_t n,
+                         bool early, uint64_t *__restrict__ out) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t a = pairs[2 * i], b = pairs[2 * i + 1];
+  if (a >= g.n || b >= g.n) {
+    out[i] = 0;
+    return;
+  }
+  uint32_t lim = early ? min(a, b) : 0xFFFFFFFFu;
+  uint32_t s = g.deg[a] <= g.deg[b] ? a : b, o = s == a ? b : a;
+  uint64_t base = g.base[s];
+  uint32_t cap = g.cap[s], deg = g.deg[s];
+  uint32_t nl = cap ? nleaves_of(cap) : 0;
+  uint64_t c = 0;
+  for (uint32_t l = 0; l < nl; l++) {
+    uint32_t k = leaf_count(g, base, cap, deg, l);
+    const uint32_t *p = g.slots + base + ((uint64_t)l << kLeafLog);
+    for (uint32_t j = 0; j < k; j++) {
+      uint32_t x = p[j];
+      if (x >= lim) goto done;
+      c += pma_has(g, o, x);
+    }
+  }
+done:
+  out[i] = c;
+}
+
+}  // namespace
+
+// ================================================================== host
+static TravState *state(sst_graph *g) {
+  if (!g->trav) {
+    g->trav = new TravState();
+    cudaMallocHost(&g->trav->h_small, 64 * sizeof(uint64_t));
+    cudaMalloc(&g->trav->d_small, 64 * sizeof(unsigned long long));
+  }
+  return g->trav;
+}
+
+static sst_status ensure_lists(sst_graph *g) {
+  TravState *t = state(g);
+  if (t->version == g->version) return SST_OK;
+  cudaStream_t s = g->stream;
+  uint32_t n = g->n;
+  SST_CUDA_TRY(t->choff.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->flag.ensure((uint64_t)n * 2 + 2));
+  SST_CUDA_TRY(t->pos.ensure((uint64_t)n * 2 + 2));
+  uint32_t *bigf = t->flag.p, *multif = t->flag.p + n + 1;
+  uint32_t *bigp = t->pos.p, *multip = t->pos.p + n + 1;
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(3 * scan_scratch_bytes((uint64_t)n + 1, 8) + 4096));
+  uint64_t *tot = g->arena.take<uint64_t>(1);
+  uint32_t *tot32 = g->arena.take<uint32_t>(2);
+  if (n) SST_LAUNCH(k_chunk_counts, blocks_for(n), kTB, 0, s, g->d_cap, n,
+                    t->choff.p, bigf, multif);
+  SST_CUDA_TRY((scan<uint64_t, OpAdd>(t->choff.p, t->choff.p, n, 0ull, OpAdd{},
+                                      true, false, tot, g->arena, s)));
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(bigf, bigp, n, 0u, OpAdd{}, true, false,
+                                      tot32, g->arena, s)));
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(multif, multip, n, 0u, OpAdd{}, true,
+                                      false, tot32 + 1, g->arena, s)));
+  uint64_t h[2];
+  uint32_t h32[2];
+  SST_CUDA_TRY(cudaMemcpyAsync(h, tot, 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaMemcpyAsync(h32, tot32, 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  t->nchunks = h[0];
+  t->nbig = h32[0];
+  t->nmulti = h32[1];
+  SST_CUDA_TRY(cudaMemcpyAsync(t->choff.p + n, &t->nchunks, 8, cudaMemcpyHostToDevice, s));
+  SST_CUDA_TRY(t->cv.ensure(t->nchunks + 1));
+  SST_CUDA_TRY(t->cl0.ensure(t->nchunks + 1));
+  SST_CUDA_TRY(t->big.ensure(t->nbig + 1));
+  SST_CUDA_TRY(t->multi.ensure(t->nmulti + 1));
+  if (n) {
+    SST_LAUNCH(k_chunk_fill, blocks_for(n), kTB, 0, s, g->d_cap, n, t->choff.p,
+               t->cv.p, t->cl0.p);
+    SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, bigf, bigp, n, t->big.p);
+    SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, multif, multip, n, t->multi.p);
+  }
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  SST_CUDA_TRY(cudaGetLastError());
+  t->version = g->version;
+  return SST_OK;
+}
+
+sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank) {
+  sst_status st = ensure_lists(g);
+  if (st != SST_OK) return st;
+  TravState *t = g->trav;
+  cudaStream_t s = g->stream;
+  uint32_t n = g->n;
+  if (n == 0) return SST_OK;
+  SST_CUDA_TRY(t->inv_deg.ensure(n));
+  SST_CUDA_TRY(t->ca.ensure(n));
+  SST_CUDA_TRY(t->cb.ensure(n));
+  SST_CUDA_TRY(t->partial.ensure(t->nchunks + 1));
+  double r0 = 1.0 / (double)n;
+  double base = (1.0 - damping) / (double)n;
+  SST_LAUNCH(k_pr_init, blocks_for(n), kTB, 0, s, g->d_deg, n, r0, t->inv_deg.p, t->ca.p);
+  if (iters == 0) {
+    // rank stays 1/n
+    std::vector<double> h(n, r0);
+    SST_CUDA_TRY(cudaMemcpyAsync(d_rank, h.data(), (uint64_t)n * 8, cudaMemcpyHostToDevice, s));
+    SST_CUDA_TRY(cudaStreamSynchronize(s));
+    return SST_OK;
+  }
+  DGraph dg = g->view();
+  double *cin = t->ca.p, *cout = t->cb.p;
+  for (uint32_t it = 0; it < iters; it++) {
+    SST_LAUNCH(k_pr_small, blocks_for(n), kTB, 0, s, dg, cin, d_rank, cout,
+               t->inv_deg.p, base, damping);
+    if (t->nchunks)
+      SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cv.p,
+                 t->cl0.p, t->nchunks, cin, d_rank, cout, t->inv_deg.p,
+                 t->partial.p, base, damping);
+    if (t->nmulti)
+      SST_LAUNCH(k_pr_fix, blocks_for(t->nmulti), kTB, 0, s, t->multi.p,
+                 t->nmulti, t->choff.p, t->partial.p, d_rank, cout, t->inv_deg.p,
+                 base, damping);
+    std::swap(cin, cout);
+  }
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths) {
+  sst_status st = ensure_lists(g);
+  if (st != SST_OK) return st;
+  TravState *t = g->trav;
+  cudaStream_t s = g->stream;
+  uint32_t n = g->n;
+  SST_CUDA_TRY(t->qa.ensure(n + 1));
+  SST_CUDA_TRY(t->qb.ensure(n + 1));
+  SST_CUDA_TRY(t->fbits.ensure(n / 32 + 2));
+  int32_t *depth = d_depths, *parent = d_parents;
+  if (!depth) {
+    SST_CUDA_TRY(t->depth_tmp.ensure(n));
+    depth = t->depth_tmp.p;
+  }
+  if (!parent) {
+    SST_CUDA_TRY(t->parent_tmp.ensure(n));
+    parent = t->parent_tmp.p;
+  }
+  DGraph dg = g->view();
+  SST_LAUNCH(k_bfs_init, blocks_for(n), kTB, 0, s, depth, parent, n, src);
+  SST_CUDA_TRY(cudaMemcpyAsync(t->qa.p, &src, 4, cudaMemcpyHostToDevice, s));
+  uint32_t sdeg = 0;
+  SST_CUDA_TRY(cudaMemcpyAsync(&sdeg, g->d_deg + src, 4, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t qn = 1, qdeg = sdeg;
+  uint32_t *q = t->qa.p, *nq = t->qb.p;
+  unsigned long long *cnt = t->d_small;
+  const uint64_t m = g->m;
+  for (int lvl = 0; qn > 0; lvl++) {
+    if ((uint64_t)lvl > n) {
+      set_error_message("BFS exceeded n levels");
+      return SST_ETIMEDOUT;
+    }
+    SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, 16, s));
+    if ((qn + qdeg) * 20 > m) {
+      SST_CUDA_TRY(cudaMemsetAsync(t->fbits.p, 0, ((uint64_t)n / 32 + 1) * 4, s));
+      SST_LAUNCH(k_q2bits, blocks_for(qn), kTB, 0, s, q, (uint32_t)qn, t->fbits.p);
+      SST_LAUNCH(k_bfs_pull_small, blocks_for(n), kTB, 0, s, dg, t->fbits.p,
+                 depth, parent, nq, cnt, lvl);
+      if (t->nbig)
+        SST_LAUNCH(k_bfs_pull_big, warp_blocks(t->nbig), kTB, 0, s, dg, t->big.p,
+                   t->nbig, t->fbits.p, depth, parent, nq, cnt, lvl);
+    } else {
+      SST_LAUNCH(k_bfs_push, warp_blocks(qn), kTB, 0, s, dg, q, (uint32_t)qn,
+                 depth, parent, nq, cnt, lvl);
+    }
+    SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, cnt, 16, cudaMemcpyDeviceToHost, s));
+    SST_CUDA_TRY(cudaStreamSynchronize(s));
+    qn = t->h_small[0];
+    qdeg = t->h_small[1];
+    std::swap(q, nq);
+  }
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+sst_status cc(sst_graph *g, uint32_t *d_labels) {
+  sst_status st = ensure_leaf_dir(g);
+  if (st != SST_OK) return st;
+  TravState *t = state(g);
+  cudaStream_t s = g->stream;
+  uint32_t n = g->n;
+  if (n == 0) return SST_OK;
+  LeafDir &D = g->dir;
+  uint32_t *par = d_labels;
+  SST_LAUNCH(k_iota, blocks_for(n), kTB, 0, s, par, n);
+  for (int round = 0; round < 1000; round++) {
+    SST_CUDA_TRY(cudaMemsetAsync(t->d_small, 0, 8, s));
+    if (D.nleaves)
+      SST_LAUNCH(k_cc_hook, warp_blocks(D.nleaves), kTB, 0, s, g->d_slots,
+                 D.owner, D.slot, D.cnt, D.nleaves, par, t->d_small);
+    SST_LAUNCH(k_cc_compress, blocks_for(n), kTB, 0, s, par, n);
+    SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, t->d_small, 8, cudaMemcpyDeviceToHost, s));
+    SST_CUDA_TRY(cudaStreamSynchronize(s));
+    if (t->h_small[0] == 0) return SST_OK;
+  }
+  set_error_message("connected components did not converge");
+  return SST_ETIMEDOUT;
+}
+
+sst_status bc(sst_graph *g, uint32_t src, double *d_dep) {
+  TravState *t = state(g);
+  uint32_t n = g->n;
+  SST_CUDA_TRY(t->depth_tmp.ensure(n));
+  sst_status st = bfs(g, src, nullptr, t->depth_tmp.p);
+  if (st != SST_OK) return st;
+  cudaStream_t s = g->stream;
+  const int32_t *depth = t->depth_tmp.p;
+  SST_CUDA_TRY(cudaMemsetAsync(t->d_small, 0, 8, s));
+  SST_LAUNCH(k_max_depth, blocks_for(n), kTB, 0, s, depth, n, t->d_small);
+  SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, t->d_small, 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint32_t D = (uint32_t)t->h_small[0];
+  SST_CUDA_TRY(t->lvl_cnt.ensure(3 * ((uint64_t)D + 2)));
+  SST_CUDA_TRY(t->lvl_list.ensure(n + 1));
+  SST_CUDA_TRY(t->sigma.ensure(n));
+  SST_CUDA_TRY(t->ratio.ensure(n));
+  uint32_t *cnt = t->lvl_cnt.p, *off = cnt + D + 2, *ctr = off + D + 2;
+  SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, 3 * ((uint64_t)D + 2) * 4, s));
+  SST_LAUNCH(k_level_count, blocks_for(n), kTB, 0, s, depth, n, cnt);
+  std::vector<uint32_t> hc(D + 2), ho(D + 2);
+  SST_CUDA_TRY(cudaMemcpyAsync(hc.data(), cnt, (D + 1) * 4, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint32_t acc = 0;
+  for (uint32_t d = 0; d <= D; d++) {
+    ho[d] = acc;
+    acc += hc[d];
+  }
+  ho[D + 1] = acc;
+  SST_CUDA_TRY(cudaMemcpyAsync(off, ho.data(), (D + 2) * 4, cudaMemcpyHostToDevice, s));
+  SST_LAUNCH(k_level_scatter, blocks_for(n), kTB, 0, s, depth, n, off, ctr,
+             t->lvl_list.p);
+  SST_LAUNCH(k_bc_init, blocks_for(n), kTB, 0, s, t->sigma.p, t->ratio.p, d_dep, n, src);
+  DGraph dg = g->view();
+  for (uint32_t d = 1; d <= D; d++) {
+    uint32_t c = hc[d];
+    const uint32_t *lst = t->lvl_list.p + ho[d];
+    SST_LAUNCH(k_sigma_small, blocks_for(c), kTB, 0, s, dg, lst, c, depth, t->sigma.p, (int32_t)d);
+    SST_LAUNCH(k_sigma_big, warp_blocks(c), kTB, 0, s, dg, lst, c, depth, t->sigma.p, (int32_t)d);
+  }
+  for (int32_t d = (int32_t)D; d >= 0; d--) {
+    uint32_t c = hc[d];
+    const uint32_t *lst = t->lvl_list.p + ho[d];
+    SST_LAUNCH(k_delta_small, blocks_for(c), kTB, 0, s, dg, lst, c, depth,
+               t->sigma.p, t->ratio.p, d_dep, d);
+    SST_LAUNCH(k_delta_big, warp_blocks(c), kTB, 0, s, dg, lst, c, depth,
+               t->sigma.p, t->ratio.p, d_dep, d);
+  }
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+sst_status tc(sst_graph *g, uint64_t *total, uint64_t *d_pv) {
+  sst_status st = ensure_leaf_dir(g);
+  if (st != SST_OK) return st;
+  TravState *t = state(g);
+  cudaStream_t s = g->stream;
+  uint32_t n = g->n;
+  LeafDir &D = g->dir;
+  uint64_t nl = D.nleaves;
+  SST_CUDA_TRY(t->tlcnt.ensure(nl + 1));
+  SST_CUDA_TRY(t->tlpre.ensure(nl + 1));
+  SST_CUDA_TRY(t->toff.ensure((uint64_t)n + 1));
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes(nl + 1, 8) + 4096));
+  if (nl)
+    SST_LAUNCH(k_tc_leafcount, warp_blocks(nl), kTB, 0, s, g->d_slots, D.owner,
+               D.slot, D.cnt, nl, g->d_deg, t->tlcnt.p);
+  SST_CUDA_TRY((scan<uint64_t, OpAdd>(t->tlcnt.p, t->tlpre.p, nl, 0ull, OpAdd{},
+                                      true, false, t->tlpre.p + nl, g->arena, s)));
+  uint64_t madj = 0;
+  SST_CUDA_TRY(cudaMemcpyAsync(&madj, t->tlpre.p + nl, 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  SST_CUDA_TRY(t->tadj.ensure(madj + 1));
+  if (nl)
+    SST_LAUNCH(k_tc_fill, warp_blocks(nl), kTB, 0, s, g->d_slots, D.owner, D.slot,
+               D.cnt, nl, g->d_deg, t->tlpre.p, t->tadj.p);
+  SST_LAUNCH(k_tc_off, blocks_for((uint64_t)n + 1), kTB, 0, s, D.vleaf,
+             t->tlpre.p, n, t->toff.p);
+  SST_CUDA_TRY(cudaMemsetAsync(t->d_small, 0, 8, s));
+  if (d_pv) SST_CUDA_TRY(cudaMemsetAsync(d_pv, 0, (uint64_t)n * 8, s));
+  if (n)
+    SST_LAUNCH(k_tc_count, warp_blocks(n), kTB, 0, s, t->toff.p, t->tadj.p, n,
+               t->d_small, reinterpret_cast<unsigned long long *>(d_pv));
+  SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, t->d_small, 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  SST_CUDA_TRY(cudaGetLastError());
+  *total = t->h_small[0];
+  return SST_OK;
+}
+
+sst_status common_neighbors_batch(sst_graph *g, const uint32_t *d_pairs,
+                                  uint64_t n, bool early_end, uint64_t *d_out) {
+  if (n == 0) return SST_OK;
+  SST_LAUNCH(k_common, blocks_for(n), kTB, 0, g->stream, g->view(), d_pairs, n,
+             early_end, d_out);
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+}  // namespace sst

@@ -1,0 +1,20 @@
+// EdgeMap/VertexMap traversal over the device PMA: BFS, PageRank, CC, BC,
+// TC and pairwise common-neighbour counts.  Output pointers are device
+// memory of the graph's GPU.
+#pragma once
+#include "graph.cuh"
+
+namespace sst {
+
+sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents,
+               int32_t *d_depths);
+sst_status pagerank(sst_graph *g, uint32_t iters, double damping,
+                    double *d_rank);
+sst_status cc(sst_graph *g, uint32_t *d_labels);
+sst_status bc(sst_graph *g, uint32_t src, double *d_dep);
+sst_status tc(sst_graph *g, uint64_t *total, uint64_t *d_per_vertex);
+sst_status common_neighbors_batch(sst_graph *g, const uint32_t *d_pairs,
+                                  uint64_t n, bool early_end,
+                                  uint64_t *d_out);
+
+}  // namespace sst

@@ -1,0 +1,79 @@
+"""Device BFS / PageRank / CC / BC / TC vs the CPU oracle.
+Depths, CC labels and triangle counts bit-exact; PR and BC within 1e-9
+relative (L-inf over the vector, normalised by its largest entry)."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-9
+
+
+@pytest.fixture(scope="module")
+def sg():
+    import __graft_entry__ as ge
+    ge.build()
+    import sstgraph_gb300
+    return sstgraph_gb300
+
+
+def graphs():
+    n = 1 << 13
+    yield "rmat13", n, oracle.symmetrize(oracle.rmat(13, 16 * n, seed=1))
+    yield "er", 5000, oracle.symmetrize(oracle.er(5000, 5000 * 4, seed=4))
+    yield "star+isolated", 50, np.array([[0, i] for i in range(1, 30)] + [[i, 0] for i in range(1, 30)], np.uint32)
+
+
+@pytest.fixture(scope="module", params=[x[0] for x in graphs()])
+def pair(request, sg):
+    name, n, edges = next(x for x in graphs() if x[0] == request.param)
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    g.insert_batch(edges)
+    o.insert_batch(edges)
+    return g, o
+
+
+def relerr(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def test_bfs(sg, pair):
+    g, o = pair
+    for src in (0, 1, g.rows - 1):
+        par, dep = sg.BFS_both(g, src)
+        exp = o.bfs(src)
+        assert np.array_equal(dep, exp)
+        # parents: a neighbour one level up
+        assert par[src] == src
+        for v in np.nonzero(exp > 0)[0][:2000]:
+            p = par[v]
+            assert exp[p] == exp[v] - 1 and o.has(int(v), int(p))
+        assert np.all(par[exp < 0] == -1)
+
+
+def test_pagerank(sg, pair):
+    g, o = pair
+    for iters in (1, 10, 20):
+        assert relerr(sg.PR_S(g, iters), o.pagerank(iters)) <= REL
+
+
+def test_cc(sg, pair):
+    g, o = pair
+    assert np.array_equal(sg.CC(g), o.cc())
+
+
+def test_bc(sg, pair):
+    g, o = pair
+    for src in (0, 3):
+        assert relerr(sg.BC(g, src), o.bc(src)) <= REL
+
+
+def test_tc(sg, pair):
+    g, o = pair
+    t, pv = sg.TC(g, per_vertex=True)
+    te, pve = o.tc(per_vertex=True)
+    assert t == te
+    assert np.array_equal(pv, pve)

@@ -1,0 +1,139 @@
+"""Device batch updates vs the CPU oracle: neighbour sets bit-exact after
+every batch (reference semantics: SparseMatrix.hpp:556-718)."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sg():
+    import __graft_entry__ as ge
+    ge.build()
+    import sstgraph_gb300
+    return sstgraph_gb300
+
+
+def same(g, o):
+    og, cg = g.csr()
+    oo, co = o.csr()
+    assert g.M() == o.M()
+    assert np.array_equal(og, oo)
+    assert np.array_equal(cg, co)
+    assert np.array_equal(g.degrees(), o.degrees())
+
+
+def test_empty_and_tiny(sg):
+    g = sg.SparseMatrixV(10)
+    o = oracle.OracleGraph(10)
+    g.insert_batch(np.zeros((0, 2), np.uint32))
+    same(g, o)
+    for e in ([[1, 2]], [[1, 2], [1, 2], [2, 2], [3, 1]], [[9, 0], [0, 9]]):
+        g.insert_batch(e)
+        o.insert_batch(e)
+        same(g, o)
+    g.remove_batch([[1, 2], [5, 5], [3, 1], [3, 1]])
+    o.remove_batch([[1, 2], [5, 5], [3, 1], [3, 1]])
+    same(g, o)
+    assert g.has(9, 0) and not g.has(1, 2)
+
+
+def test_invalid_ids_skipped(sg):
+    g = sg.SparseMatrixV(8)
+    bad = g.insert_batch([[1, 2], [8, 1], [1, 100], [3, 4]])
+    assert bad == 2
+    assert g.M() == 2
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_random_batches(sg, seed):
+    rng = np.random.default_rng(seed)
+    n = 3000
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    for it in range(12):
+        b = int(rng.integers(1, 30000))
+        e = rng.integers(0, n, size=(b, 2)).astype(np.uint32)
+        e[: b // 2, 0] %= 7  # hubs
+        if it % 3 == 2:
+            rem = np.concatenate([e[: b // 2], o.sample_edges(b // 2 + 1, seed=it)])
+            g.remove_batch(rem)
+            o.remove_batch(rem)
+        else:
+            g.insert_batch(e)
+            o.insert_batch(e)
+        same(g, o)
+
+
+def test_rmat_config1_stream(sg):
+    """RMAT scale 16, 16 edges/vertex, symmetrised, then 10 batches of 1e4."""
+    n = 1 << 16
+    base = oracle.symmetrize(oracle.rmat(16, 16 * n, seed=1))
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    g.insert_batch(base)
+    o.insert_batch(base)
+    same(g, o)
+    for i in range(10):
+        b = oracle.rmat(16, 10000, seed=2, first=i * 10000)
+        g.insert_batch(b)
+        o.insert_batch(b)
+        same(g, o)
+
+
+def test_grow_and_shrink_hub(sg):
+    n = 1 << 15
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    cols = np.arange(1, n, dtype=np.uint32)
+    e = np.stack([np.zeros_like(cols), cols], 1)
+    for part in np.array_split(e, 7):
+        g.insert_batch(part)
+        o.insert_batch(part)
+        same(g, o)
+    for part in np.array_split(e[::-1].copy(), 5):
+        g.remove_batch(part)
+        o.remove_batch(part)
+        same(g, o)
+    assert g.M() == 0
+
+
+def test_has_batch(sg):
+    n = 1 << 12
+    base = oracle.symmetrize(oracle.rmat(12, 8 * n, seed=5))
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    g.insert_batch(base)
+    o.insert_batch(base)
+    q = np.concatenate([base[:5000], oracle.rmat(12, 5000, seed=9)])
+    got = g.has_batch(q)
+    exp = np.array([o.has(int(a), int(b)) for a, b in q], np.uint8)
+    assert np.array_equal(got, exp)
+    assert g.has(int(base[0, 0]), int(base[0, 1]))
+
+
+def test_neighbors_and_sample(sg):
+    n = 1 << 12
+    base = oracle.symmetrize(oracle.rmat(12, 8 * n, seed=6))
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    g.insert_batch(base)
+    o.insert_batch(base)
+    off, cols = o.csr()
+    for v in [0, 1, 2, 17, n - 1]:
+        assert np.array_equal(g.neighbors(v), cols[off[v]:off[v + 1]])
+    assert np.array_equal(g.sample_edges(1000, seed=11), o.sample_edges(1000, seed=11))
+    assert g.touch_all_sum() == o.touch_all_sum()
+    pairs = oracle.rmat(12, 500, seed=12)
+    for early in (False, True):
+        got = g.common_neighbors_batch(pairs, early)
+        exp = [o.common_neighbors(int(a), int(b), early) for a, b in pairs]
+        assert list(got) == exp
+
+
+def test_generators_match_oracle(sg):
+    assert np.array_equal(sg.gen_rmat(14, 50000, seed=3, first=77), oracle.rmat(14, 50000, seed=3, first=77))
+    assert np.array_equal(sg.gen_er(1000003, 50000, seed=4), oracle.er(1000003, 50000, seed=4))
+    assert np.array_equal(sg.gen_ref_rmat(1 << 15, 50000), oracle.ref_rmat_stream(1 << 15, 50000))
