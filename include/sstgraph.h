@@ -172,6 +172,13 @@ SST_API sst_status sst_gen_ref_rmat(uint32_t nn, double a, double b, double c,
                             uint32_t flags);
 
 /* ---- instrumentation -------------------------------------------------- */
+/* raw device layout for structural checks (no reference counterpart):
+ * vertex table (base[rows], cap[rows], deg[rows]) and, when slots / lcnt are
+ * non-NULL, the first *nslots slab slots and their leaf counts
+ * (*nslots / 32 bytes).  *nslots returns the slab's used extent. */
+SST_API sst_status sst_raw_state(sst_graph *g, uint64_t *base, uint32_t *cap,
+                                 uint32_t *deg, uint32_t *slots, uint8_t *lcnt,
+                                 uint64_t *nslots);
 /* number of kernel launches this library issued since load */
 SST_API uint64_t sst_kernel_launches(void);
 

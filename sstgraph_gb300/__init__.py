@@ -85,6 +85,7 @@ SIGNATURES = {
     "sst_gen_er": (_i32, [_u32, _u64, _u64, _u64, _vp, _u32]),
     "sst_gen_ref_rmat": (_i32, [_u32, _dbl, _dbl, _dbl, _u64, _u64, _vp, _u32]),
     "sst_kernel_launches": (_u64, []),
+    "sst_raw_state": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64)]),
 }
 
 _lib = None
@@ -309,6 +310,25 @@ class SparseMatrixV:
         r = ctypes.c_uint64()
         _check(lib().sst_memory_size(self._h, ctypes.byref(r)))
         return r.value
+
+    def raw_state(self):
+        """(base, cap, deg, slots, lcnt): the device layout, for checks."""
+        n = self.rows
+        base = np.empty(max(n, 1), np.uint64)
+        cap = np.empty(max(n, 1), np.uint32)
+        deg = np.empty(max(n, 1), np.uint32)
+        ns = ctypes.c_uint64(0)
+        _check(lib().sst_raw_state(self._h, None, None, None, None, None, ctypes.byref(ns)))
+        used = ns.value
+        slots = np.empty(max(used, 32), np.uint32)
+        lcnt = np.empty(max(used // 32, 1), np.uint8)
+        ns = ctypes.c_uint64(used)
+        _check(lib().sst_raw_state(self._h, ctypes.c_void_p(base.ctypes.data),
+                                   ctypes.c_void_p(cap.ctypes.data),
+                                   ctypes.c_void_p(deg.ctypes.data),
+                                   ctypes.c_void_p(slots.ctypes.data),
+                                   ctypes.c_void_p(lcnt.ctypes.data), ctypes.byref(ns)))
+        return base[:n], cap[:n], deg[:n], slots[:used], lcnt[:used // 32]
 
     def sample_edges(self, count: int, seed: int, first: int = 0, out=None):
         if out is None:

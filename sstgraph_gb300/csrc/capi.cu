@@ -112,6 +112,24 @@ const char *sst_status_string(sst_status s) {
 
 uint64_t sst_kernel_launches(void) { return sst::launches(); }
 
+sst_status sst_raw_state(sst_graph *g, uint64_t *base, uint32_t *cap,
+                         uint32_t *deg, uint32_t *slots, uint8_t *lcnt,
+                         uint64_t *nslots) {
+  CHECK_G(g);
+  if (!nslots) return SST_EINVAL;
+  cudaStream_t s = g->stream;
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t n = g->n;
+  if (base) SST_CUDA_TRY(cudaMemcpy(base, g->d_base, n * 8, cudaMemcpyDeviceToHost));
+  if (cap) SST_CUDA_TRY(cudaMemcpy(cap, g->d_cap, n * 4, cudaMemcpyDeviceToHost));
+  if (deg) SST_CUDA_TRY(cudaMemcpy(deg, g->d_deg, n * 4, cudaMemcpyDeviceToHost));
+  uint64_t used = (g->bump + 31) & ~uint64_t(31);
+  if (slots) SST_CUDA_TRY(cudaMemcpy(slots, g->d_slots, std::min(*nslots, used) * 4, cudaMemcpyDeviceToHost));
+  if (lcnt) SST_CUDA_TRY(cudaMemcpy(lcnt, g->d_lcnt, std::min(*nslots, used) / 32, cudaMemcpyDeviceToHost));
+  *nslots = used;
+  return SST_OK;
+}
+
 sst_status sst_graph_create(uint32_t height, uint32_t width,
                             const sst_config *cfg, sst_graph **out) {
   if (!out) {
