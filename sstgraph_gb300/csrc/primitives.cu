@@ -45,6 +45,7 @@ __device__ __forceinline__ uint32_t rank_iteration(uint32_t d, bool valid,
     }
     run[threadIdx.x] = s;
   }
+  __syncthreads();
   uint32_t pos = valid ? wcnt[warp][d] + __popc(lt) : 0;
   __syncthreads();
   return pos;
