@@ -1,0 +1,442 @@
+"""Benchmark: SSTGraph's dynamic-graph hot path on one GB300.
+
+Workload (default): RMAT scale-24 base graph (2^24 vertices, 8*2^24 generated
+edges from stream seed 5, a/b/c/d = .57/.19/.19/.05, symmetrised -> ~268M
+directed edges), then a stream of update batches whose sizes cycle through
+1e3, 1e4, 1e5, 1e6 edges: each insert batch is 95% new RMAT edges (seed 6)
+and 5% edges sampled from the graph (existing-edge duplicates), each followed
+by an equal-size delete batch of edges sampled uniformly from the base graph.
+
+One step = one insert batch + its delete batch.  `value` = inserted edges/s
+(input batch size / insert time, as the reference reports,
+internal/test.hpp:681-683) with batches resident in HBM; `e2e` = the same
+through the C ABI from pinned host buffers (host->device copy inside the
+timed call).  PageRank (FP64 pull, 10 iterations) and BFS from vertex 0 on
+the updated graph are reported alongside, each with its HBM roofline.
+
+--impl reference times the CPU implementation of the same path (the oracle
+port in oracle/, all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIZES = [1000, 10000, 100000, 1000000]
+RMAT = dict(a=0.57, b=0.19, c=0.19)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def args_parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=int, default=24)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--pr-iters", type=int, default=10)
+    return ap.parse_args()
+
+
+def dist_init(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
+class Clocks:
+    """nvidia-smi sampler running across the timed region."""
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[3:7]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------- workload
+def batch_plan(steps, warmup):
+    return [SIZES[i % len(SIZES)] for i in range(warmup + steps)]
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_cpu(scale, plan, label):
+    """Oracle port on the host cores: build the base graph, then time
+    insert / remove of each planned batch.  Returns (edges/s, details)."""
+    import numpy as np
+
+    import oracle
+    oracle.build()
+    n = 1 << scale
+    t0 = time.time()
+    base = oracle.symmetrize(oracle.rmat(scale, 8 * n, seed=5, **RMAT))
+    o = oracle.OracleGraph(n)
+    o.insert_batch(base)
+    del base
+    build_s = time.time() - t0
+    ins_t = rem_t = 0.0
+    ins_e = 0
+    first = 0
+    for i, b in enumerate(plan):
+        k_new = b - b // 20
+        ins = np.concatenate([oracle.rmat(scale, k_new, seed=6, first=first, **RMAT),
+                              o.sample_edges(b // 20, seed=8, first=first)])
+        first += b
+        t = time.perf_counter()
+        o.insert_batch(ins)
+        ins_t += time.perf_counter() - t
+        ins_e += b
+        rem = o.sample_edges(b, seed=7, first=first)
+        t = time.perf_counter()
+        o.remove_batch(rem)
+        rem_t += time.perf_counter() - t
+    return ins_e / ins_t, {"build_s": round(build_s, 2), "insert_s": ins_t,
+                           "remove_s": rem_t, "edges": ins_e,
+                           "sample": label}
+
+
+def reference_arm(a):
+    rank, world = dist_init(a.gpus)
+    if rank != 0:
+        return
+    plan = batch_plan(a.steps, a.warmup)[a.warmup:]
+    v, det = run_cpu(a.scale, plan, f"all {len(plan)} timed batches ({sum(plan)} edges) "
+                     f"of the workload on the scale-{a.scale} base graph")
+    cores = cpu_threads()
+    line = {
+        "impl": "reference", "metric": "batch-insert edges/s", "value": v,
+        "unit": "edges/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1e3 * (det["insert_s"] + det["remove_s"]) / max(len(plan), 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic RMAT (seeded)",
+        "config": workload_config(a),
+        "cpu_baseline": {"value": v, "unit": "edges/s", "cores": cores, "kind": "port",
+                         "sample": det["sample"]},
+        "e2e": {"value": v, "unit": "edges/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "detail": det,
+        "note": "reference storage code cannot be built on the GPU host (its "
+                "sources are not shipped there); the C restatement in oracle/ is timed",
+    }
+    print(json.dumps(line))
+
+
+def workload_config(a):
+    n = 1 << a.scale
+    return {"workload": f"dynamic updates on RMAT scale-{a.scale}",
+            "vertices": n, "base_generated_edges": 8 * n, "symmetrised": True,
+            "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "seeds": {"base": 5, "insert": 6,
+                                                             "delete": 7, "dup": 8},
+            "batch_sizes": SIZES, "dup_fraction": 0.05,
+            "step": "insert batch + equal-size delete batch",
+            "l2": "flushed (256 MiB write) between timed steps",
+            "parallelism": "replicas" if a.gpus > 1 else "single GPU"}
+
+
+def main():
+    a = args_parse()
+    if a.impl == "reference":
+        return reference_arm(a)
+    import numpy as np
+    import torch
+
+    import sstgraph_gb300 as sg
+    rank, world = dist_init(a.gpus)
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    sg.lib()
+    stream = torch.cuda.Stream()
+    n = 1 << a.scale
+    hbm_peak, peak_kind = peaks()
+
+    # ---- base graph (setup, untimed)
+    g = sg.SparseMatrixV(n, device=dev, initial_slots=int(3.2 * 16 * n))
+    g.set_stream(stream.cuda_stream)
+    chunk = 1 << 25
+    total = 8 * n
+    t0 = time.time()
+    with torch.cuda.stream(stream):
+        buf = torch.empty((chunk, 2), dtype=torch.int32, device="cuda")
+        for first in range(0, total, chunk):
+            k = min(chunk, total - first)
+            sg.gen_rmat(a.scale, k, seed=5, first=first, out=buf[:k], **RMAT)
+            g.insert_batch(buf[:k])
+            g.insert_batch(buf[:k].flip(1).contiguous())
+        del buf
+    torch.cuda.synchronize()
+    build_s = time.time() - t0
+    m0 = g.M()
+
+    # ---- batches (device and pinned host copies)
+    plan = batch_plan(a.steps, a.warmup)
+    ins_d, rem_d, ins_h, rem_h = [], [], [], []
+    first = 0
+    with torch.cuda.stream(stream):
+        for b in plan:
+            k_new = b - b // 20
+            x = torch.empty((b, 2), dtype=torch.int32, device="cuda")
+            sg.gen_rmat(a.scale, k_new, seed=6, first=first, out=x[:k_new], **RMAT)
+            g.sample_edges(b // 20, seed=8, first=first, out=x[k_new:])
+            r = torch.empty((b, 2), dtype=torch.int32, device="cuda")
+            g.sample_edges(b, seed=7, first=first, out=r)
+            first += b
+            ins_d.append(x)
+            rem_d.append(r)
+            ins_h.append(x.cpu().pin_memory())
+            rem_h.append(r.cpu().pin_memory())
+    torch.cuda.synchronize()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
+
+    def run_steps(lo, hi, host, timed):
+        ti = tr = 0.0
+        edges = 0
+        for i in range(lo, hi):
+            with torch.cuda.stream(stream):
+                flush.fill_(i)
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            g.insert_batch(ins_h[i] if host else ins_d[i])
+            e1.record(stream)
+            g.remove_batch(rem_h[i] if host else rem_d[i])
+            e2.record(stream)
+            e2.synchronize()
+            ti += e0.elapsed_time(e1) / 1e3
+            tr += e1.elapsed_time(e2) / 1e3
+            edges += plan[i]
+        return ti, tr, edges
+
+    # ---- warmup + timed (device-resident batches)
+    run_steps(0, a.warmup, False, False)
+    barrier(world)
+    torch.cuda.synchronize()
+    l0 = sg.kernel_launches()
+    sg.profile_start()
+    with Clocks(dev) as clk:
+        ti, tr, edges = run_steps(a.warmup, a.warmup + a.steps, False, True)
+    torch.cuda.synchronize()
+    prof = sg.profile_collect()
+    launches = sg.kernel_launches() - l0
+    barrier(world)
+    clocks = clk.summary()
+    ti = max_over_ranks(ti, world)
+    tr = max_over_ranks(tr, world)
+    value = world * edges / ti
+    ms_per_step = 1e3 * (ti + tr) / a.steps
+
+    # ---- e2e: the same steps through host (pinned) buffers
+    run_steps(0, a.warmup, True, False)
+    eti, etr, eedges = run_steps(a.warmup, a.warmup + a.steps, True, True)
+    e2e = {"value": world * eedges / max_over_ranks(eti, world), "unit": "edges/s",
+           "h2d_bytes_per_step": int(8 * sum(plan[a.warmup:]) * 2 / a.steps),
+           "d2h_bytes_per_step": 16,
+           "note": "insert+remove via sst_insert_batch/sst_remove_batch on pinned host "
+                   "pairs; each call returns the invalid-pair count (8 B) to the host"}
+
+    # ---- pagerank and bfs on the updated graph
+    m = g.M()
+    with torch.cuda.stream(stream):
+        out = torch.empty(n, dtype=torch.float64, device="cuda")
+        sg.PR_S(g, 1, out=out)  # warm: work lists
+    torch.cuda.synchronize()
+    prt = {}
+    for it in (a.pr_iters, 2 * a.pr_iters):
+        best = 1e30
+        for _ in range(3):
+            with torch.cuda.stream(stream):
+                flush.fill_(it)
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            sg.PR_S(g, it, out=out)
+            s1.record(stream)
+            s1.synchronize()
+            best = min(best, s0.elapsed_time(s1) / 1e3)
+        prt[it] = best
+    t_iter = (prt[2 * a.pr_iters] - prt[a.pr_iters]) / a.pr_iters
+    pr_bytes = 4 * m + 24 * n
+    pr_gbs = pr_bytes / t_iter / 1e9
+    sg.profile_start()
+    sg.PR_S(g, a.pr_iters, out=out)
+    torch.cuda.synchronize()
+    pr_prof = sg.profile_collect()
+    pagerank = {"gteps": m / t_iter / 1e9, "ms_per_iter": t_iter * 1e3,
+                "algorithmic_bytes_per_iter": pr_bytes,
+                "roofline": {"bound": "hbm", "achieved": pr_gbs, "peak": hbm_peak,
+                             "unit": "GB/s", "frac": pr_gbs / hbm_peak,
+                             "peak_kind": peak_kind, "traffic": None,
+                             "kernels": "one iteration = k_pr_small + k_pr_chunks + k_pr_fix"},
+                "kernels": pr_prof}
+
+    dep = torch.empty(n, dtype=torch.int32, device="cuda")
+    sg.BFS(g, 0, depths=True, out=dep)
+    torch.cuda.synchronize()
+    bt = 1e30
+    for _ in range(3):
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        sg.BFS(g, 0, depths=True, out=dep)
+        s1.record(stream)
+        s1.synchronize()
+        bt = min(bt, s0.elapsed_time(s1) / 1e3)
+    degs = torch.from_numpy(g.degrees().astype(np.int64))
+    reached = (dep.cpu() >= 0)
+    m_r = int(degs[reached].sum())
+    bfs = {"gteps": m_r / bt / 1e9, "ms": bt * 1e3, "reached": int(reached.sum()),
+           "edges_reached": m_r,
+           "roofline": {"bound": "hbm", "achieved": (4 * m_r + 12 * n) / bt / 1e9,
+                        "peak": hbm_peak, "unit": "GB/s",
+                        "frac": (4 * m_r + 12 * n) / bt / 1e9 / hbm_peak}}
+
+    # ---- roofline of the update step's dominant kernel
+    upd_kernels = prof
+    roofline = update_roofline(prof, plan[a.warmup:], hbm_peak, peak_kind, n)
+
+    # ---- CPU baseline (bounded sample, rank 0 only)
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        sample = SIZES
+        v, det = run_cpu(a.scale, sample,
+                         f"one insert+delete batch of each size {SIZES} on the "
+                         f"scale-{a.scale} base graph (base graph build untimed)")
+        cpu = {"value": v, "unit": "edges/s", "cores": cpu_threads(), "kind": "port",
+               "sample": det["sample"], "detail": det}
+
+    g.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": "batch-insert edges/s", "value": value, "unit": "edges/s",
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic RMAT (seeded device generator; no dataset)",
+        "config": workload_config(a),
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "remove_edges_per_s": world * edges / tr,
+        "base_graph": {"edges": m0, "build_s": round(build_s, 2)},
+        "pagerank": pagerank,
+        "bfs": bfs,
+        "update_kernels": upd_kernels,
+    }
+    print(json.dumps(line))
+
+
+def update_roofline(prof, timed_plan, hbm_peak, peak_kind, n):
+    """Roofline of the update step's dominant kernel from the live timings.
+
+    Algorithmic bytes per launch (keys b of the batch):
+      k_scatter (radix pass)  16 b  (read + write one 8 B key)
+      k_hist (radix pass)      8 b
+      k_locate                 8 b + 8 b (sorted key in, flag + leaf out)
+      k_make_keys              8 b + 8 b (pair in, key out)
+    """
+    per_key = {"k_scatter": 16, "k_hist": 8, "k_locate": 16, "k_make_keys": 16}
+    name, t = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    share = t["ms"] / sum(v["ms"] for v in prof.values())
+    out = {"bound": "hbm", "kernel": name, "launches": t["launches"],
+           "ms_total": t["ms"], "share_of_step_kernel_time": share,
+           "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind, "traffic": None}
+    if name in per_key:
+        keys = 2 * sum(timed_plan)  # insert and remove batches
+        launches_per_batch = t["launches"] / (2 * len(timed_plan))
+        byts = per_key[name] * keys * launches_per_batch
+        ach = byts / (t["ms"] / 1e3) / 1e9
+        out.update({"achieved": ach, "frac": ach / hbm_peak,
+                    "algorithmic_bytes_per_launch": byts / t["launches"]})
+    else:
+        out.update({"achieved": None, "frac": None})
+    return out
+
+
+if __name__ == "__main__":
+    main()

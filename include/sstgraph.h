@@ -172,6 +172,13 @@ SST_API sst_status sst_gen_ref_rmat(uint32_t nn, double a, double b, double c,
                             uint32_t flags);
 
 /* ---- instrumentation -------------------------------------------------- */
+/* kernel profiler (the reference times whole calls with gettimeofday,
+ * internal/helpers.hpp:239-243): between start and collect every kernel
+ * launch is bracketed by CUDA events on its stream; collect writes a JSON
+ * object {"kernel": {"launches": L, "ms": T}, ...} into buf (NUL-terminated,
+ * truncated to cap) and stops profiling */
+SST_API sst_status sst_profile_start(void);
+SST_API sst_status sst_profile_collect(char *buf, uint64_t cap);
 /* raw device layout for structural checks (no reference counterpart):
  * vertex table (base[rows], cap[rows], deg[rows]) and, when slots / lcnt are
  * non-NULL, the first *nslots slab slots and their leaf counts

@@ -86,7 +86,21 @@ SIGNATURES = {
     "sst_gen_ref_rmat": (_i32, [_u32, _dbl, _dbl, _dbl, _u64, _u64, _vp, _u32]),
     "sst_kernel_launches": (_u64, []),
     "sst_raw_state": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64)]),
+    "sst_profile_start": (_i32, []),
+    "sst_profile_collect": (_i32, [ctypes.c_char_p, _u64]),
 }
+
+
+def profile_start():
+    _check(lib().sst_profile_start())
+
+
+def profile_collect() -> dict:
+    """Per-kernel {name: {"launches": L, "ms": T}} since profile_start()."""
+    import json
+    buf = ctypes.create_string_buffer(1 << 20)
+    _check(lib().sst_profile_collect(buf, len(buf)))
+    return json.loads(buf.value.decode())
 
 _lib = None
 

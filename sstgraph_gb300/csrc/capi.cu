@@ -3,12 +3,15 @@
 #include <algorithm>
 #include <cstring>
 #include <new>
+#include <string>
 
 #include "graph.cuh"
 #include "traverse.cuh"
 
 namespace sst {
 const char *error_message();
+void profile_start();
+std::string profile_collect();
 cudaError_t gen_rmat(uint32_t scale, double a, double b, double c, uint64_t seed,
                      uint64_t first, uint64_t count, uint32_t *d_pairs,
                      cudaStream_t s);
@@ -111,6 +114,20 @@ const char *sst_status_string(sst_status s) {
 }
 
 uint64_t sst_kernel_launches(void) { return sst::launches(); }
+
+sst_status sst_profile_start(void) {
+  sst::profile_start();
+  return SST_OK;
+}
+
+sst_status sst_profile_collect(char *buf, uint64_t cap) {
+  if (!buf || cap == 0) return SST_EINVAL;
+  std::string s = sst::profile_collect();
+  size_t k = std::min<size_t>(s.size(), cap - 1);
+  memcpy(buf, s.data(), k);
+  buf[k] = 0;
+  return SST_OK;
+}
 
 sst_status sst_raw_state(sst_graph *g, uint64_t *base, uint32_t *cap,
                          uint32_t *deg, uint32_t *slots, uint8_t *lcnt,

@@ -3,6 +3,11 @@
 // (digit, tile), then a stable scatter that ranks equal digits with
 // warp match_any + per-warp prefix counts in shared memory.
 #include <atomic>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
 
 #include "primitives.cuh"
 
@@ -11,6 +16,99 @@ namespace sst {
 static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 uint64_t launches() { return g_launches.load(std::memory_order_relaxed); }
+
+// ------------------------------------------------------------- profiler
+namespace {
+struct Pending {
+  const char *name;
+  cudaEvent_t a, b;
+};
+struct Totals {
+  uint64_t launches = 0;
+  double ms = 0;
+};
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+std::vector<cudaEvent_t> g_pool;
+std::vector<Pending> g_pending;
+std::map<std::string, Totals> g_totals;
+
+cudaEvent_t take_event() {
+  if (!g_pool.empty()) {
+    cudaEvent_t e = g_pool.back();
+    g_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// fold finished pairs into the totals (caller holds the lock)
+void drain(bool wait) {
+  size_t keep = 0;
+  for (size_t i = 0; i < g_pending.size(); i++) {
+    Pending &p = g_pending[i];
+    if (wait) cudaEventSynchronize(p.b);
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      Totals &t = g_totals[p.name];
+      t.launches++;
+      t.ms += ms;
+      g_pool.push_back(p.a);
+      g_pool.push_back(p.b);
+    } else {
+      cudaGetLastError();
+      g_pending[keep++] = p;
+    }
+  }
+  g_pending.resize(keep);
+}
+}  // namespace
+
+bool profiling() { return g_prof_on; }
+
+cudaEvent_t prof_begin(cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  cudaEvent_t e = take_event();
+  cudaEventRecord(e, s);
+  return e;
+}
+
+void prof_end(const char *name, cudaEvent_t start, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  cudaEvent_t e = take_event();
+  cudaEventRecord(e, s);
+  g_pending.push_back({name, start, e});
+  if (g_pending.size() > 4096) drain(false);
+}
+
+void profile_start() {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  drain(true);
+  g_totals.clear();
+  g_prof_on = true;
+}
+
+// JSON object {"kernel": {"launches": L, "ms": T}, ...}; stops profiling
+std::string profile_collect() {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_on = false;
+  drain(true);
+  std::string out = "{";
+  bool first = true;
+  for (auto &kv : g_totals) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s\"%s\": {\"launches\": %llu, \"ms\": %.6f}",
+             first ? "" : ", ", kv.first.c_str(),
+             (unsigned long long)kv.second.launches, kv.second.ms);
+    out += buf;
+    first = false;
+  }
+  out += "}";
+  g_totals.clear();
+  return out;
+}
 
 namespace {
 

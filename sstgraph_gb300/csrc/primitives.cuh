@@ -12,10 +12,20 @@ namespace sst {
 void note_launch();
 uint64_t launches();
 
+// Kernel profiler: while enabled, every launch is bracketed by a pair of
+// CUDA events on its own stream; profile_collect() folds the elapsed times
+// per kernel name.
+bool profiling();
+cudaEvent_t prof_begin(cudaStream_t s);
+void prof_end(const char *name, cudaEvent_t start, cudaStream_t s);
+
 #define SST_LAUNCH(kernel, grid, block, smem, stream, ...)                    \
   do {                                                                        \
+    cudaEvent_t _sst_ev = ::sst::profiling() ? ::sst::prof_begin(stream)      \
+                                             : nullptr;                       \
     kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);               \
     ::sst::note_launch();                                                     \
+    if (_sst_ev) ::sst::prof_end(#kernel, _sst_ev, stream);                   \
   } while (0)
 
 // ----------------------------------------------------------------- arena
