@@ -147,6 +147,17 @@ SST_API sst_status sst_bfs(sst_graph *g, uint32_t src, int32_t *parents,
 /* PR_S<double>(g, iters)  test.hpp:527 */
 SST_API sst_status sst_pagerank(sst_graph *g, uint32_t iters, double damping,
                         double *out, uint32_t flags);
+/* PageRank that allocates nothing during the call (no counterpart in the
+ * reference).  For callers that cannot let a call allocate: a serving loop
+ * under a fixed HBM budget, or a host program sharing the GPU whose other
+ * streams would stall on the device-wide synchronisation of cudaMalloc /
+ * cudaFree.  Same result as sst_pagerank; its scratch is one fixed array
+ * inside the library, so graphs are limited to 262,144 rows (larger ones get
+ * SST_EINVAL) and d_rank must be device memory.  The first call on a device
+ * looks the array up (make it before capturing a stream); calls that overlap
+ * on the GPU share the array and race. */
+SST_API sst_status sst_pagerank_noalloc(sst_graph *g, uint32_t iters,
+                                        double damping, double *d_rank);
 /* CC(g)  test.hpp:571: label = smallest vertex id of the component */
 SST_API sst_status sst_cc(sst_graph *g, uint32_t *labels, uint32_t flags);
 /* BC(g, src)  test.hpp:547: single-source dependency scores */

@@ -86,6 +86,7 @@ SIGNATURES = {
     "sst_gen_ref_rmat": (_i32, [_u32, _dbl, _dbl, _dbl, _u64, _u64, _vp, _u32]),
     "sst_kernel_launches": (_u64, []),
     "sst_raw_state": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64)]),
+    "sst_pagerank_noalloc": (_i32, [_vp, _u32, _dbl, _vp]),
     "sst_profile_start": (_i32, []),
     "sst_profile_collect": (_i32, [ctypes.c_char_p, _u64]),
 }
