@@ -56,16 +56,18 @@ template <typename T> struct DevBuf {
 struct TravState {
   uint64_t version = ~0ull;
   // chunk list of multi-leaf vertices
-  uint64_t nchunks = 0, nmulti = 0, nbig = 0;
+  uint64_t nchunks = 0, nmulti = 0, nbig = 0, nsmall = 0;
+  uint64_t inv_version = ~0ull;
   DevBuf<uint64_t> choff;   // per vertex: first chunk (n+1)
   DevBuf<uint32_t> cv, cl0; // per chunk: vertex, first leaf
   DevBuf<uint32_t> multi;   // vertices with more than one chunk
   DevBuf<uint32_t> big;     // vertices with a multi-leaf segment
+  DevBuf<uint32_t> small;   // vertices with a one-leaf segment (deg >= 1)
   DevBuf<uint32_t> flag, pos;
   // pagerank
   DevBuf<double> inv_deg, ca, cb, partial;
   // bfs
-  DevBuf<uint32_t> qa, qb, fbits;
+  DevBuf<uint32_t> qa, qb, fbits, icnt, ioff, iv, il0;
   DevBuf<int32_t> depth_tmp, parent_tmp;
   // bc
   DevBuf<double> sigma, ratio;
@@ -87,6 +89,7 @@ void trav_release(sst_graph *g) {
   t->cl0.release();
   t->multi.release();
   t->big.release();
+  t->small.release();
   t->flag.release();
   t->pos.release();
   t->inv_deg.release();
@@ -96,6 +99,10 @@ void trav_release(sst_graph *g) {
   t->qa.release();
   t->qb.release();
   t->fbits.release();
+  t->icnt.release();
+  t->ioff.release();
+  t->iv.release();
+  t->il0.release();
   t->depth_tmp.release();
   t->parent_tmp.release();
   t->sigma.release();
@@ -119,7 +126,8 @@ namespace {
 __global__ void k_chunk_counts(const uint32_t *__restrict__ cap, uint32_t n,
                                uint64_t *__restrict__ nch,
                                uint32_t *__restrict__ bigf,
-                               uint32_t *__restrict__ multif) {
+                               uint32_t *__restrict__ multif,
+                               uint32_t *__restrict__ smallf) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   uint32_t c = cap[v];
@@ -127,6 +135,7 @@ __global__ void k_chunk_counts(const uint32_t *__restrict__ cap, uint32_t n,
   nch[v] = k;
   bigf[v] = c > kLeaf;
   multif[v] = k > 1;
+  smallf[v] = c > 0 && c <= kLeaf;
 }
 
 __global__ void k_chunk_fill(const uint32_t *__restrict__ cap, uint32_t n,
@@ -150,43 +159,76 @@ __global__ void k_compact_ids(const uint32_t *__restrict__ flag,
 }
 
 // ------------------------------------------------------------- pagerank
-__global__ void k_pr_init(const uint32_t *__restrict__ deg, uint32_t n,
-                          double r0, double *__restrict__ inv_deg,
-                          double *__restrict__ contrib) {
+// Per-edge sums are exact 64-bit fixed-point integer additions: each
+// contribution rank(u)/deg(u) is rounded once to a multiple of 2^-63 and the
+// sums are order-independent.  GB300 runs FP64 at a small fraction of its
+// integer rate, so an FP64 add per edge would bound an iteration by the FP64
+// pipe instead of HBM; per-vertex arithmetic stays in FP64.
+constexpr double kFix = 9223372036854775808.0;  // 2^63
+
+__global__ void k_pr_inv(const uint32_t *__restrict__ deg, uint32_t n,
+                         double *__restrict__ inv_scaled) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   uint32_t d = deg[v];
-  double inv = d ? 1.0 / (double)d : 0.0;
-  inv_deg[v] = inv;
-  contrib[v] = r0 * inv;
+  inv_scaled[v] = d ? kFix / (double)d : 0.0;
 }
 
-// thread per vertex with a one-leaf segment: pull in ascending order
-__global__ void k_pr_small(DGraph g, const double *__restrict__ cin,
-                           double *__restrict__ rank, double *__restrict__ cout,
-                           const double *__restrict__ inv_deg, double base,
-                           double damp) {
+__global__ void k_pr_start(const uint32_t *__restrict__ deg, uint32_t n,
+                           double r0, const double *__restrict__ inv_scaled,
+                           unsigned long long *__restrict__ contrib,
+                           double *__restrict__ rank, double base) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= g.n) return;
-  uint32_t cap = g.cap[v];
-  if (cap > kLeaf) return;
-  uint32_t d = g.deg[v];
-  const uint32_t *p = g.slots + g.base[v];
-  double s = 0.0;
-  for (uint32_t i = 0; i < d; i++) s += cin[p[i]];
-  double r = base + damp * s;
-  rank[v] = r;
-  cout[v] = r * inv_deg[v];
+  if (v >= n) return;
+  contrib[v] = __double2ull_rn(r0 * inv_scaled[v]);
+  if (deg[v] == 0) rank[v] = base;  // no in-edges: constant term only
 }
 
-// warp per chunk of a multi-leaf segment
+__device__ __forceinline__ void pr_finish(uint32_t v, unsigned long long sum,
+                                          double dscale, double base,
+                                          const double *inv_scaled,
+                                          unsigned long long *cout,
+                                          double *rank, bool last) {
+  double r = fma(__ull2double_rn(sum), dscale, base);
+  cout[v] = __double2ull_rn(r * inv_scaled[v]);
+  if (last) rank[v] = r;
+}
+
+// 8 lanes per vertex with a one-leaf segment (cap <= 32): each group of 8
+// lanes reads one 32-byte sector of the leaf per step
+__global__ void k_pr_small(DGraph g, const uint32_t *__restrict__ small,
+                           uint64_t nsmall,
+                           const unsigned long long *__restrict__ cin,
+                           unsigned long long *__restrict__ cout,
+                           double *__restrict__ rank,
+                           const double *__restrict__ inv_scaled, double base,
+                           double dscale, bool last) {
+  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t i = t >> 3;
+  const uint32_t sub = threadIdx.x & 7;
+  unsigned long long acc = 0;
+  uint32_t v = 0;
+  if (i < nsmall) {
+    v = small[i];
+    uint32_t d = g.deg[v];
+    const uint32_t *p = g.slots + g.base[v];
+    for (uint32_t j = sub; j < d; j += 8) acc += cin[p[j]];
+  }
+  acc += __shfl_xor_sync(0xffffffffu, acc, 4);
+  acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+  acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+  if (i < nsmall && sub == 0) pr_finish(v, acc, dscale, base, inv_scaled, cout, rank, last);
+}
+
+// warp per chunk of <= 32 leaves of a multi-leaf segment
 __global__ void k_pr_chunks(DGraph g, const uint32_t *__restrict__ cv,
                             const uint32_t *__restrict__ cl0, uint64_t nchunks,
-                            const double *__restrict__ cin,
-                            double *__restrict__ rank, double *__restrict__ cout,
-                            const double *__restrict__ inv_deg,
-                            double *__restrict__ partial, double base,
-                            double damp) {
+                            const unsigned long long *__restrict__ cin,
+                            unsigned long long *__restrict__ cout,
+                            double *__restrict__ rank,
+                            const double *__restrict__ inv_scaled,
+                            unsigned long long *__restrict__ partial,
+                            double base, double dscale, bool last) {
   uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= nchunks) return;
@@ -195,37 +237,40 @@ __global__ void k_pr_chunks(DGraph g, const uint32_t *__restrict__ cv,
   uint32_t l0 = cl0[c], l1 = min(l0 + kChunkLeaves, nl);
   uint64_t sb = g.base[v];
   const uint8_t *lc = g.lcnt + (sb >> kLeafLog);
-  double acc = 0.0;
+  const uint32_t *sl = g.slots + sb;
+  unsigned long long acc = 0;
   for (uint32_t l = l0; l < l1; l++) {
     uint32_t cnt = lc[l];
-    if ((uint32_t)lane < cnt) acc += cin[g.slots[sb + ((uint64_t)l << kLeafLog) + lane]];
+    if ((uint32_t)lane < cnt) acc += cin[sl[((uint64_t)l << kLeafLog) + lane]];
   }
-  double s = warp_sum_d(acc);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
   if (lane == 0) {
-    if (nl <= kChunkLeaves) {
-      double r = base + damp * s;
-      rank[v] = r;
-      cout[v] = r * inv_deg[v];
-    } else {
-      partial[c] = s;
-    }
+    if (nl <= kChunkLeaves)
+      pr_finish(v, acc, dscale, base, inv_scaled, cout, rank, last);
+    else
+      partial[c] = acc;
   }
 }
 
 __global__ void k_pr_fix(const uint32_t *__restrict__ multi, uint64_t nmulti,
                          const uint64_t *__restrict__ choff,
-                         const double *__restrict__ partial,
-                         double *__restrict__ rank, double *__restrict__ cout,
-                         const double *__restrict__ inv_deg, double base,
-                         double damp) {
+                         const unsigned long long *__restrict__ partial,
+                         unsigned long long *__restrict__ cout,
+                         double *__restrict__ rank,
+                         const double *__restrict__ inv_scaled, double base,
+                         double dscale, bool last) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nmulti) return;
   uint32_t v = multi[i];
-  double s = 0.0;
+  unsigned long long s = 0;
   for (uint64_t c = choff[v]; c < choff[v + 1]; c++) s += partial[c];
-  double r = base + damp * s;
-  rank[v] = r;
-  cout[v] = r * inv_deg[v];
+  pr_finish(v, s, dscale, base, inv_scaled, cout, rank, last);
+}
+
+__global__ void k_fill_d(double *__restrict__ p, uint32_t n, double x) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n) p[v] = x;
 }
 
 // ------------------------------------------------------------- bfs
@@ -238,49 +283,82 @@ __global__ void k_bfs_init(int32_t *__restrict__ depth, int32_t *__restrict__ pa
 }
 
 // warp-aggregated append of `mine` to the next queue
+// counters: [0] queue length, [1] degree sum, [2] work items of the queue
 __device__ __forceinline__ void enqueue(bool mine, uint32_t w, uint32_t wdeg,
-                                        uint32_t *q, unsigned long long *qlen_deg) {
+                                        uint32_t witems, uint32_t *q,
+                                        unsigned long long *qlen_deg) {
   const int lane = threadIdx.x & 31;
   uint32_t m = __ballot_sync(0xffffffffu, mine);
   if (!m) return;
   uint32_t dsum = __reduce_add_sync(0xffffffffu, mine ? wdeg : 0u);
+  uint32_t isum = __reduce_add_sync(0xffffffffu, mine ? witems : 0u);
   int leader = __ffs(m) - 1;
   unsigned long long base = 0;
-  // low 32 bits: queue length, high 32 bits ignored; degree sum separate
   if (lane == leader) {
     base = atomicAdd(&qlen_deg[0], (unsigned long long)__popc(m));
     atomicAdd(&qlen_deg[1], (unsigned long long)dsum);
+    atomicAdd(&qlen_deg[2], (unsigned long long)isum);
   }
   base = __shfl_sync(0xffffffffu, base, leader);
   if (mine) q[base + __popc(m & ((1u << lane) - 1u))] = w;
 }
 
-// push: warp per frontier vertex, lanes over the slots of each leaf
-__global__ void k_bfs_push(DGraph g, const uint32_t *__restrict__ q, uint32_t qn,
+// work items of one vertex: 1 for a one-leaf segment, else one per chunk
+// of kChunkLeaves leaves
+__device__ __forceinline__ uint32_t items_of(uint32_t cap) {
+  return cap > kLeaf ? ((cap >> kLeafLog) + kChunkLeaves - 1) / kChunkLeaves : 1u;
+}
+
+__global__ void k_front_items(const uint32_t *__restrict__ q, uint32_t qn,
+                              const uint32_t *__restrict__ cap,
+                              uint32_t *__restrict__ cnt) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < qn) cnt[i] = items_of(cap[q[i]]);
+}
+
+__global__ void k_front_expand(const uint32_t *__restrict__ q, uint32_t qn,
+                               const uint32_t *__restrict__ cap,
+                               const uint32_t *__restrict__ off,
+                               uint32_t *__restrict__ iv,
+                               uint32_t *__restrict__ il0) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= qn) return;
+  uint32_t v = q[i], k = items_of(cap[v]), o = off[i];
+  for (uint32_t j = 0; j < k; j++) {
+    iv[o + j] = v;
+    il0[o + j] = j * kChunkLeaves;
+  }
+}
+
+// push: warp per work item (a frontier vertex's leaf chunk), lane = slot
+__global__ void k_bfs_push(DGraph g, const uint32_t *__restrict__ iv,
+                           const uint32_t *__restrict__ il0, uint32_t nitems,
                            int32_t *__restrict__ depth,
                            int32_t *__restrict__ parent,
                            uint32_t *__restrict__ nq,
                            unsigned long long *__restrict__ cnt, int lvl) {
   uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (i >= qn) return;
-  uint32_t u = q[i];
+  if (i >= nitems) return;
+  uint32_t u = iv[i];
   uint64_t base = g.base[u];
   uint32_t cap = g.cap[u], deg = g.deg[u];
   uint32_t nl = cap ? nleaves_of(cap) : 0;
-  for (uint32_t l = 0; l < nl; l++) {
+  uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+  for (uint32_t l = l0; l < l1; l++) {
     uint32_t c = leaf_count(g, base, cap, deg, l);
     bool mine = false;
-    uint32_t w = 0, wd = 0;
+    uint32_t w = 0, wd = 0, wi = 0;
     if ((uint32_t)lane < c) {
       w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
       if (depth[w] < 0 && atomicCAS(&depth[w], -1, lvl + 1) == -1) {
         parent[w] = (int32_t)u;
         mine = true;
         wd = g.deg[w];
+        wi = items_of(g.cap[w]);
       }
     }
-    enqueue(mine, w, wd, nq, cnt);
+    enqueue(mine, w, wd, wi, nq, cnt);
   }
 }
 
@@ -318,7 +396,7 @@ __global__ void k_bfs_pull_small(DGraph g, const uint32_t *__restrict__ fbits,
       }
     }
   }
-  enqueue(mine, v, d, nq, cnt);
+  enqueue(mine, v, d, 1u, nq, cnt);
 }
 
 // pull, multi-leaf vertices: warp per vertex, leaf by leaf, early exit
@@ -351,7 +429,7 @@ __global__ void k_bfs_pull_big(DGraph g, const uint32_t *__restrict__ big,
       found = true;
     }
   }
-  enqueue(found && lane == 0, v, g.deg[v], nq, cnt);
+  enqueue(found && lane == 0, v, g.deg[v], items_of(g.cap[v]), nq, cnt);
 }
 
 // ------------------------------------------------------------- cc
@@ -450,26 +528,85 @@ __global__ void k_sigma_small(DGraph g, const uint32_t *__restrict__ list,
   sigma[v] = s;
 }
 
-__global__ void k_sigma_big(DGraph g, const uint32_t *__restrict__ list,
-                            uint32_t cnt, const int32_t *__restrict__ depth,
-                            double *__restrict__ sigma, int32_t d) {
+// items (big vertices of the level list, one per leaf chunk)
+__global__ void k_bc_item_counts(const uint32_t *__restrict__ list, uint32_t nl,
+                                 const uint32_t *__restrict__ cap,
+                                 uint32_t *__restrict__ cnt) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nl) return;
+  uint32_t c = cap[list[p]];
+  cnt[p] = c > kLeaf ? ((c >> kLeafLog) + kChunkLeaves - 1) / kChunkLeaves : 0;
+}
+
+__global__ void k_bc_expand(const uint32_t *__restrict__ list, uint32_t nl,
+                            const uint32_t *__restrict__ cnt,
+                            const uint32_t *__restrict__ off,
+                            uint32_t *__restrict__ iv, uint32_t *__restrict__ il0) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nl) return;
+  for (uint32_t j = 0; j < cnt[p]; j++) {
+    iv[off[p] + j] = list[p];
+    il0[off[p] + j] = j * kChunkLeaves;
+  }
+}
+
+__global__ void k_gather_bounds(const uint32_t *__restrict__ off,
+                                const uint32_t *__restrict__ pos, uint32_t k,
+                                uint32_t *__restrict__ out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) out[i] = off[pos[i]];
+}
+
+// warp per chunk: partial sum of val[u] over the chunk's neighbours u at
+// depth want (sigma pass: want = d-1 over sigma; dependency pass: want =
+// d+1 over ratio)
+__global__ void k_bc_chunks(DGraph g, const uint32_t *__restrict__ iv,
+                            const uint32_t *__restrict__ il0, uint32_t i0,
+                            uint32_t ni, const int32_t *__restrict__ depth,
+                            const double *__restrict__ val, int32_t want,
+                            double *__restrict__ partial) {
   uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (i >= cnt) return;
-  uint32_t v = list[i];
-  uint32_t cap = g.cap[v];
-  if (cap <= kLeaf) return;
+  if (i >= ni) return;
+  i += i0;
+  uint32_t v = iv[i];
+  uint32_t nl = g.cap[v] >> kLeafLog;
+  uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
   uint64_t base = g.base[v];
   const uint8_t *lc = g.lcnt + (base >> kLeafLog);
   double acc = 0.0;
-  for (uint32_t l = 0; l < (cap >> kLeafLog); l++) {
+  for (uint32_t l = l0; l < l1; l++) {
     if ((uint32_t)lane < lc[l]) {
       uint32_t u = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
-      if (depth[u] == d - 1) acc += sigma[u];
+      if (depth[u] == want) acc += val[u];
     }
   }
   double s = warp_sum_d(acc);
-  if (lane == 0) sigma[v] = s;
+  if (lane == 0) partial[i] = s;
+}
+
+// thread per big vertex of the level: combine its chunk partials in order
+__global__ void k_bc_fix(const uint32_t *__restrict__ list, uint32_t p0,
+                         uint32_t np, const uint32_t *__restrict__ cnt,
+                         const uint32_t *__restrict__ off,
+                         const double *__restrict__ partial, bool sigma_pass,
+                         double *__restrict__ sigma, double *__restrict__ ratio,
+                         double *__restrict__ dep) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  p += p0;
+  uint32_t k = cnt[p];
+  if (k == 0) return;
+  double s = 0.0;
+  for (uint32_t j = 0; j < k; j++) s += partial[off[p] + j];
+  uint32_t v = list[p];
+  if (sigma_pass) {
+    sigma[v] = s;
+  } else {
+    double dv = sigma[v] * s;
+    dep[v] = dv;
+    ratio[v] = (1.0 + dv) / sigma[v];
+  }
 }
 
 // dep(v) = sigma(v) * sum over neighbours one level down of (1+dep(w))/sigma(w)
@@ -492,34 +629,6 @@ __global__ void k_delta_small(DGraph g, const uint32_t *__restrict__ list,
   double dv = sigma[v] * s;
   dep[v] = dv;
   ratio[v] = (1.0 + dv) / sigma[v];
-}
-
-__global__ void k_delta_big(DGraph g, const uint32_t *__restrict__ list,
-                            uint32_t cnt, const int32_t *__restrict__ depth,
-                            const double *__restrict__ sigma,
-                            double *__restrict__ ratio, double *__restrict__ dep,
-                            int32_t d) {
-  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (i >= cnt) return;
-  uint32_t v = list[i];
-  uint32_t cap = g.cap[v];
-  if (cap <= kLeaf) return;
-  uint64_t base = g.base[v];
-  const uint8_t *lc = g.lcnt + (base >> kLeafLog);
-  double acc = 0.0;
-  for (uint32_t l = 0; l < (cap >> kLeafLog); l++) {
-    if ((uint32_t)lane < lc[l]) {
-      uint32_t w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
-      if (depth[w] == d + 1) acc += ratio[w];
-    }
-  }
-  double s = warp_sum_d(acc);
-  if (lane == 0) {
-    double dv = sigma[v] * s;
-    dep[v] = dv;
-    ratio[v] = (1.0 + dv) / sigma[v];
-  }
 }
 
 // ------------------------------------------------------------- tc
@@ -680,40 +789,45 @@ static sst_status ensure_lists(sst_graph *g) {
   cudaStream_t s = g->stream;
   uint32_t n = g->n;
   SST_CUDA_TRY(t->choff.ensure((uint64_t)n + 1));
-  SST_CUDA_TRY(t->flag.ensure((uint64_t)n * 2 + 2));
-  SST_CUDA_TRY(t->pos.ensure((uint64_t)n * 2 + 2));
-  uint32_t *bigf = t->flag.p, *multif = t->flag.p + n + 1;
-  uint32_t *bigp = t->pos.p, *multip = t->pos.p + n + 1;
+  SST_CUDA_TRY(t->flag.ensure((uint64_t)n * 3 + 3));
+  SST_CUDA_TRY(t->pos.ensure((uint64_t)n * 3 + 3));
+  uint32_t *bigf = t->flag.p, *multif = t->flag.p + n + 1, *smallf = t->flag.p + 2 * (n + 1);
+  uint32_t *bigp = t->pos.p, *multip = t->pos.p + n + 1, *smallp = t->pos.p + 2 * (n + 1);
   g->arena.reset();
-  SST_CUDA_TRY(g->arena.reserve(3 * scan_scratch_bytes((uint64_t)n + 1, 8) + 4096));
+  SST_CUDA_TRY(g->arena.reserve(4 * scan_scratch_bytes((uint64_t)n + 1, 8) + 4096));
   uint64_t *tot = g->arena.take<uint64_t>(1);
-  uint32_t *tot32 = g->arena.take<uint32_t>(2);
+  uint32_t *tot32 = g->arena.take<uint32_t>(3);
   if (n) SST_LAUNCH(k_chunk_counts, blocks_for(n), kTB, 0, s, g->d_cap, n,
-                    t->choff.p, bigf, multif);
+                    t->choff.p, bigf, multif, smallf);
   SST_CUDA_TRY((scan<uint64_t, OpAdd>(t->choff.p, t->choff.p, n, 0ull, OpAdd{},
                                       true, false, tot, g->arena, s)));
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(bigf, bigp, n, 0u, OpAdd{}, true, false,
                                       tot32, g->arena, s)));
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(multif, multip, n, 0u, OpAdd{}, true,
                                       false, tot32 + 1, g->arena, s)));
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(smallf, smallp, n, 0u, OpAdd{}, true,
+                                      false, tot32 + 2, g->arena, s)));
   uint64_t h[2];
-  uint32_t h32[2];
+  uint32_t h32[3];
   SST_CUDA_TRY(cudaMemcpyAsync(h, tot, 8, cudaMemcpyDeviceToHost, s));
-  SST_CUDA_TRY(cudaMemcpyAsync(h32, tot32, 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaMemcpyAsync(h32, tot32, 12, cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   t->nchunks = h[0];
   t->nbig = h32[0];
   t->nmulti = h32[1];
+  t->nsmall = h32[2];
   SST_CUDA_TRY(cudaMemcpyAsync(t->choff.p + n, &t->nchunks, 8, cudaMemcpyHostToDevice, s));
   SST_CUDA_TRY(t->cv.ensure(t->nchunks + 1));
   SST_CUDA_TRY(t->cl0.ensure(t->nchunks + 1));
   SST_CUDA_TRY(t->big.ensure(t->nbig + 1));
   SST_CUDA_TRY(t->multi.ensure(t->nmulti + 1));
+  SST_CUDA_TRY(t->small.ensure(t->nsmall + 1));
   if (n) {
     SST_LAUNCH(k_chunk_fill, blocks_for(n), kTB, 0, s, g->d_cap, n, t->choff.p,
                t->cv.p, t->cl0.p);
     SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, bigf, bigp, n, t->big.p);
     SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, multif, multip, n, t->multi.p);
+    SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, smallf, smallp, n, t->small.p);
   }
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   SST_CUDA_TRY(cudaGetLastError());
@@ -728,33 +842,41 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   cudaStream_t s = g->stream;
   uint32_t n = g->n;
   if (n == 0) return SST_OK;
-  SST_CUDA_TRY(t->inv_deg.ensure(n));
   SST_CUDA_TRY(t->ca.ensure(n));
   SST_CUDA_TRY(t->cb.ensure(n));
   SST_CUDA_TRY(t->partial.ensure(t->nchunks + 1));
+  if (t->inv_version != g->version) {
+    SST_CUDA_TRY(t->inv_deg.ensure(n));
+    SST_LAUNCH(k_pr_inv, blocks_for(n), kTB, 0, s, g->d_deg, n, t->inv_deg.p);
+    t->inv_version = g->version;
+  }
   double r0 = 1.0 / (double)n;
   double base = (1.0 - damping) / (double)n;
-  SST_LAUNCH(k_pr_init, blocks_for(n), kTB, 0, s, g->d_deg, n, r0, t->inv_deg.p, t->ca.p);
   if (iters == 0) {
-    // rank stays 1/n
-    std::vector<double> h(n, r0);
-    SST_CUDA_TRY(cudaMemcpyAsync(d_rank, h.data(), (uint64_t)n * 8, cudaMemcpyHostToDevice, s));
-    SST_CUDA_TRY(cudaStreamSynchronize(s));
+    SST_LAUNCH(k_fill_d, blocks_for(n), kTB, 0, s, d_rank, n, r0);
+    SST_CUDA_TRY(cudaGetLastError());
     return SST_OK;
   }
+  unsigned long long *cin = reinterpret_cast<unsigned long long *>(t->ca.p);
+  unsigned long long *cout = reinterpret_cast<unsigned long long *>(t->cb.p);
+  unsigned long long *part = reinterpret_cast<unsigned long long *>(t->partial.p);
+  SST_LAUNCH(k_pr_start, blocks_for(n), kTB, 0, s, g->d_deg, n, r0, t->inv_deg.p,
+             cin, d_rank, base);
   DGraph dg = g->view();
-  double *cin = t->ca.p, *cout = t->cb.p;
+  const double dscale = damping / kFix;
   for (uint32_t it = 0; it < iters; it++) {
-    SST_LAUNCH(k_pr_small, blocks_for(n), kTB, 0, s, dg, cin, d_rank, cout,
-               t->inv_deg.p, base, damping);
+    bool last = it + 1 == iters;
+    if (t->nsmall)
+      SST_LAUNCH(k_pr_small, blocks_for(t->nsmall * 8), kTB, 0, s, dg, t->small.p,
+                 t->nsmall, cin, cout, d_rank, t->inv_deg.p, base, dscale, last);
     if (t->nchunks)
       SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cv.p,
-                 t->cl0.p, t->nchunks, cin, d_rank, cout, t->inv_deg.p,
-                 t->partial.p, base, damping);
+                 t->cl0.p, t->nchunks, cin, cout, d_rank, t->inv_deg.p, part,
+                 base, dscale, last);
     if (t->nmulti)
       SST_LAUNCH(k_pr_fix, blocks_for(t->nmulti), kTB, 0, s, t->multi.p,
-                 t->nmulti, t->choff.p, t->partial.p, d_rank, cout, t->inv_deg.p,
-                 base, damping);
+                 t->nmulti, t->choff.p, part, cout, d_rank, t->inv_deg.p, base,
+                 dscale, last);
     std::swap(cin, cout);
   }
   SST_CUDA_TRY(cudaGetLastError());
@@ -782,19 +904,25 @@ sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths
   DGraph dg = g->view();
   SST_LAUNCH(k_bfs_init, blocks_for(n), kTB, 0, s, depth, parent, n, src);
   SST_CUDA_TRY(cudaMemcpyAsync(t->qa.p, &src, 4, cudaMemcpyHostToDevice, s));
-  uint32_t sdeg = 0;
-  SST_CUDA_TRY(cudaMemcpyAsync(&sdeg, g->d_deg + src, 4, cudaMemcpyDeviceToHost, s));
+  uint32_t sinfo[2] = {0, 0};
+  SST_CUDA_TRY(cudaMemcpyAsync(&sinfo[0], g->d_deg + src, 4, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaMemcpyAsync(&sinfo[1], g->d_cap + src, 4, cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));
-  uint64_t qn = 1, qdeg = sdeg;
+  uint64_t qn = 1, qdeg = sinfo[0];
+  uint64_t qitems = sinfo[1] > kLeaf ? ((sinfo[1] >> kLeafLog) + kChunkLeaves - 1) / kChunkLeaves : 1;
   uint32_t *q = t->qa.p, *nq = t->qb.p;
   unsigned long long *cnt = t->d_small;
   const uint64_t m = g->m;
+  SST_CUDA_TRY(t->icnt.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->ioff.ensure((uint64_t)n + 1));
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes((uint64_t)n + 1, 4) + 4096));
   for (int lvl = 0; qn > 0; lvl++) {
     if ((uint64_t)lvl > n) {
       set_error_message("BFS exceeded n levels");
       return SST_ETIMEDOUT;
     }
-    SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, 16, s));
+    SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, 24, s));
     if ((qn + qdeg) * 20 > m) {
       SST_CUDA_TRY(cudaMemsetAsync(t->fbits.p, 0, ((uint64_t)n / 32 + 1) * 4, s));
       SST_LAUNCH(k_q2bits, blocks_for(qn), kTB, 0, s, q, (uint32_t)qn, t->fbits.p);
@@ -804,13 +932,23 @@ sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths
         SST_LAUNCH(k_bfs_pull_big, warp_blocks(t->nbig), kTB, 0, s, dg, t->big.p,
                    t->nbig, t->fbits.p, depth, parent, nq, cnt, lvl);
     } else {
-      SST_LAUNCH(k_bfs_push, warp_blocks(qn), kTB, 0, s, dg, q, (uint32_t)qn,
-                 depth, parent, nq, cnt, lvl);
+      SST_CUDA_TRY(t->iv.ensure(qitems + 1));
+      SST_CUDA_TRY(t->il0.ensure(qitems + 1));
+      SST_LAUNCH(k_front_items, blocks_for(qn), kTB, 0, s, q, (uint32_t)qn,
+                 g->d_cap, t->icnt.p);
+      g->arena.reset();
+      SST_CUDA_TRY((scan<uint32_t, OpAdd>(t->icnt.p, t->ioff.p, qn, 0u, OpAdd{},
+                                          true, false, nullptr, g->arena, s)));
+      SST_LAUNCH(k_front_expand, blocks_for(qn), kTB, 0, s, q, (uint32_t)qn,
+                 g->d_cap, t->ioff.p, t->iv.p, t->il0.p);
+      SST_LAUNCH(k_bfs_push, warp_blocks(qitems), kTB, 0, s, dg, t->iv.p, t->il0.p,
+                 (uint32_t)qitems, depth, parent, nq, cnt, lvl);
     }
-    SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, cnt, 16, cudaMemcpyDeviceToHost, s));
+    SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, cnt, 24, cudaMemcpyDeviceToHost, s));
     SST_CUDA_TRY(cudaStreamSynchronize(s));
     qn = t->h_small[0];
     qdeg = t->h_small[1];
+    qitems = t->h_small[2];
     std::swap(q, nq);
   }
   SST_CUDA_TRY(cudaGetLastError());
@@ -854,14 +992,15 @@ sst_status bc(sst_graph *g, uint32_t src, double *d_dep) {
   SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, t->d_small, 8, cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   uint32_t D = (uint32_t)t->h_small[0];
-  SST_CUDA_TRY(t->lvl_cnt.ensure(3 * ((uint64_t)D + 2)));
+  SST_CUDA_TRY(t->lvl_cnt.ensure(4 * ((uint64_t)D + 2)));
   SST_CUDA_TRY(t->lvl_list.ensure(n + 1));
   SST_CUDA_TRY(t->sigma.ensure(n));
   SST_CUDA_TRY(t->ratio.ensure(n));
-  uint32_t *cnt = t->lvl_cnt.p, *off = cnt + D + 2, *ctr = off + D + 2;
+  uint32_t *cnt = t->lvl_cnt.p, *off = cnt + D + 2, *ctr = off + D + 2,
+           *ibound = ctr + D + 2;
   SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, 3 * ((uint64_t)D + 2) * 4, s));
   SST_LAUNCH(k_level_count, blocks_for(n), kTB, 0, s, depth, n, cnt);
-  std::vector<uint32_t> hc(D + 2), ho(D + 2);
+  std::vector<uint32_t> hc(D + 2), ho(D + 2), hib(D + 2);
   SST_CUDA_TRY(cudaMemcpyAsync(hc.data(), cnt, (D + 1) * 4, cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   uint32_t acc = 0;
@@ -870,24 +1009,55 @@ sst_status bc(sst_graph *g, uint32_t src, double *d_dep) {
     acc += hc[d];
   }
   ho[D + 1] = acc;
+  const uint32_t R = acc;  // reached vertices
   SST_CUDA_TRY(cudaMemcpyAsync(off, ho.data(), (D + 2) * 4, cudaMemcpyHostToDevice, s));
   SST_LAUNCH(k_level_scatter, blocks_for(n), kTB, 0, s, depth, n, off, ctr,
              t->lvl_list.p);
+  // chunk items of the big vertices, in level-list order
+  SST_CUDA_TRY(t->icnt.ensure((uint64_t)R + 1));
+  SST_CUDA_TRY(t->ioff.ensure((uint64_t)R + 1));
+  const uint32_t *list = t->lvl_list.p;
+  SST_LAUNCH(k_bc_item_counts, blocks_for(R), kTB, 0, s, list, R, g->d_cap, t->icnt.p);
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes((uint64_t)R + 1, 4) + 4096));
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(t->icnt.p, t->ioff.p, R, 0u, OpAdd{}, true,
+                                      false, t->ioff.p + R, g->arena, s)));
+  SST_LAUNCH(k_gather_bounds, blocks_for(D + 2), kTB, 0, s, t->ioff.p, off,
+             D + 2, ibound);
+  SST_CUDA_TRY(cudaMemcpyAsync(hib.data(), ibound, (D + 2) * 4, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint32_t items = hib[D + 1];
+  SST_CUDA_TRY(t->iv.ensure((uint64_t)items + 1));
+  SST_CUDA_TRY(t->il0.ensure((uint64_t)items + 1));
+  SST_CUDA_TRY(t->partial.ensure((uint64_t)items + 1));
+  if (items)
+    SST_LAUNCH(k_bc_expand, blocks_for(R), kTB, 0, s, list, R, t->icnt.p,
+               t->ioff.p, t->iv.p, t->il0.p);
   SST_LAUNCH(k_bc_init, blocks_for(n), kTB, 0, s, t->sigma.p, t->ratio.p, d_dep, n, src);
   DGraph dg = g->view();
+  double *part = t->partial.p;
   for (uint32_t d = 1; d <= D; d++) {
-    uint32_t c = hc[d];
-    const uint32_t *lst = t->lvl_list.p + ho[d];
+    uint32_t c = hc[d], ni = hib[d + 1] - hib[d];
+    const uint32_t *lst = list + ho[d];
     SST_LAUNCH(k_sigma_small, blocks_for(c), kTB, 0, s, dg, lst, c, depth, t->sigma.p, (int32_t)d);
-    SST_LAUNCH(k_sigma_big, warp_blocks(c), kTB, 0, s, dg, lst, c, depth, t->sigma.p, (int32_t)d);
+    if (ni) {
+      SST_LAUNCH(k_bc_chunks, warp_blocks(ni), kTB, 0, s, dg, t->iv.p, t->il0.p,
+                 hib[d], ni, depth, t->sigma.p, (int32_t)d - 1, part);
+      SST_LAUNCH(k_bc_fix, blocks_for(c), kTB, 0, s, list, ho[d], c, t->icnt.p,
+                 t->ioff.p, part, true, t->sigma.p, t->ratio.p, d_dep);
+    }
   }
   for (int32_t d = (int32_t)D; d >= 0; d--) {
-    uint32_t c = hc[d];
-    const uint32_t *lst = t->lvl_list.p + ho[d];
+    uint32_t c = hc[d], ni = hib[d + 1] - hib[d];
+    const uint32_t *lst = list + ho[d];
     SST_LAUNCH(k_delta_small, blocks_for(c), kTB, 0, s, dg, lst, c, depth,
                t->sigma.p, t->ratio.p, d_dep, d);
-    SST_LAUNCH(k_delta_big, warp_blocks(c), kTB, 0, s, dg, lst, c, depth,
-               t->sigma.p, t->ratio.p, d_dep, d);
+    if (ni) {
+      SST_LAUNCH(k_bc_chunks, warp_blocks(ni), kTB, 0, s, dg, t->iv.p, t->il0.p,
+                 hib[d], ni, depth, t->ratio.p, d + 1, part);
+      SST_LAUNCH(k_bc_fix, blocks_for(c), kTB, 0, s, list, ho[d], c, t->icnt.p,
+                 t->ioff.p, part, false, t->sigma.p, t->ratio.p, d_dep);
+    }
   }
   SST_CUDA_TRY(cudaGetLastError());
   return SST_OK;

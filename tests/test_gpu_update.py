@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 import oracle
+from pma_check import check
 
 pytestmark = pytest.mark.gpu
 
@@ -16,9 +17,12 @@ def sg():
     return sstgraph_gb300
 
 
-def same(g, o):
+def same(g, o, structure=True):
     og, cg = g.csr()
     oo, co = o.csr()
+    if structure and g.rows <= 5000:
+        errs = check(g, (oo, co))
+        assert not errs, errs[:5]
     assert g.M() == o.M()
     assert np.array_equal(og, oo)
     assert np.array_equal(cg, co)
