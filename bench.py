@@ -51,6 +51,8 @@ def args_parse():
     ap.add_argument("--scale", type=int, default=24)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--pr-iters", type=int, default=10)
+    ap.add_argument("--only", default="all", choices=["all", "pagerank", "bfs"],
+                    help="run one traversal on the base graph (profiling cases)")
     return ap.parse_args()
 
 
@@ -254,6 +256,75 @@ def main():
     build_s = time.time() - t0
     m0 = g.M()
 
+    def measure_pagerank():
+        m = g.M()
+        with torch.cuda.stream(stream):
+            out = torch.empty(n, dtype=torch.float64, device="cuda")
+            sg.PR_S(g, 1, out=out)  # warm: work lists
+        torch.cuda.synchronize()
+        prt = {}
+        for it in (a.pr_iters, 2 * a.pr_iters):
+            best = 1e30
+            for _ in range(3):
+                with torch.cuda.stream(stream):
+                    pr_flush.fill_(it)
+                s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s0.record(stream)
+                sg.PR_S(g, it, out=out)
+                s1.record(stream)
+                s1.synchronize()
+                best = min(best, s0.elapsed_time(s1) / 1e3)
+            prt[it] = best
+        t_iter = (prt[2 * a.pr_iters] - prt[a.pr_iters]) / a.pr_iters
+        pr_bytes = 4 * m + 24 * n
+        pr_gbs = pr_bytes / t_iter / 1e9
+        sg.profile_start()
+        sg.PR_S(g, a.pr_iters, out=out)
+        torch.cuda.synchronize()
+        pr_prof = sg.profile_collect()
+        pagerank = {"gteps": m / t_iter / 1e9, "ms_per_iter": t_iter * 1e3,
+                    "algorithmic_bytes_per_iter": pr_bytes,
+                    "roofline": {"bound": "hbm", "achieved": pr_gbs, "peak": hbm_peak,
+                                 "unit": "GB/s", "frac": pr_gbs / hbm_peak,
+                                 "peak_kind": peak_kind, "traffic": None,
+                                 "kernels": "one iteration = k_pr_small + k_pr_chunks + k_pr_fix"},
+                    "kernels": pr_prof}
+        return pagerank
+
+    def measure_bfs():
+        m = g.M()
+        dep = torch.empty(n, dtype=torch.int32, device="cuda")
+        sg.BFS(g, 0, depths=True, out=dep)
+        torch.cuda.synchronize()
+        bt = 1e30
+        for _ in range(3):
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            sg.BFS(g, 0, depths=True, out=dep)
+            s1.record(stream)
+            s1.synchronize()
+            bt = min(bt, s0.elapsed_time(s1) / 1e3)
+        degs = torch.from_numpy(g.degrees().astype(np.int64))
+        reached = (dep.cpu() >= 0)
+        m_r = int(degs[reached].sum())
+        bfs = {"gteps": m_r / bt / 1e9, "ms": bt * 1e3, "reached": int(reached.sum()),
+               "edges_reached": m_r,
+               "roofline": {"bound": "hbm", "achieved": (4 * m_r + 12 * n) / bt / 1e9,
+                            "peak": hbm_peak, "unit": "GB/s",
+                            "frac": (4 * m_r + 12 * n) / bt / 1e9 / hbm_peak}}
+        return bfs
+
+    if a.only != "all":
+        pr_flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
+        res = {"only": a.only, "scale": a.scale, "edges": m0}
+        if a.only == "pagerank":
+            res["pagerank"] = measure_pagerank()
+        else:
+            res["bfs"] = measure_bfs()
+        g.close()
+        print(json.dumps(res))
+        return
+
     # ---- batches (device and pinned host copies)
     plan = batch_plan(a.steps, a.warmup)
     ins_d, rem_d, ins_h, rem_h = [], [], [], []
@@ -273,6 +344,7 @@ def main():
             rem_h.append(r.cpu().pin_memory())
     torch.cuda.synchronize()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
+    pr_flush = flush
 
     def run_steps(lo, hi, host, timed):
         ti = tr = 0.0
@@ -319,59 +391,8 @@ def main():
            "note": "insert+remove via sst_insert_batch/sst_remove_batch on pinned host "
                    "pairs; each call returns the invalid-pair count (8 B) to the host"}
 
-    # ---- pagerank and bfs on the updated graph
-    m = g.M()
-    with torch.cuda.stream(stream):
-        out = torch.empty(n, dtype=torch.float64, device="cuda")
-        sg.PR_S(g, 1, out=out)  # warm: work lists
-    torch.cuda.synchronize()
-    prt = {}
-    for it in (a.pr_iters, 2 * a.pr_iters):
-        best = 1e30
-        for _ in range(3):
-            with torch.cuda.stream(stream):
-                flush.fill_(it)
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            sg.PR_S(g, it, out=out)
-            s1.record(stream)
-            s1.synchronize()
-            best = min(best, s0.elapsed_time(s1) / 1e3)
-        prt[it] = best
-    t_iter = (prt[2 * a.pr_iters] - prt[a.pr_iters]) / a.pr_iters
-    pr_bytes = 4 * m + 24 * n
-    pr_gbs = pr_bytes / t_iter / 1e9
-    sg.profile_start()
-    sg.PR_S(g, a.pr_iters, out=out)
-    torch.cuda.synchronize()
-    pr_prof = sg.profile_collect()
-    pagerank = {"gteps": m / t_iter / 1e9, "ms_per_iter": t_iter * 1e3,
-                "algorithmic_bytes_per_iter": pr_bytes,
-                "roofline": {"bound": "hbm", "achieved": pr_gbs, "peak": hbm_peak,
-                             "unit": "GB/s", "frac": pr_gbs / hbm_peak,
-                             "peak_kind": peak_kind, "traffic": None,
-                             "kernels": "one iteration = k_pr_small + k_pr_chunks + k_pr_fix"},
-                "kernels": pr_prof}
-
-    dep = torch.empty(n, dtype=torch.int32, device="cuda")
-    sg.BFS(g, 0, depths=True, out=dep)
-    torch.cuda.synchronize()
-    bt = 1e30
-    for _ in range(3):
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record(stream)
-        sg.BFS(g, 0, depths=True, out=dep)
-        s1.record(stream)
-        s1.synchronize()
-        bt = min(bt, s0.elapsed_time(s1) / 1e3)
-    degs = torch.from_numpy(g.degrees().astype(np.int64))
-    reached = (dep.cpu() >= 0)
-    m_r = int(degs[reached].sum())
-    bfs = {"gteps": m_r / bt / 1e9, "ms": bt * 1e3, "reached": int(reached.sum()),
-           "edges_reached": m_r,
-           "roofline": {"bound": "hbm", "achieved": (4 * m_r + 12 * n) / bt / 1e9,
-                        "peak": hbm_peak, "unit": "GB/s",
-                        "frac": (4 * m_r + 12 * n) / bt / 1e9 / hbm_peak}}
+    pagerank = measure_pagerank()
+    bfs = measure_bfs()
 
     # ---- roofline of the update step's dominant kernel
     upd_kernels = prof
