@@ -159,39 +159,74 @@ __global__ void k_compact_ids(const uint32_t *__restrict__ flag,
 }
 
 // ------------------------------------------------------------- pagerank
-// Per-edge sums are exact 64-bit fixed-point integer additions: each
-// contribution rank(u)/deg(u) is rounded once to a multiple of 2^-63 and the
-// sums are order-independent.  GB300 runs FP64 at a small fraction of its
-// integer rate, so an FP64 add per edge would bound an iteration by the FP64
-// pipe instead of HBM; per-vertex arithmetic stays in FP64.
-constexpr double kFix = 9223372036854775808.0;  // 2^63
+// An iteration is integer-only fixed point in units of 2^-63: each
+// contribution rank(u)/deg(u) is rounded once to a multiple of 2^-63, the
+// per-edge sums are exact 64-bit integer additions (order-independent, so
+// deterministic), and rank = (1-d)/n + d*sum uses a 64x64->128-bit product
+// rounded to nearest.  GB300 runs FP64 at a small fraction of its integer
+// rate; FP64 appears only when the final ranks are written.
+__device__ __forceinline__ uint64_t mulhi_round(uint64_t a, uint64_t b) {
+  return __umul64hi(a, b) + ((a * b) >> 63);
+}
 
-__global__ void k_pr_inv(const uint32_t *__restrict__ deg, uint32_t n,
-                         double *__restrict__ inv_scaled) {
+// leaf ids are read once per iteration: keep them out of L1 so the
+// contribution gathers keep it
+__device__ __forceinline__ uint32_t ld_stream(const uint32_t *p) {
+  uint32_t v;
+  asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_keep(const unsigned long long *p) {
+  unsigned long long v;
+  asm("ld.global.nc.L1::evict_last.b64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
+
+// per vertex: round(2^64 / deg) for deg >= 2 (deg 1 passes rank through)
+__global__ void k_pr_rdeg(const uint32_t *__restrict__ deg, uint32_t n,
+                          unsigned long long *__restrict__ rdeg) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   uint32_t d = deg[v];
-  inv_scaled[v] = d ? kFix / (double)d : 0.0;
+  unsigned long long r = 0;
+  if (d >= 2) {
+    unsigned __int128 num = ((unsigned __int128)1 << 64) + (d >> 1);
+    r = (unsigned long long)(num / d);
+  }
+  rdeg[v] = r;
+}
+
+__device__ __forceinline__ unsigned long long contrib_of(unsigned long long rank,
+                                                         uint32_t deg,
+                                                         unsigned long long rd) {
+  return deg == 1 ? rank : mulhi_round(rank, rd);
 }
 
 __global__ void k_pr_start(const uint32_t *__restrict__ deg, uint32_t n,
-                           double r0, const double *__restrict__ inv_scaled,
+                           unsigned long long r0,
+                           const unsigned long long *__restrict__ rdeg,
                            unsigned long long *__restrict__ contrib,
                            double *__restrict__ rank, double base) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
-  contrib[v] = __double2ull_rn(r0 * inv_scaled[v]);
-  if (deg[v] == 0) rank[v] = base;  // no in-edges: constant term only
+  uint32_t d = deg[v];
+  contrib[v] = d ? contrib_of(r0, d, rdeg[v]) : 0ull;
+  if (d == 0) rank[v] = base;  // no in-edges: constant term only
 }
 
+struct PrConst {
+  unsigned long long B;  // (1-d)/n in 2^-63 units
+  unsigned long long D;  // d in 2^-64 units
+};
+
 __device__ __forceinline__ void pr_finish(uint32_t v, unsigned long long sum,
-                                          double dscale, double base,
-                                          const double *inv_scaled,
+                                          PrConst k, uint32_t deg,
+                                          const unsigned long long *rdeg,
                                           unsigned long long *cout,
                                           double *rank, bool last) {
-  double r = fma(__ull2double_rn(sum), dscale, base);
-  cout[v] = __double2ull_rn(r * inv_scaled[v]);
-  if (last) rank[v] = r;
+  unsigned long long r = k.B + mulhi_round(sum, k.D);
+  cout[v] = contrib_of(r, deg, rdeg[v]);
+  if (last) rank[v] = __ull2double_rn(r) * (1.0 / 9223372036854775808.0);
 }
 
 // 8 lanes per vertex with a one-leaf segment (cap <= 32): each group of 8
@@ -201,34 +236,35 @@ __global__ void k_pr_small(DGraph g, const uint32_t *__restrict__ small,
                            const unsigned long long *__restrict__ cin,
                            unsigned long long *__restrict__ cout,
                            double *__restrict__ rank,
-                           const double *__restrict__ inv_scaled, double base,
-                           double dscale, bool last) {
+                           const unsigned long long *__restrict__ rdeg,
+                           PrConst k, bool last) {
   uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint64_t i = t >> 3;
   const uint32_t sub = threadIdx.x & 7;
   unsigned long long acc = 0;
-  uint32_t v = 0;
+  uint32_t v = 0, d = 0;
   if (i < nsmall) {
     v = small[i];
-    uint32_t d = g.deg[v];
+    d = g.deg[v];
     const uint32_t *p = g.slots + g.base[v];
-    for (uint32_t j = sub; j < d; j += 8) acc += cin[p[j]];
+    for (uint32_t j = sub; j < d; j += 8) acc += ld_keep(cin + ld_stream(p + j));
   }
   acc += __shfl_xor_sync(0xffffffffu, acc, 4);
   acc += __shfl_xor_sync(0xffffffffu, acc, 2);
   acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-  if (i < nsmall && sub == 0) pr_finish(v, acc, dscale, base, inv_scaled, cout, rank, last);
+  if (i < nsmall && sub == 0) pr_finish(v, acc, k, d, rdeg, cout, rank, last);
 }
 
-// warp per chunk of <= 32 leaves of a multi-leaf segment
+// warp per chunk of <= 32 leaves of a multi-leaf segment; four leaves in
+// flight per step
 __global__ void k_pr_chunks(DGraph g, const uint32_t *__restrict__ cv,
                             const uint32_t *__restrict__ cl0, uint64_t nchunks,
                             const unsigned long long *__restrict__ cin,
                             unsigned long long *__restrict__ cout,
                             double *__restrict__ rank,
-                            const double *__restrict__ inv_scaled,
-                            unsigned long long *__restrict__ partial,
-                            double base, double dscale, bool last) {
+                            const unsigned long long *__restrict__ rdeg,
+                            unsigned long long *__restrict__ partial, PrConst k,
+                            bool last) {
   uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= nchunks) return;
@@ -237,35 +273,46 @@ __global__ void k_pr_chunks(DGraph g, const uint32_t *__restrict__ cv,
   uint32_t l0 = cl0[c], l1 = min(l0 + kChunkLeaves, nl);
   uint64_t sb = g.base[v];
   const uint8_t *lc = g.lcnt + (sb >> kLeafLog);
-  const uint32_t *sl = g.slots + sb;
+  const uint32_t *sl = g.slots + sb + lane;
   unsigned long long acc = 0;
-  for (uint32_t l = l0; l < l1; l++) {
-    uint32_t cnt = lc[l];
-    if ((uint32_t)lane < cnt) acc += cin[sl[((uint64_t)l << kLeafLog) + lane]];
+  uint32_t l = l0;
+  for (; l + 4 <= l1; l += 4) {
+    uint32_t c0 = lc[l], c1 = lc[l + 1], c2 = lc[l + 2], c3 = lc[l + 3];
+    uint32_t x0 = (uint32_t)lane < c0 ? ld_stream(sl + ((uint64_t)l << kLeafLog)) : kEmpty;
+    uint32_t x1 = (uint32_t)lane < c1 ? ld_stream(sl + ((uint64_t)(l + 1) << kLeafLog)) : kEmpty;
+    uint32_t x2 = (uint32_t)lane < c2 ? ld_stream(sl + ((uint64_t)(l + 2) << kLeafLog)) : kEmpty;
+    uint32_t x3 = (uint32_t)lane < c3 ? ld_stream(sl + ((uint64_t)(l + 3) << kLeafLog)) : kEmpty;
+    if (x0 != kEmpty) acc += ld_keep(cin + x0);
+    if (x1 != kEmpty) acc += ld_keep(cin + x1);
+    if (x2 != kEmpty) acc += ld_keep(cin + x2);
+    if (x3 != kEmpty) acc += ld_keep(cin + x3);
+  }
+  for (; l < l1; l++) {
+    if ((uint32_t)lane < lc[l]) acc += ld_keep(cin + ld_stream(sl + ((uint64_t)l << kLeafLog)));
   }
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
   if (lane == 0) {
     if (nl <= kChunkLeaves)
-      pr_finish(v, acc, dscale, base, inv_scaled, cout, rank, last);
+      pr_finish(v, acc, k, g.deg[v], rdeg, cout, rank, last);
     else
       partial[c] = acc;
   }
 }
 
-__global__ void k_pr_fix(const uint32_t *__restrict__ multi, uint64_t nmulti,
-                         const uint64_t *__restrict__ choff,
+__global__ void k_pr_fix(DGraph g, const uint32_t *__restrict__ multi,
+                         uint64_t nmulti, const uint64_t *__restrict__ choff,
                          const unsigned long long *__restrict__ partial,
                          unsigned long long *__restrict__ cout,
                          double *__restrict__ rank,
-                         const double *__restrict__ inv_scaled, double base,
-                         double dscale, bool last) {
+                         const unsigned long long *__restrict__ rdeg, PrConst k,
+                         bool last) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nmulti) return;
   uint32_t v = multi[i];
   unsigned long long s = 0;
   for (uint64_t c = choff[v]; c < choff[v + 1]; c++) s += partial[c];
-  pr_finish(v, s, dscale, base, inv_scaled, cout, rank, last);
+  pr_finish(v, s, k, g.deg[v], rdeg, cout, rank, last);
 }
 
 __global__ void k_fill_d(double *__restrict__ p, uint32_t n, double x) {
@@ -845,10 +892,19 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   SST_CUDA_TRY(t->ca.ensure(n));
   SST_CUDA_TRY(t->cb.ensure(n));
   SST_CUDA_TRY(t->partial.ensure(t->nchunks + 1));
+  unsigned long long *rdeg = reinterpret_cast<unsigned long long *>(t->inv_deg.p);
   if (t->inv_version != g->version) {
     SST_CUDA_TRY(t->inv_deg.ensure(n));
-    SST_LAUNCH(k_pr_inv, blocks_for(n), kTB, 0, s, g->d_deg, n, t->inv_deg.p);
+    rdeg = reinterpret_cast<unsigned long long *>(t->inv_deg.p);
+    SST_LAUNCH(k_pr_rdeg, blocks_for(n), kTB, 0, s, g->d_deg, n, rdeg);
     t->inv_version = g->version;
+  }
+  static bool carveout = false;
+  if (!carveout) {
+    // these kernels use no shared memory: give the SM's storage to L1
+    cudaFuncSetAttribute(k_pr_small, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaFuncSetAttribute(k_pr_chunks, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    carveout = true;
   }
   double r0 = 1.0 / (double)n;
   double base = (1.0 - damping) / (double)n;
@@ -857,26 +913,28 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
     SST_CUDA_TRY(cudaGetLastError());
     return SST_OK;
   }
+  const double two63 = 9223372036854775808.0, two64 = 18446744073709551616.0;
+  PrConst K;
+  K.B = (unsigned long long)llrint(base * two63);
+  K.D = damping >= 1.0 ? ~0ull : (unsigned long long)llrint(damping * two64 / 2.0) * 2ull;
+  unsigned long long r0f = (unsigned long long)llrint(r0 * two63);
   unsigned long long *cin = reinterpret_cast<unsigned long long *>(t->ca.p);
   unsigned long long *cout = reinterpret_cast<unsigned long long *>(t->cb.p);
   unsigned long long *part = reinterpret_cast<unsigned long long *>(t->partial.p);
-  SST_LAUNCH(k_pr_start, blocks_for(n), kTB, 0, s, g->d_deg, n, r0, t->inv_deg.p,
-             cin, d_rank, base);
+  SST_LAUNCH(k_pr_start, blocks_for(n), kTB, 0, s, g->d_deg, n, r0f, rdeg, cin,
+             d_rank, base);
   DGraph dg = g->view();
-  const double dscale = damping / kFix;
   for (uint32_t it = 0; it < iters; it++) {
     bool last = it + 1 == iters;
     if (t->nsmall)
       SST_LAUNCH(k_pr_small, blocks_for(t->nsmall * 8), kTB, 0, s, dg, t->small.p,
-                 t->nsmall, cin, cout, d_rank, t->inv_deg.p, base, dscale, last);
+                 t->nsmall, cin, cout, d_rank, rdeg, K, last);
     if (t->nchunks)
       SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cv.p,
-                 t->cl0.p, t->nchunks, cin, cout, d_rank, t->inv_deg.p, part,
-                 base, dscale, last);
+                 t->cl0.p, t->nchunks, cin, cout, d_rank, rdeg, part, K, last);
     if (t->nmulti)
-      SST_LAUNCH(k_pr_fix, blocks_for(t->nmulti), kTB, 0, s, t->multi.p,
-                 t->nmulti, t->choff.p, part, cout, d_rank, t->inv_deg.p, base,
-                 dscale, last);
+      SST_LAUNCH(k_pr_fix, blocks_for(t->nmulti), kTB, 0, s, dg, t->multi.p,
+                 t->nmulti, t->choff.p, part, cout, d_rank, rdeg, K, last);
     std::swap(cin, cout);
   }
   SST_CUDA_TRY(cudaGetLastError());
