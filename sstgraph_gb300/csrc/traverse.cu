@@ -60,6 +60,7 @@ struct TravState {
   uint64_t inv_version = ~0ull;
   DevBuf<uint64_t> choff;   // per vertex: first chunk (n+1)
   DevBuf<uint32_t> cv, cl0; // per chunk: vertex, first leaf
+  DevBuf<unsigned long long> cdesc, sdesc;  // packed chunk / one-leaf items
   DevBuf<uint32_t> multi;   // vertices with more than one chunk
   DevBuf<uint32_t> big;     // vertices with a multi-leaf segment
   DevBuf<uint32_t> small;   // vertices with a one-leaf segment (deg >= 1)
@@ -87,6 +88,8 @@ void trav_release(sst_graph *g) {
   t->choff.release();
   t->cv.release();
   t->cl0.release();
+  t->cdesc.release();
+  t->sdesc.release();
   t->multi.release();
   t->big.release();
   t->small.release();
@@ -138,17 +141,34 @@ __global__ void k_chunk_counts(const uint32_t *__restrict__ cap, uint32_t n,
   smallf[v] = c > 0 && c <= kLeaf;
 }
 
-__global__ void k_chunk_fill(const uint32_t *__restrict__ cap, uint32_t n,
+__global__ void k_chunk_fill(const uint32_t *__restrict__ cap,
+                             const uint64_t *__restrict__ base, uint32_t n,
                              const uint64_t *__restrict__ choff,
                              uint32_t *__restrict__ cv,
-                             uint32_t *__restrict__ cl0) {
+                             uint32_t *__restrict__ cl0,
+                             unsigned long long *__restrict__ cdesc) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   uint64_t c0 = choff[v], c1 = choff[v + 1];
+  uint32_t nl = cap[v] >> kLeafLog;
+  uint64_t leaf = base[v] >> kLeafLog;
+  unsigned long long single = (c1 - c0) == 1 ? 128ull : 0ull;
   for (uint64_t c = c0; c < c1; c++) {
+    uint32_t l0 = (uint32_t)((c - c0) * kChunkLeaves);
     cv[c] = v;
-    cl0[c] = (uint32_t)((c - c0) * kChunkLeaves);
+    cl0[c] = l0;
+    cdesc[c] = ((leaf + l0) << 8) | single | (unsigned long long)min(kChunkLeaves, nl - l0);
   }
+}
+
+__global__ void k_small_desc(const uint32_t *__restrict__ small, uint64_t nsmall,
+                             const uint64_t *__restrict__ base,
+                             const uint32_t *__restrict__ deg,
+                             unsigned long long *__restrict__ sdesc) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsmall) return;
+  uint32_t v = small[i];
+  sdesc[i] = ((unsigned long long)base[v] << 6) | deg[v];
 }
 
 __global__ void k_compact_ids(const uint32_t *__restrict__ flag,
@@ -229,36 +249,65 @@ __device__ __forceinline__ void pr_finish(uint32_t v, unsigned long long sum,
   if (last) rank[v] = __ull2double_rn(r) * (1.0 / 9223372036854775808.0);
 }
 
-// 8 lanes per vertex with a one-leaf segment (cap <= 32): each group of 8
-// lanes reads one 32-byte sector of the leaf per step
-__global__ void k_pr_small(DGraph g, const uint32_t *__restrict__ small,
-                           uint64_t nsmall,
+// One-leaf segments (cap <= 32): a group of 8 lanes per vertex (one 32-byte
+// sector of the leaf per lane step), four vertices per group in flight.
+// sdesc[i] = (segment base << 6) | degree.
+constexpr int kSmallPer = 4;
+
+__global__ void k_pr_small(DGraph g, const unsigned long long *__restrict__ sdesc,
+                           const uint32_t *__restrict__ small, uint64_t nsmall,
                            const unsigned long long *__restrict__ cin,
                            unsigned long long *__restrict__ cout,
                            double *__restrict__ rank,
                            const unsigned long long *__restrict__ rdeg,
                            PrConst k, bool last) {
-  uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t i = t >> 3;
+  uint64_t grp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
   const uint32_t sub = threadIdx.x & 7;
-  unsigned long long acc = 0;
-  uint32_t v = 0, d = 0;
-  if (i < nsmall) {
-    v = small[i];
-    d = g.deg[v];
-    const uint32_t *p = g.slots + g.base[v];
-    for (uint32_t j = sub; j < d; j += 8) acc += ld_keep(cin + ld_stream(p + j));
+  const uint64_t i0 = grp * kSmallPer;
+  uint32_t x[kSmallPer][4];
+  uint32_t dg[kSmallPer];
+#pragma unroll
+  for (int u = 0; u < kSmallPer; u++) {
+    uint64_t i = i0 + u;
+    unsigned long long dsc = i < nsmall ? sdesc[i] : 0ull;
+    dg[u] = (uint32_t)(dsc & 63);
+    const uint32_t *p = g.slots + (dsc >> 6);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      uint32_t j = sub + 8 * q;
+      x[u][q] = j < dg[u] ? ld_stream(p + j) : kEmpty;
+    }
   }
-  acc += __shfl_xor_sync(0xffffffffu, acc, 4);
-  acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-  acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-  if (i < nsmall && sub == 0) pr_finish(v, acc, k, d, rdeg, cout, rank, last);
+  unsigned long long acc[kSmallPer];
+#pragma unroll
+  for (int u = 0; u < kSmallPer; u++) {
+    acc[u] = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (x[u][q] != kEmpty) acc[u] += ld_keep(cin + x[u][q]);
+  }
+  unsigned long long mine = 0;
+  uint32_t mydeg = 0;
+#pragma unroll
+  for (int u = 0; u < kSmallPer; u++) {
+    unsigned long long a = acc[u];
+    a += __shfl_xor_sync(0xffffffffu, a, 4);
+    a += __shfl_xor_sync(0xffffffffu, a, 2);
+    a += __shfl_xor_sync(0xffffffffu, a, 1);
+    if (sub == (uint32_t)u) {
+      mine = a;
+      mydeg = dg[u];
+    }
+  }
+  if (sub < (uint32_t)kSmallPer && i0 + sub < nsmall)
+    pr_finish(small[i0 + sub], mine, k, mydeg, rdeg, cout, rank, last);
 }
 
 // warp per chunk of <= 32 leaves of a multi-leaf segment; four leaves in
-// flight per step
-__global__ void k_pr_chunks(DGraph g, const uint32_t *__restrict__ cv,
-                            const uint32_t *__restrict__ cl0, uint64_t nchunks,
+// flight per step.  cdesc[c] = (first leaf << 8) | (single chunk << 7) |
+// leaves in the chunk.
+__global__ void k_pr_chunks(DGraph g, const unsigned long long *__restrict__ cdesc,
+                            const uint32_t *__restrict__ cv, uint64_t nchunks,
                             const unsigned long long *__restrict__ cin,
                             unsigned long long *__restrict__ cout,
                             double *__restrict__ rank,
@@ -268,14 +317,14 @@ __global__ void k_pr_chunks(DGraph g, const uint32_t *__restrict__ cv,
   uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= nchunks) return;
-  uint32_t v = cv[c];
-  uint32_t nl = g.cap[v] >> kLeafLog;
-  uint32_t l0 = cl0[c], l1 = min(l0 + kChunkLeaves, nl);
-  uint64_t sb = g.base[v];
-  const uint8_t *lc = g.lcnt + (sb >> kLeafLog);
-  const uint32_t *sl = g.slots + sb + lane;
+  unsigned long long dsc = cdesc[c];
+  const uint64_t leaf0 = dsc >> 8;
+  const uint32_t l1 = (uint32_t)(dsc & 63);
+  const bool single = (dsc >> 7) & 1;
+  const uint8_t *lc = g.lcnt + leaf0;
+  const uint32_t *sl = g.slots + (leaf0 << kLeafLog) + lane;
   unsigned long long acc = 0;
-  uint32_t l = l0;
+  uint32_t l = 0;
   for (; l + 4 <= l1; l += 4) {
     uint32_t c0 = lc[l], c1 = lc[l + 1], c2 = lc[l + 2], c3 = lc[l + 3];
     uint32_t x0 = (uint32_t)lane < c0 ? ld_stream(sl + ((uint64_t)l << kLeafLog)) : kEmpty;
@@ -293,10 +342,12 @@ __global__ void k_pr_chunks(DGraph g, const uint32_t *__restrict__ cv,
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
   if (lane == 0) {
-    if (nl <= kChunkLeaves)
+    if (single) {
+      uint32_t v = cv[c];
       pr_finish(v, acc, k, g.deg[v], rdeg, cout, rank, last);
-    else
+    } else {
       partial[c] = acc;
+    }
   }
 }
 
@@ -869,12 +920,17 @@ static sst_status ensure_lists(sst_graph *g) {
   SST_CUDA_TRY(t->big.ensure(t->nbig + 1));
   SST_CUDA_TRY(t->multi.ensure(t->nmulti + 1));
   SST_CUDA_TRY(t->small.ensure(t->nsmall + 1));
+  SST_CUDA_TRY(t->cdesc.ensure(t->nchunks + 1));
+  SST_CUDA_TRY(t->sdesc.ensure(t->nsmall + 1));
   if (n) {
-    SST_LAUNCH(k_chunk_fill, blocks_for(n), kTB, 0, s, g->d_cap, n, t->choff.p,
-               t->cv.p, t->cl0.p);
+    SST_LAUNCH(k_chunk_fill, blocks_for(n), kTB, 0, s, g->d_cap, g->d_base, n,
+               t->choff.p, t->cv.p, t->cl0.p, t->cdesc.p);
     SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, bigf, bigp, n, t->big.p);
     SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, multif, multip, n, t->multi.p);
     SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, smallf, smallp, n, t->small.p);
+    if (t->nsmall)
+      SST_LAUNCH(k_small_desc, blocks_for(t->nsmall), kTB, 0, s, t->small.p,
+                 t->nsmall, g->d_base, g->d_deg, t->sdesc.p);
   }
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   SST_CUDA_TRY(cudaGetLastError());
@@ -927,11 +983,13 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   for (uint32_t it = 0; it < iters; it++) {
     bool last = it + 1 == iters;
     if (t->nsmall)
-      SST_LAUNCH(k_pr_small, blocks_for(t->nsmall * 8), kTB, 0, s, dg, t->small.p,
-                 t->nsmall, cin, cout, d_rank, rdeg, K, last);
+      SST_LAUNCH(k_pr_small,
+                 blocks_for((t->nsmall + kSmallPer - 1) / kSmallPer * 8), kTB, 0,
+                 s, dg, t->sdesc.p, t->small.p, t->nsmall, cin, cout, d_rank,
+                 rdeg, K, last);
     if (t->nchunks)
-      SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cv.p,
-                 t->cl0.p, t->nchunks, cin, cout, d_rank, rdeg, part, K, last);
+      SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cdesc.p,
+                 t->cv.p, t->nchunks, cin, cout, d_rank, rdeg, part, K, last);
     if (t->nmulti)
       SST_LAUNCH(k_pr_fix, blocks_for(t->nmulti), kTB, 0, s, dg, t->multi.p,
                  t->nmulti, t->choff.p, part, cout, d_rank, rdeg, K, last);
