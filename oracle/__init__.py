@@ -57,6 +57,7 @@ def lib():
             "sst_o_er": (None, [u32, u64, u64, u64, vp]),
             "sst_o_ref_rmat_stream": (None, [u32, dbl, dbl, dbl, u64, u64, vp]),
             "sst_o_new": (vp, [u32]),
+            "sst_o_new2": (vp, [u32, u32]),
             "sst_o_free": (None, [vp]),
             "sst_o_insert_batch": (None, [vp, vp, u64]),
             "sst_o_remove_batch": (None, [vp, vp, u64]),
@@ -115,9 +116,10 @@ def symmetrize(edges) -> np.ndarray:
 class OracleGraph:
     """Restated SparseMatrixV<true>: per-row sorted sets of uint32 columns."""
 
-    def __init__(self, n: int):
+    def __init__(self, n: int, width: int | None = None):
         self.n = int(n)
-        self._h = lib().sst_o_new(self.n)
+        self.width = self.n if width is None else int(width)
+        self._h = lib().sst_o_new2(self.n, self.width)
 
     def __del__(self):
         h = getattr(self, "_h", None)

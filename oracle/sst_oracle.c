@@ -152,14 +152,16 @@ void sst_o_ref_rmat_stream(uint32_t nn, double a, double b, double c,
 
 struct sst_o_graph {
   uint32_t n;
+  uint32_t width; /* column ids are < width (SparseMatrixV(height, width)) */
   uint32_t *deg;
   uint32_t *cap;
   uint32_t **adj;
 };
 
-sst_o_graph *sst_o_new(uint32_t n) {
+sst_o_graph *sst_o_new2(uint32_t n, uint32_t width) {
   sst_o_graph *g = (sst_o_graph *)calloc(1, sizeof(sst_o_graph));
   g->n = n;
+  g->width = width;
   g->deg = (uint32_t *)calloc(n ? n : 1, sizeof(uint32_t));
   g->cap = (uint32_t *)calloc(n ? n : 1, sizeof(uint32_t));
   g->adj = (uint32_t **)calloc(n ? n : 1, sizeof(uint32_t *));
@@ -239,7 +241,7 @@ static uint64_t prepare_batch(const sst_o_graph *g, const uint32_t *pairs,
   uint64_t k = 0;
   for (uint64_t i = 0; i < b; i++) {
     uint32_t r = pairs[2 * i], c = pairs[2 * i + 1];
-    if (r >= g->n || c >= g->n) continue;
+    if (r >= g->n || c >= g->width) continue;
     if (drop_loops && r == c) continue;
     keys[k++] = ((uint64_t)r << 32) | c;
   }
@@ -612,3 +614,5 @@ uint64_t sst_o_tc(const sst_o_graph *g, uint64_t *per_vertex) {
   }
   return total;
 }
+
+sst_o_graph *sst_o_new(uint32_t n) { return sst_o_new2(n, n); }

@@ -57,6 +57,8 @@ void sst_o_ref_rmat_stream(uint32_t nn, double a, double b, double c,
 
 /* ---- graph ---- */
 sst_o_graph *sst_o_new(uint32_t n);
+/* height rows, column ids below width */
+sst_o_graph *sst_o_new2(uint32_t height, uint32_t width);
 void sst_o_free(sst_o_graph *g);
 uint32_t sst_o_num_nodes(const sst_o_graph *g);
 void sst_o_insert_batch(sst_o_graph *g, const uint32_t *pairs, uint64_t b);

@@ -1,0 +1,132 @@
+"""Generate the golden fixtures in this directory from the reference's own
+code (oracle/_ref/libsstref.so: SparseMatrixV<true>, TinySetV, rMat,
+create_random_data and the .mtx loader compiled from the reference headers).
+
+Run in a checkout that has the reference tree (the reference is not shipped
+with this repository):
+
+    python -c "import oracle; oracle.build(ref=True)"
+    python tests/golden/make_golden.py [path/to/reference]
+
+Fixtures (all small, npz):
+  ref_rmat_stream.npz   rMat(2^15, hash64(0), .5, .1, .1) edges 0..19999
+                        (internal/rmat_util.h:82-131, internal/test.hpp:645-654)
+  known_answer.npz      create_random_data(10000, max, seed 0) for the four
+                        key widths of PMA_test.cpp:15-84, the sorted set a
+                        TinySetV holds after inserting them, and after
+                        removing the first half
+  rmat16_stream.npz     scale-16 RMAT base graph (16 edges/vertex, seed 1,
+                        symmetrised) built with SparseMatrixV::insert_batch,
+                        then 10 insert batches of 1e4 RMAT edges (seed 2) and
+                        5 remove batches of sampled edges: degrees and a
+                        sha256 of the CSR after every batch, touch_all_sum,
+                        common_neighbors on sampled pairs, has() on queries
+  examples_mtx.npz      examples/*.mtx through the reference loader
+                        (helpers.hpp:379-529): symmetrised edge lists and the
+                        CSR of the graph built from them
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+
+
+def csr_digest(off, cols):
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(off, np.uint64).tobytes())
+    h.update(np.ascontiguousarray(cols, np.uint32).tobytes())
+    return h.hexdigest()
+
+
+def main(ref_root):
+    R = oracle.ref()
+    # --- reference batch stream
+    out = np.empty((20000, 2), np.uint32)
+    R.ref_rmat_stream(1 << 15, 0.5, 0.1, 0.1, 20000, oracle._ptr(out))
+    np.savez_compressed(os.path.join(HERE, "ref_rmat_stream.npz"), nn=1 << 15, pairs=out)
+
+    # --- known-answer sets (PMA_test.cpp:15-84 inputs)
+    ka = {}
+    for b in (1, 2, 3, 4):
+        mx = 0xFFFFFFFF if b == 4 else (1 << (8 * b))
+        n = min(mx - 1, 10000)
+        vals = oracle.ref_random_data(n, mx, 0)
+        s = R.ref_set_new(0xFFFFFFFE)
+        for v in vals.tolist():
+            R.ref_set_insert(s, v)
+        full = np.empty(int(R.ref_set_n(s)), np.uint32)
+        R.ref_set_to_array(s, oracle._ptr(full))
+        for v in vals[: n // 2].tolist():
+            R.ref_set_remove(s, v)
+        half = np.empty(int(R.ref_set_n(s)), np.uint32)
+        R.ref_set_to_array(s, oracle._ptr(half))
+        R.ref_set_free(s)
+        ka[f"in_{b}"] = vals
+        ka[f"full_{b}"] = full
+        ka[f"half_{b}"] = half
+    np.savez_compressed(os.path.join(HERE, "known_answer.npz"), **ka)
+
+    # --- scale-16 RMAT stream through SparseMatrixV
+    scale, n = 16, 1 << 16
+    base = oracle.symmetrize(oracle.rmat(scale, 16 * n, seed=1))
+    g = oracle.RefGraph(n)
+    g.insert_batch(base)
+    digests, ms, degs = [], [], []
+
+    def snap():
+        off, cols = g.csr()
+        digests.append(csr_digest(off, cols))
+        ms.append(g.M())
+        degs.append(np.diff(off).astype(np.uint32))
+        return off, cols
+
+    snap()
+    for i in range(10):
+        g.insert_batch(oracle.rmat(scale, 10000, seed=2, first=i * 10000))
+        snap()
+    o = oracle.OracleGraph(n)  # only to draw existing edges to remove
+    o.insert_batch(base)
+    for i in range(10):
+        o.insert_batch(oracle.rmat(scale, 10000, seed=2, first=i * 10000))
+    for i in range(5):
+        rem = o.sample_edges(20000, seed=3, first=i * 20000)
+        g.remove_batch(rem)
+        o.remove_batch(rem)
+        snap()
+    off, cols = g.csr()
+    pairs = oracle.rmat(scale, 4000, seed=9)
+    cn_full = np.array([g.common_neighbors(int(a), int(b), False) for a, b in pairs], np.uint64)
+    cn_early = np.array([g.common_neighbors(int(a), int(b), True) for a, b in pairs], np.uint64)
+    q = np.concatenate([o.sample_edges(3000, seed=10), oracle.rmat(scale, 3000, seed=11)])
+    has = np.array([g.has(int(a), int(b)) for a, b in q], np.uint8)
+    np.savez_compressed(
+        os.path.join(HERE, "rmat16_stream.npz"), scale=scale, digests=np.array(digests),
+        M=np.array(ms, np.uint64), deg_final=degs[-1], deg_base=degs[0],
+        touch_all_sum=np.uint64(g.touch_all_sum()), cn_pairs=pairs, cn_full=cn_full,
+        cn_early=cn_early, has_q=q, has_ans=has)
+
+    # --- bundled examples through the reference loader
+    ex = {}
+    for name in ("star", "johnson8-2-4"):
+        rows, edges = oracle.ref_load_mtx(os.path.join(ref_root, "examples", name + ".mtx"))
+        eg = oracle.RefGraph(rows)
+        eg.insert_batch(edges)
+        off, cols = eg.csr()
+        key = name.replace("-", "_")
+        ex[f"{key}_rows"] = np.uint32(rows)
+        ex[f"{key}_edges"] = edges
+        ex[f"{key}_off"] = off
+        ex[f"{key}_cols"] = cols
+    np.savez_compressed(os.path.join(HERE, "examples_mtx.npz"), **ex)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
