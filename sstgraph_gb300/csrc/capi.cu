@@ -210,8 +210,7 @@ sst_status sst_set_stream(sst_graph *g, void *stream) {
 
 sst_status sst_sync(sst_graph *g) {
   CHECK_G(g);
-  SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
-  return SST_OK;
+  return sst::sync_checked(g);
 }
 
 static sst_status do_update(sst_graph *g, const uint32_t *pairs, uint64_t n,
@@ -227,8 +226,7 @@ static sst_status do_update(sst_graph *g, const uint32_t *pairs, uint64_t n,
   st = stage_in(g, pairs, 2 * n, flags, &d);
   if (st != SST_OK) return st;
   st = sst::update_batch(g, d, n, insert, n_invalid);
-  if (st == SST_OK && !is_dev(flags))
-    SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
+  if (st == SST_OK && !is_dev(flags)) st = sst::sync_checked(g);
   return st;
 }
 

@@ -182,72 +182,42 @@ __global__ void k_group_start(const uint32_t *__restrict__ gflag,
 }
 
 // ---------------------------------------------------------------- step 6
-// insert: warp per group
-__global__ void k_classify_insert(DGraph g, PmaParams p,
-                                  const uint64_t *__restrict__ p_ul,
+// Group-level kernels run grid-stride over the device-side group count, so
+// their grids do not scale with the batch bound.  Classification is one
+// thread per group; the rare groups whose leaf over- or underflows are
+// appended to a climb list and climbed by one warp each.
+#define GRID_STRIDE(i, n)                                                     \
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); \
+       i += (uint64_t)gridDim.x * blockDim.x)
+
+__global__ void k_classify_insert(DGraph g, const uint64_t *__restrict__ p_ul,
                                   const uint32_t *__restrict__ g_start,
                                   const uint32_t *__restrict__ d_ngroups,
-                                  const uint32_t *__restrict__ d_nitems,
                                   uint8_t *__restrict__ gtype,
                                   uint8_t *__restrict__ glev,
                                   uint32_t *__restrict__ gw0,
-                                  uint32_t *__restrict__ gw1) {
-  uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (gid >= *d_ngroups) return;
-  const uint32_t nitems = *d_nitems;
-  uint32_t j0 = g_start[gid], j1 = g_start[gid + 1];
-  uint32_t k = j1 - j0;
-  uint64_t key = p_ul[j0];
-  uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
-  uint64_t base = g.base[u];
-  uint32_t cap = g.cap[u], deg = g.deg[u];
-  uint8_t type;
-  uint32_t lev = 0, w0 = leaf, w1 = leaf + 1;
-  if (cap <= kLeaf) {
-    if (deg + k <= cap) {
-      type = kMerge;
-    } else {
-      type = kResize;
-      lev = 31;
-      w0 = 0;
-      w1 = 1;
-    }
-  } else {
-    uint64_t lbase = base >> kLeafLog;
-    uint32_t c = g.lcnt[lbase + leaf];
-    if (c + k <= kLeaf) {
-      type = kMerge;
-    } else {
-      uint32_t H = log2_floor(cap >> kLeafLog);
-      uint64_t old = c;
-      uint32_t size = 1;
-      type = kResize;
-      for (uint32_t t = 1; t <= H; t++) {
-        uint32_t nw0 = (leaf >> t) << t;
-        if (nw0 == w0)
-          old += warp_sum_lcnt(g.lcnt, lbase + w0 + size, lbase + w0 + 2 * size);
-        else
-          old += warp_sum_lcnt(g.lcnt, lbase + nw0, lbase + w0);
-        w0 = nw0;
-        size <<= 1;
-        w1 = w0 + size;
-        uint64_t kk = (uint64_t)u << 32;
-        uint32_t newc = lb_u64(p_ul, nitems, kk | w1) - lb_u64(p_ul, nitems, kk | w0);
-        if (old + newc <= window_upper(p, t, H)) {
-          type = kWindow;
-          lev = t;
-          break;
-        }
-      }
-      if (type == kResize) {
+                                  uint32_t *__restrict__ gw1,
+                                  uint32_t *__restrict__ climb,
+                                  uint32_t *__restrict__ nclimb) {
+  const uint32_t ng = *d_ngroups;
+  GRID_STRIDE(gid, ng) {
+    uint32_t j0 = g_start[gid], k = g_start[gid + 1] - j0;
+    uint64_t key = p_ul[j0];
+    uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
+    uint32_t cap = g.cap[u];
+    uint8_t type = kMerge;
+    uint32_t lev = 0, w0 = leaf, w1 = leaf + 1;
+    if (cap <= kLeaf) {
+      if (g.deg[u] + k > cap) {
+        type = kResize;
         lev = 31;
         w0 = 0;
-        w1 = cap >> kLeafLog;
+        w1 = 1;
       }
+    } else if (g.lcnt[(g.base[u] >> kLeafLog) + leaf] + k > kLeaf) {
+      type = kNone;  // decided by the climb
+      climb[atomicAdd(nclimb, 1u)] = (uint32_t)gid;
     }
-  }
-  if (lane == 0) {
     gtype[gid] = type;
     glev[gid] = (uint8_t)lev;
     gw0[gid] = w0;
@@ -261,35 +231,39 @@ __global__ void k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
                               const uint32_t *__restrict__ p_x,
                               const uint32_t *__restrict__ g_start,
                               const uint32_t *__restrict__ d_ngroups) {
-  uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (gid >= *d_ngroups) return;
-  uint32_t j0 = g_start[gid], j1 = g_start[gid + 1];
-  uint32_t k = j1 - j0;
-  uint64_t key = p_ul[j0];
-  uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
-  uint64_t base = g.base[u];
-  uint32_t cap = g.cap[u], deg = g.deg[u];
-  uint32_t c = leaf_count(g, base, cap, deg, leaf);
-  uint64_t S = base + ((uint64_t)leaf << kLeafLog);
-  uint32_t a = lane < c ? g.slots[S + lane] : kEmpty;
-  uint32_t d = lane < k ? p_x[j0 + lane] : kEmpty;
-  bool del = false;
-  for (uint32_t j = 0; j < k; j++) del |= (__shfl_sync(0xffffffffu, d, j) == a);
-  bool keep = lane < c && !del;
-  uint32_t mask = __ballot_sync(0xffffffffu, keep);
-  uint32_t pos = __popc(mask & ((1u << lane) - 1u));
-  __syncwarp();
-  if (keep) g.slots[S + pos] = a;
-  if (lane >= c - k && lane < c) g.slots[S + lane] = kEmpty;
-  if (lane == 0) {
-    if (cap > kLeaf) g.lcnt[(base >> kLeafLog) + leaf] = (uint8_t)(c - k);
-    atomicSub(&g.deg[u], k);
+  const uint32_t ng = *d_ngroups;
+  for (uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       gid < ng; gid += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+    uint32_t j0 = g_start[gid], j1 = g_start[gid + 1];
+    uint32_t k = j1 - j0;
+    uint64_t key = p_ul[j0];
+    uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
+    uint64_t base = g.base[u];
+    uint32_t cap = g.cap[u], deg = g.deg[u];
+    uint32_t c = leaf_count(g, base, cap, deg, leaf);
+    uint64_t S = base + ((uint64_t)leaf << kLeafLog);
+    uint32_t a = lane < c ? g.slots[S + lane] : kEmpty;
+    uint32_t d = lane < k ? p_x[j0 + lane] : kEmpty;
+    bool del = false;
+    for (uint32_t j = 0; j < k; j++) del |= (__shfl_sync(0xffffffffu, d, j) == a);
+    bool keep = lane < c && !del;
+    uint32_t mask = __ballot_sync(0xffffffffu, keep);
+    uint32_t pos = __popc(mask & ((1u << lane) - 1u));
+    __syncwarp();
+    if (keep) g.slots[S + pos] = a;
+    if (lane >= c - k && lane < c) g.slots[S + lane] = kEmpty;
+    if (lane == 0) {
+      if (cap > kLeaf) g.lcnt[(base >> kLeafLog) + leaf] = (uint8_t)(c - k);
+      atomicSub(&g.deg[u], k);
+    }
+    __syncwarp();
   }
 }
 
-// remove, second pass: leaves under the lower bound climb to a window or
-// resize the segment (warp per group)
+// remove, second pass (thread per group): a leaf under the lower bound goes
+// to the climb list; a one-leaf segment that emptied or fell to a quarter
+// is resized
 __global__ void k_classify_remove(DGraph g, PmaParams p,
                                   const uint64_t *__restrict__ p_ul,
                                   const uint32_t *__restrict__ g_start,
@@ -297,57 +271,94 @@ __global__ void k_classify_remove(DGraph g, PmaParams p,
                                   uint8_t *__restrict__ gtype,
                                   uint8_t *__restrict__ glev,
                                   uint32_t *__restrict__ gw0,
-                                  uint32_t *__restrict__ gw1) {
-  uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (gid >= *d_ngroups) return;
-  uint64_t key = p_ul[g_start[gid]];
-  uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
-  uint64_t base = g.base[u];
-  uint32_t cap = g.cap[u], deg = g.deg[u];  // deg is already reduced
-  uint8_t type = kNone;
-  uint32_t lev = 0, w0 = leaf, w1 = leaf + 1;
-  if (cap <= kLeaf) {
-    if (deg == 0 || (cap > 1 && 4 * deg <= cap)) {
-      type = kResize;
-      lev = 31;
-      w0 = 0;
-      w1 = 1;
-    }
-  } else {
-    uint64_t lbase = base >> kLeafLog;
-    uint32_t H = log2_floor(cap >> kLeafLog);
-    uint64_t cur = g.lcnt[lbase + leaf];
-    if (cur < window_lower(p, 0, H)) {
-      uint32_t size = 1;
-      type = kResize;
-      for (uint32_t t = 1; t <= H; t++) {
-        uint32_t nw0 = (leaf >> t) << t;
-        if (nw0 == w0)
-          cur += warp_sum_lcnt(g.lcnt, lbase + w0 + size, lbase + w0 + 2 * size);
-        else
-          cur += warp_sum_lcnt(g.lcnt, lbase + nw0, lbase + w0);
-        w0 = nw0;
-        size <<= 1;
-        w1 = w0 + size;
-        if (cur >= window_lower(p, t, H)) {
-          type = kWindow;
-          lev = t;
-          break;
-        }
-      }
-      if (type == kResize) {
+                                  uint32_t *__restrict__ gw1,
+                                  uint32_t *__restrict__ climb,
+                                  uint32_t *__restrict__ nclimb) {
+  const uint32_t ng = *d_ngroups;
+  GRID_STRIDE(gid, ng) {
+    uint64_t key = p_ul[g_start[gid]];
+    uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
+    uint32_t cap = g.cap[u], deg = g.deg[u];  // deg is already reduced
+    uint8_t type = kNone;
+    uint32_t lev = 0, w0 = leaf, w1 = leaf + 1;
+    if (cap <= kLeaf) {
+      if (deg == 0 || (cap > 1 && 4 * deg <= cap)) {
+        type = kResize;
         lev = 31;
         w0 = 0;
-        w1 = cap >> kLeafLog;
+        w1 = 1;
       }
+    } else {
+      uint32_t H = log2_floor(cap >> kLeafLog);
+      if (g.lcnt[(g.base[u] >> kLeafLog) + leaf] < window_lower(p, 0, H))
+        climb[atomicAdd(nclimb, 1u)] = (uint32_t)gid;
     }
-  }
-  if (lane == 0) {
     gtype[gid] = type;
     glev[gid] = (uint8_t)lev;
     gw0[gid] = w0;
     gw1[gid] = w1;
+  }
+}
+
+// warp per climbing group: the smallest aligned window of 2^t leaves that
+// meets the density bound (insert: upper bound with the batch's new ids in
+// the window counted; remove: lower bound), else a resize of the segment
+__global__ void k_climb(DGraph g, PmaParams p, bool insert,
+                        const uint64_t *__restrict__ p_ul,
+                        const uint32_t *__restrict__ g_start,
+                        const uint32_t *__restrict__ d_nitems,
+                        const uint32_t *__restrict__ climb,
+                        const uint32_t *__restrict__ nclimb,
+                        uint8_t *__restrict__ gtype, uint8_t *__restrict__ glev,
+                        uint32_t *__restrict__ gw0, uint32_t *__restrict__ gw1) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t nc = *nclimb, nitems = *d_nitems;
+  for (uint64_t ci = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       ci < nc; ci += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+    uint32_t gid = climb[ci];
+    uint32_t j0 = g_start[gid];
+    uint64_t key = p_ul[j0];
+    uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
+    uint32_t cap = g.cap[u];
+    uint64_t lbase = g.base[u] >> kLeafLog;
+    uint32_t H = log2_floor(cap >> kLeafLog);
+    uint64_t cur = g.lcnt[lbase + leaf];
+    uint32_t w0 = leaf, size = 1, w1 = leaf + 1, lev = 31;
+    uint8_t type = kResize;
+    const uint64_t kk = (uint64_t)u << 32;
+    for (uint32_t t = 1; t <= H; t++) {
+      uint32_t nw0 = (leaf >> t) << t;
+      if (nw0 == w0)
+        cur += warp_sum_lcnt(g.lcnt, lbase + w0 + size, lbase + w0 + 2 * size);
+      else
+        cur += warp_sum_lcnt(g.lcnt, lbase + nw0, lbase + w0);
+      w0 = nw0;
+      size <<= 1;
+      w1 = w0 + size;
+      bool ok;
+      if (insert) {
+        uint32_t newc = lb_u64(p_ul, nitems, kk | w1) - lb_u64(p_ul, nitems, kk | w0);
+        ok = cur + newc <= window_upper(p, t, H);
+      } else {
+        ok = cur >= window_lower(p, t, H);
+      }
+      if (ok) {
+        type = kWindow;
+        lev = t;
+        break;
+      }
+    }
+    if (type == kResize) {
+      w0 = 0;
+      w1 = cap >> kLeafLog;
+    }
+    if (lane == 0) {
+      gtype[gid] = type;
+      glev[gid] = (uint8_t)lev;
+      gw0[gid] = w0;
+      gw1[gid] = w1;
+    }
+    __syncwarp();
   }
 }
 
@@ -455,18 +466,10 @@ __global__ void k_task_setup(DGraph g, PmaParams p, bool insert,
                              const uint32_t *__restrict__ d_nitems,
                              uint64_t gmax, Tasks t,
                              uint32_t *__restrict__ class_cnt) {
-  uint64_t tid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (tid >= gmax) return;
-  if (tid >= *d_ntasks) {
-    if (lane == 0) {
-      t.total[tid] = 0;
-      t.nsrc[tid] = 0;
-      t.ndst[tid] = 0;
-    }
-    return;
-  }
-  const uint32_t nitems = *d_nitems;
+  const uint32_t ntasks = *d_ntasks, nitems = *d_nitems;
+  for (uint64_t tid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       tid < ntasks; tid += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
   uint32_t gid = task_group[tid];
   uint32_t u = (uint32_t)(p_ul[g_start[gid]] >> 32);
   uint8_t type = gtype[gid];
@@ -510,6 +513,8 @@ __global__ void k_task_setup(DGraph g, PmaParams p, bool insert,
     t.capn[tid] = capn;
     t.rank[tid] = rank;
     t.type[tid] = type;
+  }
+  __syncwarp();
   }
 }
 
@@ -834,6 +839,7 @@ sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
     if (cfg->grow_fill > 0) g->params.grow_fill = cfg->grow_fill;
   }
   SST_CUDA_TRY(cudaSetDevice(g->device));
+  SST_CUDA_TRY(cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, g->device));
   SST_CUDA_TRY(cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking));
   g->stream = g->own_stream;
   uint64_t n = std::max<uint64_t>(height, 1);
@@ -853,6 +859,8 @@ sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
   g->bump = 0;
   SST_CUDA_TRY(cudaMallocHost(&g->h_plan, sizeof(PlanSummary)));
   SST_CUDA_TRY(cudaMalloc(&g->d_plan, sizeof(PlanSummary)));
+  SST_CUDA_TRY(cudaMalloc(&g->d_err, sizeof(unsigned long long)));
+  SST_CUDA_TRY(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned long long), g->stream));
   SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
   return SST_OK;
 }
@@ -866,6 +874,7 @@ void graph_release(sst_graph *g) {
   cudaFree(g->d_slots);
   cudaFree(g->d_lcnt);
   cudaFree(g->d_plan);
+  cudaFree(g->d_err);
   if (g->h_plan) cudaFreeHost(g->h_plan);
   if (g->h_pinned) cudaFreeHost(g->h_pinned);
   g->arena.release();
@@ -1005,6 +1014,7 @@ sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t b,
   uint32_t *mflag = A.take<uint32_t>(b), *tflag = A.take<uint32_t>(b);
   uint32_t *mpos = A.take<uint32_t>(b), *tpos = A.take<uint32_t>(b);
   uint32_t *merge_list = A.take<uint32_t>(b), *task_group = A.take<uint32_t>(b);
+  uint32_t *climb = A.take<uint32_t>(b);
   Tasks T;
   T.u = A.take<uint32_t>(b);
   T.w0 = A.take<uint32_t>(b);
@@ -1020,7 +1030,7 @@ sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t b,
   T.out = A.take<uint64_t>(b);
   T.soff = A.take<uint64_t>(b);
   T.doff = A.take<uint64_t>(b);
-  T.err = &P->apply_err;
+  T.err = g->d_err;
   uint64_t *cstart = A.take<uint64_t>(kNumClasses);
   if (!cstart) {
     set_error_message("update scratch sizing error");
@@ -1045,16 +1055,21 @@ sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t b,
                                       &P->n_groups, A, s)));
   SST_LAUNCH(k_group_start, blocks_for(b), kTB, 0, s, gflag, gpos, &P->n_items,
              &P->n_groups, b, g_start);
-  // 6: classify
+  // 6: classify (grids capped: the kernels stride over the device count)
+  const unsigned cap_blocks = (unsigned)g->sms * 8;
+  const unsigned tgrid = std::min(blocks_for(b), cap_blocks);
+  const unsigned wgrid = std::min(warp_blocks(b), cap_blocks);
   if (insert) {
-    SST_LAUNCH(k_classify_insert, warp_blocks(b), kTB, 0, s, dg, g->params, p_ul,
-               g_start, &P->n_groups, &P->n_items, gtype, glev, gw0, gw1);
+    SST_LAUNCH(k_classify_insert, tgrid, kTB, 0, s, dg, p_ul, g_start,
+               &P->n_groups, gtype, glev, gw0, gw1, climb, &P->n_climb);
   } else {
-    SST_LAUNCH(k_leaf_delete, warp_blocks(b), kTB, 0, s, dg, p_ul, p_x, g_start,
+    SST_LAUNCH(k_leaf_delete, wgrid, kTB, 0, s, dg, p_ul, p_x, g_start,
                &P->n_groups);
-    SST_LAUNCH(k_classify_remove, warp_blocks(b), kTB, 0, s, dg, g->params, p_ul,
-               g_start, &P->n_groups, gtype, glev, gw0, gw1);
+    SST_LAUNCH(k_classify_remove, tgrid, kTB, 0, s, dg, g->params, p_ul,
+               g_start, &P->n_groups, gtype, glev, gw0, gw1, climb, &P->n_climb);
   }
+  SST_LAUNCH(k_climb, wgrid, kTB, 0, s, dg, g->params, insert, p_ul, g_start,
+             &P->n_items, climb, &P->n_climb, gtype, glev, gw0, gw1);
   // 7: dominance
   SST_LAUNCH(k_dom_keys, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
              gw0, gw1, &P->n_groups, b, fkey, bkey);
@@ -1071,20 +1086,27 @@ sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t b,
   SST_LAUNCH(k_emit, blocks_for(b), kTB, 0, s, mflag, mpos, tflag, tpos, b,
              merge_list, task_group);
   // 8: plan
-  SST_LAUNCH(k_task_setup, warp_blocks(b), kTB, 0, s, dg, g->params, insert, p_ul,
+  SST_LAUNCH(k_task_setup, wgrid, kTB, 0, s, dg, g->params, insert, p_ul,
              g_start, gtype, gw0, gw1, task_group, &P->n_tasks, &P->n_items, b, T,
              P->class_cnt);
   SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.total, T.out, b, 0ull, OpAdd{}, true,
-                                      false, &P->task_elems, A, s)));
+                                      false, &P->task_elems, A, s, &P->n_tasks)));
   SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.nsrc, T.soff, b, 0ull, OpAdd{}, true,
-                                      false, &P->src_leaves, A, s)));
+                                      false, &P->src_leaves, A, s, &P->n_tasks)));
   SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.ndst, T.doff, b, 0ull, OpAdd{}, true,
-                                      false, &P->dst_leaves, A, s)));
+                                      false, &P->dst_leaves, A, s, &P->n_tasks)));
   SST_CUDA_TRY(cudaMemcpyAsync(g->h_plan, P, sizeof(PlanSummary),
+                               cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaMemcpyAsync(&g->h_plan->apply_err, g->d_err, 8,
                                cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   SST_CUDA_TRY(cudaGetLastError());
   PlanSummary ps = *g->h_plan;
+  if (ps.apply_err) {
+    set_error_message("internal error: %llu staged ranks out of range",
+                      (unsigned long long)ps.apply_err);
+    return SST_EDEVICE;
+  }
   if (n_invalid) *n_invalid = ps.invalid;
 
   // slab space for resized segments, laid out largest class first so each
@@ -1148,20 +1170,28 @@ sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t b,
   if (insert)
     SST_LAUNCH(k_deg_add, blocks_for(b), kTB, 0, s, dg, p_ul, g_start,
                &P->n_groups, b);
-  SST_CUDA_TRY(cudaMemcpyAsync(&g->h_plan->apply_err, &P->apply_err, 8,
-                               cudaMemcpyDeviceToHost, s));
-  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  // the staging-rank check of this batch is read back with the next plan
+  // (or by sst_sync), so a batch ends without a second host synchronisation
   SST_CUDA_TRY(cudaGetLastError());
-  if (g->h_plan->apply_err) {
-    set_error_message("internal error: %llu staged ranks out of range",
-                      (unsigned long long)g->h_plan->apply_err);
-    return SST_EDEVICE;
-  }
   if (insert)
     g->m += ps.n_items;
   else
     g->m -= ps.n_items;
   if (ps.n_items) g->version++;
+  return SST_OK;
+}
+
+// Complete the graph's stream and report a staging-rank error left by an
+// earlier batch (device-pointer updates do not wait for it).
+sst_status sync_checked(sst_graph *g) {
+  SST_CUDA_TRY(cudaMemcpyAsync(&g->h_plan->apply_err, g->d_err, 8,
+                               cudaMemcpyDeviceToHost, g->stream));
+  SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
+  if (g->h_plan->apply_err) {
+    set_error_message("internal error: %llu staged ranks out of range",
+                      (unsigned long long)g->h_plan->apply_err);
+    return SST_EDEVICE;
+  }
   return SST_OK;
 }
 

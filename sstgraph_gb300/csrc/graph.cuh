@@ -17,6 +17,7 @@ struct PlanSummary {
   uint32_t n_groups;     // (row, leaf) groups among them
   uint32_t n_merge;      // leaf-local merge tasks
   uint32_t n_tasks;      // window / resize tasks
+  uint32_t n_climb;      // groups whose leaf over- or underflowed
   uint64_t task_elems;   // elements staged by window / resize tasks
   uint64_t src_leaves;   // leaves read by those tasks
   uint64_t dst_leaves;   // leaves written by those tasks
@@ -46,6 +47,7 @@ struct LeafDir {
 
 struct sst_graph {
   int device = 0;
+  int sms = 148;  // multiprocessors of the device
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
   uint32_t n = 0, width = 0;
@@ -68,6 +70,7 @@ struct sst_graph {
   sst::Arena io;     // device copies of host-pointer arguments
   sst::PlanSummary *h_plan = nullptr;  // pinned
   sst::PlanSummary *d_plan = nullptr;
+  unsigned long long *d_err = nullptr;  // staging-rank check, read lazily
   sst::LeafDir dir;
   sst::TravState *trav = nullptr;  // traversal work lists and buffers
   void *h_pinned = nullptr;  // pinned staging for host-pointer calls
@@ -101,6 +104,7 @@ sst_status sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
                         uint64_t count, uint32_t *d_pairs);
 sst_status touch_all_sum(sst_graph *g, uint64_t *out);
 sst_status repack(sst_graph *g, uint64_t extra_slots);
+sst_status sync_checked(sst_graph *g);
 
 // host staging buffer (pinned) of at least `bytes`
 void *pinned(sst_graph *g, size_t bytes);

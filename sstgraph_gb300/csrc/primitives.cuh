@@ -129,7 +129,9 @@ __device__ __forceinline__ T block_exclusive(T v, T identity, Op op, T *total) {
 
 template <typename T, typename Op>
 __global__ void k_scan_reduce(const T *__restrict__ in, uint64_t n, T identity,
-                              Op op, bool reverse, T *__restrict__ block_sums) {
+                              Op op, bool reverse, T *__restrict__ block_sums,
+                              const uint32_t *__restrict__ d_n) {
+  if (d_n && *d_n < n) n = *d_n;
   uint64_t tile0 = (uint64_t)blockIdx.x * kScanTile;
   T acc = identity;
 #pragma unroll
@@ -146,7 +148,9 @@ template <typename T, typename Op>
 __global__ void k_scan_apply(const T *__restrict__ in, T *__restrict__ out,
                              uint64_t n, T identity, Op op, bool reverse,
                              bool exclusive, const T *__restrict__ block_prefix,
-                             T *__restrict__ total_out) {
+                             T *__restrict__ total_out,
+                             const uint32_t *__restrict__ d_n) {
+  if (d_n && *d_n < n) n = *d_n;
   uint64_t tile0 = (uint64_t)blockIdx.x * kScanTile;
   T vals[kScanItems];
   T acc = identity;
@@ -173,11 +177,12 @@ __global__ void k_scan_apply(const T *__restrict__ in, T *__restrict__ out,
 }
 
 // Scan of n elements (in may equal out).  total_out (device, may be null)
-// receives the reduction of all n elements.
+// receives the reduction of all n elements.  With d_n (device, may be null)
+// only the first min(n, *d_n) elements are scanned; n sizes the launch.
 template <typename T, typename Op>
 cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
                  bool exclusive, bool reverse, T *total_out, Arena &arena,
-                 cudaStream_t s) {
+                 cudaStream_t s, const uint32_t *d_n = nullptr) {
   if (n == 0) {
     if (total_out) return cudaMemcpyAsync(total_out, &identity, sizeof(T),
                                           cudaMemcpyHostToDevice, s);
@@ -186,20 +191,21 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
   uint64_t blocks = (n + kScanTile - 1) / kScanTile;
   if (blocks == 1) {
     SST_LAUNCH((k_scan_apply<T, Op>), 1, kScanThreads, 0, s, in, out, n,
-               identity, op, reverse, exclusive, (const T *)nullptr, total_out);
+               identity, op, reverse, exclusive, (const T *)nullptr, total_out,
+               d_n);
     return cudaGetLastError();
   }
   T *sums = arena.take<T>(blocks);
   if (!sums) return cudaErrorMemoryAllocation;
   SST_LAUNCH((k_scan_reduce<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
-             n, identity, op, reverse, sums);
+             n, identity, op, reverse, sums, d_n);
   // block prefixes in block order (reverse handled inside the tiles)
   cudaError_t e = scan<T, Op>(sums, sums, blocks, identity, op, true, false,
                               (T *)nullptr, arena, s);
   if (e != cudaSuccess) return e;
   SST_LAUNCH((k_scan_apply<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
              out, n, identity, op, reverse, exclusive, (const T *)sums,
-             total_out);
+             total_out, d_n);
   return cudaGetLastError();
 }
 
