@@ -94,6 +94,15 @@ SST_API sst_status sst_insert_batch(sst_graph *g, const uint32_t *pairs, uint64_
 /* remove_batch  SparseMatrix.hpp:645-718; absent edges are no-ops */
 SST_API sst_status sst_remove_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
                             uint32_t flags, uint64_t *n_invalid);
+/* Batched form of insert_batch / remove_batch: nbatches batches, batch i
+ * being pairs[offsets[i] .. offsets[i+1]) (offsets has nbatches+1 entries,
+ * offsets[0] = 0) with ops[i] = 1 to insert, 0 to remove.  The graph ends as
+ * if the batches ran one after another; they run as one pipeline pass (the
+ * last operation on each edge decides). */
+SST_API sst_status sst_update_batches(sst_graph *g, const uint32_t *pairs,
+                                      const uint64_t *offsets,
+                                      const uint8_t *ops, uint32_t nbatches,
+                                      uint32_t flags, uint64_t *n_invalid);
 /* insert(el_t, el_t) / remove(el_t, el_t)  SparseMatrix.hpp:164-166 */
 SST_API sst_status sst_insert(sst_graph *g, uint32_t row, uint32_t col);
 SST_API sst_status sst_remove(sst_graph *g, uint32_t row, uint32_t col);

@@ -58,6 +58,7 @@ SIGNATURES = {
     "sst_status_string": (ctypes.c_char_p, [_i32]),
     "sst_insert_batch": (_i32, [_vp, _vp, _u64, _u32, ctypes.POINTER(_u64)]),
     "sst_remove_batch": (_i32, [_vp, _vp, _u64, _u32, ctypes.POINTER(_u64)]),
+    "sst_update_batches": (_i32, [_vp, _vp, _vp, _vp, _u32, _u32, ctypes.POINTER(_u64)]),
     "sst_insert": (_i32, [_vp, _u32, _u32]),
     "sst_remove": (_i32, [_vp, _u32, _u32]),
     "sst_build_from_csr": (_i32, [_vp, _vp, _vp, _u32]),
@@ -218,6 +219,42 @@ class SparseMatrixV:
         bad = ctypes.c_uint64()
         _check(lib().sst_remove_batch(self._h, p, n, flags | (SEMI_SORTED if semi_sorted else 0),
                                       ctypes.byref(bad)))
+        return bad.value
+
+    def update_batches(self, batches, ops=None) -> int:
+        """Apply a sequence of batches as one pipeline pass.
+
+        batches: list of (k, 2) pair arrays (or one concatenated array with
+        `offsets`); ops: per batch 1 = insert, 0 = remove (default: insert).
+        """
+        if isinstance(batches, tuple) and len(batches) == 2:
+            pairs, offsets = batches
+        else:
+            sizes = [len(b) for b in batches]
+            offsets = np.zeros(len(batches) + 1, np.uint64)
+            offsets[1:] = np.cumsum(sizes)
+            if batches and hasattr(batches[0], "data_ptr"):
+                import torch
+                pairs = torch.cat(list(batches)).contiguous()
+                offsets = torch.from_numpy(offsets.astype(np.int64)).to(pairs.device)
+            else:
+                pairs = np.ascontiguousarray(np.concatenate(
+                    [np.asarray(b, np.uint32).reshape(-1, 2) for b in batches]))
+        nb = len(offsets) - 1
+        if ops is None:
+            ops = [1] * nb
+        p, flags = _ptr(pairs)
+        if flags == DEVICE_PTR:
+            import torch
+            ops_t = torch.as_tensor(np.asarray(ops, np.uint8), device=pairs.device)
+            po, _ = _ptr(offsets)
+            pops, _ = _ptr(ops_t)
+        else:
+            offsets = np.ascontiguousarray(offsets, np.uint64)
+            ops_a = np.ascontiguousarray(np.asarray(ops, np.uint8))
+            po, pops = ctypes.c_void_p(offsets.ctypes.data), ctypes.c_void_p(ops_a.ctypes.data)
+        bad = ctypes.c_uint64()
+        _check(lib().sst_update_batches(self._h, p, po, pops, nb, flags, ctypes.byref(bad)))
         return bad.value
 
     def insert(self, row: int, col: int):

@@ -240,6 +240,43 @@ sst_status sst_remove_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
   return do_update(g, pairs, n, flags, n_invalid, false);
 }
 
+sst_status sst_update_batches(sst_graph *g, const uint32_t *pairs,
+                              const uint64_t *offsets, const uint8_t *ops,
+                              uint32_t nbatches, uint32_t flags,
+                              uint64_t *n_invalid) {
+  CHECK_G(g);
+  if (n_invalid) *n_invalid = 0;
+  if (nbatches == 0) return SST_OK;
+  if (!offsets || !ops) {
+    set_error_message("null offsets or ops");
+    return SST_EINVAL;
+  }
+  uint64_t N = 0;
+  if (is_dev(flags)) {
+    SST_CUDA_TRY(cudaMemcpyAsync(&N, offsets + nbatches, 8, cudaMemcpyDeviceToHost, g->stream));
+    SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
+  } else {
+    N = offsets[nbatches];
+  }
+  if (N && !pairs) {
+    set_error_message("null pairs");
+    return SST_EINVAL;
+  }
+  sst_status st = is_dev(flags) ? SST_OK
+                                : io_begin(g, N * 8 + (nbatches + 1) * 9 + 1024);
+  if (st != SST_OK) return st;
+  const uint32_t *dp = nullptr;
+  const uint64_t *doff = nullptr;
+  const uint8_t *dops = nullptr;
+  st = stage_in(g, pairs, 2 * N, flags, &dp);
+  if (st == SST_OK) st = stage_in(g, offsets, (uint64_t)nbatches + 1, flags, &doff);
+  if (st == SST_OK) st = stage_in(g, ops, (uint64_t)nbatches, flags, &dops);
+  if (st != SST_OK) return st;
+  st = sst::update_batches(g, dp, doff, dops, nbatches, N, n_invalid);
+  if (st == SST_OK && !is_dev(flags)) st = sst::sync_checked(g);
+  return st;
+}
+
 sst_status sst_insert(sst_graph *g, uint32_t row, uint32_t col) {
   uint32_t p[2] = {row, col};
   uint64_t bad = 0;

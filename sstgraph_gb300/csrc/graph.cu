@@ -979,8 +979,21 @@ static size_t update_scratch_bytes(uint64_t b) {
          (1 << 16);
 }
 
+// One pass of the update pipeline.  Either d_pairs (raw pairs: steps 1-2
+// make and sort the keys) or presorted (keys already (row << dbits | col),
+// ascending and duplicate-free, in memory outside the arena) is given.
+static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
+                               const uint64_t *presorted, uint64_t b,
+                               bool insert, uint64_t *n_invalid);
+
 sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t b,
                         bool insert, uint64_t *n_invalid) {
+  return run_pipeline(g, d_pairs, nullptr, b, insert, n_invalid);
+}
+
+static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
+                               const uint64_t *presorted, uint64_t b,
+                               bool insert, uint64_t *n_invalid) {
   if (n_invalid) *n_invalid = 0;
   if (b == 0) return SST_OK;
   if (b > 0xFFFFFFF0ull) {
@@ -1038,11 +1051,15 @@ sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t b,
   }
 
   // 1-2: keys and sort
-  SST_LAUNCH(k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n, g->width,
-             dbits, insert, keys,
-             reinterpret_cast<unsigned long long *>(&P->invalid));
-  uint64_t *sorted = keys;
-  SST_CUDA_TRY(radix_sort_u64(keys, ktmp, b, g->rbits + dbits, A, s, &sorted));
+  const uint64_t *sorted = presorted;
+  if (!presorted) {
+    SST_LAUNCH(k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n, g->width,
+               dbits, insert, keys,
+               reinterpret_cast<unsigned long long *>(&P->invalid));
+    uint64_t *out = keys;
+    SST_CUDA_TRY(radix_sort_u64(keys, ktmp, b, g->rbits + dbits, A, s, &out));
+    sorted = out;
+  }
   // 3-5: locate, pack, group
   SST_LAUNCH(k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg, insert,
              flag, leaf);
@@ -1179,6 +1196,120 @@ sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t b,
     g->m -= ps.n_items;
   if (ps.n_items) g->version++;
   return SST_OK;
+}
+
+// ------------------------------------------------------------ batched form
+// A sequence of update batches applied as one pipeline pass.  With set
+// semantics only the last operation on an edge decides whether it is present
+// afterwards, so a stable sort of all pairs by edge (payload: the batch's
+// operation) and a last-one-wins selection give the net removals and net
+// insertions, which touch disjoint edges and run as one remove pass and one
+// insert pass over already sorted keys.  Self-loops are dropped from both
+// (an inserted self-loop is skipped, a removed one is absent).
+namespace {
+__global__ void k_make_keys_batched(const uint32_t *__restrict__ pairs,
+                                    uint64_t N, const uint64_t *__restrict__ boff,
+                                    uint32_t nb, const uint8_t *__restrict__ ops,
+                                    uint32_t n, uint32_t width, int dbits,
+                                    uint64_t *__restrict__ keys,
+                                    uint32_t *__restrict__ vals,
+                                    unsigned long long *__restrict__ invalid) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  uint32_t lo = 0, hi = nb;  // batch: last with boff[b] <= i
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (boff[mid] <= i)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  uint32_t r = pairs[2 * i], c = pairs[2 * i + 1];
+  const uint64_t sent = (uint64_t)n << dbits;
+  bool ok = r < n && c < width && c != kEmpty;
+  if (!ok) atomicAdd(invalid, 1ull);
+  keys[i] = (!ok || r == c) ? sent : (((uint64_t)r << dbits) | c);
+  vals[i] = ops[lo] ? 1u : 0u;
+}
+
+__global__ void k_last_op(const uint64_t *__restrict__ keys,
+                          const uint32_t *__restrict__ vals, uint64_t N,
+                          uint64_t sent, uint32_t *__restrict__ fins,
+                          uint32_t *__restrict__ fdel) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  uint64_t k = keys[j];
+  bool last = k < sent && (j + 1 == N || keys[j + 1] != k);
+  fins[j] = last && vals[j];
+  fdel[j] = last && !vals[j];
+}
+
+__global__ void k_compact_keys(const uint64_t *__restrict__ keys,
+                               const uint32_t *__restrict__ f,
+                               const uint32_t *__restrict__ pos, uint64_t N,
+                               uint64_t *__restrict__ out) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < N && f[j]) out[pos[j]] = keys[j];
+}
+}  // namespace
+
+sst_status update_batches(sst_graph *g, const uint32_t *d_pairs,
+                          const uint64_t *d_boff, const uint8_t *d_ops,
+                          uint32_t nb, uint64_t N, uint64_t *n_invalid) {
+  if (n_invalid) *n_invalid = 0;
+  if (N == 0 || nb == 0) return SST_OK;
+  if (N > 0xFFFFFFF0ull) {
+    set_error_message("batched update of %llu pairs exceeds 2^32", (unsigned long long)N);
+    return SST_EINVAL;
+  }
+  cudaStream_t s = g->stream;
+  size_t need = N * (8 * 2 + 4 * 6 + 64) + radix_sort_scratch_bytes(N) +
+                4 * scan_scratch_bytes(N, 4) + (1 << 16);
+  if (need > g->arena.cap) {
+    sst_status st = budget_check(g, need - g->arena.cap);
+    if (st != SST_OK) return st;
+  }
+  SST_CUDA_TRY(g->arena.reserve(need));
+  Arena &A = g->arena;
+  A.reset();
+  PlanSummary *P = g->d_plan;
+  SST_CUDA_TRY(cudaMemsetAsync(P, 0, sizeof(PlanSummary), s));
+  uint64_t *keys = A.take<uint64_t>(N), *ktmp = A.take<uint64_t>(N);
+  uint32_t *vals = A.take<uint32_t>(N), *vtmp = A.take<uint32_t>(N);
+  uint32_t *fins = A.take<uint32_t>(N), *fdel = A.take<uint32_t>(N);
+  uint32_t *pins = A.take<uint32_t>(N), *pdel = A.take<uint32_t>(N);
+  if (!pdel) {
+    set_error_message("batched update scratch sizing error");
+    return SST_ENOMEM;
+  }
+  const int dbits = g->dbits;
+  const uint64_t sent = (uint64_t)g->n << dbits;
+  SST_LAUNCH(k_make_keys_batched, blocks_for(N), kTB, 0, s, d_pairs, N, d_boff,
+             nb, d_ops, g->n, g->width, dbits, keys, vals,
+             reinterpret_cast<unsigned long long *>(&P->invalid));
+  uint64_t *sk = keys;
+  uint32_t *sv = vals;
+  SST_CUDA_TRY(radix_sort_kv(keys, ktmp, vals, vtmp, N, g->rbits + dbits, A, s,
+                             &sk, &sv));
+  SST_LAUNCH(k_last_op, blocks_for(N), kTB, 0, s, sk, sv, N, sent, fins, fdel);
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(fins, pins, N, 0u, OpAdd{}, true, false,
+                                      &P->n_items, A, s)));
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(fdel, pdel, N, 0u, OpAdd{}, true, false,
+                                      &P->n_groups, A, s)));
+  SST_CUDA_TRY(cudaMemcpyAsync(g->h_plan, P, sizeof(PlanSummary),
+                               cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t n_ins = g->h_plan->n_items, n_del = g->h_plan->n_groups;
+  if (n_invalid) *n_invalid = g->h_plan->invalid;
+  if (n_ins + n_del == 0) return SST_OK;
+  uint64_t *net = nullptr;
+  SST_CUDA_TRY(cudaMallocAsync(&net, (n_ins + n_del) * 8, s));
+  SST_LAUNCH(k_compact_keys, blocks_for(N), kTB, 0, s, sk, fins, pins, N, net);
+  SST_LAUNCH(k_compact_keys, blocks_for(N), kTB, 0, s, sk, fdel, pdel, N, net + n_ins);
+  sst_status st = run_pipeline(g, nullptr, net + n_ins, n_del, false, nullptr);
+  if (st == SST_OK) st = run_pipeline(g, nullptr, net, n_ins, true, nullptr);
+  cudaFreeAsync(net, s);
+  return st;
 }
 
 // Complete the graph's stream and report a staging-rank error left by an

@@ -92,6 +92,11 @@ uint64_t graph_device_bytes(const sst_graph *g);
 // pairs are device pointers here; the C ABI stages host buffers
 sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,
                         bool insert, uint64_t *n_invalid);
+// nb batches: pairs[boff[i]..boff[i+1]) with ops[i] (1 insert, 0 remove),
+// applied as if in order; N = boff[nb]
+sst_status update_batches(sst_graph *g, const uint32_t *d_pairs,
+                          const uint64_t *d_boff, const uint8_t *d_ops,
+                          uint32_t nb, uint64_t N, uint64_t *n_invalid);
 sst_status build_from_csr(sst_graph *g, const uint64_t *d_off,
                           const uint32_t *d_cols);
 sst_status has_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,

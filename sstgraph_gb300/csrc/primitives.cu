@@ -2,6 +2,7 @@
 // counter.  Each pass: per-tile digit histograms, one exclusive scan over
 // (digit, tile), then a stable scatter that ranks equal digits with
 // warp match_any + per-warp prefix counts in shared memory.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <map>
@@ -166,7 +167,9 @@ __global__ void k_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
 
 __global__ void k_scatter(const uint64_t *__restrict__ in,
                           uint64_t *__restrict__ out, uint64_t n, int shift,
-                          const uint32_t *__restrict__ hist, uint32_t nblocks) {
+                          const uint32_t *__restrict__ hist, uint32_t nblocks,
+                          const uint32_t *__restrict__ vin,
+                          uint32_t *__restrict__ vout) {
   __shared__ uint32_t wcnt[kWarps][kRadix];
   __shared__ uint32_t run[kRadix];
   run[threadIdx.x] = hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x];
@@ -178,17 +181,27 @@ __global__ void k_scatter(const uint64_t *__restrict__ in,
     uint64_t k = valid ? in[i] : 0;
     uint32_t d = (uint32_t)(k >> shift) & 0xff;
     uint32_t pos = rank_iteration(d, valid, wcnt, run);
-    if (valid) out[pos] = k;
+    if (valid) {
+      out[pos] = k;
+      if (vin) vout[pos] = vin[i];
+    }
   }
 }
 
-// whole sort in one CTA for n <= kSmallSort: keys staged in shared memory
-__global__ void k_sort_small(uint64_t *__restrict__ keys, uint64_t n, int bits) {
-  __shared__ uint64_t buf[2][kSmallSort];
+// whole sort in one CTA for n <= TILE: keys (and payloads) staged in shared
+// memory
+template <bool KV, int TILE>
+__global__ void k_sort_small(uint64_t *__restrict__ keys,
+                             uint32_t *__restrict__ vals, uint64_t n, int bits) {
+  __shared__ uint64_t buf[2][TILE];
+  __shared__ uint32_t vbuf[KV ? 2 : 1][KV ? TILE : 1];
   __shared__ uint32_t wcnt[kWarps][kRadix];
   __shared__ uint32_t run[kRadix];
   __shared__ uint32_t h[kRadix];
-  for (uint64_t i = threadIdx.x; i < n; i += kThreads) buf[0][i] = keys[i];
+  for (uint64_t i = threadIdx.x; i < n; i += kThreads) {
+    buf[0][i] = keys[i];
+    if (KV) vbuf[0][i] = vals[i];
+  }
   int cur = 0;
   for (int shift = 0; shift < bits; shift += 8) {
     h[threadIdx.x] = 0;
@@ -222,13 +235,21 @@ __global__ void k_sort_small(uint64_t *__restrict__ keys, uint64_t n, int bits) 
       uint64_t k = valid ? buf[cur][i] : 0;
       uint32_t d = (uint32_t)(k >> shift) & 0xff;
       uint32_t pos = rank_iteration(d, valid, wcnt, run);
-      if (valid) buf[cur ^ 1][pos] = k;
+      if (valid) {
+        buf[cur ^ 1][pos] = k;
+        if (KV) vbuf[cur ^ 1][pos] = vbuf[cur][i];
+      }
     }
     __syncthreads();
     cur ^= 1;
   }
-  for (uint64_t i = threadIdx.x; i < n; i += kThreads) keys[i] = buf[cur][i];
+  for (uint64_t i = threadIdx.x; i < n; i += kThreads) {
+    keys[i] = buf[cur][i];
+    if (KV) vals[i] = vbuf[cur][i];
+  }
 }
+
+constexpr int kSmallSortKV = 1024;
 
 }  // namespace
 
@@ -238,12 +259,21 @@ size_t radix_sort_scratch_bytes(uint64_t n) {
   return ((hn * 4 + 255) & ~size_t(255)) + scan_scratch_bytes(hn, 4) + 512;
 }
 
-cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
-                           Arena &arena, cudaStream_t s, uint64_t **result) {
+static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
+                                   uint32_t *vals, uint32_t *vtmp, uint64_t n,
+                                   int bits, Arena &arena, cudaStream_t s,
+                                   uint64_t **result, uint32_t **vresult) {
   *result = keys;
+  if (vresult) *vresult = vals;
   if (n < 2 || bits <= 0) return cudaSuccess;
-  if (n <= (uint64_t)kSmallSort) {
-    SST_LAUNCH(k_sort_small, 1, kThreads, 0, s, keys, n, bits);
+  if (!vals && n <= (uint64_t)kSmallSort) {
+    SST_LAUNCH((k_sort_small<false, kSmallSort>), 1, kThreads, 0, s, keys,
+               (uint32_t *)nullptr, n, bits);
+    return cudaGetLastError();
+  }
+  if (vals && n <= (uint64_t)kSmallSortKV) {
+    SST_LAUNCH((k_sort_small<true, kSmallSortKV>), 1, kThreads, 0, s, keys, vals,
+               n, bits);
     return cudaGetLastError();
   }
   uint32_t nblocks = (uint32_t)((n + kTile - 1) / kTile);
@@ -251,6 +281,7 @@ cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
   uint32_t *hist = arena.take<uint32_t>(hn);
   if (!hist) return cudaErrorMemoryAllocation;
   uint64_t *src = keys, *dst = tmp;
+  uint32_t *vsrc = vals, *vdst = vtmp;
   for (int shift = 0; shift < bits; shift += 8) {
     SST_LAUNCH(k_hist, nblocks, kThreads, 0, s, src, n, shift, hist, nblocks);
     size_t mark = arena.used;
@@ -259,13 +290,26 @@ cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
     arena.used = mark;
     if (e != cudaSuccess) return e;
     SST_LAUNCH(k_scatter, nblocks, kThreads, 0, s, src, dst, n, shift, hist,
-               nblocks);
-    uint64_t *t = src;
-    src = dst;
-    dst = t;
+               nblocks, vsrc, vdst);
+    std::swap(src, dst);
+    std::swap(vsrc, vdst);
   }
   *result = src;
+  if (vresult) *vresult = vsrc;
   return cudaGetLastError();
+}
+
+cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
+                           Arena &arena, cudaStream_t s, uint64_t **result) {
+  return radix_sort_impl(keys, tmp, nullptr, nullptr, n, bits, arena, s, result,
+                         nullptr);
+}
+
+cudaError_t radix_sort_kv(uint64_t *keys, uint64_t *tmp, uint32_t *vals,
+                          uint32_t *vtmp, uint64_t n, int bits, Arena &arena,
+                          cudaStream_t s, uint64_t **result, uint32_t **vresult) {
+  return radix_sort_impl(keys, tmp, vals, vtmp, n, bits, arena, s, result,
+                         vresult);
 }
 
 }  // namespace sst

@@ -225,6 +225,10 @@ inline size_t scan_scratch_bytes(uint64_t n, size_t elem) {
 // digits.  keys and tmp are both n long; *result points at whichever holds
 // the sorted keys.  Batches up to kSmallSort keys sort in one CTA.
 constexpr int kSmallSort = 2048;
+// the same with a 32-bit payload per key moved along (stable)
+cudaError_t radix_sort_kv(uint64_t *keys, uint64_t *tmp, uint32_t *vals,
+                          uint32_t *vtmp, uint64_t n, int bits, Arena &arena,
+                          cudaStream_t s, uint64_t **result, uint32_t **vresult);
 cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
                            Arena &arena, cudaStream_t s, uint64_t **result);
 size_t radix_sort_scratch_bytes(uint64_t n);
