@@ -51,7 +51,8 @@ def args_parse():
     ap.add_argument("--scale", type=int, default=24)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--pr-iters", type=int, default=10)
-    ap.add_argument("--only", default="all", choices=["all", "pagerank", "bfs"],
+    ap.add_argument("--batched-batches", type=int, default=128)
+    ap.add_argument("--only", default="all", choices=["all", "pagerank", "bfs", "batched"],
                     help="run one traversal on the base graph (profiling cases)")
     return ap.parse_args()
 
@@ -314,11 +315,59 @@ def main():
                             "frac": (4 * m_r + 12 * n) / bt / 1e9 / hbm_peak}}
         return bfs
 
+    def measure_batched():
+        """The same stream of uneven insert batches (log-normal sizes, median
+        1e4, sigma 1.5, clipped to [1e3, 1e6]) applied to two device copies of
+        the graph: one insert_batch call per batch (plain form) vs one
+        update_batches call for the whole stream (batched form)."""
+        rng = np.random.default_rng(11)
+        sizes = np.clip(rng.lognormal(np.log(1e4), 1.5, a.batched_batches),
+                        1e3, 1e6).astype(np.int64)
+        bl = []
+        first = 0
+        with torch.cuda.stream(stream):
+            for sz in sizes.tolist():
+                x = torch.empty((sz, 2), dtype=torch.int32, device="cuda")
+                sg.gen_rmat(a.scale, sz, seed=12, first=first, out=x, **RMAT)
+                first += sz
+                bl.append(x)
+        torch.cuda.synchronize()
+        total_e = int(sizes.sum())
+        res = {}
+        for form in ("plain", "batched"):
+            gc = g.copy()
+            gc.set_stream(stream.cuda_stream)
+            torch.cuda.synchronize()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            if form == "plain":
+                for x in bl:
+                    gc.insert_batch(x)
+            else:
+                gc.update_batches(bl)
+            s1.record(stream)
+            s1.synchronize()
+            t = s0.elapsed_time(s1) / 1e3
+            res[form] = {"edges_per_s": total_e / t, "s": t,
+                         "check": [gc.M(), gc.touch_all_sum()]}
+            gc.close()
+        same = res["plain"]["check"] == res["batched"]["check"]
+        return {"batches": len(bl), "edges": total_e,
+                "sizes": {"min": int(sizes.min()), "median": int(np.median(sizes)),
+                          "max": int(sizes.max())},
+                "plain_edges_per_s": res["plain"]["edges_per_s"],
+                "batched_edges_per_s": res["batched"]["edges_per_s"],
+                "speedup": res["batched"]["edges_per_s"] / res["plain"]["edges_per_s"],
+                "same_graph": same,
+                "check": "M and touch_all_sum of both copies"}
+
     if a.only != "all":
         pr_flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
         res = {"only": a.only, "scale": a.scale, "edges": m0}
         if a.only == "pagerank":
             res["pagerank"] = measure_pagerank()
+        elif a.only == "batched":
+            res["batched"] = measure_batched()
         else:
             res["bfs"] = measure_bfs()
         g.close()
@@ -391,6 +440,7 @@ def main():
            "note": "insert+remove via sst_insert_batch/sst_remove_batch on pinned host "
                    "pairs; each call returns the invalid-pair count (8 B) to the host"}
 
+    batched = measure_batched()
     pagerank = measure_pagerank()
     bfs = measure_bfs()
 
@@ -425,6 +475,7 @@ def main():
         "clocks": clocks,
         "remove_edges_per_s": world * edges / tr,
         "base_graph": {"edges": m0, "build_s": round(build_s, 2)},
+        "batched_form": batched,
         "pagerank": pagerank,
         "bfs": bfs,
         "update_kernels": upd_kernels,
