@@ -141,6 +141,15 @@ SST_API sst_status sst_common_neighbors_batch(sst_graph *g, const uint32_t *pair
 SST_API sst_status sst_touch_all_sum(sst_graph *g, uint64_t *out);
 /* get_memory_size  SparseMatrix.hpp:317,528-535: device bytes held */
 SST_API sst_status sst_memory_size(sst_graph *g, uint64_t *out);
+/* degree_order_map()  SparseMatrix.hpp:737-752: map[v] = rank of v when the
+ * vertices are ordered by (degree, id) descending */
+SST_API sst_status sst_degree_order_map(sst_graph *g, uint32_t *map,
+                                        uint32_t flags);
+/* rewrite_graph(new_label_map)  SparseMatrix.hpp:754-766: a new graph (same
+ * shape, same configuration) holding every edge (u, v) as (map[u], map[v]);
+ * rows must equal columns */
+SST_API sst_status sst_rewrite_graph(sst_graph *g, const uint32_t *map,
+                                     uint32_t flags, sst_graph **out);
 /* uniform samples of existing edges: edge of rank
  * floor(draw(seed, first+i) * M / 2^64) in (row, col) order */
 SST_API sst_status sst_sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
@@ -196,8 +205,9 @@ SST_API sst_status sst_gen_ref_rmat(uint32_t nn, double a, double b, double c,
  * internal/helpers.hpp:239-243): between start and collect every kernel
  * launch is bracketed by CUDA events on its stream; collect writes a JSON
  * object {"kernel": {"launches": L, "ms": T}, ...} into buf (NUL-terminated,
- * truncated to cap) and stops profiling */
-SST_API sst_status sst_profile_start(void);
+ * truncated to cap) and stops profiling.  kernel_filter (may be NULL)
+ * limits the events to kernels whose name contains it. */
+SST_API sst_status sst_profile_start(const char *kernel_filter);
 SST_API sst_status sst_profile_collect(char *buf, uint64_t cap);
 /* raw device layout for structural checks (no reference counterpart):
  * vertex table (base[rows], cap[rows], deg[rows]) and, when slots / lcnt are

@@ -221,6 +221,8 @@ def ref():
             "ref_common_neighbors": (u64, [vp, u32, u32, i32]),
             "ref_touch_all_sum": (u64, [vp]),
             "ref_to_csr": (None, [vp, vp, vp]),
+            "ref_degree_order_map": (None, [vp, vp]),
+            "ref_rewrite_graph": (vp, [vp, vp]),
             "ref_set_new": (vp, [u32]),
             "ref_set_free": (None, [vp]),
             "ref_set_insert": (None, [vp, u32]),
@@ -285,6 +287,34 @@ class RefGraph:
 
     def touch_all_sum(self) -> int:
         return int(ref().ref_touch_all_sum(self._h))
+
+    def degree_order_map(self) -> np.ndarray:
+        out = np.empty(self.n, np.uint32)
+        ref().ref_degree_order_map(self._h, _ptr(out))
+        return out
+
+    def rewrite_graph(self, label_map) -> "RefGraph":
+        m = np.ascontiguousarray(label_map, np.uint32)
+        g = RefGraph.__new__(RefGraph)
+        g.n = self.n
+        g._h = ref().ref_rewrite_graph(self._h, _ptr(m))
+        return g
+
+
+def degree_order_map(degrees) -> np.ndarray:
+    """Restated degree_order_map (SparseMatrix.hpp:737-752): rank of each
+    vertex when ordered by (degree, id) descending."""
+    d = np.asarray(degrees, np.int64)
+    ids = np.arange(len(d), dtype=np.int64)
+    order = np.lexsort((-ids, -d))
+    out = np.empty(len(d), np.uint32)
+    out[order] = np.arange(len(d), dtype=np.uint32)
+    return out
+
+
+def relabel(edges, label_map) -> np.ndarray:
+    e = _pairs(edges)
+    return np.ascontiguousarray(np.asarray(label_map, np.uint32)[e])
 
 
 def ref_random_data(n, max_val, seed=0) -> np.ndarray:

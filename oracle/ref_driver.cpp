@@ -97,6 +97,18 @@ void ref_to_csr(void *gp, uint64_t *offsets, uint32_t *cols) {
   offsets[g->num_nodes()] = pos;
 }
 
+// degree_order_map / rewrite_graph  SparseMatrix.hpp:737-766
+void ref_degree_order_map(void *gp, uint32_t *out) {
+  Graph *g = static_cast<Graph *>(gp);
+  std::vector<uint64_t> m = g->degree_order_map();
+  for (size_t i = 0; i < m.size(); i++) out[i] = static_cast<uint32_t>(m[i]);
+}
+void *ref_rewrite_graph(void *gp, const uint32_t *map) {
+  Graph *g = static_cast<Graph *>(gp);
+  std::vector<uint64_t> m(map, map + g->num_nodes());
+  return new Graph(g->rewrite_graph(m));
+}
+
 // ---- standalone set (TinySetV) ----
 using Set = TinySetV<>;
 void *ref_set_new(uint32_t max_el) { return new Set(max_el); }

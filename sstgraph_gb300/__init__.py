@@ -76,6 +76,8 @@ SIGNATURES = {
     "sst_touch_all_sum": (_i32, [_vp, ctypes.POINTER(_u64)]),
     "sst_memory_size": (_i32, [_vp, ctypes.POINTER(_u64)]),
     "sst_sample_edges": (_i32, [_vp, _u64, _u64, _u64, _vp, _u32]),
+    "sst_degree_order_map": (_i32, [_vp, _vp, _u32]),
+    "sst_rewrite_graph": (_i32, [_vp, _vp, _u32, ctypes.POINTER(_vp)]),
     "sst_bfs": (_i32, [_vp, _u32, _vp, _vp, _u32]),
     "sst_pagerank": (_i32, [_vp, _u32, _dbl, _vp, _u32]),
     "sst_cc": (_i32, [_vp, _vp, _u32]),
@@ -88,13 +90,15 @@ SIGNATURES = {
     "sst_kernel_launches": (_u64, []),
     "sst_raw_state": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64)]),
     "sst_pagerank_noalloc": (_i32, [_vp, _u32, _dbl, _vp]),
-    "sst_profile_start": (_i32, []),
+    "sst_profile_start": (_i32, [ctypes.c_char_p]),
     "sst_profile_collect": (_i32, [ctypes.c_char_p, _u64]),
 }
 
 
-def profile_start():
-    _check(lib().sst_profile_start())
+def profile_start(kernel_filter: str | None = None):
+    """Bracket kernel launches with CUDA events (all, or those whose name
+    contains kernel_filter) until profile_collect()."""
+    _check(lib().sst_profile_start(kernel_filter.encode() if kernel_filter else None))
 
 
 def profile_collect() -> dict:
@@ -381,6 +385,23 @@ class SparseMatrixV:
                                    ctypes.c_void_p(slots.ctypes.data),
                                    ctypes.c_void_p(lcnt.ctypes.data), ctypes.byref(ns)))
         return base[:n], cap[:n], deg[:n], slots[:used], lcnt[:used // 32]
+
+    def degree_order_map(self, out=None):
+        """new label of each vertex: its rank by (degree, id) descending"""
+        if out is None:
+            out = np.empty(self.rows, np.uint32)
+        p, flags = _ptr(out)
+        _check(lib().sst_degree_order_map(self._h, p, flags))
+        return out
+
+    def rewrite_graph(self, new_label_map) -> "SparseMatrixV":
+        m = new_label_map
+        if isinstance(m, np.ndarray):
+            m = np.ascontiguousarray(m, np.uint32)
+        p, flags = _ptr(m)
+        h = ctypes.c_void_p()
+        _check(lib().sst_rewrite_graph(self._h, p, flags, ctypes.byref(h)))
+        return SparseMatrixV(0, _handle=h)
 
     def sample_edges(self, count: int, seed: int, first: int = 0, out=None):
         if out is None:

@@ -10,7 +10,7 @@
 
 namespace sst {
 const char *error_message();
-void profile_start();
+void profile_start(const char *filter);
 std::string profile_collect();
 cudaError_t gen_rmat(uint32_t scale, double a, double b, double c, uint64_t seed,
                      uint64_t first, uint64_t count, uint32_t *d_pairs,
@@ -115,8 +115,8 @@ const char *sst_status_string(sst_status s) {
 
 uint64_t sst_kernel_launches(void) { return sst::launches(); }
 
-sst_status sst_profile_start(void) {
-  sst::profile_start();
+sst_status sst_profile_start(const char *kernel_filter) {
+  sst::profile_start(kernel_filter);
   return SST_OK;
 }
 
@@ -473,6 +473,53 @@ sst_status sst_sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
   st = sst::sample_edges(g, seed, first, count, d);
   if (st != SST_OK) return st;
   return finish_out(g, pairs, d, 2 * count, flags);
+}
+
+sst_status sst_degree_order_map(sst_graph *g, uint32_t *map, uint32_t flags) {
+  CHECK_G(g);
+  if (!map) return SST_EINVAL;
+  sst_status st = is_dev(flags) ? SST_OK : io_begin(g, (uint64_t)g->n * 4 + 256);
+  if (st != SST_OK) return st;
+  uint32_t *d = nullptr;
+  st = stage_out(g, map, g->n, flags, &d);
+  if (st != SST_OK) return st;
+  st = sst::degree_order_map(g, d);
+  if (st != SST_OK) return st;
+  return finish_out(g, map, d, g->n, flags);
+}
+
+sst_status sst_rewrite_graph(sst_graph *g, const uint32_t *map, uint32_t flags,
+                             sst_graph **out) {
+  CHECK_G(g);
+  if (!map || !out) return SST_EINVAL;
+  *out = nullptr;
+  if (g->n != g->width) {
+    set_error_message("rewrite_graph needs as many rows as columns");
+    return SST_EINVAL;
+  }
+  sst_status st = is_dev(flags) ? SST_OK : io_begin(g, (uint64_t)g->n * 4 + 256);
+  if (st != SST_OK) return st;
+  const uint32_t *d = nullptr;
+  st = stage_in(g, map, g->n, flags, &d);
+  if (st != SST_OK) return st;
+  sst_config cfg{};
+  cfg.device = g->device;
+  cfg.hbm_budget_bytes = g->budget;
+  cfg.initial_slots = g->nslots;
+  cfg.upper_root = g->params.upper_root;
+  cfg.lower_root = g->params.lower_root;
+  cfg.grow_fill = g->params.grow_fill;
+  sst_graph *ng = new (std::nothrow) sst_graph();
+  if (!ng) return SST_ENOMEM;
+  st = sst::graph_init(ng, g->n, g->width, &cfg);
+  if (st == SST_OK) st = sst::rewrite_graph(g, d, ng);
+  if (st != SST_OK) {
+    sst::graph_release(ng);
+    delete ng;
+    return st;
+  }
+  *out = ng;
+  return SST_OK;
 }
 
 sst_status sst_common_neighbors_batch(sst_graph *g, const uint32_t *pairs,

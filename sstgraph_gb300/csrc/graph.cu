@@ -861,6 +861,8 @@ sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
   SST_CUDA_TRY(cudaMalloc(&g->d_plan, sizeof(PlanSummary)));
   SST_CUDA_TRY(cudaMalloc(&g->d_err, sizeof(unsigned long long)));
   SST_CUDA_TRY(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned long long), g->stream));
+  g->arena.err = g->d_err;
+  g->work.err = g->d_err;
   SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
   return SST_OK;
 }
@@ -1120,7 +1122,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   SST_CUDA_TRY(cudaGetLastError());
   PlanSummary ps = *g->h_plan;
   if (ps.apply_err) {
-    set_error_message("internal error: %llu staged ranks out of range",
+    set_error_message("internal error: %llu failed device checks (staging rank out of range or scan look-back wait ran out)",
                       (unsigned long long)ps.apply_err);
     return SST_EDEVICE;
   }
@@ -1312,6 +1314,76 @@ sst_status update_batches(sst_graph *g, const uint32_t *d_pairs,
   return st;
 }
 
+// ------------------------------------------------------------ relabelling
+// degree_order_map / rewrite_graph of SparseMatrix.hpp:737-766: vertices
+// ranked by (degree, id) descending (std::greater on the pair, so among equal
+// degrees the larger id comes first); the rewrite inserts every edge with
+// both ends relabelled.
+namespace {
+__global__ void k_degkey(const uint32_t *__restrict__ deg, uint32_t n,
+                         uint64_t *__restrict__ keys) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n) keys[v] = ((uint64_t)(0xFFFFFFFFu - deg[v]) << 32) | (0xFFFFFFFFu - v);
+}
+__global__ void k_rank_to_map(const uint64_t *__restrict__ sorted, uint32_t n,
+                              uint32_t *__restrict__ map) {
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) map[0xFFFFFFFFu - (uint32_t)sorted[r]] = r;
+}
+__global__ void k_csr_to_pairs(const uint64_t *__restrict__ off,
+                               const uint32_t *__restrict__ cols, uint32_t n,
+                               uint32_t *__restrict__ pairs);
+__global__ void k_relabel_pairs(uint32_t *__restrict__ pairs, uint64_t m,
+                                const uint32_t *__restrict__ map) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  pairs[2 * i] = map[pairs[2 * i]];
+  pairs[2 * i + 1] = map[pairs[2 * i + 1]];
+}
+}  // namespace
+
+sst_status degree_order_map(sst_graph *g, uint32_t *d_map) {
+  cudaStream_t s = g->stream;
+  uint32_t n = g->n;
+  if (n == 0) return SST_OK;
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve((uint64_t)n * 16 + radix_sort_scratch_bytes(n) + 8192));
+  uint64_t *keys = g->arena.take<uint64_t>(n), *tmp = g->arena.take<uint64_t>(n);
+  SST_LAUNCH(k_degkey, blocks_for(n), kTB, 0, s, g->d_deg, n, keys);
+  uint64_t *sorted = keys;
+  SST_CUDA_TRY(radix_sort_u64(keys, tmp, n, 64, g->arena, s, &sorted));
+  SST_LAUNCH(k_rank_to_map, blocks_for(n), kTB, 0, s, sorted, n, d_map);
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+sst_status rewrite_graph(sst_graph *g, const uint32_t *d_map, sst_graph *out) {
+  cudaStream_t s = g->stream;
+  uint32_t n = g->n;
+  uint64_t m = g->m;
+  if (m == 0) return SST_OK;
+  uint64_t *off = nullptr;
+  uint32_t *cols = nullptr, *pairs = nullptr;
+  SST_CUDA_TRY(cudaMallocAsync(&off, ((uint64_t)n + 1) * 8, s));
+  SST_CUDA_TRY(cudaMallocAsync(&cols, m * 4, s));
+  SST_CUDA_TRY(cudaMallocAsync(&pairs, m * 8, s));
+  sst_status st = to_csr(g, off, cols);
+  if (st == SST_OK) {
+    SST_LAUNCH(k_csr_to_pairs, warp_blocks(n), kTB, 0, s, off, cols, n, pairs);
+    SST_LAUNCH(k_relabel_pairs, blocks_for(m), kTB, 0, s, pairs, m, d_map);
+    SST_CUDA_TRY(cudaStreamSynchronize(s));
+    const uint64_t chunk = 1ull << 25;
+    for (uint64_t first = 0; first < m && st == SST_OK; first += chunk)
+      st = update_batch(out, pairs + 2 * first, std::min(chunk, m - first), true, nullptr);
+    cudaStreamSynchronize(out->stream);
+  }
+  cudaFreeAsync(pairs, s);
+  cudaFreeAsync(cols, s);
+  cudaFreeAsync(off, s);
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  return st;
+}
+
 // Complete the graph's stream and report a staging-rank error left by an
 // earlier batch (device-pointer updates do not wait for it).
 sst_status sync_checked(sst_graph *g) {
@@ -1319,7 +1391,7 @@ sst_status sync_checked(sst_graph *g) {
                                cudaMemcpyDeviceToHost, g->stream));
   SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
   if (g->h_plan->apply_err) {
-    set_error_message("internal error: %llu staged ranks out of range",
+    set_error_message("internal error: %llu failed device checks (staging rank out of range or scan look-back wait ran out)",
                       (unsigned long long)g->h_plan->apply_err);
     return SST_EDEVICE;
   }

@@ -97,6 +97,8 @@ sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,
 sst_status update_batches(sst_graph *g, const uint32_t *d_pairs,
                           const uint64_t *d_boff, const uint8_t *d_ops,
                           uint32_t nb, uint64_t N, uint64_t *n_invalid);
+sst_status degree_order_map(sst_graph *g, uint32_t *d_map);
+sst_status rewrite_graph(sst_graph *g, const uint32_t *d_map, sst_graph *out);
 sst_status build_from_csr(sst_graph *g, const uint64_t *d_off,
                           const uint32_t *d_cols);
 sst_status has_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,

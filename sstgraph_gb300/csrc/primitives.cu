@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <string>
@@ -67,7 +68,12 @@ void drain(bool wait) {
 }
 }  // namespace
 
-bool profiling() { return g_prof_on; }
+std::string g_prof_filter;  // profile only kernels whose name contains it
+
+bool profiling(const char *name) {
+  if (!g_prof_on) return false;
+  return g_prof_filter.empty() || strstr(name, g_prof_filter.c_str()) != nullptr;
+}
 
 cudaEvent_t prof_begin(cudaStream_t s) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -84,10 +90,11 @@ void prof_end(const char *name, cudaEvent_t start, cudaStream_t s) {
   if (g_pending.size() > 4096) drain(false);
 }
 
-void profile_start() {
+void profile_start(const char *filter) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
   drain(true);
   g_totals.clear();
+  g_prof_filter = filter ? filter : "";
   g_prof_on = true;
 }
 

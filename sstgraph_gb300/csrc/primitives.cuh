@@ -15,14 +15,14 @@ uint64_t launches();
 // Kernel profiler: while enabled, every launch is bracketed by a pair of
 // CUDA events on its own stream; profile_collect() folds the elapsed times
 // per kernel name.
-bool profiling();
+bool profiling(const char *kernel_name);
 cudaEvent_t prof_begin(cudaStream_t s);
 void prof_end(const char *name, cudaEvent_t start, cudaStream_t s);
 
 #define SST_LAUNCH(kernel, grid, block, smem, stream, ...)                    \
   do {                                                                        \
-    cudaEvent_t _sst_ev = ::sst::profiling() ? ::sst::prof_begin(stream)      \
-                                             : nullptr;                       \
+    cudaEvent_t _sst_ev =                                                     \
+        ::sst::profiling(#kernel) ? ::sst::prof_begin(stream) : nullptr;      \
     kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);               \
     ::sst::note_launch();                                                     \
     if (_sst_ev) ::sst::prof_end(#kernel, _sst_ev, stream);                   \
@@ -54,10 +54,34 @@ struct Arena {
     cap = want;
     return cudaSuccess;
   }
+  // tile status words of the single-pass scan (16 B per tile), kept apart
+  // from the bump memory so stale tags come only from earlier scans; each
+  // scan tags its words with a fresh epoch
+  uint4 *status = nullptr;
+  uint64_t status_cap = 0;
+  unsigned long long epoch = 0;
+  unsigned long long *err = nullptr;  // counts look-back waits that ran out
+
+  cudaError_t reserve_status(uint64_t tiles) {
+    if (tiles <= status_cap) return cudaSuccess;
+    if (status) cudaFree(status);
+    status = nullptr;
+    status_cap = 0;
+    uint64_t want = tiles + tiles / 4 + 64;
+    cudaError_t e = cudaMalloc(&status, want * sizeof(uint4));
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(status, 0, want * sizeof(uint4));
+    if (e != cudaSuccess) return e;
+    status_cap = want;
+    return cudaSuccess;
+  }
   void release() {
     if (base) cudaFree(base);
     base = nullptr;
     cap = used = 0;
+    if (status) cudaFree(status);
+    status = nullptr;
+    status_cap = 0;
   }
   void reset() { used = 0; }
   template <typename T> T *take(size_t count) {
@@ -176,6 +200,92 @@ __global__ void k_scan_apply(const T *__restrict__ in, T *__restrict__ out,
   }
 }
 
+// Single-pass scan with decoupled look-back (Merrill & Garland 2016): each
+// tile publishes its aggregate, then its inclusive prefix once the prefix of
+// the tiles before it is known, so one launch scans the whole array.  Tiles
+// rely on blocks being dispatched in index order; every wait on a
+// predecessor is bounded and counts a failure in *err instead of hanging.
+constexpr unsigned long long kScanAgg = 1, kScanIncl = 2;
+constexpr uint32_t kLookbackSpins = 1u << 22;
+
+template <typename T>
+__device__ __forceinline__ void tile_publish(uint4 *st, unsigned long long tag,
+                                             T v) {
+  volatile unsigned long long *w = reinterpret_cast<volatile unsigned long long *>(st);
+  unsigned long long bits = 0;
+  memcpy(&bits, &v, sizeof(T));
+  w[1] = bits;
+  __threadfence();
+  w[0] = tag;
+}
+
+template <typename T, typename Op>
+__global__ void k_scan_single(const T *__restrict__ in, T *__restrict__ out,
+                              uint64_t n, T identity, Op op, bool reverse,
+                              bool exclusive, T *__restrict__ total_out,
+                              const uint32_t *__restrict__ d_n, uint4 *status,
+                              unsigned long long epoch,
+                              unsigned long long *err) {
+  if (d_n && *d_n < n) n = *d_n;
+  const uint64_t tile = blockIdx.x;
+  uint64_t tile0 = tile * kScanTile;
+  T vals[kScanItems];
+  T acc = identity;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    uint64_t i = tile0 + (uint64_t)threadIdx.x * kScanItems + k;
+    vals[k] = i < n ? in[reverse ? n - 1 - i : i] : identity;
+    acc = op(acc, vals[k]);
+  }
+  T total;
+  T run = block_exclusive(acc, identity, op, &total);
+  __shared__ T s_prefix;
+  if (threadIdx.x == 0) {
+    const unsigned long long tagA = (epoch << 2) | kScanAgg;
+    const unsigned long long tagI = (epoch << 2) | kScanIncl;
+    T prefix = identity;
+    if (tile == 0) {
+      tile_publish(status, tagI, total);
+    } else {
+      tile_publish(status + tile, tagA, total);
+      for (int64_t j = (int64_t)tile - 1; j >= 0; j--) {
+        volatile unsigned long long *w =
+            reinterpret_cast<volatile unsigned long long *>(status + j);
+        unsigned long long tag = w[0];
+        uint32_t spins = 0;
+        while ((tag >> 2) != epoch && spins < kLookbackSpins) {
+          __nanosleep(64);
+          tag = w[0];
+          spins++;
+        }
+        if ((tag >> 2) != epoch) {
+          if (err) atomicAdd(err, 1ull);
+          break;
+        }
+        __threadfence();
+        unsigned long long bits = w[1];
+        T v;
+        memcpy(&v, &bits, sizeof(T));
+        prefix = op(v, prefix);
+        if ((tag & 3) == kScanIncl) break;
+      }
+      tile_publish(status + tile, tagI, op(prefix, total));
+    }
+    s_prefix = prefix;
+  }
+  __syncthreads();
+  run = op(s_prefix, run);
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    uint64_t i = tile0 + (uint64_t)threadIdx.x * kScanItems + k;
+    T nxt = op(run, vals[k]);
+    if (i < n) out[reverse ? n - 1 - i : i] = exclusive ? run : nxt;
+    run = nxt;
+  }
+  if (total_out && tile == gridDim.x - 1 && threadIdx.x == 0)
+    *total_out = op(s_prefix, total);
+}
+
 // Scan of n elements (in may equal out).  total_out (device, may be null)
 // receives the reduction of all n elements.  With d_n (device, may be null)
 // only the first min(n, *d_n) elements are scanned; n sizes the launch.
@@ -193,6 +303,13 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
     SST_LAUNCH((k_scan_apply<T, Op>), 1, kScanThreads, 0, s, in, out, n,
                identity, op, reverse, exclusive, (const T *)nullptr, total_out,
                d_n);
+    return cudaGetLastError();
+  }
+  if (sizeof(T) <= 8 && arena.reserve_status(blocks) == cudaSuccess) {
+    arena.epoch++;
+    SST_LAUNCH((k_scan_single<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
+               out, n, identity, op, reverse, exclusive, total_out, d_n,
+               arena.status, arena.epoch, arena.err);
     return cudaGetLastError();
   }
   T *sums = arena.take<T>(blocks);

@@ -21,6 +21,8 @@ Fixtures (all small, npz):
                         5 remove batches of sampled edges: degrees and a
                         sha256 of the CSR after every batch, touch_all_sum,
                         common_neighbors on sampled pairs, has() on queries
+  degree_order.npz      degree_order_map() of that base graph and a sha256 of
+                        rewrite_graph(map)'s CSR (SparseMatrix.hpp:737-766)
   examples_mtx.npz      examples/*.mtx through the reference loader
                         (helpers.hpp:379-529): symmetrised edge lists and the
                         CSR of the graph built from them
@@ -111,6 +113,17 @@ def main(ref_root):
         M=np.array(ms, np.uint64), deg_final=degs[-1], deg_base=degs[0],
         touch_all_sum=np.uint64(g.touch_all_sum()), cn_pairs=pairs, cn_full=cn_full,
         cn_early=cn_early, has_q=q, has_ans=has)
+
+    # --- degree-ordered relabelling of the scale-16 base graph
+    #     (SparseMatrix.hpp:737-766)
+    g0 = oracle.RefGraph(n)
+    g0.insert_batch(base)
+    dmap = g0.degree_order_map()
+    rg = g0.rewrite_graph(dmap)
+    roff, rcols = rg.csr()
+    np.savez_compressed(os.path.join(HERE, "degree_order.npz"), map=dmap,
+                        digest=np.array(csr_digest(roff, rcols)),
+                        touch_all_sum=np.uint64(rg.touch_all_sum()))
 
     # --- bundled examples through the reference loader
     ex = {}

@@ -86,6 +86,22 @@ def test_rmat16_stream_digests(sg):
     assert np.array_equal(g.has_batch(d["has_q"]), d["has_ans"])
 
 
+def test_degree_order_relabel(sg):
+    d = load("degree_order.npz")
+    n = 1 << 16
+    g = sg.SparseMatrixV(n)
+    g.insert_batch(oracle.symmetrize(oracle.rmat(16, 16 * n, seed=1)))
+    m = g.degree_order_map()
+    assert np.array_equal(m, d["map"])
+    r = g.rewrite_graph(m)
+    assert digest(*r.csr()) == str(d["digest"])
+    assert r.touch_all_sum() == int(d["touch_all_sum"])
+    # PageRank on the relabelled graph is the same vector, permuted
+    pr = sg.PR_S(g, 10)
+    prr = sg.PR_S(r, 10)
+    assert np.max(np.abs(prr[m] - pr)) <= 1e-12 * np.max(pr)
+
+
 def test_examples_mtx(sg):
     d = load("examples_mtx.npz")
     for key in ("star", "johnson8_2_4"):

@@ -69,6 +69,21 @@ def test_rmat16_stream_digests():
     assert [int(g.has(int(a), int(b))) for a, b in d["has_q"]] == list(d["has_ans"])
 
 
+def test_degree_order_relabel():
+    d = load("degree_order.npz")
+    n = 1 << 16
+    o = oracle.OracleGraph(n)
+    o.insert_batch(oracle.symmetrize(oracle.rmat(16, 16 * n, seed=1)))
+    m = oracle.degree_order_map(o.degrees())
+    assert np.array_equal(m, d["map"])
+    off, cols = o.csr()
+    rows = np.repeat(np.arange(n, dtype=np.uint32), np.diff(off).astype(np.int64))
+    r = oracle.OracleGraph(n)
+    r.insert_batch(oracle.relabel(np.stack([rows, cols], 1), m))
+    assert digest(*r.csr()) == str(d["digest"])
+    assert r.touch_all_sum() == int(d["touch_all_sum"])
+
+
 def test_examples_mtx():
     d = load("examples_mtx.npz")
     for key in ("star", "johnson8_2_4"):
