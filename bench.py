@@ -52,7 +52,9 @@ def args_parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--pr-iters", type=int, default=10)
     ap.add_argument("--batched-batches", type=int, default=128)
-    ap.add_argument("--only", default="all", choices=["all", "pagerank", "bfs", "batched"],
+    ap.add_argument("--serve-requests", type=int, default=400)
+    ap.add_argument("--serve-rate", type=float, default=300.0)
+    ap.add_argument("--only", default="all", choices=["all", "pagerank", "bfs", "batched", "serving"],
                     help="run one traversal on the base graph (profiling cases)")
     return ap.parse_args()
 
@@ -362,11 +364,77 @@ def main():
                 "same_graph": same,
                 "check": "M and touch_all_sum of both copies"}
 
+    def measure_serving():
+        """Mixed request stream through the serving loop (sst_server_*):
+        Poisson arrivals, 70% update batches (log-normal sizes, median 1e3),
+        30% queries split evenly between single-source BFS, a 5-iteration
+        PageRank refresh and per-vertex triangle counts of 1e4 random
+        vertices, under a 60 GB HBM budget.  Latency = completion - arrival."""
+        rng = np.random.default_rng(31)
+        reqs = []
+        first = 0
+        for i in range(a.serve_requests):
+            r = rng.random()
+            if r < 0.7:
+                sz = int(min(1e5, max(1, rng.lognormal(np.log(1e3), 1.0))))
+                pairs = sg.gen_rmat(a.scale, sz, seed=13, first=first, **RMAT)
+                first += sz
+                kind = "remove" if rng.random() < 0.3 else "insert"
+                reqs.append((kind, pairs))
+            elif r < 0.8:
+                reqs.append(("bfs", int(rng.integers(0, n))))
+            elif r < 0.9:
+                reqs.append(("pagerank", 5))
+            else:
+                reqs.append(("tc", rng.integers(0, n, 10000).astype(np.uint32)))
+        gaps = rng.exponential(1.0 / a.serve_rate, len(reqs))
+        srv = sg.Server(g, query_slots=4, hbm_budget_bytes=60 << 30)
+        t0 = time.perf_counter()
+        arrive = t0 + np.cumsum(gaps)
+        tickets = []
+        for (kind, arg), at in zip(reqs, arrive):
+            now = time.perf_counter()
+            if at > now:
+                time.sleep(at - now)
+            if kind == "insert":
+                t = srv.insert(arg)
+            elif kind == "remove":
+                t = srv.remove(arg)
+            elif kind == "bfs":
+                t = srv.bfs(arg)
+            elif kind == "pagerank":
+                t = srv.pagerank(arg)
+            else:
+                t = srv.tc_vertices(arg)
+            tickets.append((kind, t, arg))
+        lat = {}
+        upd_edges = 0
+        for kind, t, arg in tickets:
+            _, info = srv.wait(t)
+            lat.setdefault(kind, []).append(info["total_ms"])
+            if kind in ("insert", "remove"):
+                upd_edges += len(arg)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        slots = srv.slots
+        srv.close()
+        allv = [x for v in lat.values() for x in v]
+        summ = {k: {"n": len(v), "p50_ms": float(np.percentile(v, 50)),
+                    "p99_ms": float(np.percentile(v, 99))} for k, v in lat.items()}
+        return {"requests": len(reqs), "rate_per_s": a.serve_rate, "slots": slots,
+                "p50_ms": float(np.percentile(allv, 50)),
+                "p99_ms": float(np.percentile(allv, 99)),
+                "by_kind": summ, "update_edges_per_s": upd_edges / wall,
+                "wall_s": wall, "writer_passes": st["passes"],
+                "hbm_budget_bytes": 60 << 30}
+
     if a.only != "all":
         pr_flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
         res = {"only": a.only, "scale": a.scale, "edges": m0}
         if a.only == "pagerank":
             res["pagerank"] = measure_pagerank()
+        elif a.only == "serving":
+            res["serving"] = measure_serving()
         elif a.only == "batched":
             res["batched"] = measure_batched()
         else:
@@ -473,6 +541,7 @@ def main():
     pagerank["degree_ordered"] = pr_deg
     gr.close()
     bfs = measure_bfs()
+    serving = measure_serving()
 
     # ---- roofline of the update step's dominant kernel
     upd_kernels = {"timed_region": prof, "warmup_all_kernels": prof_all}
@@ -509,6 +578,7 @@ def main():
         "batched_form": batched,
         "pagerank": pagerank,
         "bfs": bfs,
+        "serving": serving,
         "update_kernels": upd_kernels,
     }
     print(json.dumps(line))

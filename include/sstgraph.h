@@ -186,6 +186,60 @@ SST_API sst_status sst_tc(sst_graph *g, uint64_t *total, uint64_t *per_vertex,
 /* TouchAll(g)  test.hpp:476 */
 SST_API sst_status sst_touch_all(sst_graph *g, uint64_t *out);
 
+/* per-vertex triangle counts of listed vertices: out[i] = triangles that
+ * contain vertices[i] (the serving loop's per-vertex TC query) */
+SST_API sst_status sst_tc_vertices(sst_graph *g, const uint32_t *vertices,
+                                   uint64_t k, uint64_t *out, uint32_t flags);
+
+/* ---- serving loop (no reference counterpart: the reference has no
+ *      request loop; this keeps the graph on the device and serves a mixed
+ *      stream) --------------------------------------------------------- */
+typedef struct sst_server sst_server;
+typedef struct sst_server_config {
+  uint32_t query_slots;      /* concurrent queries, each on its own snapshot */
+  uint64_t hbm_budget_bytes; /* live graph + slots must fit (0 = no budget) */
+  uint32_t max_coalesce;     /* update requests fused per pass (0 = all) */
+} sst_server_config;
+
+#define SST_REQ_INSERT 1       /* pairs[n] inserted */
+#define SST_REQ_REMOVE 2       /* pairs[n] removed */
+#define SST_REQ_BFS 3          /* out: int32 depths[rows] from src */
+#define SST_REQ_PAGERANK 4     /* out: double ranks[rows], iters, damping */
+#define SST_REQ_TC_VERTICES 5  /* pairs = n vertex ids, out: uint64 [n] */
+
+typedef struct sst_request {
+  int32_t kind;
+  const uint32_t *pairs; /* update pairs or query vertices (host; copied) */
+  uint64_t n;
+  uint32_t src;
+  uint32_t iters;
+  double damping;
+  void *out; /* host output of a query (written before completion) */
+} sst_request;
+
+typedef struct sst_request_info {
+  sst_status status;
+  uint64_t epoch;  /* update requests applied before the query's snapshot,
+                      or after the update's pass */
+  double queue_ms, run_ms, total_ms;
+} sst_request_info;
+
+/* one writer applies all pending updates per pass as a batched pass; query
+ * slots (as many as query_slots and the HBM budget allow) run queries on
+ * snapshots refreshed between passes, overlapping the writer on the GPU */
+SST_API sst_status sst_server_create(sst_graph *g, const sst_server_config *cfg,
+                                     sst_server **out);
+SST_API sst_status sst_server_slots(sst_server *s, uint32_t *slots);
+SST_API sst_status sst_server_submit(sst_server *s, const sst_request *req,
+                                     uint64_t *ticket);
+/* waits for a request; returns its status and fills info */
+SST_API sst_status sst_server_wait(sst_server *s, uint64_t ticket,
+                                   uint32_t timeout_ms, sst_request_info *info);
+SST_API sst_status sst_server_stats(sst_server *s, uint64_t *epoch,
+                                    uint64_t *passes, uint64_t *update_edges);
+/* finishes queued requests, then stops the threads and frees the slots */
+SST_API sst_status sst_server_destroy(sst_server *s);
+
 /* ---- generators (device; same streams as the CPU oracle) ------------ */
 /* RMAT edges first..first+count-1 of stream `seed`, 2^scale vertices */
 SST_API sst_status sst_gen_rmat(uint32_t scale, double a, double b, double c,

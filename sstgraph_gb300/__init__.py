@@ -45,6 +45,27 @@ class sst_config(ctypes.Structure):
                 ("grow_fill", ctypes.c_float)]
 
 
+class sst_server_config(ctypes.Structure):
+    _fields_ = [("query_slots", ctypes.c_uint32),
+                ("hbm_budget_bytes", ctypes.c_uint64),
+                ("max_coalesce", ctypes.c_uint32)]
+
+
+class sst_request(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("pairs", ctypes.c_void_p),
+                ("n", ctypes.c_uint64), ("src", ctypes.c_uint32),
+                ("iters", ctypes.c_uint32), ("damping", ctypes.c_double),
+                ("out", ctypes.c_void_p)]
+
+
+class sst_request_info(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("epoch", ctypes.c_uint64),
+                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double)]
+
+
+REQ_INSERT, REQ_REMOVE, REQ_BFS, REQ_PAGERANK, REQ_TC_VERTICES = 1, 2, 3, 4, 5
+
 # name -> (restype, argtypes); mirrors include/sstgraph.h
 _vp, _u32, _u64, _i32, _dbl = (ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64,
                                ctypes.c_int32, ctypes.c_double)
@@ -90,6 +111,14 @@ SIGNATURES = {
     "sst_kernel_launches": (_u64, []),
     "sst_raw_state": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64)]),
     "sst_pagerank_noalloc": (_i32, [_vp, _u32, _dbl, _vp]),
+    "sst_tc_vertices": (_i32, [_vp, _vp, _u64, _vp, _u32]),
+    "sst_server_create": (_i32, [_vp, ctypes.POINTER(sst_server_config), ctypes.POINTER(_vp)]),
+    "sst_server_slots": (_i32, [_vp, ctypes.POINTER(_u32)]),
+    "sst_server_submit": (_i32, [_vp, ctypes.POINTER(sst_request), ctypes.POINTER(_u64)]),
+    "sst_server_wait": (_i32, [_vp, _u64, _u32, ctypes.POINTER(sst_request_info)]),
+    "sst_server_stats": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64),
+                                ctypes.POINTER(_u64)]),
+    "sst_server_destroy": (_i32, [_vp]),
     "sst_profile_start": (_i32, [ctypes.c_char_p]),
     "sst_profile_collect": (_i32, [ctypes.c_char_p, _u64]),
 }
@@ -467,6 +496,86 @@ def TC(g: SparseMatrixV, per_vertex: bool = False):
         return total.value, pv
     _check(lib().sst_tc(g.handle, ctypes.byref(total), None, HOST_PTR))
     return total.value
+
+
+def TC_vertices(g: SparseMatrixV, vertices) -> np.ndarray:
+    """triangles containing each listed vertex"""
+    v = np.ascontiguousarray(vertices, np.uint32)
+    out = np.empty(len(v), np.uint64)
+    _check(lib().sst_tc_vertices(g.handle, ctypes.c_void_p(v.ctypes.data), len(v),
+                                 ctypes.c_void_p(out.ctypes.data), HOST_PTR))
+    return out
+
+
+class Server:
+    """Serving loop over a device-resident graph (include/sstgraph.h,
+    sst_server_*): submit updates and queries, wait for results."""
+
+    def __init__(self, g: SparseMatrixV, query_slots: int = 2,
+                 hbm_budget_bytes: int = 0, max_coalesce: int = 0):
+        self.g = g
+        cfg = sst_server_config(query_slots, hbm_budget_bytes, max_coalesce)
+        h = ctypes.c_void_p()
+        _check(lib().sst_server_create(g.handle, ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._keep = {}
+        s = ctypes.c_uint32()
+        _check(lib().sst_server_slots(h, ctypes.byref(s)))
+        self.slots = s.value
+
+    def _submit(self, req, keep):
+        t = ctypes.c_uint64()
+        _check(lib().sst_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)))
+        self._keep[t.value] = keep
+        return t.value
+
+    def insert(self, pairs) -> int:
+        p = np.ascontiguousarray(np.asarray(pairs, np.uint32).reshape(-1, 2))
+        return self._submit(sst_request(REQ_INSERT, p.ctypes.data, len(p), 0, 0, 0.0, None), (p, None))
+
+    def remove(self, pairs) -> int:
+        p = np.ascontiguousarray(np.asarray(pairs, np.uint32).reshape(-1, 2))
+        return self._submit(sst_request(REQ_REMOVE, p.ctypes.data, len(p), 0, 0, 0.0, None), (p, None))
+
+    def bfs(self, src) -> int:
+        out = np.empty(self.g.rows, np.int32)
+        return self._submit(sst_request(REQ_BFS, None, 0, src, 0, 0.0, out.ctypes.data), (None, out))
+
+    def pagerank(self, iters=5, damping=0.85) -> int:
+        out = np.empty(self.g.rows, np.float64)
+        return self._submit(sst_request(REQ_PAGERANK, None, 0, 0, iters, damping,
+                                        out.ctypes.data), (None, out))
+
+    def tc_vertices(self, vertices) -> int:
+        v = np.ascontiguousarray(vertices, np.uint32)
+        out = np.empty(len(v), np.uint64)
+        return self._submit(sst_request(REQ_TC_VERTICES, v.ctypes.data, len(v), 0, 0, 0.0,
+                                        out.ctypes.data), (v, out))
+
+    def wait(self, ticket, timeout_ms=600000):
+        """-> (result array or None, info dict)"""
+        info = sst_request_info()
+        st = lib().sst_server_wait(self._h, ticket, timeout_ms, ctypes.byref(info))
+        keep = self._keep.pop(ticket, (None, None))
+        _check(st)
+        return keep[1], {"epoch": info.epoch, "queue_ms": info.queue_ms,
+                         "run_ms": info.run_ms, "total_ms": info.total_ms}
+
+    def stats(self):
+        e, p, u = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib().sst_server_stats(self._h, ctypes.byref(e), ctypes.byref(p), ctypes.byref(u)))
+        return {"epoch": e.value, "passes": p.value, "update_edges": u.value}
+
+    def close(self):
+        if self._h:
+            lib().sst_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def TouchAll(g: SparseMatrixV) -> int:

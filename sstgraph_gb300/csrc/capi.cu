@@ -475,6 +475,23 @@ sst_status sst_sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
   return finish_out(g, pairs, d, 2 * count, flags);
 }
 
+sst_status sst_tc_vertices(sst_graph *g, const uint32_t *vertices, uint64_t k,
+                           uint64_t *out, uint32_t flags) {
+  CHECK_G(g);
+  if (k && (!vertices || !out)) return SST_EINVAL;
+  sst_status st = is_dev(flags) ? SST_OK : io_begin(g, k * 12 + 512);
+  if (st != SST_OK) return st;
+  const uint32_t *dv = nullptr;
+  st = stage_in(g, vertices, k, flags, &dv);
+  if (st != SST_OK) return st;
+  uint64_t *dout = nullptr;
+  st = stage_out(g, out, k, flags, &dout);
+  if (st != SST_OK) return st;
+  st = sst::tc_vertices(g, dv, k, dout);
+  if (st != SST_OK) return st;
+  return finish_out(g, out, dout, k, flags);
+}
+
 sst_status sst_degree_order_map(sst_graph *g, uint32_t *map, uint32_t flags) {
   CHECK_G(g);
   if (!map) return SST_EINVAL;

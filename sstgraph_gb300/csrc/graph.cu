@@ -157,6 +157,7 @@ __global__ void k_pack(const uint64_t *__restrict__ keys,
   if (i >= b || !flag[i]) return;
   uint64_t k = keys[i];
   uint32_t j = pos[i];
+  if (j >= b) return;  // positions come from a scan: never trust them blindly
   p_ul[j] = ((k >> dbits) << 32) | leaf[i];
   p_x[j] = (uint32_t)(k & ((1ull << dbits) - 1));
 }
@@ -177,8 +178,8 @@ __global__ void k_group_start(const uint32_t *__restrict__ gflag,
                               uint64_t b, uint32_t *__restrict__ g_start) {
   uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= b) return;
-  if (gflag[j]) g_start[gpos[j]] = (uint32_t)j;
-  if (j == 0) g_start[*d_ngroups] = *d_nitems;
+  if (gflag[j] && gpos[j] < b) g_start[gpos[j]] = (uint32_t)j;
+  if (j == 0 && *d_ngroups <= b) g_start[*d_ngroups] = *d_nitems;
 }
 
 // ---------------------------------------------------------------- step 6
@@ -430,8 +431,8 @@ __global__ void k_emit(const uint32_t *__restrict__ mflag,
                        uint32_t *__restrict__ task_group) {
   uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= gmax) return;
-  if (mflag[gid]) merge_list[mpos[gid]] = (uint32_t)gid;
-  if (tflag[gid]) task_group[tpos[gid]] = (uint32_t)gid;
+  if (mflag[gid] && mpos[gid] < gmax) merge_list[mpos[gid]] = (uint32_t)gid;
+  if (tflag[gid] && tpos[gid] < gmax) task_group[tpos[gid]] = (uint32_t)gid;
 }
 
 // ---------------------------------------------------------------- step 8

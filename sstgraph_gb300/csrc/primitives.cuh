@@ -62,7 +62,10 @@ struct Arena {
   unsigned long long epoch = 0;
   unsigned long long *err = nullptr;  // counts look-back waits that ran out
 
-  cudaError_t reserve_status(uint64_t tiles) {
+  // the words are zeroed on the scan's own stream (the library's streams do
+  // not synchronise with the legacy default stream), so the first scan never
+  // sees uninitialised tags
+  cudaError_t reserve_status(uint64_t tiles, cudaStream_t s) {
     if (tiles <= status_cap) return cudaSuccess;
     if (status) cudaFree(status);
     status = nullptr;
@@ -70,7 +73,7 @@ struct Arena {
     uint64_t want = tiles + tiles / 4 + 64;
     cudaError_t e = cudaMalloc(&status, want * sizeof(uint4));
     if (e != cudaSuccess) return e;
-    e = cudaMemset(status, 0, want * sizeof(uint4));
+    e = cudaMemsetAsync(status, 0, want * sizeof(uint4), s);
     if (e != cudaSuccess) return e;
     status_cap = want;
     return cudaSuccess;
@@ -305,7 +308,7 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
                d_n);
     return cudaGetLastError();
   }
-  if (sizeof(T) <= 8 && arena.reserve_status(blocks) == cudaSuccess) {
+  if (sizeof(T) <= 8 && arena.reserve_status(blocks, s) == cudaSuccess) {
     arena.epoch++;
     SST_LAUNCH((k_scan_single<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
                out, n, identity, op, reverse, exclusive, total_out, d_n,

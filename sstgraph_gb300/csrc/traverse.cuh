@@ -13,6 +13,9 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping,
 sst_status cc(sst_graph *g, uint32_t *d_labels);
 sst_status bc(sst_graph *g, uint32_t src, double *d_dep);
 sst_status tc(sst_graph *g, uint64_t *total, uint64_t *d_per_vertex);
+sst_status tc_vertices(sst_graph *g, const uint32_t *d_vs, uint64_t k,
+                       uint64_t *d_out);
+sst_status graph_copy_into(sst_graph *dst, sst_graph *src);
 sst_status common_neighbors_batch(sst_graph *g, const uint32_t *d_pairs,
                                   uint64_t n, bool early_end,
                                   uint64_t *d_out);
