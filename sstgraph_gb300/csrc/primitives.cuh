@@ -54,7 +54,7 @@ struct Arena {
     cap = want;
     return cudaSuccess;
   }
-  // tile status words of the single-pass scan (16 B per tile), kept apart
+  // tile status words of the single-pass scan (32 B per tile), kept apart
   // from the bump memory so stale tags come only from earlier scans; each
   // scan tags its words with a fresh epoch
   uint4 *status = nullptr;
@@ -71,9 +71,9 @@ struct Arena {
     status = nullptr;
     status_cap = 0;
     uint64_t want = tiles + tiles / 4 + 64;
-    cudaError_t e = cudaMalloc(&status, want * sizeof(uint4));
+    cudaError_t e = cudaMalloc(&status, 2 * want * sizeof(uint4));
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(status, 0, want * sizeof(uint4), s);
+    e = cudaMemsetAsync(status, 0, 2 * want * sizeof(uint4), s);
     if (e != cudaSuccess) return e;
     status_cap = want;
     return cudaSuccess;
@@ -211,13 +211,19 @@ __global__ void k_scan_apply(const T *__restrict__ in, T *__restrict__ out,
 constexpr unsigned long long kScanAgg = 1, kScanIncl = 2;
 constexpr uint32_t kLookbackSpins = 1u << 22;
 
+// A tile's status is two 16-byte words: {tag, aggregate} and {inclusive
+// prefix, -}.  The aggregate and the inclusive prefix live in separate
+// fields, each written before the tag that announces it and never changed
+// afterwards, so a reader takes the field that matches the tag it saw (a
+// shared field could be overwritten between the reader's tag and value
+// loads).
 template <typename T>
 __device__ __forceinline__ void tile_publish(uint4 *st, unsigned long long tag,
                                              T v) {
   volatile unsigned long long *w = reinterpret_cast<volatile unsigned long long *>(st);
   unsigned long long bits = 0;
   memcpy(&bits, &v, sizeof(T));
-  w[1] = bits;
+  w[(tag & 3) == kScanIncl ? 2 : 1] = bits;
   __threadfence();
   w[0] = tag;
 }
@@ -250,10 +256,10 @@ __global__ void k_scan_single(const T *__restrict__ in, T *__restrict__ out,
     if (tile == 0) {
       tile_publish(status, tagI, total);
     } else {
-      tile_publish(status + tile, tagA, total);
+      tile_publish(status + 2 * tile, tagA, total);
       for (int64_t j = (int64_t)tile - 1; j >= 0; j--) {
         volatile unsigned long long *w =
-            reinterpret_cast<volatile unsigned long long *>(status + j);
+            reinterpret_cast<volatile unsigned long long *>(status + 2 * j);
         unsigned long long tag = w[0];
         uint32_t spins = 0;
         while ((tag >> 2) != epoch && spins < kLookbackSpins) {
@@ -266,13 +272,14 @@ __global__ void k_scan_single(const T *__restrict__ in, T *__restrict__ out,
           break;
         }
         __threadfence();
-        unsigned long long bits = w[1];
+        const bool incl = (tag & 3) == kScanIncl;
+        unsigned long long bits = incl ? w[2] : w[1];
         T v;
         memcpy(&v, &bits, sizeof(T));
         prefix = op(v, prefix);
-        if ((tag & 3) == kScanIncl) break;
+        if (incl) break;
       }
-      tile_publish(status + tile, tagI, op(prefix, total));
+      tile_publish(status + 2 * tile, tagI, op(prefix, total));
     }
     s_prefix = prefix;
   }
