@@ -545,8 +545,7 @@ def main():
 
     # ---- roofline of the update step's dominant kernel
     upd_kernels = {"timed_region": prof, "warmup_all_kernels": prof_all}
-    roofline = update_roofline(prof, prof_all, plan[a.warmup:], hbm_peak, peak_kind,
-                               g_bits=(a.scale + 1) + a.scale)
+    roofline = update_roofline(prof, prof_all, hbm_peak, peak_kind)
 
     # ---- CPU baseline (bounded sample, rank 0 only)
     cpu = None
@@ -584,18 +583,17 @@ def main():
     print(json.dumps(line))
 
 
-def update_roofline(prof, prof_all, timed_plan, hbm_peak, peak_kind, g_bits):
+def update_roofline(prof, prof_all, hbm_peak, peak_kind):
     """Roofline of the update step's dominant kernel from its live event
     timings in the timed region (its share from the all-kernel warm-up).
 
-    Algorithmic bytes over the timed batches (b = keys of a batch, insert and
-    remove batches alike):
-      k_scatter (radix pass)  16 B per key per pass (read + write a 8 B key);
-                              a batch above 2048 keys takes ceil(bits/8)
-                              passes, smaller ones sort in one CTA
-      k_hist (radix pass)      8 B per key per pass
-      k_locate                16 B per key (sorted key in, flag + leaf out)
-      k_make_keys             16 B per key (pair in, key out)
+    Algorithmic bytes are declared by each launch site at its launch size
+    (what the kernel must read and write, independent of caching):
+      radix histogram pass   8 B per key + 4 B per block-digit counter
+      radix scatter pass     16 B per key (24 B with values) + counters
+      one-CTA sort           16 B per key (24 B with values)
+      scan                   2 x element size per element
+    achieved = declared bytes / event time, summed over the timed launches.
     """
     name, t = max(prof.items(), key=lambda kv: kv[1]["ms"])
     base = name.strip("()").split("<")[0]
@@ -603,16 +601,12 @@ def update_roofline(prof, prof_all, timed_plan, hbm_peak, peak_kind, g_bits):
     out = {"bound": "hbm", "kernel": base, "launches": t["launches"],
            "ms_total": t["ms"], "share_of_step_kernel_time": share,
            "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind, "traffic": None}
-    passes = -(-g_bits // 8)
-    keys = 2 * sum(timed_plan)
-    big = 2 * sum(b for b in timed_plan if b > 2048)
-    per = {"k_scatter": 16 * passes * big, "k_hist": 8 * passes * big,
-           "k_locate": 16 * keys, "k_make_keys": 16 * keys}
-    if base in per:
-        byts = per[base]
+    byts = t.get("bytes", 0)
+    if byts:
         ach = byts / (t["ms"] / 1e3) / 1e9
         out.update({"achieved": ach, "frac": ach / hbm_peak,
-                    "algorithmic_bytes_per_launch": byts / t["launches"]})
+                    "algorithmic_bytes_per_launch": byts / t["launches"],
+                    "avg_launch_us": 1e3 * t["ms"] / t["launches"]})
     else:
         out.update({"achieved": None, "frac": None})
     return out

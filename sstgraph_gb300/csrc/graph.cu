@@ -652,10 +652,10 @@ __device__ __forceinline__ uint64_t task_new_base(const Tasks &t, uint64_t tau,
 }
 
 // warp per destination leaf: even redistribution of the staged elements
-__global__ void k_scatter(DGraph g, Tasks t, uint32_t ntasks,
-                          uint64_t ndst_total,
-                          const uint64_t *__restrict__ class_start,
-                          const uint32_t *__restrict__ stage) {
+__global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
+                               uint64_t ndst_total,
+                               const uint64_t *__restrict__ class_start,
+                               const uint32_t *__restrict__ stage) {
   uint64_t d = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (d >= ndst_total) return;
@@ -1056,7 +1056,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   // 1-2: keys and sort
   const uint64_t *sorted = presorted;
   if (!presorted) {
-    SST_LAUNCH(k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n, g->width,
+    // pair in (8 B), key out (8 B)
+    SST_LAUNCH_B(16 * b, k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n, g->width,
                dbits, insert, keys,
                reinterpret_cast<unsigned long long *>(&P->invalid));
     uint64_t *out = keys;
@@ -1064,8 +1065,9 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     sorted = out;
   }
   // 3-5: locate, pack, group
-  SST_LAUNCH(k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg, insert,
-             flag, leaf);
+  // sorted key in (8 B), flag and leaf out (8 B)
+  SST_LAUNCH_B(16 * b, k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg,
+               insert, flag, leaf);
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(flag, pos, b, 0u, OpAdd{}, true, false,
                                       &P->n_items, A, s)));
   SST_LAUNCH(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,
@@ -1166,7 +1168,10 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
 
   // 9: apply
   if (insert && ps.n_merge)
-    SST_LAUNCH(k_leaf_merge, warp_blocks(ps.n_merge), kTB, 0, s, dg, p_ul, p_x,
+    // each merge rewrites one 128-byte leaf (read + write) and its count
+    // (the merged ids, fewer than 32 per leaf, are not counted)
+    SST_LAUNCH_B(258ull * ps.n_merge, k_leaf_merge,
+               warp_blocks(ps.n_merge), kTB, 0, s, dg, p_ul, p_x,
                g_start, merge_list, ps.n_merge);
   if (ps.n_tasks) {
     if (ps.src_leaves) {
@@ -1182,7 +1187,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
       SST_LAUNCH(k_gather_new, blocks_for(ps.n_items), kTB, 0, s, dg, T,
                  ps.n_tasks, spre, p_ul, p_x, ps.n_items, stage);
     if (ps.dst_leaves)
-      SST_LAUNCH(k_scatter, warp_blocks(ps.dst_leaves), kTB, 0, s, dg, T,
+      SST_LAUNCH(k_task_scatter, warp_blocks(ps.dst_leaves), kTB, 0, s, dg, T,
                  ps.n_tasks, ps.dst_leaves, cstart, stage);
     SST_LAUNCH(k_finalize, blocks_for(ps.n_tasks), kTB, 0, s, dg, T, ps.n_tasks,
                cstart);

@@ -24,10 +24,12 @@ namespace {
 struct Pending {
   const char *name;
   cudaEvent_t a, b;
+  uint64_t bytes;
 };
 struct Totals {
   uint64_t launches = 0;
   double ms = 0;
+  uint64_t bytes = 0;  // declared algorithmic bytes (0 where undeclared)
 };
 std::mutex g_prof_mu;
 bool g_prof_on = false;
@@ -57,6 +59,7 @@ void drain(bool wait) {
       Totals &t = g_totals[p.name];
       t.launches++;
       t.ms += ms;
+      t.bytes += p.bytes;
       g_pool.push_back(p.a);
       g_pool.push_back(p.b);
     } else {
@@ -82,11 +85,12 @@ cudaEvent_t prof_begin(cudaStream_t s) {
   return e;
 }
 
-void prof_end(const char *name, cudaEvent_t start, cudaStream_t s) {
+void prof_end(const char *name, cudaEvent_t start, cudaStream_t s,
+              uint64_t bytes) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
   cudaEvent_t e = take_event();
   cudaEventRecord(e, s);
-  g_pending.push_back({name, start, e});
+  g_pending.push_back({name, start, e, bytes});
   if (g_pending.size() > 4096) drain(false);
 }
 
@@ -107,9 +111,11 @@ std::string profile_collect() {
   bool first = true;
   for (auto &kv : g_totals) {
     char buf[256];
-    snprintf(buf, sizeof(buf), "%s\"%s\": {\"launches\": %llu, \"ms\": %.6f}",
+    snprintf(buf, sizeof(buf),
+             "%s\"%s\": {\"launches\": %llu, \"ms\": %.6f, \"bytes\": %llu}",
              first ? "" : ", ", kv.first.c_str(),
-             (unsigned long long)kv.second.launches, kv.second.ms);
+             (unsigned long long)kv.second.launches, kv.second.ms,
+             (unsigned long long)kv.second.bytes);
     out += buf;
     first = false;
   }
@@ -274,12 +280,12 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
   if (vresult) *vresult = vals;
   if (n < 2 || bits <= 0) return cudaSuccess;
   if (!vals && n <= (uint64_t)kSmallSort) {
-    SST_LAUNCH((k_sort_small<false, kSmallSort>), 1, kThreads, 0, s, keys,
+    SST_LAUNCH_B(16 * n, (k_sort_small<false, kSmallSort>), 1, kThreads, 0, s, keys,
                (uint32_t *)nullptr, n, bits);
     return cudaGetLastError();
   }
   if (vals && n <= (uint64_t)kSmallSortKV) {
-    SST_LAUNCH((k_sort_small<true, kSmallSortKV>), 1, kThreads, 0, s, keys, vals,
+    SST_LAUNCH_B(24 * n, (k_sort_small<true, kSmallSortKV>), 1, kThreads, 0, s, keys, vals,
                n, bits);
     return cudaGetLastError();
   }
@@ -289,15 +295,19 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
   if (!hist) return cudaErrorMemoryAllocation;
   uint64_t *src = keys, *dst = tmp;
   uint32_t *vsrc = vals, *vdst = vtmp;
+  // per pass: the histogram reads the keys; the scatter reads and writes keys
+  // (and values); both touch the block-digit table
+  const uint64_t hist_bytes = 8 * n + 4 * hn;
+  const uint64_t scatter_bytes = (vals ? 24 : 16) * n + 4 * hn;
   for (int shift = 0; shift < bits; shift += 8) {
-    SST_LAUNCH(k_hist, nblocks, kThreads, 0, s, src, n, shift, hist, nblocks);
+    SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, shift, hist, nblocks);
     size_t mark = arena.used;
     cudaError_t e = scan<uint32_t, OpAdd>(hist, hist, hn, 0u, OpAdd{}, true,
                                           false, nullptr, arena, s);
     arena.used = mark;
     if (e != cudaSuccess) return e;
-    SST_LAUNCH(k_scatter, nblocks, kThreads, 0, s, src, dst, n, shift, hist,
-               nblocks, vsrc, vdst);
+    SST_LAUNCH_B(scatter_bytes, k_scatter, nblocks, kThreads, 0, s, src, dst, n,
+                 shift, hist, nblocks, vsrc, vdst);
     std::swap(src, dst);
     std::swap(vsrc, vdst);
   }

@@ -14,19 +14,24 @@ uint64_t launches();
 
 // Kernel profiler: while enabled, every launch is bracketed by a pair of
 // CUDA events on its own stream; profile_collect() folds the elapsed times
-// per kernel name.
+// per kernel name, with the algorithmic bytes the launch sites declare
+// (SST_LAUNCH_B: the bytes the kernel must read and write at its launch
+// size, independent of caching).
 bool profiling(const char *kernel_name);
 cudaEvent_t prof_begin(cudaStream_t s);
-void prof_end(const char *name, cudaEvent_t start, cudaStream_t s);
+void prof_end(const char *name, cudaEvent_t start, cudaStream_t s,
+              uint64_t bytes);
 
-#define SST_LAUNCH(kernel, grid, block, smem, stream, ...)                    \
+#define SST_LAUNCH_B(bytes, kernel, grid, block, smem, stream, ...)           \
   do {                                                                        \
     cudaEvent_t _sst_ev =                                                     \
         ::sst::profiling(#kernel) ? ::sst::prof_begin(stream) : nullptr;      \
     kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);               \
     ::sst::note_launch();                                                     \
-    if (_sst_ev) ::sst::prof_end(#kernel, _sst_ev, stream);                   \
+    if (_sst_ev) ::sst::prof_end(#kernel, _sst_ev, stream, (bytes));          \
   } while (0)
+#define SST_LAUNCH(kernel, grid, block, smem, stream, ...)                    \
+  SST_LAUNCH_B(0, kernel, grid, block, smem, stream, __VA_ARGS__)
 
 // ----------------------------------------------------------------- arena
 // Bump allocator over one device buffer; reset at the start of each
@@ -309,15 +314,16 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
     return cudaSuccess;
   }
   uint64_t blocks = (n + kScanTile - 1) / kScanTile;
+  const uint64_t bytes = 2 * sizeof(T) * n;  // read in, write out
   if (blocks == 1) {
-    SST_LAUNCH((k_scan_apply<T, Op>), 1, kScanThreads, 0, s, in, out, n,
+    SST_LAUNCH_B(bytes, (k_scan_apply<T, Op>), 1, kScanThreads, 0, s, in, out, n,
                identity, op, reverse, exclusive, (const T *)nullptr, total_out,
                d_n);
     return cudaGetLastError();
   }
   if (sizeof(T) <= 8 && arena.reserve_status(blocks, s) == cudaSuccess) {
     arena.epoch++;
-    SST_LAUNCH((k_scan_single<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
+    SST_LAUNCH_B(bytes, (k_scan_single<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
                out, n, identity, op, reverse, exclusive, total_out, d_n,
                arena.status, arena.epoch, arena.err);
     return cudaGetLastError();
