@@ -157,7 +157,11 @@ SST_API sst_status sst_sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
 
 /* ---- traversal (EdgeMap/VertexMap algorithms; the algorithm library
  *      EdgeMapVertexMap is absent from the reference tree, so the entry
- *      points follow its call sites in internal/test.hpp:476-618) ------- */
+ *      points follow its call sites in internal/test.hpp:476-618) -------
+ * The graph must be symmetric (every (u,v) stored with (v,u)), as the
+ * reference drivers build it from symmetrised inputs: the pull (dense
+ * frontier) steps and PageRank read a vertex's stored row as its in-edges.
+ * On a directed graph the results are not defined. */
 /* BFS(g, src)  test.hpp:486: parents (parent[src] = src, -1 unreached)
  * and/or depths (-1 unreached); either pointer may be NULL */
 SST_API sst_status sst_bfs(sst_graph *g, uint32_t src, int32_t *parents,

@@ -254,39 +254,61 @@ __global__ void k_scan_single(const T *__restrict__ in, T *__restrict__ out,
   T total;
   T run = block_exclusive(acc, identity, op, &total);
   __shared__ T s_prefix;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    // warp 0 looks back over 32 predecessors at a time: lane k reads tile
+    // j - k; the window is folded up to the nearest tile that has published
+    // its inclusive prefix (tile 0 always does)
+    const int lane = threadIdx.x;
     const unsigned long long tagA = (epoch << 2) | kScanAgg;
     const unsigned long long tagI = (epoch << 2) | kScanIncl;
     T prefix = identity;
     if (tile == 0) {
-      tile_publish(status, tagI, total);
+      if (lane == 0) tile_publish(status, tagI, total);
     } else {
-      tile_publish(status + 2 * tile, tagA, total);
-      for (int64_t j = (int64_t)tile - 1; j >= 0; j--) {
-        volatile unsigned long long *w =
-            reinterpret_cast<volatile unsigned long long *>(status + 2 * j);
-        unsigned long long tag = w[0];
-        uint32_t spins = 0;
-        while ((tag >> 2) != epoch && spins < kLookbackSpins) {
-          __nanosleep(64);
-          tag = w[0];
-          spins++;
+      if (lane == 0) tile_publish(status + 2 * tile, tagA, total);
+      int64_t j = (int64_t)tile - 1;
+      for (;;) {
+        const int64_t mine = j - lane;
+        bool incl = false, failed = false;
+        T v = identity;
+        if (mine >= 0) {
+          volatile unsigned long long *w =
+              reinterpret_cast<volatile unsigned long long *>(status + 2 * mine);
+          unsigned long long tag = w[0];
+          uint32_t spins = 0;
+          while ((tag >> 2) != epoch && spins < kLookbackSpins) {
+            __nanosleep(32);
+            tag = w[0];
+            spins++;
+          }
+          if ((tag >> 2) != epoch) {
+            failed = true;
+          } else {
+            __threadfence();
+            incl = (tag & 3) == kScanIncl;
+            unsigned long long bits = incl ? w[2] : w[1];
+            memcpy(&v, &bits, sizeof(T));
+          }
         }
-        if ((tag >> 2) != epoch) {
-          if (err) atomicAdd(err, 1ull);
+        const unsigned im = __ballot_sync(0xffffffffu, incl);
+        const unsigned fm = __ballot_sync(0xffffffffu, failed);
+        // lanes up to the nearest inclusive one contribute (the ops are
+        // commutative, so the fold order within the window is free)
+        const int stop = im ? __ffs(im) - 1 : 31;
+        T c = lane <= stop ? v : identity;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) c = op(c, __shfl_xor_sync(0xffffffffu, c, d));
+        prefix = op(c, prefix);
+        if (fm) {
+          if (lane == 0 && err) atomicAdd(err, 1ull);
           break;
         }
-        __threadfence();
-        const bool incl = (tag & 3) == kScanIncl;
-        unsigned long long bits = incl ? w[2] : w[1];
-        T v;
-        memcpy(&v, &bits, sizeof(T));
-        prefix = op(v, prefix);
-        if (incl) break;
+        if (im || j < 32) break;
+        j -= 32;
       }
-      tile_publish(status + 2 * tile, tagI, op(prefix, total));
+      if (lane == 0) tile_publish(status + 2 * tile, tagI, op(prefix, total));
     }
-    s_prefix = prefix;
+    if (lane == 0) s_prefix = prefix;
   }
   __syncthreads();
   run = op(s_prefix, run);

@@ -66,62 +66,118 @@ sst_status graph_copy_into(sst_graph *dst, sst_graph *src) {
 }
 
 // per-vertex triangle counts of the listed vertices:
-// (1/2) * sum over v in N(u) of |N(u) n N(v)|, one warp per vertex
+// t(u) = (1/2) * sum over w in N(u) of |N(u) n N(w)| (symmetric graph).
+// Work items are (query vertex, leaf of its list), one warp each; the warp
+// takes the leaf's neighbours w one at a time and intersects N(u) and N(w)
+// cooperatively: lanes stride over the shorter list and probe the longer one
+// (binary search over its leaf heads, then within the leaf).  A hub query
+// vertex spreads over as many warps as it has leaves.
 namespace {
-__device__ __forceinline__ bool probe(const DGraph &g, uint32_t u, uint32_t x) {
-  uint32_t cap = g.cap[u];
-  if (!cap) return false;
-  uint64_t base = g.base[u];
+__device__ __forceinline__ bool probe(const DGraph &g, uint64_t base,
+                                      uint32_t cap, uint32_t deg, uint32_t x) {
   uint32_t l = find_leaf(g.slots, base, cap, x);
-  uint32_t c = leaf_count(g, base, cap, g.deg[u], l);
+  uint32_t c = leaf_count(g, base, cap, deg, l);
   const uint32_t *p = g.slots + base + ((uint64_t)l << kLeafLog);
   uint32_t pos = leaf_lower_bound(p, c, x);
   return pos < c && p[pos] == x;
 }
 
-__device__ uint64_t common_count(const DGraph &g, uint32_t a, uint32_t b) {
-  uint32_t s = g.deg[a] <= g.deg[b] ? a : b, o = s == a ? b : a;
-  uint64_t base = g.base[s];
-  uint32_t cap = g.cap[s], deg = g.deg[s];
-  uint32_t nl = cap ? nleaves_of(cap) : 0;
-  uint64_t c = 0;
+// this lane's share of |N(a) n N(b)|
+__device__ __forceinline__ uint32_t warp_common(const DGraph &g, uint32_t a,
+                                                uint32_t b, int lane) {
+  uint32_t da = g.deg[a], db = g.deg[b];
+  const uint32_t s = da <= db ? a : b, o = s == a ? b : a;
+  const uint64_t sbase = g.base[s], obase = g.base[o];
+  const uint32_t scap = g.cap[s], sdeg = g.deg[s];
+  const uint32_t ocap = g.cap[o], odeg = g.deg[o];
+  if (!scap || !ocap) return 0;
+  const uint32_t nl = scap <= kLeaf ? 1 : scap >> kLeafLog;
+  uint32_t hits = 0;
   for (uint32_t l = 0; l < nl; l++) {
-    uint32_t k = leaf_count(g, base, cap, deg, l);
-    const uint32_t *p = g.slots + base + ((uint64_t)l << kLeafLog);
-    for (uint32_t j = 0; j < k; j++) c += probe(g, o, p[j]);
-  }
-  return c;
-}
-
-__global__ void k_tc_vertices(DGraph g, const uint32_t *__restrict__ vs,
-                              uint64_t k, unsigned long long *__restrict__ out) {
-  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (i >= k) return;
-  uint32_t u = vs[i];
-  unsigned long long acc = 0;
-  if (u < g.n) {
-    uint64_t base = g.base[u];
-    uint32_t cap = g.cap[u], deg = g.deg[u];
-    uint32_t nl = cap ? nleaves_of(cap) : 0;
-    for (uint32_t l = 0; l < nl; l++) {
-      uint32_t c = leaf_count(g, base, cap, deg, l);
-      if ((uint32_t)lane < c)
-        acc += common_count(g, u, g.slots[base + ((uint64_t)l << kLeafLog) + lane]);
+    uint32_t c = leaf_count(g, sbase, scap, sdeg, l);
+    if ((uint32_t)lane < c) {
+      uint32_t x = g.slots[sbase + ((uint64_t)l << kLeafLog) + lane];
+      hits += probe(g, obase, ocap, odeg, x);
     }
   }
+  return hits;
+}
+
+__global__ void k_tcv_leaves(DGraph g, const uint32_t *__restrict__ vs,
+                             uint64_t k, uint64_t *__restrict__ nl,
+                             unsigned long long *__restrict__ out) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k) return;
+  uint32_t u = vs[i];
+  uint32_t cap = u < g.n ? g.cap[u] : 0;
+  nl[i] = cap == 0 ? 0 : (cap <= kLeaf ? 1 : cap >> kLeafLog);
+  out[i] = 0;
+}
+
+__global__ void k_tcv_count(DGraph g, const uint32_t *__restrict__ vs,
+                            uint64_t k, const uint64_t *__restrict__ off,
+                            uint64_t items, unsigned long long *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t wi = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       wi < items; wi += warps) {
+    // query i with off[i] <= wi < off[i + 1]
+    uint64_t lo = 0, hi = k;
+    while (hi - lo > 1) {
+      uint64_t mid = (lo + hi) >> 1;
+      if (off[mid] <= wi) lo = mid; else hi = mid;
+    }
+    const uint32_t u = vs[lo];
+    const uint32_t l = (uint32_t)(wi - off[lo]);
+    const uint64_t base = g.base[u];
+    const uint32_t cap = g.cap[u], deg = g.deg[u];
+    const uint32_t c = leaf_count(g, base, cap, deg, l);
+    const uint32_t mine = (uint32_t)lane < c
+        ? g.slots[base + ((uint64_t)l << kLeafLog) + lane] : kEmpty;
+    uint32_t hits = 0;
+    for (uint32_t t = 0; t < c; t++) {
+      uint32_t w = __shfl_sync(0xffffffffu, mine, t);
+      hits += warp_common(g, u, w, lane);
+    }
 #pragma unroll
-  for (int d = 16; d > 0; d >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, d);
-  if (lane == 0) out[i] = acc / 2;
+    for (int d = 16; d > 0; d >>= 1) hits += __shfl_down_sync(0xffffffffu, hits, d);
+    if (lane == 0 && hits) atomicAdd(&out[lo], (unsigned long long)hits);
+  }
+}
+
+__global__ void k_tcv_half(unsigned long long *__restrict__ out, uint64_t k) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < k) out[i] >>= 1;
 }
 }  // namespace
 
 sst_status tc_vertices(sst_graph *g, const uint32_t *d_vs, uint64_t k,
                        uint64_t *d_out) {
   if (k == 0) return SST_OK;
-  SST_LAUNCH(k_tc_vertices, (unsigned)((k * 32 + 255) / 256), 256, 0, g->stream,
-             g->view(), d_vs, k, reinterpret_cast<unsigned long long *>(d_out));
-  SST_CUDA_TRY(cudaGetLastError());
+  cudaStream_t s = g->stream;
+  unsigned long long *out = reinterpret_cast<unsigned long long *>(d_out);
+  uint64_t *nl = nullptr;
+  SST_CUDA_TRY(cudaMallocAsync(&nl, (k + 1) * 8, s));
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes(k, 8) + 4096));
+  uint64_t *tot = g->arena.take<uint64_t>(1);
+  const unsigned tb = 256;
+  SST_LAUNCH(k_tcv_leaves, (unsigned)((k + tb - 1) / tb), tb, 0, s, g->view(),
+             d_vs, k, nl, out);
+  cudaError_t e = scan<uint64_t, OpAdd>(nl, nl, k, 0ull, OpAdd{}, true, false,
+                                        tot, g->arena, s);
+  uint64_t items = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&items, tot, 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && items) {
+    uint64_t blocks = std::min<uint64_t>((items * 32 + tb - 1) / tb, (uint64_t)g->sms * 16);
+    SST_LAUNCH(k_tcv_count, (unsigned)blocks, tb, 0, s, g->view(), d_vs, k, nl,
+               items, out);
+    SST_LAUNCH(k_tcv_half, (unsigned)((k + tb - 1) / tb), tb, 0, s, out, k);
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(nl, s);
+  SST_CUDA_TRY(e);
   return SST_OK;
 }
 

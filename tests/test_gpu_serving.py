@@ -38,8 +38,10 @@ def test_results_same_alone_and_in_the_mix(sg):
     for wave in range(8):
         for _ in range(4):
             if inserted and rng.random() < 0.35:
+                # removals keep the graph symmetric: the traversals pull over
+                # out-lists, which are the in-lists only on a symmetric graph
                 src = np.concatenate(inserted)
-                p = src[rng.integers(0, len(src), int(rng.integers(1, 500)))]
+                p = oracle.symmetrize(src[rng.integers(0, len(src), int(rng.integers(1, 500)))])
                 updates.append(("remove", p))
                 tickets.append(("u", srv.remove(p)))
             else:
