@@ -54,8 +54,10 @@ def args_parse():
     ap.add_argument("--batched-batches", type=int, default=128)
     ap.add_argument("--serve-requests", type=int, default=400)
     ap.add_argument("--serve-rate", type=float, default=300.0)
-    ap.add_argument("--only", default="all", choices=["all", "pagerank", "bfs", "batched", "serving"],
-                    help="run one traversal on the base graph (profiling cases)")
+    ap.add_argument("--only", default="all",
+                    choices=["all", "updates", "pagerank", "bfs", "batched", "serving"],
+                    help="one part of the run (profiling cases): the update steps "
+                         "alone, or one traversal on the base graph")
     return ap.parse_args()
 
 
@@ -311,11 +313,15 @@ def main():
         degs = torch.from_numpy(g.degrees().astype(np.int64))
         reached = (dep.cpu() >= 0)
         m_r = int(degs[reached].sum())
+        sg.profile_start()
+        sg.BFS(g, 0, depths=True, out=dep)
+        torch.cuda.synchronize()
         bfs = {"gteps": m_r / bt / 1e9, "ms": bt * 1e3, "reached": int(reached.sum()),
                "edges_reached": m_r,
                "roofline": {"bound": "hbm", "achieved": (4 * m_r + 12 * n) / bt / 1e9,
                             "peak": hbm_peak, "unit": "GB/s",
-                            "frac": (4 * m_r + 12 * n) / bt / 1e9 / hbm_peak}}
+                            "frac": (4 * m_r + 12 * n) / bt / 1e9 / hbm_peak},
+               "kernels": sg.profile_collect()}
         return bfs
 
     def measure_batched():
@@ -428,7 +434,7 @@ def main():
                 "wall_s": wall, "writer_passes": st["passes"],
                 "hbm_budget_bytes": 60 << 30}
 
-    if a.only != "all":
+    if a.only not in ("all", "updates"):
         pr_flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
         res = {"only": a.only, "scale": a.scale, "edges": m0}
         if a.only == "pagerank":
@@ -518,30 +524,33 @@ def main():
            "note": "insert+remove via sst_insert_batch/sst_remove_batch on pinned host "
                    "pairs; each call returns the invalid-pair count (8 B) to the host"}
 
-    batched = measure_batched()
-    pagerank = measure_pagerank()
-    # the reference's degree-ordered mode (internal/test.hpp:460-467):
-    # relabel by degree, run on the relabelled copy, map results back
-    t0 = time.time()
-    dmap = torch.empty(n, dtype=torch.int32, device="cuda")
-    g.degree_order_map(out=dmap)
-    gr = g.rewrite_graph(dmap)
-    gr.set_stream(stream.cuda_stream)
-    torch.cuda.synchronize()
-    relabel_s = time.time() - t0
-    pr_deg = measure_pagerank(gr)
-    o1 = torch.empty(n, dtype=torch.float64, device="cuda")
-    o2 = torch.empty(n, dtype=torch.float64, device="cuda")
-    sg.PR_S(g, a.pr_iters, out=o1)
-    sg.PR_S(gr, a.pr_iters, out=o2)
-    torch.cuda.synchronize()
-    pr_deg["same_result_after_relabel"] = bool(
-        (o2[dmap.long()] - o1).abs().max().item() <= 1e-12 * o1.abs().max().item())
-    pr_deg["relabel_s"] = relabel_s
-    pagerank["degree_ordered"] = pr_deg
-    gr.close()
-    bfs = measure_bfs()
-    serving = measure_serving()
+    batched = pagerank = bfs = serving = None
+    if a.only == "all":
+        batched = measure_batched()
+        pagerank = measure_pagerank()
+        # the reference's degree-ordered mode (internal/test.hpp:460-467):
+        # relabel by degree, run on the relabelled copy, map results back
+        t0 = time.time()
+        dmap = torch.empty(n, dtype=torch.int32, device="cuda")
+        g.degree_order_map(out=dmap)
+        gr = g.rewrite_graph(dmap)
+        gr.set_stream(stream.cuda_stream)
+        torch.cuda.synchronize()
+        relabel_s = time.time() - t0
+        pr_deg = measure_pagerank(gr)
+        o1 = torch.empty(n, dtype=torch.float64, device="cuda")
+        o2 = torch.empty(n, dtype=torch.float64, device="cuda")
+        sg.PR_S(g, a.pr_iters, out=o1)
+        sg.PR_S(gr, a.pr_iters, out=o2)
+        torch.cuda.synchronize()
+        pr_deg["same_result_after_relabel"] = bool(
+            (o2[dmap.long()] - o1).abs().max().item() <= 1e-12 * o1.abs().max().item())
+        pr_deg["relabel_s"] = relabel_s
+        pagerank["degree_ordered"] = pr_deg
+        gr.close()
+        bfs = measure_bfs()
+        serving = measure_serving()
+
 
     # ---- roofline of the update step's dominant kernel
     upd_kernels = {"timed_region": prof, "warmup_all_kernels": prof_all}
@@ -549,7 +558,7 @@ def main():
 
     # ---- CPU baseline (bounded sample, rank 0 only)
     cpu = None
-    if rank == 0 and not a.no_cpu_baseline:
+    if rank == 0 and not a.no_cpu_baseline and a.only == "all":
         sample = SIZES
         v, det = run_cpu(a.scale, sample,
                          f"one insert+delete batch of each size {SIZES} on the "

@@ -120,8 +120,10 @@ struct OpMin {
   }
 };
 
-constexpr int kScanThreads = 256;
-constexpr int kScanItems = 8;
+// 8192-element tiles: a 1e6-element scan is ~120 tiles, so the look-back
+// of the single-pass scan meets an inclusive prefix within a few windows
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
 template <typename T, typename Op>

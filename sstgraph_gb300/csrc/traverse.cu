@@ -189,11 +189,19 @@ __device__ __forceinline__ uint64_t mulhi_round(uint64_t a, uint64_t b) {
   return __umul64hi(a, b) + ((a * b) >> 63);
 }
 
-// leaf ids are read once per iteration: keep them out of L1 so the
-// contribution gathers keep it
-__device__ __forceinline__ uint32_t ld_stream(const uint32_t *p) {
+// leaf ids are read once per iteration: keep them out of L1 and first in
+// line for eviction from L2, so the contribution gathers keep both caches
+__device__ __forceinline__ unsigned long long l2_evict_first() {
+  unsigned long long pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ uint32_t ld_stream(const uint32_t *p,
+                                              unsigned long long pol) {
   uint32_t v;
-  asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(p));
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;"
+      : "=r"(v)
+      : "l"(p), "l"(pol));
   return v;
 }
 __device__ __forceinline__ unsigned long long ld_keep(const unsigned long long *p) {
@@ -263,6 +271,7 @@ __global__ void k_pr_small(DGraph g, const unsigned long long *__restrict__ sdes
                            PrConst k, bool last) {
   uint64_t grp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
   const uint32_t sub = threadIdx.x & 7;
+  const unsigned long long pol = l2_evict_first();
   const uint64_t i0 = grp * kSmallPer;
   uint32_t x[kSmallPer][4];
   uint32_t dg[kSmallPer];
@@ -275,7 +284,7 @@ __global__ void k_pr_small(DGraph g, const unsigned long long *__restrict__ sdes
 #pragma unroll
     for (int q = 0; q < 4; q++) {
       uint32_t j = sub + 8 * q;
-      x[u][q] = j < dg[u] ? ld_stream(p + j) : kEmpty;
+      x[u][q] = j < dg[u] ? ld_stream(p + j, pol) : kEmpty;
     }
   }
   unsigned long long acc[kSmallPer];
@@ -303,9 +312,10 @@ __global__ void k_pr_small(DGraph g, const unsigned long long *__restrict__ sdes
     pr_finish(small[i0 + sub], mine, k, mydeg, rdeg, cout, rank, last);
 }
 
-// warp per chunk of <= 32 leaves of a multi-leaf segment; four leaves in
-// flight per step.  cdesc[c] = (first leaf << 8) | (single chunk << 7) |
-// leaves in the chunk.
+// warp per chunk of <= 32 leaves of a multi-leaf segment (lane = slot);
+// the chunk's leaf counts come in with one coalesced load, and eight leaves'
+// ids, then their eight gathers, are in flight per step.
+// cdesc[c] = (first leaf << 8) | (single chunk << 7) | leaves in the chunk.
 __global__ void k_pr_chunks(DGraph g, const unsigned long long *__restrict__ cdesc,
                             const uint32_t *__restrict__ cv, uint64_t nchunks,
                             const unsigned long long *__restrict__ cin,
@@ -317,27 +327,26 @@ __global__ void k_pr_chunks(DGraph g, const unsigned long long *__restrict__ cde
   uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= nchunks) return;
+  const unsigned long long pol = l2_evict_first();
   unsigned long long dsc = cdesc[c];
   const uint64_t leaf0 = dsc >> 8;
   const uint32_t l1 = (uint32_t)(dsc & 63);
   const bool single = (dsc >> 7) & 1;
-  const uint8_t *lc = g.lcnt + leaf0;
+  const uint32_t mycnt = (uint32_t)lane < l1 ? g.lcnt[leaf0 + lane] : 0u;
   const uint32_t *sl = g.slots + (leaf0 << kLeafLog) + lane;
   unsigned long long acc = 0;
-  uint32_t l = 0;
-  for (; l + 4 <= l1; l += 4) {
-    uint32_t c0 = lc[l], c1 = lc[l + 1], c2 = lc[l + 2], c3 = lc[l + 3];
-    uint32_t x0 = (uint32_t)lane < c0 ? ld_stream(sl + ((uint64_t)l << kLeafLog)) : kEmpty;
-    uint32_t x1 = (uint32_t)lane < c1 ? ld_stream(sl + ((uint64_t)(l + 1) << kLeafLog)) : kEmpty;
-    uint32_t x2 = (uint32_t)lane < c2 ? ld_stream(sl + ((uint64_t)(l + 2) << kLeafLog)) : kEmpty;
-    uint32_t x3 = (uint32_t)lane < c3 ? ld_stream(sl + ((uint64_t)(l + 3) << kLeafLog)) : kEmpty;
-    if (x0 != kEmpty) acc += ld_keep(cin + x0);
-    if (x1 != kEmpty) acc += ld_keep(cin + x1);
-    if (x2 != kEmpty) acc += ld_keep(cin + x2);
-    if (x3 != kEmpty) acc += ld_keep(cin + x3);
-  }
-  for (; l < l1; l++) {
-    if ((uint32_t)lane < lc[l]) acc += ld_keep(cin + ld_stream(sl + ((uint64_t)l << kLeafLog)));
+  for (uint32_t l = 0; l < l1; l += 8) {
+    uint32_t x[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      uint32_t cq = __shfl_sync(0xffffffffu, mycnt, (l + q) & 31);
+      if (l + q >= l1) cq = 0;
+      x[q] = (uint32_t)lane < cq ? ld_stream(sl + ((uint64_t)(l + q) << kLeafLog), pol)
+                                 : kEmpty;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      if (x[q] != kEmpty) acc += ld_keep(cin + x[q]);
   }
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
