@@ -187,6 +187,15 @@ SST_API sst_status sst_bc(sst_graph *g, uint32_t src, double *out, uint32_t flag
 /* TC(g)  test.hpp:606: triangles (each once); per_vertex may be NULL */
 SST_API sst_status sst_tc(sst_graph *g, uint64_t *total, uint64_t *per_vertex,
                   uint32_t flags);
+/* Multi-source forms (no reference counterpart; the batched traversal of
+ * k <= 64 sources).  Output is k x rows, row i for srcs[i]:
+ * sst_bfs_multi writes depths (-1 unreached), one traversal for all
+ * sources; sst_bc_multi writes for each source exactly what sst_bc writes
+ * (same arithmetic order), every launch covering all sources. */
+SST_API sst_status sst_bfs_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
+                                 int32_t *depths, uint32_t flags);
+SST_API sst_status sst_bc_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
+                                double *out, uint32_t flags);
 /* TouchAll(g)  test.hpp:476 */
 SST_API sst_status sst_touch_all(sst_graph *g, uint64_t *out);
 

@@ -103,6 +103,8 @@ SIGNATURES = {
     "sst_pagerank": (_i32, [_vp, _u32, _dbl, _vp, _u32]),
     "sst_cc": (_i32, [_vp, _vp, _u32]),
     "sst_bc": (_i32, [_vp, _u32, _vp, _u32]),
+    "sst_bfs_multi": (_i32, [_vp, _vp, _u32, _vp, _u32]),
+    "sst_bc_multi": (_i32, [_vp, _vp, _u32, _vp, _u32]),
     "sst_tc": (_i32, [_vp, ctypes.POINTER(_u64), _vp, _u32]),
     "sst_touch_all": (_i32, [_vp, ctypes.POINTER(_u64)]),
     "sst_gen_rmat": (_i32, [_u32, _dbl, _dbl, _dbl, _u64, _u64, _u64, _vp, _u32]),
@@ -486,6 +488,37 @@ def BC(g: SparseMatrixV, src: int, out=None):
     p, flags = _ptr(buf)
     _check(lib().sst_bc(g.handle, src, p, flags))
     return buf
+
+
+def _sources(srcs):
+    if hasattr(srcs, "data_ptr"):
+        return srcs, ctypes.c_void_p(srcs.data_ptr())
+    a = np.ascontiguousarray(np.asarray(srcs, np.uint32).ravel())
+    return a, ctypes.c_void_p(a.ctypes.data)
+
+
+def BFS_multi(g: SparseMatrixV, srcs, out=None):
+    """Depths from each of k <= 64 sources in one traversal: (k, rows)
+    int32, row i for srcs[i], -1 unreached."""
+    keep, sp = _sources(srcs)
+    k = len(keep)
+    if out is None:
+        out = np.empty((k, g.rows), np.int32)
+    p, flags = _ptr(out)
+    _check(lib().sst_bfs_multi(g.handle, sp, k, p, flags))
+    return out
+
+
+def BC_multi(g: SparseMatrixV, srcs, out=None):
+    """BC(g, s) for each of k <= 64 sources, every launch covering all of
+    them: (k, rows) float64, row i equal to BC(g, srcs[i])."""
+    keep, sp = _sources(srcs)
+    k = len(keep)
+    if out is None:
+        out = np.empty((k, g.rows), np.float64)
+    p, flags = _ptr(out)
+    _check(lib().sst_bc_multi(g.handle, sp, k, p, flags))
+    return out
 
 
 def TC(g: SparseMatrixV, per_vertex: bool = False):

@@ -4,6 +4,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "graph.cuh"
 #include "traverse.cuh"
@@ -575,6 +576,71 @@ sst_status sst_bfs(sst_graph *g, uint32_t src, int32_t *parents,
   if (parents) st = finish_out(g, parents, dp, g->n, flags);
   if (st == SST_OK && depths) st = finish_out(g, depths, dd, g->n, flags);
   return st;
+}
+
+// sources come to the host for validation and the source table
+static sst_status sources_to_host(sst_graph *g, const uint32_t *srcs,
+                                  uint32_t k, uint32_t flags,
+                                  std::vector<uint32_t> *out) {
+  out->resize(k);
+  if (!k) return SST_OK;
+  if (is_dev(flags)) {
+    SST_CUDA_TRY(cudaMemcpyAsync(out->data(), srcs, (uint64_t)k * 4,
+                                 cudaMemcpyDeviceToHost, g->stream));
+    SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
+  } else {
+    memcpy(out->data(), srcs, (uint64_t)k * 4);
+  }
+  for (uint32_t i = 0; i < k; i++)
+    if ((*out)[i] >= g->n) {
+      set_error_message("source %u out of range", (*out)[i]);
+      return SST_EINVAL;
+    }
+  return SST_OK;
+}
+
+sst_status sst_bfs_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
+                         int32_t *depths, uint32_t flags) {
+  CHECK_G(g);
+  if (k > 64 || (k && (!srcs || !depths))) {
+    set_error_message(k > 64 ? "at most 64 sources" : "null argument");
+    return SST_EINVAL;
+  }
+  if (!k) return SST_OK;
+  std::vector<uint32_t> hs;
+  sst_status st = sources_to_host(g, srcs, k, flags, &hs);
+  if (st != SST_OK) return st;
+  const uint64_t cnt = (uint64_t)k * g->n;
+  st = is_dev(flags) ? SST_OK : io_begin(g, cnt * 4 + 512);
+  if (st != SST_OK) return st;
+  int32_t *d = nullptr;
+  st = stage_out(g, depths, cnt, flags, &d);
+  if (st != SST_OK) return st;
+  st = sst::bfs_multi(g, hs.data(), k, d);
+  if (st != SST_OK) return st;
+  return finish_out(g, depths, d, cnt, flags);
+}
+
+sst_status sst_bc_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
+                        double *out, uint32_t flags) {
+  CHECK_G(g);
+  if (k > 64 || (k && (!srcs || !out))) {
+    set_error_message(k > 64 ? "at most 64 sources" : "null argument");
+    return SST_EINVAL;
+  }
+  if (!k) return SST_OK;
+  std::vector<uint32_t> hs;
+  sst_status st = sources_to_host(g, srcs, k, flags, &hs);
+  if (st != SST_OK) return st;
+  const uint64_t cnt = (uint64_t)k * g->n;
+  st = is_dev(flags) ? SST_OK : io_begin(g, cnt * 8 + 512);
+  if (st != SST_OK) return st;
+  double *d = nullptr;
+  st = stage_out(g, out, cnt, flags, &d);
+  if (st != SST_OK) return st;
+  st = sst::bc_multi(g, hs.data(), k, d);
+  if (st != SST_OK) return st;
+  return finish_out(g, out, d, cnt, flags);
 }
 
 sst_status sst_pagerank(sst_graph *g, uint32_t iters, double damping,

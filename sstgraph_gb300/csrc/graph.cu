@@ -862,8 +862,6 @@ sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
   SST_CUDA_TRY(cudaMalloc(&g->d_plan, sizeof(PlanSummary)));
   SST_CUDA_TRY(cudaMalloc(&g->d_err, sizeof(unsigned long long)));
   SST_CUDA_TRY(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned long long), g->stream));
-  g->arena.err = g->d_err;
-  g->work.err = g->d_err;
   SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
   return SST_OK;
 }
@@ -1125,7 +1123,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   SST_CUDA_TRY(cudaGetLastError());
   PlanSummary ps = *g->h_plan;
   if (ps.apply_err) {
-    set_error_message("internal error: %llu failed device checks (staging rank out of range or scan look-back wait ran out)",
+    set_error_message("internal error: %llu failed device checks (staging rank out of range)",
                       (unsigned long long)ps.apply_err);
     return SST_EDEVICE;
   }
@@ -1397,7 +1395,7 @@ sst_status sync_checked(sst_graph *g) {
                                cudaMemcpyDeviceToHost, g->stream));
   SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
   if (g->h_plan->apply_err) {
-    set_error_message("internal error: %llu failed device checks (staging rank out of range or scan look-back wait ran out)",
+    set_error_message("internal error: %llu failed device checks (staging rank out of range)",
                       (unsigned long long)g->h_plan->apply_err);
     return SST_EDEVICE;
   }

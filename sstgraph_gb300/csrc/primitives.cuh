@@ -59,37 +59,10 @@ struct Arena {
     cap = want;
     return cudaSuccess;
   }
-  // tile status words of the single-pass scan (32 B per tile), kept apart
-  // from the bump memory so stale tags come only from earlier scans; each
-  // scan tags its words with a fresh epoch
-  uint4 *status = nullptr;
-  uint64_t status_cap = 0;
-  unsigned long long epoch = 0;
-  unsigned long long *err = nullptr;  // counts look-back waits that ran out
-
-  // the words are zeroed on the scan's own stream (the library's streams do
-  // not synchronise with the legacy default stream), so the first scan never
-  // sees uninitialised tags
-  cudaError_t reserve_status(uint64_t tiles, cudaStream_t s) {
-    if (tiles <= status_cap) return cudaSuccess;
-    if (status) cudaFree(status);
-    status = nullptr;
-    status_cap = 0;
-    uint64_t want = tiles + tiles / 4 + 64;
-    cudaError_t e = cudaMalloc(&status, 2 * want * sizeof(uint4));
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(status, 0, 2 * want * sizeof(uint4), s);
-    if (e != cudaSuccess) return e;
-    status_cap = want;
-    return cudaSuccess;
-  }
   void release() {
     if (base) cudaFree(base);
     base = nullptr;
     cap = used = 0;
-    if (status) cudaFree(status);
-    status = nullptr;
-    status_cap = 0;
   }
   void reset() { used = 0; }
   template <typename T> T *take(size_t count) {
@@ -120,9 +93,7 @@ struct OpMin {
   }
 };
 
-// 8192-element tiles: a 1e6-element scan is ~120 tiles, so the look-back
-// of the single-pass scan meets an inclusive prefix within a few windows
-constexpr int kScanThreads = 512;
+constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
@@ -161,168 +132,113 @@ __device__ __forceinline__ T block_exclusive(T v, T identity, Op op, T *total) {
   return res;
 }
 
+// Multi-tile scans run as two launches over kScanRanges contiguous tile
+// ranges (about two blocks per SM): the first reduces each range, the
+// second has every block fold the range sums before its own and then scan
+// its range tile by tile with a running carry.  No block waits on another.
+constexpr int kScanRanges = 304;
+
+// tile t of the scan order: element i of the array (forward or reversed)
+template <typename T>
+__device__ __forceinline__ T scan_load(const T *in, uint64_t i, uint64_t n,
+                                       bool reverse, T identity) {
+  return i < n ? in[reverse ? n - 1 - i : i] : identity;
+}
+
 template <typename T, typename Op>
 __global__ void k_scan_reduce(const T *__restrict__ in, uint64_t n, T identity,
-                              Op op, bool reverse, T *__restrict__ block_sums,
+                              Op op, bool reverse, uint64_t tiles_per_range,
+                              T *__restrict__ range_sums,
                               const uint32_t *__restrict__ d_n) {
   if (d_n && *d_n < n) n = *d_n;
-  uint64_t tile0 = (uint64_t)blockIdx.x * kScanTile;
+  const uint64_t t0 = (uint64_t)blockIdx.x * tiles_per_range;
   T acc = identity;
+  for (uint64_t t = t0; t < t0 + tiles_per_range; t++) {
+    const uint64_t base = t * kScanTile;
+    if (base >= n) break;
+    // order inside a range does not matter for the total: striped loads
 #pragma unroll
-  for (int k = 0; k < kScanItems; k++) {
-    uint64_t i = tile0 + (uint64_t)threadIdx.x * kScanItems + k;
-    if (i < n) acc = op(acc, in[reverse ? n - 1 - i : i]);
+    for (int k = 0; k < kScanItems; k++)
+      acc = op(acc, scan_load(in, base + (uint64_t)k * kScanThreads + threadIdx.x,
+                              n, reverse, identity));
   }
   T total;
   block_exclusive(acc, identity, op, &total);
-  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+  if (threadIdx.x == 0) range_sums[blockIdx.x] = total;
 }
 
 template <typename T, typename Op>
-__global__ void k_scan_apply(const T *__restrict__ in, T *__restrict__ out,
-                             uint64_t n, T identity, Op op, bool reverse,
-                             bool exclusive, const T *__restrict__ block_prefix,
-                             T *__restrict__ total_out,
-                             const uint32_t *__restrict__ d_n) {
-  if (d_n && *d_n < n) n = *d_n;
-  uint64_t tile0 = (uint64_t)blockIdx.x * kScanTile;
-  T vals[kScanItems];
-  T acc = identity;
-#pragma unroll
-  for (int k = 0; k < kScanItems; k++) {
-    uint64_t i = tile0 + (uint64_t)threadIdx.x * kScanItems + k;
-    vals[k] = i < n ? in[reverse ? n - 1 - i : i] : identity;
-    acc = op(acc, vals[k]);
-  }
-  T total;
-  T run = block_exclusive(acc, identity, op, &total);
-  if (block_prefix) run = op(block_prefix[blockIdx.x], run);
-#pragma unroll
-  for (int k = 0; k < kScanItems; k++) {
-    uint64_t i = tile0 + (uint64_t)threadIdx.x * kScanItems + k;
-    T nxt = op(run, vals[k]);
-    if (i < n) out[reverse ? n - 1 - i : i] = exclusive ? run : nxt;
-    run = nxt;
-  }
-  if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
-    T t = block_prefix ? op(block_prefix[blockIdx.x], total) : total;
-    *total_out = t;
-  }
-}
-
-// Single-pass scan with decoupled look-back (Merrill & Garland 2016): each
-// tile publishes its aggregate, then its inclusive prefix once the prefix of
-// the tiles before it is known, so one launch scans the whole array.  Tiles
-// rely on blocks being dispatched in index order; every wait on a
-// predecessor is bounded and counts a failure in *err instead of hanging.
-constexpr unsigned long long kScanAgg = 1, kScanIncl = 2;
-constexpr uint32_t kLookbackSpins = 1u << 22;
-
-// A tile's status is two 16-byte words: {tag, aggregate} and {inclusive
-// prefix, -}.  The aggregate and the inclusive prefix live in separate
-// fields, each written before the tag that announces it and never changed
-// afterwards, so a reader takes the field that matches the tag it saw (a
-// shared field could be overwritten between the reader's tag and value
-// loads).
-template <typename T>
-__device__ __forceinline__ void tile_publish(uint4 *st, unsigned long long tag,
-                                             T v) {
-  volatile unsigned long long *w = reinterpret_cast<volatile unsigned long long *>(st);
-  unsigned long long bits = 0;
-  memcpy(&bits, &v, sizeof(T));
-  w[(tag & 3) == kScanIncl ? 2 : 1] = bits;
-  __threadfence();
-  w[0] = tag;
-}
-
-template <typename T, typename Op>
-__global__ void k_scan_single(const T *__restrict__ in, T *__restrict__ out,
+__global__ void k_scan_ranges(const T *__restrict__ in, T *__restrict__ out,
                               uint64_t n, T identity, Op op, bool reverse,
-                              bool exclusive, T *__restrict__ total_out,
-                              const uint32_t *__restrict__ d_n, uint4 *status,
-                              unsigned long long epoch,
-                              unsigned long long *err) {
+                              bool exclusive, uint64_t tiles_per_range,
+                              const T *__restrict__ range_sums,
+                              T *__restrict__ total_out,
+                              const uint32_t *__restrict__ d_n) {
   if (d_n && *d_n < n) n = *d_n;
-  const uint64_t tile = blockIdx.x;
-  uint64_t tile0 = tile * kScanTile;
+  __shared__ T s_carry;
+  // carry into this range: the sums of the ranges before it
+  {
+    T a = identity;
+    for (uint32_t r = threadIdx.x; r < blockIdx.x; r += kScanThreads)
+      a = op(a, range_sums[r]);
+    T tot;
+    block_exclusive(a, identity, op, &tot);
+    if (threadIdx.x == 0) s_carry = tot;
+    __syncthreads();
+  }
+  T carry = s_carry;
+  const uint64_t t0 = (uint64_t)blockIdx.x * tiles_per_range;
+  for (uint64_t t = t0; t < t0 + tiles_per_range; t++) {
+    const uint64_t base = t * kScanTile;
+    if (base >= n) break;
+    T vals[kScanItems];
+    T acc = identity;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+      vals[k] = scan_load(in, base + (uint64_t)threadIdx.x * kScanItems + k, n,
+                          reverse, identity);
+      acc = op(acc, vals[k]);
+    }
+    T total;
+    T run = op(carry, block_exclusive(acc, identity, op, &total));
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+      uint64_t i = base + (uint64_t)threadIdx.x * kScanItems + k;
+      T nxt = op(run, vals[k]);
+      if (i < n) out[reverse ? n - 1 - i : i] = exclusive ? run : nxt;
+      run = nxt;
+    }
+    carry = op(carry, total);
+  }
+  if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+    *total_out = carry;
+}
+
+// one-tile scan (n <= kScanTile)
+template <typename T, typename Op>
+__global__ void k_scan_tile(const T *__restrict__ in, T *__restrict__ out,
+                            uint64_t n, T identity, Op op, bool reverse,
+                            bool exclusive, T *__restrict__ total_out,
+                            const uint32_t *__restrict__ d_n) {
+  if (d_n && *d_n < n) n = *d_n;
   T vals[kScanItems];
   T acc = identity;
 #pragma unroll
   for (int k = 0; k < kScanItems; k++) {
-    uint64_t i = tile0 + (uint64_t)threadIdx.x * kScanItems + k;
-    vals[k] = i < n ? in[reverse ? n - 1 - i : i] : identity;
+    vals[k] = scan_load(in, (uint64_t)threadIdx.x * kScanItems + k, n, reverse,
+                        identity);
     acc = op(acc, vals[k]);
   }
   T total;
   T run = block_exclusive(acc, identity, op, &total);
-  __shared__ T s_prefix;
-  if (threadIdx.x < 32) {
-    // warp 0 looks back over 32 predecessors at a time: lane k reads tile
-    // j - k; the window is folded up to the nearest tile that has published
-    // its inclusive prefix (tile 0 always does)
-    const int lane = threadIdx.x;
-    const unsigned long long tagA = (epoch << 2) | kScanAgg;
-    const unsigned long long tagI = (epoch << 2) | kScanIncl;
-    T prefix = identity;
-    if (tile == 0) {
-      if (lane == 0) tile_publish(status, tagI, total);
-    } else {
-      if (lane == 0) tile_publish(status + 2 * tile, tagA, total);
-      int64_t j = (int64_t)tile - 1;
-      for (;;) {
-        const int64_t mine = j - lane;
-        bool incl = false, failed = false;
-        T v = identity;
-        if (mine >= 0) {
-          volatile unsigned long long *w =
-              reinterpret_cast<volatile unsigned long long *>(status + 2 * mine);
-          unsigned long long tag = w[0];
-          uint32_t spins = 0;
-          while ((tag >> 2) != epoch && spins < kLookbackSpins) {
-            __nanosleep(32);
-            tag = w[0];
-            spins++;
-          }
-          if ((tag >> 2) != epoch) {
-            failed = true;
-          } else {
-            __threadfence();
-            incl = (tag & 3) == kScanIncl;
-            unsigned long long bits = incl ? w[2] : w[1];
-            memcpy(&v, &bits, sizeof(T));
-          }
-        }
-        const unsigned im = __ballot_sync(0xffffffffu, incl);
-        const unsigned fm = __ballot_sync(0xffffffffu, failed);
-        // lanes up to the nearest inclusive one contribute (the ops are
-        // commutative, so the fold order within the window is free)
-        const int stop = im ? __ffs(im) - 1 : 31;
-        T c = lane <= stop ? v : identity;
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) c = op(c, __shfl_xor_sync(0xffffffffu, c, d));
-        prefix = op(c, prefix);
-        if (fm) {
-          if (lane == 0 && err) atomicAdd(err, 1ull);
-          break;
-        }
-        if (im || j < 32) break;
-        j -= 32;
-      }
-      if (lane == 0) tile_publish(status + 2 * tile, tagI, op(prefix, total));
-    }
-    if (lane == 0) s_prefix = prefix;
-  }
-  __syncthreads();
-  run = op(s_prefix, run);
 #pragma unroll
   for (int k = 0; k < kScanItems; k++) {
-    uint64_t i = tile0 + (uint64_t)threadIdx.x * kScanItems + k;
+    uint64_t i = (uint64_t)threadIdx.x * kScanItems + k;
     T nxt = op(run, vals[k]);
     if (i < n) out[reverse ? n - 1 - i : i] = exclusive ? run : nxt;
     run = nxt;
   }
-  if (total_out && tile == gridDim.x - 1 && threadIdx.x == 0)
-    *total_out = op(s_prefix, total);
+  if (total_out && threadIdx.x == 0) *total_out = total;
 }
 
 // Scan of n elements (in may equal out).  total_out (device, may be null)
@@ -337,44 +253,30 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
                                           cudaMemcpyHostToDevice, s);
     return cudaSuccess;
   }
-  uint64_t blocks = (n + kScanTile - 1) / kScanTile;
-  const uint64_t bytes = 2 * sizeof(T) * n;  // read in, write out
-  if (blocks == 1) {
-    SST_LAUNCH_B(bytes, (k_scan_apply<T, Op>), 1, kScanThreads, 0, s, in, out, n,
-               identity, op, reverse, exclusive, (const T *)nullptr, total_out,
-               d_n);
+  const uint64_t tiles = (n + kScanTile - 1) / kScanTile;
+  if (tiles == 1) {
+    SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_tile<T, Op>), 1, kScanThreads, 0, s,
+                 in, out, n, identity, op, reverse, exclusive, total_out, d_n);
     return cudaGetLastError();
   }
-  if (sizeof(T) <= 8 && arena.reserve_status(blocks, s) == cudaSuccess) {
-    arena.epoch++;
-    SST_LAUNCH_B(bytes, (k_scan_single<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
-               out, n, identity, op, reverse, exclusive, total_out, d_n,
-               arena.status, arena.epoch, arena.err);
-    return cudaGetLastError();
-  }
-  T *sums = arena.take<T>(blocks);
+  const uint64_t ranges = tiles < (uint64_t)kScanRanges ? tiles : (uint64_t)kScanRanges;
+  const uint64_t per = (tiles + ranges - 1) / ranges;
+  const uint64_t used = (tiles + per - 1) / per;
+  T *sums = arena.take<T>(used);
   if (!sums) return cudaErrorMemoryAllocation;
-  SST_LAUNCH((k_scan_reduce<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
-             n, identity, op, reverse, sums, d_n);
-  // block prefixes in block order (reverse handled inside the tiles)
-  cudaError_t e = scan<T, Op>(sums, sums, blocks, identity, op, true, false,
-                              (T *)nullptr, arena, s);
-  if (e != cudaSuccess) return e;
-  SST_LAUNCH((k_scan_apply<T, Op>), (unsigned)blocks, kScanThreads, 0, s, in,
-             out, n, identity, op, reverse, exclusive, (const T *)sums,
-             total_out, d_n);
+  // the reduce reads the input; the scan reads it again and writes the output
+  SST_LAUNCH_B(sizeof(T) * n, (k_scan_reduce<T, Op>), (unsigned)used, kScanThreads,
+               0, s, in, n, identity, op, reverse, per, sums, d_n);
+  SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_ranges<T, Op>), (unsigned)used,
+               kScanThreads, 0, s, in, out, n, identity, op, reverse, exclusive,
+               per, (const T *)sums, total_out, d_n);
   return cudaGetLastError();
 }
 
 // scratch bytes a scan of n elements of T takes from the arena
 inline size_t scan_scratch_bytes(uint64_t n, size_t elem) {
-  size_t bytes = 0;
-  uint64_t blocks = (n + kScanTile - 1) / kScanTile;
-  while (blocks > 1) {
-    bytes += ((blocks * elem + 255) & ~size_t(255));
-    blocks = (blocks + kScanTile - 1) / kScanTile;
-  }
-  return bytes + 256;
+  (void)n;
+  return ((kScanRanges * elem + 255) & ~size_t(255)) + 256;
 }
 
 // ----------------------------------------------------------- radix sort

@@ -78,6 +78,12 @@ struct TravState {
   // tc
   DevBuf<uint64_t> toff, tlpre, tlcnt;
   DevBuf<uint32_t> tadj;
+  // multi-source bfs: per-vertex source masks (visited, frontier, next)
+  DevBuf<unsigned long long> mvis, mfr, mfr2, mnx, msrc;
+  DevBuf<int32_t> mdepth;
+  // multi-source bc: per (source, vertex) values and per-source level tables
+  DevBuf<double> msig, mrat, mpart;
+  DevBuf<uint32_t> mlist, micnt, mioff, miv, mil0, mtab;
   uint64_t *h_small = nullptr;  // pinned readback slots
   unsigned long long *d_small = nullptr;
 };
@@ -117,6 +123,21 @@ void trav_release(sst_graph *g) {
   t->tlpre.release();
   t->tlcnt.release();
   t->tadj.release();
+  t->mvis.release();
+  t->mfr.release();
+  t->mfr2.release();
+  t->mnx.release();
+  t->msrc.release();
+  t->mdepth.release();
+  t->msig.release();
+  t->mrat.release();
+  t->mpart.release();
+  t->mlist.release();
+  t->micnt.release();
+  t->mioff.release();
+  t->miv.release();
+  t->mil0.release();
+  t->mtab.release();
   if (t->h_small) cudaFreeHost(t->h_small);
   if (t->d_small) cudaFree(t->d_small);
   delete t;
@@ -1232,6 +1253,526 @@ sst_status common_neighbors_batch(sst_graph *g, const uint32_t *d_pairs,
   if (n == 0) return SST_OK;
   SST_LAUNCH(k_common, blocks_for(n), kTB, 0, g->stream, g->view(), d_pairs, n,
              early_end, d_out);
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+
+// ================================================ multi-source BFS and BC
+// Multi-source BFS: k <= 64 sources traverse together.  Each vertex holds a
+// mask of the sources that have reached it (vis) and of those for which it
+// is on the current level (fr); one level is one pass for all sources -- a
+// push from the frontier queue while the frontier's edges are few, else a
+// pull over all unfinished vertices -- followed by one update pass that
+// turns the collected masks into new depths and the next queue.
+namespace {
+
+__global__ void k_msbfs_seed(const uint32_t *__restrict__ sv,
+                             const unsigned long long *__restrict__ sm,
+                             uint32_t cnt, uint32_t n,
+                             unsigned long long *__restrict__ vis,
+                             unsigned long long *__restrict__ fr,
+                             int32_t *__restrict__ depth,
+                             const uint32_t *__restrict__ deg,
+                             const uint32_t *__restrict__ cap,
+                             uint32_t *__restrict__ q,
+                             unsigned long long *__restrict__ qc) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  uint32_t v = sv[i];
+  unsigned long long m = sm[i];
+  vis[v] = m;
+  fr[v] = m;
+  for (unsigned long long b = m; b; b &= b - 1)
+    depth[(uint64_t)(__ffsll((long long)b) - 1) * n + v] = 0;
+  q[i] = v;
+  atomicAdd(&qc[1], (unsigned long long)deg[v]);
+  atomicAdd(&qc[2], (unsigned long long)items_of(cap[v]));
+}
+
+// push: warp per work item (a frontier vertex's leaf chunk), lane = slot
+__global__ void k_msbfs_push(DGraph g, const uint32_t *__restrict__ iv,
+                             const uint32_t *__restrict__ il0, uint32_t nitems,
+                             const unsigned long long *__restrict__ fr,
+                             const unsigned long long *__restrict__ vis,
+                             unsigned long long *__restrict__ nx) {
+  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= nitems) return;
+  uint32_t u = iv[i];
+  const unsigned long long f = fr[u];
+  uint64_t base = g.base[u];
+  uint32_t cap = g.cap[u], deg = g.deg[u];
+  uint32_t nl = cap ? nleaves_of(cap) : 0;
+  uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+  for (uint32_t l = l0; l < l1; l++) {
+    uint32_t c = leaf_count(g, base, cap, deg, l);
+    if ((uint32_t)lane < c) {
+      uint32_t w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
+      unsigned long long add = f & ~vis[w];
+      if (add) atomicOr(&nx[w], add);
+    }
+  }
+}
+
+// pull, one-leaf vertices: thread per vertex, stops once every source that
+// has not reached v is seen in the frontier
+__global__ void k_msbfs_pull_small(DGraph g, const uint32_t *__restrict__ small,
+                                   uint64_t nsmall,
+                                   const unsigned long long *__restrict__ fr,
+                                   const unsigned long long *__restrict__ vis,
+                                   unsigned long long *__restrict__ nx,
+                                   unsigned long long full) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsmall) return;
+  uint32_t v = small[i];
+  const unsigned long long need = full & ~vis[v];
+  if (!need) return;
+  const uint32_t *p = g.slots + g.base[v];
+  uint32_t d = g.deg[v];
+  unsigned long long acc = 0;
+  for (uint32_t k = 0; k < d; k++) {
+    acc |= fr[p[k]];
+    if ((acc & need) == need) break;
+  }
+  acc &= need;
+  if (acc) nx[v] = acc;
+}
+
+__device__ __forceinline__ unsigned long long warp_or64(unsigned long long x) {
+  unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)x);
+  unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(x >> 32));
+  return ((unsigned long long)hi << 32) | lo;
+}
+
+// pull, multi-leaf vertices: warp per chunk (lane = slot), early exit
+__global__ void k_msbfs_pull_chunks(DGraph g,
+                                    const unsigned long long *__restrict__ cdesc,
+                                    const uint32_t *__restrict__ cv,
+                                    uint64_t nchunks,
+                                    const unsigned long long *__restrict__ fr,
+                                    const unsigned long long *__restrict__ vis,
+                                    unsigned long long *__restrict__ nx,
+                                    unsigned long long full) {
+  uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= nchunks) return;
+  const uint32_t v = cv[c];
+  const unsigned long long need = full & ~vis[v];
+  if (!need) return;
+  const unsigned long long dsc = cdesc[c];
+  const uint64_t leaf0 = dsc >> 8;
+  const uint32_t l1 = (uint32_t)(dsc & 63);
+  const bool single = (dsc >> 7) & 1;
+  const uint32_t mycnt = (uint32_t)lane < l1 ? g.lcnt[leaf0 + lane] : 0u;
+  const uint32_t *sl = g.slots + (leaf0 << kLeafLog) + lane;
+  unsigned long long acc = 0;
+  for (uint32_t l = 0; l < l1; l += 4) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      uint32_t cq = __shfl_sync(0xffffffffu, mycnt, (l + q) & 31);
+      if (l + q >= l1) cq = 0;
+      if ((uint32_t)lane < cq) acc |= fr[sl[(uint64_t)(l + q) << kLeafLog]];
+    }
+    if ((warp_or64(acc) & need) == need) break;
+  }
+  acc = warp_or64(acc) & need;
+  if (lane == 0 && acc) {
+    if (single)
+      nx[v] = acc;
+    else
+      atomicOr(&nx[v], acc);
+  }
+}
+
+// new sources per vertex -> depths, next frontier masks and queue
+__global__ void k_msbfs_update(uint32_t n, unsigned long long *__restrict__ vis,
+                               unsigned long long *__restrict__ nx,
+                               unsigned long long *__restrict__ fr_next,
+                               int32_t *__restrict__ depth, int32_t lvl,
+                               const uint32_t *__restrict__ deg,
+                               const uint32_t *__restrict__ cap,
+                               uint32_t *__restrict__ q,
+                               unsigned long long *__restrict__ qc) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long nw = 0;
+  if (v < n) {
+    unsigned long long x = nx[v];
+    if (x) {
+      nx[v] = 0;
+      unsigned long long old = vis[v];
+      nw = x & ~old;
+      if (nw) {
+        vis[v] = old | nw;
+        for (unsigned long long b = nw; b; b &= b - 1)
+          depth[(uint64_t)(__ffsll((long long)b) - 1) * n + v] = lvl;
+      }
+    }
+    fr_next[v] = nw;
+  }
+  enqueue(nw != 0, v, nw ? deg[v] : 0u, nw ? items_of(cap[v]) : 0u, q, qc);
+}
+
+// ---- multi-source BC: the single-source passes with the source on
+// blockIdx.y; per (source, level) the list start, list count, item start and
+// item count come from tab[(s * L + d) * 4 + 0..3]
+__global__ void k_msbc_maxdepth(const int32_t *__restrict__ depth, uint32_t n,
+                                unsigned long long *__restrict__ out) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  int32_t d = v < n ? depth[(uint64_t)blockIdx.y * n + v] : -1;
+  for (int o = 16; o > 0; o >>= 1) d = max(d, __shfl_down_sync(0xffffffffu, d, o));
+  if ((threadIdx.x & 31) == 0 && d >= 0) atomicMax(out, (unsigned long long)d);
+}
+
+__global__ void k_msbc_level_count(const int32_t *__restrict__ depth, uint32_t n,
+                                   uint32_t L, uint32_t *__restrict__ cnt) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  int32_t d = depth[(uint64_t)blockIdx.y * n + v];
+  if (d >= 0) atomicAdd(&cnt[blockIdx.y * L + d], 1u);
+}
+
+__global__ void k_msbc_level_scatter(const int32_t *__restrict__ depth,
+                                     uint32_t n, uint32_t L,
+                                     const uint32_t *__restrict__ start,
+                                     uint32_t *__restrict__ ctr,
+                                     uint32_t *__restrict__ list) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  int32_t d = depth[(uint64_t)blockIdx.y * n + v];
+  if (d < 0) return;
+  uint32_t at = blockIdx.y * L + d;
+  list[start[at] + atomicAdd(&ctr[at], 1u)] = v;
+}
+
+__global__ void k_msbc_init(const uint32_t *__restrict__ srcs, uint32_t n,
+                            double *__restrict__ sigma, double *__restrict__ ratio,
+                            double *__restrict__ dep) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  uint64_t at = (uint64_t)blockIdx.y * n + v;
+  sigma[at] = v == srcs[blockIdx.y] ? 1.0 : 0.0;
+  ratio[at] = 0.0;
+  dep[at] = 0.0;
+}
+
+__global__ void k_msbc_sigma_small(DGraph g, const uint32_t *__restrict__ list,
+                                   const uint32_t *__restrict__ tab, uint32_t L,
+                                   int32_t d, const int32_t *__restrict__ depth,
+                                   double *__restrict__ sigma) {
+  const uint32_t *e = tab + ((uint64_t)blockIdx.y * L + d) * 4;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= e[1]) return;
+  uint32_t v = list[e[0] + i];
+  if (g.cap[v] > kLeaf) return;
+  const uint64_t so = (uint64_t)blockIdx.y * g.n;
+  const uint32_t *p = g.slots + g.base[v];
+  uint32_t dg = g.deg[v];
+  double acc = 0.0;
+  for (uint32_t k = 0; k < dg; k++) {
+    uint32_t u = p[k];
+    if (depth[so + u] == d - 1) acc += sigma[so + u];
+  }
+  sigma[so + v] = acc;
+}
+
+__global__ void k_msbc_chunks(DGraph g, const uint32_t *__restrict__ iv,
+                              const uint32_t *__restrict__ il0,
+                              const uint32_t *__restrict__ tab, uint32_t L,
+                              int32_t d, const int32_t *__restrict__ depth,
+                              const double *__restrict__ val, int32_t want,
+                              double *__restrict__ partial) {
+  const uint32_t *e = tab + ((uint64_t)blockIdx.y * L + d) * 4;
+  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= e[3]) return;
+  i += e[2];
+  const uint64_t so = (uint64_t)blockIdx.y * g.n;
+  uint32_t v = iv[i];
+  uint32_t nl = g.cap[v] >> kLeafLog;
+  uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+  uint64_t base = g.base[v];
+  const uint8_t *lc = g.lcnt + (base >> kLeafLog);
+  double acc = 0.0;
+  for (uint32_t l = l0; l < l1; l++) {
+    if ((uint32_t)lane < lc[l]) {
+      uint32_t u = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
+      if (depth[so + u] == want) acc += val[so + u];
+    }
+  }
+  double sum = warp_sum_d(acc);
+  if (lane == 0) partial[i] = sum;
+}
+
+__global__ void k_msbc_fix(DGraph g, const uint32_t *__restrict__ list,
+                           const uint32_t *__restrict__ tab, uint32_t L,
+                           int32_t d, const uint32_t *__restrict__ cnt,
+                           const uint32_t *__restrict__ off,
+                           const double *__restrict__ partial, bool sigma_pass,
+                           double *__restrict__ sigma, double *__restrict__ ratio,
+                           double *__restrict__ dep) {
+  const uint32_t *e = tab + ((uint64_t)blockIdx.y * L + d) * 4;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= e[1]) return;
+  uint32_t p = e[0] + i;
+  uint32_t k = cnt[p];
+  if (k == 0) return;
+  double acc = 0.0;
+  for (uint32_t j = 0; j < k; j++) acc += partial[off[p] + j];
+  const uint64_t at = (uint64_t)blockIdx.y * g.n + list[p];
+  if (sigma_pass) {
+    sigma[at] = acc;
+  } else {
+    double dv = sigma[at] * acc;
+    dep[at] = dv;
+    ratio[at] = (1.0 + dv) / sigma[at];
+  }
+}
+
+__global__ void k_msbc_delta_small(DGraph g, const uint32_t *__restrict__ list,
+                                   const uint32_t *__restrict__ tab, uint32_t L,
+                                   int32_t d, const int32_t *__restrict__ depth,
+                                   const double *__restrict__ sigma,
+                                   double *__restrict__ ratio,
+                                   double *__restrict__ dep) {
+  const uint32_t *e = tab + ((uint64_t)blockIdx.y * L + d) * 4;
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= e[1]) return;
+  uint32_t v = list[e[0] + i];
+  if (g.cap[v] > kLeaf) return;
+  const uint64_t so = (uint64_t)blockIdx.y * g.n;
+  const uint32_t *p = g.slots + g.base[v];
+  uint32_t dg = g.deg[v];
+  double acc = 0.0;
+  for (uint32_t k = 0; k < dg; k++) {
+    uint32_t w = p[k];
+    if (depth[so + w] == d + 1) acc += ratio[so + w];
+  }
+  double dv = sigma[so + v] * acc;
+  dep[so + v] = dv;
+  ratio[so + v] = (1.0 + dv) / sigma[so + v];
+}
+
+}  // namespace
+
+sst_status bfs_multi(sst_graph *g, const uint32_t *h_srcs, uint32_t k,
+                     int32_t *d_depth) {
+  if (k == 0) return SST_OK;
+  if (k > 64) {
+    set_error_message("at most 64 sources per multi-source BFS");
+    return SST_EINVAL;
+  }
+  sst_status st = ensure_lists(g);
+  if (st != SST_OK) return st;
+  TravState *t = g->trav;
+  cudaStream_t s = g->stream;
+  const uint32_t n = g->n;
+  // distinct sources with their source masks
+  std::vector<uint32_t> sv;
+  std::vector<unsigned long long> sm;
+  for (uint32_t i = 0; i < k; i++) {
+    if (h_srcs[i] >= n) {
+      set_error_message("source %u out of range", h_srcs[i]);
+      return SST_EINVAL;
+    }
+    auto it = std::find(sv.begin(), sv.end(), h_srcs[i]);
+    if (it == sv.end()) {
+      sv.push_back(h_srcs[i]);
+      sm.push_back(1ull << i);
+    } else {
+      sm[it - sv.begin()] |= 1ull << i;
+    }
+  }
+  const unsigned long long full = k == 64 ? ~0ull : (1ull << k) - 1;
+  SST_CUDA_TRY(t->mvis.ensure(n));
+  SST_CUDA_TRY(t->mfr.ensure(n));
+  SST_CUDA_TRY(t->mfr2.ensure(n));
+  SST_CUDA_TRY(t->mnx.ensure(n));
+  SST_CUDA_TRY(t->qa.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->qb.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->icnt.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->ioff.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->msrc.ensure(2 * (uint64_t)sv.size()));
+  SST_CUDA_TRY(cudaMemsetAsync(t->mvis.p, 0, (uint64_t)n * 8, s));
+  SST_CUDA_TRY(cudaMemsetAsync(t->mfr.p, 0, (uint64_t)n * 8, s));
+  SST_CUDA_TRY(cudaMemsetAsync(t->mnx.p, 0, (uint64_t)n * 8, s));
+  SST_CUDA_TRY(cudaMemsetAsync(d_depth, 0xFF, (uint64_t)k * n * 4, s));
+  unsigned long long *d_sm = t->msrc.p;
+  uint32_t *d_sv = reinterpret_cast<uint32_t *>(t->msrc.p + sv.size());
+  SST_CUDA_TRY(cudaMemcpyAsync(d_sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice, s));
+  SST_CUDA_TRY(cudaMemcpyAsync(d_sm, sm.data(), sm.size() * 8, cudaMemcpyHostToDevice, s));
+  unsigned long long *qc = t->d_small;
+  SST_CUDA_TRY(cudaMemsetAsync(qc, 0, 24, s));
+  uint32_t *q = t->qa.p, *nq = t->qb.p;
+  unsigned long long *fr = t->mfr.p, *fr2 = t->mfr2.p;
+  SST_LAUNCH(k_msbfs_seed, blocks_for(sv.size()), kTB, 0, s, d_sv, d_sm,
+             (uint32_t)sv.size(), n, t->mvis.p, fr, d_depth, g->d_deg, g->d_cap,
+             q, qc);
+  SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, qc, 24, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t qn = sv.size(), qdeg = t->h_small[1], qitems = t->h_small[2];
+  const uint64_t m = g->m;
+  DGraph dg = g->view();
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes((uint64_t)n + 1, 4) + 4096));
+  for (int32_t lvl = 0; qn > 0; lvl++) {
+    if ((uint64_t)lvl > n) {
+      set_error_message("multi-source BFS exceeded n levels");
+      return SST_ETIMEDOUT;
+    }
+    if ((qn + qdeg) * 20 > m) {
+      if (t->nsmall)
+        SST_LAUNCH(k_msbfs_pull_small, blocks_for(t->nsmall), kTB, 0, s, dg,
+                   t->small.p, t->nsmall, fr, t->mvis.p, t->mnx.p, full);
+      if (t->nchunks)
+        SST_LAUNCH(k_msbfs_pull_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg,
+                   t->cdesc.p, t->cv.p, t->nchunks, fr, t->mvis.p, t->mnx.p, full);
+    } else {
+      SST_CUDA_TRY(t->iv.ensure(qitems + 1));
+      SST_CUDA_TRY(t->il0.ensure(qitems + 1));
+      SST_LAUNCH(k_front_items, blocks_for(qn), kTB, 0, s, q, (uint32_t)qn,
+                 g->d_cap, t->icnt.p);
+      g->arena.reset();
+      SST_CUDA_TRY((scan<uint32_t, OpAdd>(t->icnt.p, t->ioff.p, qn, 0u, OpAdd{},
+                                          true, false, nullptr, g->arena, s)));
+      SST_LAUNCH(k_front_expand, blocks_for(qn), kTB, 0, s, q, (uint32_t)qn,
+                 g->d_cap, t->ioff.p, t->iv.p, t->il0.p);
+      SST_LAUNCH(k_msbfs_push, warp_blocks(qitems), kTB, 0, s, dg, t->iv.p,
+                 t->il0.p, (uint32_t)qitems, fr, t->mvis.p, t->mnx.p);
+    }
+    SST_CUDA_TRY(cudaMemsetAsync(qc, 0, 24, s));
+    SST_LAUNCH(k_msbfs_update, blocks_for(n), kTB, 0, s, n, t->mvis.p, t->mnx.p,
+               fr2, d_depth, lvl + 1, g->d_deg, g->d_cap, nq, qc);
+    SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, qc, 24, cudaMemcpyDeviceToHost, s));
+    SST_CUDA_TRY(cudaStreamSynchronize(s));
+    qn = t->h_small[0];
+    qdeg = t->h_small[1];
+    qitems = t->h_small[2];
+    std::swap(q, nq);
+    std::swap(fr, fr2);
+  }
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+sst_status bc_multi(sst_graph *g, const uint32_t *h_srcs, uint32_t k,
+                    double *d_dep) {
+  if (k == 0) return SST_OK;
+  TravState *t = state(g);
+  const uint32_t n = g->n;
+  SST_CUDA_TRY(t->mdepth.ensure((uint64_t)k * n));
+  sst_status st = bfs_multi(g, h_srcs, k, t->mdepth.p);
+  if (st != SST_OK) return st;
+  cudaStream_t s = g->stream;
+  const int32_t *depth = t->mdepth.p;
+  const dim3 vgrid(blocks_for(n), k);
+  SST_CUDA_TRY(cudaMemsetAsync(t->d_small, 0, 8, s));
+  SST_LAUNCH(k_msbc_maxdepth, vgrid, kTB, 0, s, depth, n, t->d_small);
+  SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, t->d_small, 8, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  const uint32_t D = (uint32_t)t->h_small[0];
+  const uint32_t L = D + 2;  // levels 0..D plus an end marker
+  // per (source, level): vertex counts -> list starts
+  SST_CUDA_TRY(t->mtab.ensure((uint64_t)k * L * 7));
+  uint32_t *cnt = t->mtab.p, *start = cnt + (uint64_t)k * L, *ctr = start + (uint64_t)k * L;
+  uint32_t *tab = ctr + (uint64_t)k * L;  // k * L * 4 words
+  SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, (uint64_t)k * L * 4, s));
+  SST_CUDA_TRY(cudaMemsetAsync(ctr, 0, (uint64_t)k * L * 4, s));
+  SST_LAUNCH(k_msbc_level_count, vgrid, kTB, 0, s, depth, n, L, cnt);
+  std::vector<uint32_t> hc((uint64_t)k * L), hs((uint64_t)k * L);
+  SST_CUDA_TRY(cudaMemcpyAsync(hc.data(), cnt, hc.size() * 4, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t acc = 0;
+  for (uint64_t i = 0; i < hc.size(); i++) {
+    hs[i] = (uint32_t)acc;
+    acc += hc[i];
+  }
+  if (acc >= 0xFFFFFFFFull) {
+    set_error_message("too many (source, vertex) pairs for one multi-source BC");
+    return SST_EINVAL;
+  }
+  const uint32_t RR = (uint32_t)acc;
+  SST_CUDA_TRY(cudaMemcpyAsync(start, hs.data(), hs.size() * 4, cudaMemcpyHostToDevice, s));
+  SST_CUDA_TRY(t->mlist.ensure((uint64_t)RR + 1));
+  SST_LAUNCH(k_msbc_level_scatter, vgrid, kTB, 0, s, depth, n, L, start, ctr,
+             t->mlist.p);
+  // leaf-chunk items of the multi-leaf vertices, in list order
+  SST_CUDA_TRY(t->micnt.ensure((uint64_t)RR + 1));
+  SST_CUDA_TRY(t->mioff.ensure((uint64_t)RR + 1));
+  const uint32_t *list = t->mlist.p;
+  if (RR) SST_LAUNCH(k_bc_item_counts, blocks_for(RR), kTB, 0, s, list, RR, g->d_cap, t->micnt.p);
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes((uint64_t)RR + 1, 4) + 4096));
+  SST_CUDA_TRY((scan<uint32_t, OpAdd>(t->micnt.p, t->mioff.p, RR, 0u, OpAdd{},
+                                      true, false, t->mioff.p + RR, g->arena, s)));
+  // item starts at each (source, level) list start, and the total
+  std::vector<uint32_t> hpos(hs.size() + 1);
+  for (uint64_t i = 0; i < hs.size(); i++) hpos[i] = hs[i];
+  hpos[hs.size()] = RR;
+  SST_CUDA_TRY(cudaMemcpyAsync(ctr, hpos.data(), (uint64_t)k * L * 4, cudaMemcpyHostToDevice, s));
+  std::vector<uint32_t> hib((uint64_t)k * L + 1);
+  SST_CUDA_TRY(t->mpart.ensure((uint64_t)k * L + 2));
+  uint32_t *d_ib = reinterpret_cast<uint32_t *>(t->mpart.p);
+  SST_LAUNCH(k_gather_bounds, blocks_for((uint64_t)k * L), kTB, 0, s, t->mioff.p,
+             ctr, (uint32_t)(k * L), d_ib);
+  SST_CUDA_TRY(cudaMemcpyAsync(hib.data(), d_ib, (uint64_t)k * L * 4, cudaMemcpyDeviceToHost, s));
+  uint32_t items = 0;
+  SST_CUDA_TRY(cudaMemcpyAsync(&items, t->mioff.p + RR, 4, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  hib[(uint64_t)k * L] = items;
+  // the table: list start, count, item start, item count per (source, level)
+  std::vector<uint32_t> ht((uint64_t)k * L * 4);
+  std::vector<uint32_t> maxc(L, 0), maxi(L, 0);
+  for (uint32_t sidx = 0; sidx < k; sidx++)
+    for (uint32_t d = 0; d < L; d++) {
+      uint64_t at = (uint64_t)sidx * L + d;
+      uint32_t i0 = hib[at], i1 = hib[at + 1];
+      ht[at * 4 + 0] = hs[at];
+      ht[at * 4 + 1] = hc[at];
+      ht[at * 4 + 2] = i0;
+      ht[at * 4 + 3] = i1 - i0;
+      maxc[d] = std::max(maxc[d], hc[at]);
+      maxi[d] = std::max(maxi[d], i1 - i0);
+    }
+  SST_CUDA_TRY(cudaMemcpyAsync(tab, ht.data(), ht.size() * 4, cudaMemcpyHostToDevice, s));
+  SST_CUDA_TRY(t->miv.ensure((uint64_t)items + 1));
+  SST_CUDA_TRY(t->mil0.ensure((uint64_t)items + 1));
+  SST_CUDA_TRY(t->mpart.ensure((uint64_t)items + 1));
+  if (items && RR)
+    SST_LAUNCH(k_bc_expand, blocks_for(RR), kTB, 0, s, list, RR, t->micnt.p,
+               t->mioff.p, t->miv.p, t->mil0.p);
+  SST_CUDA_TRY(t->msig.ensure((uint64_t)k * n));
+  SST_CUDA_TRY(t->mrat.ensure((uint64_t)k * n));
+  // the sources, staged in the (now free) scatter counters
+  SST_CUDA_TRY(cudaMemcpyAsync(ctr, h_srcs, (uint64_t)k * 4, cudaMemcpyHostToDevice, s));
+  SST_LAUNCH(k_msbc_init, vgrid, kTB, 0, s, ctr, n, t->msig.p, t->mrat.p, d_dep);
+  DGraph dg = g->view();
+  double *part = t->mpart.p;
+  for (uint32_t d = 1; d <= D; d++) {
+    if (maxc[d])
+      SST_LAUNCH(k_msbc_sigma_small, dim3(blocks_for(maxc[d]), k), kTB, 0, s, dg,
+                 list, tab, L, (int32_t)d, depth, t->msig.p);
+    if (maxi[d]) {
+      SST_LAUNCH(k_msbc_chunks, dim3(warp_blocks(maxi[d]), k), kTB, 0, s, dg,
+                 t->miv.p, t->mil0.p, tab, L, (int32_t)d, depth, t->msig.p,
+                 (int32_t)d - 1, part);
+      SST_LAUNCH(k_msbc_fix, dim3(blocks_for(maxc[d]), k), kTB, 0, s, dg, list,
+                 tab, L, (int32_t)d, t->micnt.p, t->mioff.p, part, true,
+                 t->msig.p, t->mrat.p, d_dep);
+    }
+  }
+  for (int32_t d = (int32_t)D; d >= 0; d--) {
+    if (maxc[d])
+      SST_LAUNCH(k_msbc_delta_small, dim3(blocks_for(maxc[d]), k), kTB, 0, s, dg,
+                 list, tab, L, d, depth, t->msig.p, t->mrat.p, d_dep);
+    if (maxi[d]) {
+      SST_LAUNCH(k_msbc_chunks, dim3(warp_blocks(maxi[d]), k), kTB, 0, s, dg,
+                 t->miv.p, t->mil0.p, tab, L, d, depth, t->mrat.p, d + 1, part);
+      SST_LAUNCH(k_msbc_fix, dim3(blocks_for(maxc[d]), k), kTB, 0, s, dg, list,
+                 tab, L, d, t->micnt.p, t->mioff.p, part, false, t->msig.p,
+                 t->mrat.p, d_dep);
+    }
+  }
   SST_CUDA_TRY(cudaGetLastError());
   return SST_OK;
 }

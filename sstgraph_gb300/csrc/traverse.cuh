@@ -12,6 +12,14 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping,
                     double *d_rank);
 sst_status cc(sst_graph *g, uint32_t *d_labels);
 sst_status bc(sst_graph *g, uint32_t src, double *d_dep);
+// k <= 64 sources (host array) in one traversal; d_depth is k x n
+// (row per source, -1 unreached)
+sst_status bfs_multi(sst_graph *g, const uint32_t *h_srcs, uint32_t k,
+                     int32_t *d_depth);
+// single-source BC of each of k <= 64 sources, all sources per launch;
+// d_dep is k x n, row s equal to bc(g, srcs[s])
+sst_status bc_multi(sst_graph *g, const uint32_t *h_srcs, uint32_t k,
+                    double *d_dep);
 sst_status tc(sst_graph *g, uint64_t *total, uint64_t *d_per_vertex);
 sst_status tc_vertices(sst_graph *g, const uint32_t *d_vs, uint64_t k,
                        uint64_t *d_out);
