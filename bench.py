@@ -55,7 +55,8 @@ def args_parse():
     ap.add_argument("--serve-requests", type=int, default=400)
     ap.add_argument("--serve-rate", type=float, default=300.0)
     ap.add_argument("--only", default="all",
-                    choices=["all", "updates", "pagerank", "bfs", "batched", "serving"],
+                    choices=["all", "updates", "pagerank", "bfs", "batched", "serving",
+                             "multi"],
                     help="one part of the run (profiling cases): the update steps "
                          "alone, or one traversal on the base graph")
     return ap.parse_args()
@@ -324,6 +325,47 @@ def main():
                "kernels": sg.profile_collect()}
         return bfs
 
+    def measure_multi():
+        """64-source BFS and 16-source BC (uniform sources) in one call each,
+        against the same sources run one call per source."""
+        rng = np.random.default_rng(17)
+        res = {}
+        for kind, k in (("bfs", 64), ("bc", 16)):
+            srcs = rng.integers(0, n, k).astype(np.uint32)
+            dt = torch.int32 if kind == "bfs" else torch.float64
+            out = torch.empty((k, n), dtype=dt, device="cuda")
+            one = torch.empty(n, dtype=dt, device="cuda")
+            multi_fn = sg.BFS_multi if kind == "bfs" else sg.BC_multi
+
+            def single(s):
+                if kind == "bfs":
+                    sg.BFS(g, int(s), depths=True, out=one)
+                else:
+                    sg.BC(g, int(s), out=one)
+            multi_fn(g, srcs, out=out)  # warm
+            torch.cuda.synchronize()
+            t = {}
+            for form in ("multi", "single"):
+                s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s0.record(stream)
+                if form == "multi":
+                    multi_fn(g, srcs, out=out)
+                else:
+                    for sidx in srcs:
+                        single(sidx)
+                s1.record(stream)
+                s1.synchronize()
+                t[form] = s0.elapsed_time(s1) / 1e3
+            # spot check: the last source's row equals its single-source result
+            single(srcs[-1])
+            torch.cuda.synchronize()
+            same = bool(torch.equal(out[k - 1], one))
+            res[kind] = {"sources": k, "multi_ms": 1e3 * t["multi"],
+                         "single_ms": 1e3 * t["single"],
+                         "speedup": t["single"] / t["multi"], "last_row_equal": same}
+            del out
+        return res
+
     def measure_batched():
         """The same stream of uneven insert batches (log-normal sizes, median
         1e4, sigma 1.5, clipped to [1e3, 1e6]) applied to two device copies of
@@ -443,6 +485,8 @@ def main():
             res["serving"] = measure_serving()
         elif a.only == "batched":
             res["batched"] = measure_batched()
+        elif a.only == "multi":
+            res["multi_source"] = measure_multi()
         else:
             res["bfs"] = measure_bfs()
         g.close()
@@ -524,7 +568,7 @@ def main():
            "note": "insert+remove via sst_insert_batch/sst_remove_batch on pinned host "
                    "pairs; each call returns the invalid-pair count (8 B) to the host"}
 
-    batched = pagerank = bfs = serving = None
+    batched = pagerank = bfs = serving = multi = None
     if a.only == "all":
         batched = measure_batched()
         pagerank = measure_pagerank()
@@ -549,6 +593,7 @@ def main():
         pagerank["degree_ordered"] = pr_deg
         gr.close()
         bfs = measure_bfs()
+        multi = measure_multi()
         serving = measure_serving()
 
 
@@ -586,6 +631,7 @@ def main():
         "batched_form": batched,
         "pagerank": pagerank,
         "bfs": bfs,
+        "multi_source": multi,
         "serving": serving,
         "update_kernels": upd_kernels,
     }

@@ -490,21 +490,34 @@ def BC(g: SparseMatrixV, src: int, out=None):
     return buf
 
 
-def _sources(srcs):
+def _sources(srcs, flags, like):
+    """Source ids where the call's flags say the arrays are (host or the
+    output tensor's device)."""
     if hasattr(srcs, "data_ptr"):
-        return srcs, ctypes.c_void_p(srcs.data_ptr())
-    a = np.ascontiguousarray(np.asarray(srcs, np.uint32).ravel())
+        if flags == DEVICE_PTR and srcs.is_cuda:
+            srcs = srcs.contiguous()
+            return srcs, ctypes.c_void_p(srcs.data_ptr())
+        srcs = srcs.cpu().numpy()
+    a = np.ascontiguousarray(np.asarray(srcs).astype(np.uint32).ravel())
+    if flags == DEVICE_PTR:
+        import torch
+        t = torch.from_numpy(a.view(np.int32)).to(like.device)
+        return t, ctypes.c_void_p(t.data_ptr())
     return a, ctypes.c_void_p(a.ctypes.data)
+
+
+def _count(srcs):
+    return int(srcs.numel()) if hasattr(srcs, "numel") else int(np.asarray(srcs).size)
 
 
 def BFS_multi(g: SparseMatrixV, srcs, out=None):
     """Depths from each of k <= 64 sources in one traversal: (k, rows)
     int32, row i for srcs[i], -1 unreached."""
-    keep, sp = _sources(srcs)
-    k = len(keep)
+    k = _count(srcs)
     if out is None:
         out = np.empty((k, g.rows), np.int32)
     p, flags = _ptr(out)
+    keep, sp = _sources(srcs, flags, out)
     _check(lib().sst_bfs_multi(g.handle, sp, k, p, flags))
     return out
 
@@ -512,11 +525,11 @@ def BFS_multi(g: SparseMatrixV, srcs, out=None):
 def BC_multi(g: SparseMatrixV, srcs, out=None):
     """BC(g, s) for each of k <= 64 sources, every launch covering all of
     them: (k, rows) float64, row i equal to BC(g, srcs[i])."""
-    keep, sp = _sources(srcs)
-    k = len(keep)
+    k = _count(srcs)
     if out is None:
         out = np.empty((k, g.rows), np.float64)
     p, flags = _ptr(out)
+    keep, sp = _sources(srcs, flags, out)
     _check(lib().sst_bc_multi(g.handle, sp, k, p, flags))
     return out
 
