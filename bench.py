@@ -108,10 +108,28 @@ class Clocks:
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+        # the timed region can be shorter than the sampling period: start it
+        # only once the sampler is producing, and stop the sampler only after
+        # it has taken one more sample
+        self.lines0 = self._wait_lines(1)
         return self
+
+    def _wait_lines(self, at_least, limit_s=3.0):
+        t0 = time.time()
+        while self.proc and time.time() - t0 < limit_s:
+            self.f.flush()
+            try:
+                k = sum(1 for _ in open(self.path))
+            except OSError:
+                k = 0
+            if k >= at_least:
+                return k
+            time.sleep(0.02)
+        return 0
 
     def __exit__(self, *a):
         if self.proc:
+            self._wait_lines(self.lines0 + 1)
             self.proc.terminate()
             self.proc.wait()
             self.f.close()

@@ -66,6 +66,9 @@ typedef struct sst_config {
   float upper_root;            /* PMA root upper density (0 = default .85) */
   float lower_root;            /* PMA root lower density (0 = default .20) */
   float grow_fill;             /* density after a resize (0 = default .70) */
+  uint32_t keep_self_loops;    /* 1 = insert (v, v) as well: rows are plain
+                                  sets (the TinySet facade); 0 = skip them as
+                                  SparseMatrix.hpp:570,602 does */
 } sst_config;
 
 /* ---- lifetime ------------------------------------------------------- */

@@ -42,7 +42,8 @@ class sst_config(ctypes.Structure):
                 ("initial_slots", ctypes.c_uint64),
                 ("upper_root", ctypes.c_float),
                 ("lower_root", ctypes.c_float),
-                ("grow_fill", ctypes.c_float)]
+                ("grow_fill", ctypes.c_float),
+                ("keep_self_loops", ctypes.c_uint32)]
 
 
 class sst_server_config(ctypes.Structure):
@@ -195,13 +196,15 @@ class SparseMatrixV:
     def __init__(self, height: int, width: int | None = None, *, device: int = 0,
                  hbm_budget_bytes: int = 0, initial_slots: int = 0,
                  upper_root: float = 0.0, lower_root: float = 0.0,
-                 grow_fill: float = 0.0, _handle=None):
+                 grow_fill: float = 0.0, keep_self_loops: bool = False,
+                 _handle=None):
         self._h = None
         if _handle is not None:
             self._h = _handle
         else:
             cfg = sst_config(device, hbm_budget_bytes, initial_slots,
-                             upper_root, lower_root, grow_fill)
+                             upper_root, lower_root, grow_fill,
+                             1 if keep_self_loops else 0)
             h = ctypes.c_void_p()
             _check(lib().sst_graph_create(height, height if width is None else width,
                                           ctypes.byref(cfg), ctypes.byref(h)))
@@ -488,6 +491,69 @@ def BC(g: SparseMatrixV, src: int, out=None):
     p, flags = _ptr(buf)
     _check(lib().sst_bc(g.handle, src, p, flags))
     return buf
+
+
+class TinySetV:
+    """One sorted set of uint32 elements in [0, max_el) on the device: the
+    reference's binary TinySetV (include/SSTGraph/TinySet.hpp:27-73) as one
+    row of a device graph that keeps (0, 0)."""
+
+    def __init__(self, max_el: int, **kw):
+        self._g = SparseMatrixV(1, max(int(max_el), 1), keep_self_loops=True, **kw)
+
+    def _pairs(self, els):
+        if hasattr(els, "data_ptr"):
+            import torch
+            e = els.to(torch.int32).reshape(-1)
+            return torch.stack([torch.zeros_like(e), e], 1).contiguous()
+        e = np.asarray(els, np.uint32).reshape(-1)
+        return np.stack([np.zeros_like(e), e], 1)
+
+    def _check_range(self, els):
+        e = np.asarray(els.cpu() if hasattr(els, "cpu") else els, np.int64).reshape(-1)
+        if e.size and (e.min() < 0 or e.max() >= self._g.cols):
+            raise SSTError(-1, "element out of range for this set")
+
+    def has(self, e: int) -> bool:
+        return self._g.has(0, int(e)) if 0 <= int(e) < self._g.cols else False
+
+    def value(self, e: int) -> bool:
+        return self.has(e)
+
+    def insert(self, e: int):
+        self._check_range([e])
+        self._g.insert(0, int(e))
+
+    def remove(self, e: int):
+        if 0 <= int(e) < self._g.cols:
+            self._g.remove(0, int(e))
+
+    def insert_batch(self, els):
+        self._check_range(els)
+        self._g.insert_batch(self._pairs(els))
+
+    def remove_batch(self, els):
+        self._g.remove_batch(self._pairs(els))
+
+    def get_n(self) -> int:
+        return self._g.M()
+
+    def get_size(self) -> int:
+        return self._g.get_memory_size()
+
+    def map(self, f, no_early_exit: bool = True):
+        """f(element) in ascending order; without no_early_exit a true return
+        stops the walk (TinySet_small.hpp:303-319)."""
+        for x in self._g.neighbors(0):
+            r = f(int(x))
+            if not no_early_exit and r:
+                return
+
+    def elements(self) -> np.ndarray:
+        return self._g.neighbors(0)
+
+    def close(self):
+        self._g.close()
 
 
 def _sources(srcs, flags, like):

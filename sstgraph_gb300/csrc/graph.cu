@@ -106,8 +106,8 @@ __device__ __forceinline__ uint32_t warp_sum_lcnt(const uint8_t *lc,
 
 // ---------------------------------------------------------------- steps 1-5
 __global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
-                            uint32_t n, uint32_t width, int dbits, bool insert,
-                            uint64_t *__restrict__ keys,
+                            uint32_t n, uint32_t width, int dbits,
+                            bool drop_loops, uint64_t *__restrict__ keys,
                             unsigned long long *__restrict__ invalid) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b) return;
@@ -115,7 +115,7 @@ __global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
   const uint64_t sent = (uint64_t)n << dbits;
   bool ok = r < n && c < width && c != kEmpty;
   if (!ok) atomicAdd(invalid, 1ull);
-  keys[i] = (!ok || (insert && r == c)) ? sent : (((uint64_t)r << dbits) | c);
+  keys[i] = (!ok || (drop_loops && r == c)) ? sent : (((uint64_t)r << dbits) | c);
 }
 
 __global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
@@ -838,6 +838,7 @@ sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
     if (cfg->upper_root > 0) g->params.upper_root = cfg->upper_root;
     if (cfg->lower_root > 0) g->params.lower_root = cfg->lower_root;
     if (cfg->grow_fill > 0) g->params.grow_fill = cfg->grow_fill;
+    g->keep_loops = cfg->keep_self_loops != 0;
   }
   SST_CUDA_TRY(cudaSetDevice(g->device));
   SST_CUDA_TRY(cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, g->device));
@@ -895,6 +896,7 @@ sst_status graph_clone(const sst_graph *src, sst_graph *dst) {
   cfg.upper_root = src->params.upper_root;
   cfg.lower_root = src->params.lower_root;
   cfg.grow_fill = src->params.grow_fill;
+  cfg.keep_self_loops = src->keep_loops ? 1u : 0u;
   sst_status st = graph_init(dst, src->n, src->width, &cfg);
   if (st != SST_OK) return st;
   SST_CUDA_TRY(cudaStreamSynchronize(src->stream));
@@ -1056,7 +1058,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   if (!presorted) {
     // pair in (8 B), key out (8 B)
     SST_LAUNCH_B(16 * b, k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n, g->width,
-               dbits, insert, keys,
+               dbits, insert && !g->keep_loops, keys,
                reinterpret_cast<unsigned long long *>(&P->invalid));
     uint64_t *out = keys;
     SST_CUDA_TRY(radix_sort_u64(keys, ktmp, b, g->rbits + dbits, A, s, &out));
@@ -1217,7 +1219,7 @@ __global__ void k_make_keys_batched(const uint32_t *__restrict__ pairs,
                                     uint64_t N, const uint64_t *__restrict__ boff,
                                     uint32_t nb, const uint8_t *__restrict__ ops,
                                     uint32_t n, uint32_t width, int dbits,
-                                    uint64_t *__restrict__ keys,
+                                    bool drop_loops, uint64_t *__restrict__ keys,
                                     uint32_t *__restrict__ vals,
                                     unsigned long long *__restrict__ invalid) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1234,7 +1236,7 @@ __global__ void k_make_keys_batched(const uint32_t *__restrict__ pairs,
   const uint64_t sent = (uint64_t)n << dbits;
   bool ok = r < n && c < width && c != kEmpty;
   if (!ok) atomicAdd(invalid, 1ull);
-  keys[i] = (!ok || r == c) ? sent : (((uint64_t)r << dbits) | c);
+  keys[i] = (!ok || (drop_loops && r == c)) ? sent : (((uint64_t)r << dbits) | c);
   vals[i] = ops[lo] ? 1u : 0u;
 }
 
@@ -1291,7 +1293,7 @@ sst_status update_batches(sst_graph *g, const uint32_t *d_pairs,
   const int dbits = g->dbits;
   const uint64_t sent = (uint64_t)g->n << dbits;
   SST_LAUNCH(k_make_keys_batched, blocks_for(N), kTB, 0, s, d_pairs, N, d_boff,
-             nb, d_ops, g->n, g->width, dbits, keys, vals,
+             nb, d_ops, g->n, g->width, dbits, !g->keep_loops, keys, vals,
              reinterpret_cast<unsigned long long *>(&P->invalid));
   uint64_t *sk = keys;
   uint32_t *sv = vals;

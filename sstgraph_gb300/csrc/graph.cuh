@@ -54,6 +54,7 @@ struct sst_graph {
   int rbits = 0, dbits = 0;
   sst::PmaParams params;
   uint64_t budget = 0;
+  bool keep_loops = false;  // inserts keep (v, v) (per-row sets)
 
   uint64_t *d_base = nullptr;
   uint32_t *d_cap = nullptr;

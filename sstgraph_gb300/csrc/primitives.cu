@@ -17,6 +17,9 @@ namespace sst {
 
 static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launches(int64_t k) {
+  g_launches.fetch_add((uint64_t)k, std::memory_order_relaxed);
+}
 uint64_t launches() { return g_launches.load(std::memory_order_relaxed); }
 
 // ------------------------------------------------------------- profiler

@@ -9,7 +9,10 @@
 
 namespace sst {
 
+// kernels launched by this library (a captured graph's kernels count when
+// the graph is launched, not when it is captured)
 void note_launch();
+void note_launches(int64_t k);
 uint64_t launches();
 
 // Kernel profiler: while enabled, every launch is bracketed by a pair of

@@ -84,6 +84,14 @@ struct TravState {
   // multi-source bc: per (source, vertex) values and per-source level tables
   DevBuf<double> msig, mrat, mpart;
   DevBuf<uint32_t> mlist, micnt, mioff, miv, mil0, mtab;
+  // PageRank iterations captured as one CUDA graph, replayed while the
+  // graph version and the call's arguments stay the same
+  cudaGraphExec_t pr_exec = nullptr;
+  uint64_t pr_version = ~0ull;
+  uint32_t pr_iters = 0;
+  double pr_damping = 0.0;
+  const void *pr_key[6] = {};  // output, stream and the buffers it reads
+  int64_t pr_kernels = 0;      // kernels in the captured graph
   uint64_t *h_small = nullptr;  // pinned readback slots
   unsigned long long *d_small = nullptr;
 };
@@ -138,6 +146,7 @@ void trav_release(sst_graph *g) {
   t->miv.release();
   t->mil0.release();
   t->mtab.release();
+  if (t->pr_exec) cudaGraphExecDestroy(t->pr_exec);
   if (t->h_small) cudaFreeHost(t->h_small);
   if (t->d_small) cudaFree(t->d_small);
   delete t;
@@ -1007,25 +1016,61 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   unsigned long long *cin = reinterpret_cast<unsigned long long *>(t->ca.p);
   unsigned long long *cout = reinterpret_cast<unsigned long long *>(t->cb.p);
   unsigned long long *part = reinterpret_cast<unsigned long long *>(t->partial.p);
-  SST_LAUNCH(k_pr_start, blocks_for(n), kTB, 0, s, g->d_deg, n, r0f, rdeg, cin,
-             d_rank, base);
-  DGraph dg = g->view();
-  for (uint32_t it = 0; it < iters; it++) {
-    bool last = it + 1 == iters;
-    if (t->nsmall)
-      SST_LAUNCH(k_pr_small,
-                 blocks_for((t->nsmall + kSmallPer - 1) / kSmallPer * 8), kTB, 0,
-                 s, dg, t->sdesc.p, t->small.p, t->nsmall, cin, cout, d_rank,
-                 rdeg, K, last);
-    if (t->nchunks)
-      SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cdesc.p,
-                 t->cv.p, t->nchunks, cin, cout, d_rank, rdeg, part, K, last);
-    if (t->nmulti)
-      SST_LAUNCH(k_pr_fix, blocks_for(t->nmulti), kTB, 0, s, dg, t->multi.p,
-                 t->nmulti, t->choff.p, part, cout, d_rank, rdeg, K, last);
-    std::swap(cin, cout);
+  auto launch_all = [&]() {
+    unsigned long long *ci = cin, *co = cout;
+    SST_LAUNCH(k_pr_start, blocks_for(n), kTB, 0, s, g->d_deg, n, r0f, rdeg, ci,
+               d_rank, base);
+    DGraph dg = g->view();
+    for (uint32_t it = 0; it < iters; it++) {
+      bool last = it + 1 == iters;
+      if (t->nsmall)
+        SST_LAUNCH(k_pr_small,
+                   blocks_for((t->nsmall + kSmallPer - 1) / kSmallPer * 8), kTB, 0,
+                   s, dg, t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank,
+                   rdeg, K, last);
+      if (t->nchunks)
+        SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cdesc.p,
+                   t->cv.p, t->nchunks, ci, co, d_rank, rdeg, part, K, last);
+      if (t->nmulti)
+        SST_LAUNCH(k_pr_fix, blocks_for(t->nmulti), kTB, 0, s, dg, t->multi.p,
+                   t->nmulti, t->choff.p, part, co, d_rank, rdeg, K, last);
+      std::swap(ci, co);
+    }
+  };
+  // replay the captured iterations when nothing they depend on changed;
+  // with the kernel profiler on, launch them one by one so each is timed
+  const void *key[6] = {d_rank, s, cin, cout, part, rdeg};
+  bool same = t->pr_exec && t->pr_version == g->version &&
+              t->pr_iters == iters && t->pr_damping == damping;
+  for (int i = 0; i < 6 && same; i++) same = t->pr_key[i] == key[i];
+  if (profiling("k_pr_chunks") || profiling("k_pr_small")) {
+    launch_all();
+    SST_CUDA_TRY(cudaGetLastError());
+    return SST_OK;
   }
-  SST_CUDA_TRY(cudaGetLastError());
+  if (!same) {
+    if (t->pr_exec) cudaGraphExecDestroy(t->pr_exec);
+    t->pr_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    const uint64_t l0 = launches();
+    SST_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    launch_all();
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    t->pr_kernels = (int64_t)(launches() - l0);
+    note_launches(-t->pr_kernels);  // captured, not launched
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&t->pr_exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      t->pr_exec = nullptr;
+      SST_CUDA_TRY(e);
+    }
+    t->pr_version = g->version;
+    t->pr_iters = iters;
+    t->pr_damping = damping;
+    for (int i = 0; i < 6; i++) t->pr_key[i] = key[i];
+  }
+  SST_CUDA_TRY(cudaGraphLaunch(t->pr_exec, s));
+  note_launches(t->pr_kernels);
   return SST_OK;
 }
 

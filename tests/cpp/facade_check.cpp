@@ -9,8 +9,56 @@
 #include <vector>
 
 #include "sstgraph/SparseMatrix.hpp"
+#include "sstgraph/TinySet.hpp"
 
 using namespace SSTGraph;
+
+// the reference's TinySet tests in miniature (Tinyset_test.cpp: insert
+// random elements below max, check membership; remove, check absence)
+static int tinyset_check() {
+  const uint32_t max = 5000;
+  TinySetV<> ts(max);
+  std::mt19937 rng(7);
+  std::set<uint32_t> model;
+  for (int i = 0; i < 3000; i++) {
+    uint32_t e = rng() % max;
+    ts.insert(e);
+    model.insert(e);
+  }
+  std::vector<uint32_t> batch;
+  for (int i = 0; i < 2000; i++) batch.push_back(rng() % max);
+  ts.insert_batch(batch.data(), batch.size());
+  model.insert(batch.begin(), batch.end());
+  ts.insert(0);  // element 0 of row 0 stays (the set keeps (0, 0))
+  model.insert(0);
+  for (uint32_t e = 0; e < max; e++)
+    if (ts.has(e) != (model.count(e) == 1)) {
+      std::printf("tinyset has(%u) differs\n", e);
+      return 1;
+    }
+  for (int i = 0; i < 1500; i++) {
+    uint32_t e = rng() % max;
+    ts.remove(e);
+    model.erase(e);
+  }
+  if (ts.get_n() != model.size()) {
+    std::printf("tinyset n %llu != %zu\n", (unsigned long long)ts.get_n(), model.size());
+    return 1;
+  }
+  std::vector<uint32_t> seen;
+  ts.map<true>([&](uint32_t e) { seen.push_back(e); });
+  if (seen != std::vector<uint32_t>(model.begin(), model.end())) {
+    std::printf("tinyset map order differs\n");
+    return 1;
+  }
+  bool threw = false;
+  try {
+    ts.insert(max);
+  } catch (const sst_error &) {
+    threw = true;
+  }
+  return threw ? 0 : 1;
+}
 
 struct collect {
   static constexpr bool no_early_exit = true;
@@ -68,6 +116,7 @@ int main() {
   std::free(par);
   std::free(pr);
   std::free(cc);
+  if (tinyset_check()) return 1;
   std::printf("facade ok: M=%llu tc=%llu\n", (unsigned long long)g.M(),
               (unsigned long long)tc);
   return 0;
