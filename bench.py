@@ -589,7 +589,11 @@ def main():
     batched = pagerank = bfs = serving = multi = None
     if a.only == "all":
         batched = measure_batched()
+        t0 = time.time()
+        tuning = sg.autotune(g)
+        tuning["tune_s"] = time.time() - t0
         pagerank = measure_pagerank()
+        pagerank["tuning"] = tuning
         # the reference's degree-ordered mode (internal/test.hpp:460-467):
         # relabel by degree, run on the relabelled copy, map results back
         t0 = time.time()

@@ -199,6 +199,21 @@ SST_API sst_status sst_bfs_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
                                  int32_t *depths, uint32_t flags);
 SST_API sst_status sst_bc_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
                                 double *out, uint32_t flags);
+/* Traversal tuning (no reference counterpart).  sst_autotune times the
+ * knobs on this graph and keeps the fastest: PageRank over chunk_leaves
+ * {8,16,32} x pr_lanes {4,8,16}, then BFS over bfs_alpha {5,10,20,40,80};
+ * pr_ms / bfs_ms report the winners' times (3 PageRank iterations; one BFS).
+ * The leaf itself stays 32 slots (one 128-byte line): it is the storage
+ * format, not a launch parameter. */
+typedef struct sst_tuning {
+  uint32_t chunk_leaves; /* leaves per warp work item of the pull lists (1..32) */
+  uint32_t pr_lanes;     /* lanes per one-leaf vertex in PageRank (4, 8, 16) */
+  uint32_t bfs_alpha;    /* BFS pulls once (frontier + its edges) * alpha > m */
+  float pr_ms, bfs_ms;
+} sst_tuning;
+SST_API sst_status sst_autotune(sst_graph *g, sst_tuning *out);
+SST_API sst_status sst_get_tuning(sst_graph *g, sst_tuning *out);
+SST_API sst_status sst_set_tuning(sst_graph *g, const sst_tuning *in);
 /* TouchAll(g)  test.hpp:476 */
 SST_API sst_status sst_touch_all(sst_graph *g, uint64_t *out);
 

@@ -46,6 +46,12 @@ class sst_config(ctypes.Structure):
                 ("keep_self_loops", ctypes.c_uint32)]
 
 
+class sst_tuning(ctypes.Structure):
+    _fields_ = [("chunk_leaves", ctypes.c_uint32), ("pr_lanes", ctypes.c_uint32),
+                ("bfs_alpha", ctypes.c_uint32), ("pr_ms", ctypes.c_float),
+                ("bfs_ms", ctypes.c_float)]
+
+
 class sst_server_config(ctypes.Structure):
     _fields_ = [("query_slots", ctypes.c_uint32),
                 ("hbm_budget_bytes", ctypes.c_uint64),
@@ -105,6 +111,9 @@ SIGNATURES = {
     "sst_cc": (_i32, [_vp, _vp, _u32]),
     "sst_bc": (_i32, [_vp, _u32, _vp, _u32]),
     "sst_bfs_multi": (_i32, [_vp, _vp, _u32, _vp, _u32]),
+    "sst_autotune": (_i32, [_vp, ctypes.POINTER(sst_tuning)]),
+    "sst_get_tuning": (_i32, [_vp, ctypes.POINTER(sst_tuning)]),
+    "sst_set_tuning": (_i32, [_vp, ctypes.POINTER(sst_tuning)]),
     "sst_bc_multi": (_i32, [_vp, _vp, _u32, _vp, _u32]),
     "sst_tc": (_i32, [_vp, ctypes.POINTER(_u64), _vp, _u32]),
     "sst_touch_all": (_i32, [_vp, ctypes.POINTER(_u64)]),
@@ -554,6 +563,29 @@ class TinySetV:
 
     def close(self):
         self._g.close()
+
+
+def _tuning_dict(t):
+    return {"chunk_leaves": t.chunk_leaves, "pr_lanes": t.pr_lanes,
+            "bfs_alpha": t.bfs_alpha, "pr_ms": t.pr_ms, "bfs_ms": t.bfs_ms}
+
+
+def autotune(g: SparseMatrixV) -> dict:
+    """Time the traversal knobs on g and keep the fastest (sst_autotune)."""
+    t = sst_tuning()
+    _check(lib().sst_autotune(g.handle, ctypes.byref(t)))
+    return _tuning_dict(t)
+
+
+def get_tuning(g: SparseMatrixV) -> dict:
+    t = sst_tuning()
+    _check(lib().sst_get_tuning(g.handle, ctypes.byref(t)))
+    return _tuning_dict(t)
+
+
+def set_tuning(g: SparseMatrixV, chunk_leaves=32, pr_lanes=8, bfs_alpha=20):
+    t = sst_tuning(chunk_leaves, pr_lanes, bfs_alpha, 0.0, 0.0)
+    _check(lib().sst_set_tuning(g.handle, ctypes.byref(t)))
 
 
 def _sources(srcs, flags, like):

@@ -643,6 +643,24 @@ sst_status sst_bc_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
   return finish_out(g, out, d, cnt, flags);
 }
 
+sst_status sst_autotune(sst_graph *g, sst_tuning *out) {
+  CHECK_G(g);
+  if (!out) return SST_EINVAL;
+  return sst::autotune(g, out);
+}
+
+sst_status sst_get_tuning(sst_graph *g, sst_tuning *out) {
+  CHECK_G(g);
+  if (!out) return SST_EINVAL;
+  return sst::get_tuning(g, out);
+}
+
+sst_status sst_set_tuning(sst_graph *g, const sst_tuning *in) {
+  CHECK_G(g);
+  if (!in) return SST_EINVAL;
+  return sst::set_tuning(g, in);
+}
+
 sst_status sst_pagerank(sst_graph *g, uint32_t iters, double damping,
                         double *out, uint32_t flags) {
   CHECK_G(g);

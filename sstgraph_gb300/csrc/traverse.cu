@@ -55,6 +55,12 @@ template <typename T> struct DevBuf {
 
 struct TravState {
   uint64_t version = ~0ull;
+  // tuning (sst_autotune): leaves per work-list chunk (<= 32), lanes per
+  // one-leaf vertex in PageRank, and the BFS switch to pull once
+  // (frontier + its edges) * bfs_alpha > m
+  uint32_t chunk_leaves = 32, pr_lanes = 8, bfs_alpha = 20;
+  uint32_t lists_cl = 0;      // chunk size the lists were built with
+  uint64_t lists_stamp = 0;   // bumped on every rebuild of the lists
   // chunk list of multi-leaf vertices
   uint64_t nchunks = 0, nmulti = 0, nbig = 0, nsmall = 0;
   uint64_t inv_version = ~0ull;
@@ -87,7 +93,8 @@ struct TravState {
   // PageRank iterations captured as one CUDA graph, replayed while the
   // graph version and the call's arguments stay the same
   cudaGraphExec_t pr_exec = nullptr;
-  uint64_t pr_version = ~0ull;
+  uint64_t pr_version = ~0ull;  // lists_stamp the graph was captured with
+  uint32_t pr_lanes_used = 0;
   uint32_t pr_iters = 0;
   double pr_damping = 0.0;
   const void *pr_key[6] = {};  // output, stream and the buffers it reads
@@ -160,11 +167,11 @@ __global__ void k_chunk_counts(const uint32_t *__restrict__ cap, uint32_t n,
                                uint64_t *__restrict__ nch,
                                uint32_t *__restrict__ bigf,
                                uint32_t *__restrict__ multif,
-                               uint32_t *__restrict__ smallf) {
+                               uint32_t *__restrict__ smallf, uint32_t cl) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   uint32_t c = cap[v];
-  uint64_t k = c > kLeaf ? ((c >> kLeafLog) + kChunkLeaves - 1) / kChunkLeaves : 0;
+  uint64_t k = c > kLeaf ? ((c >> kLeafLog) + cl - 1) / cl : 0;
   nch[v] = k;
   bigf[v] = c > kLeaf;
   multif[v] = k > 1;
@@ -176,7 +183,8 @@ __global__ void k_chunk_fill(const uint32_t *__restrict__ cap,
                              const uint64_t *__restrict__ choff,
                              uint32_t *__restrict__ cv,
                              uint32_t *__restrict__ cl0,
-                             unsigned long long *__restrict__ cdesc) {
+                             unsigned long long *__restrict__ cdesc,
+                             uint32_t cl) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   uint64_t c0 = choff[v], c1 = choff[v + 1];
@@ -184,10 +192,10 @@ __global__ void k_chunk_fill(const uint32_t *__restrict__ cap,
   uint64_t leaf = base[v] >> kLeafLog;
   unsigned long long single = (c1 - c0) == 1 ? 128ull : 0ull;
   for (uint64_t c = c0; c < c1; c++) {
-    uint32_t l0 = (uint32_t)((c - c0) * kChunkLeaves);
+    uint32_t l0 = (uint32_t)((c - c0) * cl);
     cv[c] = v;
     cl0[c] = l0;
-    cdesc[c] = ((leaf + l0) << 8) | single | (unsigned long long)min(kChunkLeaves, nl - l0);
+    cdesc[c] = ((leaf + l0) << 8) | single | (unsigned long long)min(cl, nl - l0);
   }
 }
 
@@ -287,11 +295,12 @@ __device__ __forceinline__ void pr_finish(uint32_t v, unsigned long long sum,
   if (last) rank[v] = __ull2double_rn(r) * (1.0 / 9223372036854775808.0);
 }
 
-// One-leaf segments (cap <= 32): a group of 8 lanes per vertex (one 32-byte
-// sector of the leaf per lane step), four vertices per group in flight.
-// sdesc[i] = (segment base << 6) | degree.
+// One-leaf segments (cap <= 32): a group of G lanes per vertex (G = 8: one
+// 32-byte sector of the leaf per lane step), four vertices per group in
+// flight.  sdesc[i] = (segment base << 6) | degree.
 constexpr int kSmallPer = 4;
 
+template <int G>
 __global__ void k_pr_small(DGraph g, const unsigned long long *__restrict__ sdesc,
                            const uint32_t *__restrict__ small, uint64_t nsmall,
                            const unsigned long long *__restrict__ cin,
@@ -299,11 +308,13 @@ __global__ void k_pr_small(DGraph g, const unsigned long long *__restrict__ sdes
                            double *__restrict__ rank,
                            const unsigned long long *__restrict__ rdeg,
                            PrConst k, bool last) {
-  uint64_t grp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
-  const uint32_t sub = threadIdx.x & 7;
+  static_assert(G >= kSmallPer && G <= 32 && (G & (G - 1)) == 0, "lanes per vertex");
+  constexpr int Q = 32 / G;  // slots per lane
+  uint64_t grp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const uint32_t sub = threadIdx.x & (G - 1);
   const unsigned long long pol = l2_evict_first();
   const uint64_t i0 = grp * kSmallPer;
-  uint32_t x[kSmallPer][4];
+  uint32_t x[kSmallPer][Q];
   uint32_t dg[kSmallPer];
 #pragma unroll
   for (int u = 0; u < kSmallPer; u++) {
@@ -312,8 +323,8 @@ __global__ void k_pr_small(DGraph g, const unsigned long long *__restrict__ sdes
     dg[u] = (uint32_t)(dsc & 63);
     const uint32_t *p = g.slots + (dsc >> 6);
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      uint32_t j = sub + 8 * q;
+    for (int q = 0; q < Q; q++) {
+      uint32_t j = sub + G * q;
       x[u][q] = j < dg[u] ? ld_stream(p + j, pol) : kEmpty;
     }
   }
@@ -322,7 +333,7 @@ __global__ void k_pr_small(DGraph g, const unsigned long long *__restrict__ sdes
   for (int u = 0; u < kSmallPer; u++) {
     acc[u] = 0;
 #pragma unroll
-    for (int q = 0; q < 4; q++)
+    for (int q = 0; q < Q; q++)
       if (x[u][q] != kEmpty) acc[u] += ld_keep(cin + x[u][q]);
   }
   unsigned long long mine = 0;
@@ -330,9 +341,8 @@ __global__ void k_pr_small(DGraph g, const unsigned long long *__restrict__ sdes
 #pragma unroll
   for (int u = 0; u < kSmallPer; u++) {
     unsigned long long a = acc[u];
-    a += __shfl_xor_sync(0xffffffffu, a, 4);
-    a += __shfl_xor_sync(0xffffffffu, a, 2);
-    a += __shfl_xor_sync(0xffffffffu, a, 1);
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
     if (sub == (uint32_t)u) {
       mine = a;
       mydeg = dg[u];
@@ -922,7 +932,7 @@ static TravState *state(sst_graph *g) {
 
 static sst_status ensure_lists(sst_graph *g) {
   TravState *t = state(g);
-  if (t->version == g->version) return SST_OK;
+  if (t->version == g->version && t->lists_cl == t->chunk_leaves) return SST_OK;
   cudaStream_t s = g->stream;
   uint32_t n = g->n;
   SST_CUDA_TRY(t->choff.ensure((uint64_t)n + 1));
@@ -934,8 +944,9 @@ static sst_status ensure_lists(sst_graph *g) {
   SST_CUDA_TRY(g->arena.reserve(4 * scan_scratch_bytes((uint64_t)n + 1, 8) + 4096));
   uint64_t *tot = g->arena.take<uint64_t>(1);
   uint32_t *tot32 = g->arena.take<uint32_t>(3);
+  const uint32_t cl = t->chunk_leaves;
   if (n) SST_LAUNCH(k_chunk_counts, blocks_for(n), kTB, 0, s, g->d_cap, n,
-                    t->choff.p, bigf, multif, smallf);
+                    t->choff.p, bigf, multif, smallf, cl);
   SST_CUDA_TRY((scan<uint64_t, OpAdd>(t->choff.p, t->choff.p, n, 0ull, OpAdd{},
                                       true, false, tot, g->arena, s)));
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(bigf, bigp, n, 0u, OpAdd{}, true, false,
@@ -963,7 +974,7 @@ static sst_status ensure_lists(sst_graph *g) {
   SST_CUDA_TRY(t->sdesc.ensure(t->nsmall + 1));
   if (n) {
     SST_LAUNCH(k_chunk_fill, blocks_for(n), kTB, 0, s, g->d_cap, g->d_base, n,
-               t->choff.p, t->cv.p, t->cl0.p, t->cdesc.p);
+               t->choff.p, t->cv.p, t->cl0.p, t->cdesc.p, cl);
     SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, bigf, bigp, n, t->big.p);
     SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, multif, multip, n, t->multi.p);
     SST_LAUNCH(k_compact_ids, blocks_for(n), kTB, 0, s, smallf, smallp, n, t->small.p);
@@ -974,6 +985,8 @@ static sst_status ensure_lists(sst_graph *g) {
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   SST_CUDA_TRY(cudaGetLastError());
   t->version = g->version;
+  t->lists_cl = cl;
+  t->lists_stamp++;
   return SST_OK;
 }
 
@@ -997,7 +1010,9 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   static bool carveout = false;
   if (!carveout) {
     // these kernels use no shared memory: give the SM's storage to L1
-    cudaFuncSetAttribute(k_pr_small, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaFuncSetAttribute(k_pr_small<4>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaFuncSetAttribute(k_pr_small<8>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaFuncSetAttribute(k_pr_small<16>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
     cudaFuncSetAttribute(k_pr_chunks, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
     carveout = true;
   }
@@ -1023,11 +1038,18 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
     DGraph dg = g->view();
     for (uint32_t it = 0; it < iters; it++) {
       bool last = it + 1 == iters;
-      if (t->nsmall)
-        SST_LAUNCH(k_pr_small,
-                   blocks_for((t->nsmall + kSmallPer - 1) / kSmallPer * 8), kTB, 0,
-                   s, dg, t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank,
-                   rdeg, K, last);
+      if (t->nsmall) {
+        const uint64_t groups = (t->nsmall + kSmallPer - 1) / kSmallPer;
+        if (t->pr_lanes == 4)
+          SST_LAUNCH(k_pr_small<4>, blocks_for(groups * 4), kTB, 0, s, dg,
+                     t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last);
+        else if (t->pr_lanes == 16)
+          SST_LAUNCH(k_pr_small<16>, blocks_for(groups * 16), kTB, 0, s, dg,
+                     t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last);
+        else
+          SST_LAUNCH(k_pr_small<8>, blocks_for(groups * 8), kTB, 0, s, dg,
+                     t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last);
+      }
       if (t->nchunks)
         SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cdesc.p,
                    t->cv.p, t->nchunks, ci, co, d_rank, rdeg, part, K, last);
@@ -1040,8 +1062,9 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   // replay the captured iterations when nothing they depend on changed;
   // with the kernel profiler on, launch them one by one so each is timed
   const void *key[6] = {d_rank, s, cin, cout, part, rdeg};
-  bool same = t->pr_exec && t->pr_version == g->version &&
-              t->pr_iters == iters && t->pr_damping == damping;
+  bool same = t->pr_exec && t->pr_version == t->lists_stamp &&
+              t->pr_lanes_used == t->pr_lanes && t->pr_iters == iters &&
+              t->pr_damping == damping;
   for (int i = 0; i < 6 && same; i++) same = t->pr_key[i] == key[i];
   if (profiling("k_pr_chunks") || profiling("k_pr_small")) {
     launch_all();
@@ -1064,7 +1087,8 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
       t->pr_exec = nullptr;
       SST_CUDA_TRY(e);
     }
-    t->pr_version = g->version;
+    t->pr_version = t->lists_stamp;
+    t->pr_lanes_used = t->pr_lanes;
     t->pr_iters = iters;
     t->pr_damping = damping;
     for (int i = 0; i < 6; i++) t->pr_key[i] = key[i];
@@ -1114,7 +1138,7 @@ sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths
       return SST_ETIMEDOUT;
     }
     SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, 24, s));
-    if ((qn + qdeg) * 20 > m) {
+    if ((qn + qdeg) * t->bfs_alpha > m) {
       SST_CUDA_TRY(cudaMemsetAsync(t->fbits.p, 0, ((uint64_t)n / 32 + 1) * 4, s));
       SST_LAUNCH(k_q2bits, blocks_for(qn), kTB, 0, s, q, (uint32_t)qn, t->fbits.p);
       SST_LAUNCH(k_bfs_pull_small, blocks_for(n), kTB, 0, s, dg, t->fbits.p,
@@ -1665,7 +1689,7 @@ sst_status bfs_multi(sst_graph *g, const uint32_t *h_srcs, uint32_t k,
       set_error_message("multi-source BFS exceeded n levels");
       return SST_ETIMEDOUT;
     }
-    if ((qn + qdeg) * 20 > m) {
+    if ((qn + qdeg) * t->bfs_alpha > m) {
       if (t->nsmall)
         SST_LAUNCH(k_msbfs_pull_small, blocks_for(t->nsmall), kTB, 0, s, dg,
                    t->small.p, t->nsmall, fr, t->mvis.p, t->mnx.p, full);
@@ -1819,6 +1843,112 @@ sst_status bc_multi(sst_graph *g, const uint32_t *h_srcs, uint32_t k,
     }
   }
   SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+
+// ------------------------------------------------------------- autotuner
+// Times the traversal knobs on this graph and keeps the fastest: PageRank
+// (3 iterations) over chunk sizes {8, 16, 32} x lanes {4, 8, 16}, then BFS
+// from three sources over push/pull thresholds {5, 10, 20, 40, 80}.
+sst_status get_tuning(sst_graph *g, sst_tuning *out) {
+  TravState *t = state(g);
+  out->chunk_leaves = t->chunk_leaves;
+  out->pr_lanes = t->pr_lanes;
+  out->bfs_alpha = t->bfs_alpha;
+  out->pr_ms = 0.f;
+  out->bfs_ms = 0.f;
+  return SST_OK;
+}
+
+sst_status set_tuning(sst_graph *g, const sst_tuning *in) {
+  if (in->chunk_leaves < 1 || in->chunk_leaves > 32 ||
+      (in->pr_lanes != 4 && in->pr_lanes != 8 && in->pr_lanes != 16) ||
+      in->bfs_alpha < 1) {
+    set_error_message("tuning out of range (chunk_leaves 1..32, pr_lanes 4/8/16, bfs_alpha >= 1)");
+    return SST_EINVAL;
+  }
+  TravState *t = state(g);
+  t->chunk_leaves = in->chunk_leaves;
+  t->pr_lanes = in->pr_lanes;
+  t->bfs_alpha = in->bfs_alpha;
+  return SST_OK;
+}
+
+sst_status autotune(sst_graph *g, sst_tuning *out) {
+  TravState *t = state(g);
+  const uint32_t n = g->n;
+  sst_status st = get_tuning(g, out);
+  if (st != SST_OK || n == 0 || g->m == 0) return st;
+  cudaStream_t s = g->stream;
+  double *rank = nullptr;
+  int32_t *dep = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  SST_CUDA_TRY(cudaMalloc(&rank, (uint64_t)n * 8));
+  SST_CUDA_TRY(cudaMalloc(&dep, (uint64_t)n * 4));
+  SST_CUDA_TRY(cudaEventCreate(&e0));
+  SST_CUDA_TRY(cudaEventCreate(&e1));
+  float best_pr = 1e30f, best_bfs = 1e30f;
+  uint32_t bcl = t->chunk_leaves, blanes = t->pr_lanes, balpha = t->bfs_alpha;
+  auto timed = [&](auto fn, float *ms) -> sst_status {
+    sst_status r = fn();  // warm (lists, captured graph)
+    if (r != SST_OK) return r;
+    SST_CUDA_TRY(cudaEventRecord(e0, s));
+    r = fn();
+    if (r != SST_OK) return r;
+    SST_CUDA_TRY(cudaEventRecord(e1, s));
+    SST_CUDA_TRY(cudaEventSynchronize(e1));
+    SST_CUDA_TRY(cudaEventElapsedTime(ms, e0, e1));
+    return SST_OK;
+  };
+  const uint32_t cls[3] = {8, 16, 32}, lanes[3] = {4, 8, 16};
+  for (uint32_t a = 0; a < 3 && st == SST_OK; a++)
+    for (uint32_t b = 0; b < 3 && st == SST_OK; b++) {
+      t->chunk_leaves = cls[a];
+      t->pr_lanes = lanes[b];
+      float ms = 0.f;
+      st = timed([&] { return pagerank(g, 3, 0.85, rank); }, &ms);
+      if (st == SST_OK && ms < best_pr) {
+        best_pr = ms;
+        bcl = cls[a];
+        blanes = lanes[b];
+      }
+    }
+  t->chunk_leaves = bcl;
+  t->pr_lanes = blanes;
+  // BFS sources: the first three vertices with edges along a fixed stride
+  std::vector<uint32_t> deg(n), src;
+  if (st == SST_OK) {
+    SST_CUDA_TRY(cudaMemcpy(deg.data(), g->d_deg, (uint64_t)n * 4, cudaMemcpyDeviceToHost));
+    for (uint64_t i = 0; i < n && src.size() < 3; i++) {
+      uint32_t v = (uint32_t)((i * 2654435761ull) % n);
+      if (deg[v]) src.push_back(v);
+    }
+  }
+  const uint32_t alphas[5] = {5, 10, 20, 40, 80};
+  for (uint32_t a = 0; a < 5 && st == SST_OK && !src.empty(); a++) {
+    t->bfs_alpha = alphas[a];
+    float tot = 0.f;
+    for (uint32_t v : src) {
+      float ms = 0.f;
+      st = timed([&] { return bfs(g, v, nullptr, dep); }, &ms);
+      if (st != SST_OK) break;
+      tot += ms;
+    }
+    if (st == SST_OK && tot < best_bfs) {
+      best_bfs = tot;
+      balpha = alphas[a];
+    }
+  }
+  t->bfs_alpha = balpha;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(rank);
+  cudaFree(dep);
+  if (st != SST_OK) return st;
+  get_tuning(g, out);
+  out->pr_ms = best_pr;
+  out->bfs_ms = src.empty() ? 0.f : best_bfs / (float)src.size();
   return SST_OK;
 }
 
