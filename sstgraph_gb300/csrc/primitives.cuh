@@ -136,10 +136,10 @@ __device__ __forceinline__ T block_exclusive(T v, T identity, Op op, T *total) {
 }
 
 // Multi-tile scans run as two launches over kScanRanges contiguous tile
-// ranges (about two blocks per SM): the first reduces each range, the
+// ranges (about four blocks per SM): the first reduces each range, the
 // second has every block fold the range sums before its own and then scan
 // its range tile by tile with a running carry.  No block waits on another.
-constexpr int kScanRanges = 304;
+constexpr int kScanRanges = 608;
 
 // tile t of the scan order: element i of the array (forward or reversed)
 template <typename T>

@@ -521,62 +521,108 @@ __device__ __forceinline__ bool in_front(const uint32_t *bits, uint32_t u) {
   return (bits[u >> 5] >> (u & 31)) & 1u;
 }
 
-// pull, one-leaf vertices: thread per vertex, first frontier neighbour wins
-__global__ void k_bfs_pull_small(DGraph g, const uint32_t *__restrict__ fbits,
-                                 int32_t *__restrict__ depth,
-                                 int32_t *__restrict__ parent,
-                                 uint32_t *__restrict__ nq,
-                                 unsigned long long *__restrict__ cnt, int lvl) {
-  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+// pull, one-leaf vertices (the one-leaf list): a group of 8 lanes per
+// vertex, 4 slots per lane, four vertices per group in flight; the parent is
+// the smallest frontier neighbour
+__global__ void k_bfs_pull_small8(DGraph g, const unsigned long long *__restrict__ sdesc,
+                                  const uint32_t *__restrict__ small, uint64_t nsmall,
+                                  const uint32_t *__restrict__ fbits,
+                                  int32_t *__restrict__ depth,
+                                  int32_t *__restrict__ parent,
+                                  uint32_t *__restrict__ nq,
+                                  unsigned long long *__restrict__ cnt, int lvl) {
+  const uint64_t grp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const uint32_t sub = threadIdx.x & 7;
+  const uint64_t i0 = grp * 4;
   bool mine = false;
-  uint32_t d = 0;
-  if (v < g.n && depth[v] < 0 && g.cap[v] <= kLeaf) {
-    d = g.deg[v];
-    const uint32_t *p = g.slots + g.base[v];
-    for (uint32_t i = 0; i < d; i++) {
-      uint32_t u = p[i];
-      if (in_front(fbits, u)) {
-        depth[v] = lvl + 1;
-        parent[v] = (int32_t)u;
-        mine = true;
-        break;
+  uint32_t myv = 0, mydeg = 0;
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const uint64_t i = i0 + u;
+    uint32_t v = 0, d = 0;
+    bool open = false;
+    unsigned long long dsc = 0;
+    if (i < nsmall) {
+      v = small[i];
+      open = depth[v] < 0;
+      dsc = sdesc[i];
+      d = (uint32_t)(dsc & 63);
+    }
+    uint32_t best = kEmpty;
+    if (open) {
+      const uint32_t *p = g.slots + (dsc >> 6);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        uint32_t j = sub + 8 * q;
+        if (j < d) {
+          uint32_t w = p[j];
+          if (w < best && in_front(fbits, w)) best = w;
+        }
       }
     }
+    // smallest frontier neighbour over the group's 8 lanes
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if (sub == (uint32_t)u && open && best != kEmpty) {
+      depth[v] = lvl + 1;
+      parent[v] = (int32_t)best;
+      mine = true;
+      myv = v;
+      mydeg = d;
+    }
   }
-  enqueue(mine, v, d, 1u, nq, cnt);
+  enqueue(mine, myv, mydeg, 1u, nq, cnt);
 }
 
-// pull, multi-leaf vertices: warp per vertex, leaf by leaf, early exit
-__global__ void k_bfs_pull_big(DGraph g, const uint32_t *__restrict__ big,
-                               uint64_t nbig, const uint32_t *__restrict__ fbits,
-                               int32_t *__restrict__ depth,
-                               int32_t *__restrict__ parent,
-                               uint32_t *__restrict__ nq,
-                               unsigned long long *__restrict__ cnt, int lvl) {
-  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// pull, multi-leaf vertices: warp per chunk of the work lists (lane = slot,
+// eight leaves in flight), stops at the first frontier neighbour or once
+// another chunk has claimed the vertex; the claim is a compare-and-swap on
+// its depth, so one chunk records it
+__global__ void k_bfs_pull_chunks(DGraph g, const unsigned long long *__restrict__ cdesc,
+                                  const uint32_t *__restrict__ cv, uint64_t nchunks,
+                                  const uint32_t *__restrict__ fbits,
+                                  int32_t *__restrict__ depth,
+                                  int32_t *__restrict__ parent,
+                                  uint32_t *__restrict__ nq,
+                                  unsigned long long *__restrict__ cnt, int lvl) {
+  const uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (i >= nbig) return;
-  uint32_t v = big[i];
-  if (depth[v] >= 0) return;
-  uint64_t base = g.base[v];
-  uint32_t nl = g.cap[v] >> kLeafLog;
-  const uint8_t *lc = g.lcnt + (base >> kLeafLog);
-  bool found = false;
-  for (uint32_t l = 0; l < nl && !found; l++) {
-    uint32_t c = lc[l];
-    uint32_t u = (uint32_t)lane < c ? g.slots[base + ((uint64_t)l << kLeafLog) + lane] : 0;
-    uint32_t m = __ballot_sync(0xffffffffu, (uint32_t)lane < c && in_front(fbits, u));
-    if (m) {
-      int first = __ffs(m) - 1;
-      uint32_t pu = __shfl_sync(0xffffffffu, u, first);
-      if (lane == 0) {
-        depth[v] = lvl + 1;
-        parent[v] = (int32_t)pu;
+  bool mine = false;
+  uint32_t v = 0;
+  if (c < nchunks) {
+    v = cv[c];
+    // another chunk may claim v at any time: every lane follows lane 0's
+    // reading, so the warp stays converged for its shuffles
+    if (__shfl_sync(0xffffffffu, __ldcg(depth + v), 0) < 0) {
+      const unsigned long long dsc = cdesc[c];
+      const uint64_t leaf0 = dsc >> 8;
+      const uint32_t l1 = (uint32_t)(dsc & 63);
+      const uint32_t mycnt = (uint32_t)lane < l1 ? g.lcnt[leaf0 + lane] : 0u;
+      const uint32_t *sl = g.slots + (leaf0 << kLeafLog) + lane;
+      uint32_t found = kEmpty;
+      for (uint32_t l = 0; l < l1 && found == kEmpty; l += 8) {
+        uint32_t x[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          uint32_t cq = __shfl_sync(0xffffffffu, mycnt, (l + q) & 31);
+          if (l + q >= l1) cq = 0;
+          x[q] = (uint32_t)lane < cq ? sl[(uint64_t)(l + q) << kLeafLog] : kEmpty;
+        }
+        uint32_t best = kEmpty;
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+          if (x[q] != kEmpty && x[q] < best && in_front(fbits, x[q])) best = x[q];
+        found = __reduce_min_sync(0xffffffffu, best);
+        if (found == kEmpty && __shfl_sync(0xffffffffu, __ldcg(depth + v), 0) >= 0)
+          break;  // claimed by another chunk
       }
-      found = true;
+      if (found != kEmpty && lane == 0 && atomicCAS(&depth[v], -1, lvl + 1) == -1) {
+        parent[v] = (int32_t)found;
+        mine = true;
+      }
     }
   }
-  enqueue(found && lane == 0, v, g.deg[v], items_of(g.cap[v]), nq, cnt);
+  enqueue(mine, v, mine ? g.deg[v] : 0u, mine ? items_of(g.cap[v]) : 0u, nq, cnt);
 }
 
 // ------------------------------------------------------------- cc
@@ -1141,11 +1187,14 @@ sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths
     if ((qn + qdeg) * t->bfs_alpha > m) {
       SST_CUDA_TRY(cudaMemsetAsync(t->fbits.p, 0, ((uint64_t)n / 32 + 1) * 4, s));
       SST_LAUNCH(k_q2bits, blocks_for(qn), kTB, 0, s, q, (uint32_t)qn, t->fbits.p);
-      SST_LAUNCH(k_bfs_pull_small, blocks_for(n), kTB, 0, s, dg, t->fbits.p,
-                 depth, parent, nq, cnt, lvl);
-      if (t->nbig)
-        SST_LAUNCH(k_bfs_pull_big, warp_blocks(t->nbig), kTB, 0, s, dg, t->big.p,
-                   t->nbig, t->fbits.p, depth, parent, nq, cnt, lvl);
+      if (t->nsmall)
+        SST_LAUNCH(k_bfs_pull_small8, blocks_for((t->nsmall + 3) / 4 * 8), kTB, 0,
+                   s, dg, t->sdesc.p, t->small.p, t->nsmall, t->fbits.p, depth,
+                   parent, nq, cnt, lvl);
+      if (t->nchunks)
+        SST_LAUNCH(k_bfs_pull_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg,
+                   t->cdesc.p, t->cv.p, t->nchunks, t->fbits.p, depth, parent,
+                   nq, cnt, lvl);
     } else {
       SST_CUDA_TRY(t->iv.ensure(qitems + 1));
       SST_CUDA_TRY(t->il0.ensure(qitems + 1));
