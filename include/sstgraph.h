@@ -114,6 +114,20 @@ SST_API sst_status sst_remove(sst_graph *g, uint32_t row, uint32_t col);
 SST_API sst_status sst_build_from_csr(sst_graph *g, const uint64_t *offsets,
                               const uint32_t *cols, uint32_t flags);
 
+/* ---- graph files (the reference drivers' readers,
+ *      internal/helpers.hpp:379-657) -------------------------------------
+ * .mtx (Matrix Market coordinate, one-based, every entry symmetrised in file
+ * order, values ignored, rows must equal cols) and PBBS .adj / .adj.shuf
+ * (AdjacencyGraph / WeightedAdjacencyGraph, weights ignored).  Host only:
+ * sst_read_graph_file returns the (row, col) pairs in *pairs (free with
+ * sst_free); sst_load_graph_file builds a rows x rows graph from them with
+ * one batch insert, as the reference's drivers do (internal/test.hpp:427-450). */
+SST_API sst_status sst_read_graph_file(const char *path, uint32_t *rows,
+                                       uint64_t *n_pairs, uint32_t **pairs);
+SST_API void sst_free(void *p);
+SST_API sst_status sst_load_graph_file(const char *path, const sst_config *cfg,
+                                       sst_graph **out);
+
 /* ---- queries -------------------------------------------------------- */
 /* has(el_t, el_t)  SparseMatrix.hpp:162,721-727 ; out[i] = 0/1 */
 SST_API sst_status sst_has_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,

@@ -112,6 +112,11 @@ SIGNATURES = {
     "sst_bc": (_i32, [_vp, _u32, _vp, _u32]),
     "sst_bfs_multi": (_i32, [_vp, _vp, _u32, _vp, _u32]),
     "sst_autotune": (_i32, [_vp, ctypes.POINTER(sst_tuning)]),
+    "sst_read_graph_file": (_i32, [ctypes.c_char_p, ctypes.POINTER(_u32),
+                                   ctypes.POINTER(_u64), ctypes.POINTER(_vp)]),
+    "sst_free": (None, [_vp]),
+    "sst_load_graph_file": (_i32, [ctypes.c_char_p, ctypes.POINTER(sst_config),
+                                   ctypes.POINTER(_vp)]),
     "sst_get_tuning": (_i32, [_vp, ctypes.POINTER(sst_tuning)]),
     "sst_set_tuning": (_i32, [_vp, ctypes.POINTER(sst_tuning)]),
     "sst_bc_multi": (_i32, [_vp, _vp, _u32, _vp, _u32]),
@@ -563,6 +568,29 @@ class TinySetV:
 
     def close(self):
         self._g.close()
+
+
+def read_graph_file(path: str):
+    """(rows, pairs) of a .mtx / .adj file as the reference's readers give
+    them (internal/helpers.hpp:379-657): pairs is an (n, 2) uint32 array."""
+    rows, cnt, p = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_void_p()
+    _check(lib().sst_read_graph_file(os.fsencode(path), ctypes.byref(rows),
+                                     ctypes.byref(cnt), ctypes.byref(p)))
+    try:
+        n = cnt.value
+        buf = (ctypes.c_uint32 * max(2 * n, 1)).from_address(p.value)
+        pairs = np.frombuffer(buf, np.uint32, 2 * n).reshape(n, 2).copy()
+    finally:
+        lib().sst_free(p)
+    return rows.value, pairs
+
+
+def load_graph_file(path: str, device: int = 0) -> "SparseMatrixV":
+    """Device graph built from a .mtx / .adj file (sst_load_graph_file)."""
+    cfg = sst_config(device, 0, 0, 0.0, 0.0, 0.0, 0)
+    h = ctypes.c_void_p()
+    _check(lib().sst_load_graph_file(os.fsencode(path), ctypes.byref(cfg), ctypes.byref(h)))
+    return SparseMatrixV(0, _handle=h)
 
 
 def _tuning_dict(t):

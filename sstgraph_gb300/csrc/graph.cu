@@ -587,7 +587,9 @@ __global__ void k_gather_old(DGraph g, Tasks t, uint32_t ntasks,
   uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (s >= nsrc_total) return;
-  uint64_t tau = task_of(t.soff, ntasks, s);
+  // lane 0 finds the leaf's task; the warp shares it
+  uint64_t tau = lane == 0 ? task_of(t.soff, ntasks, s) : 0;
+  tau = __shfl_sync(0xffffffffu, tau, 0);
   uint32_t u = t.u[tau];
   uint32_t l = t.w0[tau] + (uint32_t)(s - t.soff[tau]);
   uint64_t base = g.base[u];
@@ -651,7 +653,9 @@ __device__ __forceinline__ uint64_t task_new_base(const Tasks &t, uint64_t tau,
   return class_start[log2_floor(capn)] + (uint64_t)t.rank[tau] * capn;
 }
 
-// warp per destination leaf: even redistribution of the staged elements
+// warp per destination leaf: even redistribution of the staged elements.
+// Lane 0 finds the leaf's task and its share of the task's elements (32-bit
+// arithmetic: a task holds fewer than 2^32 elements) and broadcasts them.
 __global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
                                uint64_t ndst_total,
                                const uint64_t *__restrict__ class_start,
@@ -659,27 +663,33 @@ __global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
   uint64_t d = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (d >= ndst_total) return;
-  uint64_t tau = task_of(t.doff, ntasks, d);
-  uint64_t i = d - t.doff[tau];
-  uint64_t NL = t.ndst[tau], T = t.total[tau];
-  uint64_t per = T / NL, ext = T % NL;
-  uint32_t cnt = (uint32_t)(per + (i < ext));
-  uint64_t start = i * per + (i < ext ? i : ext);
-  uint64_t S;
-  uint32_t leafsize = kLeaf;
-  bool multi = true;
-  if (t.type[tau] == kResize) {
-    uint64_t capn = t.capn[tau];
-    S = task_new_base(t, tau, class_start) + (i << kLeafLog);
-    if (capn <= kLeaf) {
-      leafsize = (uint32_t)capn;
-      multi = false;
+  uint64_t S = 0, src = 0;
+  uint32_t cnt = 0, leafsize = kLeaf, multi = 1;
+  if (lane == 0) {
+    uint64_t tau = task_of(t.doff, ntasks, d);
+    uint32_t i = (uint32_t)(d - t.doff[tau]);
+    uint32_t NL = (uint32_t)t.ndst[tau], T = (uint32_t)t.total[tau];
+    uint32_t per = T / NL, ext = T - per * NL;
+    cnt = per + (i < ext);
+    src = t.out[tau] + (uint64_t)i * per + (i < ext ? i : ext);
+    if (t.type[tau] == kResize) {
+      uint64_t capn = t.capn[tau];
+      S = task_new_base(t, tau, class_start) + ((uint64_t)i << kLeafLog);
+      if (capn <= kLeaf) {
+        leafsize = (uint32_t)capn;
+        multi = 0;
+      }
+    } else {
+      S = g.base[t.u[tau]] + ((uint64_t)(t.w0[tau] + i) << kLeafLog);
     }
-  } else {
-    S = g.base[t.u[tau]] + ((uint64_t)(t.w0[tau] + i) << kLeafLog);
   }
+  S = __shfl_sync(0xffffffffu, S, 0);
+  src = __shfl_sync(0xffffffffu, src, 0);
+  cnt = __shfl_sync(0xffffffffu, cnt, 0);
+  leafsize = __shfl_sync(0xffffffffu, leafsize, 0);
+  multi = __shfl_sync(0xffffffffu, multi, 0);
   if ((uint32_t)lane < leafsize)
-    g.slots[S + lane] = (uint32_t)lane < cnt ? stage[t.out[tau] + start + lane] : kEmpty;
+    g.slots[S + lane] = (uint32_t)lane < cnt ? stage[src + lane] : kEmpty;
   if (lane == 0 && multi) g.lcnt[S >> kLeafLog] = (uint8_t)cnt;
 }
 
