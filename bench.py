@@ -9,9 +9,9 @@ by an equal-size delete batch of edges sampled uniformly from the base graph.
 
 One step = one insert batch + its delete batch.  `value` = inserted edges/s
 (input batch size / insert time, as the reference reports,
-internal/test.hpp:681-683) with batches resident in HBM; `e2e` = the same
-through the C ABI from pinned host buffers (host->device copy inside the
-timed call).  PageRank (FP64 pull, 10 iterations) and BFS from vertex 0 on
+internal/test.hpp:681-683) with batches resident in HBM; `e2e` = steps of
+the same sizes with fresh batches through the C ABI from pinned host buffers
+(host->device copy inside the timed call).  PageRank (FP64 pull, 10 iterations) and BFS from vertex 0 on
 the updated graph are reported alongside, each with its HBM roofline.
 
 --impl reference times the CPU implementation of the same path (the oracle
@@ -511,28 +511,32 @@ def main():
         print(json.dumps(res))
         return
 
-    # ---- batches (device and pinned host copies)
+    # ---- batches: inserts are 95% new RMAT edges and 5% sampled existing
+    # edges, removes are sampled existing edges (sampled from the graph as it
+    # is when the batches are made)
     plan = batch_plan(a.steps, a.warmup)
-    ins_d, rem_d, ins_h, rem_h = [], [], [], []
-    first = 0
-    with torch.cuda.stream(stream):
-        for b in plan:
-            k_new = b - b // 20
-            x = torch.empty((b, 2), dtype=torch.int32, device="cuda")
-            sg.gen_rmat(a.scale, k_new, seed=6, first=first, out=x[:k_new], **RMAT)
-            g.sample_edges(b // 20, seed=8, first=first, out=x[k_new:])
-            r = torch.empty((b, 2), dtype=torch.int32, device="cuda")
-            g.sample_edges(b, seed=7, first=first, out=r)
-            first += b
-            ins_d.append(x)
-            rem_d.append(r)
-            ins_h.append(x.cpu().pin_memory())
-            rem_h.append(r.cpu().pin_memory())
-    torch.cuda.synchronize()
+
+    def make_batches(first, host):
+        ins, rem = [], []
+        with torch.cuda.stream(stream):
+            for b in plan:
+                k_new = b - b // 20
+                x = torch.empty((b, 2), dtype=torch.int32, device="cuda")
+                sg.gen_rmat(a.scale, k_new, seed=6, first=first, out=x[:k_new], **RMAT)
+                g.sample_edges(b // 20, seed=8, first=first, out=x[k_new:])
+                r = torch.empty((b, 2), dtype=torch.int32, device="cuda")
+                g.sample_edges(b, seed=7, first=first, out=r)
+                first += b
+                ins.append(x.cpu().pin_memory() if host else x)
+                rem.append(r.cpu().pin_memory() if host else r)
+        torch.cuda.synchronize()
+        return ins, rem, first
+
+    ins_d, rem_d, next_first = make_batches(0, host=False)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
     pr_flush = flush
 
-    def run_steps(lo, hi, host, timed):
+    def run_steps(lo, hi, ins, rem):
         ti = tr = 0.0
         edges = 0
         for i in range(lo, hi):
@@ -540,9 +544,9 @@ def main():
                 flush.fill_(i)
             e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             e0.record(stream)
-            g.insert_batch(ins_h[i] if host else ins_d[i])
+            g.insert_batch(ins[i])
             e1.record(stream)
-            g.remove_batch(rem_h[i] if host else rem_d[i])
+            g.remove_batch(rem[i])
             e2.record(stream)
             e2.synchronize()
             ti += e0.elapsed_time(e1) / 1e3
@@ -555,7 +559,7 @@ def main():
     # the timed region brackets only that kernel, to keep event overhead out
     # of the step time.
     sg.profile_start()
-    run_steps(0, a.warmup, False, False)
+    run_steps(0, a.warmup, ins_d, rem_d)
     torch.cuda.synchronize()
     warm_prof = sg.profile_collect()
     dom = max(warm_prof.items(), key=lambda kv: kv[1]["ms"])[0]
@@ -565,7 +569,7 @@ def main():
     l0 = sg.kernel_launches()
     sg.profile_start(dom_name)
     with Clocks(dev) as clk:
-        ti, tr, edges = run_steps(a.warmup, a.warmup + a.steps, False, True)
+        ti, tr, edges = run_steps(a.warmup, a.warmup + a.steps, ins_d, rem_d)
     torch.cuda.synchronize()
     prof = sg.profile_collect()
     prof_all = warm_prof
@@ -577,9 +581,12 @@ def main():
     value = world * edges / ti
     ms_per_step = 1e3 * (ti + tr) / a.steps
 
-    # ---- e2e: the same steps through host (pinned) buffers
-    run_steps(0, a.warmup, True, False)
-    eti, etr, eedges = run_steps(a.warmup, a.warmup + a.steps, True, True)
+    # ---- e2e: steps of the same sizes through host (pinned) buffers, with
+    # fresh batches (the device pass's edges are already in the graph)
+    del ins_d, rem_d
+    ins_h, rem_h, next_first = make_batches(next_first, host=True)
+    run_steps(0, a.warmup, ins_h, rem_h)
+    eti, etr, eedges = run_steps(a.warmup, a.warmup + a.steps, ins_h, rem_h)
     e2e = {"value": world * eedges / max_over_ranks(eti, world), "unit": "edges/s",
            "h2d_bytes_per_step": int(8 * sum(plan[a.warmup:]) * 2 / a.steps),
            "d2h_bytes_per_step": 16,

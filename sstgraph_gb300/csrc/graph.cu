@@ -539,13 +539,15 @@ __global__ void k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul,
   uint64_t S = base + ((uint64_t)leaf << kLeafLog);
   uint32_t a = lane < c ? g.slots[S + lane] : kEmpty;
   uint32_t x = lane < k ? p_x[j0 + lane] : kEmpty;
+  // merged ranks in O(k) steps (k new ids, usually one or two): an old id
+  // moves up by the new ids below it; new id j lands at j + the old ids
+  // below it (a ballot per new id)
   uint32_t pa = lane, px = lane;
-#pragma unroll 8
-  for (int j = 0; j < 32; j++) {
+  for (uint32_t j = 0; j < k; j++) {
     uint32_t xj = __shfl_sync(0xffffffffu, x, j);
-    uint32_t aj = __shfl_sync(0xffffffffu, a, j);
-    pa += ((uint32_t)j < k && xj < a);
-    px += ((uint32_t)j < c && aj < x);
+    pa += xj < a;
+    uint32_t below = __popc(__ballot_sync(0xffffffffu, (uint32_t)lane < c && a < xj));
+    if ((uint32_t)lane == j) px = j + below;
   }
   __syncwarp();
   if (lane < c) g.slots[S + pa] = a;
