@@ -189,17 +189,27 @@ __global__ void k_scatter(const uint64_t *__restrict__ in,
   __shared__ uint32_t wcnt[kWarps][kRadix];
   __shared__ uint32_t run[kRadix];
   run[threadIdx.x] = hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x];
+  // the tile's keys (and values) come in at once, ahead of the ranking
+  // rounds, so the rounds do not wait on memory
+  const uint64_t t0 = (uint64_t)blockIdx.x * kTile;
+  uint64_t kk[kItems];
+  uint32_t vv[kItems];
+#pragma unroll
+  for (int it = 0; it < kItems; it++) {
+    uint64_t i = t0 + (uint64_t)it * kThreads + threadIdx.x;
+    kk[it] = i < n ? in[i] : 0;
+    vv[it] = (vin && i < n) ? vin[i] : 0u;
+  }
   __syncthreads();
-  uint64_t t0 = (uint64_t)blockIdx.x * kTile;
+#pragma unroll
   for (int it = 0; it < kItems; it++) {
     uint64_t i = t0 + (uint64_t)it * kThreads + threadIdx.x;
     bool valid = i < n;
-    uint64_t k = valid ? in[i] : 0;
-    uint32_t d = (uint32_t)(k >> shift) & 0xff;
+    uint32_t d = (uint32_t)(kk[it] >> shift) & 0xff;
     uint32_t pos = rank_iteration(d, valid, wcnt, run);
     if (valid) {
-      out[pos] = k;
-      if (vin) vout[pos] = vin[i];
+      out[pos] = kk[it];
+      if (vin) vout[pos] = vv[it];
     }
   }
 }
