@@ -226,6 +226,19 @@ __global__ void k_classify_insert(DGraph g, const uint64_t *__restrict__ p_ul,
   }
 }
 
+constexpr int kGroupsPerWarp = 4;
+
+// The leaf holding slot S, read as its whole aligned 128-byte line (always
+// inside the slab: slabs are whole lines, and a one-leaf segment never
+// crosses a line), then each lane's slot of the leaf by a shuffle: the load
+// does not wait on the leaf's count.
+__device__ __forceinline__ uint32_t leaf_slot(uint32_t linev, uint64_t S,
+                                              uint32_t c, int lane) {
+  const uint32_t o = (uint32_t)(S & (kLeaf - 1));
+  uint32_t a = __shfl_sync(0xffffffffu, linev, (o + lane) & 31);
+  return (uint32_t)lane < c ? a : kEmpty;
+}
+
 // remove, first pass: delete inside each touched leaf (warp per group) and
 // take the count off the row's degree
 __global__ void k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
@@ -233,32 +246,60 @@ __global__ void k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
                               const uint32_t *__restrict__ g_start,
                               const uint32_t *__restrict__ d_ngroups) {
   const int lane = threadIdx.x & 31;
+  constexpr int Q = kGroupsPerWarp;
   const uint32_t ng = *d_ngroups;
-  for (uint64_t gid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-       gid < ng; gid += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
-    uint32_t j0 = g_start[gid], j1 = g_start[gid + 1];
-    uint32_t k = j1 - j0;
-    uint64_t key = p_ul[j0];
-    uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
-    uint64_t base = g.base[u];
-    uint32_t cap = g.cap[u], deg = g.deg[u];
-    uint32_t c = leaf_count(g, base, cap, deg, leaf);
-    uint64_t S = base + ((uint64_t)leaf << kLeafLog);
-    uint32_t a = lane < c ? g.slots[S + lane] : kEmpty;
-    uint32_t d = lane < k ? p_x[j0 + lane] : kEmpty;
-    bool del = false;
-    for (uint32_t j = 0; j < k; j++) del |= (__shfl_sync(0xffffffffu, d, j) == a);
-    bool keep = lane < c && !del;
-    uint32_t mask = __ballot_sync(0xffffffffu, keep);
-    uint32_t pos = __popc(mask & ((1u << lane) - 1u));
-    __syncwarp();
-    if (keep) g.slots[S + pos] = a;
-    if (lane >= c - k && lane < c) g.slots[S + lane] = kEmpty;
-    if (lane == 0) {
-      if (cap > kLeaf) g.lcnt[(base >> kLeafLog) + leaf] = (uint8_t)(c - k);
-      atomicSub(&g.deg[u], k);
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       w * Q < ng; w += nw) {
+    // kGroupsPerWarp groups per round, each stage's loads issued together
+    uint32_t j0[Q], k[Q], d[Q], linev[Q], c[Q], cap[Q], deg[Q];
+    uint64_t key[Q], base[Q], S[Q];
+    bool ok[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      uint64_t gid = w * Q + q;
+      ok[q] = gid < ng;
+      j0[q] = ok[q] ? g_start[gid] : 0;
+      k[q] = ok[q] ? g_start[gid + 1] - j0[q] : 0;
     }
-    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      key[q] = ok[q] ? p_ul[j0[q]] : 0;
+      d[q] = (uint32_t)lane < k[q] ? p_x[j0[q] + lane] : kEmpty;
+    }
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      uint32_t u = (uint32_t)(key[q] >> 32);
+      base[q] = ok[q] ? g.base[u] : 0;
+      cap[q] = ok[q] ? g.cap[u] : 0;
+      deg[q] = ok[q] ? g.deg[u] : 0;
+    }
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      uint32_t leaf = (uint32_t)key[q];
+      S[q] = base[q] + ((uint64_t)leaf << kLeafLog);
+      linev[q] = ok[q] ? g.slots[(S[q] & ~uint64_t(kLeaf - 1)) + lane] : kEmpty;
+      c[q] = ok[q] ? leaf_count(g, base[q], cap[q], deg[q], leaf) : 0;
+    }
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      if (!ok[q]) break;
+      const uint32_t a = leaf_slot(linev[q], S[q], c[q], lane);
+      bool del = false;
+      for (uint32_t j = 0; j < k[q]; j++) del |= (__shfl_sync(0xffffffffu, d[q], j) == a);
+      bool keep = (uint32_t)lane < c[q] && !del;
+      uint32_t mask = __ballot_sync(0xffffffffu, keep);
+      uint32_t pos = __popc(mask & ((1u << lane) - 1u));
+      __syncwarp();
+      if (keep) g.slots[S[q] + pos] = a;
+      if ((uint32_t)lane >= c[q] - k[q] && (uint32_t)lane < c[q]) g.slots[S[q] + lane] = kEmpty;
+      if (lane == 0) {
+        if (cap[q] > kLeaf)
+          g.lcnt[(base[q] >> kLeafLog) + (uint32_t)key[q]] = (uint8_t)(c[q] - k[q]);
+        atomicSub(&g.deg[(uint32_t)(key[q] >> 32)], k[q]);
+      }
+      __syncwarp();
+    }
   }
 }
 
@@ -520,39 +561,67 @@ __global__ void k_task_setup(DGraph g, PmaParams p, bool insert,
 }
 
 // ---------------------------------------------------------------- step 9
+// warp per kGroupsPerWarp merge groups; each stage's loads for all of them
+// are issued together (the groups are independent leaves)
 __global__ void k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul,
                              const uint32_t *__restrict__ p_x,
                              const uint32_t *__restrict__ g_start,
                              const uint32_t *__restrict__ merge_list,
                              uint32_t nmerge) {
-  uint64_t tid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (tid >= nmerge) return;
-  uint32_t gid = merge_list[tid];
-  uint32_t j0 = g_start[gid], j1 = g_start[gid + 1];
-  uint32_t k = j1 - j0;
-  uint64_t key = p_ul[j0];
-  uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
-  uint64_t base = g.base[u];
-  uint32_t cap = g.cap[u], deg = g.deg[u];
-  uint32_t c = leaf_count(g, base, cap, deg, leaf);
-  uint64_t S = base + ((uint64_t)leaf << kLeafLog);
-  uint32_t a = lane < c ? g.slots[S + lane] : kEmpty;
-  uint32_t x = lane < k ? p_x[j0 + lane] : kEmpty;
-  // merged ranks in O(k) steps (k new ids, usually one or two): an old id
-  // moves up by the new ids below it; new id j lands at j + the old ids
-  // below it (a ballot per new id)
-  uint32_t pa = lane, px = lane;
-  for (uint32_t j = 0; j < k; j++) {
-    uint32_t xj = __shfl_sync(0xffffffffu, x, j);
-    pa += xj < a;
-    uint32_t below = __popc(__ballot_sync(0xffffffffu, (uint32_t)lane < c && a < xj));
-    if ((uint32_t)lane == j) px = j + below;
+  constexpr int Q = kGroupsPerWarp;
+  if (w * Q >= nmerge) return;
+  uint32_t j0[Q], k[Q], x[Q], linev[Q], c[Q], cap[Q];
+  uint64_t key[Q], base[Q], S[Q];
+  bool ok[Q];
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    ok[q] = w * Q + q < nmerge;
+    uint32_t gid = ok[q] ? merge_list[w * Q + q] : 0;
+    j0[q] = ok[q] ? g_start[gid] : 0;
+    k[q] = ok[q] ? g_start[gid + 1] - j0[q] : 0;
   }
-  __syncwarp();
-  if (lane < c) g.slots[S + pa] = a;
-  if (lane < k) g.slots[S + px] = x;
-  if (lane == 0 && cap > kLeaf) g.lcnt[(base >> kLeafLog) + leaf] = (uint8_t)(c + k);
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    key[q] = ok[q] ? p_ul[j0[q]] : 0;
+    x[q] = (uint32_t)lane < k[q] ? p_x[j0[q] + lane] : kEmpty;
+  }
+  uint32_t deg[Q];
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    uint32_t u = (uint32_t)(key[q] >> 32);
+    base[q] = ok[q] ? g.base[u] : 0;
+    cap[q] = ok[q] ? g.cap[u] : 0;
+    deg[q] = ok[q] ? g.deg[u] : 0;
+  }
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    uint32_t leaf = (uint32_t)key[q];
+    S[q] = base[q] + ((uint64_t)leaf << kLeafLog);
+    linev[q] = ok[q] ? g.slots[(S[q] & ~uint64_t(kLeaf - 1)) + lane] : kEmpty;
+    c[q] = ok[q] ? leaf_count(g, base[q], cap[q], deg[q], leaf) : 0;
+  }
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    if (!ok[q]) break;
+    const uint32_t a = leaf_slot(linev[q], S[q], c[q], lane);
+    // merged ranks in O(k) steps (k new ids, usually one or two): an old id
+    // moves up by the new ids below it; new id j lands at j + the old ids
+    // below it (a ballot per new id)
+    uint32_t pa = lane, px = lane;
+    for (uint32_t j = 0; j < k[q]; j++) {
+      uint32_t xj = __shfl_sync(0xffffffffu, x[q], j);
+      pa += xj < a;
+      uint32_t below = __popc(__ballot_sync(0xffffffffu, (uint32_t)lane < c[q] && a < xj));
+      if ((uint32_t)lane == j) px = j + below;
+    }
+    __syncwarp();
+    if ((uint32_t)lane < c[q]) g.slots[S[q] + pa] = a;
+    if ((uint32_t)lane < k[q]) g.slots[S[q] + px] = x[q];
+    if (lane == 0 && cap[q] > kLeaf)
+      g.lcnt[(base[q] >> kLeafLog) + (uint32_t)key[q]] = (uint8_t)(c[q] + k[q]);
+  }
 }
 
 __device__ __forceinline__ uint64_t task_of(const uint64_t *off, uint32_t ntasks,
@@ -1183,7 +1252,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     // each merge rewrites one 128-byte leaf (read + write) and its count
     // (the merged ids, fewer than 32 per leaf, are not counted)
     SST_LAUNCH_B(258ull * ps.n_merge, k_leaf_merge,
-               warp_blocks(ps.n_merge), kTB, 0, s, dg, p_ul, p_x,
+               warp_blocks((ps.n_merge + kGroupsPerWarp - 1) / kGroupsPerWarp),
+               kTB, 0, s, dg, p_ul, p_x,
                g_start, merge_list, ps.n_merge);
   if (ps.n_tasks) {
     if (ps.src_leaves) {
