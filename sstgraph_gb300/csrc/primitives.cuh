@@ -141,6 +141,30 @@ __device__ __forceinline__ T block_exclusive(T v, T identity, Op op, T *total) {
 // its range tile by tile with a running carry.  No block waits on another.
 constexpr int kScanRanges = 608;
 
+// A tile's results leave through shared memory: each thread holds items
+// t*kScanItems .. +kScanItems-1 of the tile, which it writes to a padded
+// buffer (stride kScanItems+1, no bank conflicts for 4-byte elements), and
+// the block then stores the tile striped, so each store instruction writes
+// whole sectors.
+template <typename T>
+__device__ __forceinline__ void store_tile(T *out, uint64_t base, uint64_t n,
+                                           bool reverse, const T *vals) {
+  __shared__ T sbuf[kScanThreads * (kScanItems + 1)];
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++)
+    sbuf[threadIdx.x * (kScanItems + 1) + k] = vals[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    const uint32_t e = (uint32_t)k * kScanThreads + threadIdx.x;
+    const uint64_t i = base + e;
+    if (i < n)
+      out[reverse ? n - 1 - i : i] =
+          sbuf[(e / kScanItems) * (kScanItems + 1) + e % kScanItems];
+  }
+  __syncthreads();
+}
+
 // tile t of the scan order: element i of the array (forward or reversed)
 template <typename T>
 __device__ __forceinline__ T scan_load(const T *in, uint64_t i, uint64_t n,
@@ -206,11 +230,11 @@ __global__ void k_scan_ranges(const T *__restrict__ in, T *__restrict__ out,
     T run = op(carry, block_exclusive(acc, identity, op, &total));
 #pragma unroll
     for (int k = 0; k < kScanItems; k++) {
-      uint64_t i = base + (uint64_t)threadIdx.x * kScanItems + k;
       T nxt = op(run, vals[k]);
-      if (i < n) out[reverse ? n - 1 - i : i] = exclusive ? run : nxt;
+      vals[k] = exclusive ? run : nxt;
       run = nxt;
     }
+    store_tile(out, base, n, reverse, vals);
     carry = op(carry, total);
   }
   if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
@@ -236,11 +260,11 @@ __global__ void k_scan_tile(const T *__restrict__ in, T *__restrict__ out,
   T run = block_exclusive(acc, identity, op, &total);
 #pragma unroll
   for (int k = 0; k < kScanItems; k++) {
-    uint64_t i = (uint64_t)threadIdx.x * kScanItems + k;
     T nxt = op(run, vals[k]);
-    if (i < n) out[reverse ? n - 1 - i : i] = exclusive ? run : nxt;
+    vals[k] = exclusive ? run : nxt;
     run = nxt;
   }
+  store_tile(out, 0, n, reverse, vals);
   if (total_out && threadIdx.x == 0) *total_out = total;
 }
 
