@@ -181,11 +181,15 @@ __global__ void k_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
   hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
 
+// Scatter of one pass; with hist_next it also counts the next pass's digit
+// of every key in the tile the key lands in (hist_next zeroed beforehand),
+// so the next pass needs no histogram launch.
 __global__ void k_scatter(const uint64_t *__restrict__ in,
                           uint64_t *__restrict__ out, uint64_t n, int shift,
                           const uint32_t *__restrict__ hist, uint32_t nblocks,
                           const uint32_t *__restrict__ vin,
-                          uint32_t *__restrict__ vout) {
+                          uint32_t *__restrict__ vout,
+                          uint32_t *__restrict__ hist_next, int next_shift) {
   __shared__ uint32_t wcnt[kWarps][kRadix];
   __shared__ uint32_t run[kRadix];
   run[threadIdx.x] = hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x];
@@ -210,6 +214,10 @@ __global__ void k_scatter(const uint64_t *__restrict__ in,
     if (valid) {
       out[pos] = kk[it];
       if (vin) vout[pos] = vv[it];
+      if (hist_next)
+        atomicAdd(&hist_next[(uint64_t)((kk[it] >> next_shift) & 0xff) * nblocks +
+                             pos / kTile],
+                  1u);
     }
   }
 }
@@ -282,7 +290,7 @@ constexpr int kSmallSortKV = 1024;
 size_t radix_sort_scratch_bytes(uint64_t n) {
   uint64_t nblocks = (n + kTile - 1) / kTile;
   uint64_t hn = nblocks * kRadix;
-  return ((hn * 4 + 255) & ~size_t(255)) + scan_scratch_bytes(hn, 4) + 512;
+  return 2 * ((hn * 4 + 255) & ~size_t(255)) + scan_scratch_bytes(hn, 4) + 512;
 }
 
 static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
@@ -304,25 +312,34 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
   }
   uint32_t nblocks = (uint32_t)((n + kTile - 1) / kTile);
   uint64_t hn = (uint64_t)nblocks * kRadix;
+  // digit-major tile histograms of this pass and the next (ping-pong)
   uint32_t *hist = arena.take<uint32_t>(hn);
-  if (!hist) return cudaErrorMemoryAllocation;
+  uint32_t *hnext = arena.take<uint32_t>(hn);
+  if (!hist || !hnext) return cudaErrorMemoryAllocation;
   uint64_t *src = keys, *dst = tmp;
   uint32_t *vsrc = vals, *vdst = vtmp;
-  // per pass: the histogram reads the keys; the scatter reads and writes keys
-  // (and values); both touch the block-digit table
+  // the first pass's histogram reads the keys; every scatter reads and
+  // writes keys (and values) and touches the tile-digit tables
   const uint64_t hist_bytes = 8 * n + 4 * hn;
-  const uint64_t scatter_bytes = (vals ? 24 : 16) * n + 4 * hn;
+  const uint64_t scatter_bytes = (vals ? 24 : 16) * n + 8 * hn;
+  SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, 0, hist, nblocks);
   for (int shift = 0; shift < bits; shift += 8) {
-    SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, shift, hist, nblocks);
     size_t mark = arena.used;
     cudaError_t e = scan<uint32_t, OpAdd>(hist, hist, hn, 0u, OpAdd{}, true,
                                           false, nullptr, arena, s);
     arena.used = mark;
     if (e != cudaSuccess) return e;
+    const bool more = shift + 8 < bits;
+    if (more) {
+      e = cudaMemsetAsync(hnext, 0, hn * 4, s);
+      if (e != cudaSuccess) return e;
+    }
     SST_LAUNCH_B(scatter_bytes, k_scatter, nblocks, kThreads, 0, s, src, dst, n,
-                 shift, hist, nblocks, vsrc, vdst);
+                 shift, hist, nblocks, vsrc, vdst, more ? hnext : nullptr,
+                 shift + 8);
     std::swap(src, dst);
     std::swap(vsrc, vdst);
+    std::swap(hist, hnext);
   }
   *result = src;
   if (vresult) *vresult = vsrc;
