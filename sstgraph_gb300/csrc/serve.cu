@@ -361,10 +361,12 @@ sst_status sst_server_create(sst_graph *g, const sst_server_config *cfg,
   s->g = g;
   if (cfg) s->cfg = *cfg;
   uint32_t want = s->cfg.query_slots ? s->cfg.query_slots : 2;
-  // admission: each slot holds a snapshot about the size of the live graph
-  // plus traversal buffers (~40 B per vertex)
+  // admission: the live graph (with its update scratch) plus, per slot, a
+  // snapshot -- vertex table, slab and leaf counts, no update scratch -- and
+  // its traversal buffers (~40 B per vertex)
   uint64_t graph_bytes = sst::graph_device_bytes(g);
-  uint64_t per_slot = graph_bytes + (uint64_t)g->n * 40;
+  uint64_t per_slot = (uint64_t)g->n * 16 + g->nslots * 4 + g->nslots / sst::kLeaf +
+                      (uint64_t)g->n * 40;
   if (s->cfg.hbm_budget_bytes) {
     uint64_t room = s->cfg.hbm_budget_bytes > graph_bytes ? s->cfg.hbm_budget_bytes - graph_bytes : 0;
     uint64_t fit = room / std::max<uint64_t>(per_slot, 1);
