@@ -215,7 +215,8 @@ SST_API sst_status sst_bc_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
                                 double *out, uint32_t flags);
 /* Traversal tuning (no reference counterpart).  sst_autotune times the
  * knobs on this graph and keeps the fastest: PageRank over chunk_leaves
- * {8,16,32} x pr_lanes {4,8,16}, then BFS over bfs_alpha {5,10,20,40,80};
+ * {8,16,32} x pr_lanes {4,8,16}, then pr_hot {0,8192,16384,24576}, then BFS
+ * over bfs_alpha {5,10,20,40,80};
  * pr_ms / bfs_ms report the winners' times (3 PageRank iterations; one BFS).
  * The leaf itself stays 32 slots (one 128-byte line): it is the storage
  * format, not a launch parameter. */
@@ -224,6 +225,9 @@ typedef struct sst_tuning {
   uint32_t pr_lanes;     /* lanes per one-leaf vertex in PageRank (4, 8, 16) */
   uint32_t bfs_alpha;    /* BFS pulls once (frontier + its edges) * alpha > m */
   float pr_ms, bfs_ms;
+  uint32_t pr_hot;       /* PageRank: contributions of ids below this staged in
+                            shared memory (0..24576; pays on degree-ordered
+                            graphs, sst_degree_order_map) */
 } sst_tuning;
 SST_API sst_status sst_autotune(sst_graph *g, sst_tuning *out);
 SST_API sst_status sst_get_tuning(sst_graph *g, sst_tuning *out);

@@ -49,7 +49,7 @@ class sst_config(ctypes.Structure):
 class sst_tuning(ctypes.Structure):
     _fields_ = [("chunk_leaves", ctypes.c_uint32), ("pr_lanes", ctypes.c_uint32),
                 ("bfs_alpha", ctypes.c_uint32), ("pr_ms", ctypes.c_float),
-                ("bfs_ms", ctypes.c_float)]
+                ("bfs_ms", ctypes.c_float), ("pr_hot", ctypes.c_uint32)]
 
 
 class sst_server_config(ctypes.Structure):
@@ -595,7 +595,8 @@ def load_graph_file(path: str, device: int = 0) -> "SparseMatrixV":
 
 def _tuning_dict(t):
     return {"chunk_leaves": t.chunk_leaves, "pr_lanes": t.pr_lanes,
-            "bfs_alpha": t.bfs_alpha, "pr_ms": t.pr_ms, "bfs_ms": t.bfs_ms}
+            "bfs_alpha": t.bfs_alpha, "pr_hot": t.pr_hot, "pr_ms": t.pr_ms,
+            "bfs_ms": t.bfs_ms}
 
 
 def autotune(g: SparseMatrixV) -> dict:
@@ -611,8 +612,8 @@ def get_tuning(g: SparseMatrixV) -> dict:
     return _tuning_dict(t)
 
 
-def set_tuning(g: SparseMatrixV, chunk_leaves=32, pr_lanes=8, bfs_alpha=20):
-    t = sst_tuning(chunk_leaves, pr_lanes, bfs_alpha, 0.0, 0.0)
+def set_tuning(g: SparseMatrixV, chunk_leaves=32, pr_lanes=8, bfs_alpha=20, pr_hot=0):
+    t = sst_tuning(chunk_leaves, pr_lanes, bfs_alpha, 0.0, 0.0, pr_hot)
     _check(lib().sst_set_tuning(g.handle, ctypes.byref(t)))
 
 

@@ -59,6 +59,8 @@ struct TravState {
   // one-leaf vertex in PageRank, and the BFS switch to pull once
   // (frontier + its edges) * bfs_alpha > m
   uint32_t chunk_leaves = 32, pr_lanes = 8, bfs_alpha = 20;
+  uint32_t pr_hot = 0;        // contributions staged in shared memory
+  uint32_t pr_hot_used = ~0u; // pr_hot of the captured graph
   uint32_t lists_cl = 0;      // chunk size the lists were built with
   uint64_t lists_stamp = 0;   // bumped on every rebuild of the lists
   // chunk list of multi-leaf vertices
@@ -396,6 +398,124 @@ __global__ void k_pr_chunks(DGraph g, const unsigned long long *__restrict__ cde
       pr_finish(v, acc, k, g.deg[v], rdeg, cout, rank, last);
     } else {
       partial[c] = acc;
+    }
+  }
+}
+
+// ---- PageRank with the contributions of ids below `hot` staged in shared
+// memory once per block: on a degree-ordered graph (highest degree first,
+// sst_degree_order_map) those are the vertices most edges point to, so
+// their gathers leave L2 alone.  Blocks are persistent and stride over the
+// work; the loops stay warp-uniform for the shuffles.
+__device__ __forceinline__ void stage_hot(unsigned long long *sh,
+                                          const unsigned long long *cin,
+                                          uint32_t hot) {
+  for (uint32_t i = threadIdx.x; i < hot; i += blockDim.x) sh[i] = cin[i];
+  __syncthreads();
+}
+__device__ __forceinline__ unsigned long long gather(const unsigned long long *sh,
+                                                     const unsigned long long *cin,
+                                                     uint32_t x, uint32_t hot) {
+  return x < hot ? sh[x] : ld_keep(cin + x);
+}
+
+template <int G>
+__global__ void k_pr_small_hot(DGraph g, const unsigned long long *__restrict__ sdesc,
+                               const uint32_t *__restrict__ small, uint64_t nsmall,
+                               const unsigned long long *__restrict__ cin,
+                               unsigned long long *__restrict__ cout,
+                               double *__restrict__ rank,
+                               const unsigned long long *__restrict__ rdeg,
+                               PrConst k, bool last, uint32_t hot) {
+  extern __shared__ unsigned long long sh[];
+  constexpr int Q = 32 / G;
+  stage_hot(sh, cin, hot);
+  const unsigned long long pol = l2_evict_first();
+  const uint32_t sub = threadIdx.x & (G - 1);
+  const uint64_t per_warp = (32 / G) * kSmallPer;  // vertices per warp round
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t rounds = (nsmall + per_warp - 1) / per_warp;
+  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       w < rounds; w += nwarps) {
+    const uint64_t i0 = (w * (32 / G) + ((threadIdx.x & 31) / G)) * kSmallPer;
+    uint32_t x[kSmallPer][Q];
+    uint32_t dg[kSmallPer];
+#pragma unroll
+    for (int u = 0; u < kSmallPer; u++) {
+      uint64_t i = i0 + u;
+      unsigned long long dsc = i < nsmall ? sdesc[i] : 0ull;
+      dg[u] = (uint32_t)(dsc & 63);
+      const uint32_t *p = g.slots + (dsc >> 6);
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        uint32_t j = sub + G * q;
+        x[u][q] = j < dg[u] ? ld_stream(p + j, pol) : kEmpty;
+      }
+    }
+    unsigned long long mine = 0;
+    uint32_t mydeg = 0;
+#pragma unroll
+    for (int u = 0; u < kSmallPer; u++) {
+      unsigned long long a = 0;
+#pragma unroll
+      for (int q = 0; q < Q; q++)
+        if (x[u][q] != kEmpty) a += gather(sh, cin, x[u][q], hot);
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (sub == (uint32_t)u) {
+        mine = a;
+        mydeg = dg[u];
+      }
+    }
+    if (sub < (uint32_t)kSmallPer && i0 + sub < nsmall)
+      pr_finish(small[i0 + sub], mine, k, mydeg, rdeg, cout, rank, last);
+  }
+}
+
+__global__ void k_pr_chunks_hot(DGraph g, const unsigned long long *__restrict__ cdesc,
+                                const uint32_t *__restrict__ cv, uint64_t nchunks,
+                                const unsigned long long *__restrict__ cin,
+                                unsigned long long *__restrict__ cout,
+                                double *__restrict__ rank,
+                                const unsigned long long *__restrict__ rdeg,
+                                unsigned long long *__restrict__ partial, PrConst k,
+                                bool last, uint32_t hot) {
+  extern __shared__ unsigned long long sh[];
+  stage_hot(sh, cin, hot);
+  const int lane = threadIdx.x & 31;
+  const unsigned long long pol = l2_evict_first();
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       c < nchunks; c += nwarps) {
+    unsigned long long dsc = cdesc[c];
+    const uint64_t leaf0 = dsc >> 8;
+    const uint32_t l1 = (uint32_t)(dsc & 63);
+    const bool single = (dsc >> 7) & 1;
+    const uint32_t mycnt = (uint32_t)lane < l1 ? g.lcnt[leaf0 + lane] : 0u;
+    const uint32_t *sl = g.slots + (leaf0 << kLeafLog) + lane;
+    unsigned long long acc = 0;
+    for (uint32_t l = 0; l < l1; l += 8) {
+      uint32_t x[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        uint32_t cq = __shfl_sync(0xffffffffu, mycnt, (l + q) & 31);
+        if (l + q >= l1) cq = 0;
+        x[q] = (uint32_t)lane < cq ? ld_stream(sl + ((uint64_t)(l + q) << kLeafLog), pol)
+                                   : kEmpty;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (x[q] != kEmpty) acc += gather(sh, cin, x[q], hot);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+    if (lane == 0) {
+      if (single) {
+        uint32_t v = cv[c];
+        pr_finish(v, acc, k, g.deg[v], rdeg, cout, rank, last);
+      } else {
+        partial[c] = acc;
+      }
     }
   }
 }
@@ -1087,6 +1207,23 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   unsigned long long *cin = reinterpret_cast<unsigned long long *>(t->ca.p);
   unsigned long long *cout = reinterpret_cast<unsigned long long *>(t->cb.p);
   unsigned long long *part = reinterpret_cast<unsigned long long *>(t->partial.p);
+  // the shared-memory cache: at most the rows, at most 24,576 entries
+  // (192 KiB); persistent grids sized by occupancy at that footprint
+  const uint32_t hot = std::min<uint32_t>(t->pr_hot, std::min<uint32_t>(n, 24576));
+  const size_t hot_bytes = (size_t)hot * 8;
+  unsigned hot_grid[4] = {1, 1, 1, 1};
+  if (hot) {
+    const void *fns[4] = {(const void *)k_pr_small_hot<4>, (const void *)k_pr_small_hot<8>,
+                          (const void *)k_pr_small_hot<16>, (const void *)k_pr_chunks_hot};
+    for (int i = 0; i < 4; i++) {
+      SST_CUDA_TRY(cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)hot_bytes));
+      int per_sm = 0;
+      SST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], 1024,
+                                                                 hot_bytes));
+      hot_grid[i] = (unsigned)std::max(1, per_sm) * (unsigned)g->sms;
+    }
+  }
   auto launch_all = [&]() {
     unsigned long long *ci = cin, *co = cout;
     SST_LAUNCH(k_pr_start, blocks_for(n), kTB, 0, s, g->d_deg, n, r0f, rdeg, ci,
@@ -1094,7 +1231,17 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
     DGraph dg = g->view();
     for (uint32_t it = 0; it < iters; it++) {
       bool last = it + 1 == iters;
-      if (t->nsmall) {
+      if (hot && t->nsmall) {
+        if (t->pr_lanes == 4)
+          SST_LAUNCH(k_pr_small_hot<4>, hot_grid[0], 1024, hot_bytes, s, dg,
+                     t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot);
+        else if (t->pr_lanes == 16)
+          SST_LAUNCH(k_pr_small_hot<16>, hot_grid[2], 1024, hot_bytes, s, dg,
+                     t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot);
+        else
+          SST_LAUNCH(k_pr_small_hot<8>, hot_grid[1], 1024, hot_bytes, s, dg,
+                     t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot);
+      } else if (t->nsmall) {
         const uint64_t groups = (t->nsmall + kSmallPer - 1) / kSmallPer;
         if (t->pr_lanes == 4)
           SST_LAUNCH(k_pr_small<4>, blocks_for(groups * 4), kTB, 0, s, dg,
@@ -1106,7 +1253,10 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
           SST_LAUNCH(k_pr_small<8>, blocks_for(groups * 8), kTB, 0, s, dg,
                      t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last);
       }
-      if (t->nchunks)
+      if (hot && t->nchunks)
+        SST_LAUNCH(k_pr_chunks_hot, hot_grid[3], 1024, hot_bytes, s, dg, t->cdesc.p,
+                   t->cv.p, t->nchunks, ci, co, d_rank, rdeg, part, K, last, hot);
+      else if (t->nchunks)
         SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cdesc.p,
                    t->cv.p, t->nchunks, ci, co, d_rank, rdeg, part, K, last);
       if (t->nmulti)
@@ -1119,8 +1269,8 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   // with the kernel profiler on, launch them one by one so each is timed
   const void *key[6] = {d_rank, s, cin, cout, part, rdeg};
   bool same = t->pr_exec && t->pr_version == t->lists_stamp &&
-              t->pr_lanes_used == t->pr_lanes && t->pr_iters == iters &&
-              t->pr_damping == damping;
+              t->pr_lanes_used == t->pr_lanes && t->pr_hot_used == t->pr_hot &&
+              t->pr_iters == iters && t->pr_damping == damping;
   for (int i = 0; i < 6 && same; i++) same = t->pr_key[i] == key[i];
   if (profiling("k_pr_chunks") || profiling("k_pr_small")) {
     launch_all();
@@ -1145,6 +1295,7 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
     }
     t->pr_version = t->lists_stamp;
     t->pr_lanes_used = t->pr_lanes;
+    t->pr_hot_used = t->pr_hot;
     t->pr_iters = iters;
     t->pr_damping = damping;
     for (int i = 0; i < 6; i++) t->pr_key[i] = key[i];
@@ -1908,13 +2059,15 @@ sst_status bc_multi(sst_graph *g, const uint32_t *h_srcs, uint32_t k,
 
 // ------------------------------------------------------------- autotuner
 // Times the traversal knobs on this graph and keeps the fastest: PageRank
-// (3 iterations) over chunk sizes {8, 16, 32} x lanes {4, 8, 16}, then BFS
-// from three sources over push/pull thresholds {5, 10, 20, 40, 80}.
+// (3 iterations) over chunk sizes {8, 16, 32} x lanes {4, 8, 16}, then its
+// shared-memory cache {0, 8192, 16384, 24576}, then BFS from three sources
+// over push/pull thresholds {5, 10, 20, 40, 80}.
 sst_status get_tuning(sst_graph *g, sst_tuning *out) {
   TravState *t = state(g);
   out->chunk_leaves = t->chunk_leaves;
   out->pr_lanes = t->pr_lanes;
   out->bfs_alpha = t->bfs_alpha;
+  out->pr_hot = t->pr_hot;
   out->pr_ms = 0.f;
   out->bfs_ms = 0.f;
   return SST_OK;
@@ -1923,14 +2076,16 @@ sst_status get_tuning(sst_graph *g, sst_tuning *out) {
 sst_status set_tuning(sst_graph *g, const sst_tuning *in) {
   if (in->chunk_leaves < 1 || in->chunk_leaves > 32 ||
       (in->pr_lanes != 4 && in->pr_lanes != 8 && in->pr_lanes != 16) ||
-      in->bfs_alpha < 1) {
-    set_error_message("tuning out of range (chunk_leaves 1..32, pr_lanes 4/8/16, bfs_alpha >= 1)");
+      in->bfs_alpha < 1 || in->pr_hot > 24576) {
+    set_error_message("tuning out of range (chunk_leaves 1..32, pr_lanes 4/8/16, "
+                      "bfs_alpha >= 1, pr_hot <= 24576)");
     return SST_EINVAL;
   }
   TravState *t = state(g);
   t->chunk_leaves = in->chunk_leaves;
   t->pr_lanes = in->pr_lanes;
   t->bfs_alpha = in->bfs_alpha;
+  t->pr_hot = in->pr_hot;
   return SST_OK;
 }
 
@@ -1975,6 +2130,20 @@ sst_status autotune(sst_graph *g, sst_tuning *out) {
     }
   t->chunk_leaves = bcl;
   t->pr_lanes = blanes;
+  // then the shared-memory cache of the lowest ids (pays on degree-ordered
+  // graphs)
+  uint32_t bhot = 0;
+  const uint32_t hots[3] = {8192, 16384, 24576};
+  for (uint32_t a = 0; a < 3 && st == SST_OK; a++) {
+    t->pr_hot = hots[a];
+    float ms = 0.f;
+    st = timed([&] { return pagerank(g, 3, 0.85, rank); }, &ms);
+    if (st == SST_OK && ms < best_pr) {
+      best_pr = ms;
+      bhot = hots[a];
+    }
+  }
+  t->pr_hot = bhot;
   // BFS sources: the first three vertices with edges along a fixed stride
   std::vector<uint32_t> deg(n), src;
   if (st == SST_OK) {

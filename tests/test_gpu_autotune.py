@@ -37,15 +37,16 @@ def test_every_setting_same_result(sg, pair):
     exp_multi = np.stack([o.bfs(int(s)) for s in srcs])
     for cl in (1, 4, 8, 16, 32):
         for lanes in (4, 8, 16):
-            for alpha in (1, 20, 1000):
-                sg.set_tuning(g, chunk_leaves=cl, pr_lanes=lanes, bfs_alpha=alpha)
+            for alpha, hot in ((1, 0), (20, 4096), (1000, 24576)):
+                sg.set_tuning(g, chunk_leaves=cl, pr_lanes=lanes, bfs_alpha=alpha,
+                              pr_hot=hot)
                 assert sg.get_tuning(g)["chunk_leaves"] == cl
                 pr = sg.PR_S(g, 7)
                 if ref_pr is None:
                     ref_pr = pr
                     exp = o.pagerank(7)
                     assert np.max(np.abs(pr - exp)) <= 1e-9 * np.max(np.abs(exp))
-                assert np.array_equal(pr, ref_pr), (cl, lanes, alpha)
+                assert np.array_equal(pr, ref_pr), (cl, lanes, alpha, hot)
                 assert np.array_equal(sg.BFS(g, 3, depths=True), exp_bfs)
                 assert np.array_equal(sg.BFS_multi(g, srcs), exp_multi)
     sg.set_tuning(g)
@@ -57,6 +58,7 @@ def test_autotune_picks_from_space(sg, pair):
     assert t["chunk_leaves"] in (8, 16, 32)
     assert t["pr_lanes"] in (4, 8, 16)
     assert t["bfs_alpha"] in (5, 10, 20, 40, 80)
+    assert t["pr_hot"] in (0, 8192, 16384, 24576)
     assert t["pr_ms"] > 0 and t["bfs_ms"] > 0
     assert sg.get_tuning(g)["bfs_alpha"] == t["bfs_alpha"]
     exp = o.pagerank(10)
@@ -67,6 +69,6 @@ def test_autotune_picks_from_space(sg, pair):
 def test_bad_settings_refused(sg, pair):
     g, _ = pair
     for kw in ({"chunk_leaves": 0}, {"chunk_leaves": 33}, {"pr_lanes": 5},
-               {"bfs_alpha": 0}):
+               {"bfs_alpha": 0}, {"pr_hot": 24577}):
         with pytest.raises(sg.SSTError):
             sg.set_tuning(g, **kw)
