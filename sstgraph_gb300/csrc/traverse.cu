@@ -660,27 +660,25 @@ __global__ void k_bfs_pull_small8(DGraph g, const unsigned long long *__restrict
   for (int u = 0; u < 4; u++) {
     const uint64_t i = i0 + u;
     uint32_t v = 0, d = 0;
+    bool open = false;
     unsigned long long dsc = 0;
     if (i < nsmall) {
       v = small[i];
+      open = depth[v] < 0;
       dsc = sdesc[i];
       d = (uint32_t)(dsc & 63);
     }
-    // the depth check and the leaf's ids load together (the ids are read
-    // whether or not v turns out visited)
-    const uint32_t *p = g.slots + (dsc >> 6);
-    uint32_t w[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      uint32_t j = sub + 8 * q;
-      w[q] = j < d ? p[j] : kEmpty;
-    }
-    const bool open = i < nsmall && depth[v] < 0;
     uint32_t best = kEmpty;
     if (open) {
+      const uint32_t *p = g.slots + (dsc >> 6);
 #pragma unroll
-      for (int q = 0; q < 4; q++)
-        if (w[q] < best && in_front(fbits, w[q])) best = w[q];
+      for (int q = 0; q < 4; q++) {
+        uint32_t j = sub + 8 * q;
+        if (j < d) {
+          uint32_t w = p[j];
+          if (w < best && in_front(fbits, w)) best = w;
+        }
+      }
     }
     // smallest frontier neighbour over the group's 8 lanes
 #pragma unroll
@@ -713,20 +711,14 @@ __global__ void k_bfs_pull_chunks(DGraph g, const unsigned long long *__restrict
   uint32_t v = 0;
   if (c < nchunks) {
     v = cv[c];
-    const unsigned long long dsc = cdesc[c];
-    const uint64_t leaf0 = dsc >> 8;
-    const uint32_t l1 = (uint32_t)(dsc & 63);
-    const uint32_t *sl = g.slots + (leaf0 << kLeafLog) + lane;
-    // the depth check, the leaf counts and the first eight leaves' ids load
-    // together; the ids are masked by the counts afterwards
-    uint32_t pre[8];
-#pragma unroll
-    for (int q = 0; q < 8; q++)
-      pre[q] = (uint32_t)q < l1 ? sl[(uint64_t)q << kLeafLog] : kEmpty;
-    const uint32_t mycnt = (uint32_t)lane < l1 ? g.lcnt[leaf0 + lane] : 0u;
     // another chunk may claim v at any time: every lane follows lane 0's
     // reading, so the warp stays converged for its shuffles
     if (__shfl_sync(0xffffffffu, __ldcg(depth + v), 0) < 0) {
+      const unsigned long long dsc = cdesc[c];
+      const uint64_t leaf0 = dsc >> 8;
+      const uint32_t l1 = (uint32_t)(dsc & 63);
+      const uint32_t mycnt = (uint32_t)lane < l1 ? g.lcnt[leaf0 + lane] : 0u;
+      const uint32_t *sl = g.slots + (leaf0 << kLeafLog) + lane;
       uint32_t found = kEmpty;
       for (uint32_t l = 0; l < l1 && found == kEmpty; l += 8) {
         uint32_t x[8];
@@ -734,9 +726,7 @@ __global__ void k_bfs_pull_chunks(DGraph g, const unsigned long long *__restrict
         for (int q = 0; q < 8; q++) {
           uint32_t cq = __shfl_sync(0xffffffffu, mycnt, (l + q) & 31);
           if (l + q >= l1) cq = 0;
-          uint32_t id = l == 0 ? pre[q]
-                               : (l + q < l1 ? sl[(uint64_t)(l + q) << kLeafLog] : kEmpty);
-          x[q] = (uint32_t)lane < cq ? id : kEmpty;
+          x[q] = (uint32_t)lane < cq ? sl[(uint64_t)(l + q) << kLeafLog] : kEmpty;
         }
         uint32_t best = kEmpty;
 #pragma unroll
