@@ -241,7 +241,8 @@ __device__ __forceinline__ uint32_t leaf_slot(uint32_t linev, uint64_t S,
 
 // remove, first pass: delete inside each touched leaf (warp per group) and
 // take the count off the row's degree
-__global__ void k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
+__global__ void __launch_bounds__(256, 4)
+k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
                               const uint32_t *__restrict__ p_x,
                               const uint32_t *__restrict__ g_start,
                               const uint32_t *__restrict__ d_ngroups) {
@@ -563,7 +564,8 @@ __global__ void k_task_setup(DGraph g, PmaParams p, bool insert,
 // ---------------------------------------------------------------- step 9
 // warp per kGroupsPerWarp merge groups; each stage's loads for all of them
 // are issued together (the groups are independent leaves)
-__global__ void k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul,
+__global__ void __launch_bounds__(256, 4)
+k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul,
                              const uint32_t *__restrict__ p_x,
                              const uint32_t *__restrict__ g_start,
                              const uint32_t *__restrict__ merge_list,
