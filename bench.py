@@ -610,7 +610,9 @@ def main():
         gr.set_stream(stream.cuda_stream)
         torch.cuda.synchronize()
         relabel_s = time.time() - t0
+        tuning_deg = sg.autotune(gr)
         pr_deg = measure_pagerank(gr)
+        pr_deg["tuning"] = tuning_deg
         o1 = torch.empty(n, dtype=torch.float64, device="cuda")
         o2 = torch.empty(n, dtype=torch.float64, device="cuda")
         sg.PR_S(g, a.pr_iters, out=o1)
