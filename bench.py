@@ -454,7 +454,7 @@ def main():
             else:
                 reqs.append(("tc", rng.integers(0, n, 10000).astype(np.uint32)))
         gaps = rng.exponential(1.0 / a.serve_rate, len(reqs))
-        srv = sg.Server(g, query_slots=4, hbm_budget_bytes=60 << 30)
+        srv = sg.Server(g, query_slots=2, hbm_budget_bytes=60 << 30)
         t0 = time.perf_counter()
         arrive = t0 + np.cumsum(gaps)
         tickets = []

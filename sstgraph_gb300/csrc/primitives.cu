@@ -284,6 +284,7 @@ __global__ void k_sort_small(uint64_t *__restrict__ keys,
 }
 
 constexpr int kSmallSortKV = 1024;
+constexpr uint32_t kFuseHistBlocks = 64;  // 256K keys
 
 }  // namespace
 
@@ -329,16 +330,24 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
                                           false, nullptr, arena, s);
     arena.used = mark;
     if (e != cudaSuccess) return e;
+    // the next pass's histogram rides on this scatter only for small sorts:
+    // on large ones every block's keys of one digit land in the same one or
+    // two destination tiles, and the atomics on those counters serialise
     const bool more = shift + 8 < bits;
-    if (more) {
+    const bool fuse = more && nblocks <= kFuseHistBlocks;
+    if (fuse) {
       e = cudaMemsetAsync(hnext, 0, hn * 4, s);
       if (e != cudaSuccess) return e;
     }
     SST_LAUNCH_B(scatter_bytes, k_scatter, nblocks, kThreads, 0, s, src, dst, n,
-                 shift, hist, nblocks, vsrc, vdst, more ? hnext : nullptr,
+                 shift, hist, nblocks, vsrc, vdst, fuse ? hnext : nullptr,
                  shift + 8);
     std::swap(src, dst);
     std::swap(vsrc, vdst);
+    // unfused: the next pass's histogram over this pass's output
+    if (more && !fuse)
+      SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, shift + 8,
+                   hnext, nblocks);
     std::swap(hist, hnext);
   }
   *result = src;

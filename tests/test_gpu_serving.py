@@ -124,9 +124,15 @@ def test_budget_limits_slots(sg):
     n = 1 << 12
     g = sg.SparseMatrixV(n)
     g.insert_batch(oracle.symmetrize(oracle.rmat(12, 8 * n, seed=4)))
-    big = g.get_memory_size()
-    srv = sg.Server(g, query_slots=8, hbm_budget_bytes=big * 3 + n * 120)
-    assert 1 <= srv.slots < 8
-    srv.close()
-    with pytest.raises(sg.SSTError):
-        sg.Server(g, query_slots=2, hbm_budget_bytes=big // 2)
+    big = g.get_memory_size()  # the live graph, update scratch included
+    # a slot costs one snapshot (vertex table, slab, traversal buffers):
+    # admission grows with the budget and stops at the request
+    counts = []
+    for extra in (big // 8, big // 2, 2 * big, 64 * big):
+        srv = sg.Server(g, query_slots=8, hbm_budget_bytes=big + extra)
+        counts.append(srv.slots)
+        srv.close()
+    assert counts == sorted(counts) and counts[-1] == 8 and counts[0] < 8
+    assert all(1 <= c <= 8 for c in counts)
+    with pytest.raises(sg.SSTError):  # no room for one snapshot
+        sg.Server(g, query_slots=2, hbm_budget_bytes=big + 1024)
