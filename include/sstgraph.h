@@ -69,6 +69,8 @@ typedef struct sst_config {
   uint32_t keep_self_loops;    /* 1 = insert (v, v) as well: rows are plain
                                   sets (the TinySet facade); 0 = skip them as
                                   SparseMatrix.hpp:570,602 does */
+  uint32_t weighted;           /* 1 = every edge carries a uint32 value
+                                  (SparseMatrixV<true, uint32_t>) */
 } sst_config;
 
 /* ---- lifetime ------------------------------------------------------- */
@@ -106,6 +108,23 @@ SST_API sst_status sst_update_batches(sst_graph *g, const uint32_t *pairs,
                                       const uint64_t *offsets,
                                       const uint8_t *ops, uint32_t nbatches,
                                       uint32_t flags, uint64_t *n_invalid);
+/* Weighted graphs (sst_config.weighted = 1; SparseMatrixV<true, uint32_t>,
+ * internal/test.hpp:699-846): insert_batch with one value per pair.  An edge
+ * already present takes the new value, and of several equal pairs in one
+ * batch the last value given wins (the reference's insert updates the value
+ * of a present key, PMA.hpp:1137-1145).  Plain sst_insert_batch on a
+ * weighted graph gives value 1.  The batched form, relabelling and building
+ * from a CSR take unweighted graphs only (SST_ESTATE). */
+SST_API sst_status sst_insert_batch_weighted(sst_graph *g, const uint32_t *pairs,
+                                             const uint32_t *values, uint64_t n,
+                                             uint32_t flags, uint64_t *n_invalid);
+/* value(el_t, el_t)  SparseMatrix.hpp:727: values[i] of pair i (0 where
+ * absent); found may be NULL */
+SST_API sst_status sst_values_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
+                                   uint32_t *values, uint8_t *found, uint32_t flags);
+/* the whole weighted graph as a CSR with its values */
+SST_API sst_status sst_to_csr_values(sst_graph *g, uint64_t *offsets, uint32_t *cols,
+                                     uint32_t *values, uint32_t flags);
 /* insert(el_t, el_t) / remove(el_t, el_t)  SparseMatrix.hpp:164-166 */
 SST_API sst_status sst_insert(sst_graph *g, uint32_t row, uint32_t col);
 SST_API sst_status sst_remove(sst_graph *g, uint32_t row, uint32_t col);
@@ -232,6 +251,10 @@ typedef struct sst_tuning {
 SST_API sst_status sst_autotune(sst_graph *g, sst_tuning *out);
 SST_API sst_status sst_get_tuning(sst_graph *g, sst_tuning *out);
 SST_API sst_status sst_set_tuning(sst_graph *g, const sst_tuning *in);
+/* BF(g, src)  test.hpp:611-634: shortest-path lengths over the edge values
+ * of a weighted graph (push Bellman-Ford); unreachable = INT32_MAX, lengths
+ * at or above 2^31-1 saturate there.  Directed: rows are out-edges. */
+SST_API sst_status sst_bf(sst_graph *g, uint32_t src, int32_t *dist, uint32_t flags);
 /* TouchAll(g)  test.hpp:476 */
 SST_API sst_status sst_touch_all(sst_graph *g, uint64_t *out);
 

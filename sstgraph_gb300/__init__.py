@@ -43,7 +43,8 @@ class sst_config(ctypes.Structure):
                 ("upper_root", ctypes.c_float),
                 ("lower_root", ctypes.c_float),
                 ("grow_fill", ctypes.c_float),
-                ("keep_self_loops", ctypes.c_uint32)]
+                ("keep_self_loops", ctypes.c_uint32),
+                ("weighted", ctypes.c_uint32)]
 
 
 class sst_tuning(ctypes.Structure):
@@ -100,6 +101,10 @@ SIGNATURES = {
     "sst_get_degree": (_i32, [_vp, _u32, ctypes.POINTER(_u32)]),
     "sst_neighbors": (_i32, [_vp, _u32, _vp, _u64, ctypes.POINTER(_u64)]),
     "sst_to_csr": (_i32, [_vp, _vp, _vp, _u32]),
+    "sst_insert_batch_weighted": (_i32, [_vp, _vp, _vp, _u64, _u32, ctypes.POINTER(_u64)]),
+    "sst_values_batch": (_i32, [_vp, _vp, _u64, _vp, _vp, _u32]),
+    "sst_to_csr_values": (_i32, [_vp, _vp, _vp, _vp, _u32]),
+    "sst_bf": (_i32, [_vp, _u32, _vp, _u32]),
     "sst_common_neighbors_batch": (_i32, [_vp, _vp, _u64, ctypes.c_int, _vp, _u32]),
     "sst_touch_all_sum": (_i32, [_vp, ctypes.POINTER(_u64)]),
     "sst_memory_size": (_i32, [_vp, ctypes.POINTER(_u64)]),
@@ -211,14 +216,14 @@ class SparseMatrixV:
                  hbm_budget_bytes: int = 0, initial_slots: int = 0,
                  upper_root: float = 0.0, lower_root: float = 0.0,
                  grow_fill: float = 0.0, keep_self_loops: bool = False,
-                 _handle=None):
+                 weighted: bool = False, _handle=None):
         self._h = None
         if _handle is not None:
             self._h = _handle
         else:
             cfg = sst_config(device, hbm_budget_bytes, initial_slots,
                              upper_root, lower_root, grow_fill,
-                             1 if keep_self_loops else 0)
+                             1 if keep_self_loops else 0, 1 if weighted else 0)
             h = ctypes.c_void_p()
             _check(lib().sst_graph_create(height, height if width is None else width,
                                           ctypes.byref(cfg), ctypes.byref(h)))
@@ -390,6 +395,44 @@ class SparseMatrixV:
                                 ctypes.c_void_p(cols.ctypes.data), HOST_PTR))
         return off, cols[:m]
 
+    def insert_batch_weighted(self, edges, values) -> int:
+        """Insert (row, col) pairs with one uint32 value each (weighted
+        graphs); a present edge takes the new value, the last of equal pairs
+        wins.  Returns the count of pairs out of range."""
+        e, n = _pairs(edges)
+        p, flags = _ptr(e)
+        if flags == DEVICE_PTR:
+            v = values.contiguous()
+        else:
+            v = np.ascontiguousarray(np.asarray(values).astype(np.uint32).reshape(-1))
+        assert (v.numel() if hasattr(v, "numel") else v.size) == n
+        pv, _ = _ptr(v)
+        bad = ctypes.c_uint64()
+        _check(lib().sst_insert_batch_weighted(self._h, p, pv, n, flags, ctypes.byref(bad)))
+        return bad.value
+
+    def values(self, edges):
+        """(values, found) of (row, col) pairs on a weighted graph (host)."""
+        e = np.ascontiguousarray(np.asarray(edges, np.uint32).reshape(-1, 2))
+        n = e.shape[0]
+        vals = np.empty(max(n, 1), np.uint32)
+        found = np.empty(max(n, 1), np.uint8)
+        _check(lib().sst_values_batch(self._h, ctypes.c_void_p(e.ctypes.data), n,
+                                      ctypes.c_void_p(vals.ctypes.data),
+                                      ctypes.c_void_p(found.ctypes.data), HOST_PTR))
+        return vals[:n], found[:n].astype(bool)
+
+    def csr_values(self):
+        """(offsets, cols, values) of a weighted graph (host)."""
+        m = self.M()
+        off = np.empty(self.rows + 1, np.uint64)
+        cols = np.empty(max(m, 1), np.uint32)
+        vals = np.empty(max(m, 1), np.uint32)
+        _check(lib().sst_to_csr_values(self._h, ctypes.c_void_p(off.ctypes.data),
+                                       ctypes.c_void_p(cols.ctypes.data),
+                                       ctypes.c_void_p(vals.ctypes.data), HOST_PTR))
+        return off, cols[:m], vals[:m]
+
     def common_neighbors(self, a: int, b: int, early_end: bool = False) -> int:
         return int(self.common_neighbors_batch(np.array([[a, b]], np.uint32), early_end)[0])
 
@@ -490,6 +533,15 @@ def PR_S(g: SparseMatrixV, iters: int = 10, damping: float = 0.85, out=None):
     buf = _out(g, np.float64, out)
     p, flags = _ptr(buf)
     _check(lib().sst_pagerank(g.handle, iters, damping, p, flags))
+    return buf
+
+
+def BF(g: SparseMatrixV, src: int, out=None):
+    """Shortest-path lengths from src over the edge values of a weighted
+    graph (int32, unreachable = 2^31-1), as the reference drivers' BF."""
+    buf = _out(g, np.int32, out)
+    p, flags = _ptr(buf)
+    _check(lib().sst_bf(g.handle, src, p, flags))
     return buf
 
 

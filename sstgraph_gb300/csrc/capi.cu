@@ -215,18 +215,21 @@ sst_status sst_sync(sst_graph *g) {
 }
 
 static sst_status do_update(sst_graph *g, const uint32_t *pairs, uint64_t n,
-                            uint32_t flags, uint64_t *n_invalid, bool insert) {
+                            uint32_t flags, uint64_t *n_invalid, bool insert,
+                            const uint32_t *values = nullptr) {
   CHECK_G(g);
   if (n && !pairs) {
     set_error_message("null pairs");
     return SST_EINVAL;
   }
-  sst_status st = is_dev(flags) ? SST_OK : io_begin(g, n * 8 + 256);
+  sst_status st = is_dev(flags) ? SST_OK : io_begin(g, n * 12 + 512);
   if (st != SST_OK) return st;
-  const uint32_t *d = nullptr;
+  const uint32_t *d = nullptr, *dv = nullptr;
   st = stage_in(g, pairs, 2 * n, flags, &d);
   if (st != SST_OK) return st;
-  st = sst::update_batch(g, d, n, insert, n_invalid);
+  if (values) st = stage_in(g, values, n, flags, &dv);
+  if (st != SST_OK) return st;
+  st = sst::update_batch(g, d, n, insert, n_invalid, dv);
   if (st == SST_OK && !is_dev(flags)) st = sst::sync_checked(g);
   return st;
 }
@@ -241,11 +244,58 @@ sst_status sst_remove_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
   return do_update(g, pairs, n, flags, n_invalid, false);
 }
 
+sst_status sst_insert_batch_weighted(sst_graph *g, const uint32_t *pairs,
+                                     const uint32_t *values, uint64_t n,
+                                     uint32_t flags, uint64_t *n_invalid) {
+  CHECK_G(g);
+  if (!g->weighted) {
+    set_error_message("the graph was not created weighted (sst_config.weighted)");
+    return SST_ESTATE;
+  }
+  if (n && !values) {
+    set_error_message("null values");
+    return SST_EINVAL;
+  }
+  return do_update(g, pairs, n, flags, n_invalid, true, values);
+}
+
+sst_status sst_values_batch(sst_graph *g, const uint32_t *pairs, uint64_t n,
+                            uint32_t *values, uint8_t *found, uint32_t flags) {
+  CHECK_G(g);
+  if (!g->weighted) {
+    set_error_message("the graph was not created weighted (sst_config.weighted)");
+    return SST_ESTATE;
+  }
+  if (n && (!pairs || !values)) {
+    set_error_message("null argument");
+    return SST_EINVAL;
+  }
+  sst_status st = is_dev(flags) ? SST_OK : io_begin(g, n * 13 + 1024);
+  if (st != SST_OK) return st;
+  const uint32_t *d = nullptr;
+  st = stage_in(g, pairs, 2 * n, flags, &d);
+  if (st != SST_OK) return st;
+  uint32_t *dval = nullptr;
+  uint8_t *dfound = nullptr;
+  st = stage_out(g, values, n, flags, &dval);
+  if (st == SST_OK && found) st = stage_out(g, found, n, flags, &dfound);
+  if (st != SST_OK) return st;
+  st = sst::has_batch(g, d, n, dfound, dval);
+  if (st != SST_OK) return st;
+  if (found) st = finish_out(g, found, dfound, n, flags);
+  if (st != SST_OK) return st;
+  return finish_out(g, values, dval, n, flags);
+}
+
 sst_status sst_update_batches(sst_graph *g, const uint32_t *pairs,
                               const uint64_t *offsets, const uint8_t *ops,
                               uint32_t nbatches, uint32_t flags,
                               uint64_t *n_invalid) {
   CHECK_G(g);
+  if (g->weighted) {
+    set_error_message("the batched form takes unweighted graphs only");
+    return SST_ESTATE;
+  }
   if (n_invalid) *n_invalid = 0;
   if (nbatches == 0) return SST_OK;
   if (!offsets || !ops) {
@@ -303,6 +353,10 @@ sst_status sst_remove(sst_graph *g, uint32_t row, uint32_t col) {
 sst_status sst_build_from_csr(sst_graph *g, const uint64_t *offsets,
                               const uint32_t *cols, uint32_t flags) {
   CHECK_G(g);
+  if (g->weighted) {
+    set_error_message("building from a CSR takes unweighted graphs only");
+    return SST_ESTATE;
+  }
   if (!offsets) {
     set_error_message("null offsets");
     return SST_EINVAL;
@@ -426,24 +480,42 @@ sst_status sst_neighbors(sst_graph *g, uint32_t v, uint32_t *out, uint64_t cap,
   return SST_OK;
 }
 
-sst_status sst_to_csr(sst_graph *g, uint64_t *offsets, uint32_t *cols,
-                      uint32_t flags) {
+static sst_status csr_out(sst_graph *g, uint64_t *offsets, uint32_t *cols,
+                          uint32_t *vals, uint32_t flags) {
   CHECK_G(g);
   if (!offsets || (g->m && !cols)) return SST_EINVAL;
-  if (is_dev(flags)) return sst::to_csr(g, offsets, cols);
+  if (is_dev(flags)) return sst::to_csr(g, offsets, cols, vals);
   uint64_t *doff = nullptr;
-  uint32_t *dcols = nullptr;
+  uint32_t *dcols = nullptr, *dvals = nullptr;
   SST_CUDA_TRY(cudaMalloc(&doff, ((uint64_t)g->n + 1) * 8));
   SST_CUDA_TRY(cudaMalloc(&dcols, std::max<uint64_t>(g->m, 1) * 4));
-  sst_status st = sst::to_csr(g, doff, dcols);
+  if (vals) SST_CUDA_TRY(cudaMalloc(&dvals, std::max<uint64_t>(g->m, 1) * 4));
+  sst_status st = sst::to_csr(g, doff, dcols, dvals);
   if (st == SST_OK) {
     cudaMemcpyAsync(offsets, doff, ((uint64_t)g->n + 1) * 8, cudaMemcpyDeviceToHost, g->stream);
     if (g->m) cudaMemcpyAsync(cols, dcols, g->m * 4, cudaMemcpyDeviceToHost, g->stream);
+    if (g->m && vals) cudaMemcpyAsync(vals, dvals, g->m * 4, cudaMemcpyDeviceToHost, g->stream);
     if (cudaStreamSynchronize(g->stream) != cudaSuccess) st = SST_EDEVICE;
   }
   cudaFree(doff);
   cudaFree(dcols);
+  if (dvals) cudaFree(dvals);
   return st;
+}
+
+sst_status sst_to_csr(sst_graph *g, uint64_t *offsets, uint32_t *cols,
+                      uint32_t flags) {
+  return csr_out(g, offsets, cols, nullptr, flags);
+}
+
+sst_status sst_to_csr_values(sst_graph *g, uint64_t *offsets, uint32_t *cols,
+                             uint32_t *values, uint32_t flags) {
+  if (g && !g->weighted) {
+    set_error_message("the graph was not created weighted (sst_config.weighted)");
+    return SST_ESTATE;
+  }
+  if (g && g->m && !values) return SST_EINVAL;
+  return csr_out(g, offsets, cols, values, flags);
 }
 
 sst_status sst_touch_all_sum(sst_graph *g, uint64_t *out) {
@@ -509,6 +581,10 @@ sst_status sst_degree_order_map(sst_graph *g, uint32_t *map, uint32_t flags) {
 sst_status sst_rewrite_graph(sst_graph *g, const uint32_t *map, uint32_t flags,
                              sst_graph **out) {
   CHECK_G(g);
+  if (g->weighted) {
+    set_error_message("relabelling takes unweighted graphs only");
+    return SST_ESTATE;
+  }
   if (!map || !out) return SST_EINVAL;
   *out = nullptr;
   if (g->n != g->width) {
@@ -641,6 +717,23 @@ sst_status sst_bc_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
   st = sst::bc_multi(g, hs.data(), k, d);
   if (st != SST_OK) return st;
   return finish_out(g, out, d, cnt, flags);
+}
+
+sst_status sst_bf(sst_graph *g, uint32_t src, int32_t *dist, uint32_t flags) {
+  CHECK_G(g);
+  if (!dist) return SST_EINVAL;
+  if (src >= g->n) {
+    set_error_message("source out of range");
+    return SST_EINVAL;
+  }
+  sst_status st = is_dev(flags) ? SST_OK : io_begin(g, (uint64_t)g->n * 4 + 256);
+  if (st != SST_OK) return st;
+  int32_t *d = nullptr;
+  st = stage_out(g, dist, g->n, flags, &d);
+  if (st != SST_OK) return st;
+  st = sst::bellman_ford(g, src, d);
+  if (st != SST_OK) return st;
+  return finish_out(g, dist, d, g->n, flags);
 }
 
 sst_status sst_autotune(sst_graph *g, sst_tuning *out) {

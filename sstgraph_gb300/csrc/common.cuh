@@ -38,6 +38,7 @@ struct DGraph {
   uint32_t *deg;
   uint32_t *slots;
   uint8_t *lcnt;
+  uint32_t *vals;  // per-slot edge values of a weighted graph, else null
 };
 
 // Density bounds of the device PMA (own choice, in the spirit of the

@@ -108,9 +108,14 @@ __device__ __forceinline__ uint32_t warp_sum_lcnt(const uint8_t *lc,
 __global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
                             uint32_t n, uint32_t width, int dbits,
                             bool drop_loops, uint64_t *__restrict__ keys,
-                            unsigned long long *__restrict__ invalid) {
+                            unsigned long long *__restrict__ invalid,
+                            const uint32_t *__restrict__ w,
+                            uint32_t *__restrict__ wv) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b) return;
+  // weighted graphs: the pair's value (1 when the call gives none) rides
+  // with the key through the sort
+  if (wv) wv[i] = w ? w[i] : 1u;
   uint32_t r = pairs[2 * i], c = pairs[2 * i + 1];
   const uint64_t sent = (uint64_t)n << dbits;
   bool ok = r < n && c < width && c != kEmpty;
@@ -118,15 +123,20 @@ __global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
   keys[i] = (!ok || (drop_loops && r == c)) ? sent : (((uint64_t)r << dbits) | c);
 }
 
+// Of a run of equal keys the last (in input order: the sort is stable) is
+// the one applied, so on a weighted graph the last value given wins, as
+// sequential inserts would leave it (PMA.hpp:1137-1145).  A weighted insert
+// of an edge already present overwrites its value here, in place.
 __global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
                          int dbits, DGraph g, bool insert,
                          uint32_t *__restrict__ flag,
-                         uint32_t *__restrict__ leaf_out) {
+                         uint32_t *__restrict__ leaf_out,
+                         const uint32_t *__restrict__ wv) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b) return;
   const uint64_t sent = (uint64_t)g.n << dbits;
   uint64_t k = keys[i];
-  if (k >= sent || (i > 0 && keys[i - 1] == k)) {
+  if (k >= sent || (i + 1 < b && keys[i + 1] == k)) {
     flag[i] = 0;
     leaf_out[i] = 0;
     return;
@@ -143,6 +153,8 @@ __global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
     const uint32_t *p = g.slots + base + ((uint64_t)l << kLeafLog);
     uint32_t pos = leaf_lower_bound(p, c, x);
     present = pos < c && p[pos] == x;
+    if (present && insert && wv && g.vals)
+      g.vals[base + ((uint64_t)l << kLeafLog) + pos] = wv[i];
   }
   flag[i] = insert ? !present : present;
   leaf_out[i] = l;
@@ -152,7 +164,8 @@ __global__ void k_pack(const uint64_t *__restrict__ keys,
                        const uint32_t *__restrict__ flag,
                        const uint32_t *__restrict__ pos,
                        const uint32_t *__restrict__ leaf, uint64_t b, int dbits,
-                       uint64_t *__restrict__ p_ul, uint32_t *__restrict__ p_x) {
+                       uint64_t *__restrict__ p_ul, uint32_t *__restrict__ p_x,
+                       const uint32_t *__restrict__ wv, uint32_t *__restrict__ p_w) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b || !flag[i]) return;
   uint64_t k = keys[i];
@@ -160,6 +173,7 @@ __global__ void k_pack(const uint64_t *__restrict__ keys,
   if (j >= b) return;  // positions come from a scan: never trust them blindly
   p_ul[j] = ((k >> dbits) << 32) | leaf[i];
   p_x[j] = (uint32_t)(k & ((1ull << dbits) - 1));
+  if (p_w) p_w[j] = wv[i];
 }
 
 __global__ void k_group_flags(const uint64_t *__restrict__ p_ul,
@@ -291,8 +305,10 @@ k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
       bool keep = (uint32_t)lane < c[q] && !del;
       uint32_t mask = __ballot_sync(0xffffffffu, keep);
       uint32_t pos = __popc(mask & ((1u << lane) - 1u));
+      const uint32_t av = (g.vals && (uint32_t)lane < c[q]) ? g.vals[S[q] + lane] : 0u;
       __syncwarp();
       if (keep) g.slots[S[q] + pos] = a;
+      if (keep && g.vals) g.vals[S[q] + pos] = av;
       if ((uint32_t)lane >= c[q] - k[q] && (uint32_t)lane < c[q]) g.slots[S[q] + lane] = kEmpty;
       if (lane == 0) {
         if (cap[q] > kLeaf)
@@ -494,6 +510,8 @@ struct Tasks {
   uint64_t *soff;    // exclusive prefix of nsrc
   uint64_t *doff;    // exclusive prefix of ndst
   unsigned long long *err;  // count of out-of-range staging ranks
+  uint32_t *stage_v;        // weighted graphs: values staged beside the ids
+  const uint32_t *p_w;      // weighted graphs: values of the packed items
 };
 
 // warp per task slot (all gmax slots, so the prefix scans see zeros beyond
@@ -569,7 +587,7 @@ k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul,
                              const uint32_t *__restrict__ p_x,
                              const uint32_t *__restrict__ g_start,
                              const uint32_t *__restrict__ merge_list,
-                             uint32_t nmerge) {
+                             uint32_t nmerge, const uint32_t *__restrict__ p_w) {
   const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   constexpr int Q = kGroupsPerWarp;
@@ -618,9 +636,14 @@ k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul,
       uint32_t below = __popc(__ballot_sync(0xffffffffu, (uint32_t)lane < c[q] && a < xj));
       if ((uint32_t)lane == j) px = j + below;
     }
+    // values move with their ids (weighted graphs)
+    const uint32_t av = (g.vals && (uint32_t)lane < c[q]) ? g.vals[S[q] + lane] : 0u;
+    const uint32_t xv = (g.vals && (uint32_t)lane < k[q]) ? (p_w ? p_w[j0[q] + lane] : 1u) : 0u;
     __syncwarp();
     if ((uint32_t)lane < c[q]) g.slots[S[q] + pa] = a;
     if ((uint32_t)lane < k[q]) g.slots[S[q] + px] = x[q];
+    if (g.vals && (uint32_t)lane < c[q]) g.vals[S[q] + pa] = av;
+    if (g.vals && (uint32_t)lane < k[q]) g.vals[S[q] + px] = xv;
     if (lane == 0 && cap[q] > kLeaf)
       g.lcnt[(base[q] >> kLeafLog) + (uint32_t)key[q]] = (uint8_t)(c[q] + k[q]);
   }
@@ -676,6 +699,8 @@ __global__ void k_gather_old(DGraph g, Tasks t, uint32_t ntasks,
     return;
   }
   stage[t.out[tau] + rank] = a;
+  if (t.stage_v)
+    t.stage_v[t.out[tau] + rank] = g.vals[base + ((uint64_t)l << kLeafLog) + lane];
 }
 
 // thread per packed item owned by a task: new elements to their merged rank
@@ -718,6 +743,7 @@ __global__ void k_gather_new(DGraph g, Tasks t, uint32_t ntasks,
     return;
   }
   stage[t.out[tau] + rank] = x;
+  if (t.stage_v) t.stage_v[t.out[tau] + rank] = t.p_w ? t.p_w[j] : 1u;
 }
 
 __device__ __forceinline__ uint64_t task_new_base(const Tasks &t, uint64_t tau,
@@ -763,6 +789,7 @@ __global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
   multi = __shfl_sync(0xffffffffu, multi, 0);
   if ((uint32_t)lane < leafsize)
     g.slots[S + lane] = (uint32_t)lane < cnt ? stage[src + lane] : kEmpty;
+  if (g.vals && (uint32_t)lane < cnt) g.vals[S + lane] = t.stage_v[src + lane];
   if (lane == 0 && multi) g.lcnt[S >> kLeafLog] = (uint8_t)cnt;
 }
 
@@ -814,7 +841,9 @@ __global__ void k_repack_copy(const uint32_t *__restrict__ cap, uint32_t n,
                               const uint32_t *__restrict__ oslots,
                               const uint8_t *__restrict__ olcnt,
                               uint32_t *__restrict__ nslots_,
-                              uint8_t *__restrict__ nlcnt) {
+                              uint8_t *__restrict__ nlcnt,
+                              const uint32_t *__restrict__ ovals,
+                              uint32_t *__restrict__ nvals) {
   uint64_t v = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (v >= n) return;
@@ -822,6 +851,8 @@ __global__ void k_repack_copy(const uint32_t *__restrict__ cap, uint32_t n,
   if (c == 0) return;
   uint64_t ob = oldbase[v], nb = newbase[v];
   for (uint64_t i = lane; i < c; i += 32) nslots_[nb + i] = oslots[ob + i];
+  if (ovals)
+    for (uint64_t i = lane; i < c; i += 32) nvals[nb + i] = ovals[ob + i];
   if (c > kLeaf)
     for (uint64_t l = lane; l < (c >> kLeafLog); l += 32)
       nlcnt[(nb >> kLeafLog) + l] = olcnt[(ob >> kLeafLog) + l];
@@ -877,7 +908,7 @@ void *pinned(sst_graph *g, size_t bytes) {
 }
 
 uint64_t graph_device_bytes(const sst_graph *g) {
-  return (uint64_t)g->n * 16 + g->nslots * 4 + g->nslots / kLeaf +
+  return (uint64_t)g->n * 16 + g->nslots * (g->weighted ? 8 : 4) + g->nslots / kLeaf +
          g->arena.cap + g->work.cap +
          g->dir.cap * (4 + 8 + 4 + 8) + (uint64_t)(g->n + 1) * 8;
 }
@@ -893,7 +924,7 @@ static sst_status budget_check(sst_graph *g, uint64_t extra) {
 }
 
 static sst_status alloc_slab(sst_graph *g, uint64_t nslots, uint32_t **slots,
-                             uint8_t **lcnt) {
+                             uint8_t **lcnt, uint32_t **vals) {
   if (cudaMalloc(slots, nslots * 4) != cudaSuccess) {
     cudaGetLastError();
     set_error_message("cannot allocate a slab of %llu slots",
@@ -904,6 +935,15 @@ static sst_status alloc_slab(sst_graph *g, uint64_t nslots, uint32_t **slots,
     cudaGetLastError();
     cudaFree(*slots);
     set_error_message("cannot allocate leaf counts");
+    return SST_ENOMEM;
+  }
+  *vals = nullptr;
+  if (g->weighted && cudaMalloc(vals, nslots * 4) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(*slots);
+    cudaFree(*lcnt);
+    set_error_message("cannot allocate a value slab of %llu slots",
+                      (unsigned long long)nslots);
     return SST_ENOMEM;
   }
   return SST_OK;
@@ -922,6 +962,7 @@ sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
     if (cfg->lower_root > 0) g->params.lower_root = cfg->lower_root;
     if (cfg->grow_fill > 0) g->params.grow_fill = cfg->grow_fill;
     g->keep_loops = cfg->keep_self_loops != 0;
+    g->weighted = cfg->weighted != 0;
   }
   SST_CUDA_TRY(cudaSetDevice(g->device));
   SST_CUDA_TRY(cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, g->device));
@@ -938,7 +979,7 @@ sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
   slots = (slots + kLeaf - 1) & ~uint64_t(kLeaf - 1);
   sst_status st = budget_check(g, slots * 4 + slots / kLeaf);
   if (st != SST_OK) return st;
-  st = alloc_slab(g, slots, &g->d_slots, &g->d_lcnt);
+  st = alloc_slab(g, slots, &g->d_slots, &g->d_lcnt, &g->d_vals);
   if (st != SST_OK) return st;
   g->nslots = slots;
   g->bump = 0;
@@ -957,6 +998,7 @@ void graph_release(sst_graph *g) {
   cudaFree(g->d_cap);
   cudaFree(g->d_deg);
   cudaFree(g->d_slots);
+  cudaFree(g->d_vals);
   cudaFree(g->d_lcnt);
   cudaFree(g->d_plan);
   cudaFree(g->d_err);
@@ -980,6 +1022,7 @@ sst_status graph_clone(const sst_graph *src, sst_graph *dst) {
   cfg.lower_root = src->params.lower_root;
   cfg.grow_fill = src->params.grow_fill;
   cfg.keep_self_loops = src->keep_loops ? 1u : 0u;
+  cfg.weighted = src->weighted ? 1u : 0u;
   sst_status st = graph_init(dst, src->n, src->width, &cfg);
   if (st != SST_OK) return st;
   SST_CUDA_TRY(cudaStreamSynchronize(src->stream));
@@ -988,6 +1031,8 @@ sst_status graph_clone(const sst_graph *src, sst_graph *dst) {
   SST_CUDA_TRY(cudaMemcpyAsync(dst->d_cap, src->d_cap, n * 4, cudaMemcpyDeviceToDevice, dst->stream));
   SST_CUDA_TRY(cudaMemcpyAsync(dst->d_deg, src->d_deg, n * 4, cudaMemcpyDeviceToDevice, dst->stream));
   SST_CUDA_TRY(cudaMemcpyAsync(dst->d_slots, src->d_slots, src->bump * 4, cudaMemcpyDeviceToDevice, dst->stream));
+  if (src->d_vals)
+    SST_CUDA_TRY(cudaMemcpyAsync(dst->d_vals, src->d_vals, src->bump * 4, cudaMemcpyDeviceToDevice, dst->stream));
   SST_CUDA_TRY(cudaMemcpyAsync(dst->d_lcnt, src->d_lcnt, src->bump / kLeaf + 1, cudaMemcpyDeviceToDevice, dst->stream));
   SST_CUDA_TRY(cudaStreamSynchronize(dst->stream));
   dst->bump = src->bump;
@@ -1030,9 +1075,9 @@ sst_status repack(sst_graph *g, uint64_t extra) {
     cudaFree(tmp);
     return st;
   }
-  uint32_t *nslots_;
+  uint32_t *nslots_, *nvals;
   uint8_t *nlcnt;
-  st = alloc_slab(g, nsl, &nslots_, &nlcnt);
+  st = alloc_slab(g, nsl, &nslots_, &nlcnt, &nvals);
   if (st != SST_OK) {
     cudaFree(tmp);
     return st;
@@ -1042,15 +1087,17 @@ sst_status repack(sst_graph *g, uint64_t extra) {
     SST_LAUNCH(k_repack_assign, blocks_for(n), kTB, 0, s, g->d_cap, n, cstart,
                cnt + kNumClasses, newbase);
     SST_LAUNCH(k_repack_copy, warp_blocks(n), kTB, 0, s, g->d_cap, n, g->d_base,
-               newbase, g->d_slots, g->d_lcnt, nslots_, nlcnt);
+               newbase, g->d_slots, g->d_lcnt, nslots_, nlcnt, g->d_vals, nvals);
     SST_CUDA_TRY(cudaMemcpyAsync(g->d_base, newbase, (uint64_t)n * 8, cudaMemcpyDeviceToDevice, s));
   }
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   SST_CUDA_TRY(cudaGetLastError());
   cudaFree(g->d_slots);
   cudaFree(g->d_lcnt);
+  cudaFree(g->d_vals);
   g->d_slots = nslots_;
   g->d_lcnt = nlcnt;
+  g->d_vals = nvals;
   g->nslots = nsl;
   g->bump = live;
   cudaFree(tmp);
@@ -1060,7 +1107,7 @@ sst_status repack(sst_graph *g, uint64_t extra) {
 // bytes of arena scratch an update batch of b pairs takes
 static size_t update_scratch_bytes(uint64_t b) {
   size_t per = 8 * 2 + 4 * 4 + 8 + 4 + 4 * 3 + 1 * 2 + 4 * 2 + 8 * 4 + 4 * 6 +
-               8 * 8 + 4 * 4 + 1 + 64;
+               8 * 8 + 4 * 4 + 1 + 64 + 4 * 3 /* values */;
   return b * per + radix_sort_scratch_bytes(b) + 8 * scan_scratch_bytes(b, 8) +
          (1 << 16);
 }
@@ -1070,16 +1117,19 @@ static size_t update_scratch_bytes(uint64_t b) {
 // ascending and duplicate-free, in memory outside the arena) is given.
 static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                                const uint64_t *presorted, uint64_t b,
-                               bool insert, uint64_t *n_invalid);
+                               bool insert, uint64_t *n_invalid,
+                               const uint32_t *d_w);
 
 sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t b,
-                        bool insert, uint64_t *n_invalid) {
-  return run_pipeline(g, d_pairs, nullptr, b, insert, n_invalid);
+                        bool insert, uint64_t *n_invalid, const uint32_t *d_w) {
+  return run_pipeline(g, d_pairs, nullptr, b, insert, n_invalid, d_w);
 }
 
+// d_w: the pairs' values on a weighted graph (null: value 1)
 static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                                const uint64_t *presorted, uint64_t b,
-                               bool insert, uint64_t *n_invalid) {
+                               bool insert, uint64_t *n_invalid,
+                               const uint32_t *d_w) {
   if (n_invalid) *n_invalid = 0;
   if (b == 0) return SST_OK;
   if (b > 0xFFFFFFF0ull) {
@@ -1130,6 +1180,14 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   T.soff = A.take<uint64_t>(b);
   T.doff = A.take<uint64_t>(b);
   T.err = g->d_err;
+  // weighted graphs: values beside the keys (sorted with them) and the packed
+  // items
+  const bool wt = g->weighted && insert && !presorted;
+  uint32_t *wv = wt ? A.take<uint32_t>(b) : nullptr;
+  uint32_t *wtmp = wt ? A.take<uint32_t>(b) : nullptr;
+  uint32_t *p_w = wt ? A.take<uint32_t>(b) : nullptr;
+  T.stage_v = nullptr;  // set with the staging below
+  T.p_w = p_w;
   uint64_t *cstart = A.take<uint64_t>(kNumClasses);
   if (!cstart) {
     set_error_message("update scratch sizing error");
@@ -1142,19 +1200,26 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     // pair in (8 B), key out (8 B)
     SST_LAUNCH_B(16 * b, k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n, g->width,
                dbits, insert && !g->keep_loops, keys,
-               reinterpret_cast<unsigned long long *>(&P->invalid));
+               reinterpret_cast<unsigned long long *>(&P->invalid), d_w, wv);
     uint64_t *out = keys;
-    SST_CUDA_TRY(radix_sort_u64(keys, ktmp, b, g->rbits + dbits, A, s, &out));
+    if (wt) {
+      uint32_t *wout = wv;
+      SST_CUDA_TRY(radix_sort_kv(keys, ktmp, wv, wtmp, b, g->rbits + dbits, A, s,
+                                 &out, &wout));
+      wv = wout;
+    } else {
+      SST_CUDA_TRY(radix_sort_u64(keys, ktmp, b, g->rbits + dbits, A, s, &out));
+    }
     sorted = out;
   }
   // 3-5: locate, pack, group
   // sorted key in (8 B), flag and leaf out (8 B)
   SST_LAUNCH_B(16 * b, k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg,
-               insert, flag, leaf);
+               insert, flag, leaf, wt ? wv : nullptr);
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(flag, pos, b, 0u, OpAdd{}, true, false,
                                       &P->n_items, A, s)));
   SST_LAUNCH(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,
-             p_ul, p_x);
+             p_ul, p_x, wv, p_w);
   SST_LAUNCH(k_group_flags, blocks_for(b), kTB, 0, s, p_ul, &P->n_items, b, gflag);
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(gflag, gpos, b, 0u, OpAdd{}, true, false,
                                       &P->n_groups, A, s)));
@@ -1238,7 +1303,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   SST_CUDA_TRY(cudaMemcpyAsync(cstart, hs, sizeof(hstart), cudaMemcpyHostToDevice, s));
 
   // staging for window / resize tasks
-  size_t wneed = ps.task_elems * 4 + ps.src_leaves * 16 + scan_scratch_bytes(ps.src_leaves, 8) + 4096;
+  size_t wneed = ps.task_elems * (g->weighted ? 8 : 4) + ps.src_leaves * 16 +
+                 scan_scratch_bytes(ps.src_leaves, 8) + 4096;
   if (wneed > g->work.cap) {
     sst_status st = budget_check(g, wneed - g->work.cap);
     if (st != SST_OK) return st;
@@ -1246,6 +1312,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   SST_CUDA_TRY(g->work.reserve(wneed));
   g->work.reset();
   uint32_t *stage = g->work.take<uint32_t>(ps.task_elems);
+  if (g->weighted) T.stage_v = g->work.take<uint32_t>(ps.task_elems);
   uint64_t *scnt = g->work.take<uint64_t>(ps.src_leaves);
   uint64_t *spre = g->work.take<uint64_t>(ps.src_leaves);
 
@@ -1256,7 +1323,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     SST_LAUNCH_B(258ull * ps.n_merge, k_leaf_merge,
                warp_blocks((ps.n_merge + kGroupsPerWarp - 1) / kGroupsPerWarp),
                kTB, 0, s, dg, p_ul, p_x,
-               g_start, merge_list, ps.n_merge);
+               g_start, merge_list, ps.n_merge, p_w);
   if (ps.n_tasks) {
     if (ps.src_leaves) {
       SST_LAUNCH(k_src_counts, blocks_for(ps.src_leaves), kTB, 0, s, dg, T,
@@ -1398,8 +1465,8 @@ sst_status update_batches(sst_graph *g, const uint32_t *d_pairs,
   SST_CUDA_TRY(cudaMallocAsync(&net, (n_ins + n_del) * 8, s));
   SST_LAUNCH(k_compact_keys, blocks_for(N), kTB, 0, s, sk, fins, pins, N, net);
   SST_LAUNCH(k_compact_keys, blocks_for(N), kTB, 0, s, sk, fdel, pdel, N, net + n_ins);
-  sst_status st = run_pipeline(g, nullptr, net + n_ins, n_del, false, nullptr);
-  if (st == SST_OK) st = run_pipeline(g, nullptr, net, n_ins, true, nullptr);
+  sst_status st = run_pipeline(g, nullptr, net + n_ins, n_del, false, nullptr, nullptr);
+  if (st == SST_OK) st = run_pipeline(g, nullptr, net, n_ins, true, nullptr, nullptr);
   cudaFreeAsync(net, s);
   return st;
 }
@@ -1502,24 +1569,29 @@ __global__ void k_csr_to_pairs(const uint64_t *__restrict__ off,
   }
 }
 
+// membership of each pair; with vals (weighted graphs) also the edge's
+// value (0 where absent)
 __global__ void k_has(DGraph g, const uint32_t *__restrict__ pairs, uint64_t n,
-                      uint8_t *__restrict__ out) {
+                      uint8_t *__restrict__ out, uint32_t *__restrict__ vals) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t u = pairs[2 * i], x = pairs[2 * i + 1];
   uint8_t r = 0;
+  uint32_t v = 0;
   if (u < g.n) {
     uint64_t base = g.base[u];
     uint32_t cap = g.cap[u];
     if (cap) {
       uint32_t l = find_leaf(g.slots, base, cap, x);
       uint32_t c = leaf_count(g, base, cap, g.deg[u], l);
-      const uint32_t *p = g.slots + base + ((uint64_t)l << kLeafLog);
-      uint32_t pos = leaf_lower_bound(p, c, x);
-      r = pos < c && p[pos] == x;
+      const uint64_t S = base + ((uint64_t)l << kLeafLog);
+      uint32_t pos = leaf_lower_bound(g.slots + S, c, x);
+      r = pos < c && g.slots[S + pos] == x;
+      if (r && vals) v = g.vals[S + pos];
     }
   }
-  out[i] = r;
+  if (out) out[i] = r;
+  if (vals) vals[i] = v;
 }
 
 __global__ void k_vertex_leaves(const uint32_t *__restrict__ cap, uint32_t n,
@@ -1622,9 +1694,10 @@ sst_status build_from_csr(sst_graph *g, const uint64_t *d_off,
 }
 
 sst_status has_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,
-                     uint8_t *d_out) {
+                     uint8_t *d_out, uint32_t *d_vals) {
   if (n == 0) return SST_OK;
-  SST_LAUNCH(k_has, blocks_for(n), kTB, 0, g->stream, g->view(), d_pairs, n, d_out);
+  SST_LAUNCH(k_has, blocks_for(n), kTB, 0, g->stream, g->view(), d_pairs, n, d_out,
+             d_vals);
   SST_CUDA_TRY(cudaGetLastError());
   return SST_OK;
 }
@@ -1679,7 +1752,8 @@ sst_status ensure_leaf_dir(sst_graph *g) {
   return SST_OK;
 }
 
-sst_status to_csr(sst_graph *g, uint64_t *d_off, uint32_t *d_cols) {
+sst_status to_csr(sst_graph *g, uint64_t *d_off, uint32_t *d_cols,
+                  uint32_t *d_vals) {
   sst_status st = ensure_leaf_dir(g);
   if (st != SST_OK) return st;
   cudaStream_t s = g->stream;
@@ -1695,6 +1769,9 @@ sst_status to_csr(sst_graph *g, uint64_t *d_off, uint32_t *d_cols) {
   if (D.nleaves)
     SST_LAUNCH(k_dir_copy, warp_blocks(D.nleaves), kTB, 0, s, g->d_slots, D.slot,
                D.cnt, D.pre, D.nleaves, d_cols);
+  if (D.nleaves && d_vals && g->d_vals)  // values in the same CSR order
+    SST_LAUNCH(k_dir_copy, warp_blocks(D.nleaves), kTB, 0, s, g->d_vals, D.slot,
+               D.cnt, D.pre, D.nleaves, d_vals);
   SST_CUDA_TRY(cudaGetLastError());
   return SST_OK;
 }

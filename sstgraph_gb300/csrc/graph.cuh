@@ -61,6 +61,8 @@ struct sst_graph {
   uint32_t *d_deg = nullptr;
   uint32_t *d_slots = nullptr;
   uint8_t *d_lcnt = nullptr;
+  uint32_t *d_vals = nullptr;  // weighted graphs: one value per slot
+  bool weighted = false;
   uint64_t nslots = 0;
   uint64_t bump = 0;
   uint64_t m = 0;
@@ -78,7 +80,7 @@ struct sst_graph {
   size_t h_pinned_cap = 0;
 
   sst::DGraph view() const {
-    return sst::DGraph{n, width, d_base, d_cap, d_deg, d_slots, d_lcnt};
+    return sst::DGraph{n, width, d_base, d_cap, d_deg, d_slots, d_lcnt, d_vals};
   }
 };
 
@@ -91,8 +93,10 @@ sst_status graph_clone(const sst_graph *src, sst_graph *dst);
 uint64_t graph_device_bytes(const sst_graph *g);
 
 // pairs are device pointers here; the C ABI stages host buffers
+// d_w: per-pair values for a weighted graph (null: value 1)
 sst_status update_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,
-                        bool insert, uint64_t *n_invalid);
+                        bool insert, uint64_t *n_invalid,
+                        const uint32_t *d_w = nullptr);
 // nb batches: pairs[boff[i]..boff[i+1]) with ops[i] (1 insert, 0 remove),
 // applied as if in order; N = boff[nb]
 sst_status update_batches(sst_graph *g, const uint32_t *d_pairs,
@@ -102,10 +106,12 @@ sst_status degree_order_map(sst_graph *g, uint32_t *d_map);
 sst_status rewrite_graph(sst_graph *g, const uint32_t *d_map, sst_graph *out);
 sst_status build_from_csr(sst_graph *g, const uint64_t *d_off,
                           const uint32_t *d_cols);
+// d_out (membership) and d_vals (values, weighted graphs) may each be null
 sst_status has_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,
-                     uint8_t *d_out);
+                     uint8_t *d_out, uint32_t *d_vals = nullptr);
 sst_status ensure_leaf_dir(sst_graph *g);
-sst_status to_csr(sst_graph *g, uint64_t *d_off, uint32_t *d_cols);
+sst_status to_csr(sst_graph *g, uint64_t *d_off, uint32_t *d_cols,
+                  uint32_t *d_vals = nullptr);
 sst_status neighbors(sst_graph *g, uint32_t v, uint32_t *d_out, uint64_t cap,
                      uint64_t *deg);
 sst_status sample_edges(sst_graph *g, uint64_t seed, uint64_t first,

@@ -41,12 +41,15 @@ sst_status graph_copy_into(sst_graph *dst, sst_graph *src) {
     cudaStreamSynchronize(dst->stream);
     cudaFree(dst->d_slots);
     cudaFree(dst->d_lcnt);
+    cudaFree(dst->d_vals);
     dst->d_slots = nullptr;
     dst->d_lcnt = nullptr;
+    dst->d_vals = nullptr;
     uint64_t want = std::max(used + used / 4, src->nslots);
     want = (want + kLeaf - 1) & ~uint64_t(kLeaf - 1);
     SST_CUDA_TRY(cudaMalloc(&dst->d_slots, want * 4));
     SST_CUDA_TRY(cudaMalloc(&dst->d_lcnt, want / kLeaf + 1));
+    if (dst->weighted) SST_CUDA_TRY(cudaMalloc(&dst->d_vals, want * 4));
     dst->nslots = want;
   }
   uint64_t n = std::max<uint64_t>(src->n, 1);
@@ -57,6 +60,8 @@ sst_status graph_copy_into(sst_graph *dst, sst_graph *src) {
   if (used) {
     SST_CUDA_TRY(cudaMemcpyAsync(dst->d_slots, src->d_slots, used * 4, cudaMemcpyDeviceToDevice, s));
     SST_CUDA_TRY(cudaMemcpyAsync(dst->d_lcnt, src->d_lcnt, used / kLeaf, cudaMemcpyDeviceToDevice, s));
+    if (src->d_vals)
+      SST_CUDA_TRY(cudaMemcpyAsync(dst->d_vals, src->d_vals, used * 4, cudaMemcpyDeviceToDevice, s));
   }
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   dst->bump = src->bump;
@@ -365,7 +370,8 @@ sst_status sst_server_create(sst_graph *g, const sst_server_config *cfg,
   // snapshot -- vertex table, slab and leaf counts, no update scratch -- and
   // its traversal buffers (~40 B per vertex)
   uint64_t graph_bytes = sst::graph_device_bytes(g);
-  uint64_t per_slot = (uint64_t)g->n * 16 + g->nslots * 4 + g->nslots / sst::kLeaf +
+  uint64_t per_slot = (uint64_t)g->n * 16 + g->nslots * (g->weighted ? 8 : 4) +
+                      g->nslots / sst::kLeaf +
                       (uint64_t)g->n * 40;
   if (s->cfg.hbm_budget_bytes) {
     uint64_t room = s->cfg.hbm_budget_bytes > graph_bytes ? s->cfg.hbm_budget_bytes - graph_bytes : 0;

@@ -2170,4 +2170,126 @@ sst_status autotune(sst_graph *g, sst_tuning *out) {
   return SST_OK;
 }
 
+
+// ------------------------------------------------------------- bellman-ford
+// Single-source shortest paths over a weighted graph (edge values as
+// lengths): the reference drivers' BF(g, src) (internal/test.hpp:611-634;
+// the algorithm library itself is absent).  Rounds of push relaxation from
+// the vertices whose distance dropped in the previous round: a warp per
+// frontier chunk (lane = slot) lowers dist[v] to dist[u] + w(u, v) by
+// atomicMin on 64-bit distances, and the first thread to stamp v with the
+// round enqueues it.  Lengths are unsigned, so no round count exceeds n.
+namespace {
+constexpr unsigned long long kInfDist = ~0ull;
+
+__global__ void k_bf_init(unsigned long long *__restrict__ dist,
+                          uint32_t *__restrict__ stamp, uint32_t n, uint32_t src) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  dist[v] = v == src ? 0ull : kInfDist;
+  stamp[v] = 0;
+}
+
+__global__ void k_bf_push(DGraph g, const uint32_t *__restrict__ iv,
+                          const uint32_t *__restrict__ il0, uint32_t nitems,
+                          unsigned long long *__restrict__ dist,
+                          uint32_t *__restrict__ stamp, uint32_t round,
+                          uint32_t *__restrict__ nq,
+                          unsigned long long *__restrict__ cnt) {
+  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= nitems) return;
+  const uint32_t u = iv[i];
+  const unsigned long long du = __ldcg(dist + u);
+  const uint64_t base = g.base[u];
+  const uint32_t cap = g.cap[u], deg = g.deg[u];
+  const uint32_t nl = cap ? nleaves_of(cap) : 0;
+  const uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+  for (uint32_t l = l0; l < l1; l++) {
+    const uint32_t c = leaf_count(g, base, cap, deg, l);
+    bool mine = false;
+    uint32_t v = 0, vd = 0, vi = 0;
+    if ((uint32_t)lane < c) {
+      const uint64_t at = base + ((uint64_t)l << kLeafLog) + lane;
+      v = g.slots[at];
+      const unsigned long long nd = du + g.vals[at];
+      if (nd < __ldcg(dist + v) && atomicMin(dist + v, nd) > nd &&
+          atomicExch(stamp + v, round) != round) {
+        mine = true;
+        vd = g.deg[v];
+        vi = items_of(g.cap[v]);
+      }
+    }
+    enqueue(mine, v, vd, vi, nq, cnt);
+  }
+}
+
+__global__ void k_bf_out(const unsigned long long *__restrict__ dist, uint32_t n,
+                         int32_t *__restrict__ out) {
+  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const unsigned long long d = dist[v];
+  out[v] = d >= 0x7FFFFFFFull ? 0x7FFFFFFF : (int32_t)d;
+}
+}  // namespace
+
+static uint64_t items_of_host(uint32_t cap) {
+  return cap > kLeaf ? ((cap >> kLeafLog) + kChunkLeaves - 1) / kChunkLeaves : 1;
+}
+
+sst_status bellman_ford(sst_graph *g, uint32_t src, int32_t *d_out) {
+  if (!g->weighted || !g->d_vals) {
+    set_error_message("Bellman-Ford needs a weighted graph (sst_config.weighted)");
+    return SST_ESTATE;
+  }
+  TravState *t = state(g);
+  cudaStream_t s = g->stream;
+  const uint32_t n = g->n;
+  if (n == 0) return SST_OK;
+  SST_CUDA_TRY(t->msrc.ensure(n));  // 64-bit distances
+  SST_CUDA_TRY(t->qa.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->qb.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->fbits.ensure((uint64_t)n + 1));  // round stamps
+  SST_CUDA_TRY(t->icnt.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->ioff.ensure((uint64_t)n + 1));
+  unsigned long long *dist = t->msrc.p;
+  uint32_t *stamp = t->fbits.p;
+  SST_LAUNCH(k_bf_init, blocks_for(n), kTB, 0, s, dist, stamp, n, src);
+  SST_CUDA_TRY(cudaMemcpyAsync(t->qa.p, &src, 4, cudaMemcpyHostToDevice, s));
+  uint32_t scap = 0;
+  SST_CUDA_TRY(cudaMemcpyAsync(&scap, g->d_cap + src, 4, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t qn = 1, qitems = items_of_host(scap);
+  uint32_t *q = t->qa.p, *nq = t->qb.p;
+  unsigned long long *cnt = t->d_small;
+  DGraph dg = g->view();
+  for (uint32_t round = 1; qn > 0; round++) {
+    if (round > n + 1) {
+      set_error_message("Bellman-Ford did not settle in n rounds");
+      return SST_ETIMEDOUT;
+    }
+    SST_CUDA_TRY(t->iv.ensure(qitems + 1));
+    SST_CUDA_TRY(t->il0.ensure(qitems + 1));
+    SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, 24, s));
+    SST_LAUNCH(k_front_items, blocks_for(qn), kTB, 0, s, q, (uint32_t)qn,
+               g->d_cap, t->icnt.p);
+    g->arena.reset();
+    SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes(qn, 4) + 4096));
+    SST_CUDA_TRY((scan<uint32_t, OpAdd>(t->icnt.p, t->ioff.p, qn, 0u, OpAdd{},
+                                        true, false, nullptr, g->arena, s)));
+    SST_LAUNCH(k_front_expand, blocks_for(qn), kTB, 0, s, q, (uint32_t)qn,
+               g->d_cap, t->ioff.p, t->iv.p, t->il0.p);
+    SST_LAUNCH(k_bf_push, warp_blocks(qitems), kTB, 0, s, dg, t->iv.p, t->il0.p,
+               (uint32_t)qitems, dist, stamp, round, nq, cnt);
+    SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, cnt, 24, cudaMemcpyDeviceToHost, s));
+    SST_CUDA_TRY(cudaStreamSynchronize(s));
+    qn = t->h_small[0];
+    qitems = t->h_small[2];
+    std::swap(q, nq);
+  }
+  SST_LAUNCH(k_bf_out, blocks_for(n), kTB, 0, s, dist, n, d_out);
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
 }  // namespace sst

@@ -21,6 +21,9 @@ sst_status bfs_multi(sst_graph *g, const uint32_t *h_srcs, uint32_t k,
 sst_status bc_multi(sst_graph *g, const uint32_t *h_srcs, uint32_t k,
                     double *d_dep);
 sst_status tc(sst_graph *g, uint64_t *total, uint64_t *d_per_vertex);
+// shortest-path lengths from src over edge values (weighted graphs);
+// unreachable and lengths >= 2^31-1 read INT32_MAX
+sst_status bellman_ford(sst_graph *g, uint32_t src, int32_t *d_out);
 sst_status get_tuning(sst_graph *g, sst_tuning *out);
 sst_status set_tuning(sst_graph *g, const sst_tuning *in);
 sst_status autotune(sst_graph *g, sst_tuning *out);
