@@ -9,7 +9,9 @@
 //    reference sorts it in place, SparseMatrix.hpp:578,664);
 //  - map_neighbors / map_range call host functors on copied-out neighbour
 //    lists (same order and early-exit rules, SparseMatrix.hpp:179-315);
-//  - only the binary CSR form (SparseMatrixV<true>) exists.
+//  - the binary CSR form (SparseMatrixV<true>) and the uint32-weighted one
+//    (SparseMatrixV<true, uint32_t>, test.hpp:699-846) exist; on the
+//    weighted form the batched update, relabel and CSR build are refused.
 #pragma once
 
 #include <cstdint>
@@ -39,18 +41,36 @@ inline void check(sst_status s) {
   if (s != SST_OK) throw sst_error(s, sst_last_error_message());
 }
 
-template <bool is_csr_ = true> class SparseMatrixV {
+template <bool is_csr_ = true, typename... Ts> class SparseMatrixV {
   static_assert(is_csr_, "the device graph is stored by rows (CSR) only");
+  static constexpr bool weighted = sizeof...(Ts) == 1;
+  static_assert(sizeof...(Ts) == 0 ||
+                    (weighted && std::is_same_v<std::tuple<Ts...>, std::tuple<uint32_t>>),
+                "edge values are uint32_t (or none)");
+  using edge_t = std::tuple<el_t, el_t, Ts...>;
   sst_graph *g_ = nullptr;
 
-  static std::vector<uint32_t> flatten(const std::tuple<el_t, el_t> *edges,
-                                       uint64_t n) {
+  static std::vector<uint32_t> flatten(const edge_t *edges, uint64_t n) {
     std::vector<uint32_t> p(2 * n);
     for (uint64_t i = 0; i < n; i++) {
       p[2 * i] = std::get<0>(edges[i]);
       p[2 * i + 1] = std::get<1>(edges[i]);
     }
     return p;
+  }
+  static std::vector<uint32_t> values_of(const edge_t *edges, uint64_t n) {
+    std::vector<uint32_t> v(n);
+    if constexpr (weighted)
+      for (uint64_t i = 0; i < n; i++) v[i] = std::get<2>(edges[i]);
+    return v;
+  }
+  static const sst_config *config() {
+    static sst_config cfg = [] {
+      sst_config c{};
+      c.weighted = weighted ? 1u : 0u;
+      return c;
+    }();
+    return &cfg;
   }
 
   std::vector<uint32_t> neighbours(uint64_t i) const {
@@ -63,7 +83,7 @@ template <bool is_csr_ = true> class SparseMatrixV {
 
  public:
   SparseMatrixV(el_t height, el_t width, const sst_config *cfg = nullptr) {
-    check(sst_graph_create(height, width, cfg, &g_));
+    check(sst_graph_create(height, width, cfg ? cfg : config(), &g_));
   }
   explicit SparseMatrixV(sst_graph *adopt) : g_(adopt) {}
   SparseMatrixV(const SparseMatrixV &o) { check(sst_graph_clone(o.g_, &g_)); }
@@ -126,19 +146,32 @@ template <bool is_csr_ = true> class SparseMatrixV {
     check(sst_has(g_, row, col, &r));
     return r != 0;
   }
-  bool value(el_t row, el_t col) const { return has(row, col); }
+  // binary: membership; weighted: the edge's value (0 where absent)
+  auto value(el_t row, el_t col) const {
+    if constexpr (weighted) {
+      uint32_t p[2] = {row, col}, v = 0;
+      check(sst_values_batch(g_, p, 1, &v, nullptr, 0u));
+      return v;
+    } else {
+      return has(row, col);
+    }
+  }
   void insert(el_t row, el_t col) { check(sst_insert(g_, row, col)); }
   void insert(std::tuple<el_t, el_t> e) { insert(std::get<0>(e), std::get<1>(e)); }
   void remove(el_t row, el_t col) { check(sst_remove(g_, row, col)); }
 
-  void insert_batch(std::tuple<el_t, el_t> *edges, uint64_t n,
-                    bool semi_sorted = false) {
+  void insert_batch(edge_t *edges, uint64_t n, bool semi_sorted = false) {
     std::vector<uint32_t> p = flatten(edges, n);
-    check(sst_insert_batch(g_, p.data(), n, semi_sorted ? SST_SEMI_SORTED : 0u,
-                           nullptr));
+    if constexpr (weighted) {
+      std::vector<uint32_t> v = values_of(edges, n);
+      check(sst_insert_batch_weighted(g_, p.data(), v.data(), n,
+                                      semi_sorted ? SST_SEMI_SORTED : 0u, nullptr));
+    } else {
+      check(sst_insert_batch(g_, p.data(), n, semi_sorted ? SST_SEMI_SORTED : 0u,
+                             nullptr));
+    }
   }
-  void remove_batch(std::tuple<el_t, el_t> *edges, uint64_t n,
-                    bool semi_sorted = false) {
+  void remove_batch(edge_t *edges, uint64_t n, bool semi_sorted = false) {
     std::vector<uint32_t> p = flatten(edges, n);
     check(sst_remove_batch(g_, p.data(), n, semi_sorted ? SST_SEMI_SORTED : 0u,
                            nullptr));
@@ -222,6 +255,11 @@ template <class T, class G> T *PR_S(const G &g, long iters) {
 template <class G> double *BC(const G &g, uint32_t src) {
   double *out = static_cast<double *>(std::malloc(g.num_nodes() * sizeof(double)));
   SSTGraph::check(sst_bc(g.handle(), src, out, 0));
+  return out;
+}
+template <class G> int32_t *BF(const G &g, uint32_t src) {
+  int32_t *out = static_cast<int32_t *>(std::malloc(g.num_nodes() * sizeof(int32_t)));
+  SSTGraph::check(sst_bf(g.handle(), src, out, 0));
   return out;
 }
 template <class G> uint32_t *CC(const G &g) {

@@ -15,6 +15,32 @@ using namespace SSTGraph;
 
 // the reference's TinySet tests in miniature (Tinyset_test.cpp: insert
 // random elements below max, check membership; remove, check absence)
+// the weighted form: values, overwrite on re-insert, Bellman-Ford on a
+// small chain with a shortcut
+static int weighted_check() {
+  SparseMatrixV<true, uint32_t> w(6, 6);
+  std::vector<std::tuple<el_t, el_t, uint32_t>> es = {
+      {0, 1, 4}, {1, 2, 3}, {2, 3, 2}, {0, 3, 20}, {3, 4, 1}, {0, 1, 5}};
+  w.insert_batch(es.data(), es.size());
+  if (w.value(0, 1) != 5 || w.value(0, 3) != 20 || w.value(4, 3) != 0) {
+    std::printf("weighted values differ\n");
+    return 1;
+  }
+  std::vector<std::tuple<el_t, el_t, uint32_t>> upd = {{0, 3, 7}};
+  w.insert_batch(upd.data(), upd.size());
+  int32_t *d = EdgeMapVertexMap::BF(w, 0);
+  // 0->3 costs 7 directly (was 20), 0->1->2->3 costs 10; 0->3->4 costs 8
+  const int32_t exp[6] = {0, 5, 8, 7, 8, 0x7FFFFFFF};
+  for (int v = 0; v < 6; v++)
+    if (d[v] != exp[v]) {
+      std::printf("BF[%d] = %d, expected %d\n", v, d[v], exp[v]);
+      std::free(d);
+      return 1;
+    }
+  std::free(d);
+  return 0;
+}
+
 static int tinyset_check() {
   const uint32_t max = 5000;
   TinySetV<> ts(max);
@@ -117,6 +143,7 @@ int main() {
   std::free(pr);
   std::free(cc);
   if (tinyset_check()) return 1;
+  if (weighted_check()) return 1;
   std::printf("facade ok: M=%llu tc=%llu\n", (unsigned long long)g.M(),
               (unsigned long long)tc);
   return 0;
