@@ -28,6 +28,7 @@
 // PMA.hpp:612-702 (redistribute / double_list / half_list),
 // PMA.hpp:1185-1222 (take: lower-bound climb).
 #include <algorithm>
+#include <cstddef>
 #include <cstdarg>
 #include <cstring>
 #include <vector>
@@ -456,8 +457,7 @@ __global__ void k_dom_classify(const uint64_t *__restrict__ p_ul,
                                const uint64_t *__restrict__ fscan,
                                const uint64_t *__restrict__ bscan,
                                const uint32_t *__restrict__ d_ngroups,
-                               uint64_t gmax, uint32_t *__restrict__ mflag,
-                               uint32_t *__restrict__ tflag) {
+                               uint64_t gmax, uint64_t *__restrict__ mt) {
   uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= gmax) return;
   uint32_t mf = 0, tf = 0;
@@ -477,20 +477,21 @@ __global__ void k_dom_classify(const uint64_t *__restrict__ p_ul,
       tf = !dom;
     }
   }
-  mflag[gid] = mf;
-  tflag[gid] = tf;
+  // merge flag in the low word, task flag in the high word: one scan of
+  // the packed words gives both positions (the counts stay below 2^32)
+  mt[gid] = ((uint64_t)tf << 32) | mf;
 }
 
-__global__ void k_emit(const uint32_t *__restrict__ mflag,
-                       const uint32_t *__restrict__ mpos,
-                       const uint32_t *__restrict__ tflag,
-                       const uint32_t *__restrict__ tpos, uint64_t gmax,
+__global__ void k_emit(const uint64_t *__restrict__ mt,
+                       const uint64_t *__restrict__ mtpos, uint64_t gmax,
                        uint32_t *__restrict__ merge_list,
                        uint32_t *__restrict__ task_group) {
   uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= gmax) return;
-  if (mflag[gid] && mpos[gid] < gmax) merge_list[mpos[gid]] = (uint32_t)gid;
-  if (tflag[gid] && tpos[gid] < gmax) task_group[tpos[gid]] = (uint32_t)gid;
+  const uint64_t f = mt[gid], p = mtpos[gid];
+  const uint32_t mpos = (uint32_t)p, tpos = (uint32_t)(p >> 32);
+  if ((uint32_t)f && mpos < gmax) merge_list[mpos] = (uint32_t)gid;
+  if ((f >> 32) && tpos < gmax) task_group[tpos] = (uint32_t)gid;
 }
 
 // ---------------------------------------------------------------- step 8
@@ -1160,8 +1161,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   uint8_t *gtype = A.take<uint8_t>(b), *glev = A.take<uint8_t>(b);
   uint32_t *gw0 = A.take<uint32_t>(b), *gw1 = A.take<uint32_t>(b);
   uint64_t *fkey = A.take<uint64_t>(b), *bkey = A.take<uint64_t>(b);
-  uint32_t *mflag = A.take<uint32_t>(b), *tflag = A.take<uint32_t>(b);
-  uint32_t *mpos = A.take<uint32_t>(b), *tpos = A.take<uint32_t>(b);
+  uint64_t *mt = A.take<uint64_t>(b), *mtpos = A.take<uint64_t>(b);
   uint32_t *merge_list = A.take<uint32_t>(b), *task_group = A.take<uint32_t>(b);
   uint32_t *climb = A.take<uint32_t>(b);
   Tasks T;
@@ -1248,13 +1248,14 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   SST_CUDA_TRY((scan<uint64_t, OpMin>(bkey, bkey, b, ~0ull, OpMin{}, true, true,
                                       nullptr, A, s)));
   SST_LAUNCH(k_dom_classify, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
-             fkey, bkey, &P->n_groups, b, mflag, tflag);
-  SST_CUDA_TRY((scan<uint32_t, OpAdd>(mflag, mpos, b, 0u, OpAdd{}, true, false,
-                                      &P->n_merge, A, s)));
-  SST_CUDA_TRY((scan<uint32_t, OpAdd>(tflag, tpos, b, 0u, OpAdd{}, true, false,
-                                      &P->n_tasks, A, s)));
-  SST_LAUNCH(k_emit, blocks_for(b), kTB, 0, s, mflag, mpos, tflag, tpos, b,
-             merge_list, task_group);
+             fkey, bkey, &P->n_groups, b, mt);
+  // totals land as one word on (n_merge, n_tasks), adjacent in the plan
+  static_assert(offsetof(PlanSummary, n_tasks) == offsetof(PlanSummary, n_merge) + 4 &&
+                    offsetof(PlanSummary, n_merge) % 8 == 0,
+                "n_merge and n_tasks share one aligned 64-bit word");
+  SST_CUDA_TRY((scan<uint64_t, OpAdd>(mt, mtpos, b, 0ull, OpAdd{}, true, false,
+                                      reinterpret_cast<uint64_t *>(&P->n_merge), A, s)));
+  SST_LAUNCH(k_emit, blocks_for(b), kTB, 0, s, mt, mtpos, b, merge_list, task_group);
   // 8: plan
   SST_LAUNCH(k_task_setup, wgrid, kTB, 0, s, dg, g->params, insert, p_ul,
              g_start, gtype, gw0, gw1, task_group, &P->n_tasks, &P->n_items, b, T,
