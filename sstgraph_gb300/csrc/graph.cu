@@ -105,6 +105,10 @@ __device__ __forceinline__ uint32_t warp_sum_lcnt(const uint8_t *lc,
   return __reduce_add_sync(0xffffffffu, s);
 }
 
+// count word of an item's leaf: the leaf's element count, plus this bit
+// when the row is a multi-leaf segment (its leaves keep counts in lcnt)
+constexpr uint32_t kMultiLeaf = 1u << 8;
+
 // ---------------------------------------------------------------- steps 1-5
 __global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
                             uint32_t n, uint32_t width, int dbits,
@@ -132,7 +136,8 @@ __global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
                          int dbits, DGraph g, bool insert,
                          uint32_t *__restrict__ flag,
                          uint32_t *__restrict__ leaf_out,
-                         const uint32_t *__restrict__ wv) {
+                         const uint32_t *__restrict__ wv,
+                         uint64_t *__restrict__ lS, uint32_t *__restrict__ lc) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b) return;
   const uint64_t sent = (uint64_t)g.n << dbits;
@@ -142,6 +147,8 @@ __global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
     leaf_out[i] = 0;
     return;
   }
+  uint64_t S = 0;
+  uint32_t cw = 0;
   uint32_t u = (uint32_t)(k >> dbits);
   uint32_t x = (uint32_t)(k & ((1ull << dbits) - 1));
   uint64_t base = g.base[u];
@@ -156,9 +163,13 @@ __global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
     present = pos < c && p[pos] == x;
     if (present && insert && wv && g.vals)
       g.vals[base + ((uint64_t)l << kLeafLog) + pos] = wv[i];
+    S = base + ((uint64_t)l << kLeafLog);
+    cw = c | (cap > kLeaf ? kMultiLeaf : 0u);
   }
   flag[i] = insert ? !present : present;
   leaf_out[i] = l;
+  lS[i] = S;
+  lc[i] = cw;
 }
 
 __global__ void k_pack(const uint64_t *__restrict__ keys,
@@ -166,7 +177,9 @@ __global__ void k_pack(const uint64_t *__restrict__ keys,
                        const uint32_t *__restrict__ pos,
                        const uint32_t *__restrict__ leaf, uint64_t b, int dbits,
                        uint64_t *__restrict__ p_ul, uint32_t *__restrict__ p_x,
-                       const uint32_t *__restrict__ wv, uint32_t *__restrict__ p_w) {
+                       const uint32_t *__restrict__ wv, uint32_t *__restrict__ p_w,
+                       const uint64_t *__restrict__ lS, const uint32_t *__restrict__ lc,
+                       uint64_t *__restrict__ p_S, uint32_t *__restrict__ p_c) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b || !flag[i]) return;
   uint64_t k = keys[i];
@@ -175,6 +188,18 @@ __global__ void k_pack(const uint64_t *__restrict__ keys,
   p_ul[j] = ((k >> dbits) << 32) | leaf[i];
   p_x[j] = (uint32_t)(k & ((1ull << dbits) - 1));
   if (p_w) p_w[j] = wv[i];
+  p_S[j] = lS[i];
+  p_c[j] = lc[i];
+}
+
+// after a repack moved the segments: the items' leaf starts again
+__global__ void k_fix_leaf_start(DGraph g, const uint64_t *__restrict__ p_ul,
+                                 const uint32_t *__restrict__ d_nitems,
+                                 uint64_t b, uint64_t *__restrict__ p_S) {
+  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= b || j >= *d_nitems) return;
+  const uint64_t key = p_ul[j];
+  p_S[j] = g.base[(uint32_t)(key >> 32)] + ((uint64_t)(uint32_t)key << kLeafLog);
 }
 
 __global__ void k_group_flags(const uint64_t *__restrict__ p_ul,
@@ -255,21 +280,23 @@ __device__ __forceinline__ uint32_t leaf_slot(uint32_t linev, uint64_t S,
 }
 
 // remove, first pass: delete inside each touched leaf (warp per group) and
-// take the count off the row's degree
+// take the count off the row's degree.  Each item carries its leaf's start
+// and count word from the locate step, so a group costs three dependent
+// loads: its item range, the items, the leaf.
 __global__ void __launch_bounds__(256, 4)
 k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
-                              const uint32_t *__restrict__ p_x,
-                              const uint32_t *__restrict__ g_start,
-                              const uint32_t *__restrict__ d_ngroups) {
+              const uint32_t *__restrict__ p_x,
+              const uint64_t *__restrict__ p_S, const uint32_t *__restrict__ p_c,
+              const uint32_t *__restrict__ g_start,
+              const uint32_t *__restrict__ d_ngroups) {
   const int lane = threadIdx.x & 31;
   constexpr int Q = kGroupsPerWarp;
   const uint32_t ng = *d_ngroups;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
        w * Q < ng; w += nw) {
-    // kGroupsPerWarp groups per round, each stage's loads issued together
-    uint32_t j0[Q], k[Q], d[Q], linev[Q], c[Q], cap[Q], deg[Q];
-    uint64_t key[Q], base[Q], S[Q];
+    uint32_t j0[Q], k[Q], d[Q], linev[Q], cw[Q], u[Q];
+    uint64_t S[Q];
     bool ok[Q];
 #pragma unroll
     for (int q = 0; q < Q; q++) {
@@ -280,41 +307,32 @@ k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
     }
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-      key[q] = ok[q] ? p_ul[j0[q]] : 0;
+      S[q] = ok[q] ? p_S[j0[q]] : 0;
+      cw[q] = ok[q] ? p_c[j0[q]] : 0;
+      u[q] = ok[q] ? (uint32_t)(p_ul[j0[q]] >> 32) : 0;
       d[q] = (uint32_t)lane < k[q] ? p_x[j0[q] + lane] : kEmpty;
     }
 #pragma unroll
-    for (int q = 0; q < Q; q++) {
-      uint32_t u = (uint32_t)(key[q] >> 32);
-      base[q] = ok[q] ? g.base[u] : 0;
-      cap[q] = ok[q] ? g.cap[u] : 0;
-      deg[q] = ok[q] ? g.deg[u] : 0;
-    }
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-      uint32_t leaf = (uint32_t)key[q];
-      S[q] = base[q] + ((uint64_t)leaf << kLeafLog);
+    for (int q = 0; q < Q; q++)
       linev[q] = ok[q] ? g.slots[(S[q] & ~uint64_t(kLeaf - 1)) + lane] : kEmpty;
-      c[q] = ok[q] ? leaf_count(g, base[q], cap[q], deg[q], leaf) : 0;
-    }
 #pragma unroll
     for (int q = 0; q < Q; q++) {
       if (!ok[q]) break;
-      const uint32_t a = leaf_slot(linev[q], S[q], c[q], lane);
+      const uint32_t c = cw[q] & 0xff;
+      const uint32_t a = leaf_slot(linev[q], S[q], c, lane);
       bool del = false;
       for (uint32_t j = 0; j < k[q]; j++) del |= (__shfl_sync(0xffffffffu, d[q], j) == a);
-      bool keep = (uint32_t)lane < c[q] && !del;
+      bool keep = (uint32_t)lane < c && !del;
       uint32_t mask = __ballot_sync(0xffffffffu, keep);
       uint32_t pos = __popc(mask & ((1u << lane) - 1u));
-      const uint32_t av = (g.vals && (uint32_t)lane < c[q]) ? g.vals[S[q] + lane] : 0u;
+      const uint32_t av = (g.vals && (uint32_t)lane < c) ? g.vals[S[q] + lane] : 0u;
       __syncwarp();
       if (keep) g.slots[S[q] + pos] = a;
       if (keep && g.vals) g.vals[S[q] + pos] = av;
-      if ((uint32_t)lane >= c[q] - k[q] && (uint32_t)lane < c[q]) g.slots[S[q] + lane] = kEmpty;
+      if ((uint32_t)lane >= c - k[q] && (uint32_t)lane < c) g.slots[S[q] + lane] = kEmpty;
       if (lane == 0) {
-        if (cap[q] > kLeaf)
-          g.lcnt[(base[q] >> kLeafLog) + (uint32_t)key[q]] = (uint8_t)(c[q] - k[q]);
-        atomicSub(&g.deg[(uint32_t)(key[q] >> 32)], k[q]);
+        if (cw[q] & kMultiLeaf) g.lcnt[S[q] >> kLeafLog] = (uint8_t)(c - k[q]);
+        atomicSub(&g.deg[u[q]], k[q]);
       }
       __syncwarp();
     }
@@ -484,13 +502,17 @@ __global__ void k_dom_classify(const uint64_t *__restrict__ p_ul,
 
 __global__ void k_emit(const uint64_t *__restrict__ mt,
                        const uint64_t *__restrict__ mtpos, uint64_t gmax,
-                       uint32_t *__restrict__ merge_list,
+                       const uint32_t *__restrict__ g_start,
+                       uint64_t *__restrict__ merge_jk,
                        uint32_t *__restrict__ task_group) {
   uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= gmax) return;
   const uint64_t f = mt[gid], p = mtpos[gid];
   const uint32_t mpos = (uint32_t)p, tpos = (uint32_t)(p >> 32);
-  if ((uint32_t)f && mpos < gmax) merge_list[mpos] = (uint32_t)gid;
+  if ((uint32_t)f && mpos < gmax) {
+    const uint32_t j0 = g_start[gid];
+    merge_jk[mpos] = ((uint64_t)j0 << 32) | (g_start[gid + 1] - j0);
+  }
   if ((f >> 32) && tpos < gmax) task_group[tpos] = (uint32_t)gid;
 }
 
@@ -582,51 +604,42 @@ __global__ void k_task_setup(DGraph g, PmaParams p, bool insert,
 
 // ---------------------------------------------------------------- step 9
 // warp per kGroupsPerWarp merge groups; each stage's loads for all of them
-// are issued together (the groups are independent leaves)
+// are issued together (the groups are independent leaves).  merge_jk[t] =
+// (first item << 32) | item count of merge group t; the items carry their
+// leaf's start and count word, so a group costs three dependent loads.
 __global__ void __launch_bounds__(256, 4)
-k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul,
-                             const uint32_t *__restrict__ p_x,
-                             const uint32_t *__restrict__ g_start,
-                             const uint32_t *__restrict__ merge_list,
-                             uint32_t nmerge, const uint32_t *__restrict__ p_w) {
+k_leaf_merge(DGraph g, const uint32_t *__restrict__ p_x,
+             const uint64_t *__restrict__ p_S, const uint32_t *__restrict__ p_c,
+             const uint64_t *__restrict__ merge_jk, uint32_t nmerge,
+             const uint32_t *__restrict__ p_w) {
   const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   constexpr int Q = kGroupsPerWarp;
   if (w * Q >= nmerge) return;
-  uint32_t j0[Q], k[Q], x[Q], linev[Q], c[Q], cap[Q];
-  uint64_t key[Q], base[Q], S[Q];
+  uint32_t j0[Q], k[Q], x[Q], linev[Q], cw[Q];
+  uint64_t S[Q];
   bool ok[Q];
 #pragma unroll
   for (int q = 0; q < Q; q++) {
     ok[q] = w * Q + q < nmerge;
-    uint32_t gid = ok[q] ? merge_list[w * Q + q] : 0;
-    j0[q] = ok[q] ? g_start[gid] : 0;
-    k[q] = ok[q] ? g_start[gid + 1] - j0[q] : 0;
+    const uint64_t jk = ok[q] ? merge_jk[w * Q + q] : 0;
+    j0[q] = (uint32_t)(jk >> 32);
+    k[q] = (uint32_t)jk;
   }
 #pragma unroll
   for (int q = 0; q < Q; q++) {
-    key[q] = ok[q] ? p_ul[j0[q]] : 0;
+    S[q] = ok[q] ? p_S[j0[q]] : 0;
+    cw[q] = ok[q] ? p_c[j0[q]] : 0;
     x[q] = (uint32_t)lane < k[q] ? p_x[j0[q] + lane] : kEmpty;
   }
-  uint32_t deg[Q];
 #pragma unroll
-  for (int q = 0; q < Q; q++) {
-    uint32_t u = (uint32_t)(key[q] >> 32);
-    base[q] = ok[q] ? g.base[u] : 0;
-    cap[q] = ok[q] ? g.cap[u] : 0;
-    deg[q] = ok[q] ? g.deg[u] : 0;
-  }
-#pragma unroll
-  for (int q = 0; q < Q; q++) {
-    uint32_t leaf = (uint32_t)key[q];
-    S[q] = base[q] + ((uint64_t)leaf << kLeafLog);
+  for (int q = 0; q < Q; q++)
     linev[q] = ok[q] ? g.slots[(S[q] & ~uint64_t(kLeaf - 1)) + lane] : kEmpty;
-    c[q] = ok[q] ? leaf_count(g, base[q], cap[q], deg[q], leaf) : 0;
-  }
 #pragma unroll
   for (int q = 0; q < Q; q++) {
     if (!ok[q]) break;
-    const uint32_t a = leaf_slot(linev[q], S[q], c[q], lane);
+    const uint32_t c = cw[q] & 0xff;
+    const uint32_t a = leaf_slot(linev[q], S[q], c, lane);
     // merged ranks in O(k) steps (k new ids, usually one or two): an old id
     // moves up by the new ids below it; new id j lands at j + the old ids
     // below it (a ballot per new id)
@@ -634,19 +647,18 @@ k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul,
     for (uint32_t j = 0; j < k[q]; j++) {
       uint32_t xj = __shfl_sync(0xffffffffu, x[q], j);
       pa += xj < a;
-      uint32_t below = __popc(__ballot_sync(0xffffffffu, (uint32_t)lane < c[q] && a < xj));
+      uint32_t below = __popc(__ballot_sync(0xffffffffu, (uint32_t)lane < c && a < xj));
       if ((uint32_t)lane == j) px = j + below;
     }
     // values move with their ids (weighted graphs)
-    const uint32_t av = (g.vals && (uint32_t)lane < c[q]) ? g.vals[S[q] + lane] : 0u;
+    const uint32_t av = (g.vals && (uint32_t)lane < c) ? g.vals[S[q] + lane] : 0u;
     const uint32_t xv = (g.vals && (uint32_t)lane < k[q]) ? (p_w ? p_w[j0[q] + lane] : 1u) : 0u;
     __syncwarp();
-    if ((uint32_t)lane < c[q]) g.slots[S[q] + pa] = a;
+    if ((uint32_t)lane < c) g.slots[S[q] + pa] = a;
     if ((uint32_t)lane < k[q]) g.slots[S[q] + px] = x[q];
-    if (g.vals && (uint32_t)lane < c[q]) g.vals[S[q] + pa] = av;
+    if (g.vals && (uint32_t)lane < c) g.vals[S[q] + pa] = av;
     if (g.vals && (uint32_t)lane < k[q]) g.vals[S[q] + px] = xv;
-    if (lane == 0 && cap[q] > kLeaf)
-      g.lcnt[(base[q] >> kLeafLog) + (uint32_t)key[q]] = (uint8_t)(c[q] + k[q]);
+    if (lane == 0 && (cw[q] & kMultiLeaf)) g.lcnt[S[q] >> kLeafLog] = (uint8_t)(c + k[q]);
   }
 }
 
@@ -1108,7 +1120,8 @@ sst_status repack(sst_graph *g, uint64_t extra) {
 // bytes of arena scratch an update batch of b pairs takes
 static size_t update_scratch_bytes(uint64_t b) {
   size_t per = 8 * 2 + 4 * 4 + 8 + 4 + 4 * 3 + 1 * 2 + 4 * 2 + 8 * 4 + 4 * 6 +
-               8 * 8 + 4 * 4 + 1 + 64 + 4 * 3 /* values */;
+               8 * 8 + 4 * 4 + 1 + 64 + 4 * 3 /* values */ +
+               8 + 4 + 8 + 4 + 4 /* leaf starts and counts, merge ranges */;
   return b * per + radix_sort_scratch_bytes(b) + 8 * scan_scratch_bytes(b, 8) +
          (1 << 16);
 }
@@ -1162,7 +1175,11 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   uint32_t *gw0 = A.take<uint32_t>(b), *gw1 = A.take<uint32_t>(b);
   uint64_t *fkey = A.take<uint64_t>(b), *bkey = A.take<uint64_t>(b);
   uint64_t *mt = A.take<uint64_t>(b), *mtpos = A.take<uint64_t>(b);
-  uint32_t *merge_list = A.take<uint32_t>(b), *task_group = A.take<uint32_t>(b);
+  uint64_t *merge_jk = A.take<uint64_t>(b);
+  uint32_t *task_group = A.take<uint32_t>(b);
+  // per key, then per packed item: the leaf's start slot and count word
+  uint64_t *lS = A.take<uint64_t>(b), *p_S = A.take<uint64_t>(b);
+  uint32_t *lc = A.take<uint32_t>(b), *p_c = A.take<uint32_t>(b);
   uint32_t *climb = A.take<uint32_t>(b);
   Tasks T;
   T.u = A.take<uint32_t>(b);
@@ -1215,11 +1232,11 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   // 3-5: locate, pack, group
   // sorted key in (8 B), flag and leaf out (8 B)
   SST_LAUNCH_B(16 * b, k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg,
-               insert, flag, leaf, wt ? wv : nullptr);
+               insert, flag, leaf, wt ? wv : nullptr, lS, lc);
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(flag, pos, b, 0u, OpAdd{}, true, false,
                                       &P->n_items, A, s)));
   SST_LAUNCH(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,
-             p_ul, p_x, wv, p_w);
+             p_ul, p_x, wv, p_w, lS, lc, p_S, p_c);
   SST_LAUNCH(k_group_flags, blocks_for(b), kTB, 0, s, p_ul, &P->n_items, b, gflag);
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(gflag, gpos, b, 0u, OpAdd{}, true, false,
                                       &P->n_groups, A, s)));
@@ -1233,7 +1250,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     SST_LAUNCH(k_classify_insert, tgrid, kTB, 0, s, dg, p_ul, g_start,
                &P->n_groups, gtype, glev, gw0, gw1, climb, &P->n_climb);
   } else {
-    SST_LAUNCH(k_leaf_delete, wgrid, kTB, 0, s, dg, p_ul, p_x, g_start,
+    SST_LAUNCH(k_leaf_delete, wgrid, kTB, 0, s, dg, p_ul, p_x, p_S, p_c, g_start,
                &P->n_groups);
     SST_LAUNCH(k_classify_remove, tgrid, kTB, 0, s, dg, g->params, p_ul,
                g_start, &P->n_groups, gtype, glev, gw0, gw1, climb, &P->n_climb);
@@ -1255,7 +1272,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                 "n_merge and n_tasks share one aligned 64-bit word");
   SST_CUDA_TRY((scan<uint64_t, OpAdd>(mt, mtpos, b, 0ull, OpAdd{}, true, false,
                                       reinterpret_cast<uint64_t *>(&P->n_merge), A, s)));
-  SST_LAUNCH(k_emit, blocks_for(b), kTB, 0, s, mt, mtpos, b, merge_list, task_group);
+  SST_LAUNCH(k_emit, blocks_for(b), kTB, 0, s, mt, mtpos, b, g_start, merge_jk,
+             task_group);
   // 8: plan
   SST_LAUNCH(k_task_setup, wgrid, kTB, 0, s, dg, g->params, insert, p_ul,
              g_start, gtype, gw0, gw1, task_group, &P->n_tasks, &P->n_items, b, T,
@@ -1290,6 +1308,10 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     if (st != SST_OK) return st;
     dg = g->view();
     start = (g->bump + kLeaf - 1) & ~uint64_t(kLeaf - 1);
+    // segments moved: the items' leaf starts for the merges below
+    if (ps.n_items)
+      SST_LAUNCH(k_fix_leaf_start, blocks_for(ps.n_items), kTB, 0, s, dg, p_ul,
+                 &P->n_items, ps.n_items, p_S);
   }
   uint64_t hstart[kNumClasses];
   uint64_t off = start;
@@ -1322,9 +1344,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     // each merge rewrites one 128-byte leaf (read + write) and its count
     // (the merged ids, fewer than 32 per leaf, are not counted)
     SST_LAUNCH_B(258ull * ps.n_merge, k_leaf_merge,
-               warp_blocks((ps.n_merge + kGroupsPerWarp - 1) / kGroupsPerWarp),
-               kTB, 0, s, dg, p_ul, p_x,
-               g_start, merge_list, ps.n_merge, p_w);
+                 warp_blocks((ps.n_merge + kGroupsPerWarp - 1) / kGroupsPerWarp),
+                 kTB, 0, s, dg, p_x, p_S, p_c, merge_jk, ps.n_merge, p_w);
   if (ps.n_tasks) {
     if (ps.src_leaves) {
       SST_LAUNCH(k_src_counts, blocks_for(ps.src_leaves), kTB, 0, s, dg, T,
