@@ -419,8 +419,10 @@ __device__ __forceinline__ unsigned long long gather(const unsigned long long *s
   return x < hot ? sh[x] : ld_keep(cin + x);
 }
 
+constexpr int kHotThreads = 512;  // 4 blocks of 16 warps per SM
+
 template <int G>
-__global__ void k_pr_small_hot(DGraph g, const unsigned long long *__restrict__ sdesc,
+__global__ void __launch_bounds__(kHotThreads, 4) k_pr_small_hot(DGraph g, const unsigned long long *__restrict__ sdesc,
                                const uint32_t *__restrict__ small, uint64_t nsmall,
                                const unsigned long long *__restrict__ cin,
                                unsigned long long *__restrict__ cout,
@@ -472,7 +474,7 @@ __global__ void k_pr_small_hot(DGraph g, const unsigned long long *__restrict__ 
   }
 }
 
-__global__ void k_pr_chunks_hot(DGraph g, const unsigned long long *__restrict__ cdesc,
+__global__ void __launch_bounds__(kHotThreads, 4) k_pr_chunks_hot(DGraph g, const unsigned long long *__restrict__ cdesc,
                                 const uint32_t *__restrict__ cv, uint64_t nchunks,
                                 const unsigned long long *__restrict__ cin,
                                 unsigned long long *__restrict__ cout,
@@ -1198,7 +1200,8 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   unsigned long long *cout = reinterpret_cast<unsigned long long *>(t->cb.p);
   unsigned long long *part = reinterpret_cast<unsigned long long *>(t->partial.p);
   // the shared-memory cache: at most the rows, at most 24,576 entries
-  // (192 KiB); persistent grids sized by occupancy at that footprint
+  // (192 KiB), one copy per block; persistent grids sized by occupancy at
+  // that footprint (more than 8,192 entries leaves under three blocks/SM)
   const uint32_t hot = std::min<uint32_t>(t->pr_hot, std::min<uint32_t>(n, 24576));
   const size_t hot_bytes = (size_t)hot * 8;
   unsigned hot_grid[4] = {1, 1, 1, 1};
@@ -1209,7 +1212,7 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
       SST_CUDA_TRY(cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)hot_bytes));
       int per_sm = 0;
-      SST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], 1024,
+      SST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], kHotThreads,
                                                                  hot_bytes));
       hot_grid[i] = (unsigned)std::max(1, per_sm) * (unsigned)g->sms;
     }
@@ -1223,13 +1226,13 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
       bool last = it + 1 == iters;
       if (hot && t->nsmall) {
         if (t->pr_lanes == 4)
-          SST_LAUNCH(k_pr_small_hot<4>, hot_grid[0], 1024, hot_bytes, s, dg,
+          SST_LAUNCH(k_pr_small_hot<4>, hot_grid[0], kHotThreads, hot_bytes, s, dg,
                      t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot);
         else if (t->pr_lanes == 16)
-          SST_LAUNCH(k_pr_small_hot<16>, hot_grid[2], 1024, hot_bytes, s, dg,
+          SST_LAUNCH(k_pr_small_hot<16>, hot_grid[2], kHotThreads, hot_bytes, s, dg,
                      t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot);
         else
-          SST_LAUNCH(k_pr_small_hot<8>, hot_grid[1], 1024, hot_bytes, s, dg,
+          SST_LAUNCH(k_pr_small_hot<8>, hot_grid[1], kHotThreads, hot_bytes, s, dg,
                      t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot);
       } else if (t->nsmall) {
         const uint64_t groups = (t->nsmall + kSmallPer - 1) / kSmallPer;
@@ -1244,7 +1247,7 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
                      t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last);
       }
       if (hot && t->nchunks)
-        SST_LAUNCH(k_pr_chunks_hot, hot_grid[3], 1024, hot_bytes, s, dg, t->cdesc.p,
+        SST_LAUNCH(k_pr_chunks_hot, hot_grid[3], kHotThreads, hot_bytes, s, dg, t->cdesc.p,
                    t->cv.p, t->nchunks, ci, co, d_rank, rdeg, part, K, last, hot);
       else if (t->nchunks)
         SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cdesc.p,
@@ -2050,7 +2053,7 @@ sst_status bc_multi(sst_graph *g, const uint32_t *h_srcs, uint32_t k,
 // ------------------------------------------------------------- autotuner
 // Times the traversal knobs on this graph and keeps the fastest: PageRank
 // (3 iterations) over chunk sizes {8, 16, 32} x lanes {4, 8, 16}, then its
-// shared-memory cache {0, 8192, 16384, 24576}, then BFS from three sources
+// shared-memory cache {0, 2048, 4096, 8192}, then BFS from three sources
 // over push/pull thresholds {5, 10, 20, 40, 80}.
 sst_status get_tuning(sst_graph *g, sst_tuning *out) {
   TravState *t = state(g);
@@ -2123,7 +2126,7 @@ sst_status autotune(sst_graph *g, sst_tuning *out) {
   // then the shared-memory cache of the lowest ids (pays on degree-ordered
   // graphs)
   uint32_t bhot = 0;
-  const uint32_t hots[3] = {8192, 16384, 24576};
+  const uint32_t hots[3] = {2048, 4096, 8192};
   for (uint32_t a = 0; a < 3 && st == SST_OK; a++) {
     t->pr_hot = hots[a];
     float ms = 0.f;
