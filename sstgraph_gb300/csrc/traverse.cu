@@ -572,6 +572,47 @@ __device__ __forceinline__ void enqueue(bool mine, uint32_t w, uint32_t wdeg,
   if (mine) q[base + __popc(m & ((1u << lane) - 1u))] = w;
 }
 
+// Block-aggregated form of enqueue for kernels in which every thread of the
+// block calls it once: one atomic per counter per block (the three queue
+// counters are single addresses, so per-warp atomics from a whole grid
+// serialise on them).
+__device__ __forceinline__ void enqueue_block(bool mine, uint32_t w, uint32_t wdeg,
+                                              uint32_t witems, uint32_t *q,
+                                              unsigned long long *qlen_deg) {
+  __shared__ uint32_t s_cnt[kTB / 32];
+  __shared__ unsigned long long s_base, s_deg, s_items;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t m = __ballot_sync(0xffffffffu, mine);
+  const uint32_t dsum = __reduce_add_sync(0xffffffffu, mine ? wdeg : 0u);
+  const uint32_t isum = __reduce_add_sync(0xffffffffu, mine ? witems : 0u);
+  if (threadIdx.x == 0) {
+    s_deg = 0;
+    s_items = 0;
+  }
+  if (lane == 0) s_cnt[warp] = __popc(m);
+  __syncthreads();
+  if (lane == 0 && m) {
+    atomicAdd(&s_deg, (unsigned long long)dsum);
+    atomicAdd(&s_items, (unsigned long long)isum);
+  }
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+#pragma unroll
+    for (int k = 0; k < kTB / 32; k++) {
+      uint32_t c = s_cnt[k];
+      s_cnt[k] = tot;
+      tot += c;
+    }
+    s_base = tot ? atomicAdd(&qlen_deg[0], (unsigned long long)tot) : 0ull;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && (s_deg || s_items)) {
+    atomicAdd(&qlen_deg[1], s_deg);
+    atomicAdd(&qlen_deg[2], s_items);
+  }
+  if (mine) q[s_base + s_cnt[warp] + __popc(m & ((1u << lane) - 1u))] = w;
+}
+
 // work items of one vertex: 1 for a one-leaf segment, else one per chunk
 // of kChunkLeaves leaves
 __device__ __forceinline__ uint32_t items_of(uint32_t cap) {
@@ -693,7 +734,7 @@ __global__ void k_bfs_pull_small8(DGraph g, const unsigned long long *__restrict
       mydeg = d;
     }
   }
-  enqueue(mine, myv, mydeg, 1u, nq, cnt);
+  enqueue_block(mine, myv, mydeg, 1u, nq, cnt);
 }
 
 // pull, multi-leaf vertices: warp per chunk of the work lists (lane = slot,
@@ -744,7 +785,7 @@ __global__ void k_bfs_pull_chunks(DGraph g, const unsigned long long *__restrict
       }
     }
   }
-  enqueue(mine, v, mine ? g.deg[v] : 0u, mine ? items_of(g.cap[v]) : 0u, nq, cnt);
+  enqueue_block(mine, v, mine ? g.deg[v] : 0u, mine ? items_of(g.cap[v]) : 0u, nq, cnt);
 }
 
 // ------------------------------------------------------------- cc
@@ -1682,7 +1723,7 @@ __global__ void k_msbfs_update(uint32_t n, unsigned long long *__restrict__ vis,
     }
     fr_next[v] = nw;
   }
-  enqueue(nw != 0, v, nw ? deg[v] : 0u, nw ? items_of(cap[v]) : 0u, q, qc);
+  enqueue_block(nw != 0, v, nw ? deg[v] : 0u, nw ? items_of(cap[v]) : 0u, q, qc);
 }
 
 // ---- multi-source BC: the single-source passes with the source on
