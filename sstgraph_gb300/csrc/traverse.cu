@@ -640,36 +640,75 @@ __global__ void k_front_expand(const uint32_t *__restrict__ q, uint32_t qn,
   }
 }
 
-// push: warp per work item (a frontier vertex's leaf chunk), lane = slot
+// push: warp per work item (a frontier vertex's leaf chunk), lane = slot.
+// Newly reached vertices are staged in shared memory (a block's warps can
+// find at most kTB/32 * kChunkLeaves * 32 of them) and the block reserves
+// its stretch of the next queue with one atomic per counter at the end.
 __global__ void k_bfs_push(DGraph g, const uint32_t *__restrict__ iv,
                            const uint32_t *__restrict__ il0, uint32_t nitems,
                            int32_t *__restrict__ depth,
                            int32_t *__restrict__ parent,
                            uint32_t *__restrict__ nq,
                            unsigned long long *__restrict__ cnt, int lvl) {
-  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  __shared__ uint32_t stage[(kTB / 32) * kChunkLeaves * 32];
+  __shared__ uint32_t s_n;
+  __shared__ unsigned long long s_deg, s_items, s_base;
+  if (threadIdx.x == 0) {
+    s_n = 0;
+    s_deg = 0;
+    s_items = 0;
+  }
+  __syncthreads();
+  const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (i >= nitems) return;
-  uint32_t u = iv[i];
-  uint64_t base = g.base[u];
-  uint32_t cap = g.cap[u], deg = g.deg[u];
-  uint32_t nl = cap ? nleaves_of(cap) : 0;
-  uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
-  for (uint32_t l = l0; l < l1; l++) {
-    uint32_t c = leaf_count(g, base, cap, deg, l);
-    bool mine = false;
-    uint32_t w = 0, wd = 0, wi = 0;
-    if ((uint32_t)lane < c) {
-      w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
-      if (depth[w] < 0 && atomicCAS(&depth[w], -1, lvl + 1) == -1) {
-        parent[w] = (int32_t)u;
-        mine = true;
-        wd = g.deg[w];
-        wi = items_of(g.cap[w]);
+  if (i < nitems) {
+    const uint32_t u = iv[i];
+    const uint64_t base = g.base[u];
+    const uint32_t cap = g.cap[u], deg = g.deg[u];
+    const uint32_t nl = cap ? nleaves_of(cap) : 0;
+    const uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+    unsigned long long dsum = 0, isum = 0;
+    for (uint32_t l = l0; l < l1; l++) {
+      const uint32_t c = leaf_count(g, base, cap, deg, l);
+      bool mine = false;
+      uint32_t w = 0;
+      if ((uint32_t)lane < c) {
+        w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
+        if (depth[w] < 0 && atomicCAS(&depth[w], -1, lvl + 1) == -1) {
+          parent[w] = (int32_t)u;
+          mine = true;
+          dsum += g.deg[w];
+          isum += items_of(g.cap[w]);
+        }
+      }
+      const uint32_t m = __ballot_sync(0xffffffffu, mine);
+      if (m) {
+        uint32_t at = 0;
+        if (lane == __ffs(m) - 1) at = atomicAdd(&s_n, (uint32_t)__popc(m));
+        at = __shfl_sync(0xffffffffu, at, __ffs(m) - 1);
+        if (mine) stage[at + __popc(m & ((1u << lane) - 1u))] = w;
       }
     }
-    enqueue(mine, w, wd, wi, nq, cnt);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      dsum += __shfl_xor_sync(0xffffffffu, dsum, d);
+      isum += __shfl_xor_sync(0xffffffffu, isum, d);
+    }
+    if (lane == 0 && (dsum || isum)) {
+      atomicAdd(&s_deg, dsum);
+      atomicAdd(&s_items, isum);
+    }
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_base = s_n ? atomicAdd(&cnt[0], (unsigned long long)s_n) : 0ull;
+    if (s_deg || s_items) {
+      atomicAdd(&cnt[1], s_deg);
+      atomicAdd(&cnt[2], s_items);
+    }
+  }
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < s_n; k += blockDim.x) nq[s_base + k] = stage[k];
 }
 
 __global__ void k_q2bits(const uint32_t *__restrict__ q, uint32_t qn,
@@ -2240,32 +2279,70 @@ __global__ void k_bf_push(DGraph g, const uint32_t *__restrict__ iv,
                           uint32_t *__restrict__ stamp, uint32_t round,
                           uint32_t *__restrict__ nq,
                           unsigned long long *__restrict__ cnt) {
-  uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // next-round vertices staged in shared memory, one queue reservation per
+  // block (as in the BFS push)
+  __shared__ uint32_t stage[(kTB / 32) * kChunkLeaves * 32];
+  __shared__ uint32_t s_n;
+  __shared__ unsigned long long s_deg, s_items, s_base;
+  if (threadIdx.x == 0) {
+    s_n = 0;
+    s_deg = 0;
+    s_items = 0;
+  }
+  __syncthreads();
+  const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (i >= nitems) return;
-  const uint32_t u = iv[i];
-  const unsigned long long du = __ldcg(dist + u);
-  const uint64_t base = g.base[u];
-  const uint32_t cap = g.cap[u], deg = g.deg[u];
-  const uint32_t nl = cap ? nleaves_of(cap) : 0;
-  const uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
-  for (uint32_t l = l0; l < l1; l++) {
-    const uint32_t c = leaf_count(g, base, cap, deg, l);
-    bool mine = false;
-    uint32_t v = 0, vd = 0, vi = 0;
-    if ((uint32_t)lane < c) {
-      const uint64_t at = base + ((uint64_t)l << kLeafLog) + lane;
-      v = g.slots[at];
-      const unsigned long long nd = du + g.vals[at];
-      if (nd < __ldcg(dist + v) && atomicMin(dist + v, nd) > nd &&
-          atomicExch(stamp + v, round) != round) {
-        mine = true;
-        vd = g.deg[v];
-        vi = items_of(g.cap[v]);
+  if (i < nitems) {
+    const uint32_t u = iv[i];
+    const unsigned long long du = __ldcg(dist + u);
+    const uint64_t base = g.base[u];
+    const uint32_t cap = g.cap[u], deg = g.deg[u];
+    const uint32_t nl = cap ? nleaves_of(cap) : 0;
+    const uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+    unsigned long long dsum = 0, isum = 0;
+    for (uint32_t l = l0; l < l1; l++) {
+      const uint32_t c = leaf_count(g, base, cap, deg, l);
+      bool mine = false;
+      uint32_t v = 0;
+      if ((uint32_t)lane < c) {
+        const uint64_t at = base + ((uint64_t)l << kLeafLog) + lane;
+        v = g.slots[at];
+        const unsigned long long nd = du + g.vals[at];
+        if (nd < __ldcg(dist + v) && atomicMin(dist + v, nd) > nd &&
+            atomicExch(stamp + v, round) != round) {
+          mine = true;
+          dsum += g.deg[v];
+          isum += items_of(g.cap[v]);
+        }
+      }
+      const uint32_t m = __ballot_sync(0xffffffffu, mine);
+      if (m) {
+        uint32_t at = 0;
+        if (lane == __ffs(m) - 1) at = atomicAdd(&s_n, (uint32_t)__popc(m));
+        at = __shfl_sync(0xffffffffu, at, __ffs(m) - 1);
+        if (mine) stage[at + __popc(m & ((1u << lane) - 1u))] = v;
       }
     }
-    enqueue(mine, v, vd, vi, nq, cnt);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      dsum += __shfl_xor_sync(0xffffffffu, dsum, d);
+      isum += __shfl_xor_sync(0xffffffffu, isum, d);
+    }
+    if (lane == 0 && (dsum || isum)) {
+      atomicAdd(&s_deg, dsum);
+      atomicAdd(&s_items, isum);
+    }
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_base = s_n ? atomicAdd(&cnt[0], (unsigned long long)s_n) : 0ull;
+    if (s_deg || s_items) {
+      atomicAdd(&cnt[1], s_deg);
+      atomicAdd(&cnt[2], s_items);
+    }
+  }
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < s_n; k += blockDim.x) nq[s_base + k] = stage[k];
 }
 
 __global__ void k_bf_out(const unsigned long long *__restrict__ dist, uint32_t n,
