@@ -872,18 +872,41 @@ __global__ void k_cc_compress(uint32_t *__restrict__ par, uint32_t n) {
 }
 
 // ------------------------------------------------------------- bc
+// Level bookkeeping: the per-level counters are a handful of addresses hit
+// by every vertex, so lanes of a warp that share a level add once (match),
+// and the maximum depth is taken per block before its one atomic.
+__device__ __forceinline__ uint32_t level_add(uint32_t *ctr, int32_t d, bool on) {
+  const uint32_t key = on ? (uint32_t)d : 0xffffffffu;
+  const uint32_t peers = __match_any_sync(0xffffffffu, key);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (on && lane == leader) base = atomicAdd(ctr, (uint32_t)__popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void block_max_to(int32_t d, unsigned long long *out) {
+  __shared__ int32_t s_max;
+  if (threadIdx.x == 0) s_max = -1;
+  __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) d = max(d, __shfl_down_sync(0xffffffffu, d, o));
+  if ((threadIdx.x & 31) == 0 && d >= 0) atomicMax(&s_max, d);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_max >= 0) atomicMax(out, (unsigned long long)s_max);
+}
+
 __global__ void k_max_depth(const int32_t *__restrict__ depth, uint32_t n,
                             unsigned long long *__restrict__ out) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  int32_t d = v < n ? depth[v] : -1;
-  for (int o = 16; o > 0; o >>= 1) d = max(d, __shfl_down_sync(0xffffffffu, d, o));
-  if ((threadIdx.x & 31) == 0 && d >= 0) atomicMax(out, (unsigned long long)d);
+  block_max_to(v < n ? depth[v] : -1, out);
 }
 
 __global__ void k_level_count(const int32_t *__restrict__ depth, uint32_t n,
                               uint32_t *__restrict__ cnt) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v < n && depth[v] >= 0) atomicAdd(&cnt[depth[v]], 1u);
+  const int32_t d = v < n ? depth[v] : -1;
+  level_add(cnt + (d >= 0 ? d : 0), d, d >= 0);
 }
 
 __global__ void k_level_scatter(const int32_t *__restrict__ depth, uint32_t n,
@@ -891,9 +914,9 @@ __global__ void k_level_scatter(const int32_t *__restrict__ depth, uint32_t n,
                                 uint32_t *__restrict__ ctr,
                                 uint32_t *__restrict__ list) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= n || depth[v] < 0) return;
-  int32_t d = depth[v];
-  list[off[d] + atomicAdd(&ctr[d], 1u)] = v;
+  const int32_t d = v < n ? depth[v] : -1;
+  const uint32_t at = level_add(ctr + (d >= 0 ? d : 0), d, d >= 0);
+  if (d >= 0) list[off[d] + at] = v;
 }
 
 __global__ void k_bc_init(double *__restrict__ sigma, double *__restrict__ ratio,
@@ -1771,17 +1794,14 @@ __global__ void k_msbfs_update(uint32_t n, unsigned long long *__restrict__ vis,
 __global__ void k_msbc_maxdepth(const int32_t *__restrict__ depth, uint32_t n,
                                 unsigned long long *__restrict__ out) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  int32_t d = v < n ? depth[(uint64_t)blockIdx.y * n + v] : -1;
-  for (int o = 16; o > 0; o >>= 1) d = max(d, __shfl_down_sync(0xffffffffu, d, o));
-  if ((threadIdx.x & 31) == 0 && d >= 0) atomicMax(out, (unsigned long long)d);
+  block_max_to(v < n ? depth[(uint64_t)blockIdx.y * n + v] : -1, out);
 }
 
 __global__ void k_msbc_level_count(const int32_t *__restrict__ depth, uint32_t n,
                                    uint32_t L, uint32_t *__restrict__ cnt) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= n) return;
-  int32_t d = depth[(uint64_t)blockIdx.y * n + v];
-  if (d >= 0) atomicAdd(&cnt[blockIdx.y * L + d], 1u);
+  const int32_t d = v < n ? depth[(uint64_t)blockIdx.y * n + v] : -1;
+  level_add(cnt + blockIdx.y * L + (d >= 0 ? d : 0), d, d >= 0);
 }
 
 __global__ void k_msbc_level_scatter(const int32_t *__restrict__ depth,
@@ -1790,11 +1810,10 @@ __global__ void k_msbc_level_scatter(const int32_t *__restrict__ depth,
                                      uint32_t *__restrict__ ctr,
                                      uint32_t *__restrict__ list) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= n) return;
-  int32_t d = depth[(uint64_t)blockIdx.y * n + v];
-  if (d < 0) return;
-  uint32_t at = blockIdx.y * L + d;
-  list[start[at] + atomicAdd(&ctr[at], 1u)] = v;
+  const int32_t d = v < n ? depth[(uint64_t)blockIdx.y * n + v] : -1;
+  const uint32_t a = blockIdx.y * L + (d >= 0 ? d : 0);
+  const uint32_t at = level_add(ctr + a, d, d >= 0);
+  if (d >= 0) list[start[a] + at] = v;
 }
 
 __global__ void k_msbc_init(const uint32_t *__restrict__ srcs, uint32_t n,
