@@ -640,75 +640,55 @@ __global__ void k_front_expand(const uint32_t *__restrict__ q, uint32_t qn,
   }
 }
 
-// push: warp per work item (a frontier vertex's leaf chunk), lane = slot.
-// Newly reached vertices are staged in shared memory (a block's warps can
-// find at most kTB/32 * kChunkLeaves * 32 of them) and the block reserves
-// its stretch of the next queue with one atomic per counter at the end.
+// push: warp per work item (a frontier vertex's leaf chunk), lane = slot;
+// each leaf's newly reached vertices take their queue positions with one
+// atomic per warp, and the warp adds its degree and work-item sums once
 __global__ void k_bfs_push(DGraph g, const uint32_t *__restrict__ iv,
                            const uint32_t *__restrict__ il0, uint32_t nitems,
                            int32_t *__restrict__ depth,
                            int32_t *__restrict__ parent,
                            uint32_t *__restrict__ nq,
                            unsigned long long *__restrict__ cnt, int lvl) {
-  __shared__ uint32_t stage[(kTB / 32) * kChunkLeaves * 32];
-  __shared__ uint32_t s_n;
-  __shared__ unsigned long long s_deg, s_items, s_base;
-  if (threadIdx.x == 0) {
-    s_n = 0;
-    s_deg = 0;
-    s_items = 0;
-  }
-  __syncthreads();
   const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (i < nitems) {
-    const uint32_t u = iv[i];
-    const uint64_t base = g.base[u];
-    const uint32_t cap = g.cap[u], deg = g.deg[u];
-    const uint32_t nl = cap ? nleaves_of(cap) : 0;
-    const uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
-    unsigned long long dsum = 0, isum = 0;
-    for (uint32_t l = l0; l < l1; l++) {
-      const uint32_t c = leaf_count(g, base, cap, deg, l);
-      bool mine = false;
-      uint32_t w = 0;
-      if ((uint32_t)lane < c) {
-        w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
-        if (depth[w] < 0 && atomicCAS(&depth[w], -1, lvl + 1) == -1) {
-          parent[w] = (int32_t)u;
-          mine = true;
-          dsum += g.deg[w];
-          isum += items_of(g.cap[w]);
-        }
-      }
-      const uint32_t m = __ballot_sync(0xffffffffu, mine);
-      if (m) {
-        uint32_t at = 0;
-        if (lane == __ffs(m) - 1) at = atomicAdd(&s_n, (uint32_t)__popc(m));
-        at = __shfl_sync(0xffffffffu, at, __ffs(m) - 1);
-        if (mine) stage[at + __popc(m & ((1u << lane) - 1u))] = w;
+  if (i >= nitems) return;
+  const uint32_t u = iv[i];
+  const uint64_t base = g.base[u];
+  const uint32_t cap = g.cap[u], deg = g.deg[u];
+  const uint32_t nl = cap ? nleaves_of(cap) : 0;
+  const uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+  unsigned long long dsum = 0, isum = 0;
+  for (uint32_t l = l0; l < l1; l++) {
+    const uint32_t c = leaf_count(g, base, cap, deg, l);
+    bool mine = false;
+    uint32_t w = 0;
+    if ((uint32_t)lane < c) {
+      w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
+      if (depth[w] < 0 && atomicCAS(&depth[w], -1, lvl + 1) == -1) {
+        parent[w] = (int32_t)u;
+        mine = true;
+        dsum += g.deg[w];
+        isum += items_of(g.cap[w]);
       }
     }
+    const uint32_t m = __ballot_sync(0xffffffffu, mine);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long at = 0;
+      if (lane == leader) at = atomicAdd(&cnt[0], (unsigned long long)__popc(m));
+      at = __shfl_sync(0xffffffffu, at, leader);
+      if (mine) nq[at + __popc(m & ((1u << lane) - 1u))] = w;
+    }
+  }
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-      dsum += __shfl_xor_sync(0xffffffffu, dsum, d);
-      isum += __shfl_xor_sync(0xffffffffu, isum, d);
-    }
-    if (lane == 0 && (dsum || isum)) {
-      atomicAdd(&s_deg, dsum);
-      atomicAdd(&s_items, isum);
-    }
+  for (int d = 16; d > 0; d >>= 1) {
+    dsum += __shfl_xor_sync(0xffffffffu, dsum, d);
+    isum += __shfl_xor_sync(0xffffffffu, isum, d);
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s_base = s_n ? atomicAdd(&cnt[0], (unsigned long long)s_n) : 0ull;
-    if (s_deg || s_items) {
-      atomicAdd(&cnt[1], s_deg);
-      atomicAdd(&cnt[2], s_items);
-    }
+  if (lane == 0 && (dsum || isum)) {
+    atomicAdd(&cnt[1], dsum);
+    atomicAdd(&cnt[2], isum);
   }
-  __syncthreads();
-  for (uint32_t k = threadIdx.x; k < s_n; k += blockDim.x) nq[s_base + k] = stage[k];
 }
 
 __global__ void k_q2bits(const uint32_t *__restrict__ q, uint32_t qn,
