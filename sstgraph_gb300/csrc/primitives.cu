@@ -1,7 +1,10 @@
 // Stable LSD radix sort of 64-bit keys (8-bit digits) and the launch
-// counter.  Each pass: per-tile digit histograms, one exclusive scan over
-// (digit, tile), then a stable scatter that ranks equal digits with
-// warp match_any + per-warp prefix counts in shared memory.
+// counter.  Each pass: per-tile digit counts, their exclusive scan over
+// (digit, tile), then a stable scatter in which every warp ranks its own
+// contiguous slice of the tile (a digit match from ballots, warp-private
+// counters), the tile is reordered in shared memory and leaves in runs of
+// one digit.  Sorts of up to 64 tiles fold the scan and the next pass's
+// counts into the scatter: one launch a pass.
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
@@ -134,147 +137,266 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kItems = 16;
 constexpr int kTile = kThreads * kItems;  // 4096
 constexpr int kRadix = 256;
+constexpr uint32_t kNoDigit = 0xffffffffu;  // an item past the end
+// Sorts of at most this many tiles run one launch per pass: every block
+// prefixes the raw tile counts itself and counts the next pass's digits as
+// it scatters.  Larger sorts scan the counts in separate launches: there
+// every block's keys of one digit land in the same one or two destination
+// tiles, and atomics on those counters would serialise.
+constexpr uint32_t kFuseHistBlocks = 64;  // 256K keys
 
-// Stable ranking of one iteration's 256 keys (one per thread, in index
-// order).  run[d] holds the next output position for digit d and is
-// advanced.  Returns the output position of this thread's key.
-__device__ __forceinline__ uint32_t rank_iteration(uint32_t d, bool valid,
-                                                   uint32_t (*wcnt)[kRadix],
-                                                   uint32_t *run) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int w = 0; w < kWarps; w++) wcnt[w][threadIdx.x] = 0;
-  __syncthreads();
-  uint32_t key = valid ? d : 0xffffffffu;
-  uint32_t peers = __match_any_sync(0xffffffffu, key);
-  uint32_t lt = peers & ((1u << lane) - 1u);
-  if (valid && lt == 0) wcnt[warp][d] = __popc(peers);
-  __syncthreads();
-  {
-    uint32_t s = run[threadIdx.x];
-#pragma unroll
-    for (int w = 0; w < kWarps; w++) {
-      uint32_t c = wcnt[w][threadIdx.x];
-      wcnt[w][threadIdx.x] = s;
-      s += c;
-    }
-    run[threadIdx.x] = s;
-  }
-  __syncthreads();
-  uint32_t pos = valid ? wcnt[warp][d] + __popc(lt) : 0;
-  __syncthreads();
-  return pos;
+// Offset of this thread's item `it` in a warp-contiguous tile of ITEMS items
+// per thread: warp w owns [w * ITEMS * 32, (w + 1) * ITEMS * 32), item it of
+// lane l sits at w * ITEMS * 32 + it * 32 + l.  Loads stay coalesced, and a
+// warp's items in (it, lane) order are in index order, so a warp ranks its
+// own items without the rest of the block.
+template <int ITEMS>
+__device__ __forceinline__ uint32_t tile_offset(int it) {
+  return (threadIdx.x >> 5) * (ITEMS * 32) + it * 32 + (threadIdx.x & 31);
 }
 
-__global__ void k_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
-                       uint32_t *__restrict__ hist, uint32_t nblocks) {
+// Lanes of the warp holding the same 8-bit digit as this lane (valid lanes
+// only): one ballot per digit bit, each lane keeping the lanes that agree
+// with it on every bit.  Eight ballots issue far faster than one
+// __match_any_sync.
+__device__ __forceinline__ uint32_t same_digit_lanes(uint32_t d, bool valid) {
+  uint32_t m = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    const bool on = (d >> b) & 1u;
+    const uint32_t bb = __ballot_sync(0xffffffffu, on);
+    m &= on ? bb : ~bb;
+  }
+  return m;
+}
+
+// Stable rank of each of the warp's items among the warp's earlier items of
+// the same digit.  wc (the warp's 256 counters, zero and visible to the
+// warp on entry) ends as the warp's count of each digit.  Items past the
+// end carry kNoDigit.
+template <int ITEMS>
+__device__ __forceinline__ void warp_rank(const uint32_t (&dg)[ITEMS],
+                                          uint32_t (&lr)[ITEMS], uint32_t *wc) {
+  const uint32_t below = (1u << (threadIdx.x & 31)) - 1u;
+#pragma unroll
+  for (int it = 0; it < ITEMS; it++) {
+    const uint32_t d = dg[it];
+    const bool valid = d != kNoDigit;
+    const uint32_t peers = same_digit_lanes(d, valid);
+    const uint32_t c = valid ? wc[d] : 0u;
+    lr[it] = c + __popc(peers & below);
+    __syncwarp();
+    if (valid && (peers & below) == 0) wc[d] = c + __popc(peers);
+    __syncwarp();
+  }
+}
+
+// Exclusive scan of one value per thread over the block, in thread order
+// (one __syncthreads inside).
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *wsum) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t o = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= d) inc += o;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  uint32_t off = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) off += w < warp ? wsum[w] : 0u;
+  return off + inc - v;
+}
+
+// Per-tile digit counts at hist[d * dstride + tile * bstride]: digit-major
+// (dstride = tiles, bstride = 1) for the scanned form, tile-major
+// (dstride = 1, bstride = 256) for the fused one.  With `zero` the blocks
+// also clear that table at the same indices.
+__global__ void __launch_bounds__(kThreads)
+k_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
+       uint32_t *__restrict__ hist, uint32_t dstride, uint32_t bstride,
+       uint32_t *__restrict__ zero) {
   __shared__ uint32_t h[kRadix];
   h[threadIdx.x] = 0;
   __syncthreads();
-  uint64_t t0 = (uint64_t)blockIdx.x * kTile;
+  const uint64_t t0 = (uint64_t)blockIdx.x * kTile;
 #pragma unroll 4
   for (int it = 0; it < kItems; it++) {
     uint64_t i = t0 + (uint64_t)it * kThreads + threadIdx.x;
     if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xff], 1u);
   }
   __syncthreads();
-  hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+  const uint64_t at = (uint64_t)threadIdx.x * dstride + (uint64_t)blockIdx.x * bstride;
+  hist[at] = h[threadIdx.x];
+  if (zero) zero[at] = 0;
 }
 
-// Scatter of one pass; with hist_next it also counts the next pass's digit
-// of every key in the tile the key lands in (hist_next zeroed beforehand),
-// so the next pass needs no histogram launch.
-__global__ void k_scatter(const uint64_t *__restrict__ in,
-                          uint64_t *__restrict__ out, uint64_t n, int shift,
-                          const uint32_t *__restrict__ hist, uint32_t nblocks,
-                          const uint32_t *__restrict__ vin,
-                          uint32_t *__restrict__ vout,
-                          uint32_t *__restrict__ hist_next, int next_shift) {
-  __shared__ uint32_t wcnt[kWarps][kRadix];
-  __shared__ uint32_t run[kRadix];
-  run[threadIdx.x] = hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x];
+// One pass's stable scatter of a tile.  The warps rank their slices, the
+// tile is laid out in shared memory in (digit, index) order, and the block
+// writes it out in that order, so the keys of one digit leave as one run of
+// consecutive addresses (whole sectors, not one 8-byte write per lane).
+//  raw: hist holds the raw tile-major counts (hist[tile * 256 + d]); every
+//    block prefixes them itself (all digits below d over all tiles, plus
+//    digit d over the tiles before its own), counts the next pass's digit
+//    of each key into its destination tile's counter of hist_next (zero on
+//    entry) and clears hist_zero (the counters of the pass after next).
+//  otherwise: hist holds the scanned digit-major offsets.
+// Dynamic shared memory: scatter_smem_bytes<KV>().
+template <bool KV>
+constexpr size_t scatter_smem_bytes() {
+  return (size_t)kTile * 8 + (KV ? (size_t)kTile * 4 : 0) +
+         (size_t)kWarps * kRadix * 4 + kRadix * 4 + kWarps * 4;
+}
+
+template <bool KV>
+__global__ void __launch_bounds__(kThreads)
+k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
+          uint64_t n, int shift, const uint32_t *__restrict__ hist,
+          uint32_t nblocks, bool raw, const uint32_t *__restrict__ vin,
+          uint32_t *__restrict__ vout, uint32_t *__restrict__ hist_next,
+          int next_shift, uint32_t *__restrict__ hist_zero) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t *skeys = reinterpret_cast<uint64_t *>(smem);
+  uint32_t *svals = reinterpret_cast<uint32_t *>(smem + (size_t)kTile * 8);
+  uint32_t(*wcnt)[kRadix] = reinterpret_cast<uint32_t(*)[kRadix]>(
+      smem + (size_t)kTile * 8 + (KV ? (size_t)kTile * 4 : 0));
+  uint32_t *adj = &wcnt[kWarps - 1][kRadix - 1] + 1;  // [kRadix]
+  uint32_t *wsum = adj + kRadix;                        // [kWarps]
+  const int warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) wcnt[w][threadIdx.x] = 0;
   // the tile's keys (and values) come in at once, ahead of the ranking
-  // rounds, so the rounds do not wait on memory
   const uint64_t t0 = (uint64_t)blockIdx.x * kTile;
   uint64_t kk[kItems];
-  uint32_t vv[kItems];
+  uint32_t vv[KV ? kItems : 1];
+  uint32_t dg[kItems];
 #pragma unroll
   for (int it = 0; it < kItems; it++) {
-    uint64_t i = t0 + (uint64_t)it * kThreads + threadIdx.x;
+    const uint64_t i = t0 + tile_offset<kItems>(it);
     kk[it] = i < n ? in[i] : 0;
-    vv[it] = (vin && i < n) ? vin[i] : 0u;
+    if (KV) vv[it] = i < n ? vin[i] : 0u;
+    dg[it] = i < n ? (uint32_t)(kk[it] >> shift) & 0xff : kNoDigit;
   }
+  // gbase: output position of this tile's first key of digit threadIdx.x
+  uint32_t gbase;
+  if (raw) {
+    uint32_t before = 0, total = 0;
+#pragma unroll 8
+    for (uint32_t b = 0; b < nblocks; b++) {
+      const uint32_t c = hist[(uint64_t)b * kRadix + threadIdx.x];
+      before += b < blockIdx.x ? c : 0u;
+      total += c;
+    }
+    gbase = block_excl_scan(total, wsum) + before;
+  } else {
+    gbase = hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x];
+    __syncthreads();
+  }
+  uint32_t lr[kItems];
+  warp_rank<kItems>(dg, lr, wcnt[warp]);
+  __syncthreads();
+  // tile-local start of each digit, then of each warp's share of it
+  uint32_t tcount = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) tcount += wcnt[w][threadIdx.x];
+  const uint32_t tstart = block_excl_scan(tcount, wsum);
+  uint32_t s = tstart;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) {
+    const uint32_t c = wcnt[w][threadIdx.x];
+    wcnt[w][threadIdx.x] = s;
+    s += c;
+  }
+  adj[threadIdx.x] = gbase - tstart;  // output position = adj[d] + local
   __syncthreads();
 #pragma unroll
   for (int it = 0; it < kItems; it++) {
-    uint64_t i = t0 + (uint64_t)it * kThreads + threadIdx.x;
-    bool valid = i < n;
-    uint32_t d = (uint32_t)(kk[it] >> shift) & 0xff;
-    uint32_t pos = rank_iteration(d, valid, wcnt, run);
-    if (valid) {
-      out[pos] = kk[it];
-      if (vin) vout[pos] = vv[it];
-      if (hist_next)
-        atomicAdd(&hist_next[(uint64_t)((kk[it] >> next_shift) & 0xff) * nblocks +
-                             pos / kTile],
-                  1u);
-    }
+    if (dg[it] == kNoDigit) continue;
+    const uint32_t lp = wcnt[warp][dg[it]] + lr[it];
+    skeys[lp] = kk[it];
+    if (KV) svals[lp] = vv[it];
+  }
+  __syncthreads();
+  if (hist_zero) hist_zero[(uint64_t)blockIdx.x * kRadix + threadIdx.x] = 0;
+  const uint32_t tn = (uint32_t)(n - t0 < (uint64_t)kTile ? n - t0 : kTile);
+  for (uint32_t j = threadIdx.x; j < tn; j += kThreads) {
+    const uint64_t key = skeys[j];
+    const uint32_t pos = adj[(key >> shift) & 0xff] + j;
+    out[pos] = key;
+    if (KV) vout[pos] = svals[j];
+    if (hist_next)
+      atomicAdd(&hist_next[(uint64_t)(pos / kTile) * kRadix +
+                           ((key >> next_shift) & 0xff)],
+                1u);
   }
 }
 
-// whole sort in one CTA for n <= TILE: keys (and payloads) staged in shared
-// memory
+// The key-value scatter's shared memory is above the 48 KB default: raise
+// its limit once per device (before the first launch there).
+cudaError_t scatter_smem_optin() {
+  static std::atomic<uint64_t> done{0};  // one bit per device below 64
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 64 && ((done.load(std::memory_order_relaxed) >> dev) & 1)) return cudaSuccess;
+  e = cudaFuncSetAttribute(k_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)scatter_smem_bytes<true>());
+  if (e == cudaSuccess && dev < 64) done.fetch_or(1ull << dev, std::memory_order_relaxed);
+  return e;
+}
+
+// Whole sort in one CTA for n <= TILE: keys (and payloads) staged in shared
+// memory; each pass ranks warp-contiguous items as k_scatter does, the digit
+// offsets coming from a block scan of the warps' counts.
 template <bool KV, int TILE>
-__global__ void k_sort_small(uint64_t *__restrict__ keys,
-                             uint32_t *__restrict__ vals, uint64_t n, int bits) {
+__global__ void __launch_bounds__(kThreads)
+k_sort_small(uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
+             uint64_t n, int bits) {
+  constexpr int IT = TILE / kThreads;
   __shared__ uint64_t buf[2][TILE];
   __shared__ uint32_t vbuf[KV ? 2 : 1][KV ? TILE : 1];
   __shared__ uint32_t wcnt[kWarps][kRadix];
-  __shared__ uint32_t run[kRadix];
-  __shared__ uint32_t h[kRadix];
+  __shared__ uint32_t wsum[kWarps];
+  const int warp = threadIdx.x >> 5;
   for (uint64_t i = threadIdx.x; i < n; i += kThreads) {
     buf[0][i] = keys[i];
     if (KV) vbuf[0][i] = vals[i];
   }
   int cur = 0;
   for (int shift = 0; shift < bits; shift += 8) {
-    h[threadIdx.x] = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) wcnt[w][threadIdx.x] = 0;
+    __syncthreads();  // counters clear; the previous pass's keys in place
+    uint64_t kk[IT];
+    uint32_t dg[IT], lr[IT];
+#pragma unroll
+    for (int it = 0; it < IT; it++) {
+      const uint32_t o = tile_offset<IT>(it);
+      kk[it] = o < n ? buf[cur][o] : 0;
+      dg[it] = o < n ? (uint32_t)(kk[it] >> shift) & 0xff : kNoDigit;
+    }
+    warp_rank<IT>(dg, lr, wcnt[warp]);
     __syncthreads();
-    for (uint64_t i = threadIdx.x; i < n; i += kThreads)
-      atomicAdd(&h[(buf[cur][i] >> shift) & 0xff], 1u);
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      // exclusive scan of 256 bins by one warp, 8 bins per lane
-      uint32_t loc[8], s = 0;
+    uint32_t tot = 0;
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        loc[j] = s;
-        s += h[threadIdx.x * 8 + j];
-      }
-      uint32_t inc = s;
+    for (int w = 0; w < kWarps; w++) tot += wcnt[w][threadIdx.x];
+    uint32_t s = block_excl_scan(tot, wsum);
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        uint32_t o = __shfl_up_sync(0xffffffffu, inc, d);
-        if ((int)threadIdx.x >= d) inc += o;
-      }
-      uint32_t excl = inc - s;
-#pragma unroll
-      for (int j = 0; j < 8; j++) run[threadIdx.x * 8 + j] = excl + loc[j];
+    for (int w = 0; w < kWarps; w++) {
+      const uint32_t c = wcnt[w][threadIdx.x];
+      wcnt[w][threadIdx.x] = s;
+      s += c;
     }
     __syncthreads();
-    int iters = (int)((n + kThreads - 1) / kThreads);
-    for (int it = 0; it < iters; it++) {
-      uint64_t i = (uint64_t)it * kThreads + threadIdx.x;
-      bool valid = i < n;
-      uint64_t k = valid ? buf[cur][i] : 0;
-      uint32_t d = (uint32_t)(k >> shift) & 0xff;
-      uint32_t pos = rank_iteration(d, valid, wcnt, run);
-      if (valid) {
-        buf[cur ^ 1][pos] = k;
-        if (KV) vbuf[cur ^ 1][pos] = vbuf[cur][i];
-      }
+#pragma unroll
+    for (int it = 0; it < IT; it++) {
+      if (dg[it] == kNoDigit) continue;
+      const uint32_t pos = wcnt[warp][dg[it]] + lr[it];
+      buf[cur ^ 1][pos] = kk[it];
+      if (KV) vbuf[cur ^ 1][pos] = vbuf[cur][tile_offset<IT>(it)];
     }
-    __syncthreads();
+    __syncthreads();  // all reads of the counters done before the next pass
     cur ^= 1;
   }
   for (uint64_t i = threadIdx.x; i < n; i += kThreads) {
@@ -284,14 +406,13 @@ __global__ void k_sort_small(uint64_t *__restrict__ keys,
 }
 
 constexpr int kSmallSortKV = 1024;
-constexpr uint32_t kFuseHistBlocks = 64;  // 256K keys
 
 }  // namespace
 
 size_t radix_sort_scratch_bytes(uint64_t n) {
   uint64_t nblocks = (n + kTile - 1) / kTile;
   uint64_t hn = nblocks * kRadix;
-  return 2 * ((hn * 4 + 255) & ~size_t(255)) + scan_scratch_bytes(hn, 4) + 512;
+  return 3 * ((hn * 4 + 255) & ~size_t(255)) + scan_scratch_bytes(hn, 4) + 512;
 }
 
 static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
@@ -311,44 +432,67 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
                n, bits);
     return cudaGetLastError();
   }
-  uint32_t nblocks = (uint32_t)((n + kTile - 1) / kTile);
-  uint64_t hn = (uint64_t)nblocks * kRadix;
-  // digit-major tile histograms of this pass and the next (ping-pong)
-  uint32_t *hist = arena.take<uint32_t>(hn);
-  uint32_t *hnext = arena.take<uint32_t>(hn);
-  if (!hist || !hnext) return cudaErrorMemoryAllocation;
+  const uint32_t nblocks = (uint32_t)((n + kTile - 1) / kTile);
+  const uint64_t hn = (uint64_t)nblocks * kRadix;
+  if (vals) {
+    cudaError_t e = scatter_smem_optin();
+    if (e != cudaSuccess) return e;
+  }
   uint64_t *src = keys, *dst = tmp;
   uint32_t *vsrc = vals, *vdst = vtmp;
-  // the first pass's histogram reads the keys; every scatter reads and
-  // writes keys (and values) and touches the tile-digit tables
+  // every scatter reads and writes keys (and values) and reads the counts
   const uint64_t hist_bytes = 8 * n + 4 * hn;
   const uint64_t scatter_bytes = (vals ? 24 : 16) * n + 8 * hn;
-  SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, 0, hist, nblocks);
-  for (int shift = 0; shift < bits; shift += 8) {
-    size_t mark = arena.used;
-    cudaError_t e = scan<uint32_t, OpAdd>(hist, hist, hn, 0u, OpAdd{}, true,
-                                          false, nullptr, arena, s);
-    arena.used = mark;
-    if (e != cudaSuccess) return e;
-    // the next pass's histogram rides on this scatter only for small sorts:
-    // on large ones every block's keys of one digit land in the same one or
-    // two destination tiles, and the atomics on those counters serialise
-    const bool more = shift + 8 < bits;
-    const bool fuse = more && nblocks <= kFuseHistBlocks;
-    if (fuse) {
-      e = cudaMemsetAsync(hnext, 0, hn * 4, s);
-      if (e != cudaSuccess) return e;
+  if (nblocks <= kFuseHistBlocks) {
+    // three tile-major count tables in rotation: pass p reads table p % 3,
+    // counts into (p + 1) % 3 and clears (p + 2) % 3
+    uint32_t *h[3];
+    for (auto &t : h)
+      if (!(t = arena.take<uint32_t>(hn))) return cudaErrorMemoryAllocation;
+    SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, 0, h[0],
+                 1u, (uint32_t)kRadix, h[1]);
+    int p = 0;
+    for (int shift = 0; shift < bits; shift += 8, p++) {
+      const bool more = shift + 8 < bits;
+      uint32_t *nx = more ? h[(p + 1) % 3] : nullptr;
+      uint32_t *zr = more ? h[(p + 2) % 3] : nullptr;
+      if (vals)
+        SST_LAUNCH_B(scatter_bytes, k_scatter<true>, nblocks, kThreads,
+                     scatter_smem_bytes<true>(), s, src,
+                     dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
+                     shift + 8, zr);
+      else
+        SST_LAUNCH_B(scatter_bytes, k_scatter<false>, nblocks, kThreads,
+                     scatter_smem_bytes<false>(), s, src,
+                     dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
+                     shift + 8, zr);
+      std::swap(src, dst);
+      std::swap(vsrc, vdst);
     }
-    SST_LAUNCH_B(scatter_bytes, k_scatter, nblocks, kThreads, 0, s, src, dst, n,
-                 shift, hist, nblocks, vsrc, vdst, fuse ? hnext : nullptr,
-                 shift + 8);
-    std::swap(src, dst);
-    std::swap(vsrc, vdst);
-    // unfused: the next pass's histogram over this pass's output
-    if (more && !fuse)
-      SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, shift + 8,
-                   hnext, nblocks);
-    std::swap(hist, hnext);
+  } else {
+    uint32_t *hist = arena.take<uint32_t>(hn);
+    if (!hist) return cudaErrorMemoryAllocation;
+    for (int shift = 0; shift < bits; shift += 8) {
+      SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, shift,
+                   hist, nblocks, 1u, (uint32_t *)nullptr);
+      size_t mark = arena.used;
+      cudaError_t e = scan<uint32_t, OpAdd>(hist, hist, hn, 0u, OpAdd{}, true,
+                                            false, nullptr, arena, s);
+      arena.used = mark;
+      if (e != cudaSuccess) return e;
+      if (vals)
+        SST_LAUNCH_B(scatter_bytes, k_scatter<true>, nblocks, kThreads,
+                     scatter_smem_bytes<true>(), s, src,
+                     dst, n, shift, hist, nblocks, false, vsrc, vdst,
+                     (uint32_t *)nullptr, 0, (uint32_t *)nullptr);
+      else
+        SST_LAUNCH_B(scatter_bytes, k_scatter<false>, nblocks, kThreads,
+                     scatter_smem_bytes<false>(), s, src,
+                     dst, n, shift, hist, nblocks, false, vsrc, vdst,
+                     (uint32_t *)nullptr, 0, (uint32_t *)nullptr);
+      std::swap(src, dst);
+      std::swap(vsrc, vdst);
+    }
   }
   *result = src;
   if (vresult) *vresult = vsrc;

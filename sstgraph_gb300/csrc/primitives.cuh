@@ -140,6 +140,8 @@ __device__ __forceinline__ T block_exclusive(T v, T identity, Op op, T *total) {
 // second has every block fold the range sums before its own and then scan
 // its range tile by tile with a running carry.  No block waits on another.
 constexpr int kScanRanges = 608;
+// scans of at most this many tiles (32K elements) run as one block
+constexpr uint64_t kScanOneBlockTiles = 8;
 
 // A tile's results leave through shared memory: each thread holds items
 // t*kScanItems .. +kScanItems-1 of the tile, which it writes to a padded
@@ -284,6 +286,14 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
   if (tiles == 1) {
     SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_tile<T, Op>), 1, kScanThreads, 0, s,
                  in, out, n, identity, op, reverse, exclusive, total_out, d_n);
+    return cudaGetLastError();
+  }
+  if (tiles <= kScanOneBlockTiles) {
+    // one block walks the tiles with a running carry: one launch, where the
+    // two-launch form would pay a second launch's latency for little work
+    SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_ranges<T, Op>), 1, kScanThreads, 0,
+                 s, in, out, n, identity, op, reverse, exclusive, tiles,
+                 (const T *)nullptr, total_out, d_n);
     return cudaGetLastError();
   }
   const uint64_t ranges = tiles < (uint64_t)kScanRanges ? tiles : (uint64_t)kScanRanges;

@@ -44,6 +44,29 @@ def test_empty_and_tiny(sg):
     assert g.has(9, 0) and not g.has(1, 2)
 
 
+@pytest.mark.parametrize("b", [2, 1024, 1025, 2048, 2049, 4096, 4097, 100000,
+                               262144, 262145, 400000])
+def test_batch_sizes_across_sort_forms(sg, b):
+    """Batch sizes on both sides of each form of the key sort: one CTA
+    (up to 2048 keys), one launch a pass (up to 64 tiles of 4096 keys) and
+    the scanned form; each batch holds a hub row (skewed high digits) and
+    repeated pairs, and half of it is removed again."""
+    n = 1 << 14
+    rng = np.random.default_rng(b)
+    e = rng.integers(0, n, (b, 2)).astype(np.uint32)
+    e[: b // 8, 0] = 5
+    e[b - b // 10:] = e[: b // 10]
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    g.insert_batch(e)
+    o.insert_batch(e)
+    same(g, o, structure=False)
+    g.remove_batch(e[::2])
+    o.remove_batch(e[::2])
+    same(g, o, structure=False)
+    g.close()
+
+
 def test_invalid_ids_skipped(sg):
     g = sg.SparseMatrixV(8)
     bad = g.insert_batch([[1, 2], [8, 1], [1, 100], [3, 4]])

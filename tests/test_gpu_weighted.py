@@ -66,6 +66,25 @@ def test_random_weighted_stream(sg, seed):
     g.close()
 
 
+@pytest.mark.parametrize("b", [1024, 1025, 4097, 262144, 262145])
+def test_last_value_wins_across_sort_forms(sg, b):
+    """Repeated pairs with different values in one batch, at sizes on both
+    sides of each form of the key-value sort: the sort is stable, so the
+    last value of each pair is the one stored."""
+    n = 1 << 13
+    rng = np.random.default_rng(b)
+    p = rng.integers(0, n, (b, 2)).astype(np.uint32)
+    p[: b // 8, 0] = 3
+    p[b - b // 5:] = p[: b // 5]
+    v = rng.integers(0, 1 << 31, b).astype(np.uint32)
+    g = sg.SparseMatrixV(n, weighted=True)
+    o = WeightedOracle(n)
+    g.insert_batch_weighted(p, v)
+    o.insert_batch(p, v)
+    same(g, o)
+    g.close()
+
+
 def test_overwrite_and_duplicates_in_one_batch(sg):
     g = sg.SparseMatrixV(10, weighted=True)
     g.insert_batch_weighted(np.array([[1, 2], [1, 3], [1, 2]], np.uint32), [5, 6, 7])
