@@ -641,14 +641,16 @@ __global__ void k_front_expand(const uint32_t *__restrict__ q, uint32_t qn,
 }
 
 // push: warp per work item (a frontier vertex's leaf chunk), lane = slot;
-// each leaf's newly reached vertices take their queue positions with one
-// atomic per warp, and the warp adds its degree and work-item sums once
-__global__ void k_bfs_push(DGraph g, const uint32_t *__restrict__ iv,
-                           const uint32_t *__restrict__ il0, uint32_t nitems,
-                           int32_t *__restrict__ depth,
-                           int32_t *__restrict__ parent,
-                           uint32_t *__restrict__ nq,
-                           unsigned long long *__restrict__ cnt, int lvl) {
+// four leaves' slots, depths and claims are in flight at once, their newly
+// reached vertices take queue positions with one atomic per warp and batch,
+// and the warp adds its degree and work-item sums once
+__global__ void __launch_bounds__(kTB, 8)
+k_bfs_push(DGraph g, const uint32_t *__restrict__ iv,
+           const uint32_t *__restrict__ il0, uint32_t nitems,
+           int32_t *__restrict__ depth, int32_t *__restrict__ parent,
+           uint32_t *__restrict__ nq, unsigned long long *__restrict__ cnt,
+           int lvl) {
+  constexpr int kBatch = 4;  // leaves whose slots are in flight at once
   const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (i >= nitems) return;
@@ -657,27 +659,47 @@ __global__ void k_bfs_push(DGraph g, const uint32_t *__restrict__ iv,
   const uint32_t cap = g.cap[u], deg = g.deg[u];
   const uint32_t nl = cap ? nleaves_of(cap) : 0;
   const uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+  // a one-leaf segment holds deg ids; a multi-leaf segment's leaves hold
+  // their ids packed left with EMPTY after them, so no leaf counts are read
+  const uint32_t lim = cap <= kLeaf ? deg : kLeaf;
+  const uint32_t below = (1u << lane) - 1u;
   unsigned long long dsum = 0, isum = 0;
-  for (uint32_t l = l0; l < l1; l++) {
-    const uint32_t c = leaf_count(g, base, cap, deg, l);
-    bool mine = false;
-    uint32_t w = 0;
-    if ((uint32_t)lane < c) {
-      w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
-      if (depth[w] < 0 && atomicCAS(&depth[w], -1, lvl + 1) == -1) {
-        parent[w] = (int32_t)u;
-        mine = true;
-        dsum += g.deg[w];
-        isum += items_of(g.cap[w]);
-      }
+  for (uint32_t l = l0; l < l1; l += kBatch) {
+    uint32_t w[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; k++)
+      w[k] = (l + k < l1 && (uint32_t)lane < lim)
+                 ? g.slots[base + ((uint64_t)(l + k) << kLeafLog) + lane]
+                 : kEmpty;
+    int32_t dd[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; k++) dd[k] = w[k] != kEmpty ? depth[w[k]] : 0;
+    uint32_t mine = 0;  // bit k: this lane claimed w[k]
+#pragma unroll
+    for (int k = 0; k < kBatch; k++)
+      if (dd[k] < 0 && atomicCAS(&depth[w[k]], -1, lvl + 1) == -1)
+        mine |= 1u << k;
+    // one queue reservation per batch, in (leaf, lane) order; leaves past
+    // the chunk's end (warp-uniform) take no ballot
+    uint32_t mm[kBatch], total = 0;
+#pragma unroll
+    for (int k = 0; k < kBatch; k++) {
+      mm[k] = l + k < l1 ? __ballot_sync(0xffffffffu, (mine >> k) & 1u) : 0u;
+      total += __popc(mm[k]);
     }
-    const uint32_t m = __ballot_sync(0xffffffffu, mine);
-    if (m) {
-      const int leader = __ffs(m) - 1;
-      unsigned long long at = 0;
-      if (lane == leader) at = atomicAdd(&cnt[0], (unsigned long long)__popc(m));
-      at = __shfl_sync(0xffffffffu, at, leader);
-      if (mine) nq[at + __popc(m & ((1u << lane) - 1u))] = w;
+    if (total == 0) continue;
+    unsigned long long at = 0;
+    if (lane == 0) at = atomicAdd(&cnt[0], (unsigned long long)total);
+    at = __shfl_sync(0xffffffffu, at, 0);
+#pragma unroll
+    for (int k = 0; k < kBatch; k++) {
+      if ((mine >> k) & 1u) {
+        nq[at + __popc(mm[k] & below)] = w[k];
+        parent[w[k]] = (int32_t)u;
+        dsum += g.deg[w[k]];
+        isum += items_of(g.cap[w[k]]);
+      }
+      at += __popc(mm[k]);
     }
   }
 #pragma unroll
@@ -1646,11 +1668,12 @@ __global__ void k_msbfs_seed(const uint32_t *__restrict__ sv,
 }
 
 // push: warp per work item (a frontier vertex's leaf chunk), lane = slot
-__global__ void k_msbfs_push(DGraph g, const uint32_t *__restrict__ iv,
-                             const uint32_t *__restrict__ il0, uint32_t nitems,
-                             const unsigned long long *__restrict__ fr,
-                             const unsigned long long *__restrict__ vis,
-                             unsigned long long *__restrict__ nx) {
+__global__ void __launch_bounds__(kTB, 8)
+k_msbfs_push(DGraph g, const uint32_t *__restrict__ iv,
+             const uint32_t *__restrict__ il0, uint32_t nitems,
+             const unsigned long long *__restrict__ fr,
+             const unsigned long long *__restrict__ vis,
+             unsigned long long *__restrict__ nx) {
   uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (i >= nitems) return;
@@ -1660,13 +1683,23 @@ __global__ void k_msbfs_push(DGraph g, const uint32_t *__restrict__ iv,
   uint32_t cap = g.cap[u], deg = g.deg[u];
   uint32_t nl = cap ? nleaves_of(cap) : 0;
   uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
-  for (uint32_t l = l0; l < l1; l++) {
-    uint32_t c = leaf_count(g, base, cap, deg, l);
-    if ((uint32_t)lane < c) {
-      uint32_t w = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
-      unsigned long long add = f & ~vis[w];
-      if (add) atomicOr(&nx[w], add);
-    }
+  // four leaves' slots and visited masks in flight at once; leaves keep
+  // their ids packed left with EMPTY after them
+  constexpr int kBatch = 4;
+  const uint32_t lim = cap <= kLeaf ? deg : kLeaf;
+  for (uint32_t l = l0; l < l1; l += kBatch) {
+    uint32_t w[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; k++)
+      w[k] = (l + k < l1 && (uint32_t)lane < lim)
+                 ? g.slots[base + ((uint64_t)(l + k) << kLeafLog) + lane]
+                 : kEmpty;
+    unsigned long long add[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; k++) add[k] = w[k] != kEmpty ? f & ~vis[w[k]] : 0ull;
+#pragma unroll
+    for (int k = 0; k < kBatch; k++)
+      if (add[k]) atomicOr(&nx[w[k]], add[k]);
   }
 }
 
@@ -1843,13 +1876,25 @@ __global__ void k_msbc_chunks(DGraph g, const uint32_t *__restrict__ iv,
   uint32_t nl = g.cap[v] >> kLeafLog;
   uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
   uint64_t base = g.base[v];
-  const uint8_t *lc = g.lcnt + (base >> kLeafLog);
+  // eight leaves' slots, depths and values in flight at once (the leaves of
+  // a multi-leaf segment keep their ids packed left with EMPTY after them);
+  // each lane still adds in leaf order
+  constexpr int kBatch = 8;
   double acc = 0.0;
-  for (uint32_t l = l0; l < l1; l++) {
-    if ((uint32_t)lane < lc[l]) {
-      uint32_t u = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
-      if (depth[so + u] == want) acc += val[so + u];
-    }
+  for (uint32_t l = l0; l < l1; l += kBatch) {
+    uint32_t u[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; k++)
+      u[k] = l + k < l1 ? g.slots[base + ((uint64_t)(l + k) << kLeafLog) + lane] : kEmpty;
+    bool on[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; k++) on[k] = u[k] != kEmpty && depth[so + u[k]] == want;
+    double x[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; k++) x[k] = on[k] ? val[so + u[k]] : 0.0;
+#pragma unroll
+    for (int k = 0; k < kBatch; k++)
+      if (on[k]) acc += x[k];
   }
   double sum = warp_sum_d(acc);
   if (lane == 0) partial[i] = sum;
@@ -2272,12 +2317,13 @@ __global__ void k_bf_init(unsigned long long *__restrict__ dist,
   stamp[v] = 0;
 }
 
-__global__ void k_bf_push(DGraph g, const uint32_t *__restrict__ iv,
-                          const uint32_t *__restrict__ il0, uint32_t nitems,
-                          unsigned long long *__restrict__ dist,
-                          uint32_t *__restrict__ stamp, uint32_t round,
-                          uint32_t *__restrict__ nq,
-                          unsigned long long *__restrict__ cnt) {
+__global__ void __launch_bounds__(kTB, 5)
+k_bf_push(DGraph g, const uint32_t *__restrict__ iv,
+          const uint32_t *__restrict__ il0, uint32_t nitems,
+          unsigned long long *__restrict__ dist,
+          uint32_t *__restrict__ stamp, uint32_t round,
+          uint32_t *__restrict__ nq,
+          unsigned long long *__restrict__ cnt) {
   // next-round vertices staged in shared memory, one queue reservation per
   // block (as in the BFS push)
   __shared__ uint32_t stage[(kTB / 32) * kChunkLeaves * 32];
@@ -2299,27 +2345,49 @@ __global__ void k_bf_push(DGraph g, const uint32_t *__restrict__ iv,
     const uint32_t nl = cap ? nleaves_of(cap) : 0;
     const uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
     unsigned long long dsum = 0, isum = 0;
-    for (uint32_t l = l0; l < l1; l++) {
-      const uint32_t c = leaf_count(g, base, cap, deg, l);
-      bool mine = false;
-      uint32_t v = 0;
-      if ((uint32_t)lane < c) {
-        const uint64_t at = base + ((uint64_t)l << kLeafLog) + lane;
-        v = g.slots[at];
-        const unsigned long long nd = du + g.vals[at];
-        if (nd < __ldcg(dist + v) && atomicMin(dist + v, nd) > nd &&
-            atomicExch(stamp + v, round) != round) {
-          mine = true;
-          dsum += g.deg[v];
-          isum += items_of(g.cap[v]);
-        }
+    // four leaves' slots, lengths and distances in flight at once; leaves
+    // keep their ids packed left with EMPTY after them
+    constexpr int kBatch = 4;
+    const uint32_t lim = cap <= kLeaf ? deg : kLeaf;
+    const uint32_t below = (1u << lane) - 1u;
+    for (uint32_t l = l0; l < l1; l += kBatch) {
+      uint32_t v[kBatch], len[kBatch];
+#pragma unroll
+      for (int k = 0; k < kBatch; k++) {
+        const uint64_t at = base + ((uint64_t)(l + k) << kLeafLog) + lane;
+        const bool in = l + k < l1 && (uint32_t)lane < lim;
+        v[k] = in ? g.slots[at] : kEmpty;
+        len[k] = in ? g.vals[at] : 0u;
       }
-      const uint32_t m = __ballot_sync(0xffffffffu, mine);
-      if (m) {
-        uint32_t at = 0;
-        if (lane == __ffs(m) - 1) at = atomicAdd(&s_n, (uint32_t)__popc(m));
-        at = __shfl_sync(0xffffffffu, at, __ffs(m) - 1);
-        if (mine) stage[at + __popc(m & ((1u << lane) - 1u))] = v;
+      unsigned long long dv[kBatch];
+#pragma unroll
+      for (int k = 0; k < kBatch; k++) dv[k] = v[k] != kEmpty ? __ldcg(dist + v[k]) : 0ull;
+      uint32_t mine = 0;  // bit k: this lane enqueues v[k]
+#pragma unroll
+      for (int k = 0; k < kBatch; k++) {
+        const unsigned long long nd = du + len[k];
+        if (v[k] != kEmpty && nd < dv[k] && atomicMin(dist + v[k], nd) > nd &&
+            atomicExch(stamp + v[k], round) != round)
+          mine |= 1u << k;
+      }
+      uint32_t mm[kBatch], total = 0;
+#pragma unroll
+      for (int k = 0; k < kBatch; k++) {
+        mm[k] = l + k < l1 ? __ballot_sync(0xffffffffu, (mine >> k) & 1u) : 0u;
+        total += __popc(mm[k]);
+      }
+      if (total == 0) continue;
+      uint32_t at = 0;
+      if (lane == 0) at = atomicAdd(&s_n, total);
+      at = __shfl_sync(0xffffffffu, at, 0);
+#pragma unroll
+      for (int k = 0; k < kBatch; k++) {
+        if ((mine >> k) & 1u) {
+          stage[at + __popc(mm[k] & below)] = v[k];
+          dsum += g.deg[v[k]];
+          isum += items_of(g.cap[v[k]]);
+        }
+        at += __popc(mm[k]);
       }
     }
 #pragma unroll
