@@ -1260,12 +1260,15 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   // 7: dominance
   SST_LAUNCH(k_dom_keys, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
              gw0, gw1, &P->n_groups, b, fkey, bkey);
-  SST_CUDA_TRY((scan<uint64_t, OpMax>(fkey, fkey, b, 0ull, OpMax{}, true, false,
+  // the scans run out of place into merge_jk and mtpos, which hold nothing
+  // until the merge/task scan and k_emit below overwrite them
+  uint64_t *fscan = merge_jk, *bscan = mtpos;
+  SST_CUDA_TRY((scan<uint64_t, OpMax>(fkey, fscan, b, 0ull, OpMax{}, true, false,
                                       nullptr, A, s)));
-  SST_CUDA_TRY((scan<uint64_t, OpMin>(bkey, bkey, b, ~0ull, OpMin{}, true, true,
+  SST_CUDA_TRY((scan<uint64_t, OpMin>(bkey, bscan, b, ~0ull, OpMin{}, true, true,
                                       nullptr, A, s)));
   SST_LAUNCH(k_dom_classify, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
-             fkey, bkey, &P->n_groups, b, mt);
+             fscan, bscan, &P->n_groups, b, mt);
   // totals land as one word on (n_merge, n_tasks), adjacent in the plan
   static_assert(offsetof(PlanSummary, n_tasks) == offsetof(PlanSummary, n_merge) + 4 &&
                     offsetof(PlanSummary, n_merge) % 8 == 0,

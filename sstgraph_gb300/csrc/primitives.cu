@@ -25,6 +25,13 @@ void note_launches(int64_t k) {
 }
 uint64_t launches() { return g_launches.load(std::memory_order_relaxed); }
 
+static std::atomic<unsigned long long> g_scan_epoch{0};
+unsigned long long next_scan_tag() {
+  const unsigned long long e =
+      (g_scan_epoch.fetch_add(1, std::memory_order_relaxed) + 1) & kScanEpochMask;
+  return kScanTag | (e << 2);
+}
+
 // ------------------------------------------------------------- profiler
 namespace {
 struct Pending {
@@ -470,13 +477,16 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
       std::swap(vsrc, vdst);
     }
   } else {
+    // counts and their scan in separate tables (the single-pass scan runs
+    // out of place)
+    uint32_t *cnts = arena.take<uint32_t>(hn);
     uint32_t *hist = arena.take<uint32_t>(hn);
-    if (!hist) return cudaErrorMemoryAllocation;
+    if (!cnts || !hist) return cudaErrorMemoryAllocation;
     for (int shift = 0; shift < bits; shift += 8) {
       SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, shift,
-                   hist, nblocks, 1u, (uint32_t *)nullptr);
+                   cnts, nblocks, 1u, (uint32_t *)nullptr);
       size_t mark = arena.used;
-      cudaError_t e = scan<uint32_t, OpAdd>(hist, hist, hn, 0u, OpAdd{}, true,
+      cudaError_t e = scan<uint32_t, OpAdd>(cnts, hist, hn, 0u, OpAdd{}, true,
                                             false, nullptr, arena, s);
       arena.used = mark;
       if (e != cudaSuccess) return e;

@@ -14,6 +14,8 @@ namespace sst {
 void note_launch();
 void note_launches(int64_t k);
 uint64_t launches();
+// a tag unique to one single-pass scan launch (see ScanStatus)
+unsigned long long next_scan_tag();
 
 // Kernel profiler: while enabled, every launch is bracketed by a pair of
 // CUDA events on its own stream; profile_collect() folds the elapsed times
@@ -270,6 +272,172 @@ __global__ void k_scan_tile(const T *__restrict__ in, T *__restrict__ out,
   if (total_out && threadIdx.x == 0) *total_out = total;
 }
 
+// ------------------------------------------------- single-pass scan
+// Status of one tile of the single-pass scan.  flag = tag | state, where the
+// tag (kScanTag | epoch << 2) is unique to the launch: a flag left in the
+// same memory by an earlier launch, or by whatever the arena held there
+// before, never matches.  State 1: agg holds the tile's reduction; state 2:
+// incl holds the reduction of every tile up to and including this one.
+// The two values sit in separate fields, so a reader that saw state 1 reads
+// an aggregate that is never overwritten.
+template <typename T>
+struct ScanStatus {
+  unsigned long long flag;
+  T agg;
+  T incl;
+};
+constexpr unsigned long long kScanTag = 0x5CA5ull << 48;
+constexpr unsigned long long kScanEpochMask = (1ull << 46) - 1;
+// polls of one predecessor's flag (with a growing sleep) before a tile stops
+// waiting and reduces the inputs of the tiles it still lacks itself
+constexpr int kLookbackPolls = 1 << 13;
+
+template <typename T>
+__device__ __forceinline__ void scan_publish(ScanStatus<T> *s,
+                                             unsigned long long tag, int state,
+                                             T v) {
+  if (state == 1)
+    *(volatile T *)&s->agg = v;
+  else
+    *(volatile T *)&s->incl = v;
+  __threadfence();
+  *(volatile unsigned long long *)&s->flag = tag | (unsigned long long)state;
+}
+
+template <typename T, typename Op>
+__device__ __forceinline__ T warp_reduce_all(T v, Op op) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, d));
+  return v;
+}
+
+// The reduction of tiles 0 .. tile-1, by the whole block of tile `tile`
+// (> 0).  Each round thread k reads the flag of the tile k + 1 below the
+// nearest tile not folded in yet, and the block folds every tile down to the
+// nearest inclusive prefix (or all 256 when there is none and goes on).
+// Every wait is bounded: if a predecessor that is needed has not published
+// in time, the block reduces the inputs of tiles 0 .. j itself (the scan is
+// out of place, so the inputs are intact).
+template <typename T, typename Op>
+__device__ T scan_lookback(const ScanStatus<T> *st, uint64_t tile,
+                           unsigned long long tag, T identity, Op op,
+                           const T *in, uint64_t n, bool reverse) {
+  __shared__ int s_stop, s_fail;
+  __shared__ T s_part[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T excl = identity;
+  int64_t j = (int64_t)tile - 1;  // nearest tile not folded in yet
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_stop = kScanThreads;
+      s_fail = kScanThreads;
+    }
+    const int64_t t = j - (int64_t)threadIdx.x;
+    // tiles below tile 0 act as an empty inclusive prefix
+    unsigned long long f = tag | 2ull;
+    if (t >= 0) {
+      for (int p = 0;; p++) {
+        f = *(volatile const unsigned long long *)&st[t].flag;
+        if ((f & ~3ull) == tag && (f & 3ull) != 0) break;
+        if (p == kLookbackPolls) {
+          f = 0;
+          break;
+        }
+        __nanosleep(p < 64 ? 32 : 512);
+      }
+    }
+    __syncthreads();  // s_stop / s_fail set
+    if ((f & 3ull) == 2ull) atomicMin(&s_stop, (int)threadIdx.x);
+    if (f == 0) atomicMin(&s_fail, (int)threadIdx.x);
+    __syncthreads();
+    const int stop = s_stop, fail = s_fail;
+    if (fail <= stop && fail < kScanThreads) {
+      // a needed predecessor never published: reduce its inputs and all below
+      T a = identity;
+      const uint64_t end = (uint64_t)(j + 1) * kScanTile;
+      for (uint64_t i = threadIdx.x; i < end; i += kScanThreads)
+        a = op(a, scan_load(in, i, n, reverse, identity));
+      a = warp_reduce_all(a, op);
+      if (lane == 0) s_part[warp] = a;
+      __syncthreads();
+      T r = identity;
+#pragma unroll
+      for (int w = 0; w < kScanThreads / 32; w++) r = op(r, s_part[w]);
+      return op(r, excl);
+    }
+    __threadfence();
+    T v = identity;
+    if ((int)threadIdx.x <= stop && t >= 0)
+      v = (int)threadIdx.x == stop ? *(volatile const T *)&st[t].incl
+                                   : *(volatile const T *)&st[t].agg;
+    v = warp_reduce_all(v, op);
+    if (lane == 0) s_part[warp] = v;
+    __syncthreads();
+    T r = identity;
+#pragma unroll
+    for (int w = 0; w < kScanThreads / 32; w++) r = op(r, s_part[w]);
+    excl = op(r, excl);
+    if (stop < kScanThreads) return excl;
+    j -= kScanThreads;
+    __syncthreads();  // s_part read by every thread before the next round
+  }
+}
+
+// Single-pass scan (out of place): block b scans tile b, publishes its
+// aggregate, looks back for its prefix and publishes its inclusive prefix.
+// Tile b waits only on the aggregates of tiles below it, which the hardware
+// starts first and which depend on nothing.
+template <typename T, typename Op>
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_lb(const T *__restrict__ in, T *__restrict__ out, uint64_t n,
+          T identity, Op op, bool reverse, bool exclusive,
+          T *__restrict__ total_out, const uint32_t *__restrict__ d_n,
+          ScanStatus<T> *st, unsigned long long tag) {
+  if (d_n && *d_n < n) n = *d_n;
+  const uint64_t tile = blockIdx.x, base = tile * kScanTile;
+  if (base >= n) {
+    if (tile == 0 && total_out && threadIdx.x == 0) *total_out = identity;
+    return;
+  }
+  T vals[kScanItems];
+  T acc = identity;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    vals[k] = scan_load(in, base + (uint64_t)threadIdx.x * kScanItems + k, n,
+                        reverse, identity);
+    acc = op(acc, vals[k]);
+  }
+  T total;
+  T run = block_exclusive(acc, identity, op, &total);
+  T carry = identity;
+  if (tile == 0) {
+    if (threadIdx.x == 0) scan_publish(&st[0], tag, 2, total);
+  } else {
+    if (threadIdx.x == 0) scan_publish(&st[tile], tag, 1, total);
+    carry = scan_lookback(st, tile, tag, identity, op, in, n, reverse);
+    if (threadIdx.x == 0) scan_publish(&st[tile], tag, 2, op(carry, total));
+  }
+  run = op(carry, run);
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    T nxt = op(run, vals[k]);
+    vals[k] = exclusive ? run : nxt;
+    run = nxt;
+  }
+  store_tile(out, base, n, reverse, vals);
+  if (total_out && threadIdx.x == 0 && n - base <= (uint64_t)kScanTile)
+    *total_out = op(carry, total);
+}
+
+inline bool stream_capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+    cudaGetLastError();
+    return true;  // unknown: take the form that needs no per-launch tag
+  }
+  return cs != cudaStreamCaptureStatusNone;
+}
+
 // Scan of n elements (in may equal out).  total_out (device, may be null)
 // receives the reduction of all n elements.  With d_n (device, may be null)
 // only the first min(n, *d_n) elements are scanned; n sizes the launch.
@@ -287,6 +455,18 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
     SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_tile<T, Op>), 1, kScanThreads, 0, s,
                  in, out, n, identity, op, reverse, exclusive, total_out, d_n);
     return cudaGetLastError();
+  }
+  // one launch with look-back, unless the scan is in place (the bounded
+  // look-back's fallback rereads inputs) or being captured into a graph (a
+  // replay would reuse the launch's tag)
+  if (in != out && !stream_capturing(s)) {
+    ScanStatus<T> *st = arena.take<ScanStatus<T>>(tiles);
+    if (st) {
+      SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_lb<T, Op>), (unsigned)tiles,
+                   kScanThreads, 0, s, in, out, n, identity, op, reverse,
+                   exclusive, total_out, d_n, st, next_scan_tag());
+      return cudaGetLastError();
+    }
   }
   if (tiles <= kScanOneBlockTiles) {
     // one block walks the tiles with a running carry: one launch, where the
@@ -310,10 +490,14 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
   return cudaGetLastError();
 }
 
-// scratch bytes a scan of n elements of T takes from the arena
+// scratch bytes a scan of n elements of T takes from the arena: the tile
+// status of the single-pass form (8 + 2 * elem bytes a tile), else the range
+// sums of the two-launch form
 inline size_t scan_scratch_bytes(uint64_t n, size_t elem) {
-  (void)n;
-  return ((kScanRanges * elem + 255) & ~size_t(255)) + 256;
+  const uint64_t tiles = (n + kScanTile - 1) / kScanTile;
+  const size_t st = (tiles * (8 + 2 * elem) + 255) & ~size_t(255);
+  const size_t rs = ((kScanRanges * elem + 255) & ~size_t(255)) + 256;
+  return st > rs ? st : rs;
 }
 
 // ----------------------------------------------------------- radix sort
