@@ -384,44 +384,61 @@ def main():
             del out
         return res
 
-    def measure_batched():
+    def measure_batched(reps=3):
         """The same stream of uneven insert batches (log-normal sizes, median
         1e4, sigma 1.5, clipped to [1e3, 1e6]) applied to two device copies of
         the graph: one insert_batch call per batch (plain form) vs one
-        update_batches call for the whole stream (batched form)."""
+        update_batches call for the whole stream (batched form).  Each copy
+        first takes a disjoint warm-up stream of the same sizes in the same
+        form (untimed: scratch grown, kernels loaded), so the timed stream
+        measures the steady state; median of `reps` copies per form."""
         rng = np.random.default_rng(11)
         sizes = np.clip(rng.lognormal(np.log(1e4), 1.5, a.batched_batches),
                         1e3, 1e6).astype(np.int64)
-        bl = []
-        first = 0
-        with torch.cuda.stream(stream):
-            for sz in sizes.tolist():
-                x = torch.empty((sz, 2), dtype=torch.int32, device="cuda")
-                sg.gen_rmat(a.scale, sz, seed=12, first=first, out=x, **RMAT)
-                first += sz
-                bl.append(x)
-        torch.cuda.synchronize()
+
+        def stream_of(first):
+            out = []
+            with torch.cuda.stream(stream):
+                for sz in sizes.tolist():
+                    x = torch.empty((sz, 2), dtype=torch.int32, device="cuda")
+                    sg.gen_rmat(a.scale, sz, seed=12, first=first, out=x, **RMAT)
+                    first += sz
+                    out.append(x)
+            return out
+
         total_e = int(sizes.sum())
+        warm, bl = stream_of(0), stream_of(total_e)
+        torch.cuda.synchronize()
         res = {}
         for form in ("plain", "batched"):
-            gc = g.copy()
-            gc.set_stream(stream.cuda_stream)
-            torch.cuda.synchronize()
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            if form == "plain":
-                for x in bl:
-                    gc.insert_batch(x)
-            else:
-                gc.update_batches(bl)
-            s1.record(stream)
-            s1.synchronize()
-            t = s0.elapsed_time(s1) / 1e3
-            res[form] = {"edges_per_s": total_e / t, "s": t,
-                         "check": [gc.M(), gc.touch_all_sum()]}
-            gc.close()
-        same = res["plain"]["check"] == res["batched"]["check"]
-        return {"batches": len(bl), "edges": total_e,
+            times, checks = [], []
+            for _ in range(reps):
+                gc = g.copy()
+                gc.set_stream(stream.cuda_stream)
+                if form == "plain":
+                    for x in warm:
+                        gc.insert_batch(x)
+                else:
+                    gc.update_batches(warm)
+                torch.cuda.synchronize()
+                s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s0.record(stream)
+                if form == "plain":
+                    for x in bl:
+                        gc.insert_batch(x)
+                else:
+                    gc.update_batches(bl)
+                s1.record(stream)
+                s1.synchronize()
+                times.append(s0.elapsed_time(s1) / 1e3)
+                checks.append([gc.M(), gc.touch_all_sum()])
+                gc.close()
+            t = float(np.median(times))
+            res[form] = {"edges_per_s": total_e / t, "s": t, "check": checks[0],
+                         "same_each_rep": all(c == checks[0] for c in checks)}
+        same = (res["plain"]["check"] == res["batched"]["check"] and
+                res["plain"]["same_each_rep"] and res["batched"]["same_each_rep"])
+        return {"batches": len(bl), "edges": total_e, "reps": reps,
                 "sizes": {"min": int(sizes.min()), "median": int(np.median(sizes)),
                           "max": int(sizes.max())},
                 "plain_edges_per_s": res["plain"]["edges_per_s"],
