@@ -19,6 +19,9 @@ namespace sst {
 namespace {
 constexpr int kTB = 256;
 constexpr uint32_t kChunkLeaves = 32;
+// leaves per work item of the push-style kernels (frontier expansion):
+// smaller than kChunkLeaves so a hub's chunks spread over more warps
+constexpr uint32_t kPushLeaves = 8;
 
 inline unsigned blocks_for(uint64_t n, int per = kTB) {
   uint64_t b = (n + per - 1) / per;
@@ -613,10 +616,10 @@ __device__ __forceinline__ void enqueue_block(bool mine, uint32_t w, uint32_t wd
   if (mine) q[s_base + s_cnt[warp] + __popc(m & ((1u << lane) - 1u))] = w;
 }
 
-// work items of one vertex: 1 for a one-leaf segment, else one per chunk
-// of kChunkLeaves leaves
+// push work items of one vertex: 1 for a one-leaf segment, else one per
+// chunk of kPushLeaves leaves
 __device__ __forceinline__ uint32_t items_of(uint32_t cap) {
-  return cap > kLeaf ? ((cap >> kLeafLog) + kChunkLeaves - 1) / kChunkLeaves : 1u;
+  return cap > kLeaf ? ((cap >> kLeafLog) + kPushLeaves - 1) / kPushLeaves : 1u;
 }
 
 __global__ void k_front_items(const uint32_t *__restrict__ q, uint32_t qn,
@@ -636,7 +639,7 @@ __global__ void k_front_expand(const uint32_t *__restrict__ q, uint32_t qn,
   uint32_t v = q[i], k = items_of(cap[v]), o = off[i];
   for (uint32_t j = 0; j < k; j++) {
     iv[o + j] = v;
-    il0[o + j] = j * kChunkLeaves;
+    il0[o + j] = j * kPushLeaves;
   }
 }
 
@@ -658,7 +661,7 @@ k_bfs_push(DGraph g, const uint32_t *__restrict__ iv,
   const uint64_t base = g.base[u];
   const uint32_t cap = g.cap[u], deg = g.deg[u];
   const uint32_t nl = cap ? nleaves_of(cap) : 0;
-  const uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+  const uint32_t l0 = il0[i], l1 = min(l0 + kPushLeaves, nl);
   // a one-leaf segment holds deg ids; a multi-leaf segment's leaves hold
   // their ids packed left with EMPTY after them, so no leaf counts are read
   const uint32_t lim = cap <= kLeaf ? deg : kLeaf;
@@ -1429,7 +1432,7 @@ sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths
   SST_CUDA_TRY(cudaMemcpyAsync(&sinfo[1], g->d_cap + src, 4, cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   uint64_t qn = 1, qdeg = sinfo[0];
-  uint64_t qitems = sinfo[1] > kLeaf ? ((sinfo[1] >> kLeafLog) + kChunkLeaves - 1) / kChunkLeaves : 1;
+  uint64_t qitems = sinfo[1] > kLeaf ? ((sinfo[1] >> kLeafLog) + kPushLeaves - 1) / kPushLeaves : 1;
   uint32_t *q = t->qa.p, *nq = t->qb.p;
   unsigned long long *cnt = t->d_small;
   const uint64_t m = g->m;
@@ -1682,7 +1685,7 @@ k_msbfs_push(DGraph g, const uint32_t *__restrict__ iv,
   uint64_t base = g.base[u];
   uint32_t cap = g.cap[u], deg = g.deg[u];
   uint32_t nl = cap ? nleaves_of(cap) : 0;
-  uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+  uint32_t l0 = il0[i], l1 = min(l0 + kPushLeaves, nl);
   // four leaves' slots and visited masks in flight at once; leaves keep
   // their ids packed left with EMPTY after them
   constexpr int kBatch = 4;
@@ -2326,7 +2329,7 @@ k_bf_push(DGraph g, const uint32_t *__restrict__ iv,
           unsigned long long *__restrict__ cnt) {
   // next-round vertices staged in shared memory, one queue reservation per
   // block (as in the BFS push)
-  __shared__ uint32_t stage[(kTB / 32) * kChunkLeaves * 32];
+  __shared__ uint32_t stage[(kTB / 32) * kPushLeaves * 32];
   __shared__ uint32_t s_n;
   __shared__ unsigned long long s_deg, s_items, s_base;
   if (threadIdx.x == 0) {
@@ -2343,7 +2346,7 @@ k_bf_push(DGraph g, const uint32_t *__restrict__ iv,
     const uint64_t base = g.base[u];
     const uint32_t cap = g.cap[u], deg = g.deg[u];
     const uint32_t nl = cap ? nleaves_of(cap) : 0;
-    const uint32_t l0 = il0[i], l1 = min(l0 + kChunkLeaves, nl);
+    const uint32_t l0 = il0[i], l1 = min(l0 + kPushLeaves, nl);
     unsigned long long dsum = 0, isum = 0;
     // four leaves' slots, lengths and distances in flight at once; leaves
     // keep their ids packed left with EMPTY after them
@@ -2422,7 +2425,7 @@ __global__ void k_bf_out(const unsigned long long *__restrict__ dist, uint32_t n
 }  // namespace
 
 static uint64_t items_of_host(uint32_t cap) {
-  return cap > kLeaf ? ((cap >> kLeafLog) + kChunkLeaves - 1) / kChunkLeaves : 1;
+  return cap > kLeaf ? ((cap >> kLeafLog) + kPushLeaves - 1) / kPushLeaves : 1;
 }
 
 sst_status bellman_ford(sst_graph *g, uint32_t src, int32_t *d_out) {
