@@ -279,10 +279,12 @@ __device__ __forceinline__ uint32_t leaf_slot(uint32_t linev, uint64_t S,
   return (uint32_t)lane < c ? a : kEmpty;
 }
 
-// remove, first pass: delete inside each touched leaf (warp per group) and
-// take the count off the row's degree.  Each item carries its leaf's start
-// and count word from the locate step, so a group costs three dependent
-// loads: its item range, the items, the leaf.
+// remove, first pass: delete inside each touched leaf and take the count
+// off the row's degree.  A warp takes 32 groups at a time: lane l first
+// loads group l's item range and its first item's leaf start, count word and
+// row (two dependent loads for all 32 groups at once), then the groups go
+// kGroupsPerWarp at a time with their items and leaf lines loaded together,
+// one dependent load per batch.
 __global__ void __launch_bounds__(256, 4)
 k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
               const uint32_t *__restrict__ p_x,
@@ -294,47 +296,55 @@ k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
   const uint32_t ng = *d_ngroups;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-       w * Q < ng; w += nw) {
-    uint32_t j0[Q], k[Q], d[Q], linev[Q], cw[Q], u[Q];
-    uint64_t S[Q];
-    bool ok[Q];
+       w * 32 < ng; w += nw) {
+    const uint64_t gl = w * 32 + lane;
+    const bool okl = gl < ng;
+    const uint32_t j0l = okl ? g_start[gl] : 0;
+    const uint32_t kl = okl ? g_start[gl + 1] - j0l : 0;
+    const uint64_t Sl = okl ? p_S[j0l] : 0;
+    const uint32_t cwl = okl ? p_c[j0l] : 0;
+    const uint32_t ul = okl ? (uint32_t)(p_ul[j0l] >> 32) : 0;
+    const uint32_t cnt = ng - w * 32 < 32 ? (uint32_t)(ng - w * 32) : 32u;
+    for (uint32_t q0 = 0; q0 < cnt; q0 += Q) {
+      uint32_t j0[Q], k[Q], d[Q], linev[Q], cw[Q], u[Q];
+      uint64_t S[Q];
+      bool ok[Q];
 #pragma unroll
-    for (int q = 0; q < Q; q++) {
-      uint64_t gid = w * Q + q;
-      ok[q] = gid < ng;
-      j0[q] = ok[q] ? g_start[gid] : 0;
-      k[q] = ok[q] ? g_start[gid + 1] - j0[q] : 0;
-    }
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-      S[q] = ok[q] ? p_S[j0[q]] : 0;
-      cw[q] = ok[q] ? p_c[j0[q]] : 0;
-      u[q] = ok[q] ? (uint32_t)(p_ul[j0[q]] >> 32) : 0;
-      d[q] = (uint32_t)lane < k[q] ? p_x[j0[q] + lane] : kEmpty;
-    }
-#pragma unroll
-    for (int q = 0; q < Q; q++)
-      linev[q] = ok[q] ? g.slots[(S[q] & ~uint64_t(kLeaf - 1)) + lane] : kEmpty;
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-      if (!ok[q]) break;
-      const uint32_t c = cw[q] & 0xff;
-      const uint32_t a = leaf_slot(linev[q], S[q], c, lane);
-      bool del = false;
-      for (uint32_t j = 0; j < k[q]; j++) del |= (__shfl_sync(0xffffffffu, d[q], j) == a);
-      bool keep = (uint32_t)lane < c && !del;
-      uint32_t mask = __ballot_sync(0xffffffffu, keep);
-      uint32_t pos = __popc(mask & ((1u << lane) - 1u));
-      const uint32_t av = (g.vals && (uint32_t)lane < c) ? g.vals[S[q] + lane] : 0u;
-      __syncwarp();
-      if (keep) g.slots[S[q] + pos] = a;
-      if (keep && g.vals) g.vals[S[q] + pos] = av;
-      if ((uint32_t)lane >= c - k[q] && (uint32_t)lane < c) g.slots[S[q] + lane] = kEmpty;
-      if (lane == 0) {
-        if (cw[q] & kMultiLeaf) g.lcnt[S[q] >> kLeafLog] = (uint8_t)(c - k[q]);
-        atomicSub(&g.deg[u[q]], k[q]);
+      for (int q = 0; q < Q; q++) {
+        const int src = (int)((q0 + q) & 31);
+        ok[q] = q0 + q < cnt;
+        j0[q] = __shfl_sync(0xffffffffu, j0l, src);
+        k[q] = ok[q] ? __shfl_sync(0xffffffffu, kl, src) : 0;
+        S[q] = __shfl_sync(0xffffffffu, Sl, src);
+        cw[q] = __shfl_sync(0xffffffffu, cwl, src);
+        u[q] = __shfl_sync(0xffffffffu, ul, src);
       }
-      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        d[q] = (uint32_t)lane < k[q] ? p_x[j0[q] + lane] : kEmpty;
+        linev[q] = ok[q] ? g.slots[(S[q] & ~uint64_t(kLeaf - 1)) + lane] : kEmpty;
+      }
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        if (!ok[q]) break;
+        const uint32_t c = cw[q] & 0xff;
+        const uint32_t a = leaf_slot(linev[q], S[q], c, lane);
+        bool del = false;
+        for (uint32_t j = 0; j < k[q]; j++) del |= (__shfl_sync(0xffffffffu, d[q], j) == a);
+        bool keep = (uint32_t)lane < c && !del;
+        uint32_t mask = __ballot_sync(0xffffffffu, keep);
+        uint32_t pos = __popc(mask & ((1u << lane) - 1u));
+        const uint32_t av = (g.vals && (uint32_t)lane < c) ? g.vals[S[q] + lane] : 0u;
+        __syncwarp();
+        if (keep) g.slots[S[q] + pos] = a;
+        if (keep && g.vals) g.vals[S[q] + pos] = av;
+        if ((uint32_t)lane >= c - k[q] && (uint32_t)lane < c) g.slots[S[q] + lane] = kEmpty;
+        if (lane == 0) {
+          if (cw[q] & kMultiLeaf) g.lcnt[S[q] >> kLeafLog] = (uint8_t)(c - k[q]);
+          atomicSub(&g.deg[u[q]], k[q]);
+        }
+        __syncwarp();
+      }
     }
   }
 }
@@ -603,62 +613,73 @@ __global__ void k_task_setup(DGraph g, PmaParams p, bool insert,
 }
 
 // ---------------------------------------------------------------- step 9
-// warp per kGroupsPerWarp merge groups; each stage's loads for all of them
-// are issued together (the groups are independent leaves).  merge_jk[t] =
-// (first item << 32) | item count of merge group t; the items carry their
-// leaf's start and count word, so a group costs three dependent loads.
+// merge_jk[t] = (first item << 32) | item count of merge group t.  A warp
+// takes 32 groups at a time: lane l first loads group l's item range and its
+// first item's leaf start and count word (two dependent loads for all 32
+// groups at once), then the groups go kGroupsPerWarp at a time with their
+// items and leaf lines loaded together, one dependent load per batch.
 __global__ void __launch_bounds__(256, 4)
 k_leaf_merge(DGraph g, const uint32_t *__restrict__ p_x,
              const uint64_t *__restrict__ p_S, const uint32_t *__restrict__ p_c,
              const uint64_t *__restrict__ merge_jk, uint32_t nmerge,
              const uint32_t *__restrict__ p_w) {
-  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   constexpr int Q = kGroupsPerWarp;
-  if (w * Q >= nmerge) return;
-  uint32_t j0[Q], k[Q], x[Q], linev[Q], cw[Q];
-  uint64_t S[Q];
-  bool ok[Q];
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       w * 32 < nmerge; w += nw) {
+    const uint64_t gl = w * 32 + lane;
+    const bool okl = gl < nmerge;
+    const uint64_t jkl = okl ? merge_jk[gl] : 0;
+    const uint32_t j0l = (uint32_t)(jkl >> 32), kl = (uint32_t)jkl;
+    const uint64_t Sl = okl ? p_S[j0l] : 0;
+    const uint32_t cwl = okl ? p_c[j0l] : 0;
+    const uint32_t cnt = nmerge - w * 32 < 32 ? (uint32_t)(nmerge - w * 32) : 32u;
+    for (uint32_t q0 = 0; q0 < cnt; q0 += Q) {
+      uint32_t j0[Q], k[Q], x[Q], linev[Q], cw[Q];
+      uint64_t S[Q];
+      bool ok[Q];
 #pragma unroll
-  for (int q = 0; q < Q; q++) {
-    ok[q] = w * Q + q < nmerge;
-    const uint64_t jk = ok[q] ? merge_jk[w * Q + q] : 0;
-    j0[q] = (uint32_t)(jk >> 32);
-    k[q] = (uint32_t)jk;
-  }
+      for (int q = 0; q < Q; q++) {
+        const int src = (int)((q0 + q) & 31);
+        ok[q] = q0 + q < cnt;
+        j0[q] = __shfl_sync(0xffffffffu, j0l, src);
+        k[q] = ok[q] ? __shfl_sync(0xffffffffu, kl, src) : 0;
+        S[q] = __shfl_sync(0xffffffffu, Sl, src);
+        cw[q] = __shfl_sync(0xffffffffu, cwl, src);
+      }
 #pragma unroll
-  for (int q = 0; q < Q; q++) {
-    S[q] = ok[q] ? p_S[j0[q]] : 0;
-    cw[q] = ok[q] ? p_c[j0[q]] : 0;
-    x[q] = (uint32_t)lane < k[q] ? p_x[j0[q] + lane] : kEmpty;
-  }
+      for (int q = 0; q < Q; q++) {
+        x[q] = (uint32_t)lane < k[q] ? p_x[j0[q] + lane] : kEmpty;
+        linev[q] = ok[q] ? g.slots[(S[q] & ~uint64_t(kLeaf - 1)) + lane] : kEmpty;
+      }
 #pragma unroll
-  for (int q = 0; q < Q; q++)
-    linev[q] = ok[q] ? g.slots[(S[q] & ~uint64_t(kLeaf - 1)) + lane] : kEmpty;
-#pragma unroll
-  for (int q = 0; q < Q; q++) {
-    if (!ok[q]) break;
-    const uint32_t c = cw[q] & 0xff;
-    const uint32_t a = leaf_slot(linev[q], S[q], c, lane);
-    // merged ranks in O(k) steps (k new ids, usually one or two): an old id
-    // moves up by the new ids below it; new id j lands at j + the old ids
-    // below it (a ballot per new id)
-    uint32_t pa = lane, px = lane;
-    for (uint32_t j = 0; j < k[q]; j++) {
-      uint32_t xj = __shfl_sync(0xffffffffu, x[q], j);
-      pa += xj < a;
-      uint32_t below = __popc(__ballot_sync(0xffffffffu, (uint32_t)lane < c && a < xj));
-      if ((uint32_t)lane == j) px = j + below;
+      for (int q = 0; q < Q; q++) {
+        if (!ok[q]) break;
+        const uint32_t c = cw[q] & 0xff;
+        const uint32_t a = leaf_slot(linev[q], S[q], c, lane);
+        // merged ranks in O(k) steps (k new ids, usually one or two): an old
+        // id moves up by the new ids below it; new id j lands at j + the old
+        // ids below it (a ballot per new id)
+        uint32_t pa = lane, px = lane;
+        for (uint32_t j = 0; j < k[q]; j++) {
+          uint32_t xj = __shfl_sync(0xffffffffu, x[q], j);
+          pa += xj < a;
+          uint32_t below = __popc(__ballot_sync(0xffffffffu, (uint32_t)lane < c && a < xj));
+          if ((uint32_t)lane == j) px = j + below;
+        }
+        // values move with their ids (weighted graphs)
+        const uint32_t av = (g.vals && (uint32_t)lane < c) ? g.vals[S[q] + lane] : 0u;
+        const uint32_t xv = (g.vals && (uint32_t)lane < k[q]) ? (p_w ? p_w[j0[q] + lane] : 1u) : 0u;
+        __syncwarp();
+        if ((uint32_t)lane < c) g.slots[S[q] + pa] = a;
+        if ((uint32_t)lane < k[q]) g.slots[S[q] + px] = x[q];
+        if (g.vals && (uint32_t)lane < c) g.vals[S[q] + pa] = av;
+        if (g.vals && (uint32_t)lane < k[q]) g.vals[S[q] + px] = xv;
+        if (lane == 0 && (cw[q] & kMultiLeaf)) g.lcnt[S[q] >> kLeafLog] = (uint8_t)(c + k[q]);
+        __syncwarp();
+      }
     }
-    // values move with their ids (weighted graphs)
-    const uint32_t av = (g.vals && (uint32_t)lane < c) ? g.vals[S[q] + lane] : 0u;
-    const uint32_t xv = (g.vals && (uint32_t)lane < k[q]) ? (p_w ? p_w[j0[q] + lane] : 1u) : 0u;
-    __syncwarp();
-    if ((uint32_t)lane < c) g.slots[S[q] + pa] = a;
-    if ((uint32_t)lane < k[q]) g.slots[S[q] + px] = x[q];
-    if (g.vals && (uint32_t)lane < c) g.vals[S[q] + pa] = av;
-    if (g.vals && (uint32_t)lane < k[q]) g.vals[S[q] + px] = xv;
-    if (lane == 0 && (cw[q] & kMultiLeaf)) g.lcnt[S[q] >> kLeafLog] = (uint8_t)(c + k[q]);
   }
 }
 
@@ -1347,7 +1368,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     // each merge rewrites one 128-byte leaf (read + write) and its count
     // (the merged ids, fewer than 32 per leaf, are not counted)
     SST_LAUNCH_B(258ull * ps.n_merge, k_leaf_merge,
-                 warp_blocks((ps.n_merge + kGroupsPerWarp - 1) / kGroupsPerWarp),
+                 std::min(warp_blocks((ps.n_merge + 31) / 32), (unsigned)g->sms * 8),
                  kTB, 0, s, dg, p_x, p_S, p_c, merge_jk, ps.n_merge, p_w);
   if (ps.n_tasks) {
     if (ps.src_leaves) {
