@@ -20,6 +20,7 @@ port in oracle/, all host threads) on the same workload.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -56,7 +57,7 @@ def args_parse():
     ap.add_argument("--serve-rate", type=float, default=300.0)
     ap.add_argument("--only", default="all",
                     choices=["all", "updates", "pagerank", "bfs", "batched", "serving",
-                             "multi"],
+                             "multi", "compact"],
                     help="one part of the run (profiling cases): the update steps "
                          "alone, or one traversal on the base graph")
     return ap.parse_args()
@@ -316,6 +317,66 @@ def main():
                     "kernels": pr_prof}
         return pagerank
 
+    def measure_compact():
+        """Byte-width snapshot of the bench graph (sst_compact_*): build time,
+        storage against the live PMA graph, and PageRank read from the
+        compressed rows (bit-equal to sst_pagerank) against the PMA PageRank."""
+        m = g.M()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c = sg.CompactGraph(g)
+        build_s = time.perf_counter() - t0
+        c.set_stream(stream.cuda_stream)
+        info = c.info()
+        out = torch.empty(n, dtype=torch.float64, device="cuda")
+        c.pagerank(1, out=out)
+        torch.cuda.synchronize()
+        prt = {}
+        for it in (a.pr_iters, 2 * a.pr_iters):
+            best = 1e30
+            for _ in range(3):
+                with torch.cuda.stream(stream):
+                    pr_flush.fill_(it)
+                s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s0.record(stream)
+                c.pagerank(it, out=out)
+                s1.record(stream)
+                s1.synchronize()
+                best = min(best, s0.elapsed_time(s1) / 1e3)
+            prt[it] = best
+        t_iter = (prt[2 * a.pr_iters] - prt[a.pr_iters]) / a.pr_iters
+        ref = torch.empty(n, dtype=torch.float64, device="cuda")
+        with torch.cuda.stream(stream):
+            sg.PR_S(g, a.pr_iters, out=ref)
+            c.pagerank(a.pr_iters, out=out)
+        torch.cuda.synchronize()
+        equal = bool(torch.equal(out.view(torch.int64), ref.view(torch.int64)))
+        sg.profile_start()
+        c.pagerank(a.pr_iters, out=out)
+        torch.cuda.synchronize()
+        cprof = sg.profile_collect()
+        sg.profile_start()
+        sg.PR_S(g, a.pr_iters, out=ref)
+        torch.cuda.synchronize()
+        pprof = sg.profile_collect()
+        # the live graph's storage: vertex table (base, cap, deg) and the
+        # slab's used slots with their leaf counts
+        nslots = ctypes.c_uint64()
+        sg.lib().sst_raw_state(g.handle, None, None, None, None, None, ctypes.byref(nslots))
+        pma_storage = 16 * n + 4 * nslots.value + nslots.value // 32
+        c.close()
+        return {"build_s": build_s, "edges": m,
+                "storage_bytes": info["storage_bytes"],
+                "bytes_per_edge": info["storage_bytes"] / max(m, 1),
+                "pma_storage_bytes": pma_storage,
+                "pma_bytes_per_edge": pma_storage / max(m, 1),
+                "graph_device_bytes": g.get_memory_size(),
+                "rows_per_width": info["rows_per_width"],
+                "pagerank_ms_per_iter": t_iter * 1e3,
+                "pagerank_bytes_per_iter": info["storage_bytes"] + 24 * n,
+                "pagerank_equal_to_pma": equal,
+                "kernels": cprof, "pma_kernels": pprof}
+
     def measure_bfs():
         m = g.M()
         dep = torch.empty(n, dtype=torch.int32, device="cuda")
@@ -522,6 +583,8 @@ def main():
             res["batched"] = measure_batched()
         elif a.only == "multi":
             res["multi_source"] = measure_multi()
+        elif a.only == "compact":
+            res["compact"] = measure_compact()
         else:
             res["bfs"] = measure_bfs()
         g.close()
@@ -610,7 +673,7 @@ def main():
            "note": "insert+remove via sst_insert_batch/sst_remove_batch on pinned host "
                    "pairs; each call returns the invalid-pair count (8 B) to the host"}
 
-    batched = pagerank = bfs = serving = multi = None
+    batched = pagerank = bfs = serving = multi = compact = None
     if a.only == "all":
         batched = measure_batched()
         t0 = time.time()
@@ -642,6 +705,7 @@ def main():
         gr.close()
         bfs = measure_bfs()
         multi = measure_multi()
+        compact = measure_compact()
         serving = measure_serving()
 
 
@@ -680,6 +744,7 @@ def main():
         "pagerank": pagerank,
         "bfs": bfs,
         "multi_source": multi,
+        "compact_snapshot": compact,
         "serving": serving,
         "update_kernels": upd_kernels,
     }

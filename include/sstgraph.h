@@ -263,6 +263,40 @@ SST_API sst_status sst_touch_all(sst_graph *g, uint64_t *out);
 SST_API sst_status sst_tc_vertices(sst_graph *g, const uint32_t *vertices,
                                    uint64_t k, uint64_t *out, uint32_t flags);
 
+/* ---- byte-width snapshot: the device form of TinySetV_small's rows
+ *      (TinySet_small.hpp:204-293,852-881).  Each row keeps the low B bytes
+ *      of its ids (B = 4, 3, 2, 1 by the row's length, with the reference's
+ *      thresholds), bucketed by the high part; read-only, built from a
+ *      graph's current contents, independent of it afterwards. ---------- */
+typedef struct sst_compact sst_compact;
+/* get_thresholds(max_el)  TinySet_small.hpp:227-263: rows with fewer than
+ * t[0] ids keep 4-byte keys, fewer than t[1] 3-byte, fewer than t[2]
+ * 2-byte, the rest 1-byte (host only, no device needed) */
+SST_API sst_status sst_compact_widths(uint64_t max_el, uint32_t thresholds[3]);
+/* snapshot of g (unweighted graphs; weighted ones get SST_ESTATE) */
+SST_API sst_status sst_compact_create(sst_graph *g, sst_compact **out);
+SST_API sst_status sst_compact_destroy(sst_compact *c);
+/* storage_bytes: the rows and their index; device_bytes: everything the
+ * snapshot holds (with PageRank work lists and buffers); rows_per_width[i]:
+ * rows stored with (i + 1)-byte keys.  Any pointer may be NULL. */
+SST_API sst_status sst_compact_info(sst_compact *c, uint64_t *storage_bytes,
+                                    uint64_t *device_bytes, uint64_t *edges,
+                                    uint64_t rows_per_width[4]);
+/* the snapshot decoded as a CSR (offsets[rows+1], cols[M]) */
+SST_API sst_status sst_compact_to_csr(sst_compact *c, uint64_t *offsets,
+                                      uint32_t *cols, uint32_t flags);
+/* has(row, col) per pair, out[i] = 0/1 */
+SST_API sst_status sst_compact_has_batch(sst_compact *c, const uint32_t *pairs,
+                                         uint64_t n, uint8_t *out, uint32_t flags);
+/* PR_S<double>  test.hpp:527 on the snapshot: the same result, bit for bit,
+ * as sst_pagerank on the graph it was taken from */
+SST_API sst_status sst_compact_pagerank(sst_compact *c, uint32_t iters,
+                                        double damping, double *out,
+                                        uint32_t flags);
+/* the stream the snapshot's work runs on (NULL: its own), as sst_set_stream */
+SST_API sst_status sst_compact_set_stream(sst_compact *c, void *stream);
+SST_API sst_status sst_compact_sync(sst_compact *c);
+
 /* ---- serving loop (no reference counterpart: the reference has no
  *      request loop; this keeps the graph on the device and serves a mixed
  *      stream) --------------------------------------------------------- */

@@ -237,6 +237,8 @@ def ref():
             "ref_load_mtx": (u64, [ctypes.c_char_p, ctypes.POINTER(u32),
                                    ctypes.POINTER(vp)]),
             "ref_free": (None, [vp]),
+            "ref_tinyset_thresholds": (None, [u64, vp]),
+            "ref_tinyset_width": (u32, [u64, vp, u64]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

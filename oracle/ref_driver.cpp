@@ -14,6 +14,7 @@
 //   map_neighbors_no_early_exit           include/SSTGraph/SparseMatrix.hpp:243
 //   touch_all_sum                         include/SSTGraph/SparseMatrix.hpp:436
 //   TinySetV                              include/SSTGraph/TinySet.hpp:8-73
+//   TinySetV_small get_thresholds, get_b  include/SSTGraph/TinySet_small.hpp:129-135,227-263
 //   rMat / random_aspen / hash64 / hash32 include/SSTGraph/internal/rmat_util.h:29-131
 //   create_random_data                    include/SSTGraph/internal/helpers.hpp:752
 //   get_edges_from_file_mtx               include/SSTGraph/internal/helpers.hpp:379
@@ -125,6 +126,25 @@ uint64_t ref_set_to_array(void *s, uint32_t *out) {
   uint64_t k = 0;
   static_cast<Set *>(s)->map<true>([&](el_t e) { out[k++] = e; });
   return k;
+}
+
+// ---- byte-width rows: TinySetV_small's key width ----
+// get_thresholds  TinySet_small.hpp:227-263
+void ref_tinyset_thresholds(uint64_t max_el, uint32_t *out) {
+  auto d = TinySetV_small<>::get_thresholds(max_el);
+  out[0] = d.thresh_24;
+  out[1] = d.thresh_16;
+  out[2] = d.thresh_8;
+}
+// get_b() of a TinySetV_small over max_el after inserting els[0..k)
+// (TinySet_small.hpp:129-130; the width follows the count, :204-214)
+uint32_t ref_tinyset_width(uint64_t max_el, const uint32_t *els, uint64_t k) {
+  auto d = TinySetV_small<>::get_thresholds(max_el);
+  TinySetV_small<> ts;
+  for (uint64_t i = 0; i < k; i++) ts.insert(std::tuple<el_t>(els[i]), d);
+  uint32_t b = ts.get_b();
+  ts.destroy(d);
+  return b;
 }
 
 // ---- generators ----

@@ -141,6 +141,16 @@ SIGNATURES = {
     "sst_server_stats": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64),
                                 ctypes.POINTER(_u64)]),
     "sst_server_destroy": (_i32, [_vp]),
+    "sst_compact_widths": (_i32, [_u64, _vp]),
+    "sst_compact_create": (_i32, [_vp, ctypes.POINTER(_vp)]),
+    "sst_compact_destroy": (_i32, [_vp]),
+    "sst_compact_info": (_i32, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64),
+                                ctypes.POINTER(_u64), _vp]),
+    "sst_compact_to_csr": (_i32, [_vp, _vp, _vp, _u32]),
+    "sst_compact_has_batch": (_i32, [_vp, _vp, _u64, _vp, _u32]),
+    "sst_compact_pagerank": (_i32, [_vp, _u32, _dbl, _vp, _u32]),
+    "sst_compact_sync": (_i32, [_vp]),
+    "sst_compact_set_stream": (_i32, [_vp, _vp]),
     "sst_profile_start": (_i32, [ctypes.c_char_p]),
     "sst_profile_collect": (_i32, [ctypes.c_char_p, _u64]),
 }
@@ -620,6 +630,79 @@ class TinySetV:
 
     def close(self):
         self._g.close()
+
+
+def compact_widths(max_el: int):
+    """get_thresholds (TinySet_small.hpp:227-263) for rows over max_el
+    columns: rows with fewer than t[0] ids keep 4-byte keys, fewer than t[1]
+    3-byte, fewer than t[2] 2-byte, the rest 1-byte."""
+    t = np.zeros(3, np.uint32)
+    _check(lib().sst_compact_widths(int(max_el), ctypes.c_void_p(t.ctypes.data)))
+    return [int(x) for x in t]
+
+
+class CompactGraph:
+    """Read-only byte-width snapshot of a SparseMatrixV: each row keeps the
+    low B bytes of its ids, bucketed by the high part, as the reference's
+    TinySetV_small rows do (TinySet_small.hpp:204-293,852-881)."""
+
+    def __init__(self, g: SparseMatrixV):
+        h = ctypes.c_void_p()
+        _check(lib().sst_compact_create(g.handle, ctypes.byref(h)))
+        self._h = h
+        self.rows = g.rows
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sst_compact_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        sb, db, m = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        pw = np.zeros(4, np.uint64)
+        _check(lib().sst_compact_info(self._h, ctypes.byref(sb), ctypes.byref(db),
+                                      ctypes.byref(m), ctypes.c_void_p(pw.ctypes.data)))
+        return {"storage_bytes": sb.value, "device_bytes": db.value, "edges": m.value,
+                "rows_per_width": {i + 1: int(pw[i]) for i in range(4)}}
+
+    def csr(self):
+        m = self.info()["edges"]
+        off = np.empty(self.rows + 1, np.uint64)
+        cols = np.empty(max(m, 1), np.uint32)
+        _check(lib().sst_compact_to_csr(self._h, ctypes.c_void_p(off.ctypes.data),
+                                        ctypes.c_void_p(cols.ctypes.data), HOST_PTR))
+        return off, cols[:m]
+
+    def has_batch(self, edges, out=None):
+        e, n = _pairs(edges)
+        p, flags = _ptr(e)
+        if out is None:
+            if flags == DEVICE_PTR:
+                import torch
+                out = torch.empty(n, dtype=torch.uint8, device=e.device)
+            else:
+                out = np.empty(n, np.uint8)
+        po, _ = _ptr(out)
+        _check(lib().sst_compact_has_batch(self._h, p, n, po, flags))
+        return out
+
+    def pagerank(self, iters: int = 10, damping: float = 0.85, out=None):
+        buf = np.empty(self.rows, np.float64) if out is None else out
+        p, flags = _ptr(buf)
+        _check(lib().sst_compact_pagerank(self._h, iters, damping, p, flags))
+        return buf
+
+    def sync(self):
+        _check(lib().sst_compact_sync(self._h))
+
+    def set_stream(self, stream_ptr: int | None):
+        _check(lib().sst_compact_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
 
 
 def read_graph_file(path: str):

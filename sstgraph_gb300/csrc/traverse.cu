@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "prfixed.cuh"
 #include "traverse.cuh"
 
 namespace sst {
@@ -222,83 +223,36 @@ __global__ void k_compact_ids(const uint32_t *__restrict__ flag,
 }
 
 // ------------------------------------------------------------- pagerank
-// An iteration is integer-only fixed point in units of 2^-63: each
-// contribution rank(u)/deg(u) is rounded once to a multiple of 2^-63, the
-// per-edge sums are exact 64-bit integer additions (order-independent, so
-// deterministic), and rank = (1-d)/n + d*sum uses a 64x64->128-bit product
-// rounded to nearest.  GB300 runs FP64 at a small fraction of its integer
-// rate; FP64 appears only when the final ranks are written.
-__device__ __forceinline__ uint64_t mulhi_round(uint64_t a, uint64_t b) {
-  return __umul64hi(a, b) + ((a * b) >> 63);
-}
-
-// leaf ids are read once per iteration: keep them out of L1 and first in
-// line for eviction from L2, so the contribution gathers keep both caches
-__device__ __forceinline__ unsigned long long l2_evict_first() {
-  unsigned long long pol;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
-__device__ __forceinline__ uint32_t ld_stream(const uint32_t *p,
-                                              unsigned long long pol) {
-  uint32_t v;
-  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;"
-      : "=r"(v)
-      : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ unsigned long long ld_keep(const unsigned long long *p) {
-  unsigned long long v;
-  asm("ld.global.nc.L1::evict_last.b64 %0, [%1];" : "=l"(v) : "l"(p));
-  return v;
-}
+// The fixed-point arithmetic (units of 2^-63, exact integer sums) is in
+// prfixed.cuh, shared with the byte-width snapshot's PageRank.
 
 // per vertex: round(2^64 / deg) for deg >= 2 (deg 1 passes rank through)
 __global__ void k_pr_rdeg(const uint32_t *__restrict__ deg, uint32_t n,
                           unsigned long long *__restrict__ rdeg) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
-  uint32_t d = deg[v];
-  unsigned long long r = 0;
-  if (d >= 2) {
-    unsigned __int128 num = ((unsigned __int128)1 << 64) + (d >> 1);
-    r = (unsigned long long)(num / d);
-  }
-  rdeg[v] = r;
+  rdeg[v] = pr_rdeg_of(deg[v]);
 }
 
-__device__ __forceinline__ unsigned long long contrib_of(unsigned long long rank,
-                                                         uint32_t deg,
-                                                         unsigned long long rd) {
-  return deg == 1 ? rank : mulhi_round(rank, rd);
-}
-
+// a vertex with an empty row is in no work list, so no iteration writes its
+// contribution: zero it in both buffers (a directed graph's rows may still
+// name it)
 __global__ void k_pr_start(const uint32_t *__restrict__ deg, uint32_t n,
                            unsigned long long r0,
                            const unsigned long long *__restrict__ rdeg,
                            unsigned long long *__restrict__ contrib,
+                           unsigned long long *__restrict__ contrib2,
                            double *__restrict__ rank, double base) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   uint32_t d = deg[v];
   contrib[v] = d ? contrib_of(r0, d, rdeg[v]) : 0ull;
-  if (d == 0) rank[v] = base;  // no in-edges: constant term only
+  if (d == 0) {
+    contrib2[v] = 0ull;
+    rank[v] = base;  // no in-edges: constant term only
+  }
 }
 
-struct PrConst {
-  unsigned long long B;  // (1-d)/n in 2^-63 units
-  unsigned long long D;  // d in 2^-64 units
-};
-
-__device__ __forceinline__ void pr_finish(uint32_t v, unsigned long long sum,
-                                          PrConst k, uint32_t deg,
-                                          const unsigned long long *rdeg,
-                                          unsigned long long *cout,
-                                          double *rank, bool last) {
-  unsigned long long r = k.B + mulhi_round(sum, k.D);
-  cout[v] = contrib_of(r, deg, rdeg[v]);
-  if (last) rank[v] = __ull2double_rn(r) * (1.0 / 9223372036854775808.0);
-}
 
 // One-leaf segments (cap <= 32): a group of G lanes per vertex (G = 8: one
 // 32-byte sector of the leaf per lane step), four vertices per group in
@@ -1299,11 +1253,8 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
     SST_CUDA_TRY(cudaGetLastError());
     return SST_OK;
   }
-  const double two63 = 9223372036854775808.0, two64 = 18446744073709551616.0;
-  PrConst K;
-  K.B = (unsigned long long)llrint(base * two63);
-  K.D = damping >= 1.0 ? ~0ull : (unsigned long long)llrint(damping * two64 / 2.0) * 2ull;
-  unsigned long long r0f = (unsigned long long)llrint(r0 * two63);
+  unsigned long long r0f = 0;
+  const PrConst K = pr_const(n, damping, &r0f);
   unsigned long long *cin = reinterpret_cast<unsigned long long *>(t->ca.p);
   unsigned long long *cout = reinterpret_cast<unsigned long long *>(t->cb.p);
   unsigned long long *part = reinterpret_cast<unsigned long long *>(t->partial.p);
@@ -1327,7 +1278,7 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   }
   auto launch_all = [&]() {
     unsigned long long *ci = cin, *co = cout;
-    SST_LAUNCH(k_pr_start, blocks_for(n), kTB, 0, s, g->d_deg, n, r0f, rdeg, ci,
+    SST_LAUNCH(k_pr_start, blocks_for(n), kTB, 0, s, g->d_deg, n, r0f, rdeg, ci, co,
                d_rank, base);
     DGraph dg = g->view();
     for (uint32_t it = 0; it < iters; it++) {

@@ -26,6 +26,12 @@ Fixtures (all small, npz):
   examples_mtx.npz      examples/*.mtx through the reference loader
                         (helpers.hpp:379-529): symmetrised edge lists and the
                         CSR of the graph built from them
+  tinyset_widths.npz    TinySetV_small::get_thresholds(max_el) for a range of
+                        column counts (TinySet_small.hpp:227-263), and the key
+                        width get_b() of a reference set after inserting k
+                        distinct ids, for k on both sides of each threshold
+
+`--only tinyset_widths` writes that fixture alone.
 """
 import hashlib
 import os
@@ -45,6 +51,40 @@ def csr_digest(off, cols):
     h.update(np.ascontiguousarray(off, np.uint64).tobytes())
     h.update(np.ascontiguousarray(cols, np.uint32).tobytes())
     return h.hexdigest()
+
+
+TINYSET_MAX_ELS = [1, 2, 100, 255, 256, 257, 1024, 65535, 65536, 65537,
+                   1 << 20, 3000000, 1 << 24, (1 << 24) + 1, 1 << 25, 1 << 30,
+                   0xFFFFFFFF]
+
+
+def tinyset_widths():
+    import ctypes
+    R = oracle.ref()
+    th = np.zeros((len(TINYSET_MAX_ELS), 3), np.uint32)
+    for i, mx in enumerate(TINYSET_MAX_ELS):
+        t = np.zeros(3, np.uint32)
+        R.ref_tinyset_thresholds(mx, ctypes.c_void_p(t.ctypes.data))
+        th[i] = t
+    # widths of real reference sets: k distinct ids below max_el (seed 7)
+    rng = np.random.default_rng(7)
+    rows = []
+    for mx in (1 << 10, 1 << 16, 1 << 20, 1 << 24):
+        t = np.zeros(3, np.uint32)
+        R.ref_tinyset_thresholds(mx, ctypes.c_void_p(t.ctypes.data))
+        ks = {1, 2, 3}
+        for x in t.tolist():
+            for k in (x - 1, x, x + 1):
+                if 1 <= k <= min(mx, 1 << 21):
+                    ks.add(k)
+        for k in sorted(ks):
+            els = rng.choice(mx, size=k, replace=False).astype(np.uint32)
+            b = R.ref_tinyset_width(mx, ctypes.c_void_p(els.ctypes.data), k)
+            rows.append((mx, k, b))
+    w = np.array(rows, np.uint64)
+    np.savez_compressed(os.path.join(HERE, "tinyset_widths.npz"),
+                        max_el=np.array(TINYSET_MAX_ELS, np.uint64), thresholds=th,
+                        width_max_el=w[:, 0], width_count=w[:, 1], width=w[:, 2])
 
 
 def main(ref_root):
@@ -138,8 +178,13 @@ def main(ref_root):
         ex[f"{key}_off"] = off
         ex[f"{key}_cols"] = cols
     np.savez_compressed(os.path.join(HERE, "examples_mtx.npz"), **ex)
+    tinyset_widths()
     print("golden fixtures written to", HERE)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if "--only" in sys.argv and sys.argv[-1] == "tinyset_widths":
+        tinyset_widths()
+    else:
+        main(args[0] if args else "/root/reference")
