@@ -72,12 +72,19 @@ sst_status graph_copy_into(sst_graph *dst, sst_graph *src) {
 
 // per-vertex triangle counts of the listed vertices:
 // t(u) = (1/2) * sum over w in N(u) of |N(u) n N(w)| (symmetric graph).
-// Work items are (query vertex, leaf of its list), one warp each; the warp
-// takes the leaf's neighbours w one at a time and intersects N(u) and N(w)
-// cooperatively: lanes stride over the shorter list and probe the longer one
-// (binary search over its leaf heads, then within the leaf).  A hub query
-// vertex spreads over as many warps as it has leaves.
+// Three passes over work items:
+//  1. leaf items (query, leaf of N(u)); each item and lane is a pair slot
+//     holding the neighbour w in that slot of the leaf (or nothing);
+//  2. each pair's cost: the shorter of N(u) and N(w), in chunks of 32
+//     leaves;
+//  3. a warp per chunk: lanes take the chunk's leaves of the shorter list one
+//     at a time and probe each id in the longer list (binary search over its
+//     leaf heads, then within the leaf).
+// A pair of two long lists spreads over as many warps as the shorter one has
+// 32-leaf chunks, so no warp walks a long list alone.
 namespace {
+constexpr uint32_t kTcvChunkLeaves = 32;
+
 __device__ __forceinline__ bool probe(const DGraph &g, uint64_t base,
                                       uint32_t cap, uint32_t deg, uint32_t x) {
   uint32_t l = find_leaf(g.slots, base, cap, x);
@@ -87,25 +94,8 @@ __device__ __forceinline__ bool probe(const DGraph &g, uint64_t base,
   return pos < c && p[pos] == x;
 }
 
-// this lane's share of |N(a) n N(b)|
-__device__ __forceinline__ uint32_t warp_common(const DGraph &g, uint32_t a,
-                                                uint32_t b, int lane) {
-  uint32_t da = g.deg[a], db = g.deg[b];
-  const uint32_t s = da <= db ? a : b, o = s == a ? b : a;
-  const uint64_t sbase = g.base[s], obase = g.base[o];
-  const uint32_t scap = g.cap[s], sdeg = g.deg[s];
-  const uint32_t ocap = g.cap[o], odeg = g.deg[o];
-  if (!scap || !ocap) return 0;
-  const uint32_t nl = scap <= kLeaf ? 1 : scap >> kLeafLog;
-  uint32_t hits = 0;
-  for (uint32_t l = 0; l < nl; l++) {
-    uint32_t c = leaf_count(g, sbase, scap, sdeg, l);
-    if ((uint32_t)lane < c) {
-      uint32_t x = g.slots[sbase + ((uint64_t)l << kLeafLog) + lane];
-      hits += probe(g, obase, ocap, odeg, x);
-    }
-  }
-  return hits;
+__device__ __forceinline__ uint32_t leaves_of(uint32_t cap) {
+  return cap == 0 ? 0 : (cap <= kLeaf ? 1 : cap >> kLeafLog);
 }
 
 __global__ void k_tcv_leaves(DGraph g, const uint32_t *__restrict__ vs,
@@ -114,39 +104,77 @@ __global__ void k_tcv_leaves(DGraph g, const uint32_t *__restrict__ vs,
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= k) return;
   uint32_t u = vs[i];
-  uint32_t cap = u < g.n ? g.cap[u] : 0;
-  nl[i] = cap == 0 ? 0 : (cap <= kLeaf ? 1 : cap >> kLeafLog);
+  nl[i] = u < g.n ? leaves_of(g.cap[u]) : 0;
   out[i] = 0;
 }
 
-__global__ void k_tcv_count(DGraph g, const uint32_t *__restrict__ vs,
-                            uint64_t k, const uint64_t *__restrict__ off,
-                            uint64_t items, unsigned long long *__restrict__ out) {
+// pass 2: warp per leaf item; lane = pair slot
+__global__ void k_tcv_pairs(DGraph g, const uint32_t *__restrict__ vs, uint64_t k,
+                            const uint64_t *__restrict__ loff, uint64_t items,
+                            uint32_t *__restrict__ pq, uint32_t *__restrict__ pw,
+                            uint32_t *__restrict__ cost) {
   const int lane = threadIdx.x & 31;
   const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t wi = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
        wi < items; wi += warps) {
-    // query i with off[i] <= wi < off[i + 1]
+    // query q with loff[q] <= wi < loff[q + 1]
     uint64_t lo = 0, hi = k;
     while (hi - lo > 1) {
-      uint64_t mid = (lo + hi) >> 1;
-      if (off[mid] <= wi) lo = mid; else hi = mid;
+      const uint64_t mid = (lo + hi) >> 1;
+      if (loff[mid] <= wi) lo = mid; else hi = mid;
     }
     const uint32_t u = vs[lo];
-    const uint32_t l = (uint32_t)(wi - off[lo]);
+    const uint32_t l = (uint32_t)(wi - loff[lo]);
     const uint64_t base = g.base[u];
     const uint32_t cap = g.cap[u], deg = g.deg[u];
     const uint32_t c = leaf_count(g, base, cap, deg, l);
-    const uint32_t mine = (uint32_t)lane < c
-        ? g.slots[base + ((uint64_t)l << kLeafLog) + lane] : kEmpty;
+    const uint32_t w = (uint32_t)lane < c ? g.slots[base + ((uint64_t)l << kLeafLog) + lane]
+                                          : kEmpty;
+    uint32_t chunks = 0;
+    if (w != kEmpty) {
+      const uint32_t s = deg <= g.deg[w] ? u : w;  // the shorter list
+      chunks = (leaves_of(g.cap[s]) + kTcvChunkLeaves - 1) / kTcvChunkLeaves;
+    }
+    pw[wi * 32 + lane] = w;
+    cost[wi * 32 + lane] = chunks;
+    if (lane == 0) pq[wi] = (uint32_t)lo;
+  }
+}
+
+// pass 3: warp per chunk of a pair
+__global__ void k_tcv_count(DGraph g, const uint32_t *__restrict__ vs,
+                            const uint32_t *__restrict__ pq,
+                            const uint32_t *__restrict__ pw,
+                            const uint32_t *__restrict__ coff, uint64_t nslots,
+                            uint64_t nchunks, unsigned long long *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t ci = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       ci < nchunks; ci += warps) {
+    // pair slot p: the last with coff[p] <= ci (slots of cost 0 share their
+    // offset with the next slot, so the last one is the pair that owns ci)
+    uint64_t lo = 0, hi = nslots;
+    while (hi - lo > 1) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (coff[mid] <= ci) lo = mid; else hi = mid;
+    }
+    const uint32_t q = pq[lo >> 5], w = pw[lo], u = vs[q];
+    const uint32_t j = (uint32_t)(ci - coff[lo]);  // chunk of the pair
+    const uint32_t s = g.deg[u] <= g.deg[w] ? u : w, o = s == u ? w : u;
+    const uint64_t sbase = g.base[s], obase = g.base[o];
+    const uint32_t scap = g.cap[s], sdeg = g.deg[s];
+    const uint32_t ocap = g.cap[o], odeg = g.deg[o];
+    const uint32_t l0 = j * kTcvChunkLeaves;
+    const uint32_t l1 = min(l0 + kTcvChunkLeaves, leaves_of(scap));
     uint32_t hits = 0;
-    for (uint32_t t = 0; t < c; t++) {
-      uint32_t w = __shfl_sync(0xffffffffu, mine, t);
-      hits += warp_common(g, u, w, lane);
+    for (uint32_t l = l0; l < l1; l++) {
+      const uint32_t c = leaf_count(g, sbase, scap, sdeg, l);
+      if ((uint32_t)lane < c)
+        hits += probe(g, obase, ocap, odeg, g.slots[sbase + ((uint64_t)l << kLeafLog) + lane]);
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) hits += __shfl_down_sync(0xffffffffu, hits, d);
-    if (lane == 0 && hits) atomicAdd(&out[lo], (unsigned long long)hits);
+    if (lane == 0 && hits) atomicAdd(&out[q], (unsigned long long)hits);
   }
 }
 
@@ -161,27 +189,58 @@ sst_status tc_vertices(sst_graph *g, const uint32_t *d_vs, uint64_t k,
   if (k == 0) return SST_OK;
   cudaStream_t s = g->stream;
   unsigned long long *out = reinterpret_cast<unsigned long long *>(d_out);
-  uint64_t *nl = nullptr;
-  SST_CUDA_TRY(cudaMallocAsync(&nl, (k + 1) * 8, s));
-  g->arena.reset();
-  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes(k, 8) + 4096));
-  uint64_t *tot = g->arena.take<uint64_t>(1);
   const unsigned tb = 256;
-  SST_LAUNCH(k_tcv_leaves, (unsigned)((k + tb - 1) / tb), tb, 0, s, g->view(),
-             d_vs, k, nl, out);
-  cudaError_t e = scan<uint64_t, OpAdd>(nl, nl, k, 0ull, OpAdd{}, true, false,
-                                        tot, g->arena, s);
+  const uint64_t cap_blocks = (uint64_t)g->sms * 16;
+  // pass 1: leaf items per query
+  uint64_t *loff = nullptr;
+  SST_CUDA_TRY(cudaMallocAsync(&loff, (k + 1) * 8, s));
+  g->arena.reset();
+  cudaError_t e = g->arena.reserve(scan_scratch_bytes(k, 8) + 4096);
+  uint64_t *tot = e == cudaSuccess ? g->arena.take<uint64_t>(1) : nullptr;
+  if (e == cudaSuccess && !tot) e = cudaErrorMemoryAllocation;
   uint64_t items = 0;
+  if (e == cudaSuccess) {
+    SST_LAUNCH(k_tcv_leaves, (unsigned)((k + tb - 1) / tb), tb, 0, s, g->view(),
+               d_vs, k, loff, out);
+    e = scan<uint64_t, OpAdd>(loff, loff, k, 0ull, OpAdd{}, true, false, tot,
+                              g->arena, s);
+  }
   if (e == cudaSuccess) e = cudaMemcpyAsync(&items, tot, 8, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  // pass 2: pair slots and their chunk counts
+  uint32_t *pq = nullptr, *pw = nullptr, *cost = nullptr, *coff = nullptr;
+  const uint64_t nslots = items * 32;
+  uint32_t nchunks = 0;
   if (e == cudaSuccess && items) {
-    uint64_t blocks = std::min<uint64_t>((items * 32 + tb - 1) / tb, (uint64_t)g->sms * 16);
-    SST_LAUNCH(k_tcv_count, (unsigned)blocks, tb, 0, s, g->view(), d_vs, k, nl,
-               items, out);
-    SST_LAUNCH(k_tcv_half, (unsigned)((k + tb - 1) / tb), tb, 0, s, out, k);
-    e = cudaGetLastError();
+    e = cudaMallocAsync(&pq, items * 4, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&pw, nslots * 4, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&cost, nslots * 4, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&coff, nslots * 4, s);
+    if (e == cudaSuccess) {
+      g->arena.reset();
+      e = g->arena.reserve(scan_scratch_bytes(nslots, 4) + 4096);
+    }
+    uint32_t *ctot = e == cudaSuccess ? g->arena.take<uint32_t>(1) : nullptr;
+    if (e == cudaSuccess && !ctot) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) {
+      SST_LAUNCH(k_tcv_pairs, (unsigned)std::min<uint64_t>((items * 32 + tb - 1) / tb, cap_blocks),
+                 tb, 0, s, g->view(), d_vs, k, loff, items, pq, pw, cost);
+      e = scan<uint32_t, OpAdd>(cost, coff, nslots, 0u, OpAdd{}, true, false, ctot,
+                                g->arena, s);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&nchunks, ctot, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // pass 3
+    if (e == cudaSuccess && nchunks) {
+      SST_LAUNCH(k_tcv_count,
+                 (unsigned)std::min<uint64_t>(((uint64_t)nchunks * 32 + tb - 1) / tb, cap_blocks),
+                 tb, 0, s, g->view(), d_vs, pq, pw, coff, nslots, nchunks, out);
+      SST_LAUNCH(k_tcv_half, (unsigned)((k + tb - 1) / tb), tb, 0, s, out, k);
+      e = cudaGetLastError();
+    }
   }
-  cudaFreeAsync(nl, s);
+  for (void *p : {(void *)loff, (void *)pq, (void *)pw, (void *)cost, (void *)coff})
+    if (p) cudaFreeAsync(p, s);
   SST_CUDA_TRY(e);
   return SST_OK;
 }
