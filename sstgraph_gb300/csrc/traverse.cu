@@ -695,41 +695,51 @@ __global__ void k_bfs_pull_small8(DGraph g, const unsigned long long *__restrict
   const uint64_t grp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
   const uint32_t sub = threadIdx.x & 7;
   const uint64_t i0 = grp * 4;
+  // each stage's loads for the group's four vertices go out together: the
+  // list entries, then their depths, then the open ones' slots, then the
+  // frontier bits of those neighbours
+  uint32_t v[4], d[4];
+  unsigned long long dsc[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const bool in = i0 + u < nsmall;
+    v[u] = in ? small[i0 + u] : 0u;
+    dsc[u] = in ? sdesc[i0 + u] : 0ull;
+    d[u] = (uint32_t)(dsc[u] & 63);
+  }
+  bool open[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) open[u] = i0 + u < nsmall && depth[v[u]] < 0;
+  uint32_t w[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const uint32_t j = sub + 8 * q;
+      w[u][q] = (open[u] && j < d[u]) ? g.slots[(dsc[u] >> 6) + j] : kEmpty;
+    }
+  uint32_t fb[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) fb[u][q] = w[u][q] != kEmpty ? fbits[w[u][q] >> 5] : 0u;
   bool mine = false;
   uint32_t myv = 0, mydeg = 0;
 #pragma unroll
   for (int u = 0; u < 4; u++) {
-    const uint64_t i = i0 + u;
-    uint32_t v = 0, d = 0;
-    bool open = false;
-    unsigned long long dsc = 0;
-    if (i < nsmall) {
-      v = small[i];
-      open = depth[v] < 0;
-      dsc = sdesc[i];
-      d = (uint32_t)(dsc & 63);
-    }
     uint32_t best = kEmpty;
-    if (open) {
-      const uint32_t *p = g.slots + (dsc >> 6);
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        uint32_t j = sub + 8 * q;
-        if (j < d) {
-          uint32_t w = p[j];
-          if (w < best && in_front(fbits, w)) best = w;
-        }
-      }
-    }
+    for (int q = 0; q < 4; q++)
+      if (((fb[u][q] >> (w[u][q] & 31)) & 1u) && w[u][q] < best) best = w[u][q];
     // smallest frontier neighbour over the group's 8 lanes
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
-    if (sub == (uint32_t)u && open && best != kEmpty) {
-      depth[v] = lvl + 1;
-      parent[v] = (int32_t)best;
+    if (sub == (uint32_t)u && open[u] && best != kEmpty) {
+      depth[v[u]] = lvl + 1;
+      parent[v[u]] = (int32_t)best;
       mine = true;
-      myv = v;
-      mydeg = d;
+      myv = v[u];
+      mydeg = d[u];
     }
   }
   enqueue_block(mine, myv, mydeg, 1u, nq, cnt);
@@ -752,13 +762,14 @@ __global__ void k_bfs_pull_chunks(DGraph g, const unsigned long long *__restrict
   uint32_t v = 0;
   if (c < nchunks) {
     v = cv[c];
+    // the chunk's descriptor and leaf counts load beside the depth check
+    const unsigned long long dsc = cdesc[c];
+    const uint64_t leaf0 = dsc >> 8;
+    const uint32_t l1 = (uint32_t)(dsc & 63);
+    const uint32_t mycnt = (uint32_t)lane < l1 ? g.lcnt[leaf0 + lane] : 0u;
     // another chunk may claim v at any time: every lane follows lane 0's
     // reading, so the warp stays converged for its shuffles
     if (__shfl_sync(0xffffffffu, __ldcg(depth + v), 0) < 0) {
-      const unsigned long long dsc = cdesc[c];
-      const uint64_t leaf0 = dsc >> 8;
-      const uint32_t l1 = (uint32_t)(dsc & 63);
-      const uint32_t mycnt = (uint32_t)lane < l1 ? g.lcnt[leaf0 + lane] : 0u;
       const uint32_t *sl = g.slots + (leaf0 << kLeafLog) + lane;
       uint32_t found = kEmpty;
       for (uint32_t l = 0; l < l1 && found == kEmpty; l += 8) {
@@ -769,10 +780,14 @@ __global__ void k_bfs_pull_chunks(DGraph g, const unsigned long long *__restrict
           if (l + q >= l1) cq = 0;
           x[q] = (uint32_t)lane < cq ? sl[(uint64_t)(l + q) << kLeafLog] : kEmpty;
         }
+        // the eight frontier words load together, then the smallest hit
+        uint32_t fw[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) fw[q] = x[q] != kEmpty ? fbits[x[q] >> 5] : 0u;
         uint32_t best = kEmpty;
 #pragma unroll
         for (int q = 0; q < 8; q++)
-          if (x[q] != kEmpty && x[q] < best && in_front(fbits, x[q])) best = x[q];
+          if (((fw[q] >> (x[q] & 31)) & 1u) && x[q] < best) best = x[q];
         found = __reduce_min_sync(0xffffffffu, best);
         if (found == kEmpty && __shfl_sync(0xffffffffu, __ldcg(depth + v), 0) >= 0)
           break;  // claimed by another chunk
