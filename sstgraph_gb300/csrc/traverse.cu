@@ -1688,8 +1688,14 @@ __global__ void k_msbfs_pull_small(DGraph g, const uint32_t *__restrict__ small,
   const uint32_t *p = g.slots + g.base[v];
   uint32_t d = g.deg[v];
   unsigned long long acc = 0;
-  for (uint32_t k = 0; k < d; k++) {
-    acc |= fr[p[k]];
+  // four neighbours' ids, then their four masks, in flight per step
+  for (uint32_t k = 0; k < d; k += 4) {
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) w[q] = k + q < d ? p[k + q] : kEmpty;
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (w[q] != kEmpty) acc |= fr[w[q]];
     if ((acc & need) == need) break;
   }
   acc &= need;
