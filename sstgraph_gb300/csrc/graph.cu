@@ -211,16 +211,24 @@ __global__ void k_group_flags(const uint64_t *__restrict__ p_ul,
   gflag[j] = (j < n && (j == 0 || p_ul[j] != p_ul[j - 1])) ? 1u : 0u;
 }
 
-__global__ void k_group_start(const uint32_t *__restrict__ gflag,
-                              const uint32_t *__restrict__ gpos,
-                              const uint32_t *__restrict__ d_nitems,
-                              const uint32_t *__restrict__ d_ngroups,
-                              uint64_t b, uint32_t *__restrict__ g_start) {
-  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= b) return;
-  if (gflag[j] && gpos[j] < b) g_start[gpos[j]] = (uint32_t)j;
-  if (j == 0 && *d_ngroups <= b) g_start[*d_ngroups] = *d_nitems;
-}
+// Group starts, fused into the scan of the group flags: item j that opens
+// a group records itself at its group's index; the last item closes the
+// list with g_start[groups] = items (g_start[0] = 0 when there are none).
+struct GroupStartEpi {
+  const uint32_t *gflag;
+  const uint32_t *d_nitems;
+  uint64_t b;
+  uint32_t *g_start;
+  __device__ __forceinline__ void operator()(uint64_t j, uint32_t gp) const {
+    const uint32_t f = gflag[j];
+    if (f && gp < b) g_start[gp] = (uint32_t)j;
+    const uint32_t ni = *d_nitems;
+    if (ni == 0 ? j == 0 : j + 1 == ni) {
+      const uint32_t ng = gp + f;
+      if (ng <= b) g_start[ng] = ni;
+    }
+  }
+};
 
 // ---------------------------------------------------------------- step 6
 // Group-level kernels run grid-stride over the device-side group count, so
@@ -1190,7 +1198,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   uint32_t *leaf = A.take<uint32_t>(b);
   uint64_t *p_ul = A.take<uint64_t>(b);
   uint32_t *p_x = A.take<uint32_t>(b);
-  uint32_t *gflag = A.take<uint32_t>(b), *gpos = A.take<uint32_t>(b);
+  uint32_t *gflag = A.take<uint32_t>(b);
   uint32_t *g_start = A.take<uint32_t>(b + 1);
   uint8_t *gtype = A.take<uint8_t>(b), *glev = A.take<uint8_t>(b);
   uint32_t *gw0 = A.take<uint32_t>(b), *gw1 = A.take<uint32_t>(b);
@@ -1259,10 +1267,9 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   SST_LAUNCH(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,
              p_ul, p_x, wv, p_w, lS, lc, p_S, p_c);
   SST_LAUNCH(k_group_flags, blocks_for(b), kTB, 0, s, p_ul, &P->n_items, b, gflag);
-  SST_CUDA_TRY((scan<uint32_t, OpAdd>(gflag, gpos, b, 0u, OpAdd{}, true, false,
-                                      &P->n_groups, A, s)));
-  SST_LAUNCH(k_group_start, blocks_for(b), kTB, 0, s, gflag, gpos, &P->n_items,
-             &P->n_groups, b, g_start);
+  SST_CUDA_TRY((scan_epi<uint32_t, OpAdd, GroupStartEpi>(
+      gflag, b, 0u, OpAdd{}, true, false, &P->n_groups, A, s, nullptr,
+      GroupStartEpi{gflag, &P->n_items, b, g_start}, false)));
   // 6: classify (grids capped: the kernels stride over the device count)
   const unsigned cap_blocks = (unsigned)g->sms * 8;
   const unsigned tgrid = std::min(blocks_for(b), cap_blocks);

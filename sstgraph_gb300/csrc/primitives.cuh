@@ -150,8 +150,18 @@ constexpr uint64_t kScanOneBlockTiles = 8;
 // buffer (stride kScanItems+1, no bank conflicts for 4-byte elements), and
 // the block then stores the tile striped, so each store instruction writes
 // whole sectors.
+// A scan's results go to an epilogue: epi(i, r) for element i (its index
+// in the array, whatever the scan direction) and its result r.  StoreOut
+// writes them out; a fused consumer (the update pipeline's compactions)
+// uses them in place, saving the launch that would read them back.
 template <typename T>
-__device__ __forceinline__ void store_tile(T *out, uint64_t base, uint64_t n,
+struct StoreOut {
+  T *out;
+  __device__ __forceinline__ void operator()(uint64_t i, T r) const { out[i] = r; }
+};
+
+template <typename T, typename Epi>
+__device__ __forceinline__ void store_tile(const Epi &epi, uint64_t base, uint64_t n,
                                            bool reverse, const T *vals) {
   __shared__ T sbuf[kScanThreads * (kScanItems + 1)];
 #pragma unroll
@@ -163,8 +173,8 @@ __device__ __forceinline__ void store_tile(T *out, uint64_t base, uint64_t n,
     const uint32_t e = (uint32_t)k * kScanThreads + threadIdx.x;
     const uint64_t i = base + e;
     if (i < n)
-      out[reverse ? n - 1 - i : i] =
-          sbuf[(e / kScanItems) * (kScanItems + 1) + e % kScanItems];
+      epi(reverse ? n - 1 - i : i,
+          sbuf[(e / kScanItems) * (kScanItems + 1) + e % kScanItems]);
   }
   __syncthreads();
 }
@@ -198,8 +208,8 @@ __global__ void k_scan_reduce(const T *__restrict__ in, uint64_t n, T identity,
   if (threadIdx.x == 0) range_sums[blockIdx.x] = total;
 }
 
-template <typename T, typename Op>
-__global__ void k_scan_ranges(const T *__restrict__ in, T *__restrict__ out,
+template <typename T, typename Op, typename Epi = StoreOut<T>>
+__global__ void k_scan_ranges(const T *__restrict__ in, Epi out,
                               uint64_t n, T identity, Op op, bool reverse,
                               bool exclusive, uint64_t tiles_per_range,
                               const T *__restrict__ range_sums,
@@ -246,8 +256,8 @@ __global__ void k_scan_ranges(const T *__restrict__ in, T *__restrict__ out,
 }
 
 // one-tile scan (n <= kScanTile)
-template <typename T, typename Op>
-__global__ void k_scan_tile(const T *__restrict__ in, T *__restrict__ out,
+template <typename T, typename Op, typename Epi = StoreOut<T>>
+__global__ void k_scan_tile(const T *__restrict__ in, Epi out,
                             uint64_t n, T identity, Op op, bool reverse,
                             bool exclusive, T *__restrict__ total_out,
                             const uint32_t *__restrict__ d_n) {
@@ -387,9 +397,9 @@ __device__ T scan_lookback(const ScanStatus<T> *st, uint64_t tile,
 // aggregate, looks back for its prefix and publishes its inclusive prefix.
 // Tile b waits only on the aggregates of tiles below it, which the hardware
 // starts first and which depend on nothing.
-template <typename T, typename Op>
+template <typename T, typename Op, typename Epi = StoreOut<T>>
 __global__ void __launch_bounds__(kScanThreads)
-k_scan_lb(const T *__restrict__ in, T *__restrict__ out, uint64_t n,
+k_scan_lb(const T *__restrict__ in, Epi out, uint64_t n,
           T identity, Op op, bool reverse, bool exclusive,
           T *__restrict__ total_out, const uint32_t *__restrict__ d_n,
           ScanStatus<T> *st, unsigned long long tag) {
@@ -438,13 +448,16 @@ inline bool stream_capturing(cudaStream_t s) {
   return cs != cudaStreamCaptureStatusNone;
 }
 
-// Scan of n elements (in may equal out).  total_out (device, may be null)
-// receives the reduction of all n elements.  With d_n (device, may be null)
-// only the first min(n, *d_n) elements are scanned; n sizes the launch.
-template <typename T, typename Op>
-cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
-                 bool exclusive, bool reverse, T *total_out, Arena &arena,
-                 cudaStream_t s, const uint32_t *d_n = nullptr) {
+// Scan of n elements whose results go to the epilogue epi (StoreOut for a
+// plain scan; see store_tile).  total_out (device, may be null) receives the
+// reduction of all n elements.  With d_n (device, may be null) only the first
+// min(n, *d_n) elements are scanned; n sizes the launch.  in_place: the
+// epilogue writes the input array (the single-pass form, whose bounded
+// look-back may reread inputs, is not used then).
+template <typename T, typename Op, typename Epi>
+cudaError_t scan_epi(const T *in, uint64_t n, T identity, Op op, bool exclusive,
+                     bool reverse, T *total_out, Arena &arena, cudaStream_t s,
+                     const uint32_t *d_n, Epi epi, bool in_place) {
   if (n == 0) {
     if (total_out) return cudaMemcpyAsync(total_out, &identity, sizeof(T),
                                           cudaMemcpyHostToDevice, s);
@@ -452,18 +465,18 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
   }
   const uint64_t tiles = (n + kScanTile - 1) / kScanTile;
   if (tiles == 1) {
-    SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_tile<T, Op>), 1, kScanThreads, 0, s,
-                 in, out, n, identity, op, reverse, exclusive, total_out, d_n);
+    SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_tile<T, Op, Epi>), 1, kScanThreads, 0, s,
+                 in, epi, n, identity, op, reverse, exclusive, total_out, d_n);
     return cudaGetLastError();
   }
   // one launch with look-back, unless the scan is in place (the bounded
   // look-back's fallback rereads inputs) or being captured into a graph (a
   // replay would reuse the launch's tag)
-  if (in != out && !stream_capturing(s)) {
+  if (!in_place && !stream_capturing(s)) {
     ScanStatus<T> *st = arena.take<ScanStatus<T>>(tiles);
     if (st) {
-      SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_lb<T, Op>), (unsigned)tiles,
-                   kScanThreads, 0, s, in, out, n, identity, op, reverse,
+      SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_lb<T, Op, Epi>), (unsigned)tiles,
+                   kScanThreads, 0, s, in, epi, n, identity, op, reverse,
                    exclusive, total_out, d_n, st, next_scan_tag());
       return cudaGetLastError();
     }
@@ -471,8 +484,8 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
   if (tiles <= kScanOneBlockTiles) {
     // one block walks the tiles with a running carry: one launch, where the
     // two-launch form would pay a second launch's latency for little work
-    SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_ranges<T, Op>), 1, kScanThreads, 0,
-                 s, in, out, n, identity, op, reverse, exclusive, tiles,
+    SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_ranges<T, Op, Epi>), 1, kScanThreads, 0,
+                 s, in, epi, n, identity, op, reverse, exclusive, tiles,
                  (const T *)nullptr, total_out, d_n);
     return cudaGetLastError();
   }
@@ -484,10 +497,19 @@ cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
   // the reduce reads the input; the scan reads it again and writes the output
   SST_LAUNCH_B(sizeof(T) * n, (k_scan_reduce<T, Op>), (unsigned)used, kScanThreads,
                0, s, in, n, identity, op, reverse, per, sums, d_n);
-  SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_ranges<T, Op>), (unsigned)used,
-               kScanThreads, 0, s, in, out, n, identity, op, reverse, exclusive,
+  SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_ranges<T, Op, Epi>), (unsigned)used,
+               kScanThreads, 0, s, in, epi, n, identity, op, reverse, exclusive,
                per, (const T *)sums, total_out, d_n);
   return cudaGetLastError();
+}
+
+// Scan of n elements into out (in may equal out).
+template <typename T, typename Op>
+cudaError_t scan(const T *in, T *out, uint64_t n, T identity, Op op,
+                 bool exclusive, bool reverse, T *total_out, Arena &arena,
+                 cudaStream_t s, const uint32_t *d_n = nullptr) {
+  return scan_epi<T, Op, StoreOut<T>>(in, n, identity, op, exclusive, reverse, total_out,
+                                      arena, s, d_n, StoreOut<T>{out}, in == out);
 }
 
 // scratch bytes a scan of n elements of T takes from the arena: the tile
