@@ -110,22 +110,47 @@ __device__ __forceinline__ uint32_t warp_sum_lcnt(const uint8_t *lc,
 constexpr uint32_t kMultiLeaf = 1u << 8;
 
 // ---------------------------------------------------------------- steps 1-5
+// Keys of a batch.  Two forms:
+//  - nkeys null: key i of pair i, the sentinel n << dbits for a pair that
+//    is dropped (an id out of range, or a self-loop the insert skips); the
+//    stable sort keeps equal keys in input order (weighted graphs: the last
+//    value wins);
+//  - nkeys set: only the kept keys, packed to the front in any order
+//    (*nkeys of them, a warp reservation each); equal keys are equal there,
+//    so their order does not matter, and the sort needs no bit for the
+//    sentinel row.
 __global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
                             uint32_t n, uint32_t width, int dbits,
                             bool drop_loops, uint64_t *__restrict__ keys,
                             unsigned long long *__restrict__ invalid,
                             const uint32_t *__restrict__ w,
-                            uint32_t *__restrict__ wv) {
-  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= b) return;
-  // weighted graphs: the pair's value (1 when the call gives none) rides
-  // with the key through the sort
-  if (wv) wv[i] = w ? w[i] : 1u;
-  uint32_t r = pairs[2 * i], c = pairs[2 * i + 1];
-  const uint64_t sent = (uint64_t)n << dbits;
-  bool ok = r < n && c < width && c != kEmpty;
-  if (!ok) atomicAdd(invalid, 1ull);
-  keys[i] = (!ok || (drop_loops && r == c)) ? sent : (((uint64_t)r << dbits) | c);
+                            uint32_t *__restrict__ wv,
+                            uint32_t *__restrict__ nkeys) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in = i < b;
+  uint32_t r = 0, c = 0;
+  bool ok = false;
+  if (in) {
+    // weighted graphs: the pair's value (1 when the call gives none) rides
+    // with the key through the sort
+    if (wv) wv[i] = w ? w[i] : 1u;
+    r = pairs[2 * i];
+    c = pairs[2 * i + 1];
+    ok = r < n && c < width && c != kEmpty;
+    if (!ok) atomicAdd(invalid, 1ull);
+  }
+  const bool keep = ok && !(drop_loops && r == c);
+  const uint64_t key = ((uint64_t)r << dbits) | c;
+  if (!nkeys) {
+    if (in) keys[i] = keep ? key : (uint64_t)n << dbits;
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  const uint32_t m = __ballot_sync(0xffffffffu, keep);
+  uint32_t at = 0;
+  if (lane == 0 && m) at = atomicAdd(nkeys, (uint32_t)__popc(m));
+  at = __shfl_sync(0xffffffffu, at, 0);
+  if (keep) keys[at + __popc(m & ((1u << lane) - 1u))] = key;
 }
 
 // Of a run of equal keys the last (in input order: the sort is stable) is
@@ -137,12 +162,15 @@ __global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
                          uint32_t *__restrict__ flag,
                          uint32_t *__restrict__ leaf_out,
                          const uint32_t *__restrict__ wv,
-                         uint64_t *__restrict__ lS, uint32_t *__restrict__ lc) {
+                         uint64_t *__restrict__ lS, uint32_t *__restrict__ lc,
+                         const uint32_t *__restrict__ nkeys) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b) return;
   const uint64_t sent = (uint64_t)g.n << dbits;
-  uint64_t k = keys[i];
-  if (k >= sent || (i + 1 < b && keys[i + 1] == k)) {
+  // a compacting key build leaves nkeys sorted keys and nothing after them
+  const uint64_t nk = nkeys ? *nkeys : b;
+  uint64_t k = i < nk ? keys[i] : sent;
+  if (k >= sent || (i + 1 < nk && keys[i + 1] == k)) {
     flag[i] = 0;
     leaf_out[i] = 0;
     return;
@@ -1242,11 +1270,15 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
 
   // 1-2: keys and sort
   const uint64_t *sorted = presorted;
+  uint32_t *nkeys = nullptr;
   if (!presorted) {
     // pair in (8 B), key out (8 B)
+    // unweighted keys are compacted (see k_make_keys): their rows are below
+    // n, one bit fewer to sort when n is a power of two
+    nkeys = wt ? nullptr : &P->n_keys;
     SST_LAUNCH_B(16 * b, k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n, g->width,
                dbits, insert && !g->keep_loops, keys,
-               reinterpret_cast<unsigned long long *>(&P->invalid), d_w, wv);
+               reinterpret_cast<unsigned long long *>(&P->invalid), d_w, wv, nkeys);
     uint64_t *out = keys;
     if (wt) {
       uint32_t *wout = wv;
@@ -1254,14 +1286,15 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                                  &out, &wout));
       wv = wout;
     } else {
-      SST_CUDA_TRY(radix_sort_u64(keys, ktmp, b, g->rbits + dbits, A, s, &out));
+      SST_CUDA_TRY(radix_sort_u64(keys, ktmp, b, bits_for(g->n ? g->n - 1 : 0) + dbits,
+                                  A, s, &out, nkeys));
     }
     sorted = out;
   }
   // 3-5: locate, pack, group
   // sorted key in (8 B), flag and leaf out (8 B)
   SST_LAUNCH_B(16 * b, k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg,
-               insert, flag, leaf, wt ? wv : nullptr, lS, lc);
+               insert, flag, leaf, wt ? wv : nullptr, lS, lc, nkeys);
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(flag, pos, b, 0u, OpAdd{}, true, false,
                                       &P->n_items, A, s)));
   SST_LAUNCH(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,

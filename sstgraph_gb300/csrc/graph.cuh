@@ -24,6 +24,7 @@ struct PlanSummary {
   uint64_t invalid;      // pairs with an id out of range
   uint32_t class_cnt[kNumClasses];  // new segments per capacity class
   unsigned long long apply_err;     // staged ranks out of range (must be 0)
+  uint32_t n_keys;                  // keys kept by a compacting key build
 };
 
 // Flattened list of all leaves in vertex order: the iteration space of the

@@ -223,7 +223,8 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *wsum) 
 __global__ void __launch_bounds__(kThreads)
 k_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
        uint32_t *__restrict__ hist, uint32_t dstride, uint32_t bstride,
-       uint32_t *__restrict__ zero) {
+       uint32_t *__restrict__ zero, const uint32_t *__restrict__ d_n) {
+  if (d_n && *d_n < n) n = *d_n;
   __shared__ uint32_t h[kRadix];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -262,7 +263,9 @@ k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
           uint64_t n, int shift, const uint32_t *__restrict__ hist,
           uint32_t nblocks, bool raw, const uint32_t *__restrict__ vin,
           uint32_t *__restrict__ vout, uint32_t *__restrict__ hist_next,
-          int next_shift, uint32_t *__restrict__ hist_zero) {
+          int next_shift, uint32_t *__restrict__ hist_zero,
+          const uint32_t *__restrict__ d_n) {
+  if (d_n && *d_n < n) n = *d_n;
   extern __shared__ __align__(16) unsigned char smem[];
   uint64_t *skeys = reinterpret_cast<uint64_t *>(smem);
   uint32_t *svals = reinterpret_cast<uint32_t *>(smem + (size_t)kTile * 8);
@@ -326,7 +329,7 @@ k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
   }
   __syncthreads();
   if (hist_zero) hist_zero[(uint64_t)blockIdx.x * kRadix + threadIdx.x] = 0;
-  const uint32_t tn = (uint32_t)(n - t0 < (uint64_t)kTile ? n - t0 : kTile);
+  const uint32_t tn = t0 >= n ? 0u : (uint32_t)(n - t0 < (uint64_t)kTile ? n - t0 : kTile);
   for (uint32_t j = threadIdx.x; j < tn; j += kThreads) {
     const uint64_t key = skeys[j];
     const uint32_t pos = adj[(key >> shift) & 0xff] + j;
@@ -359,7 +362,8 @@ cudaError_t scatter_smem_optin() {
 template <bool KV, int TILE>
 __global__ void __launch_bounds__(kThreads)
 k_sort_small(uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
-             uint64_t n, int bits) {
+             uint64_t n, int bits, const uint32_t *__restrict__ d_n) {
+  if (d_n && *d_n < n) n = *d_n;
   constexpr int IT = TILE / kThreads;
   __shared__ uint64_t buf[2][TILE];
   __shared__ uint32_t vbuf[KV ? 2 : 1][KV ? TILE : 1];
@@ -425,18 +429,19 @@ size_t radix_sort_scratch_bytes(uint64_t n) {
 static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
                                    uint32_t *vals, uint32_t *vtmp, uint64_t n,
                                    int bits, Arena &arena, cudaStream_t s,
-                                   uint64_t **result, uint32_t **vresult) {
+                                   uint64_t **result, uint32_t **vresult,
+                                   const uint32_t *d_n) {
   *result = keys;
   if (vresult) *vresult = vals;
   if (n < 2 || bits <= 0) return cudaSuccess;
   if (!vals && n <= (uint64_t)kSmallSort) {
     SST_LAUNCH_B(16 * n, (k_sort_small<false, kSmallSort>), 1, kThreads, 0, s, keys,
-               (uint32_t *)nullptr, n, bits);
+               (uint32_t *)nullptr, n, bits, d_n);
     return cudaGetLastError();
   }
   if (vals && n <= (uint64_t)kSmallSortKV) {
     SST_LAUNCH_B(24 * n, (k_sort_small<true, kSmallSortKV>), 1, kThreads, 0, s, keys, vals,
-               n, bits);
+               n, bits, d_n);
     return cudaGetLastError();
   }
   const uint32_t nblocks = (uint32_t)((n + kTile - 1) / kTile);
@@ -457,7 +462,7 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
     for (auto &t : h)
       if (!(t = arena.take<uint32_t>(hn))) return cudaErrorMemoryAllocation;
     SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, 0, h[0],
-                 1u, (uint32_t)kRadix, h[1]);
+                 1u, (uint32_t)kRadix, h[1], d_n);
     int p = 0;
     for (int shift = 0; shift < bits; shift += 8, p++) {
       const bool more = shift + 8 < bits;
@@ -467,12 +472,12 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
         SST_LAUNCH_B(scatter_bytes, k_scatter<true>, nblocks, kThreads,
                      scatter_smem_bytes<true>(), s, src,
                      dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
-                     shift + 8, zr);
+                     shift + 8, zr, d_n);
       else
         SST_LAUNCH_B(scatter_bytes, k_scatter<false>, nblocks, kThreads,
                      scatter_smem_bytes<false>(), s, src,
                      dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
-                     shift + 8, zr);
+                     shift + 8, zr, d_n);
       std::swap(src, dst);
       std::swap(vsrc, vdst);
     }
@@ -484,7 +489,7 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
     if (!cnts || !hist) return cudaErrorMemoryAllocation;
     for (int shift = 0; shift < bits; shift += 8) {
       SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, shift,
-                   cnts, nblocks, 1u, (uint32_t *)nullptr);
+                   cnts, nblocks, 1u, (uint32_t *)nullptr, d_n);
       size_t mark = arena.used;
       cudaError_t e = scan<uint32_t, OpAdd>(cnts, hist, hn, 0u, OpAdd{}, true,
                                             false, nullptr, arena, s);
@@ -494,12 +499,12 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
         SST_LAUNCH_B(scatter_bytes, k_scatter<true>, nblocks, kThreads,
                      scatter_smem_bytes<true>(), s, src,
                      dst, n, shift, hist, nblocks, false, vsrc, vdst,
-                     (uint32_t *)nullptr, 0, (uint32_t *)nullptr);
+                     (uint32_t *)nullptr, 0, (uint32_t *)nullptr, d_n);
       else
         SST_LAUNCH_B(scatter_bytes, k_scatter<false>, nblocks, kThreads,
                      scatter_smem_bytes<false>(), s, src,
                      dst, n, shift, hist, nblocks, false, vsrc, vdst,
-                     (uint32_t *)nullptr, 0, (uint32_t *)nullptr);
+                     (uint32_t *)nullptr, 0, (uint32_t *)nullptr, d_n);
       std::swap(src, dst);
       std::swap(vsrc, vdst);
     }
@@ -510,16 +515,17 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
 }
 
 cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
-                           Arena &arena, cudaStream_t s, uint64_t **result) {
+                           Arena &arena, cudaStream_t s, uint64_t **result,
+                           const uint32_t *d_n) {
   return radix_sort_impl(keys, tmp, nullptr, nullptr, n, bits, arena, s, result,
-                         nullptr);
+                         nullptr, d_n);
 }
 
 cudaError_t radix_sort_kv(uint64_t *keys, uint64_t *tmp, uint32_t *vals,
                           uint32_t *vtmp, uint64_t n, int bits, Arena &arena,
                           cudaStream_t s, uint64_t **result, uint32_t **vresult) {
   return radix_sort_impl(keys, tmp, vals, vtmp, n, bits, arena, s, result,
-                         vresult);
+                         vresult, nullptr);
 }
 
 }  // namespace sst

@@ -531,8 +531,11 @@ constexpr int kSmallSort = 2048;
 cudaError_t radix_sort_kv(uint64_t *keys, uint64_t *tmp, uint32_t *vals,
                           uint32_t *vtmp, uint64_t n, int bits, Arena &arena,
                           cudaStream_t s, uint64_t **result, uint32_t **vresult);
+// d_n (device, may be null): sort only the first min(n, *d_n) keys; n sizes
+// the launches, the rest of the arrays is left as it was
 cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
-                           Arena &arena, cudaStream_t s, uint64_t **result);
+                           Arena &arena, cudaStream_t s, uint64_t **result,
+                           const uint32_t *d_n = nullptr);
 size_t radix_sort_scratch_bytes(uint64_t n);
 
 }  // namespace sst
