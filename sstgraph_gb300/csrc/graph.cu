@@ -110,47 +110,84 @@ __device__ __forceinline__ uint32_t warp_sum_lcnt(const uint8_t *lc,
 constexpr uint32_t kMultiLeaf = 1u << 8;
 
 // ---------------------------------------------------------------- steps 1-5
-// Keys of a batch.  Two forms:
-//  - nkeys null: key i of pair i, the sentinel n << dbits for a pair that
-//    is dropped (an id out of range, or a self-loop the insert skips); the
-//    stable sort keeps equal keys in input order (weighted graphs: the last
-//    value wins);
-//  - nkeys set: only the kept keys, packed to the front in any order
-//    (*nkeys of them, a warp reservation each); equal keys are equal there,
-//    so their order does not matter, and the sort needs no bit for the
-//    sentinel row.
+// Keys of a batch, in one of two forms.
+// k_make_keys: key i of pair i, the sentinel n << dbits for a pair that is
+// dropped (an id out of range, or a self-loop the insert skips); the stable
+// sort keeps equal keys in input order (weighted graphs: the last value
+// given wins).
 __global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
                             uint32_t n, uint32_t width, int dbits,
                             bool drop_loops, uint64_t *__restrict__ keys,
                             unsigned long long *__restrict__ invalid,
                             const uint32_t *__restrict__ w,
-                            uint32_t *__restrict__ wv,
-                            uint32_t *__restrict__ nkeys) {
+                            uint32_t *__restrict__ wv) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool in = i < b;
-  uint32_t r = 0, c = 0;
-  bool ok = false;
-  if (in) {
-    // weighted graphs: the pair's value (1 when the call gives none) rides
-    // with the key through the sort
-    if (wv) wv[i] = w ? w[i] : 1u;
-    r = pairs[2 * i];
-    c = pairs[2 * i + 1];
-    ok = r < n && c < width && c != kEmpty;
-    if (!ok) atomicAdd(invalid, 1ull);
+  if (i >= b) return;
+  // weighted graphs: the pair's value (1 when the call gives none) rides
+  // with the key through the sort
+  if (wv) wv[i] = w ? w[i] : 1u;
+  const uint32_t r = pairs[2 * i], c = pairs[2 * i + 1];
+  const bool ok = r < n && c < width && c != kEmpty;
+  if (!ok) atomicAdd(invalid, 1ull);
+  keys[i] = (!ok || (drop_loops && r == c)) ? (uint64_t)n << dbits
+                                            : (((uint64_t)r << dbits) | c);
+}
+
+// k_make_keys_packed: only the kept keys, packed to the front in any order
+// (*nkeys of them; one reservation per block of kPackItems x 256 pairs).
+// Equal keys are equal, so their order does not matter (unweighted
+// graphs), and the sort needs no bit for the sentinel row.
+constexpr int kPackItems = 8;
+__global__ void __launch_bounds__(256)
+k_make_keys_packed(const uint32_t *__restrict__ pairs, uint64_t b, uint32_t n,
+                   uint32_t width, int dbits, bool drop_loops,
+                   uint64_t *__restrict__ keys,
+                   unsigned long long *__restrict__ invalid,
+                   uint32_t *__restrict__ nkeys) {
+  __shared__ uint32_t s_warp[8];
+  __shared__ uint32_t s_base;
+  const uint64_t t0 = (uint64_t)blockIdx.x * (256 * kPackItems);
+  uint64_t key[kPackItems];
+  uint32_t kept = 0, bad = 0;  // bit k: item k is kept
+#pragma unroll
+  for (int k = 0; k < kPackItems; k++) {
+    const uint64_t i = t0 + (uint64_t)k * 256 + threadIdx.x;
+    uint32_t r = 0, c = 0;
+    if (i < b) {
+      r = pairs[2 * i];
+      c = pairs[2 * i + 1];
+    }
+    const bool ok = i < b && r < n && c < width && c != kEmpty;
+    bad += i < b && !ok;
+    if (ok && !(drop_loops && r == c)) kept |= 1u << k;
+    key[k] = ((uint64_t)r << dbits) | c;
   }
-  const bool keep = ok && !(drop_loops && r == c);
-  const uint64_t key = ((uint64_t)r << dbits) | c;
-  if (!nkeys) {
-    if (in) keys[i] = keep ? key : (uint64_t)n << dbits;
-    return;
+  const uint32_t keep = __popc(kept);
+  if (bad) atomicAdd(invalid, (unsigned long long)bad);
+  // block prefix of the kept counts, one reservation for the block
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = keep;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t o = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= d) inc += o;
   }
-  const int lane = threadIdx.x & 31;
-  const uint32_t m = __ballot_sync(0xffffffffu, keep);
-  uint32_t at = 0;
-  if (lane == 0 && m) at = atomicAdd(nkeys, (uint32_t)__popc(m));
-  at = __shfl_sync(0xffffffffu, at, 0);
-  if (keep) keys[at + __popc(m & ((1u << lane) - 1u))] = key;
+  if (lane == 31) s_warp[warp] = inc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (int w = 0; w < 8; w++) {
+      const uint32_t c = s_warp[w];
+      s_warp[w] = tot;
+      tot += c;
+    }
+    s_base = tot ? atomicAdd(nkeys, tot) : 0u;
+  }
+  __syncthreads();
+  const uint64_t at = (uint64_t)s_base + s_warp[warp] + inc - keep;
+#pragma unroll
+  for (int k = 0; k < kPackItems; k++)
+    if ((kept >> k) & 1u) keys[at + __popc(kept & ((1u << k) - 1u))] = key[k];
 }
 
 // Of a run of equal keys the last (in input order: the sort is stable) is
@@ -1276,9 +1313,14 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     // unweighted keys are compacted (see k_make_keys): their rows are below
     // n, one bit fewer to sort when n is a power of two
     nkeys = wt ? nullptr : &P->n_keys;
-    SST_LAUNCH_B(16 * b, k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n, g->width,
-               dbits, insert && !g->keep_loops, keys,
-               reinterpret_cast<unsigned long long *>(&P->invalid), d_w, wv, nkeys);
+    if (wt)
+      SST_LAUNCH_B(16 * b, k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n,
+                   g->width, dbits, insert && !g->keep_loops, keys,
+                   reinterpret_cast<unsigned long long *>(&P->invalid), d_w, wv);
+    else
+      SST_LAUNCH_B(16 * b, k_make_keys_packed, blocks_for(b, kTB * kPackItems), kTB, 0, s,
+                   d_pairs, b, g->n, g->width, dbits, insert && !g->keep_loops, keys,
+                   reinterpret_cast<unsigned long long *>(&P->invalid), nkeys);
     uint64_t *out = keys;
     if (wt) {
       uint32_t *wout = wv;
