@@ -756,26 +756,25 @@ k_leaf_merge(DGraph g, const uint32_t *__restrict__ p_x,
   }
 }
 
-__device__ __forceinline__ uint64_t task_of(const uint64_t *off, uint32_t ntasks,
-                                            uint64_t idx) {
-  // last task whose offset <= idx (offsets non-decreasing; a task with zero
-  // leaves shares its offset with the next one)
-  uint64_t lo = 0, hi = ntasks;
-  while (hi - lo > 1) {
-    uint64_t mid = (lo + hi) >> 1;
-    if (off[mid] <= idx)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
+// the task of every source and destination leaf of the window / resize
+// tasks (a warp per task fills its two ranges), so the apply kernels find a
+// leaf's task with one load, not a binary search over the offsets
+__global__ void k_task_index(Tasks t, uint32_t ntasks, uint32_t *__restrict__ stask,
+                             uint32_t *__restrict__ dtask) {
+  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= ntasks) return;
+  const uint64_t s0 = t.soff[w], ns = t.nsrc[w], d0 = t.doff[w], nd = t.ndst[w];
+  for (uint64_t j = lane; j < ns; j += 32) stask[s0 + j] = (uint32_t)w;
+  for (uint64_t j = lane; j < nd; j += 32) dtask[d0 + j] = (uint32_t)w;
 }
 
 __global__ void k_src_counts(DGraph g, Tasks t, uint32_t ntasks,
-                             uint64_t nsrc_total, uint64_t *__restrict__ scnt) {
+                             uint64_t nsrc_total, uint64_t *__restrict__ scnt,
+                             const uint32_t *__restrict__ stask) {
   uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsrc_total) return;
-  uint64_t tau = task_of(t.soff, ntasks, s);
+  uint64_t tau = stask[s];
   uint32_t u = t.u[tau];
   uint32_t l = t.w0[tau] + (uint32_t)(s - t.soff[tau]);
   scnt[s] = leaf_count(g, g.base[u], g.cap[u], g.deg[u], l);
@@ -786,13 +785,12 @@ __global__ void k_gather_old(DGraph g, Tasks t, uint32_t ntasks,
                              uint64_t nsrc_total,
                              const uint64_t *__restrict__ spre,
                              const uint32_t *__restrict__ p_x,
-                             uint32_t *__restrict__ stage) {
+                             uint32_t *__restrict__ stage,
+                             const uint32_t *__restrict__ stask) {
   uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (s >= nsrc_total) return;
-  // lane 0 finds the leaf's task; the warp shares it
-  uint64_t tau = lane == 0 ? task_of(t.soff, ntasks, s) : 0;
-  tau = __shfl_sync(0xffffffffu, tau, 0);
+  const uint64_t tau = stask[s];
   uint32_t u = t.u[tau];
   uint32_t l = t.w0[tau] + (uint32_t)(s - t.soff[tau]);
   uint64_t base = g.base[u];
@@ -865,14 +863,15 @@ __device__ __forceinline__ uint64_t task_new_base(const Tasks &t, uint64_t tau,
 __global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
                                uint64_t ndst_total,
                                const uint64_t *__restrict__ class_start,
-                               const uint32_t *__restrict__ stage) {
+                               const uint32_t *__restrict__ stage,
+                               const uint32_t *__restrict__ dtask) {
   uint64_t d = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (d >= ndst_total) return;
   uint64_t S = 0, src = 0;
   uint32_t cnt = 0, leafsize = kLeaf, multi = 1;
   if (lane == 0) {
-    uint64_t tau = task_of(t.doff, ntasks, d);
+    const uint64_t tau = dtask[d];
     uint32_t i = (uint32_t)(d - t.doff[tau]);
     uint32_t NL = (uint32_t)t.ndst[tau], T = (uint32_t)t.total[tau];
     uint32_t per = T / NL, ext = T - per * NL;
@@ -1432,8 +1431,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   SST_CUDA_TRY(cudaMemcpyAsync(cstart, hs, sizeof(hstart), cudaMemcpyHostToDevice, s));
 
   // staging for window / resize tasks
-  size_t wneed = ps.task_elems * (g->weighted ? 8 : 4) + ps.src_leaves * 16 +
-                 scan_scratch_bytes(ps.src_leaves, 8) + 4096;
+  size_t wneed = ps.task_elems * (g->weighted ? 8 : 4) + ps.src_leaves * 20 +
+                 ps.dst_leaves * 4 + scan_scratch_bytes(ps.src_leaves, 8) + 4096;
   if (wneed > g->work.cap) {
     sst_status st = budget_check(g, wneed - g->work.cap);
     if (st != SST_OK) return st;
@@ -1444,6 +1443,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   if (g->weighted) T.stage_v = g->work.take<uint32_t>(ps.task_elems);
   uint64_t *scnt = g->work.take<uint64_t>(ps.src_leaves);
   uint64_t *spre = g->work.take<uint64_t>(ps.src_leaves);
+  uint32_t *stask = g->work.take<uint32_t>(ps.src_leaves);
+  uint32_t *dtask = g->work.take<uint32_t>(ps.dst_leaves);
 
   // 9: apply
   if (insert && ps.n_merge)
@@ -1453,21 +1454,24 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                  std::min(warp_blocks((ps.n_merge + 31) / 32), (unsigned)g->sms * 8),
                  kTB, 0, s, dg, p_x, p_S, p_c, merge_jk, ps.n_merge, p_w);
   if (ps.n_tasks) {
+    if (ps.src_leaves || ps.dst_leaves)
+      SST_LAUNCH(k_task_index, warp_blocks(ps.n_tasks), kTB, 0, s, T, ps.n_tasks, stask,
+                 dtask);
     if (ps.src_leaves) {
       SST_LAUNCH(k_src_counts, blocks_for(ps.src_leaves), kTB, 0, s, dg, T,
-                 ps.n_tasks, ps.src_leaves, scnt);
+                 ps.n_tasks, ps.src_leaves, scnt, stask);
       SST_CUDA_TRY((scan<uint64_t, OpAdd>(scnt, spre, ps.src_leaves, 0ull,
                                           OpAdd{}, true, false, nullptr,
                                           g->work, s)));
       SST_LAUNCH(k_gather_old, warp_blocks(ps.src_leaves), kTB, 0, s, dg, T,
-                 ps.n_tasks, ps.src_leaves, spre, p_x, stage);
+                 ps.n_tasks, ps.src_leaves, spre, p_x, stage, stask);
     }
     if (insert && ps.n_items)
       SST_LAUNCH(k_gather_new, blocks_for(ps.n_items), kTB, 0, s, dg, T,
                  ps.n_tasks, spre, p_ul, p_x, ps.n_items, stage);
     if (ps.dst_leaves)
       SST_LAUNCH(k_task_scatter, warp_blocks(ps.dst_leaves), kTB, 0, s, dg, T,
-                 ps.n_tasks, ps.dst_leaves, cstart, stage);
+                 ps.n_tasks, ps.dst_leaves, cstart, stage, dtask);
     SST_LAUNCH(k_finalize, blocks_for(ps.n_tasks), kTB, 0, s, dg, T, ps.n_tasks,
                cstart);
   }
