@@ -57,12 +57,11 @@ int bits_for(uint64_t x) {
   return b;
 }
 
-// Lower bound (first index with a[i] >= x) in a sorted array, by a whole
-// warp (every lane gets the answer): each
-// round the 32 lanes probe 32 evenly spaced positions and the range shrinks
-// to the gap between the last probe below x and the next one, so a range of
-// 1e6 items takes four dependent rounds instead of twenty.  Searches
-// [lo, hi).
+// Lower bound (first index with a[i] >= x) of [lo, hi) in a sorted array,
+// by a whole warp (every lane gets the answer): each round the 32 lanes
+// probe 32 evenly spaced positions and the range shrinks to the gap between
+// the last probe below x and the next one, so a range of 1e6 items takes
+// four dependent rounds instead of twenty.
 __device__ __forceinline__ uint32_t warp_lb_u64(const uint64_t *a, uint32_t lo,
                                                 uint32_t hi, uint64_t x) {
   const uint32_t lane = threadIdx.x & 31;
