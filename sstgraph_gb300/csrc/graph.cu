@@ -779,14 +779,18 @@ k_leaf_merge(DGraph g, const uint32_t *__restrict__ p_x,
 // the task of every source and destination leaf of the window / resize
 // tasks (a warp per task fills its two ranges), so the apply kernels find a
 // leaf's task with one load, not a binary search over the offsets
+// (and, on an insert, the task of each new item that a task takes; itask is
+// all ones beforehand)
 __global__ void k_task_index(Tasks t, uint32_t ntasks, uint32_t *__restrict__ stask,
-                             uint32_t *__restrict__ dtask) {
+                             uint32_t *__restrict__ dtask, uint32_t *__restrict__ itask) {
   const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (w >= ntasks) return;
   const uint64_t s0 = t.soff[w], ns = t.nsrc[w], d0 = t.doff[w], nd = t.ndst[w];
   for (uint64_t j = lane; j < ns; j += 32) stask[s0 + j] = (uint32_t)w;
   for (uint64_t j = lane; j < nd; j += 32) dtask[d0 + j] = (uint32_t)w;
+  if (itask)
+    for (uint32_t j = t.newbeg[w] + lane; j < t.newend[w]; j += 32) itask[j] = (uint32_t)w;
 }
 
 __global__ void k_src_counts(DGraph g, Tasks t, uint32_t ntasks,
@@ -833,14 +837,13 @@ __global__ void k_gather_new(DGraph g, Tasks t, uint32_t ntasks,
                              const uint64_t *__restrict__ spre,
                              const uint64_t *__restrict__ p_ul,
                              const uint32_t *__restrict__ p_x, uint32_t nitems,
-                             uint32_t *__restrict__ stage) {
+                             uint32_t *__restrict__ stage,
+                             const uint32_t *__restrict__ itask) {
   uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nitems || ntasks == 0) return;
-  uint64_t key = p_ul[j];
-  if (key < t.key[0]) return;
-  uint64_t tau = last_le_u64(t.key, ntasks, key);
-  uint32_t u = (uint32_t)(key >> 32);
-  if (t.u[tau] != u || j < t.newbeg[tau] || j >= t.newend[tau]) return;
+  const uint32_t tau = itask[j];
+  if (tau == kEmpty) return;  // a leaf merge takes this item
+  const uint32_t u = (uint32_t)(p_ul[j] >> 32);
   uint32_t x = p_x[j];
   uint64_t base = g.base[u];
   uint32_t cap = g.cap[u], deg = g.deg[u];
@@ -1452,7 +1455,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
 
   // staging for window / resize tasks
   size_t wneed = ps.task_elems * (g->weighted ? 8 : 4) + ps.src_leaves * 20 +
-                 ps.dst_leaves * 4 + scan_scratch_bytes(ps.src_leaves, 8) + 4096;
+                 ps.dst_leaves * 4 + (uint64_t)ps.n_items * 4 +
+                 scan_scratch_bytes(ps.src_leaves, 8) + 4096;
   if (wneed > g->work.cap) {
     sst_status st = budget_check(g, wneed - g->work.cap);
     if (st != SST_OK) return st;
@@ -1465,6 +1469,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   uint64_t *spre = g->work.take<uint64_t>(ps.src_leaves);
   uint32_t *stask = g->work.take<uint32_t>(ps.src_leaves);
   uint32_t *dtask = g->work.take<uint32_t>(ps.dst_leaves);
+  uint32_t *itask = insert && ps.n_tasks && ps.n_items ? g->work.take<uint32_t>(ps.n_items)
+                                                       : nullptr;
 
   // 9: apply
   if (insert && ps.n_merge)
@@ -1474,9 +1480,10 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                  std::min(warp_blocks((ps.n_merge + 31) / 32), (unsigned)g->sms * 8),
                  kTB, 0, s, dg, p_x, p_S, p_c, merge_jk, ps.n_merge, p_w);
   if (ps.n_tasks) {
-    if (ps.src_leaves || ps.dst_leaves)
-      SST_LAUNCH(k_task_index, warp_blocks(ps.n_tasks), kTB, 0, s, T, ps.n_tasks, stask,
-                 dtask);
+    if (itask)
+      SST_CUDA_TRY(cudaMemsetAsync(itask, 0xFF, (uint64_t)ps.n_items * 4, s));
+    SST_LAUNCH(k_task_index, warp_blocks(ps.n_tasks), kTB, 0, s, T, ps.n_tasks, stask,
+               dtask, itask);
     if (ps.src_leaves) {
       SST_LAUNCH(k_src_counts, blocks_for(ps.src_leaves), kTB, 0, s, dg, T,
                  ps.n_tasks, ps.src_leaves, scnt, stask);
@@ -1488,7 +1495,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     }
     if (insert && ps.n_items)
       SST_LAUNCH(k_gather_new, blocks_for(ps.n_items), kTB, 0, s, dg, T,
-                 ps.n_tasks, spre, p_ul, p_x, ps.n_items, stage);
+                 ps.n_tasks, spre, p_ul, p_x, ps.n_items, stage, itask);
     if (ps.dst_leaves)
       SST_LAUNCH(k_task_scatter, warp_blocks(ps.dst_leaves), kTB, 0, s, dg, T,
                  ps.n_tasks, ps.dst_leaves, cstart, stage, dtask);
