@@ -3,7 +3,7 @@
 // (digit, tile), then a stable scatter in which every warp ranks its own
 // contiguous slice of the tile (a digit match from ballots, warp-private
 // counters), the tile is reordered in shared memory and leaves in runs of
-// one digit.  Sorts of up to 64 tiles fold the scan and the next pass's
+// one digit.  Sorts of up to 256 tiles fold the scan and the next pass's
 // counts into the scatter: one launch a pass.
 #include <algorithm>
 #include <atomic>
@@ -146,11 +146,10 @@ constexpr int kTile = kThreads * kItems;  // 4096
 constexpr int kRadix = 256;
 constexpr uint32_t kNoDigit = 0xffffffffu;  // an item past the end
 // Sorts of at most this many tiles run one launch per pass: every block
-// prefixes the raw tile counts itself and counts the next pass's digits as
-// it scatters.  Larger sorts scan the counts in separate launches: there
-// every block's keys of one digit land in the same one or two destination
-// tiles, and atomics on those counters would serialise.
-constexpr uint32_t kFuseHistBlocks = 64;  // 256K keys
+// prefixes the raw tile counts itself (reading all of them: the cost grows
+// with the square of the tiles) and counts the next pass's digits as it
+// scatters.  Larger sorts count and scan in separate launches.
+constexpr uint32_t kFuseHistBlocks = 256;  // 1M keys
 
 // Offset of this thread's item `it` in a warp-contiguous tile of ITEMS items
 // per thread: warp w owns [w * ITEMS * 32, (w + 1) * ITEMS * 32), item it of
@@ -258,7 +257,7 @@ constexpr size_t scatter_smem_bytes() {
 }
 
 template <bool KV>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
 k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
           uint64_t n, int shift, const uint32_t *__restrict__ hist,
           uint32_t nblocks, bool raw, const uint32_t *__restrict__ vin,
@@ -291,12 +290,39 @@ k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
   // gbase: output position of this tile's first key of digit threadIdx.x
   uint32_t gbase;
   if (raw) {
+    // the tiles' counts summed by the block's warps: warp w takes every
+    // kWarps-th tile row from w, each lane eight consecutive digits through
+    // two 16-byte loads; the partial sums meet in shared memory (the key
+    // staging area, unused until the write-out)
+    const int lane = threadIdx.x & 31;
+    uint32_t bef[8], tot[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) bef[k] = tot[k] = 0;
+#pragma unroll 4
+    for (uint32_t b = warp; b < nblocks; b += kWarps) {
+      const uint4 *row = reinterpret_cast<const uint4 *>(hist + (uint64_t)b * kRadix) + lane * 2;
+      const uint4 x0 = row[0], x1 = row[1];
+      const uint32_t v[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+      const bool below = b < blockIdx.x;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        tot[k] += v[k];
+        bef[k] += below ? v[k] : 0u;
+      }
+    }
+    uint32_t *pb = reinterpret_cast<uint32_t *>(smem);  // [kWarps][kRadix]
+    uint32_t *pt = pb + kWarps * kRadix;                // [kWarps][kRadix]
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      pb[warp * kRadix + lane * 8 + k] = bef[k];
+      pt[warp * kRadix + lane * 8 + k] = tot[k];
+    }
+    __syncthreads();
     uint32_t before = 0, total = 0;
-#pragma unroll 8
-    for (uint32_t b = 0; b < nblocks; b++) {
-      const uint32_t c = hist[(uint64_t)b * kRadix + threadIdx.x];
-      before += b < blockIdx.x ? c : 0u;
-      total += c;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) {
+      before += pb[w * kRadix + threadIdx.x];
+      total += pt[w * kRadix + threadIdx.x];
     }
     gbase = block_excl_scan(total, wsum) + before;
   } else {
