@@ -266,16 +266,6 @@ __global__ void k_pack(const uint64_t *__restrict__ keys,
   p_c[j] = lc[i];
 }
 
-// after a repack moved the segments: the items' leaf starts again
-__global__ void k_fix_leaf_start(DGraph g, const uint64_t *__restrict__ p_ul,
-                                 const uint32_t *__restrict__ d_nitems,
-                                 uint64_t b, uint64_t *__restrict__ p_S) {
-  uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= b || j >= *d_nitems) return;
-  const uint64_t key = p_ul[j];
-  p_S[j] = g.base[(uint32_t)(key >> 32)] + ((uint64_t)(uint32_t)key << kLeafLog);
-}
-
 __global__ void k_group_flags(const uint64_t *__restrict__ p_ul,
                               const uint32_t *__restrict__ d_nitems, uint64_t b,
                               uint32_t *__restrict__ gflag) {
@@ -714,10 +704,11 @@ __global__ void k_task_setup(DGraph g, PmaParams p, bool insert,
 __global__ void __launch_bounds__(256, 4)
 k_leaf_merge(DGraph g, const uint32_t *__restrict__ p_x,
              const uint64_t *__restrict__ p_S, const uint32_t *__restrict__ p_c,
-             const uint64_t *__restrict__ merge_jk, uint32_t nmerge,
+             const uint64_t *__restrict__ merge_jk, const uint32_t *__restrict__ d_nmerge,
              const uint32_t *__restrict__ p_w) {
   const int lane = threadIdx.x & 31;
   constexpr int Q = kGroupsPerWarp;
+  const uint32_t nmerge = *d_nmerge;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
        w * 32 < nmerge; w += nw) {
@@ -1139,6 +1130,8 @@ void graph_release(sst_graph *g) {
   trav_release(g);
   if (g->own_stream) cudaStreamDestroy(g->own_stream);
   g->own_stream = nullptr;
+  if (g->plan_ready) cudaEventDestroy(g->plan_ready);
+  g->plan_ready = nullptr;
   g->stream = nullptr;
 }
 
@@ -1416,7 +1409,17 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                                cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaMemcpyAsync(&g->h_plan->apply_err, g->d_err, 8,
                                cudaMemcpyDeviceToHost, s));
-  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  if (!g->plan_ready)
+    SST_CUDA_TRY(cudaEventCreateWithFlags(&g->plan_ready, cudaEventDisableTiming));
+  SST_CUDA_TRY(cudaEventRecord(g->plan_ready, s));
+  // 9a: the leaf merges need nothing from the host (their count is on the
+  // device), so they run while the host reads the plan and stages the rest
+  // (merges and tasks touch disjoint leaves; a repack below copies the merged
+  // leaves as they are)
+  if (insert)
+    SST_LAUNCH(k_leaf_merge, std::min(warp_blocks((b + 31) / 32), (unsigned)g->sms * 8),
+               kTB, 0, s, dg, p_x, p_S, p_c, merge_jk, &P->n_merge, p_w);
+  SST_CUDA_TRY(cudaEventSynchronize(g->plan_ready));
   SST_CUDA_TRY(cudaGetLastError());
   PlanSummary ps = *g->h_plan;
   if (ps.apply_err) {
@@ -1436,10 +1439,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     if (st != SST_OK) return st;
     dg = g->view();
     start = (g->bump + kLeaf - 1) & ~uint64_t(kLeaf - 1);
-    // segments moved: the items' leaf starts for the merges below
-    if (ps.n_items)
-      SST_LAUNCH(k_fix_leaf_start, blocks_for(ps.n_items), kTB, 0, s, dg, p_ul,
-                 &P->n_items, ps.n_items, p_S);
+    // the items' leaf starts (p_S) point into the old slab now, but the leaf
+    // merges and deletes that read them have run already
   }
   uint64_t hstart[kNumClasses];
   uint64_t off = start;
@@ -1472,13 +1473,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   uint32_t *itask = insert && ps.n_tasks && ps.n_items ? g->work.take<uint32_t>(ps.n_items)
                                                        : nullptr;
 
-  // 9: apply
-  if (insert && ps.n_merge)
-    // each merge rewrites one 128-byte leaf (read + write) and its count
-    // (the merged ids, fewer than 32 per leaf, are not counted)
-    SST_LAUNCH_B(258ull * ps.n_merge, k_leaf_merge,
-                 std::min(warp_blocks((ps.n_merge + 31) / 32), (unsigned)g->sms * 8),
-                 kTB, 0, s, dg, p_x, p_S, p_c, merge_jk, ps.n_merge, p_w);
+  // 9b: apply the window / resize tasks
   if (ps.n_tasks) {
     if (itask)
       SST_CUDA_TRY(cudaMemsetAsync(itask, 0xFF, (uint64_t)ps.n_items * 4, s));

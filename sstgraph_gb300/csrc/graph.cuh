@@ -51,6 +51,7 @@ struct sst_graph {
   int sms = 148;  // multiprocessors of the device
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  cudaEvent_t plan_ready = nullptr;  // an update's plan has reached the host
   uint32_t n = 0, width = 0;
   int rbits = 0, dbits = 0;
   sst::PmaParams params;

@@ -144,6 +144,8 @@ __device__ __forceinline__ T block_exclusive(T v, T identity, Op op, T *total) {
 constexpr int kScanRanges = 608;
 // scans of at most this many tiles (32K elements) run as one block
 constexpr uint64_t kScanOneBlockTiles = 8;
+// single-pass (look-back) scans up to this many tiles (4M elements)
+constexpr uint64_t kScanLookbackTiles = 1024;
 
 // A tile's results leave through shared memory: each thread holds items
 // t*kScanItems .. +kScanItems-1 of the tile, which it writes to a padded
@@ -470,9 +472,11 @@ cudaError_t scan_epi(const T *in, uint64_t n, T identity, Op op, bool exclusive,
     return cudaGetLastError();
   }
   // one launch with look-back, unless the scan is in place (the bounded
-  // look-back's fallback rereads inputs) or being captured into a graph (a
-  // replay would reuse the launch's tag)
-  if (!in_place && !stream_capturing(s)) {
+  // look-back's fallback rereads inputs), being captured into a graph (a
+  // replay would reuse the launch's tag) or longer than kScanLookbackTiles
+  // (past 256 tiles a look-back takes several rounds, and past about 1024
+  // the two-launch form is faster)
+  if (!in_place && tiles <= kScanLookbackTiles && !stream_capturing(s)) {
     ScanStatus<T> *st = arena.take<ScanStatus<T>>(tiles);
     if (st) {
       SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_lb<T, Op, Epi>), (unsigned)tiles,
