@@ -1132,6 +1132,11 @@ void graph_release(sst_graph *g) {
   g->own_stream = nullptr;
   if (g->plan_ready) cudaEventDestroy(g->plan_ready);
   g->plan_ready = nullptr;
+  if (g->side) cudaStreamDestroy(g->side);
+  if (g->fork_ev) cudaEventDestroy(g->fork_ev);
+  if (g->merge_done) cudaEventDestroy(g->merge_done);
+  g->side = nullptr;
+  g->fork_ev = g->merge_done = nullptr;
   g->stream = nullptr;
 }
 
@@ -1225,6 +1230,18 @@ sst_status repack(sst_graph *g, uint64_t extra) {
   cudaFree(tmp);
   return SST_OK;
 }
+
+// The graph's stream waits for an update's leaf merges on the side stream:
+// at wait(), or when the pipeline returns early.
+struct MergeJoin {
+  cudaStream_t s;
+  cudaEvent_t ev;
+  void wait() {
+    if (ev) cudaStreamWaitEvent(s, ev, 0);
+    ev = nullptr;
+  }
+  ~MergeJoin() { wait(); }
+};
 
 // bytes of arena scratch an update batch of b pairs takes
 static size_t update_scratch_bytes(uint64_t b) {
@@ -1395,6 +1412,26 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                                       reinterpret_cast<uint64_t *>(&P->n_merge), A, s)));
   SST_LAUNCH(k_emit, blocks_for(b), kTB, 0, s, mt, mtpos, b, g_start, merge_jk,
              task_group);
+  // 9a: the leaf merges need nothing more (their count is on the device):
+  // on an insert they run on a second stream from here, beside the task
+  // planning, the plan readback and the window / resize tasks.  They touch
+  // disjoint leaves: a group inside a task's window (or a resized row) is
+  // that task's, not a merge.  Every later step that could meet them -- a
+  // repack of the slab, the degree update, the end of the batch -- waits.
+  MergeJoin join{s, nullptr};
+  if (insert) {
+    if (!g->side) {
+      SST_CUDA_TRY(cudaStreamCreateWithFlags(&g->side, cudaStreamNonBlocking));
+      SST_CUDA_TRY(cudaEventCreateWithFlags(&g->fork_ev, cudaEventDisableTiming));
+      SST_CUDA_TRY(cudaEventCreateWithFlags(&g->merge_done, cudaEventDisableTiming));
+    }
+    SST_CUDA_TRY(cudaEventRecord(g->fork_ev, s));
+    SST_CUDA_TRY(cudaStreamWaitEvent(g->side, g->fork_ev, 0));
+    SST_LAUNCH(k_leaf_merge, std::min(warp_blocks((b + 31) / 32), (unsigned)g->sms * 8),
+               kTB, 0, g->side, dg, p_x, p_S, p_c, merge_jk, &P->n_merge, p_w);
+    SST_CUDA_TRY(cudaEventRecord(g->merge_done, g->side));
+    join.ev = g->merge_done;
+  }
   // 8: plan
   SST_LAUNCH(k_task_setup, wgrid, kTB, 0, s, dg, g->params, insert, p_ul,
              g_start, gtype, gw0, gw1, task_group, &P->n_tasks, &P->n_items, b, T,
@@ -1412,13 +1449,6 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   if (!g->plan_ready)
     SST_CUDA_TRY(cudaEventCreateWithFlags(&g->plan_ready, cudaEventDisableTiming));
   SST_CUDA_TRY(cudaEventRecord(g->plan_ready, s));
-  // 9a: the leaf merges need nothing from the host (their count is on the
-  // device), so they run while the host reads the plan and stages the rest
-  // (merges and tasks touch disjoint leaves; a repack below copies the merged
-  // leaves as they are)
-  if (insert)
-    SST_LAUNCH(k_leaf_merge, std::min(warp_blocks((b + 31) / 32), (unsigned)g->sms * 8),
-               kTB, 0, s, dg, p_x, p_S, p_c, merge_jk, &P->n_merge, p_w);
   SST_CUDA_TRY(cudaEventSynchronize(g->plan_ready));
   SST_CUDA_TRY(cudaGetLastError());
   PlanSummary ps = *g->h_plan;
@@ -1435,6 +1465,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   for (int c = 0; c < kNumClasses; c++) grow += (uint64_t)ps.class_cnt[c] << c;
   uint64_t start = (g->bump + kLeaf - 1) & ~uint64_t(kLeaf - 1);
   if (grow > 0 && start + grow > g->nslots) {
+    join.wait();  // the merges write the slab the repack copies and frees
     sst_status st = repack(g, grow);
     if (st != SST_OK) return st;
     dg = g->view();
@@ -1497,6 +1528,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     SST_LAUNCH(k_finalize, blocks_for(ps.n_tasks), kTB, 0, s, dg, T, ps.n_tasks,
                cstart);
   }
+  join.wait();
   if (insert)
     SST_LAUNCH(k_deg_add, blocks_for(b), kTB, 0, s, dg, p_ul, g_start,
                &P->n_groups, b);

@@ -52,6 +52,8 @@ struct sst_graph {
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
   cudaEvent_t plan_ready = nullptr;  // an update's plan has reached the host
+  cudaStream_t side = nullptr;       // an update's leaf merges, beside its tasks
+  cudaEvent_t fork_ev = nullptr, merge_done = nullptr;
   uint32_t n = 0, width = 0;
   int rbits = 0, dbits = 0;
   sst::PmaParams params;
