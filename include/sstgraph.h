@@ -87,6 +87,12 @@ SST_API sst_status sst_graph_clone(const sst_graph *g, sst_graph **out);
  * library's own stream */
 SST_API sst_status sst_set_stream(sst_graph *g, void *stream);
 SST_API sst_status sst_sync(sst_graph *g);
+/* Launch mode of update batches (no reference counterpart).  1 (default):
+ * the planning launches of a raw-pair, unweighted batch of up to 2^18 pairs
+ * (key sort to plan readback) are captured once per batch size and graph
+ * layout and replayed as one CUDA graph launch; 0: every kernel is launched
+ * directly.  Results are the same either way. */
+SST_API sst_status sst_set_plan_graphs(sst_graph *g, int enable);
 SST_API const char *sst_last_error_message(void);
 SST_API const char *sst_status_string(sst_status s);
 

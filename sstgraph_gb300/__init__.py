@@ -82,6 +82,7 @@ SIGNATURES = {
     "sst_graph_destroy": (_i32, [_vp]),
     "sst_graph_clone": (_i32, [_vp, ctypes.POINTER(_vp)]),
     "sst_set_stream": (_i32, [_vp, _vp]),
+    "sst_set_plan_graphs": (_i32, [_vp, ctypes.c_int]),
     "sst_sync": (_i32, [_vp]),
     "sst_last_error_message": (ctypes.c_char_p, []),
     "sst_status_string": (ctypes.c_char_p, [_i32]),
@@ -266,6 +267,11 @@ class SparseMatrixV:
 
     def set_stream(self, stream_ptr: int | None):
         _check(lib().sst_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def set_plan_graphs(self, enable: bool):
+        """Replay small batches' planning launches as CUDA graphs (default)
+        or launch every kernel directly; results are the same."""
+        _check(lib().sst_set_plan_graphs(self._h, 1 if enable else 0))
 
     def sync(self):
         _check(lib().sst_sync(self._h))

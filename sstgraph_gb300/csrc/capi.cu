@@ -209,6 +209,14 @@ sst_status sst_set_stream(sst_graph *g, void *stream) {
   return SST_OK;
 }
 
+sst_status sst_set_plan_graphs(sst_graph *g, int enable) {
+  CHECK_G(g);
+  SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
+  g->plan_graphs = enable != 0;
+  if (!enable) sst::plan_cache_release(g);
+  return SST_OK;
+}
+
 sst_status sst_sync(sst_graph *g) {
   CHECK_G(g);
   return sst::sync_checked(g);

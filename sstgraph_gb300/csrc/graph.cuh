@@ -9,6 +9,7 @@
 #include "primitives.cuh"
 
 namespace sst {
+struct PlanCache;  // captured planning launches of update batches (graph.cu)
 
 // Summary of a planned batch, copied to the host once per batch: it sizes
 // the apply launches, the window scratch and the slab allocation.
@@ -52,8 +53,11 @@ struct sst_graph {
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
   cudaEvent_t plan_ready = nullptr;  // an update's plan has reached the host
-  cudaStream_t side = nullptr;       // an update's leaf merges, beside its tasks
+  cudaStream_t side = nullptr;  // an update's leaf merges, beside its tasks;
+                                // its planning launches are captured here
   cudaEvent_t fork_ev = nullptr, merge_done = nullptr;
+  sst::PlanCache *plans = nullptr;  // captured planning launches
+  bool plan_graphs = true;  // replay planning launches (off: launch directly)
   uint32_t n = 0, width = 0;
   int rbits = 0, dbits = 0;
   sst::PmaParams params;
@@ -93,6 +97,7 @@ namespace sst {
 sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
                       const sst_config *cfg);
 void graph_release(sst_graph *g);
+void plan_cache_release(sst_graph *g);
 sst_status graph_clone(const sst_graph *src, sst_graph *dst);
 uint64_t graph_device_bytes(const sst_graph *g);
 

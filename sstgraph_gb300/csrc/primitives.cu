@@ -86,8 +86,12 @@ void drain(bool wait) {
 
 std::string g_prof_filter;  // profile only kernels whose name contains it
 
+static thread_local bool t_prof_paused = false;
+ProfPause::ProfPause() : prev(t_prof_paused) { t_prof_paused = true; }
+ProfPause::~ProfPause() { t_prof_paused = prev; }
+
 bool profiling(const char *name) {
-  if (!g_prof_on) return false;
+  if (!g_prof_on || t_prof_paused) return false;
   return g_prof_filter.empty() || strstr(name, g_prof_filter.c_str()) != nullptr;
 }
 

@@ -23,6 +23,13 @@ unsigned long long next_scan_tag();
 // (SST_LAUNCH_B: the bytes the kernel must read and write at its launch
 // size, independent of caching).
 bool profiling(const char *kernel_name);
+// While alive, launches from this thread are not timed one by one (a stream
+// capture records them into a graph, whose replay is timed as a whole).
+struct ProfPause {
+  ProfPause();
+  ~ProfPause();
+  bool prev;
+};
 cudaEvent_t prof_begin(cudaStream_t s);
 void prof_end(const char *name, cudaEvent_t start, cudaStream_t s,
               uint64_t bytes);
