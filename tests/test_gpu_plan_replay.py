@@ -1,5 +1,6 @@
 """Update batches up to 2^18 pairs replay their planning launches (sort to
-plan readback) from a captured CUDA graph.  The replayed form must give the
+plan readback) from a captured CUDA graph, sized by the batch's size class
+(b rounded up to m * 2^k, m in 4..7) and working on the device-side count.  The replayed form must give the
 same graph as the directly launched form (sst_set_plan_graphs off) and as
 the oracle: on cache hits with new contents, on new device buffers, after
 repacks that move the slab, past the cache's capacity and under the kernel
@@ -55,6 +56,12 @@ def test_same_size_new_contents(sg):
     run(sg, 5000, [1000] * 6 + [7, 7, 7, 1, 1, 4096, 4096, 4097], seed=1)
 
 
+def test_sizes_sharing_a_class(sg):
+    # 897..1024 share one launch size, as do 65..80 and 4097..5120
+    run(sg, 5000, [1024, 897, 1000, 1023, 897, 65, 80, 77, 66, 5120, 4097, 4500, 5000],
+        seed=8)
+
+
 def test_across_sort_forms(sg):
     # one CTA sort, single-launch passes and the largest replayed size
     run(sg, 1 << 16, [2048, 2049, 30000, 30000, (1 << 18) - 1, 1 << 18, (1 << 18) + 1],
@@ -67,8 +74,12 @@ def test_repacks_move_the_slab(sg):
 
 
 def test_more_sizes_than_cached(sg):
-    sizes = [100 + 37 * i for i in range(20)]
-    run(sg, 4000, sizes + sizes[:6], seed=4)
+    # every size class (64 .. 2^18: 49 of them, one more than the cache
+    # holds), one size below each class's bound, then the first ones again
+    classes = [64] + [m << k for k in range(4, 16) for m in (5, 6, 7, 8)]
+    assert len(classes) == 49 and classes[-1] == 1 << 18
+    sizes = [c - 1 - (c >> 4) for c in classes]
+    run(sg, 4000, sizes + sizes[:8], seed=4)
 
 
 def test_new_device_buffers(sg):
