@@ -755,6 +755,14 @@ def main():
     print(json.dumps(line))
 
 
+# DRAM bytes (read + write) per launch from one ncu capture of the kernel's
+# launches at the bench's batch sizes (dram__bytes_read.sum +
+# dram__bytes_write.sum; k_scan_lb: its 64 launches of 1e6-pair batches,
+# whose scan sizes do not depend on the graph's scale; the scans' writes stay
+# in L2 within the launch)
+NCU_TRAFFIC = {"k_scan_lb": 4.11e6}
+
+
 def update_roofline(prof, prof_all, hbm_peak, peak_kind):
     """Roofline of the update step's dominant kernel from its live event
     timings in the timed region (its share from the all-kernel warm-up).
@@ -772,7 +780,8 @@ def update_roofline(prof, prof_all, hbm_peak, peak_kind):
     share = prof_all.get(name, t)["ms"] / sum(v["ms"] for v in prof_all.values())
     out = {"bound": "hbm", "kernel": base, "launches": t["launches"],
            "ms_total": t["ms"], "share_of_step_kernel_time": share,
-           "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind, "traffic": None}
+           "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind,
+           "traffic": NCU_TRAFFIC.get(base)}
     byts = t.get("bytes", 0)
     if byts:
         ach = byts / (t["ms"] / 1e3) / 1e9
