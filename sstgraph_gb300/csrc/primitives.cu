@@ -147,6 +147,11 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kItems = 16;
 constexpr int kTile = kThreads * kItems;  // 4096
+// Sorts of at most kSmallTileKeys keys (without values) use tiles of
+// kSmallItems items per thread: four times the blocks, each ranking a
+// quarter of the keys, so a pass's dependent chain is shorter.
+constexpr int kSmallItems = 4;
+constexpr uint64_t kSmallTileKeys = 256ull * kThreads * kSmallItems;  // 2^18
 constexpr int kRadix = 256;
 constexpr uint32_t kNoDigit = 0xffffffffu;  // an item past the end
 // Sorts of at most this many tiles run one launch per pass: every block
@@ -223,6 +228,7 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *wsum) 
 // (dstride = tiles, bstride = 1) for the scanned form, tile-major
 // (dstride = 1, bstride = 256) for the fused one.  With `zero` the blocks
 // also clear that table at the same indices.
+template <int IT>
 __global__ void __launch_bounds__(kThreads)
 k_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
        uint32_t *__restrict__ hist, uint32_t dstride, uint32_t bstride,
@@ -231,9 +237,9 @@ k_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
   __shared__ uint32_t h[kRadix];
   h[threadIdx.x] = 0;
   __syncthreads();
-  const uint64_t t0 = (uint64_t)blockIdx.x * kTile;
+  const uint64_t t0 = (uint64_t)blockIdx.x * (kThreads * IT);
 #pragma unroll 4
-  for (int it = 0; it < kItems; it++) {
+  for (int it = 0; it < IT; it++) {
     uint64_t i = t0 + (uint64_t)it * kThreads + threadIdx.x;
     if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xff], 1u);
   }
@@ -253,14 +259,22 @@ k_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
 //    of each key into its destination tile's counter of hist_next (zero on
 //    entry) and clears hist_zero (the counters of the pass after next).
 //  otherwise: hist holds the scanned digit-major offsets.
-// Dynamic shared memory: scatter_smem_bytes<KV>().
-template <bool KV>
+// Dynamic shared memory: scatter_smem_bytes<KV, IT>(), IT items per thread.
+// The staging area (keys and values of the tile) also holds the raw form's
+// two [kWarps][kRadix] partial-sum tables before the ranking.
+template <bool KV, int IT>
+constexpr size_t scatter_stage_bytes() {
+  return (size_t)kThreads * IT * (KV ? 12 : 8) > (size_t)2 * kWarps * kRadix * 4
+             ? (size_t)kThreads * IT * (KV ? 12 : 8)
+             : (size_t)2 * kWarps * kRadix * 4;
+}
+template <bool KV, int IT>
 constexpr size_t scatter_smem_bytes() {
-  return (size_t)kTile * 8 + (KV ? (size_t)kTile * 4 : 0) +
-         (size_t)kWarps * kRadix * 4 + kRadix * 4 + kWarps * 4;
+  return scatter_stage_bytes<KV, IT>() + (size_t)kWarps * kRadix * 4 + kRadix * 4 +
+         kWarps * 4;
 }
 
-template <bool KV>
+template <bool KV, int IT>
 __global__ void __launch_bounds__(kThreads, 2)
 k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
           uint64_t n, int shift, const uint32_t *__restrict__ hist,
@@ -268,25 +282,26 @@ k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
           uint32_t *__restrict__ vout, uint32_t *__restrict__ hist_next,
           int next_shift, uint32_t *__restrict__ hist_zero,
           const uint32_t *__restrict__ d_n) {
+  constexpr int TILE = kThreads * IT;
   if (d_n && *d_n < n) n = *d_n;
   extern __shared__ __align__(16) unsigned char smem[];
   uint64_t *skeys = reinterpret_cast<uint64_t *>(smem);
-  uint32_t *svals = reinterpret_cast<uint32_t *>(smem + (size_t)kTile * 8);
+  uint32_t *svals = reinterpret_cast<uint32_t *>(smem + (size_t)TILE * 8);
   uint32_t(*wcnt)[kRadix] = reinterpret_cast<uint32_t(*)[kRadix]>(
-      smem + (size_t)kTile * 8 + (KV ? (size_t)kTile * 4 : 0));
+      smem + scatter_stage_bytes<KV, IT>());
   uint32_t *adj = &wcnt[kWarps - 1][kRadix - 1] + 1;  // [kRadix]
   uint32_t *wsum = adj + kRadix;                        // [kWarps]
   const int warp = threadIdx.x >> 5;
 #pragma unroll
   for (int w = 0; w < kWarps; w++) wcnt[w][threadIdx.x] = 0;
   // the tile's keys (and values) come in at once, ahead of the ranking
-  const uint64_t t0 = (uint64_t)blockIdx.x * kTile;
-  uint64_t kk[kItems];
-  uint32_t vv[KV ? kItems : 1];
-  uint32_t dg[kItems];
+  const uint64_t t0 = (uint64_t)blockIdx.x * TILE;
+  uint64_t kk[IT];
+  uint32_t vv[KV ? IT : 1];
+  uint32_t dg[IT];
 #pragma unroll
-  for (int it = 0; it < kItems; it++) {
-    const uint64_t i = t0 + tile_offset<kItems>(it);
+  for (int it = 0; it < IT; it++) {
+    const uint64_t i = t0 + tile_offset<IT>(it);
     kk[it] = i < n ? in[i] : 0;
     if (KV) vv[it] = i < n ? vin[i] : 0u;
     dg[it] = i < n ? (uint32_t)(kk[it] >> shift) & 0xff : kNoDigit;
@@ -333,8 +348,8 @@ k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
     gbase = hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x];
     __syncthreads();
   }
-  uint32_t lr[kItems];
-  warp_rank<kItems>(dg, lr, wcnt[warp]);
+  uint32_t lr[IT];
+  warp_rank<IT>(dg, lr, wcnt[warp]);
   __syncthreads();
   // tile-local start of each digit, then of each warp's share of it
   uint32_t tcount = 0;
@@ -351,7 +366,7 @@ k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
   adj[threadIdx.x] = gbase - tstart;  // output position = adj[d] + local
   __syncthreads();
 #pragma unroll
-  for (int it = 0; it < kItems; it++) {
+  for (int it = 0; it < IT; it++) {
     if (dg[it] == kNoDigit) continue;
     const uint32_t lp = wcnt[warp][dg[it]] + lr[it];
     skeys[lp] = kk[it];
@@ -359,14 +374,14 @@ k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
   }
   __syncthreads();
   if (hist_zero) hist_zero[(uint64_t)blockIdx.x * kRadix + threadIdx.x] = 0;
-  const uint32_t tn = t0 >= n ? 0u : (uint32_t)(n - t0 < (uint64_t)kTile ? n - t0 : kTile);
+  const uint32_t tn = t0 >= n ? 0u : (uint32_t)(n - t0 < (uint64_t)TILE ? n - t0 : TILE);
   for (uint32_t j = threadIdx.x; j < tn; j += kThreads) {
     const uint64_t key = skeys[j];
     const uint32_t pos = adj[(key >> shift) & 0xff] + j;
     out[pos] = key;
     if (KV) vout[pos] = svals[j];
     if (hist_next)
-      atomicAdd(&hist_next[(uint64_t)(pos / kTile) * kRadix +
+      atomicAdd(&hist_next[(uint64_t)(pos / TILE) * kRadix +
                            ((key >> next_shift) & 0xff)],
                 1u);
   }
@@ -380,8 +395,8 @@ cudaError_t scatter_smem_optin() {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 64 && ((done.load(std::memory_order_relaxed) >> dev) & 1)) return cudaSuccess;
-  e = cudaFuncSetAttribute(k_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)scatter_smem_bytes<true>());
+  e = cudaFuncSetAttribute(k_scatter<true, kItems>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)scatter_smem_bytes<true, kItems>());
   if (e == cudaSuccess && dev < 64) done.fetch_or(1ull << dev, std::memory_order_relaxed);
   return e;
 }
@@ -451,9 +466,87 @@ constexpr int kSmallSortKV = 1024;
 }  // namespace
 
 size_t radix_sort_scratch_bytes(uint64_t n) {
-  uint64_t nblocks = (n + kTile - 1) / kTile;
+  const uint64_t tile = n <= kSmallTileKeys ? (uint64_t)kThreads * kSmallItems : kTile;
+  uint64_t nblocks = (n + tile - 1) / tile;
   uint64_t hn = nblocks * kRadix;
   return 3 * ((hn * 4 + 255) & ~size_t(255)) + scan_scratch_bytes(hn, 4) + 512;
+}
+
+// The multi-tile sort with tiles of IT items per thread (see radix_sort_impl).
+template <int IT>
+static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *vals,
+                                    uint32_t *vtmp, uint64_t n, int bits, Arena &arena,
+                                    cudaStream_t s, uint64_t **result,
+                                    uint32_t **vresult, const uint32_t *d_n) {
+  constexpr int TILE = kThreads * IT;
+  const uint32_t nblocks = (uint32_t)((n + TILE - 1) / TILE);
+  const uint64_t hn = (uint64_t)nblocks * kRadix;
+  if (vals) {
+    cudaError_t e = scatter_smem_optin();
+    if (e != cudaSuccess) return e;
+  }
+  uint64_t *src = keys, *dst = tmp;
+  uint32_t *vsrc = vals, *vdst = vtmp;
+  // every scatter reads and writes keys (and values) and reads the counts
+  const uint64_t hist_bytes = 8 * n + 4 * hn;
+  const uint64_t scatter_bytes = (vals ? 24 : 16) * n + 8 * hn;
+  if (nblocks <= kFuseHistBlocks) {
+    // three tile-major count tables in rotation: pass p reads table p % 3,
+    // counts into (p + 1) % 3 and clears (p + 2) % 3
+    uint32_t *h[3];
+    for (auto &t : h)
+      if (!(t = arena.take<uint32_t>(hn))) return cudaErrorMemoryAllocation;
+    SST_LAUNCH_B(hist_bytes, k_hist<IT>, nblocks, kThreads, 0, s, src, n, 0, h[0],
+                 1u, (uint32_t)kRadix, h[1], d_n);
+    int p = 0;
+    for (int shift = 0; shift < bits; shift += 8, p++) {
+      const bool more = shift + 8 < bits;
+      uint32_t *nx = more ? h[(p + 1) % 3] : nullptr;
+      uint32_t *zr = more ? h[(p + 2) % 3] : nullptr;
+      if (vals)
+        SST_LAUNCH_B(scatter_bytes, (k_scatter<true, IT>), nblocks, kThreads,
+                     (scatter_smem_bytes<true, IT>()), s, src,
+                     dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
+                     shift + 8, zr, d_n);
+      else
+        SST_LAUNCH_B(scatter_bytes, (k_scatter<false, IT>), nblocks, kThreads,
+                     (scatter_smem_bytes<false, IT>()), s, src,
+                     dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
+                     shift + 8, zr, d_n);
+      std::swap(src, dst);
+      std::swap(vsrc, vdst);
+    }
+  } else {
+    // counts and their scan in separate tables (the single-pass scan runs
+    // out of place)
+    uint32_t *cnts = arena.take<uint32_t>(hn);
+    uint32_t *hist = arena.take<uint32_t>(hn);
+    if (!cnts || !hist) return cudaErrorMemoryAllocation;
+    for (int shift = 0; shift < bits; shift += 8) {
+      SST_LAUNCH_B(hist_bytes, k_hist<IT>, nblocks, kThreads, 0, s, src, n, shift,
+                   cnts, nblocks, 1u, (uint32_t *)nullptr, d_n);
+      size_t mark = arena.used;
+      cudaError_t e = scan<uint32_t, OpAdd>(cnts, hist, hn, 0u, OpAdd{}, true,
+                                            false, nullptr, arena, s);
+      arena.used = mark;
+      if (e != cudaSuccess) return e;
+      if (vals)
+        SST_LAUNCH_B(scatter_bytes, (k_scatter<true, IT>), nblocks, kThreads,
+                     (scatter_smem_bytes<true, IT>()), s, src,
+                     dst, n, shift, hist, nblocks, false, vsrc, vdst,
+                     (uint32_t *)nullptr, 0, (uint32_t *)nullptr, d_n);
+      else
+        SST_LAUNCH_B(scatter_bytes, (k_scatter<false, IT>), nblocks, kThreads,
+                     (scatter_smem_bytes<false, IT>()), s, src,
+                     dst, n, shift, hist, nblocks, false, vsrc, vdst,
+                     (uint32_t *)nullptr, 0, (uint32_t *)nullptr, d_n);
+      std::swap(src, dst);
+      std::swap(vsrc, vdst);
+    }
+  }
+  *result = src;
+  if (vresult) *vresult = vsrc;
+  return cudaGetLastError();
 }
 
 static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
@@ -474,74 +567,11 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
                n, bits, d_n);
     return cudaGetLastError();
   }
-  const uint32_t nblocks = (uint32_t)((n + kTile - 1) / kTile);
-  const uint64_t hn = (uint64_t)nblocks * kRadix;
-  if (vals) {
-    cudaError_t e = scatter_smem_optin();
-    if (e != cudaSuccess) return e;
-  }
-  uint64_t *src = keys, *dst = tmp;
-  uint32_t *vsrc = vals, *vdst = vtmp;
-  // every scatter reads and writes keys (and values) and reads the counts
-  const uint64_t hist_bytes = 8 * n + 4 * hn;
-  const uint64_t scatter_bytes = (vals ? 24 : 16) * n + 8 * hn;
-  if (nblocks <= kFuseHistBlocks) {
-    // three tile-major count tables in rotation: pass p reads table p % 3,
-    // counts into (p + 1) % 3 and clears (p + 2) % 3
-    uint32_t *h[3];
-    for (auto &t : h)
-      if (!(t = arena.take<uint32_t>(hn))) return cudaErrorMemoryAllocation;
-    SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, 0, h[0],
-                 1u, (uint32_t)kRadix, h[1], d_n);
-    int p = 0;
-    for (int shift = 0; shift < bits; shift += 8, p++) {
-      const bool more = shift + 8 < bits;
-      uint32_t *nx = more ? h[(p + 1) % 3] : nullptr;
-      uint32_t *zr = more ? h[(p + 2) % 3] : nullptr;
-      if (vals)
-        SST_LAUNCH_B(scatter_bytes, k_scatter<true>, nblocks, kThreads,
-                     scatter_smem_bytes<true>(), s, src,
-                     dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
-                     shift + 8, zr, d_n);
-      else
-        SST_LAUNCH_B(scatter_bytes, k_scatter<false>, nblocks, kThreads,
-                     scatter_smem_bytes<false>(), s, src,
-                     dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
-                     shift + 8, zr, d_n);
-      std::swap(src, dst);
-      std::swap(vsrc, vdst);
-    }
-  } else {
-    // counts and their scan in separate tables (the single-pass scan runs
-    // out of place)
-    uint32_t *cnts = arena.take<uint32_t>(hn);
-    uint32_t *hist = arena.take<uint32_t>(hn);
-    if (!cnts || !hist) return cudaErrorMemoryAllocation;
-    for (int shift = 0; shift < bits; shift += 8) {
-      SST_LAUNCH_B(hist_bytes, k_hist, nblocks, kThreads, 0, s, src, n, shift,
-                   cnts, nblocks, 1u, (uint32_t *)nullptr, d_n);
-      size_t mark = arena.used;
-      cudaError_t e = scan<uint32_t, OpAdd>(cnts, hist, hn, 0u, OpAdd{}, true,
-                                            false, nullptr, arena, s);
-      arena.used = mark;
-      if (e != cudaSuccess) return e;
-      if (vals)
-        SST_LAUNCH_B(scatter_bytes, k_scatter<true>, nblocks, kThreads,
-                     scatter_smem_bytes<true>(), s, src,
-                     dst, n, shift, hist, nblocks, false, vsrc, vdst,
-                     (uint32_t *)nullptr, 0, (uint32_t *)nullptr, d_n);
-      else
-        SST_LAUNCH_B(scatter_bytes, k_scatter<false>, nblocks, kThreads,
-                     scatter_smem_bytes<false>(), s, src,
-                     dst, n, shift, hist, nblocks, false, vsrc, vdst,
-                     (uint32_t *)nullptr, 0, (uint32_t *)nullptr, d_n);
-      std::swap(src, dst);
-      std::swap(vsrc, vdst);
-    }
-  }
-  *result = src;
-  if (vresult) *vresult = vsrc;
-  return cudaGetLastError();
+  if (!vals && n <= kSmallTileKeys)
+    return radix_sort_tiles<kSmallItems>(keys, tmp, vals, vtmp, n, bits, arena, s, result,
+                                         vresult, d_n);
+  return radix_sort_tiles<kItems>(keys, tmp, vals, vtmp, n, bits, arena, s, result, vresult,
+                                  d_n);
 }
 
 cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,

@@ -45,12 +45,13 @@ def test_empty_and_tiny(sg):
 
 
 @pytest.mark.parametrize("b", [2, 1024, 1025, 2048, 2049, 4096, 4097, 100000,
-                               262144, 262145, 400000])
+                               262144, 262145, 400000, 1048576, 1048577])
 def test_batch_sizes_across_sort_forms(sg, b):
     """Batch sizes on both sides of each form of the key sort: one CTA
-    (up to 2048 keys), one launch a pass (up to 64 tiles of 4096 keys) and
-    the scanned form; each batch holds a hub row (skewed high digits) and
-    repeated pairs, and half of it is removed again."""
+    (up to 2048 keys), one launch a pass over tiles of 1024 keys (up to 2^18
+    keys) or of 4096 keys (up to 256 tiles), and the scanned form; each
+    batch holds a hub row (skewed high digits) and repeated pairs, and half
+    of it is removed again."""
     n = 1 << 14
     rng = np.random.default_rng(b)
     e = rng.integers(0, n, (b, 2)).astype(np.uint32)
