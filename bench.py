@@ -757,10 +757,12 @@ def main():
 
 # DRAM bytes (read + write) per launch from one ncu capture of the kernel's
 # launches at the bench's batch sizes (dram__bytes_read.sum +
-# dram__bytes_write.sum; k_scan_lb: its 64 launches of 1e6-pair batches,
-# whose scan sizes do not depend on the graph's scale; the scans' writes stay
-# in L2 within the launch)
-NCU_TRAFFIC = {"k_scan_lb": 4.11e6}
+# dram__bytes_write.sum; k_scan_lb: its 40 launches over whole 1e6-element
+# arrays in 1e6-pair batches, whose scan sizes do not depend on the graph's
+# scale; the scans' writes stay in L2 within the launch.  Scans over a
+# device-side count are profiled apart.  k_scatter: its 48 passes over 1e6
+# keys, 245 tiles of 4096; the scattered keys stay in L2 within the launch.)
+NCU_TRAFFIC = {"k_scan_lb": 6.43e6, "k_scatter": 8.46e6}
 
 
 def update_roofline(prof, prof_all, hbm_peak, peak_kind):
