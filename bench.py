@@ -57,7 +57,7 @@ def args_parse():
     ap.add_argument("--serve-rate", type=float, default=300.0)
     ap.add_argument("--only", default="all",
                     choices=["all", "updates", "pagerank", "bfs", "batched", "serving",
-                             "multi", "compact"],
+                             "multi", "compact", "extras"],
                     help="one part of the run (profiling cases): the update steps "
                          "alone, or one traversal on the base graph")
     return ap.parse_args()
@@ -404,6 +404,75 @@ def main():
                "kernels": sg.profile_collect()}
         return bfs
 
+    def measure_extras():
+        """The rows beside the update path: parse and device build of a .mtx
+        file (sst_read_graph_file, sst_load_graph_file) and Bellman-Ford
+        (sst_bf) on a weighted RMAT graph."""
+        import tempfile
+        res = {}
+        # ingest: RMAT scale 18, 16 generated edges per vertex, one line each
+        sc, per = 18, 16
+        nn = 1 << sc
+        k = per * nn
+        x = torch.empty((k, 2), dtype=torch.int32, device="cuda")
+        with torch.cuda.stream(stream):
+            sg.gen_rmat(sc, k, seed=21, out=x, **RMAT)
+        torch.cuda.synchronize()
+        e = (x.cpu().numpy().astype(np.int64) + 1).astype(str)  # 1-based ids
+        body = "\n".join(np.char.add(np.char.add(e[:, 0], " "), e[:, 1]).tolist())
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, f"rmat{sc}.mtx")
+            with open(path, "w") as f:
+                f.write(f"%%MatrixMarket matrix coordinate pattern symmetric\n{nn} {nn} {k}\n")
+                f.write(body + "\n")
+            size = os.path.getsize(path)
+            t0 = time.perf_counter()
+            rows, pairs = sg.read_graph_file(path)
+            t_read = time.perf_counter() - t0
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            gl = sg.load_graph_file(path, device=dev)
+            gl.sync()
+            t_load = time.perf_counter() - t0
+            m_l = gl.M()
+            gl.close()
+        res["ingest"] = {"file": f"RMAT scale {sc}, {k} lines (.mtx, symmetric)",
+                         "file_bytes": size, "pairs": int(len(pairs)),
+                         "read_s": t_read, "read_mb_per_s": size / t_read / 1e6,
+                         "load_s": t_load, "stored_edges": m_l,
+                         "load_edges_per_s": m_l / t_load,
+                         "note": "read: parse to host pairs; load: parse, then the "
+                                 "device bulk build"}
+        # Bellman-Ford: RMAT scale 22, 16 edges per vertex, values 1..255
+        sc = 22
+        nn = 1 << sc
+        k = 16 * nn
+        gw = sg.SparseMatrixV(nn, device=dev, weighted=True)
+        gw.set_stream(stream.cuda_stream)
+        gen = torch.Generator(device="cuda").manual_seed(22)
+        with torch.cuda.stream(stream):
+            x = torch.empty((k, 2), dtype=torch.int32, device="cuda")
+            sg.gen_rmat(sc, k, seed=22, out=x, **RMAT)
+            v = torch.randint(1, 256, (k,), dtype=torch.int32, device="cuda", generator=gen)
+            gw.insert_batch_weighted(x, v)
+            out = torch.empty(nn, dtype=torch.int32, device="cuda")
+            sg.BF(gw, 0, out=out)
+        torch.cuda.synchronize()
+        bt = 1e30
+        for _ in range(3):
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            sg.BF(gw, 0, out=out)
+            s1.record(stream)
+            s1.synchronize()
+            bt = min(bt, s0.elapsed_time(s1) / 1e3)
+        reached = int((out < 2 ** 31 - 1).sum().item())
+        res["bellman_ford"] = {"graph": f"weighted RMAT scale {sc}, {k} generated edges, "
+                                        "values 1..255", "edges": gw.M(), "ms": bt * 1e3,
+                               "reached": reached, "edges_per_s": gw.M() / bt}
+        gw.close()
+        return res
+
     def measure_multi():
         """64-source BFS and 16-source BC (uniform sources) in one call each,
         against the same sources run one call per source."""
@@ -583,6 +652,8 @@ def main():
             res["batched"] = measure_batched()
         elif a.only == "multi":
             res["multi_source"] = measure_multi()
+        elif a.only == "extras":
+            res["extras"] = measure_extras()
         elif a.only == "compact":
             res["compact"] = measure_compact()
         else:
@@ -677,7 +748,7 @@ def main():
            "note": "insert+remove via sst_insert_batch/sst_remove_batch on pinned host "
                    "pairs; each call returns the invalid-pair count (8 B) to the host"}
 
-    batched = pagerank = bfs = serving = multi = compact = None
+    batched = pagerank = bfs = serving = multi = compact = extras = None
     if a.only == "all":
         batched = measure_batched()
         t0 = time.time()
@@ -710,6 +781,7 @@ def main():
         bfs = measure_bfs()
         multi = measure_multi()
         compact = measure_compact()
+        extras = measure_extras()
         serving = measure_serving()
 
 
@@ -749,6 +821,7 @@ def main():
         "bfs": bfs,
         "multi_source": multi,
         "compact_snapshot": compact,
+        "ingest_and_weighted": extras,
         "serving": serving,
         "update_kernels": upd_kernels,
     }
