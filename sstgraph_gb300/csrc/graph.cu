@@ -351,18 +351,28 @@ __device__ __forceinline__ uint32_t leaf_slot(uint32_t linev, uint64_t S,
   return (uint32_t)lane < c ? a : kEmpty;
 }
 
-// remove, first pass: delete inside each touched leaf and take the count
-// off the row's degree.  A warp takes 32 groups at a time: lane l first
-// loads group l's item range and its first item's leaf start, count word and
-// row (two dependent loads for all 32 groups at once), then the groups go
-// kGroupsPerWarp at a time with their items and leaf lines loaded together,
-// one dependent load per batch.
+// remove: delete inside each touched leaf, take the count off the row's
+// degree and classify the group: a leaf of a multi-leaf segment under the
+// lower bound goes to the climb list; a one-leaf segment that emptied or
+// fell to a quarter is resized.  (A one-leaf row has exactly one group, so
+// its degree afterwards is its leaf's new count.)  lo_leaf is a one-leaf
+// window's lower bound in a multi-leaf segment, window_lower(p, 0, H), the
+// same for every H >= 1 (computed once on the host: no per-group FP64).
+// A warp takes 32 groups at a time: lane l first loads group l's item
+// range, its first item's leaf
+// start, count word and key, and its row's capacity (three dependent loads
+// for all 32 groups at once), then the groups go kGroupsPerWarp at a time
+// with their items and leaf lines loaded together, one dependent load per
+// batch.
 __global__ void __launch_bounds__(256, 4)
-k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
+k_leaf_delete(DGraph g, uint32_t lo_leaf, const uint64_t *__restrict__ p_ul,
               const uint32_t *__restrict__ p_x,
               const uint64_t *__restrict__ p_S, const uint32_t *__restrict__ p_c,
               const uint32_t *__restrict__ g_start,
-              const uint32_t *__restrict__ d_ngroups) {
+              const uint32_t *__restrict__ d_ngroups,
+              uint8_t *__restrict__ gtype, uint8_t *__restrict__ glev,
+              uint32_t *__restrict__ gw0, uint32_t *__restrict__ gw1,
+              uint32_t *__restrict__ climb, uint32_t *__restrict__ nclimb) {
   const int lane = threadIdx.x & 31;
   constexpr int Q = kGroupsPerWarp;
   const uint32_t ng = *d_ngroups;
@@ -375,10 +385,12 @@ k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
     const uint32_t kl = okl ? g_start[gl + 1] - j0l : 0;
     const uint64_t Sl = okl ? p_S[j0l] : 0;
     const uint32_t cwl = okl ? p_c[j0l] : 0;
-    const uint32_t ul = okl ? (uint32_t)(p_ul[j0l] >> 32) : 0;
+    const uint64_t keyl = okl ? p_ul[j0l] : 0;
+    const uint32_t ul = (uint32_t)(keyl >> 32), leafl = (uint32_t)keyl;
+    const uint32_t capl = okl ? g.cap[ul] : 0;
     const uint32_t cnt = ng - w * 32 < 32 ? (uint32_t)(ng - w * 32) : 32u;
     for (uint32_t q0 = 0; q0 < cnt; q0 += Q) {
-      uint32_t j0[Q], k[Q], d[Q], linev[Q], cw[Q], u[Q];
+      uint32_t j0[Q], k[Q], d[Q], linev[Q], cw[Q], u[Q], cp[Q], lf[Q];
       uint64_t S[Q];
       bool ok[Q];
 #pragma unroll
@@ -390,6 +402,8 @@ k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
         S[q] = __shfl_sync(0xffffffffu, Sl, src);
         cw[q] = __shfl_sync(0xffffffffu, cwl, src);
         u[q] = __shfl_sync(0xffffffffu, ul, src);
+        cp[q] = __shfl_sync(0xffffffffu, capl, src);
+        lf[q] = __shfl_sync(0xffffffffu, leafl, src);
       }
 #pragma unroll
       for (int q = 0; q < Q; q++) {
@@ -412,51 +426,30 @@ k_leaf_delete(DGraph g, const uint64_t *__restrict__ p_ul,
         if (keep && g.vals) g.vals[S[q] + pos] = av;
         if ((uint32_t)lane >= c - k[q] && (uint32_t)lane < c) g.slots[S[q] + lane] = kEmpty;
         if (lane == 0) {
-          if (cw[q] & kMultiLeaf) g.lcnt[S[q] >> kLeafLog] = (uint8_t)(c - k[q]);
+          const uint32_t nc = c - k[q];
+          if (cw[q] & kMultiLeaf) g.lcnt[S[q] >> kLeafLog] = (uint8_t)nc;
           atomicSub(&g.deg[u[q]], k[q]);
+          const uint32_t gid = (uint32_t)(w * 32) + q0 + q;
+          uint8_t type = kNone;
+          uint32_t lev = 0, w0 = lf[q], w1 = lf[q] + 1;
+          if (cp[q] <= kLeaf) {
+            if (nc == 0 || (cp[q] > 1 && 4 * nc <= cp[q])) {
+              type = kResize;
+              lev = 31;
+              w0 = 0;
+              w1 = 1;
+            }
+          } else if (nc < lo_leaf) {
+            climb[atomicAdd(nclimb, 1u)] = gid;
+          }
+          gtype[gid] = type;
+          glev[gid] = (uint8_t)lev;
+          gw0[gid] = w0;
+          gw1[gid] = w1;
         }
         __syncwarp();
       }
     }
-  }
-}
-
-// remove, second pass (thread per group): a leaf under the lower bound goes
-// to the climb list; a one-leaf segment that emptied or fell to a quarter
-// is resized
-__global__ void k_classify_remove(DGraph g, PmaParams p,
-                                  const uint64_t *__restrict__ p_ul,
-                                  const uint32_t *__restrict__ g_start,
-                                  const uint32_t *__restrict__ d_ngroups,
-                                  uint8_t *__restrict__ gtype,
-                                  uint8_t *__restrict__ glev,
-                                  uint32_t *__restrict__ gw0,
-                                  uint32_t *__restrict__ gw1,
-                                  uint32_t *__restrict__ climb,
-                                  uint32_t *__restrict__ nclimb) {
-  const uint32_t ng = *d_ngroups;
-  GRID_STRIDE(gid, ng) {
-    uint64_t key = p_ul[g_start[gid]];
-    uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
-    uint32_t cap = g.cap[u], deg = g.deg[u];  // deg is already reduced
-    uint8_t type = kNone;
-    uint32_t lev = 0, w0 = leaf, w1 = leaf + 1;
-    if (cap <= kLeaf) {
-      if (deg == 0 || (cap > 1 && 4 * deg <= cap)) {
-        type = kResize;
-        lev = 31;
-        w0 = 0;
-        w1 = 1;
-      }
-    } else {
-      uint32_t H = log2_floor(cap >> kLeafLog);
-      if (g.lcnt[(g.base[u] >> kLeafLog) + leaf] < window_lower(p, 0, H))
-        climb[atomicAdd(nclimb, 1u)] = (uint32_t)gid;
-    }
-    gtype[gid] = type;
-    glev[gid] = (uint8_t)lev;
-    gw0[gid] = w0;
-    gw1[gid] = w1;
   }
 }
 
@@ -1525,9 +1518,9 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
       SST_LAUNCH(k_classify_insert, tgrid, kTB, 0, s, dg, p_ul, g_start,
                  &P->n_groups, gtype, glev, gw0, gw1, climb, &P->n_climb);
     } else {
-      SST_LAUNCH(k_leaf_delete, wgrid, kTB, 0, s, dg, p_ul, p_x, p_S, p_c, g_start,
-                 &P->n_groups);
-      SST_LAUNCH(k_classify_remove, tgrid, kTB, 0, s, dg, g->params, p_ul,
+      // multi-leaf segments have H >= 1 (at least two leaves)
+      SST_LAUNCH(k_leaf_delete, wgrid, kTB, 0, s, dg,
+                 (uint32_t)window_lower(g->params, 0, 1), p_ul, p_x, p_S, p_c,
                  g_start, &P->n_groups, gtype, glev, gw0, gw1, climb, &P->n_climb);
     }
     SST_LAUNCH(k_climb, wgrid, kTB, 0, s, dg, g->params, insert, p_ul, g_start,
