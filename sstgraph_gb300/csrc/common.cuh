@@ -18,6 +18,7 @@
 // 2^floor(log2 log2 N) slots).  Segment bases are aligned to min(cap, 32)
 // slots.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -68,17 +69,31 @@ __host__ __device__ inline uint32_t log2_floor(uint64_t x) {
 }
 
 __host__ __device__ inline uint64_t next_pow2(uint64_t x) {
-  uint64_t p = 1;
-  while (p < x) p <<= 1;
-  return p;
+  if (x <= 1) return 1;
+#ifdef __CUDA_ARCH__
+  return 1ull << (64 - __clzll((long long)(x - 1)));
+#else
+  return 1ull << (64 - __builtin_clzll(x - 1));
+#endif
 }
 
-// Capacity for a segment that must hold `total` elements after a resize.
-__host__ __device__ inline uint64_t cap_for(uint64_t total, float fill) {
+// 2^24 / fill rounded up (fill clamped to [1/128, 1]): the resize target
+// density as a fixed-point reciprocal, computed once on the host, so that
+// sizing a segment takes one integer product instead of an FP64 division
+// per resize.
+inline uint64_t fill_inv_q24(float fill) {
+  const double f = fill < 1.0f / 128 ? 1.0 / 128 : (fill > 1.0f ? 1.0 : (double)fill);
+  return (uint64_t)ceil(16777216.0 / f);
+}
+
+// Capacity for a segment that must hold `total` (< 2^32) elements after a
+// resize: at least total / fill + 1 slots, a power of two, and at least two
+// leaves once above one leaf.
+__host__ __device__ inline uint64_t cap_for(uint64_t total, uint64_t inv_q24) {
   if (total == 0) return 0;
   if (total <= kLeaf) return next_pow2(total);
-  uint64_t want = (uint64_t)((double)total / (double)fill) + 1;
-  uint64_t c = next_pow2(want);
+  const uint64_t want = ((total * inv_q24) >> 24) + 1;
+  const uint64_t c = next_pow2(want);
   return c < 2 * kLeaf ? 2 * kLeaf : c;
 }
 

@@ -624,7 +624,7 @@ struct Tasks {
 
 // warp per task slot (all gmax slots, so the prefix scans see zeros beyond
 // the task count)
-__global__ void k_task_setup(DGraph g, PmaParams p, bool insert,
+__global__ void k_task_setup(DGraph g, uint64_t inv_fill, bool insert,
                              const uint64_t *__restrict__ p_ul,
                              const uint32_t *__restrict__ g_start,
                              const uint8_t *__restrict__ gtype,
@@ -667,7 +667,7 @@ __global__ void k_task_setup(DGraph g, PmaParams p, bool insert,
       nb = warp_lb_u64(p_ul, 0, j0 + 1, kk);
       ne = warp_lb_u64(p_ul, j0, nitems, kk + (1ull << 32));
     }
-    capn = cap_for(old + (ne - nb), p.grow_fill);
+    capn = cap_for(old + (ne - nb), inv_fill);
     ndst = capn == 0 ? 0 : nleaves_of((uint32_t)capn);
     if (lane == 0 && capn > 0) rank = atomicAdd(&class_cnt[log2_floor(capn)], 1u);
   }
@@ -1550,8 +1550,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
       if (st != SST_OK) return st;
     }
     // 8: plan
-    SST_LAUNCH(k_task_setup, wgrid, kTB, 0, s, dg, g->params, insert, p_ul,
-               g_start, gtype, gw0, gw1, task_group, &P->n_tasks, &P->n_items, b, T,
+    SST_LAUNCH(k_task_setup, wgrid, kTB, 0, s, dg, fill_inv_q24(g->params.grow_fill), insert,
+               p_ul, g_start, gtype, gw0, gw1, task_group, &P->n_tasks, &P->n_items, b, T,
                P->class_cnt);
     SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.total, T.out, b, 0ull, OpAdd{}, true,
                                         false, &P->task_elems, A, s, &P->n_tasks)));
