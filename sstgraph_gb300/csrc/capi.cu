@@ -49,13 +49,24 @@ sst_status io_begin(sst_graph *g, size_t bytes) {
   return SST_OK;
 }
 
-// device copy of a host input array (or the device pointer itself)
+// device copy of a host input array (or the device pointer itself).  With
+// `mapped`, for an input the kernels read once: pinned host memory is read
+// by the kernel in place (over the host link, no separate copy).
 template <typename T>
 sst_status stage_in(sst_graph *g, const T *p, uint64_t count, uint32_t flags,
-                    const T **out) {
+                    const T **out, bool mapped = false) {
   if (is_dev(flags) || count == 0) {
     *out = p;
     return SST_OK;
+  }
+  if (mapped) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+        a.devicePointer) {
+      *out = static_cast<const T *>(a.devicePointer);
+      return SST_OK;
+    }
+    cudaGetLastError();  // pageable memory: copy it below
   }
   T *d = g->io.take<T>(count);
   if (!d) {
@@ -232,10 +243,12 @@ static sst_status do_update(sst_graph *g, const uint32_t *pairs, uint64_t n,
   }
   sst_status st = is_dev(flags) ? SST_OK : io_begin(g, n * 12 + 512);
   if (st != SST_OK) return st;
+  // the key build reads each pair (and value) once: pinned host inputs are
+  // read in place; the plan readback inside the update comes after it
   const uint32_t *d = nullptr, *dv = nullptr;
-  st = stage_in(g, pairs, 2 * n, flags, &d);
+  st = stage_in(g, pairs, 2 * n, flags, &d, true);
   if (st != SST_OK) return st;
-  if (values) st = stage_in(g, values, n, flags, &dv);
+  if (values) st = stage_in(g, values, n, flags, &dv, true);
   if (st != SST_OK) return st;
   st = sst::update_batch(g, d, n, insert, n_invalid, dv);
   if (st == SST_OK && !is_dev(flags)) st = sst::sync_checked(g);

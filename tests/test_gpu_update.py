@@ -165,3 +165,40 @@ def test_generators_match_oracle(sg):
     assert np.array_equal(sg.gen_rmat(14, 50000, seed=3, first=77), oracle.rmat(14, 50000, seed=3, first=77))
     assert np.array_equal(sg.gen_er(1000003, 50000, seed=4), oracle.er(1000003, 50000, seed=4))
     assert np.array_equal(sg.gen_ref_rmat(1 << 15, 50000), oracle.ref_rmat_stream(1 << 15, 50000))
+
+
+def test_pinned_host_inputs(sg):
+    """Pinned host pairs (read by the key build in place) and pageable ones
+    (copied first) give the same graph as the oracle."""
+    torch = pytest.importorskip("torch")
+    n = 1 << 12
+    rng = np.random.default_rng(21)
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    for i, b in enumerate([1, 1000, 70000, 300000, 5000]):
+        e = rng.integers(0, n, (b, 2)).astype(np.uint32)
+        pinned = torch.from_numpy(e.view(np.int32)).pin_memory()
+        if i % 2:
+            g.remove_batch(pinned)
+            o.remove_batch(e)
+            g.insert_batch(e[: b // 2])
+            o.insert_batch(e[: b // 2])
+        else:
+            g.insert_batch(pinned)
+            o.insert_batch(e)
+        same(g, o, structure=False)
+    w = sg.SparseMatrixV(n, weighted=True)
+    e = rng.integers(0, n, (4000, 2)).astype(np.uint32)
+    v = rng.integers(0, 1000, 4000).astype(np.uint32)
+    w.insert_batch_weighted(torch.from_numpy(e.view(np.int32)).pin_memory(),
+                            torch.from_numpy(v.view(np.int32)).pin_memory())
+    vals, found = w.values(e)
+    last = {}
+    for (r, c), x in zip(e.tolist(), v.tolist()):
+        if r != c:
+            last[(r, c)] = x
+    exp = np.array([last.get((r, c), 0) for r, c in e.tolist()], np.uint32)
+    ok = np.array([(r, c) in last for r, c in e.tolist()])
+    assert np.array_equal(found, ok) and np.array_equal(vals[ok], exp[ok])
+    g.close()
+    w.close()
