@@ -409,7 +409,6 @@ def main():
         """The rows beside the update path: parse and device build of a .mtx
         file (sst_read_graph_file, sst_load_graph_file) and Bellman-Ford
         (sst_bf) on a weighted RMAT graph."""
-        import tempfile
         res = {}
         # ingest: RMAT scale 18, 16 generated edges per vertex, one line each
         sc, per = 18, 16
