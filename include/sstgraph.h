@@ -88,7 +88,7 @@ SST_API sst_status sst_graph_clone(const sst_graph *g, sst_graph **out);
 SST_API sst_status sst_set_stream(sst_graph *g, void *stream);
 SST_API sst_status sst_sync(sst_graph *g);
 /* Launch mode of update batches (no reference counterpart).  1 (default):
- * the planning launches of a raw-pair, unweighted batch of up to 2^18 pairs
+ * the planning launches of a raw-pair, unweighted batch of up to 2^20 pairs
  * (key sort to plan readback) are captured once per batch size and graph
  * layout and replayed as one CUDA graph launch; 0: every kernel is launched
  * directly.  Results are the same either way. */

@@ -1241,8 +1241,8 @@ struct MergeJoin {
 // An update's planning launches (sort to plan readback) replayed as one CUDA
 // graph.  They depend on the batch size, the operation and where the graph
 // and the scratch live; an entry is used only when all of these match.
-constexpr uint64_t kPlanGraphMaxBatch = 1u << 18;
-constexpr size_t kPlanGraphs = 48;
+constexpr uint64_t kPlanGraphMaxBatch = 1u << 20;
+constexpr size_t kPlanGraphs = 56;
 
 // Launch size of a replayed batch of b pairs: b rounded up to m * 2^k with
 // m in 4..7 (at least 64), so batches of nearby sizes share one captured

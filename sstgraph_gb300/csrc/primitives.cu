@@ -472,6 +472,15 @@ size_t radix_sort_scratch_bytes(uint64_t n) {
   return 3 * ((hn * 4 + 255) & ~size_t(255)) + scan_scratch_bytes(hn, 4) + 512;
 }
 
+// profiler name of a scatter pass, by its tile size
+template <bool KV, int IT>
+constexpr const char *scatter_name() {
+  if constexpr (IT == kSmallItems)
+    return KV ? "(k_scatter<true, 4>)" : "(k_scatter<false, 4>)";
+  else
+    return KV ? "(k_scatter<true, 16>)" : "(k_scatter<false, 16>)";
+}
+
 // The multi-tile sort with tiles of IT items per thread (see radix_sort_impl).
 template <int IT>
 static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *vals,
@@ -504,12 +513,12 @@ static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *val
       uint32_t *nx = more ? h[(p + 1) % 3] : nullptr;
       uint32_t *zr = more ? h[(p + 2) % 3] : nullptr;
       if (vals)
-        SST_LAUNCH_B(scatter_bytes, (k_scatter<true, IT>), nblocks, kThreads,
+        SST_LAUNCH_NB((scatter_name<true, IT>()), scatter_bytes, (k_scatter<true, IT>), nblocks, kThreads,
                      (scatter_smem_bytes<true, IT>()), s, src,
                      dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
                      shift + 8, zr, d_n);
       else
-        SST_LAUNCH_B(scatter_bytes, (k_scatter<false, IT>), nblocks, kThreads,
+        SST_LAUNCH_NB((scatter_name<false, IT>()), scatter_bytes, (k_scatter<false, IT>), nblocks, kThreads,
                      (scatter_smem_bytes<false, IT>()), s, src,
                      dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
                      shift + 8, zr, d_n);
@@ -531,12 +540,12 @@ static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *val
       arena.used = mark;
       if (e != cudaSuccess) return e;
       if (vals)
-        SST_LAUNCH_B(scatter_bytes, (k_scatter<true, IT>), nblocks, kThreads,
+        SST_LAUNCH_NB((scatter_name<true, IT>()), scatter_bytes, (k_scatter<true, IT>), nblocks, kThreads,
                      (scatter_smem_bytes<true, IT>()), s, src,
                      dst, n, shift, hist, nblocks, false, vsrc, vdst,
                      (uint32_t *)nullptr, 0, (uint32_t *)nullptr, d_n);
       else
-        SST_LAUNCH_B(scatter_bytes, (k_scatter<false, IT>), nblocks, kThreads,
+        SST_LAUNCH_NB((scatter_name<false, IT>()), scatter_bytes, (k_scatter<false, IT>), nblocks, kThreads,
                      (scatter_smem_bytes<false, IT>()), s, src,
                      dst, n, shift, hist, nblocks, false, vsrc, vdst,
                      (uint32_t *)nullptr, 0, (uint32_t *)nullptr, d_n);

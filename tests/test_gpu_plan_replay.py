@@ -1,8 +1,8 @@
-"""Update batches up to 2^18 pairs replay their planning launches (sort to
+"""Update batches up to 2^20 pairs replay their planning launches (sort to
 plan readback) from a captured CUDA graph, sized by the batch's size class
-(b rounded up to m * 2^k, m in 4..7) and working on the device-side count.  The replayed form must give the
-same graph as the directly launched form (sst_set_plan_graphs off) and as
-the oracle: on cache hits with new contents, on new device buffers, after
+(b rounded up to m * 2^k, m in 4..7) and working on the device-side count.
+The replayed form must give the same graph as the directly launched form
+(sst_set_plan_graphs off) and as the oracle: on cache hits with new contents, on new device buffers, after
 repacks that move the slab, past the cache's capacity and under the kernel
 profiler."""
 import numpy as np
@@ -64,8 +64,8 @@ def test_sizes_sharing_a_class(sg):
 
 def test_across_sort_forms(sg):
     # one CTA sort, single-launch passes and the largest replayed size
-    run(sg, 1 << 16, [2048, 2049, 30000, 30000, (1 << 18) - 1, 1 << 18, (1 << 18) + 1],
-        seed=2)
+    run(sg, 1 << 16, [2048, 2049, 30000, 30000, (1 << 18) - 1, 1 << 18, (1 << 18) + 1,
+                      (1 << 20) - 1, 1 << 20, (1 << 20) + 1], seed=2)
 
 
 def test_repacks_move_the_slab(sg):
@@ -74,10 +74,10 @@ def test_repacks_move_the_slab(sg):
 
 
 def test_more_sizes_than_cached(sg):
-    # every size class (64 .. 2^18: 49 of them, one more than the cache
+    # every size class (64 .. 2^20: 57 of them, one more than the cache
     # holds), one size below each class's bound, then the first ones again
-    classes = [64] + [m << k for k in range(4, 16) for m in (5, 6, 7, 8)]
-    assert len(classes) == 49 and classes[-1] == 1 << 18
+    classes = [64] + [m << k for k in range(4, 18) for m in (5, 6, 7, 8)]
+    assert len(classes) == 57 and classes[-1] == 1 << 20
     sizes = [c - 1 - (c >> 4) for c in classes]
     run(sg, 4000, sizes + sizes[:8], seed=4)
 
