@@ -52,13 +52,16 @@ def args_parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scale", type=int, default=24)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the oracle replay of the bench graph's batches")
     ap.add_argument("--pr-iters", type=int, default=10)
-    ap.add_argument("--batched-batches", type=int, default=128)
+    ap.add_argument("--batched-batches", type=int, default=512)
     ap.add_argument("--serve-requests", type=int, default=400)
     ap.add_argument("--serve-rate", type=float, default=300.0)
+    ap.add_argument("--serve-scale", type=int, default=25)
     ap.add_argument("--only", default="all",
                     choices=["all", "updates", "pagerank", "bfs", "batched", "serving",
-                             "multi", "compact", "extras"],
+                             "multi", "compact", "extras", "static"],
                     help="one part of the run (profiling cases): the update steps "
                          "alone, or one traversal on the base graph")
     return ap.parse_args()
@@ -208,6 +211,37 @@ def run_cpu(scale, plan, label):
     return ins_e / ins_t, {"build_s": round(build_s, 2), "insert_s": ins_t,
                            "remove_s": rem_t, "edges": ins_e,
                            "sample": label}
+
+
+def check_parity(g, scale, applied):
+    """Replay the bench graph's history on the oracle port (host threads):
+    the scale-`scale` base graph, then every update batch in the order it
+    was applied; compare the device graph's whole CSR with the oracle's."""
+    import hashlib
+
+    import numpy as np
+
+    import oracle
+    oracle.build()
+    n = 1 << scale
+    t0 = time.time()
+    base = oracle.symmetrize(oracle.rmat(scale, 8 * n, seed=5, **RMAT))
+    o = oracle.OracleGraph(n)
+    o.insert_batch(base)
+    del base
+    for op, x in applied:
+        getattr(o, op + "_batch")(x)
+    off_o, col_o = o.csr()
+    off_g, col_g = g.csr()
+    equal = bool(o.M() == g.M() and np.array_equal(off_o, off_g) and
+                 np.array_equal(col_o, col_g))
+    digest = hashlib.sha256(off_g.tobytes())
+    digest.update(col_g.tobytes())
+    return {"equal": equal, "edges": int(g.M()), "batches_replayed": len(applied),
+            "csr_sha256": digest.hexdigest(), "oracle_s": round(time.time() - t0, 2),
+            "check": "whole CSR (offsets and columns) of the device graph after the "
+                     "timed, end-to-end and kernel-pass batches = the oracle port's "
+                     "after replaying the same base graph and batches"}
 
 
 def reference_arm(a):
@@ -473,6 +507,129 @@ def main():
         gw.close()
         return res
 
+    def measure_static():
+        """Static analytics at scale (RMAT scale 22, 8 * 2^22 generated edges,
+        seed 3; Erdos-Renyi, 2^22 vertices, average degree 16, seed 4; both
+        symmetrised): BFS from 0, PageRank 20 iterations, CC, BC from 0 and
+        TC on the device (best of 3 after a warm-up, CUDA events), each with
+        its HBM roofline from its algorithmic bytes, beside the oracle port
+        on all host threads (one warm-up, then one timed run) on the same
+        graph, whose results are checked against the device's (depths, CC
+        labels and triangle counts equal; PageRank and BC within 1e-9)."""
+        import oracle
+        oracle.build()
+        out = {}
+        nn = 1 << 22
+        specs = [("rmat22", lambda x, first, k: sg.gen_rmat(22, k, seed=3, first=first,
+                                                             out=x, **RMAT),
+                  lambda: oracle.rmat(22, 8 * nn, seed=3, **RMAT)),
+                 ("er22", lambda x, first, k: sg.gen_er(nn, k, seed=4, first=first, out=x),
+                  lambda: oracle.er(nn, 8 * nn, seed=4))]
+        for name, dev_gen, cpu_gen in specs:
+            gg = sg.SparseMatrixV(nn, device=dev)
+            gg.set_stream(stream.cuda_stream)
+            total, ch = 8 * nn, 1 << 24
+            with torch.cuda.stream(stream):
+                x = torch.empty((ch, 2), dtype=torch.int32, device="cuda")
+                for first in range(0, total, ch):
+                    k = min(ch, total - first)
+                    dev_gen(x[:k], first, k)
+                    gg.insert_batch(x[:k])
+                    gg.insert_batch(x[:k].flip(1).contiguous())
+                del x
+            torch.cuda.synchronize()
+            m = gg.M()
+            tuning = sg.autotune(gg)
+            off, cols = gg.csr()
+            deg = np.diff(off.astype(np.int64))
+            rows = np.repeat(np.arange(nn, dtype=np.int64), deg)
+            low = cols.astype(np.int64) < rows
+            dl = np.bincount(rows[low], minlength=nn).astype(np.int64)
+            tc_bytes = 4 * int((dl[rows[low]] + dl[cols[low].astype(np.int64)]).sum()) + 4 * m
+            del off, cols, rows, low
+            dep = torch.empty(nn, dtype=torch.int32, device="cuda")
+            pr = torch.empty(nn, dtype=torch.float64, device="cuda")
+            lab = torch.empty(nn, dtype=torch.int32, device="cuda")
+            bc = torch.empty(nn, dtype=torch.float64, device="cuda")
+            tcv = {}
+            runs = {"bfs": lambda: sg.BFS(gg, 0, depths=True, out=dep),
+                    "pagerank20": lambda: sg.PR_S(gg, 20, out=pr),
+                    "cc": lambda: sg.CC(gg, out=lab),
+                    "bc": lambda: sg.BC(gg, 0, out=bc),
+                    "tc": lambda: tcv.__setitem__("t", sg.TC(gg))}
+            gpu = {}
+            for alg, fn in runs.items():
+                fn()
+                torch.cuda.synchronize()
+                best = 1e30
+                for _ in range(3):
+                    with torch.cuda.stream(stream):
+                        pr_flush.fill_(1)
+                    s0, s1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+                    s0.record(stream)
+                    fn()
+                    s1.record(stream)
+                    s1.synchronize()
+                    best = min(best, s0.elapsed_time(s1) / 1e3)
+                gpu[alg] = best
+            sg.profile_start("k_cc_hook")
+            sg.CC(gg, out=lab)
+            torch.cuda.synchronize()
+            cc_rounds = sum(v["launches"] for v in sg.profile_collect().values())
+            d_dep = dep.cpu().numpy()
+            m_r = int(deg[d_dep >= 0].sum())
+            byts = {"bfs": 4 * m_r + 12 * nn, "pagerank20": 20 * (4 * m + 24 * nn),
+                    "cc": cc_rounds * (4 * m + 8 * nn), "bc": 8 * m_r + 28 * nn,
+                    "tc": tc_bytes}
+            res = {"vertices": nn, "edges": m, "tuning": tuning, "bfs_edges_reached": m_r,
+                   "cc_rounds": cc_rounds, "triangles": tcv["t"], "algorithms": {}}
+            # the oracle port on the same graph, all host threads
+            pairs = oracle.symmetrize(cpu_gen())
+            t0 = time.perf_counter()
+            o = oracle.OracleGraph(nn)
+            o.insert_batch(pairs)
+            res["cpu_build_s"] = time.perf_counter() - t0
+            del pairs
+            cpu_fn = {"bfs": lambda: o.bfs(0), "pagerank20": lambda: o.pagerank(20),
+                      "cc": o.cc, "bc": lambda: o.bc(0), "tc": o.tc}
+            cpu, cres = {}, {}
+            for alg, fn in cpu_fn.items():
+                if alg != "tc":
+                    fn()
+                t0 = time.perf_counter()
+                cres[alg] = fn()
+                cpu[alg] = time.perf_counter() - t0
+            dev_res = {"bfs": d_dep, "pagerank20": pr.cpu().numpy(), "cc": lab.cpu().numpy(),
+                       "bc": bc.cpu().numpy(), "tc": tcv["t"]}
+
+            def agree(alg):
+                a, b = dev_res[alg], cres[alg]
+                if alg in ("pagerank20", "bc"):
+                    return bool(np.max(np.abs(a - b)) <= 1e-9 * max(np.max(np.abs(b)), 1e-300))
+                if alg == "cc":
+                    return bool(np.array_equal(a.view(np.uint32), b))
+                return bool(np.array_equal(a, b))
+            for alg in runs:
+                gbs = byts[alg] / gpu[alg] / 1e9
+                r = {"gpu_ms": 1e3 * gpu[alg], "cpu_ms": 1e3 * cpu[alg],
+                     "speedup": cpu[alg] / gpu[alg], "algorithmic_bytes": byts[alg],
+                     "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak,
+                                  "unit": "GB/s", "frac": gbs / hbm_peak},
+                     "matches_oracle": agree(alg)}
+                if alg == "bfs":
+                    r["gteps"] = m_r / gpu[alg] / 1e9
+                if alg == "pagerank20":
+                    r["gteps"] = 20 * m / gpu[alg] / 1e9
+                res["algorithms"][alg] = r
+            res["cpu_cores"] = cpu_threads()
+            out[name] = res
+            del o
+            gg.close()
+        out["bytes"] = {"bfs": "4 m_r + 12 n", "pagerank20": "20 (4 m + 24 n)",
+                        "cc": "rounds (4 m + 8 n)", "bc": "8 m_r + 28 n",
+                        "tc": "sum over (u, v), v < u of 4 (d<(u) + d<(v)) + 4 m"}
+        return out
+
     def measure_multi():
         """64-source BFS and 16-source BC (uniform sources) in one call each,
         against the same sources run one call per source."""
@@ -515,23 +672,32 @@ def main():
         return res
 
     def measure_batched(reps=3):
-        """The same stream of uneven insert batches (log-normal sizes, median
-        1e4, sigma 1.5, clipped to [1e3, 1e6]) applied to two device copies of
-        the graph: one insert_batch call per batch (plain form) vs one
-        update_batches call for the whole stream (batched form).  Each copy
-        first takes a disjoint warm-up stream of the same sizes in the same
-        form (untimed: scratch grown, kernels loaded), so the timed stream
-        measures the steady state; median of `reps` copies per form."""
+        """The batched-form configuration: 512 update batches with log-normal
+        sizes (floor(exp(N(ln 1e4, 1.5))), capped at 1e7, no lower clip);
+        every fourth batch removes edges sampled from the graph, the others
+        insert RMAT edges.  The same stream is applied to device copies of
+        the graph in two forms: one insert_batch / remove_batch call per
+        batch (plain) and one update_batches call for the whole stream
+        (batched).  Each copy first takes a disjoint warm-up stream of the
+        same sizes in the same form (untimed: scratch grown, kernels loaded),
+        so the timed stream measures the steady state; median of `reps`
+        copies per form.  The two forms' final graphs are compared whole
+        (CSR)."""
         rng = np.random.default_rng(11)
-        sizes = np.clip(rng.lognormal(np.log(1e4), 1.5, a.batched_batches),
-                        1e3, 1e6).astype(np.int64)
+        sizes = np.minimum(np.floor(np.exp(rng.normal(np.log(1e4), 1.5, a.batched_batches))),
+                           1e7).astype(np.int64)
+        sizes = np.maximum(sizes, 1)
+        ops = [0 if i % 4 == 3 else 1 for i in range(len(sizes))]
 
         def stream_of(first):
             out = []
             with torch.cuda.stream(stream):
-                for sz in sizes.tolist():
+                for sz, op in zip(sizes.tolist(), ops):
                     x = torch.empty((sz, 2), dtype=torch.int32, device="cuda")
-                    sg.gen_rmat(a.scale, sz, seed=12, first=first, out=x, **RMAT)
+                    if op:
+                        sg.gen_rmat(a.scale, sz, seed=12, first=first, out=x, **RMAT)
+                    else:
+                        g.sample_edges(sz, seed=14, first=first, out=x)
                     first += sz
                     out.append(x)
             return out
@@ -540,106 +706,168 @@ def main():
         warm, bl = stream_of(0), stream_of(total_e)
         torch.cuda.synchronize()
         res = {}
+        csr = {}
         for form in ("plain", "batched"):
             times, checks = [], []
-            for _ in range(reps):
+            for rep in range(reps):
                 gc = g.copy()
                 gc.set_stream(stream.cuda_stream)
                 if form == "plain":
-                    for x in warm:
-                        gc.insert_batch(x)
+                    for x, op in zip(warm, ops):
+                        (gc.insert_batch if op else gc.remove_batch)(x)
                 else:
-                    gc.update_batches(warm)
+                    gc.update_batches(warm, ops)
                 torch.cuda.synchronize()
                 s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 s0.record(stream)
                 if form == "plain":
-                    for x in bl:
-                        gc.insert_batch(x)
+                    for x, op in zip(bl, ops):
+                        (gc.insert_batch if op else gc.remove_batch)(x)
                 else:
-                    gc.update_batches(bl)
+                    gc.update_batches(bl, ops)
                 s1.record(stream)
                 s1.synchronize()
                 times.append(s0.elapsed_time(s1) / 1e3)
                 checks.append([gc.M(), gc.touch_all_sum()])
+                if rep == 0:
+                    csr[form] = gc.csr()
                 gc.close()
             t = float(np.median(times))
             res[form] = {"edges_per_s": total_e / t, "s": t, "check": checks[0],
                          "same_each_rep": all(c == checks[0] for c in checks)}
         same = (res["plain"]["check"] == res["batched"]["check"] and
-                res["plain"]["same_each_rep"] and res["batched"]["same_each_rep"])
+                res["plain"]["same_each_rep"] and res["batched"]["same_each_rep"] and
+                all(np.array_equal(x, y) for x, y in zip(csr["plain"], csr["batched"])))
+        del csr
         return {"batches": len(bl), "edges": total_e, "reps": reps,
+                "removes": int(len(ops) - sum(ops)),
                 "sizes": {"min": int(sizes.min()), "median": int(np.median(sizes)),
-                          "max": int(sizes.max())},
+                          "mean": float(sizes.mean()), "max": int(sizes.max())},
                 "plain_edges_per_s": res["plain"]["edges_per_s"],
                 "batched_edges_per_s": res["batched"]["edges_per_s"],
+                "plain_s": res["plain"]["s"], "batched_s": res["batched"]["s"],
                 "speedup": res["batched"]["edges_per_s"] / res["plain"]["edges_per_s"],
                 "same_graph": same,
-                "check": "M and touch_all_sum of both copies"}
+                "check": "whole CSR, M and touch_all_sum of both forms' final graphs"}
 
     def measure_serving():
-        """Mixed request stream through the serving loop (sst_server_*):
-        Poisson arrivals, 70% update batches (log-normal sizes, median 1e3),
-        30% queries split evenly between single-source BFS, a 5-iteration
-        PageRank refresh and per-vertex triangle counts of 1e4 random
-        vertices, under a 60 GB HBM budget.  Latency = completion - arrival."""
+        """The serving configuration: an RMAT scale-`serve_scale` graph (8 * n
+        generated edges, seed 7, symmetrised) held on the device, its bulk-
+        load scratch released, served under a 60 GB HBM budget.  Requests:
+        70% update batches (log-normal sizes, median 1e3, sigma 1, at most
+        1e5; 30% of them remove edges sampled from the graph, the rest insert
+        RMAT edges), 30% queries split evenly between single-source BFS, a
+        5-iteration PageRank refresh and per-vertex triangle counts of 1e4
+        random vertices.  Two runs: Poisson arrivals at `serve_rate`/s for
+        latency (completion - arrival), then every request of a second stream
+        offered at once (load above capacity) for the sustained rates."""
+        sc = a.serve_scale
+        nn = 1 << sc
+        gs = sg.SparseMatrixV(nn, device=dev, initial_slots=int(3.2 * 16 * nn))
+        gs.set_stream(stream.cuda_stream)
+        total, ch = 8 * nn, 1 << 25
+        t0 = time.time()
+        with torch.cuda.stream(stream):
+            x = torch.empty((ch, 2), dtype=torch.int32, device="cuda")
+            for first in range(0, total, ch):
+                k = min(ch, total - first)
+                sg.gen_rmat(sc, k, seed=7, first=first, out=x[:k], **RMAT)
+                gs.insert_batch(x[:k])
+                gs.insert_batch(x[:k].flip(1).contiguous())
+            del x
+        torch.cuda.synchronize()
+        build_s = time.time() - t0
+        mem_loaded = gs.get_memory_size()
+        gs.release_scratch()
+        mem_trimmed = gs.get_memory_size()
         rng = np.random.default_rng(31)
-        reqs = []
-        first = 0
-        for i in range(a.serve_requests):
-            r = rng.random()
-            if r < 0.7:
-                sz = int(min(1e5, max(1, rng.lognormal(np.log(1e3), 1.0))))
-                pairs = sg.gen_rmat(a.scale, sz, seed=13, first=first, **RMAT)
-                first += sz
-                kind = "remove" if rng.random() < 0.3 else "insert"
-                reqs.append((kind, pairs))
-            elif r < 0.8:
-                reqs.append(("bfs", int(rng.integers(0, n))))
-            elif r < 0.9:
-                reqs.append(("pagerank", 5))
-            else:
-                reqs.append(("tc", rng.integers(0, n, 10000).astype(np.uint32)))
-        gaps = rng.exponential(1.0 / a.serve_rate, len(reqs))
-        srv = sg.Server(g, query_slots=2, hbm_budget_bytes=60 << 30)
-        t0 = time.perf_counter()
-        arrive = t0 + np.cumsum(gaps)
-        tickets = []
-        for (kind, arg), at in zip(reqs, arrive):
-            now = time.perf_counter()
-            if at > now:
-                time.sleep(at - now)
-            if kind == "insert":
-                t = srv.insert(arg)
-            elif kind == "remove":
-                t = srv.remove(arg)
-            elif kind == "bfs":
-                t = srv.bfs(arg)
-            elif kind == "pagerank":
-                t = srv.pagerank(arg)
-            else:
-                t = srv.tc_vertices(arg)
-            tickets.append((kind, t, arg))
-        lat = {}
-        upd_edges = 0
-        for kind, t, arg in tickets:
-            _, info = srv.wait(t)
-            lat.setdefault(kind, []).append(info["total_ms"])
-            if kind in ("insert", "remove"):
-                upd_edges += len(arg)
-        wall = time.perf_counter() - t0
-        st = srv.stats()
+        first = [0]
+
+        def make_requests(count):
+            reqs = []
+            for _ in range(count):
+                r = rng.random()
+                if r < 0.7:
+                    sz = int(min(1e5, max(1, rng.lognormal(np.log(1e3), 1.0))))
+                    if rng.random() < 0.3:
+                        reqs.append(("remove", gs.sample_edges(sz, seed=15, first=first[0])))
+                    else:
+                        reqs.append(("insert", sg.gen_rmat(sc, sz, seed=13, first=first[0],
+                                                           **RMAT)))
+                    first[0] += sz
+                elif r < 0.8:
+                    reqs.append(("bfs", int(rng.integers(0, nn))))
+                elif r < 0.9:
+                    reqs.append(("pagerank", 5))
+                else:
+                    reqs.append(("tc", rng.integers(0, nn, 10000).astype(np.uint32)))
+            return reqs
+
+        def run(srv, reqs, arrive):
+            tickets = []
+            t0 = time.perf_counter()
+            for (kind, arg), at in zip(reqs, arrive):
+                if at is not None:
+                    now = time.perf_counter()
+                    if t0 + at > now:
+                        time.sleep(t0 + at - now)
+                if kind == "insert":
+                    t = srv.insert(arg)
+                elif kind == "remove":
+                    t = srv.remove(arg)
+                elif kind == "bfs":
+                    t = srv.bfs(arg)
+                elif kind == "pagerank":
+                    t = srv.pagerank(arg)
+                else:
+                    t = srv.tc_vertices(arg)
+                tickets.append((kind, t, arg, time.perf_counter() - t0))
+            lat = {}
+            upd_edges = queries = 0
+            upd_end = qry_end = 0.0  # completion of the last update / query
+            for kind, t, arg, at in tickets:
+                _, info = srv.wait(t)
+                lat.setdefault(kind, []).append(info["total_ms"])
+                end = at + info["total_ms"] / 1e3
+                if kind in ("insert", "remove"):
+                    upd_edges += len(arg)
+                    upd_end = max(upd_end, end)
+                else:
+                    queries += 1
+                    qry_end = max(qry_end, end)
+            wall = time.perf_counter() - t0
+            allv = [x for v in lat.values() for x in v]
+            return {"requests": len(reqs), "wall_s": wall,
+                    "p50_ms": float(np.percentile(allv, 50)),
+                    "p99_ms": float(np.percentile(allv, 99)),
+                    "by_kind": {k: {"n": len(v), "p50_ms": float(np.percentile(v, 50)),
+                                    "p99_ms": float(np.percentile(v, 99))}
+                                for k, v in lat.items()},
+                    "update_edges": upd_edges, "updates_done_s": upd_end,
+                    "update_edges_per_s": upd_edges / max(upd_end, 1e-9),
+                    "queries": queries, "queries_done_s": qry_end,
+                    "queries_per_s": queries / max(qry_end, 1e-9)}
+
+        lat_reqs = make_requests(a.serve_requests)
+        sat_reqs = make_requests(2 * a.serve_requests)
+        srv = sg.Server(gs, query_slots=4, hbm_budget_bytes=60 << 30)
         slots = srv.slots
+        gaps = rng.exponential(1.0 / a.serve_rate, len(lat_reqs))
+        latency = run(srv, lat_reqs, np.cumsum(gaps).tolist())
+        latency["rate_per_s"] = a.serve_rate
+        sat = run(srv, sat_reqs, [None] * len(sat_reqs))
+        sat["offered"] = "all requests submitted at once (offered load above capacity)"
+        st = srv.stats()
         srv.close()
-        allv = [x for v in lat.values() for x in v]
-        summ = {k: {"n": len(v), "p50_ms": float(np.percentile(v, 50)),
-                    "p99_ms": float(np.percentile(v, 99))} for k, v in lat.items()}
-        return {"requests": len(reqs), "rate_per_s": a.serve_rate, "slots": slots,
-                "p50_ms": float(np.percentile(allv, 50)),
-                "p99_ms": float(np.percentile(allv, 99)),
-                "by_kind": summ, "update_edges_per_s": upd_edges / wall,
-                "wall_s": wall, "writer_passes": st["passes"],
-                "hbm_budget_bytes": 60 << 30}
+        out = {"scale": sc, "vertices": nn, "edges": gs.M(), "build_s": build_s,
+               "graph_bytes_after_load": mem_loaded, "graph_bytes_trimmed": mem_trimmed,
+               "hbm_budget_bytes": 60 << 30, "slots": slots,
+               "p50_ms": latency["p50_ms"], "p99_ms": latency["p99_ms"],
+               "sustained_update_edges_per_s": sat["update_edges_per_s"],
+               "latency_run": latency, "saturation_run": sat,
+               "writer_passes": st["passes"]}
+        gs.close()
+        return out
 
     if a.only not in ("all", "updates"):
         pr_flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
@@ -656,6 +884,8 @@ def main():
             res["extras"] = measure_extras()
         elif a.only == "compact":
             res["compact"] = measure_compact()
+        elif a.only == "static":
+            res["static_analytics"] = measure_static()
         else:
             res["bfs"] = measure_bfs()
         g.close()
@@ -682,6 +912,15 @@ def main():
                 rem.append(r.cpu().pin_memory() if host else r)
         torch.cuda.synchronize()
         return ins, rem, first
+
+    # every batch applied to g, in order, as host arrays: the oracle replays
+    # them after the timed region to check the final graph (parity)
+    applied = []
+
+    def record(ins, rem, lo, hi):
+        for i in range(lo, hi):
+            for op, x in (("insert", ins[i]), ("remove", rem[i])):
+                applied.append((op, x.cpu().numpy().view(np.uint32).reshape(-1, 2).copy()))
 
     ins_d, rem_d, next_first = make_batches(0, host=False)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
@@ -711,6 +950,7 @@ def main():
     # cannot be timed one by one, so the timed region runs without the
     # kernel profiler; per-kernel times come from a pass after it (below).
     run_steps(0, a.warmup, ins_d, rem_d)
+    record(ins_d, rem_d, 0, a.warmup + a.steps)
     barrier(world)
     torch.cuda.synchronize()
     l0 = sg.kernel_launches()
@@ -729,6 +969,7 @@ def main():
     # fresh batches (the device pass's edges are already in the graph)
     del ins_d, rem_d
     ins_h, rem_h, next_first = make_batches(next_first, host=True)
+    record(ins_h, rem_h, 0, a.warmup + a.steps)
     run_steps(0, a.warmup, ins_h, rem_h)
     eti, etr, eedges = run_steps(a.warmup, a.warmup + a.steps, ins_h, rem_h)
     e2e = {"value": world * eedges / max_over_ranks(eti, world), "unit": "edges/s",
@@ -738,10 +979,13 @@ def main():
                    "pairs; each call returns the invalid-pair count (8 B) to the host"}
     del ins_h, rem_h
 
-    # ---- kernel times: one step of each batch size on fresh batches, every
-    # kernel launched directly (planning graphs off) and bracketed by events
+    # ---- kernel times: one step of each batch size on fresh batches, the
+    # kernels a replay runs launched one by one (same size classes and scan
+    # forms as the timed region: sst_set_plan_graphs mode 2) and bracketed
+    # by events
     ins_p, rem_p, next_first = make_batches(next_first, host=False, sizes=SIZES)
-    g.set_plan_graphs(False)
+    record(ins_p, rem_p, 0, len(SIZES))
+    g.set_plan_graphs(2)
     sg.profile_start()
     run_steps(0, len(SIZES), ins_p, rem_p)
     torch.cuda.synchronize()
@@ -750,7 +994,14 @@ def main():
     prof = prof_all
     del ins_p, rem_p
 
-    batched = pagerank = bfs = serving = multi = compact = extras = None
+    # ---- parity at full size: the oracle port replays the base graph and
+    # every batch above; the device graph's CSR must equal its CSR
+    parity = None
+    if rank == 0 and not a.no_parity:
+        parity = check_parity(g, a.scale, applied)
+    del applied
+
+    batched = pagerank = bfs = serving = multi = compact = extras = static = None
     if a.only == "all":
         batched = measure_batched()
         t0 = time.time()
@@ -784,14 +1035,23 @@ def main():
         multi = measure_multi()
         compact = measure_compact()
         extras = measure_extras()
+        if rank == 0 and not a.no_cpu_baseline:
+            static = measure_static()
         serving = measure_serving()
 
 
     # ---- roofline of the update step's dominant kernel
     upd_kernels = {"kernel_pass": prof_all,
                    "note": "one step of each batch size on fresh batches after the timed "
-                           "region, every kernel launched directly and event-timed"}
+                           "region; the kernels the timed region replays (same forms) "
+                           "launched one by one and event-timed"}
     roofline = update_roofline(prof, prof_all, hbm_peak, peak_kind)
+    # the whole step against the same peak: 28 B per input pair (read 8 B,
+    # one sort write + read 16 B, write 4 B) over insert + delete time
+    step_pairs = 2 * sum(plan[a.warmup:]) / a.steps
+    step_gbs = 28 * step_pairs / (ms_per_step / 1e3) / 1e9
+    roofline["whole_step"] = {"pairs_per_step": step_pairs, "bytes_per_pair": 28,
+                              "achieved": step_gbs, "frac": step_gbs / hbm_peak}
 
     # ---- CPU baseline (bounded sample, rank 0 only)
     cpu = None
@@ -814,6 +1074,7 @@ def main():
         "data": "synthetic RMAT (seeded device generator; no dataset)",
         "config": workload_config(a),
         "roofline": roofline,
+        "parity": parity,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches,
@@ -826,6 +1087,7 @@ def main():
         "multi_source": multi,
         "compact_snapshot": compact,
         "ingest_and_weighted": extras,
+        "static_analytics": static,
         "serving": serving,
         "update_kernels": upd_kernels,
     }
@@ -845,7 +1107,8 @@ NCU_TRAFFIC = {"(k_scan_lb<T, Op, Epi>)": 6.43e6, "(k_scatter<false, 16>)": 8.46
 def update_roofline(prof, prof_all, hbm_peak, peak_kind):
     """Roofline of the update step's dominant kernel from its live event
     timings in the kernel pass after the timed region (one step of each
-    batch size, every kernel launched directly), with its share there.
+    batch size, the kernels the timed region runs launched one by one), with
+    its share there.
 
     Algorithmic bytes are declared by each launch site at its launch size
     (what the kernel must read and write, independent of caching):

@@ -91,7 +91,9 @@ SST_API sst_status sst_sync(sst_graph *g);
  * the planning launches of a raw-pair, unweighted batch of up to 2^20 pairs
  * (key sort to plan readback) are captured once per batch size and graph
  * layout and replayed as one CUDA graph launch; 0: every kernel is launched
- * directly.  Results are the same either way. */
+ * directly; 2: the launches a replay would run (same size classes, same
+ * kernel forms) are launched directly, so a profiler can time each of them.
+ * Results are the same in every mode. */
 SST_API sst_status sst_set_plan_graphs(sst_graph *g, int enable);
 SST_API const char *sst_last_error_message(void);
 SST_API const char *sst_status_string(sst_status s);
@@ -181,8 +183,15 @@ SST_API sst_status sst_common_neighbors_batch(sst_graph *g, const uint32_t *pair
                                       uint64_t *out, uint32_t flags);
 /* touch_all_sum  SparseMatrix.hpp:436-454 */
 SST_API sst_status sst_touch_all_sum(sst_graph *g, uint64_t *out);
-/* get_memory_size  SparseMatrix.hpp:317,528-535: device bytes held */
+/* get_memory_size  SparseMatrix.hpp:317,528-535: device bytes held (the
+ * storage, plus the scratch the graph keeps between calls) */
 SST_API sst_status sst_memory_size(sst_graph *g, uint64_t *out);
+/* Frees the scratch a graph keeps between calls (no reference counterpart:
+ * the reference allocates per call): update-batch scratch, staging, the
+ * captured planning graphs, the leaf directory and the traversal buffers.
+ * The next call that needs them allocates them again; tuning is kept.
+ * Useful after a bulk load, whose large batches grow the scratch. */
+SST_API sst_status sst_release_scratch(sst_graph *g);
 /* degree_order_map()  SparseMatrix.hpp:737-752: map[v] = rank of v when the
  * vertices are ordered by (degree, id) descending */
 SST_API sst_status sst_degree_order_map(sst_graph *g, uint32_t *map,
@@ -203,7 +212,10 @@ SST_API sst_status sst_sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
  * The graph must be symmetric (every (u,v) stored with (v,u)), as the
  * reference drivers build it from symmetrised inputs: the pull (dense
  * frontier) steps and PageRank read a vertex's stored row as its in-edges.
- * On a directed graph the results are not defined. */
+ * On a directed graph the results are not defined.  Every traversal entry
+ * point below (and the serving loop, and the snapshot's PageRank) needs as
+ * many rows as columns and returns SST_EINVAL otherwise: column ids index
+ * per-vertex arrays of `rows` entries. */
 /* BFS(g, src)  test.hpp:486: parents (parent[src] = src, -1 unreached)
  * and/or depths (-1 unreached); either pointer may be NULL */
 SST_API sst_status sst_bfs(sst_graph *g, uint32_t src, int32_t *parents,
@@ -215,8 +227,10 @@ SST_API sst_status sst_pagerank(sst_graph *g, uint32_t iters, double damping,
  * reference).  For callers that cannot let a call allocate: a serving loop
  * under a fixed HBM budget, or a host program sharing the GPU whose other
  * streams would stall on the device-wide synchronisation of cudaMalloc /
- * cudaFree.  Same result as sst_pagerank; its scratch is one fixed array
- * inside the library, so graphs are limited to 262,144 rows (larger ones get
+ * cudaFree.  Matches sst_pagerank within 1e-9 relative (it sums FP64
+ * values in warp order, not sst_pagerank's exact fixed-point sums); its
+ * scratch is one fixed array inside the library, so graphs are limited to
+ * 262,144 rows (larger ones, and graphs with more columns than rows, get
  * SST_EINVAL) and d_rank must be device memory.  The first call on a device
  * looks the array up (make it before capturing a stream); calls that overlap
  * on the GPU share the array and race. */
@@ -384,6 +398,14 @@ SST_API sst_status sst_raw_state(sst_graph *g, uint64_t *base, uint32_t *cap,
                                  uint64_t *nslots);
 /* number of kernel launches this library issued since load */
 SST_API uint64_t sst_kernel_launches(void);
+/* Diagnostic (no reference counterpart): how many times a tile of the
+ * single-pass scans (update batches, launched directly) polls a
+ * predecessor's status before it stops waiting and reduces the
+ * predecessors' inputs itself.  Default 8192; 0 makes every tile after the
+ * first take that fallback.  Results are the same for every value; the
+ * setting is process-wide and returns the previous value in *old (may be
+ * NULL). */
+SST_API sst_status sst_set_scan_lookback_polls(uint32_t polls, uint32_t *old);
 
 #ifdef __cplusplus
 }

@@ -443,25 +443,81 @@ void sst_o_sample_edges(const sst_o_graph *g, uint64_t seed, uint64_t first,
 
 /* BFS depths; -1 = unreached.  The reference returns parents and derives
  * depths by chasing them (internal/test.hpp:486-509); depths are unique, so
- * they are the parity target. */
-void sst_o_bfs(const sst_o_graph *g, uint32_t src, int32_t *depth) {
-  for (uint32_t v = 0; v < g->n; v++) depth[v] = -1;
-  if (src >= g->n) return;
-  uint32_t *q = (uint32_t *)malloc((size_t)g->n * sizeof(uint32_t));
-  uint64_t h = 0, t = 0;
-  q[t++] = src;
+ * they are the parity target.  Level-synchronous over the host threads:
+ * each level's vertices claim unvisited neighbours with a compare-and-swap,
+ * so the depths do not depend on the claim order. */
+static int nthreads_max(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+static int thread_id(void) {
+#ifdef _OPENMP
+  return omp_get_thread_num();
+#else
+  return 0;
+#endif
+}
+
+/* vertices reached, in level order, into order[] (may be NULL); returns
+ * their count */
+static uint64_t bfs_levels(const sst_o_graph *g, uint32_t src, int32_t *depth,
+                           uint32_t *order) {
+  const uint32_t n = g->n;
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < (int64_t)n; v++) depth[v] = -1;
+  if (src >= n) return 0;
+  uint32_t *q = order ? order : (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+  const int nt = nthreads_max();
+  uint32_t **buf = (uint32_t **)calloc((size_t)nt, sizeof(uint32_t *));
+  uint64_t *bcap = (uint64_t *)calloc((size_t)nt, sizeof(uint64_t));
+  uint64_t *bcnt = (uint64_t *)calloc((size_t)nt + 1, sizeof(uint64_t));
+  uint64_t head = 0, tail = 1;
+  q[0] = src;
   depth[src] = 0;
-  while (h < t) {
-    uint32_t v = q[h++];
-    for (uint32_t i = 0; i < g->deg[v]; i++) {
-      uint32_t w = g->adj[v][i];
-      if (depth[w] < 0) {
-        depth[w] = depth[v] + 1;
-        q[t++] = w;
+  for (int32_t d = 0; head < tail; d++) {
+    memset(bcnt, 0, ((size_t)nt + 1) * sizeof(uint64_t));
+#pragma omp parallel
+    {
+      const int t = thread_id();
+#pragma omp for schedule(dynamic, 64)
+      for (int64_t k = (int64_t)head; k < (int64_t)tail; k++) {
+        const uint32_t v = q[k];
+        for (uint32_t i = 0; i < g->deg[v]; i++) {
+          const uint32_t w = g->adj[v][i];
+          int32_t expect = -1;
+          if (depth[w] < 0 &&
+              __atomic_compare_exchange_n(&depth[w], &expect, d + 1, 0, __ATOMIC_RELAXED,
+                                          __ATOMIC_RELAXED)) {
+            if (bcnt[t] == bcap[t]) {
+              bcap[t] = bcap[t] ? 2 * bcap[t] : 1024;
+              buf[t] = (uint32_t *)realloc(buf[t], bcap[t] * sizeof(uint32_t));
+            }
+            buf[t][bcnt[t]++] = w;
+          }
+        }
       }
     }
+    uint64_t at = tail;
+    for (int t = 0; t < nt; t++) {
+      memcpy(q + at, buf[t], bcnt[t] * sizeof(uint32_t));
+      at += bcnt[t];
+    }
+    head = tail;
+    tail = at;
   }
-  free(q);
+  for (int t = 0; t < nt; t++) free(buf[t]);
+  free(buf);
+  free(bcap);
+  free(bcnt);
+  if (!order) free(q);
+  return tail;
+}
+
+void sst_o_bfs(const sst_o_graph *g, uint32_t src, int32_t *depth) {
+  bfs_levels(g, src, depth, NULL);
 }
 
 /* PageRank, pull form over the (symmetric) neighbour sets, in FP64:
@@ -490,85 +546,96 @@ void sst_o_pagerank(const sst_o_graph *g, uint32_t iters, double damping,
   free(contrib);
 }
 
-/* connected components: label = smallest vertex id in the component */
+/* connected components: label = smallest vertex id in the component.
+ * Concurrent union-find over the host threads: a root is only ever linked
+ * below a smaller root (compare-and-swap on the larger one), so every
+ * component's final root is its smallest id. */
+static uint32_t uf_find(uint32_t *par, uint32_t v) {
+  for (;;) {
+    uint32_t p = __atomic_load_n(&par[v], __ATOMIC_RELAXED);
+    if (p == v) return v;
+    uint32_t gp = __atomic_load_n(&par[p], __ATOMIC_RELAXED);
+    if (gp != p) __atomic_compare_exchange_n(&par[v], &p, gp, 0, __ATOMIC_RELAXED,
+                                             __ATOMIC_RELAXED); /* halving */
+    v = gp;
+  }
+}
+
 void sst_o_cc(const sst_o_graph *g, uint32_t *label) {
-  uint32_t n = g->n;
-  for (uint32_t v = 0; v < n; v++) label[v] = UINT32_MAX;
-  uint32_t *q = (uint32_t *)malloc((size_t)(n ? n : 1) * sizeof(uint32_t));
-  for (uint32_t s = 0; s < n; s++) {
-    if (label[s] != UINT32_MAX) continue;
-    uint64_t h = 0, t = 0;
-    q[t++] = s;
-    label[s] = s;
-    while (h < t) {
-      uint32_t v = q[h++];
-      for (uint32_t i = 0; i < g->deg[v]; i++) {
-        uint32_t w = g->adj[v][i];
-        if (label[w] == UINT32_MAX) {
-          label[w] = s;
-          q[t++] = w;
-        }
+  const uint32_t n = g->n;
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < (int64_t)n; v++) label[v] = (uint32_t)v;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t uu = 0; uu < (int64_t)n; uu++) {
+    const uint32_t u = (uint32_t)uu;
+    for (uint32_t i = 0; i < g->deg[u]; i++) {
+      const uint32_t w = g->adj[u][i];
+      if (w >= n) continue;
+      for (;;) {
+        uint32_t a = uf_find(label, u), b = uf_find(label, w);
+        if (a == b) break;
+        uint32_t hi = a > b ? a : b, lo = a > b ? b : a, expect = hi;
+        if (__atomic_compare_exchange_n(&label[hi], &expect, lo, 0, __ATOMIC_RELAXED,
+                                        __ATOMIC_RELAXED))
+          break;
       }
     }
   }
-  free(q);
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < (int64_t)n; v++) label[v] = uf_find(label, (uint32_t)v);
+  /* the finds above only shorten paths: a second pass settles every label
+   * on its root */
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < (int64_t)n; v++) label[v] = label[label[v]];
 }
 
 /* Single-source betweenness dependencies (Brandes 2001), FP64:
  *   sigma(src) = 1, sigma(w) = sum_{v in N(w), depth v = depth w - 1} sigma(v)
  *   dep(v) = sum_{w in N(v), depth w = depth v + 1} sigma(v)/sigma(w) * (1 + dep(w))
  * sums in ascending neighbour order; unreached vertices get 0; the source
- * keeps its own dep by the same formula. */
+ * keeps its own dep by the same formula.  Each level's vertices run in
+ * parallel (their sums read only the levels before, resp. after, them), so
+ * every value is the same sum in the same order as a serial pass. */
 void sst_o_bc(const sst_o_graph *g, uint32_t src, double *dep) {
-  uint32_t n = g->n;
-  int32_t *depth = (int32_t *)malloc((size_t)(n ? n : 1) * sizeof(int32_t));
-  double *sigma = (double *)calloc(n ? n : 1, sizeof(double));
-  uint32_t *order = (uint32_t *)malloc((size_t)(n ? n : 1) * sizeof(uint32_t));
-  for (uint32_t v = 0; v < n; v++) dep[v] = 0.0;
-  if (src >= n) {
-    free(depth);
-    free(sigma);
-    free(order);
-    return;
-  }
-  sst_o_bfs(g, src, depth);
-  /* vertices in non-decreasing depth (BFS order is one) */
-  uint64_t t = 0, h = 0;
-  order[t++] = src;
-  {
-    char *seen = (char *)calloc(n, 1);
-    seen[src] = 1;
-    while (h < t) {
-      uint32_t v = order[h++];
-      for (uint32_t i = 0; i < g->deg[v]; i++) {
-        uint32_t w = g->adj[v][i];
-        if (!seen[w]) {
-          seen[w] = 1;
-          order[t++] = w;
-        }
-      }
-    }
-    free(seen);
-  }
+  const uint32_t n = g->n;
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < (int64_t)n; v++) dep[v] = 0.0;
+  if (src >= n) return;
+  int32_t *depth = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+  double *sigma = (double *)calloc(n, sizeof(double));
+  uint32_t *order = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+  const uint64_t t = bfs_levels(g, src, depth, order);
+  /* level boundaries in order[] (level-synchronous BFS emits by level) */
+  const int32_t maxd = depth[order[t - 1]];
+  uint64_t *lvl = (uint64_t *)calloc((size_t)maxd + 2, sizeof(uint64_t));
+  for (uint64_t k = 0; k < t; k++) lvl[depth[order[k]] + 1]++;
+  for (int32_t d = 0; d <= maxd; d++) lvl[d + 1] += lvl[d];
   sigma[src] = 1.0;
-  for (uint64_t k = 1; k < t; k++) {
-    uint32_t w = order[k];
-    double s = 0.0;
-    for (uint32_t i = 0; i < g->deg[w]; i++) {
-      uint32_t v = g->adj[w][i];
-      if (depth[v] == depth[w] - 1) s += sigma[v];
+  for (int32_t d = 1; d <= maxd; d++) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t k = (int64_t)lvl[d]; k < (int64_t)lvl[d + 1]; k++) {
+      const uint32_t w = order[k];
+      double s = 0.0;
+      for (uint32_t i = 0; i < g->deg[w]; i++) {
+        const uint32_t v = g->adj[w][i];
+        if (depth[v] == d - 1) s += sigma[v];
+      }
+      sigma[w] = s;
     }
-    sigma[w] = s;
   }
-  for (uint64_t k = t; k-- > 0;) {
-    uint32_t v = order[k];
-    double s = 0.0;
-    for (uint32_t i = 0; i < g->deg[v]; i++) {
-      uint32_t w = g->adj[v][i];
-      if (depth[w] == depth[v] + 1) s += sigma[v] / sigma[w] * (1.0 + dep[w]);
+  for (int32_t d = maxd; d >= 0; d--) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t k = (int64_t)lvl[d]; k < (int64_t)lvl[d + 1]; k++) {
+      const uint32_t v = order[k];
+      double s = 0.0;
+      for (uint32_t i = 0; i < g->deg[v]; i++) {
+        const uint32_t w = g->adj[v][i];
+        if (depth[w] == d + 1) s += sigma[v] / sigma[w] * (1.0 + dep[w]);
+      }
+      dep[v] = s;
     }
-    dep[v] = s;
   }
+  free(lvl);
   free(order);
   free(sigma);
   free(depth);

@@ -109,6 +109,7 @@ SIGNATURES = {
     "sst_common_neighbors_batch": (_i32, [_vp, _vp, _u64, ctypes.c_int, _vp, _u32]),
     "sst_touch_all_sum": (_i32, [_vp, ctypes.POINTER(_u64)]),
     "sst_memory_size": (_i32, [_vp, ctypes.POINTER(_u64)]),
+    "sst_release_scratch": (_i32, [_vp]),
     "sst_sample_edges": (_i32, [_vp, _u64, _u64, _u64, _vp, _u32]),
     "sst_degree_order_map": (_i32, [_vp, _vp, _u32]),
     "sst_rewrite_graph": (_i32, [_vp, _vp, _u32, ctypes.POINTER(_vp)]),
@@ -132,6 +133,7 @@ SIGNATURES = {
     "sst_gen_er": (_i32, [_u32, _u64, _u64, _u64, _vp, _u32]),
     "sst_gen_ref_rmat": (_i32, [_u32, _dbl, _dbl, _dbl, _u64, _u64, _vp, _u32]),
     "sst_kernel_launches": (_u64, []),
+    "sst_set_scan_lookback_polls": (_i32, [_u32, ctypes.POINTER(_u32)]),
     "sst_raw_state": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64)]),
     "sst_pagerank_noalloc": (_i32, [_vp, _u32, _dbl, _vp]),
     "sst_tc_vertices": (_i32, [_vp, _vp, _u64, _vp, _u32]),
@@ -212,6 +214,15 @@ def _pairs(edges):
     return e, e.shape[0]
 
 
+def set_scan_lookback_polls(polls: int) -> int:
+    """Polls of a predecessor's status in the single-pass scans before a
+    tile reduces the inputs itself (0: every tile does); returns the previous
+    setting.  Results do not depend on it."""
+    old = ctypes.c_uint32()
+    _check(lib().sst_set_scan_lookback_polls(int(polls), ctypes.byref(old)))
+    return old.value
+
+
 def kernel_launches() -> int:
     return int(lib().sst_kernel_launches())
 
@@ -268,10 +279,13 @@ class SparseMatrixV:
     def set_stream(self, stream_ptr: int | None):
         _check(lib().sst_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
 
-    def set_plan_graphs(self, enable: bool):
-        """Replay small batches' planning launches as CUDA graphs (default)
-        or launch every kernel directly; results are the same."""
-        _check(lib().sst_set_plan_graphs(self._h, 1 if enable else 0))
+    def set_plan_graphs(self, enable):
+        """Replay small batches' planning launches as CUDA graphs (True /
+        1, default), launch every kernel directly (False / 0), or launch the
+        kernels a replay runs directly (2: for per-kernel timing); results
+        are the same."""
+        mode = enable if isinstance(enable, int) and not isinstance(enable, bool) else (1 if enable else 0)
+        _check(lib().sst_set_plan_graphs(self._h, mode))
 
     def sync(self):
         _check(lib().sst_sync(self._h))
@@ -473,6 +487,11 @@ class SparseMatrixV:
         r = ctypes.c_uint64()
         _check(lib().sst_memory_size(self._h, ctypes.byref(r)))
         return r.value
+
+    def release_scratch(self):
+        """Free the scratch the graph keeps between calls (update, staging,
+        traversal buffers); it is allocated again when needed."""
+        _check(lib().sst_release_scratch(self._h))
 
     def raw_state(self):
         """(base, cap, deg, slots, lcnt): the device layout, for checks."""

@@ -37,6 +37,19 @@ using sst::set_error_message;
     }                                                                         \
   } while (0)
 
+// Traversals index per-vertex arrays of `rows` entries by column id, so a
+// graph with more columns than rows would send them past those arrays: they
+// take square graphs only (the reference's drivers build square, symmetric
+// graphs, internal/test.hpp:407-450).
+#define CHECK_SQUARE(g, what)                                                 \
+  do {                                                                        \
+    if ((g)->n != (g)->width) {                                               \
+      set_error_message("%s needs as many rows as columns (%u x %u)", what,  \
+                        (g)->n, (g)->width);                                  \
+      return SST_EINVAL;                                                      \
+    }                                                                         \
+  } while (0)
+
 namespace {
 
 bool is_dev(uint32_t flags) { return (flags & SST_DEVICE_PTR) != 0; }
@@ -126,6 +139,12 @@ const char *sst_status_string(sst_status s) {
 }
 
 uint64_t sst_kernel_launches(void) { return sst::launches(); }
+
+sst_status sst_set_scan_lookback_polls(uint32_t polls, uint32_t *old) {
+  if (old) *old = (uint32_t)sst::lookback_polls();
+  sst::set_lookback_polls(polls > (1u << 30) ? (1 << 30) : (int)polls);
+  return SST_OK;
+}
 
 sst_status sst_profile_start(const char *kernel_filter) {
   sst::profile_start(kernel_filter);
@@ -223,7 +242,12 @@ sst_status sst_set_stream(sst_graph *g, void *stream) {
 sst_status sst_set_plan_graphs(sst_graph *g, int enable) {
   CHECK_G(g);
   SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
+  if (enable < 0 || enable > 2) {
+    set_error_message("plan graph mode must be 0, 1 or 2");
+    return SST_EINVAL;
+  }
   g->plan_graphs = enable != 0;
+  g->plan_direct = enable == 2;
   if (!enable) sst::plan_cache_release(g);
   return SST_OK;
 }
@@ -549,6 +573,11 @@ sst_status sst_touch_all(sst_graph *g, uint64_t *out) {
   return sst_touch_all_sum(g, out);
 }
 
+sst_status sst_release_scratch(sst_graph *g) {
+  CHECK_G(g);
+  return sst::release_scratch(g);
+}
+
 sst_status sst_memory_size(sst_graph *g, uint64_t *out) {
   if (!g || !out) return SST_EINVAL;
   *out = sst::graph_device_bytes(g);
@@ -572,6 +601,7 @@ sst_status sst_sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
 sst_status sst_tc_vertices(sst_graph *g, const uint32_t *vertices, uint64_t k,
                            uint64_t *out, uint32_t flags) {
   CHECK_G(g);
+  CHECK_SQUARE(g, "sst_tc_vertices");
   if (k && (!vertices || !out)) return SST_EINVAL;
   sst_status st = is_dev(flags) ? SST_OK : io_begin(g, k * 12 + 512);
   if (st != SST_OK) return st;
@@ -658,6 +688,7 @@ sst_status sst_common_neighbors_batch(sst_graph *g, const uint32_t *pairs,
 sst_status sst_bfs(sst_graph *g, uint32_t src, int32_t *parents,
                    int32_t *depths, uint32_t flags) {
   CHECK_G(g);
+  CHECK_SQUARE(g, "sst_bfs");
   if (src >= g->n) {
     set_error_message("source out of range");
     return SST_EINVAL;
@@ -699,6 +730,7 @@ static sst_status sources_to_host(sst_graph *g, const uint32_t *srcs,
 sst_status sst_bfs_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
                          int32_t *depths, uint32_t flags) {
   CHECK_G(g);
+  CHECK_SQUARE(g, "sst_bfs_multi");
   if (k > 64 || (k && (!srcs || !depths))) {
     set_error_message(k > 64 ? "at most 64 sources" : "null argument");
     return SST_EINVAL;
@@ -721,6 +753,7 @@ sst_status sst_bfs_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
 sst_status sst_bc_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
                         double *out, uint32_t flags) {
   CHECK_G(g);
+  CHECK_SQUARE(g, "sst_bc_multi");
   if (k > 64 || (k && (!srcs || !out))) {
     set_error_message(k > 64 ? "at most 64 sources" : "null argument");
     return SST_EINVAL;
@@ -742,6 +775,7 @@ sst_status sst_bc_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
 
 sst_status sst_bf(sst_graph *g, uint32_t src, int32_t *dist, uint32_t flags) {
   CHECK_G(g);
+  CHECK_SQUARE(g, "sst_bf");
   if (!dist) return SST_EINVAL;
   if (src >= g->n) {
     set_error_message("source out of range");
@@ -759,6 +793,7 @@ sst_status sst_bf(sst_graph *g, uint32_t src, int32_t *dist, uint32_t flags) {
 
 sst_status sst_autotune(sst_graph *g, sst_tuning *out) {
   CHECK_G(g);
+  CHECK_SQUARE(g, "sst_autotune");
   if (!out) return SST_EINVAL;
   return sst::autotune(g, out);
 }
@@ -778,6 +813,7 @@ sst_status sst_set_tuning(sst_graph *g, const sst_tuning *in) {
 sst_status sst_pagerank(sst_graph *g, uint32_t iters, double damping,
                         double *out, uint32_t flags) {
   CHECK_G(g);
+  CHECK_SQUARE(g, "sst_pagerank");
   if (!out) return SST_EINVAL;
   sst_status st = is_dev(flags) ? SST_OK : io_begin(g, (uint64_t)g->n * 8 + 256);
   if (st != SST_OK) return st;
@@ -791,6 +827,7 @@ sst_status sst_pagerank(sst_graph *g, uint32_t iters, double damping,
 
 sst_status sst_cc(sst_graph *g, uint32_t *labels, uint32_t flags) {
   CHECK_G(g);
+  CHECK_SQUARE(g, "sst_cc");
   if (!labels) return SST_EINVAL;
   sst_status st = is_dev(flags) ? SST_OK : io_begin(g, (uint64_t)g->n * 4 + 256);
   if (st != SST_OK) return st;
@@ -804,6 +841,7 @@ sst_status sst_cc(sst_graph *g, uint32_t *labels, uint32_t flags) {
 
 sst_status sst_bc(sst_graph *g, uint32_t src, double *out, uint32_t flags) {
   CHECK_G(g);
+  CHECK_SQUARE(g, "sst_bc");
   if (!out || src >= g->n) {
     set_error_message("bad argument to sst_bc");
     return SST_EINVAL;
@@ -821,6 +859,7 @@ sst_status sst_bc(sst_graph *g, uint32_t src, double *out, uint32_t flags) {
 sst_status sst_tc(sst_graph *g, uint64_t *total, uint64_t *per_vertex,
                   uint32_t flags) {
   CHECK_G(g);
+  CHECK_SQUARE(g, "sst_tc");
   if (!total) return SST_EINVAL;
   sst_status st = is_dev(flags) ? SST_OK : io_begin(g, (uint64_t)g->n * 8 + 256);
   if (st != SST_OK) return st;

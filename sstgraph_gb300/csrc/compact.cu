@@ -904,6 +904,11 @@ sst_status sst_compact_pagerank(sst_compact *c, uint32_t iters, double damping,
   sst_status st = compact_dev_check(c);
   if (st != SST_OK) return st;
   if (!out) return SST_EINVAL;
+  if (c->n != c->width) {  // column ids index per-row vectors
+    sst::set_error_message("sst_compact_pagerank needs as many rows as columns (%u x %u)",
+                           c->n, c->width);
+    return SST_EINVAL;
+  }
   SST_CUDA_TRY(cudaSetDevice(c->device));
   if (flags & SST_DEVICE_PTR) {
     st = sst::compact_pagerank(c, iters, damping, out);

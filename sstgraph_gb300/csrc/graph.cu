@@ -1022,8 +1022,21 @@ void *pinned(sst_graph *g, size_t bytes) {
 
 uint64_t graph_device_bytes(const sst_graph *g) {
   return (uint64_t)g->n * 16 + g->nslots * (g->weighted ? 8 : 4) + g->nslots / kLeaf +
-         g->arena.cap + g->work.cap +
-         g->dir.cap * (4 + 8 + 4 + 8) + (uint64_t)(g->n + 1) * 8;
+         g->arena.cap + g->work.cap + g->io.cap +
+         g->dir.cap * (4 + 8 + 4 + 8) + (uint64_t)(g->n + 1) * 8 + trav_device_bytes(g);
+}
+
+sst_status release_scratch(sst_graph *g) {
+  sst_status st = sync_checked(g);  // reads the last batch's device check
+  if (st != SST_OK) return st;
+  if (g->side) SST_CUDA_TRY(cudaStreamSynchronize(g->side));
+  plan_cache_release(g);  // captured launches point into the arena
+  g->arena.release();
+  g->work.release();
+  g->io.release();
+  g->dir.release();
+  trav_trim(g);
+  return SST_OK;
 }
 
 static sst_status budget_check(sst_graph *g, uint64_t extra) {
@@ -1569,9 +1582,15 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   // replayed for small batches (the kernel profiler times a replay as one
   // entry, update_plan_graph)
   if (replay) {
-    sst_status st = plan_graph_launch(g, b, insert, dg, s, [&](cudaStream_t cs) {
-      return plan(cs, false);
-    });
+    sst_status st;
+    if (g->plan_direct) {
+      CaptureForms forms;
+      st = plan(s, false);
+    } else {
+      st = plan_graph_launch(g, b, insert, dg, s, [&](cudaStream_t cs) {
+        return plan(cs, false);
+      });
+    }
     if (st != SST_OK) return st;
     if (insert) {
       st = fork_merges(s);

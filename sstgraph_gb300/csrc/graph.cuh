@@ -58,6 +58,8 @@ struct sst_graph {
   cudaEvent_t fork_ev = nullptr, merge_done = nullptr;
   sst::PlanCache *plans = nullptr;  // captured planning launches
   bool plan_graphs = true;  // replay planning launches (off: launch directly)
+  bool plan_direct = false; // with plan_graphs: launch them directly, in the
+                            // kernel forms of a replay (per-kernel timing)
   uint32_t n = 0, width = 0;
   int rbits = 0, dbits = 0;
   sst::PmaParams params;
@@ -132,5 +134,12 @@ sst_status sync_checked(sst_graph *g);
 // host staging buffer (pinned) of at least `bytes`
 void *pinned(sst_graph *g, size_t bytes);
 void trav_release(sst_graph *g);
+// frees the traversal buffers and work lists (kept: the tuning)
+void trav_trim(sst_graph *g);
+uint64_t trav_device_bytes(const sst_graph *g);
+// frees every buffer the graph rebuilds on demand: update scratch, task
+// staging, host-call staging, captured planning graphs, the leaf directory
+// and the traversal buffers
+sst_status release_scratch(sst_graph *g);
 
 }  // namespace sst

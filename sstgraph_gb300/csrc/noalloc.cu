@@ -4,13 +4,16 @@
 // loop that holds a fixed HBM budget must not have a request fail half-way
 // on an allocation, and a host program that shares the GPU with other
 // streams cannot afford cudaMalloc / cudaFree, which synchronise the whole
-// device.  This entry point runs the pull PageRank of sst_pagerank with its
+// device.  This entry point runs a pull PageRank with sst_pagerank's
+// definition (results within 1e-9 relative: it sums FP64 values in warp
+// order, where sst_pagerank sums exact fixed-point integers) with its
 // scratch -- the two vectors of per-vertex contributions rank/deg -- in one
 // file-scope device array of fixed size, so the call itself issues kernels
 // and nothing else.  The graph handle and the output vector are the
 // caller's, allocated beforehand.
 //
-// Limits and sharing: graphs up to kNoAllocMaxVertices rows.  Every call in
+// Limits and sharing: square graphs (column ids index the contribution
+// vectors) of up to kNoAllocMaxVertices rows.  Every call in
 // the process uses the same array, on whatever stream the graph is bound to:
 // two calls that overlap on the GPU (different streams, or different graphs
 // on the same device at once) race on it.  Each call initialises the part
@@ -103,6 +106,12 @@ sst_status sst_pagerank_noalloc(sst_graph *g, uint32_t iters, double damping,
   using namespace sst;
   if (!g || !d_rank) {
     set_error_message("sst_pagerank_noalloc: null graph or output");
+    return SST_EINVAL;
+  }
+  // column ids index the contribution vectors, which hold one entry per row
+  if (g->n != g->width) {
+    set_error_message("sst_pagerank_noalloc needs as many rows as columns (%u x %u)",
+                      g->n, g->width);
     return SST_EINVAL;
   }
   if (g->n > kNoAllocMaxVertices) {

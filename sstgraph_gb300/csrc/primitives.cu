@@ -32,6 +32,14 @@ unsigned long long next_scan_tag() {
   return kScanTag | (e << 2);
 }
 
+thread_local bool t_capture_forms = false;
+
+static std::atomic<int> g_lookback_polls{kLookbackPolls};
+int lookback_polls() { return g_lookback_polls.load(std::memory_order_relaxed); }
+void set_lookback_polls(int polls) {
+  g_lookback_polls.store(polls < 0 ? 0 : polls, std::memory_order_relaxed);
+}
+
 // ------------------------------------------------------------- profiler
 namespace {
 struct Pending {

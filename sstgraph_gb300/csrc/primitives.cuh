@@ -16,6 +16,11 @@ void note_launches(int64_t k);
 uint64_t launches();
 // a tag unique to one single-pass scan launch (see ScanStatus)
 unsigned long long next_scan_tag();
+// polls of a predecessor's flag before a single-pass scan tile reduces the
+// predecessors' inputs itself (kLookbackPolls unless set; 0: no tile waits,
+// every tile after the first takes that fallback)
+int lookback_polls();
+void set_lookback_polls(int polls);
 
 // Kernel profiler: while enabled, every launch is bracketed by a pair of
 // CUDA events on its own stream; profile_collect() folds the elapsed times
@@ -342,7 +347,7 @@ __device__ __forceinline__ T warp_reduce_all(T v, Op op) {
 template <typename T, typename Op>
 __device__ T scan_lookback(const ScanStatus<T> *st, uint64_t tile,
                            unsigned long long tag, T identity, Op op,
-                           const T *in, uint64_t n, bool reverse) {
+                           const T *in, uint64_t n, bool reverse, int polls) {
   __shared__ int s_stop, s_fail;
   __shared__ T s_part[kScanThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -357,11 +362,11 @@ __device__ T scan_lookback(const ScanStatus<T> *st, uint64_t tile,
     // tiles below tile 0 act as an empty inclusive prefix
     unsigned long long f = tag | 2ull;
     if (t >= 0) {
-      for (int p = 0;; p++) {
-        f = *(volatile const unsigned long long *)&st[t].flag;
-        if ((f & ~3ull) == tag && (f & 3ull) != 0) break;
-        if (p == kLookbackPolls) {
-          f = 0;
+      f = 0;  // polls == 0: treated as never published
+      for (int p = 0; p < polls; p++) {
+        const unsigned long long x = *(volatile const unsigned long long *)&st[t].flag;
+        if ((x & ~3ull) == tag && (x & 3ull) != 0) {
+          f = x;
           break;
         }
         __nanosleep(p < 64 ? 32 : 512);
@@ -413,7 +418,7 @@ __global__ void __launch_bounds__(kScanThreads)
 k_scan_lb(const T *__restrict__ in, Epi out, uint64_t n,
           T identity, Op op, bool reverse, bool exclusive,
           T *__restrict__ total_out, const uint32_t *__restrict__ d_n,
-          ScanStatus<T> *st, unsigned long long tag) {
+          ScanStatus<T> *st, unsigned long long tag, int polls) {
   if (d_n && *d_n < n) n = *d_n;
   const uint64_t tile = blockIdx.x, base = tile * kScanTile;
   if (base >= n) {
@@ -435,7 +440,7 @@ k_scan_lb(const T *__restrict__ in, Epi out, uint64_t n,
     if (threadIdx.x == 0) scan_publish(&st[0], tag, 2, total);
   } else {
     if (threadIdx.x == 0) scan_publish(&st[tile], tag, 1, total);
-    carry = scan_lookback(st, tile, tag, identity, op, in, n, reverse);
+    carry = scan_lookback(st, tile, tag, identity, op, in, n, reverse, polls);
     if (threadIdx.x == 0) scan_publish(&st[tile], tag, 2, op(carry, total));
   }
   run = op(carry, run);
@@ -450,7 +455,18 @@ k_scan_lb(const T *__restrict__ in, Epi out, uint64_t n,
     *total_out = op(carry, total);
 }
 
+// While alive, scans launched from this thread take the forms a stream
+// capture would (no per-launch tag): kernels launched directly then match
+// the ones a replayed capture runs, so they can be timed one by one.
+extern thread_local bool t_capture_forms;
+struct CaptureForms {
+  bool prev;
+  CaptureForms() : prev(t_capture_forms) { t_capture_forms = true; }
+  ~CaptureForms() { t_capture_forms = prev; }
+};
+
 inline bool stream_capturing(cudaStream_t s) {
+  if (t_capture_forms) return true;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
     cudaGetLastError();
@@ -493,7 +509,7 @@ cudaError_t scan_epi(const T *in, uint64_t n, T identity, Op op, bool exclusive,
       SST_LAUNCH_NB(d_n ? "(k_scan_lb<T, Op, Epi>, device count)" : "(k_scan_lb<T, Op, Epi>)",
                     d_n ? 0 : 2 * sizeof(T) * n, (k_scan_lb<T, Op, Epi>), (unsigned)tiles,
                     kScanThreads, 0, s, in, epi, n, identity, op, reverse,
-                    exclusive, total_out, d_n, st, next_scan_tag());
+                    exclusive, total_out, d_n, st, next_scan_tag(), lookback_polls());
       return cudaGetLastError();
     }
   }

@@ -420,6 +420,10 @@ sst_status sst_server_create(sst_graph *g, const sst_server_config *cfg,
     return SST_EINVAL;
   }
   *out = nullptr;
+  if (g->n != g->width) {  // queries are traversals: square graphs only
+    sst::set_error_message("a server needs a graph with as many rows as columns");
+    return SST_EINVAL;
+  }
   sst_server *s = new (std::nothrow) sst_server();
   if (!s) return SST_ENOMEM;
   s->g = g;

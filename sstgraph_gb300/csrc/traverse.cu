@@ -109,9 +109,9 @@ struct TravState {
   unsigned long long *d_small = nullptr;
 };
 
-void trav_release(sst_graph *g) {
-  TravState *t = g->trav;
-  if (!t) return;
+// frees every buffer and the captured PageRank graph; the tuning stays, and
+// the work lists are rebuilt by the next traversal
+static void trav_buffers_release(TravState *t) {
   t->choff.release();
   t->cv.release();
   t->cl0.release();
@@ -160,10 +160,45 @@ void trav_release(sst_graph *g) {
   t->mil0.release();
   t->mtab.release();
   if (t->pr_exec) cudaGraphExecDestroy(t->pr_exec);
+  t->pr_exec = nullptr;
+  t->version = ~0ull;
+  t->inv_version = ~0ull;
+  t->lists_stamp++;
+}
+
+void trav_trim(sst_graph *g) {
+  if (g->trav) trav_buffers_release(g->trav);
+}
+
+void trav_release(sst_graph *g) {
+  TravState *t = g->trav;
+  if (!t) return;
+  trav_buffers_release(t);
   if (t->h_small) cudaFreeHost(t->h_small);
   if (t->d_small) cudaFree(t->d_small);
   delete t;
   g->trav = nullptr;
+}
+
+uint64_t trav_device_bytes(const sst_graph *g) {
+  const TravState *t = g->trav;
+  if (!t) return 0;
+  uint64_t b = 0;
+  auto add = [&](uint64_t cap, size_t elem) { b += cap * elem; };
+  add(t->choff.cap, 8); add(t->cv.cap, 4); add(t->cl0.cap, 4); add(t->cdesc.cap, 8);
+  add(t->sdesc.cap, 8); add(t->multi.cap, 4); add(t->big.cap, 4); add(t->small.cap, 4);
+  add(t->flag.cap, 4); add(t->pos.cap, 4); add(t->inv_deg.cap, 8); add(t->ca.cap, 8);
+  add(t->cb.cap, 8); add(t->partial.cap, 8); add(t->qa.cap, 4); add(t->qb.cap, 4);
+  add(t->fbits.cap, 4); add(t->icnt.cap, 4); add(t->ioff.cap, 4); add(t->iv.cap, 4);
+  add(t->il0.cap, 4); add(t->depth_tmp.cap, 4); add(t->parent_tmp.cap, 4);
+  add(t->sigma.cap, 8); add(t->ratio.cap, 8); add(t->lvl_list.cap, 4);
+  add(t->lvl_cnt.cap, 4); add(t->par.cap, 4); add(t->toff.cap, 8); add(t->tlpre.cap, 8);
+  add(t->tlcnt.cap, 8); add(t->tadj.cap, 4); add(t->mvis.cap, 8); add(t->mfr.cap, 8);
+  add(t->mfr2.cap, 8); add(t->mnx.cap, 8); add(t->msrc.cap, 8); add(t->mdepth.cap, 4);
+  add(t->msig.cap, 8); add(t->mrat.cap, 8); add(t->mpart.cap, 8); add(t->mlist.cap, 4);
+  add(t->micnt.cap, 4); add(t->mioff.cap, 4); add(t->miv.cap, 4); add(t->mil0.cap, 4);
+  add(t->mtab.cap, 4);
+  return b;
 }
 
 namespace {
@@ -1024,11 +1059,18 @@ __global__ void k_delta_small(DGraph g, const uint32_t *__restrict__ list,
 }
 
 // ------------------------------------------------------------- tc
-// rank order used to orient each undirected edge once: (degree, id)
+// rank order used to orient each undirected edge once: (degree, id).  Each
+// vertex keeps the neighbours that rank above it (N+), so a hub keeps only
+// the few neighbours of even higher degree and the lists stay short; every
+// triangle is counted once, at its lowest-ranked vertex.
 __device__ __forceinline__ bool rank_less(const uint32_t *deg, uint32_t a,
                                           uint32_t b) {
   uint32_t da = deg[a], db = deg[b];
   return da < db || (da == db && a < b);
+}
+__device__ __forceinline__ bool ranks_above(const uint32_t *deg, uint32_t w,
+                                            uint32_t u) {
+  return rank_less(deg, u, w);
 }
 
 __global__ void k_tc_leafcount(const uint32_t *__restrict__ slots,
@@ -1042,7 +1084,7 @@ __global__ void k_tc_leafcount(const uint32_t *__restrict__ slots,
   if (k >= nleaves) return;
   uint32_t u = owner[k];
   bool keep = false;
-  if ((uint32_t)lane < cnt[k]) keep = rank_less(deg, slots[slot[k] + lane], u);
+  if ((uint32_t)lane < cnt[k]) keep = ranks_above(deg, slots[slot[k] + lane], u);
   uint32_t m = __ballot_sync(0xffffffffu, keep);
   if (lane == 0) out[k] = __popc(m);
 }
@@ -1062,7 +1104,7 @@ __global__ void k_tc_fill(const uint32_t *__restrict__ slots,
   bool keep = false;
   if ((uint32_t)lane < cnt[k]) {
     w = slots[slot[k] + lane];
-    keep = rank_less(deg, w, u);
+    keep = ranks_above(deg, w, u);
   }
   uint32_t m = __ballot_sync(0xffffffffu, keep);
   if (keep) adj[lpre[k] + __popc(m & ((1u << lane) - 1u))] = w;
@@ -1088,38 +1130,89 @@ __device__ __forceinline__ bool sorted_has(const uint32_t *a, uint64_t n,
   return lo < n && a[lo] == x;
 }
 
-// warp per vertex u: for v in N+(u) (lane-strided), w in N+(v): w in N+(u)?
-__global__ void k_tc_count(const uint64_t *__restrict__ off,
-                           const uint32_t *__restrict__ adj, uint32_t n,
-                           unsigned long long *__restrict__ total,
-                           unsigned long long *__restrict__ pv) {
-  uint64_t u = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Warp per vertex u (the lowest-ranked vertex of the triangles it counts):
+// N+(u) goes into a hash set in the warp's shared memory (open addressing,
+// at most half full); then for each v in N+(u) in turn the warp's lanes
+// stride over N+(v) (coalesced) and probe the set for each w.  A list too
+// long for the set is probed by binary search in global memory instead.
+constexpr uint32_t kTcHash = 2048;  // set slots per warp (8 KiB)
+constexpr int kTcWarps = 8;         // warps per block
+
+// multiplicative hashing (Knuth): the top `bits` bits of x * 2^32/phi
+__device__ __forceinline__ uint32_t tc_hash(uint32_t x, int bits) {
+  return (x * 0x9E3779B1u) >> (32 - bits);
+}
+
+__global__ void __launch_bounds__(kTcWarps * 32, 3)
+k_tc_count(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
+           uint32_t n, unsigned long long *__restrict__ total,
+           unsigned long long *__restrict__ pv) {
+  extern __shared__ uint32_t tc_sh[];
   const int lane = threadIdx.x & 31;
-  if (u >= n) return;
-  uint64_t a0 = off[u], a1 = off[u + 1];
-  const uint32_t *A = adj + a0;
-  uint64_t na = a1 - a0;
+  uint32_t *tab = tc_sh + (threadIdx.x >> 5) * kTcHash;
+  const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   unsigned long long local = 0;
-  for (uint64_t i = lane; i < na; i += 32) {
-    uint32_t v = A[i];
-    uint64_t b0 = off[v], b1 = off[v + 1];
-    unsigned long long cv = 0;
-    for (uint64_t j = b0; j < b1; j++) {
-      uint32_t w = adj[j];
-      if (sorted_has(A, na, w)) {
-        cv++;
-        if (pv) atomicAdd(&pv[w], 1ull);
+  for (uint64_t u = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n;
+       u += warps) {
+    const uint64_t a0 = off[u];
+    const uint64_t na = off[u + 1] - a0;
+    if (na < 2) continue;  // a triangle needs two neighbours above u
+    const uint32_t *A = adj + a0;
+    const bool hashed = na <= kTcHash / 2;
+    uint32_t mask = 0;
+    int bits = 5;
+    if (hashed) {
+      while ((1ull << bits) < 2 * na) bits++;
+      mask = (1u << bits) - 1;
+      for (uint32_t i = lane; i <= mask; i += 32) tab[i] = kEmpty;
+      __syncwarp();
+      for (uint64_t i = lane; i < na; i += 32) {
+        const uint32_t x = A[i];
+        uint32_t h = tc_hash(x, bits);
+        while (atomicCAS(&tab[h], kEmpty, x) != kEmpty) h = (h + 1) & mask;
       }
+      __syncwarp();
     }
-    if (pv && cv) atomicAdd(&pv[v], cv);
-    local += cv;
+    unsigned long long cu = 0;
+    for (uint64_t i = 0; i < na; i++) {
+      const uint32_t v = A[i];
+      const uint64_t b0 = off[v], b1 = off[v + 1];
+      unsigned long long cv = 0;
+      for (uint64_t j = b0 + lane; j < b1; j += 32) {
+        const uint32_t w = adj[j];
+        bool hit;
+        if (hashed) {
+          uint32_t h = tc_hash(w, bits), x;
+          while ((x = tab[h]) != w && x != kEmpty) h = (h + 1) & mask;
+          hit = x == w;
+        } else {
+          hit = sorted_has(A, na, w);
+        }
+        if (hit) {
+          cv++;
+          if (pv) atomicAdd(&pv[w], 1ull);
+        }
+      }
+      if (pv) {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) cv += __shfl_xor_sync(0xffffffffu, cv, d);
+        if (lane == 0 && cv) atomicAdd(&pv[v], cv);
+        if (lane != 0) cv = 0;  // counted once, by lane 0, below
+      }
+      cu += cv;
+    }
+    if (pv) {
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) cu += __shfl_xor_sync(0xffffffffu, cu, d);
+      if (lane == 0 && cu) atomicAdd(&pv[u], cu);
+      if (lane != 0) cu = 0;
+    }
+    local += cu;
+    __syncwarp();  // the set is rebuilt for the next u
   }
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) local += __shfl_down_sync(0xffffffffu, local, d);
-  if (lane == 0 && local) {
-    atomicAdd(total, local);
-    if (pv) atomicAdd(&pv[u], local);
-  }
+  if (lane == 0 && local) atomicAdd(total, local);
 }
 
 // ------------------------------------------------------------- pairs
@@ -1584,9 +1677,19 @@ sst_status tc(sst_graph *g, uint64_t *total, uint64_t *d_pv) {
              t->tlpre.p, n, t->toff.p);
   SST_CUDA_TRY(cudaMemsetAsync(t->d_small, 0, 8, s));
   if (d_pv) SST_CUDA_TRY(cudaMemsetAsync(d_pv, 0, (uint64_t)n * 8, s));
-  if (n)
-    SST_LAUNCH(k_tc_count, warp_blocks(n), kTB, 0, s, t->toff.p, t->tadj.p, n,
+  if (n) {
+    const size_t shm = (size_t)kTcWarps * kTcHash * 4;
+    SST_CUDA_TRY(cudaFuncSetAttribute(k_tc_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)shm));
+    int per_sm = 0;
+    SST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc_count,
+                                                               kTcWarps * 32, shm));
+    const uint64_t want = ((uint64_t)n + kTcWarps - 1) / kTcWarps;
+    const unsigned grid = (unsigned)std::min<uint64_t>(
+        want, (uint64_t)std::max(per_sm, 1) * g->sms * 8);
+    SST_LAUNCH(k_tc_count, grid, kTcWarps * 32, shm, s, t->toff.p, t->tadj.p, n,
                t->d_small, reinterpret_cast<unsigned long long *>(d_pv));
+  }
   SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, t->d_small, 8, cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   SST_CUDA_TRY(cudaGetLastError());

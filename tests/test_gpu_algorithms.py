@@ -77,3 +77,31 @@ def test_tc(sg, pair):
     te, pve = o.tc(per_vertex=True)
     assert t == te
     assert np.array_equal(pv, pve)
+
+
+def test_traversals_refuse_non_square_graph(sg):
+    """A graph with more columns than rows would send column ids past the
+    traversals' per-vertex arrays: every traversal refuses it on the host,
+    before any launch, with SST_EINVAL."""
+    g = sg.SparseMatrixV(8, 1 << 20)
+    g.insert_batch(np.array([[1, (1 << 20) - 1], [2, 3]], dtype=np.uint32))
+    calls = [
+        ("BFS", lambda: sg.BFS(g, 1, depths=True)),
+        ("PR_S", lambda: sg.PR_S(g, 5)),
+        ("CC", lambda: sg.CC(g)),
+        ("BC", lambda: sg.BC(g, 1)),
+        ("TC", lambda: sg.TC(g, per_vertex=True)),
+        ("BFS_multi", lambda: sg.BFS_multi(g, [1, 2])),
+        ("BC_multi", lambda: sg.BC_multi(g, [1, 2])),
+        ("TC_vertices", lambda: sg.TC_vertices(g, [1, 2])),
+        ("autotune", lambda: sg.autotune(g)),
+        ("CompactGraph.pagerank", lambda: sg.CompactGraph(g).pagerank(5)),
+        ("Server", lambda: sg.Server(g)),
+    ]
+    for name, call in calls:
+        with pytest.raises(sg.SSTError) as e:
+            call()
+        assert e.value.status == -1, name
+        assert "rows as columns" in str(e.value), name
+    # the graph itself is still usable
+    assert g.has(1, (1 << 20) - 1) and g.M() == 2

@@ -130,3 +130,34 @@ def test_under_the_profiler(sg):
         prof = sg.profile_collect()
     assert prof["update_plan_graph"]["launches"] == 4  # the replaying graph's
     assert "k_make_keys_packed" in prof
+
+
+def test_direct_launch_of_replay_forms(sg):
+    """Mode 2 launches the kernels a replay runs one by one (same size
+    classes, two-launch scans): same graph as the replayed form and the
+    oracle, and the profiler sees the two-launch scans, not the
+    single-pass look-back form."""
+    n = 1 << 14
+    rng = np.random.default_rng(9)
+    a = sg.SparseMatrixV(n)
+    d = sg.SparseMatrixV(n)
+    d.set_plan_graphs(2)
+    o = oracle.OracleGraph(n)
+    seen = set()
+    for op, e in batches(rng, n, [1000, 30000, 200000, 1 << 20, 5000, 4096], o):
+        getattr(a, op + "_batch")(e)
+        getattr(o, op + "_batch")(e)
+        sg.profile_start()
+        getattr(d, op + "_batch")(e)
+        d.sync()
+        seen |= set(sg.profile_collect())
+        assert equal(a, d)
+        assert equal(a, o)
+    # a planning scan of 200000 keys (49 tiles) takes the two-launch form
+    # (range reduction, then ranges) as in a replay; launched directly
+    # outside mode 2 it would be the single-pass look-back
+    assert any("k_scan_reduce" in k for k in seen), sorted(seen)
+    assert any("k_scatter" in k for k in seen), sorted(seen)
+    assert "update_plan_graph" not in seen
+    a.close()
+    d.close()

@@ -202,3 +202,70 @@ def test_pinned_host_inputs(sg):
     assert np.array_equal(found, ok) and np.array_equal(vals[ok], exp[ok])
     g.close()
     w.close()
+
+
+@pytest.mark.parametrize("polls", [0, 1])
+def test_scan_lookback_fallback(sg, polls):
+    """The single-pass scans' bounded wait: with a poll limit of 0 every
+    tile after the first stops waiting at once and reduces its
+    predecessors' inputs itself (1: after one look at the flag).  Update
+    batches launched directly (so their scans take the single-pass form)
+    must still match the oracle, after inserts and removes."""
+    n = 1 << 16
+    base = oracle.symmetrize(oracle.rmat(16, 8 * n, seed=11))
+    g = sg.SparseMatrixV(n)
+    g.set_plan_graphs(False)
+    o = oracle.OracleGraph(n)
+    g.insert_batch(base)
+    o.insert_batch(base)
+    old = sg.set_scan_lookback_polls(polls)
+    try:
+        sg.profile_start("k_scan_lb")
+        for i, b in enumerate((30000, 200000, 1000000)):
+            e = oracle.rmat(16, b, seed=100 + i)
+            g.insert_batch(e)
+            o.insert_batch(e)
+            same(g, o, structure=False)
+            r = o.sample_edges(b // 2, seed=200 + i)
+            g.remove_batch(r)
+            o.remove_batch(r)
+            same(g, o, structure=False)
+        prof = sg.profile_collect()
+    finally:
+        sg.set_scan_lookback_polls(old)
+    assert sum(v["launches"] for k, v in prof.items() if "k_scan_lb" in k) > 0, prof
+    assert sg.set_scan_lookback_polls(old) == old
+
+
+def test_release_scratch_after_bulk_load(sg):
+    """A large batch grows the update scratch; sst_release_scratch gives it
+    back (the memory size falls to about the storage), and the graph keeps
+    working: updates, traversals and tuning after the release match the
+    oracle."""
+    n = 1 << 16
+    base = oracle.symmetrize(oracle.rmat(16, 16 * n, seed=21))
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    g.insert_batch(base)
+    o.insert_batch(base)
+    sg.set_tuning(g, chunk_leaves=16, pr_lanes=4, bfs_alpha=10)
+    sg.PR_S(g, 3)
+    grown = g.get_memory_size()
+    g.release_scratch()
+    trimmed = g.get_memory_size()
+    # the 2M-pair load's scratch is hundreds of bytes a pair, the storage
+    # about 6 bytes an edge
+    assert 4 * trimmed < grown, (trimmed, grown)
+    assert sg.get_tuning(g)["chunk_leaves"] == 16
+    # symmetric updates keep the graph a valid traversal input
+    e = oracle.symmetrize(oracle.rmat(16, 50000, seed=22))
+    g.insert_batch(e)
+    o.insert_batch(e)
+    same(g, o, structure=False)
+    g.release_scratch()
+    r = oracle.symmetrize(o.sample_edges(20000, seed=23))
+    g.remove_batch(r)
+    o.remove_batch(r)
+    same(g, o, structure=False)
+    g.release_scratch()
+    assert np.array_equal(sg.CC(g), o.cc())
