@@ -57,7 +57,9 @@ def args_parse():
     ap.add_argument("--pr-iters", type=int, default=10)
     ap.add_argument("--batched-batches", type=int, default=512)
     ap.add_argument("--serve-requests", type=int, default=400)
-    ap.add_argument("--serve-rate", type=float, default=300.0)
+    # offered load of the serving latency run (requests/s): below the
+    # measured capacity at scale 25, so the latencies are not queueing alone
+    ap.add_argument("--serve-rate", type=float, default=150.0)
     ap.add_argument("--serve-scale", type=int, default=25)
     ap.add_argument("--only", default="all",
                     choices=["all", "updates", "pagerank", "bfs", "batched", "serving",
@@ -572,17 +574,13 @@ def main():
                     s1.synchronize()
                     best = min(best, s0.elapsed_time(s1) / 1e3)
                 gpu[alg] = best
-            sg.profile_start("k_cc_hook")
-            sg.CC(gg, out=lab)
-            torch.cuda.synchronize()
-            cc_rounds = sum(v["launches"] for v in sg.profile_collect().values())
             d_dep = dep.cpu().numpy()
             m_r = int(deg[d_dep >= 0].sum())
             byts = {"bfs": 4 * m_r + 12 * nn, "pagerank20": 20 * (4 * m + 24 * nn),
-                    "cc": cc_rounds * (4 * m + 8 * nn), "bc": 8 * m_r + 28 * nn,
+                    "cc": 4 * m + 8 * nn, "bc": 8 * m_r + 28 * nn,
                     "tc": tc_bytes}
             res = {"vertices": nn, "edges": m, "tuning": tuning, "bfs_edges_reached": m_r,
-                   "cc_rounds": cc_rounds, "triangles": tcv["t"], "algorithms": {}}
+                   "triangles": tcv["t"], "algorithms": {}}
             # the oracle port on the same graph, all host threads
             pairs = oracle.symmetrize(cpu_gen())
             t0 = time.perf_counter()
@@ -626,7 +624,8 @@ def main():
             del o
             gg.close()
         out["bytes"] = {"bfs": "4 m_r + 12 n", "pagerank20": "20 (4 m + 24 n)",
-                        "cc": "rounds (4 m + 8 n)", "bc": "8 m_r + 28 n",
+                        "cc": "4 m + 8 n (one pass over the edges and labels)",
+                        "bc": "8 m_r + 28 n",
                         "tc": "sum over (u, v), v < u of 4 (d<(u) + d<(v)) + 4 m"}
         return out
 
@@ -926,7 +925,9 @@ def main():
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
     pr_flush = flush
 
-    def run_steps(lo, hi, ins, rem):
+    per_size = {}  # batch size -> [insert s, remove s, steps] of timed steps
+
+    def run_steps(lo, hi, ins, rem, sizes=None):
         ti = tr = 0.0
         edges = 0
         for i in range(lo, hi):
@@ -939,9 +940,15 @@ def main():
             g.remove_batch(rem[i])
             e2.record(stream)
             e2.synchronize()
-            ti += e0.elapsed_time(e1) / 1e3
-            tr += e1.elapsed_time(e2) / 1e3
+            a_, b_ = e0.elapsed_time(e1) / 1e3, e1.elapsed_time(e2) / 1e3
+            ti += a_
+            tr += b_
             edges += plan[i]
+            if sizes is not None:
+                ps = sizes.setdefault(plan[i], [0.0, 0.0, 0])
+                ps[0] += a_
+                ps[1] += b_
+                ps[2] += 1
         return ti, tr, edges
 
     # ---- warmup + timed (device-resident batches).  Batches up to 2^20
@@ -955,7 +962,7 @@ def main():
     torch.cuda.synchronize()
     l0 = sg.kernel_launches()
     with Clocks(dev) as clk:
-        ti, tr, edges = run_steps(a.warmup, a.warmup + a.steps, ins_d, rem_d)
+        ti, tr, edges = run_steps(a.warmup, a.warmup + a.steps, ins_d, rem_d, per_size)
     torch.cuda.synchronize()
     launches = sg.kernel_launches() - l0
     barrier(world)
@@ -1080,6 +1087,8 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks,
         "remove_edges_per_s": world * edges / tr,
+        "per_batch_size": {str(b): {"insert_us": 1e6 * v[0] / v[2], "remove_us": 1e6 * v[1] / v[2],
+                                    "steps": v[2]} for b, v in sorted(per_size.items())},
         "base_graph": {"edges": m0, "build_s": round(build_s, 2)},
         "batched_form": batched,
         "pagerank": pagerank,

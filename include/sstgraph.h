@@ -254,7 +254,7 @@ SST_API sst_status sst_bc_multi(sst_graph *g, const uint32_t *srcs, uint32_t k,
                                 double *out, uint32_t flags);
 /* Traversal tuning (no reference counterpart).  sst_autotune times the
  * knobs on this graph and keeps the fastest: PageRank over chunk_leaves
- * {8,16,32} x pr_lanes {4,8,16}, then pr_hot {0,2048,4096,8192}, then BFS
+ * {8,16,32} x pr_lanes {4,8,16}, then pr_hot {0,2048,4096,8192,16384,24576}, then BFS
  * over bfs_alpha {5,10,20,40,80};
  * pr_ms / bfs_ms report the winners' times (3 PageRank iterations; one BFS).
  * The leaf itself stays 32 slots (one 128-byte line): it is the storage

@@ -1113,6 +1113,8 @@ sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
   SST_CUDA_TRY(cudaMalloc(&g->d_plan, sizeof(PlanSummary)));
   SST_CUDA_TRY(cudaMalloc(&g->d_err, sizeof(unsigned long long)));
   SST_CUDA_TRY(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned long long), g->stream));
+  SST_CUDA_TRY(cudaMalloc(&g->d_scan_epoch, sizeof(unsigned long long)));
+  SST_CUDA_TRY(cudaMemsetAsync(g->d_scan_epoch, 0, sizeof(unsigned long long), g->stream));
   SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
   return SST_OK;
 }
@@ -1128,6 +1130,7 @@ void graph_release(sst_graph *g) {
   cudaFree(g->d_lcnt);
   cudaFree(g->d_plan);
   cudaFree(g->d_err);
+  cudaFree(g->d_scan_epoch);
   if (g->h_plan) cudaFreeHost(g->h_plan);
   if (g->h_pinned) cudaFreeHost(g->h_pinned);
   g->arena.release();
@@ -1498,6 +1501,9 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   // fixed sequence of launches over device-resident counts; `fork` starts
   // the merges after k_emit (a captured sequence starts them after its end).
   auto plan = [&](cudaStream_t s, bool fork) -> sst_status {
+    // a replayed sequence tags its single-pass scans from the device
+    DeviceScanTags tags(replay ? g->d_scan_epoch : nullptr);
+    if (replay) SST_CUDA_TRY(tags.bump(s));
     if (!presorted) {
       uint64_t *out = keys;
       if (wt) {

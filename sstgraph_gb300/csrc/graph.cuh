@@ -84,6 +84,7 @@ struct sst_graph {
   sst::PlanSummary *h_plan = nullptr;  // pinned
   sst::PlanSummary *d_plan = nullptr;
   unsigned long long *d_err = nullptr;  // staging-rank check, read lazily
+  unsigned long long *d_scan_epoch = nullptr;  // tags of captured scans
   sst::LeafDir dir;
   sst::TravState *trav = nullptr;  // traversal work lists and buffers
   void *h_pinned = nullptr;  // pinned staging for host-pointer calls

@@ -33,6 +33,21 @@ unsigned long long next_scan_tag() {
 }
 
 thread_local bool t_capture_forms = false;
+thread_local DeviceScanTags *t_scan_tags = nullptr;
+
+namespace {
+__global__ void k_scan_epoch_bump(unsigned long long *epoch) { *epoch += 1; }
+}  // namespace
+
+DeviceScanTags::DeviceScanTags(unsigned long long *e) : epoch(e), prev(t_scan_tags) {
+  t_scan_tags = this;  // with a null epoch: host tags, as without one
+}
+DeviceScanTags::~DeviceScanTags() { t_scan_tags = prev; }
+cudaError_t DeviceScanTags::bump(cudaStream_t s) {
+  next = 0;
+  SST_LAUNCH(k_scan_epoch_bump, 1, 1, 0, s, epoch);
+  return cudaGetLastError();
+}
 
 static std::atomic<int> g_lookback_polls{kLookbackPolls};
 int lookback_polls() { return g_lookback_polls.load(std::memory_order_relaxed); }
@@ -395,6 +410,149 @@ k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
   }
 }
 
+// ---- one-sweep passes (after Adinets and Merrill, "Onesweep", 2022).
+// k_hist_all reads the keys once and counts every pass's digits (global
+// totals, no per-tile tables) and clears the passes' tile status words.
+// Each pass is then one launch: a block ranks its tile as k_scatter does,
+// publishes its per-digit count, and thread d finds the count of digit d in
+// all tiles before its own by looking back over their status words (an
+// inclusive prefix ends the walk, an aggregate is added and the walk goes
+// on).  A status word is (state << 30) | count, state 1 = this tile's
+// count, 2 = the count of this and every earlier tile; 0 = not yet
+// published.  Every wait is bounded: a tile that has not published in time
+// is counted from its keys instead, and the walk goes on.
+constexpr uint32_t kOsAgg = 1u << 30, kOsIncl = 2u << 30, kOsMask = kOsAgg - 1;
+constexpr int kOsPolls = 1 << 14;
+
+template <int IT>
+__global__ void __launch_bounds__(kThreads)
+k_hist_all(const uint64_t *__restrict__ keys, uint64_t n, int passes,
+           uint32_t *__restrict__ totals, uint32_t *__restrict__ status,
+           uint64_t status_words, const uint32_t *__restrict__ d_n) {
+  if (d_n && *d_n < n) n = *d_n;
+  __shared__ uint32_t h[8][kRadix];
+  for (int p = 0; p < passes; p++) h[p][threadIdx.x] = 0;
+  __syncthreads();
+  const uint64_t t0 = (uint64_t)blockIdx.x * (kThreads * IT);
+#pragma unroll 4
+  for (int it = 0; it < IT; it++) {
+    const uint64_t i = t0 + (uint64_t)it * kThreads + threadIdx.x;
+    if (i < n) {
+      const uint64_t k = keys[i];
+      for (int p = 0; p < passes; p++) atomicAdd(&h[p][(k >> (8 * p)) & 0xff], 1u);
+    }
+  }
+  __syncthreads();
+  for (int p = 0; p < passes; p++)
+    if (h[p][threadIdx.x]) atomicAdd(&totals[p * kRadix + threadIdx.x], h[p][threadIdx.x]);
+  for (uint64_t i = (uint64_t)blockIdx.x * kThreads + threadIdx.x; i < status_words;
+       i += (uint64_t)gridDim.x * kThreads)
+    status[i] = 0;
+}
+
+// count of digit d among the keys of tile t (the bounded wait's fallback)
+__device__ __forceinline__ uint32_t os_count_tile(const uint64_t *in, uint64_t n,
+                                                  uint64_t t, int tile, int shift,
+                                                  uint32_t d) {
+  uint32_t c = 0;
+  const uint64_t a = t * (uint64_t)tile;
+  const uint64_t e = a + tile < n ? a + tile : n;
+  for (uint64_t i = a; i < e; i++) c += ((uint32_t)(in[i] >> shift) & 0xff) == d;
+  return c;
+}
+
+template <bool KV, int IT>
+__global__ void __launch_bounds__(kThreads, 2)
+k_scatter_os(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
+             uint64_t n, int shift, const uint32_t *__restrict__ totals,
+             uint32_t *__restrict__ status, const uint32_t *__restrict__ vin,
+             uint32_t *__restrict__ vout, const uint32_t *__restrict__ d_n) {
+  constexpr int TILE = kThreads * IT;
+  if (d_n && *d_n < n) n = *d_n;
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t *skeys = reinterpret_cast<uint64_t *>(smem);
+  uint32_t *svals = reinterpret_cast<uint32_t *>(smem + (size_t)TILE * 8);
+  uint32_t(*wcnt)[kRadix] = reinterpret_cast<uint32_t(*)[kRadix]>(
+      smem + scatter_stage_bytes<KV, IT>());
+  uint32_t *adj = &wcnt[kWarps - 1][kRadix - 1] + 1;  // [kRadix]
+  uint32_t *wsum = adj + kRadix;                        // [kWarps]
+  const int warp = threadIdx.x >> 5;
+  const uint32_t d = threadIdx.x;  // this thread's digit in the bookkeeping
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) wcnt[w][d] = 0;
+  const uint64_t tile = blockIdx.x;
+  const uint64_t t0 = tile * TILE;
+  uint64_t kk[IT];
+  uint32_t vv[KV ? IT : 1];
+  uint32_t dg[IT];
+#pragma unroll
+  for (int it = 0; it < IT; it++) {
+    const uint64_t i = t0 + tile_offset<IT>(it);
+    kk[it] = i < n ? in[i] : 0;
+    if (KV) vv[it] = i < n ? vin[i] : 0u;
+    dg[it] = i < n ? (uint32_t)(kk[it] >> shift) & 0xff : kNoDigit;
+  }
+  __syncthreads();
+  uint32_t lr[IT];
+  warp_rank<IT>(dg, lr, wcnt[warp]);
+  __syncthreads();
+  uint32_t tcount = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) tcount += wcnt[w][d];
+  // publish this tile's count of digit d, then find the earlier tiles'
+  uint32_t *mine = status + tile * kRadix + d;
+  uint32_t before = 0;
+  if (tile == 0) {
+    atomicExch(mine, kOsIncl | tcount);
+  } else {
+    atomicExch(mine, kOsAgg | tcount);
+    for (int64_t t = (int64_t)tile - 1; t >= 0; t--) {
+      const volatile uint32_t *sp = status + (uint64_t)t * kRadix + d;
+      uint32_t v = *sp;
+      for (int p = 0; (v & ~kOsMask) == 0 && p < kOsPolls; p++) {
+        __nanosleep(p < 32 ? 20 : 200);
+        v = *sp;
+      }
+      if ((v & ~kOsMask) == 0) {  // never published: count its keys
+        before += os_count_tile(in, n, (uint64_t)t, TILE, shift, d);
+        continue;
+      }
+      before += v & kOsMask;
+      if ((v & ~kOsMask) == kOsIncl) break;
+    }
+    atomicExch(mine, kOsIncl | (before + tcount));
+  }
+  // global start of digit d: all keys of smaller digits, then the earlier
+  // tiles' keys of digit d
+  const uint32_t gbase = block_excl_scan(totals[d], wsum) + before;
+  __syncthreads();  // wsum is read by every thread before it is reused
+  const uint32_t tstart = block_excl_scan(tcount, wsum);
+  uint32_t sacc = tstart;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) {
+    const uint32_t c = wcnt[w][d];
+    wcnt[w][d] = sacc;
+    sacc += c;
+  }
+  adj[d] = gbase - tstart;
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < IT; it++) {
+    if (dg[it] == kNoDigit) continue;
+    const uint32_t lp = wcnt[warp][dg[it]] + lr[it];
+    skeys[lp] = kk[it];
+    if (KV) svals[lp] = vv[it];
+  }
+  __syncthreads();
+  const uint32_t tn = t0 >= n ? 0u : (uint32_t)(n - t0 < (uint64_t)TILE ? n - t0 : TILE);
+  for (uint32_t j = threadIdx.x; j < tn; j += kThreads) {
+    const uint64_t key = skeys[j];
+    const uint32_t pos = adj[(key >> shift) & 0xff] + j;
+    out[pos] = key;
+    if (KV) vout[pos] = svals[j];
+  }
+}
+
 // The key-value scatter's shared memory is above the 48 KB default: raise
 // its limit once per device (before the first launch there).
 cudaError_t scatter_smem_optin() {
@@ -405,6 +563,10 @@ cudaError_t scatter_smem_optin() {
   if (dev < 64 && ((done.load(std::memory_order_relaxed) >> dev) & 1)) return cudaSuccess;
   e = cudaFuncSetAttribute(k_scatter<true, kItems>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)scatter_smem_bytes<true, kItems>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_scatter_os<true, kItems>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)scatter_smem_bytes<true, kItems>());
   if (e == cudaSuccess && dev < 64) done.fetch_or(1ull << dev, std::memory_order_relaxed);
   return e;
 }
@@ -477,7 +639,11 @@ size_t radix_sort_scratch_bytes(uint64_t n) {
   const uint64_t tile = n <= kSmallTileKeys ? (uint64_t)kThreads * kSmallItems : kTile;
   uint64_t nblocks = (n + tile - 1) / tile;
   uint64_t hn = nblocks * kRadix;
-  return 3 * ((hn * 4 + 255) & ~size_t(255)) + scan_scratch_bytes(hn, 4) + 512;
+  // the one-sweep form: digit totals and up to eight passes' tile status;
+  // the counting forms: three count tables or counts and their scan
+  const size_t os = 8 * kRadix * 4 + 8 * ((hn * 4 + 255) & ~size_t(255)) + 512;
+  const size_t cnt = 3 * ((hn * 4 + 255) & ~size_t(255)) + scan_scratch_bytes(hn, 4) + 512;
+  return os > cnt ? os : cnt;
 }
 
 // profiler name of a scatter pass, by its tile size
@@ -487,6 +653,14 @@ constexpr const char *scatter_name() {
     return KV ? "(k_scatter<true, 4>)" : "(k_scatter<false, 4>)";
   else
     return KV ? "(k_scatter<true, 16>)" : "(k_scatter<false, 16>)";
+}
+
+template <bool KV, int IT>
+constexpr const char *scatter_os_name() {
+  if constexpr (IT == kSmallItems)
+    return KV ? "(k_scatter_os<true, 4>)" : "(k_scatter_os<false, 4>)";
+  else
+    return KV ? "(k_scatter_os<true, 16>)" : "(k_scatter_os<false, 16>)";
 }
 
 // The multi-tile sort with tiles of IT items per thread (see radix_sort_impl).
@@ -507,7 +681,31 @@ static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *val
   // every scatter reads and writes keys (and values) and reads the counts
   const uint64_t hist_bytes = 8 * n + 4 * hn;
   const uint64_t scatter_bytes = (vals ? 24 : 16) * n + 8 * hn;
-  if (nblocks <= kFuseHistBlocks) {
+  const int passes = (bits + 7) / 8;
+  if (n < (1ull << 30) && passes <= 8) {
+    // one sweep: all passes' digit totals in one read, then one launch a
+    // pass whose tiles find their offsets by looking back
+    uint32_t *totals = arena.take<uint32_t>(8 * kRadix);
+    uint32_t *status = arena.take<uint32_t>((uint64_t)passes * hn);
+    if (!totals || !status) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMemsetAsync(totals, 0, (size_t)passes * kRadix * 4, s);
+    if (e != cudaSuccess) return e;
+    SST_LAUNCH_NB("(k_hist_all)", 8 * n, k_hist_all<IT>, nblocks, kThreads, 0, s, src, n,
+                  passes, totals, status, (uint64_t)passes * hn, d_n);
+    for (int p = 0; p < passes; p++) {
+      const uint64_t sb = (vals ? 24 : 16) * n + 8 * (uint64_t)kRadix * nblocks;
+      if (vals)
+        SST_LAUNCH_NB((scatter_os_name<true, IT>()), sb, (k_scatter_os<true, IT>), nblocks,
+                      kThreads, (scatter_smem_bytes<true, IT>()), s, src, dst, n, 8 * p,
+                      totals + p * kRadix, status + (uint64_t)p * hn, vsrc, vdst, d_n);
+      else
+        SST_LAUNCH_NB((scatter_os_name<false, IT>()), sb, (k_scatter_os<false, IT>), nblocks,
+                      kThreads, (scatter_smem_bytes<false, IT>()), s, src, dst, n, 8 * p,
+                      totals + p * kRadix, status + (uint64_t)p * hn, vsrc, vdst, d_n);
+      std::swap(src, dst);
+      std::swap(vsrc, vdst);
+    }
+  } else if (nblocks <= kFuseHistBlocks) {
     // three tile-major count tables in rotation: pass p reads table p % 3,
     // counts into (p + 1) % 3 and clears (p + 2) % 3
     uint32_t *h[3];

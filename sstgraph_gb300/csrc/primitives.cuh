@@ -313,6 +313,8 @@ struct ScanStatus {
   T incl;
 };
 constexpr unsigned long long kScanTag = 0x5CA5ull << 48;
+// scans a captured sequence may tag per device epoch (DeviceScanTags)
+constexpr uint32_t kScanTagsPerEpoch = 64;
 constexpr unsigned long long kScanEpochMask = (1ull << 46) - 1;
 // polls of one predecessor's flag (with a growing sleep) before a tile stops
 // waiting and reduces the inputs of the tiles it still lacks itself
@@ -418,7 +420,11 @@ __global__ void __launch_bounds__(kScanThreads)
 k_scan_lb(const T *__restrict__ in, Epi out, uint64_t n,
           T identity, Op op, bool reverse, bool exclusive,
           T *__restrict__ total_out, const uint32_t *__restrict__ d_n,
-          ScanStatus<T> *st, unsigned long long tag, int polls) {
+          ScanStatus<T> *st, unsigned long long tag, int polls,
+          const unsigned long long *__restrict__ d_epoch) {
+  if (d_epoch)  // the epoch is written before this launch, in stream order
+    tag = kScanTag |
+          (((*d_epoch * kScanTagsPerEpoch + (tag & 0xFF)) & kScanEpochMask) << 2);
   if (d_n && *d_n < n) n = *d_n;
   const uint64_t tile = blockIdx.x, base = tile * kScanTile;
   if (base >= n) {
@@ -465,6 +471,24 @@ struct CaptureForms {
   ~CaptureForms() { t_capture_forms = prev; }
 };
 
+// Device-side scan tags, for single-pass scans that are captured into a
+// CUDA graph (a tag fixed at capture would repeat in every replay).  While
+// a DeviceScanTags is alive on a thread, the single-pass scans launched
+// from it take their tag from a device epoch word instead of the host:
+// bump() launches a one-thread kernel that advances the epoch (once per
+// launched or replayed sequence, before its first scan), and the k-th scan
+// after it tags its status words with (epoch * 64 + k), so no two scans of
+// any two replays share a tag.
+struct DeviceScanTags {
+  unsigned long long *epoch = nullptr;  // device word
+  uint32_t next = 0;                    // scans issued since bump()
+  DeviceScanTags *prev = nullptr;
+  explicit DeviceScanTags(unsigned long long *e);
+  ~DeviceScanTags();
+  cudaError_t bump(cudaStream_t s);
+};
+extern thread_local DeviceScanTags *t_scan_tags;
+
 inline bool stream_capturing(cudaStream_t s) {
   if (t_capture_forms) return true;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -501,15 +525,19 @@ cudaError_t scan_epi(const T *in, uint64_t n, T identity, Op op, bool exclusive,
   // replay would reuse the launch's tag) or longer than kScanLookbackTiles
   // (past 256 tiles a look-back takes several rounds, and past about 1024
   // the two-launch form is faster)
-  if (!in_place && tiles <= kScanLookbackTiles && !stream_capturing(s)) {
+  DeviceScanTags *dt = t_scan_tags;
+  const bool dev_tags = dt && dt->epoch && dt->next < kScanTagsPerEpoch;
+  if (!in_place && tiles <= kScanLookbackTiles && (dev_tags || !stream_capturing(s))) {
     ScanStatus<T> *st = arena.take<ScanStatus<T>>(tiles);
     if (st) {
       // a scan whose element count is on the device (d_n) is profiled
       // apart, with no declared bytes: its launch size overstates its work
+      const unsigned long long tag = dev_tags ? (unsigned long long)dt->next++ : next_scan_tag();
       SST_LAUNCH_NB(d_n ? "(k_scan_lb<T, Op, Epi>, device count)" : "(k_scan_lb<T, Op, Epi>)",
                     d_n ? 0 : 2 * sizeof(T) * n, (k_scan_lb<T, Op, Epi>), (unsigned)tiles,
                     kScanThreads, 0, s, in, epi, n, identity, op, reverse,
-                    exclusive, total_out, d_n, st, next_scan_tag(), lookback_polls());
+                    exclusive, total_out, d_n, st, tag, lookback_polls(),
+                    dev_tags ? (const unsigned long long *)dt->epoch : nullptr);
       return cudaGetLastError();
     }
   }

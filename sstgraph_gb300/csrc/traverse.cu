@@ -412,9 +412,14 @@ __device__ __forceinline__ unsigned long long gather(const unsigned long long *s
 }
 
 constexpr int kHotThreads = 512;  // 4 blocks of 16 warps per SM
+// a cache above kHotBig entries leaves room for one block per SM: that block
+// takes 1024 threads
+constexpr uint32_t kHotBig = 8192;
 
-template <int G>
-__global__ void __launch_bounds__(kHotThreads, 4) k_pr_small_hot(DGraph g, const unsigned long long *__restrict__ sdesc,
+// launch bounds: 512-thread blocks at least two to an SM (64 registers a
+// thread), 1024-thread blocks (large caches) one to an SM
+template <int G, int T = kHotThreads>
+__global__ void __launch_bounds__(T, T == 1024 ? 1 : 2) k_pr_small_hot(DGraph g, const unsigned long long *__restrict__ sdesc,
                                const uint32_t *__restrict__ small, uint64_t nsmall,
                                const unsigned long long *__restrict__ cin,
                                unsigned long long *__restrict__ cout,
@@ -466,7 +471,8 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pr_small_hot(DGraph g, const
   }
 }
 
-__global__ void __launch_bounds__(kHotThreads, 4) k_pr_chunks_hot(DGraph g, const unsigned long long *__restrict__ cdesc,
+template <int T = kHotThreads>
+__global__ void __launch_bounds__(T, T == 1024 ? 1 : 2) k_pr_chunks_hot(DGraph g, const unsigned long long *__restrict__ cdesc,
                                 const uint32_t *__restrict__ cv, uint64_t nchunks,
                                 const unsigned long long *__restrict__ cin,
                                 unsigned long long *__restrict__ cout,
@@ -848,30 +854,120 @@ __global__ void k_iota(uint32_t *__restrict__ p, uint32_t n) {
   if (v < n) p[v] = v;
 }
 
-// warp per leaf: hook the two roots of every edge (w < u) smaller-to-larger
-__global__ void k_cc_hook(const uint32_t *__restrict__ slots,
-                          const uint32_t *__restrict__ owner,
-                          const uint64_t *__restrict__ slot,
-                          const uint32_t *__restrict__ cnt, uint64_t nleaves,
-                          uint32_t *__restrict__ par,
-                          unsigned long long *__restrict__ changed) {
-  uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (k >= nleaves) return;
-  uint32_t u = owner[k];
-  bool ch = false;
-  if ((uint32_t)lane < cnt[k]) {
-    uint32_t w = slots[slot[k] + lane];
-    if (w < u) {
-      uint32_t ru = cc_root(par, u), rw = cc_root(par, w);
-      if (ru != rw) {
-        uint32_t hi = max(ru, rw), lo = min(ru, rw);
-        atomicMin(&par[hi], lo);
-        ch = true;
-      }
+// Connected components after Afforest (Sutton, Ben-Nun, Barak 2018):
+//  1. link every vertex to its first two neighbours (two rounds, each
+//     followed by compression);
+//  2. sample 1024 vertices' roots and take the most frequent one, c: the
+//     largest component so far;
+//  3. link every edge of every vertex whose root is not c (on a symmetric
+//     graph an edge with one end in c is linked from its other end), then
+//     compress.
+// A root is only ever linked below a smaller root (compare-and-swap on the
+// larger one), so every component's final root -- its label -- is its
+// smallest vertex id, independent of the order the links happen in.
+__device__ __forceinline__ uint32_t ld_par(const uint32_t *par, uint32_t x) {
+  return __ldcg(par + x);
+}
+
+// link the trees of u and v; err counts links that gave up (they cannot
+// fail to progress; the bound only keeps every loop finite)
+__device__ __forceinline__ void cc_link(uint32_t *par, uint32_t u, uint32_t v,
+                                        unsigned long long *err) {
+  uint32_t p1 = ld_par(par, u), p2 = ld_par(par, v);
+  for (int it = 0; p1 != p2; it++) {
+    if (it == (1 << 20)) {
+      atomicAdd(err, 1ull);
+      return;
     }
+    const uint32_t hi = max(p1, p2), lo = min(p1, p2);
+    const uint32_t ph = ld_par(par, hi);
+    if (ph == lo) return;
+    if (ph == hi && atomicCAS(&par[hi], hi, lo) == hi) return;
+    p1 = ld_par(par, ld_par(par, hi));
+    p2 = ld_par(par, lo);
   }
-  if (__any_sync(0xffffffffu, ch) && lane == 0) atomicAdd(changed, 1ull);
+}
+
+// round r of the sampling: u links to its r-th neighbour in its first leaf
+__global__ void k_cc_sample(DGraph g, uint32_t r, uint32_t *__restrict__ par,
+                            unsigned long long *__restrict__ err) {
+  const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= g.n) return;
+  const uint32_t cap = g.cap[u];
+  if (!cap) return;
+  const uint64_t base = g.base[u];
+  const uint32_t c0 = leaf_count(g, base, cap, g.deg[u], 0);
+  if (r < c0) cc_link(par, u, g.slots[base + r], err);
+}
+
+// the most frequent root among 1024 sampled vertices (ties: the smaller)
+__global__ void __launch_bounds__(1024) k_cc_giant(const uint32_t *__restrict__ par,
+                                                   uint32_t n,
+                                                   unsigned long long *__restrict__ out) {
+  __shared__ uint32_t lab[1024];
+  __shared__ unsigned long long best;
+  const uint32_t t = threadIdx.x;
+  const uint32_t v = (uint32_t)(mix64(0x5EEDull + t) % n);
+  lab[t] = par[v];
+  if (t == 0) best = 0;
+  __syncthreads();
+  for (uint32_t k = 2; k <= 1024; k <<= 1)  // bitonic sort, ascending
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      const uint32_t o = t ^ j;
+      if (o > t) {
+        const uint32_t a = lab[t], b = lab[o];
+        const bool up = (t & k) == 0;
+        if ((a > b) == up) {
+          lab[t] = b;
+          lab[o] = a;
+        }
+      }
+      __syncthreads();
+    }
+  if (t == 0 || lab[t] != lab[t - 1]) {
+    uint32_t e = t + 1;
+    while (e < 1024 && lab[e] == lab[t]) e++;
+    // larger count first, then the smaller label
+    atomicMax(&best, ((unsigned long long)(e - t) << 32) | (0xFFFFFFFFu - lab[t]));
+  }
+  __syncthreads();
+  if (t == 0) out[0] = 0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFu);
+}
+
+// phase 3, one-leaf vertices: thread per vertex
+__global__ void k_cc_rest_small(DGraph g, const unsigned long long *__restrict__ sdesc,
+                                const uint32_t *__restrict__ small, uint64_t nsmall,
+                                const unsigned long long *__restrict__ giant,
+                                uint32_t *__restrict__ par,
+                                unsigned long long *__restrict__ err) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsmall) return;
+  const uint32_t u = small[i];
+  if (ld_par(par, u) == (uint32_t)*giant) return;
+  const unsigned long long d = sdesc[i];
+  const uint32_t *p = g.slots + (d >> 6);
+  const uint32_t deg = (uint32_t)(d & 63);
+  for (uint32_t j = 0; j < deg; j++) cc_link(par, u, p[j], err);
+}
+
+// phase 3, multi-leaf vertices: warp per chunk of leaves, lane = slot
+__global__ void k_cc_rest_chunks(DGraph g, const unsigned long long *__restrict__ cdesc,
+                                 const uint32_t *__restrict__ cv, uint64_t nchunks,
+                                 const unsigned long long *__restrict__ giant,
+                                 uint32_t *__restrict__ par,
+                                 unsigned long long *__restrict__ err) {
+  const uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= nchunks) return;
+  const uint32_t u = cv[c];
+  if (ld_par(par, u) == (uint32_t)*giant) return;
+  const unsigned long long dsc = cdesc[c];
+  const uint64_t leaf0 = dsc >> 8;
+  const uint32_t nl = (uint32_t)(dsc & 63);
+  for (uint32_t l = 0; l < nl; l++) {
+    const uint32_t cnt = g.lcnt[leaf0 + l];
+    if ((uint32_t)lane < cnt) cc_link(par, u, g.slots[((leaf0 + l) << kLeafLog) + lane], err);
+  }
 }
 
 __global__ void k_cc_compress(uint32_t *__restrict__ par, uint32_t n) {
@@ -1174,6 +1270,35 @@ k_tc_count(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
       __syncwarp();
     }
     unsigned long long cu = 0;
+    if (hashed && na <= 32) {
+      // a short N+(u): each lane walks one v's list alone (the lists are
+      // short too on such graphs), probing the set
+      if ((uint64_t)lane < na) {
+        const uint32_t v = A[lane];
+        const uint64_t b0 = off[v], b1 = off[v + 1];
+        unsigned long long cv = 0;
+        for (uint64_t j = b0; j < b1; j++) {
+          const uint32_t w = adj[j];
+          uint32_t h = tc_hash(w, bits), x;
+          while ((x = tab[h]) != w && x != kEmpty) h = (h + 1) & mask;
+          if (x == w) {
+            cv++;
+            if (pv) atomicAdd(&pv[w], 1ull);
+          }
+        }
+        if (pv && cv) atomicAdd(&pv[v], cv);
+        cu = cv;
+      }
+      if (pv) {
+        unsigned long long t = cu;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) t += __shfl_xor_sync(0xffffffffu, t, d);
+        if (lane == 0 && t) atomicAdd(&pv[u], t);
+      }
+      local += cu;
+      __syncwarp();
+      continue;
+    }
     for (uint64_t i = 0; i < na; i++) {
       const uint32_t v = A[i];
       const uint64_t b0 = off[v], b1 = off[v + 1];
@@ -1371,15 +1496,20 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   // that footprint (more than 8,192 entries leaves under three blocks/SM)
   const uint32_t hot = std::min<uint32_t>(t->pr_hot, std::min<uint32_t>(n, 24576));
   const size_t hot_bytes = (size_t)hot * 8;
+  const bool big = hot > kHotBig;  // 1024-thread blocks
+  const int hot_threads = big ? 1024 : kHotThreads;
   unsigned hot_grid[4] = {1, 1, 1, 1};
   if (hot) {
-    const void *fns[4] = {(const void *)k_pr_small_hot<4>, (const void *)k_pr_small_hot<8>,
-                          (const void *)k_pr_small_hot<16>, (const void *)k_pr_chunks_hot};
+    const void *fns[4] = {
+        big ? (const void *)k_pr_small_hot<4, 1024> : (const void *)k_pr_small_hot<4>,
+        big ? (const void *)k_pr_small_hot<8, 1024> : (const void *)k_pr_small_hot<8>,
+        big ? (const void *)k_pr_small_hot<16, 1024> : (const void *)k_pr_small_hot<16>,
+        big ? (const void *)k_pr_chunks_hot<1024> : (const void *)k_pr_chunks_hot<>};
     for (int i = 0; i < 4; i++) {
       SST_CUDA_TRY(cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)hot_bytes));
       int per_sm = 0;
-      SST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], kHotThreads,
+      SST_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], hot_threads,
                                                                  hot_bytes));
       hot_grid[i] = (unsigned)std::max(1, per_sm) * (unsigned)g->sms;
     }
@@ -1392,15 +1522,22 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
     for (uint32_t it = 0; it < iters; it++) {
       bool last = it + 1 == iters;
       if (hot && t->nsmall) {
+#define SST_PR_SMALL_HOT(G, I)                                                        \
+  do {                                                                              \
+    if (big)                                                                        \
+      SST_LAUNCH((k_pr_small_hot<G, 1024>), hot_grid[I], 1024, hot_bytes, s, dg,    \
+                 t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot); \
+    else                                                                            \
+      SST_LAUNCH((k_pr_small_hot<G>), hot_grid[I], kHotThreads, hot_bytes, s, dg,   \
+                 t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot); \
+  } while (0)
         if (t->pr_lanes == 4)
-          SST_LAUNCH(k_pr_small_hot<4>, hot_grid[0], kHotThreads, hot_bytes, s, dg,
-                     t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot);
+          SST_PR_SMALL_HOT(4, 0);
         else if (t->pr_lanes == 16)
-          SST_LAUNCH(k_pr_small_hot<16>, hot_grid[2], kHotThreads, hot_bytes, s, dg,
-                     t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot);
+          SST_PR_SMALL_HOT(16, 2);
         else
-          SST_LAUNCH(k_pr_small_hot<8>, hot_grid[1], kHotThreads, hot_bytes, s, dg,
-                     t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last, hot);
+          SST_PR_SMALL_HOT(8, 1);
+#undef SST_PR_SMALL_HOT
       } else if (t->nsmall) {
         const uint64_t groups = (t->nsmall + kSmallPer - 1) / kSmallPer;
         if (t->pr_lanes == 4)
@@ -1413,8 +1550,11 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
           SST_LAUNCH(k_pr_small<8>, blocks_for(groups * 8), kTB, 0, s, dg,
                      t->sdesc.p, t->small.p, t->nsmall, ci, co, d_rank, rdeg, K, last);
       }
-      if (hot && t->nchunks)
-        SST_LAUNCH(k_pr_chunks_hot, hot_grid[3], kHotThreads, hot_bytes, s, dg, t->cdesc.p,
+      if (hot && t->nchunks && big)
+        SST_LAUNCH(k_pr_chunks_hot<1024>, hot_grid[3], 1024, hot_bytes, s, dg, t->cdesc.p,
+                   t->cv.p, t->nchunks, ci, co, d_rank, rdeg, part, K, last, hot);
+      else if (hot && t->nchunks)
+        SST_LAUNCH(k_pr_chunks_hot<>, hot_grid[3], kHotThreads, hot_bytes, s, dg, t->cdesc.p,
                    t->cv.p, t->nchunks, ci, co, d_rank, rdeg, part, K, last, hot);
       else if (t->nchunks)
         SST_LAUNCH(k_pr_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cdesc.p,
@@ -1541,27 +1681,38 @@ sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths
 }
 
 sst_status cc(sst_graph *g, uint32_t *d_labels) {
-  sst_status st = ensure_leaf_dir(g);
+  sst_status st = ensure_lists(g);
   if (st != SST_OK) return st;
-  TravState *t = state(g);
+  TravState *t = g->trav;
   cudaStream_t s = g->stream;
-  uint32_t n = g->n;
+  const uint32_t n = g->n;
   if (n == 0) return SST_OK;
-  LeafDir &D = g->dir;
   uint32_t *par = d_labels;
+  unsigned long long *giant = t->d_small, *err = t->d_small + 1;
+  SST_CUDA_TRY(cudaMemsetAsync(t->d_small, 0, 16, s));
+  const DGraph dg = g->view();
   SST_LAUNCH(k_iota, blocks_for(n), kTB, 0, s, par, n);
-  for (int round = 0; round < 1000; round++) {
-    SST_CUDA_TRY(cudaMemsetAsync(t->d_small, 0, 8, s));
-    if (D.nleaves)
-      SST_LAUNCH(k_cc_hook, warp_blocks(D.nleaves), kTB, 0, s, g->d_slots,
-                 D.owner, D.slot, D.cnt, D.nleaves, par, t->d_small);
+  for (uint32_t r = 0; r < 2; r++) {
+    SST_LAUNCH(k_cc_sample, blocks_for(n), kTB, 0, s, dg, r, par, err);
     SST_LAUNCH(k_cc_compress, blocks_for(n), kTB, 0, s, par, n);
-    SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, t->d_small, 8, cudaMemcpyDeviceToHost, s));
-    SST_CUDA_TRY(cudaStreamSynchronize(s));
-    if (t->h_small[0] == 0) return SST_OK;
   }
-  set_error_message("connected components did not converge");
-  return SST_ETIMEDOUT;
+  SST_LAUNCH(k_cc_giant, 1, 1024, 0, s, par, n, giant);
+  if (t->nsmall)
+    SST_LAUNCH(k_cc_rest_small, blocks_for(t->nsmall), kTB, 0, s, dg, t->sdesc.p,
+               t->small.p, t->nsmall, giant, par, err);
+  if (t->nchunks)
+    SST_LAUNCH(k_cc_rest_chunks, warp_blocks(t->nchunks), kTB, 0, s, dg, t->cdesc.p,
+               t->cv.p, t->nchunks, giant, par, err);
+  SST_LAUNCH(k_cc_compress, blocks_for(n), kTB, 0, s, par, n);
+  SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, t->d_small, 16, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  SST_CUDA_TRY(cudaGetLastError());
+  if (t->h_small[1]) {
+    set_error_message("connected components: %llu links gave up",
+                      (unsigned long long)t->h_small[1]);
+    return SST_ETIMEDOUT;
+  }
+  return SST_OK;
 }
 
 sst_status bc(sst_graph *g, uint32_t src, double *d_dep) {
@@ -2328,8 +2479,8 @@ sst_status autotune(sst_graph *g, sst_tuning *out) {
   // then the shared-memory cache of the lowest ids (pays on degree-ordered
   // graphs)
   uint32_t bhot = 0;
-  const uint32_t hots[3] = {2048, 4096, 8192};
-  for (uint32_t a = 0; a < 3 && st == SST_OK; a++) {
+  const uint32_t hots[5] = {2048, 4096, 8192, 16384, 24576};
+  for (uint32_t a = 0; a < 5 && st == SST_OK; a++) {
     t->pr_hot = hots[a];
     float ms = 0.f;
     st = timed([&] { return pagerank(g, 3, 0.85, rank); }, &ms);

@@ -134,9 +134,9 @@ def test_under_the_profiler(sg):
 
 def test_direct_launch_of_replay_forms(sg):
     """Mode 2 launches the kernels a replay runs one by one (same size
-    classes, two-launch scans): same graph as the replayed form and the
-    oracle, and the profiler sees the two-launch scans, not the
-    single-pass look-back form."""
+    classes; single-pass scans tagged from the device epoch, which a
+    one-thread kernel advances per sequence): same graph as the replayed
+    form and the oracle."""
     n = 1 << 14
     rng = np.random.default_rng(9)
     a = sg.SparseMatrixV(n)
@@ -153,10 +153,9 @@ def test_direct_launch_of_replay_forms(sg):
         seen |= set(sg.profile_collect())
         assert equal(a, d)
         assert equal(a, o)
-    # a planning scan of 200000 keys (49 tiles) takes the two-launch form
-    # (range reduction, then ranges) as in a replay; launched directly
-    # outside mode 2 it would be the single-pass look-back
-    assert any("k_scan_reduce" in k for k in seen), sorted(seen)
+    # the sequence advances the device epoch its scans take their tags from
+    assert "k_scan_epoch_bump" in seen, sorted(seen)
+    assert any("k_scan_lb" in k for k in seen), sorted(seen)
     assert any("k_scatter" in k for k in seen), sorted(seen)
     assert "update_plan_graph" not in seen
     a.close()
