@@ -1127,21 +1127,41 @@ def update_roofline(prof, prof_all, hbm_peak, peak_kind):
       scan                   2 x element size per element
     achieved = declared bytes / event time, summed over the timed launches.
     """
-    name, t = max(prof.items(), key=lambda kv: kv[1]["ms"])
-    base = name.strip("()").split("<")[0]
-    share = prof_all.get(name, t)["ms"] / sum(v["ms"] for v in prof_all.values())
-    out = {"bound": "hbm", "kernel": base, "launches": t["launches"],
-           "ms_total": t["ms"], "share_of_step_kernel_time": share,
+    # the profiler names a kernel's forms apart (template instances, scans
+    # over a device-side count): group them by kernel function, as the ncu
+    # launch-list summary in profiles/ does
+    def func(nm):
+        return nm.strip("()").split("<")[0].split(",")[0].strip()
+
+    groups = {}
+    for nm, v in prof.items():
+        g = groups.setdefault(func(nm), {"launches": 0, "ms": 0.0, "forms": []})
+        g["launches"] += v["launches"]
+        g["ms"] += v["ms"]
+        g["forms"].append(nm)
+    base, grp = max(groups.items(), key=lambda kv: kv[1]["ms"])
+    share = grp["ms"] / sum(v["ms"] for v in prof_all.values())
+    # achieved: the launches whose algorithmic bytes are declared (a scan
+    # over a device-side count declares none: its launch size overstates
+    # its work)
+    decl = [prof[nm] for nm in grp["forms"] if prof[nm].get("bytes", 0)]
+    traffic = [NCU_TRAFFIC[nm] for nm in grp["forms"] if nm in NCU_TRAFFIC]
+    out = {"bound": "hbm", "kernel": base, "launches": grp["launches"],
+           "ms_total": grp["ms"], "share_of_step_kernel_time": share,
+           "forms": grp["forms"],
            "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind,
-           "traffic": NCU_TRAFFIC.get(name),
+           "traffic": traffic[0] if traffic else None,
            "traffic_basis": "DRAM read + write per launch at 1e6-pair batches (ncu); "
                             "the kernel pass's launches span all four batch sizes"}
-    byts = t.get("bytes", 0)
-    if byts:
-        ach = byts / (t["ms"] / 1e3) / 1e9
+    if decl:
+        byts = sum(v["bytes"] for v in decl)
+        ms = sum(v["ms"] for v in decl)
+        nl = sum(v["launches"] for v in decl)
+        ach = byts / (ms / 1e3) / 1e9
         out.update({"achieved": ach, "frac": ach / hbm_peak,
-                    "algorithmic_bytes_per_launch": byts / t["launches"],
-                    "avg_launch_us": 1e3 * t["ms"] / t["launches"]})
+                    "algorithmic_bytes_per_launch": byts / nl,
+                    "avg_launch_us": 1e3 * ms / nl,
+                    "declared_launches": nl})
     else:
         out.update({"achieved": None, "frac": None})
     return out

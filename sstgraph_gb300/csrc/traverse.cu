@@ -1232,6 +1232,8 @@ __device__ __forceinline__ bool sorted_has(const uint32_t *a, uint64_t n,
 // stride over N+(v) (coalesced) and probe the set for each w.  A list too
 // long for the set is probed by binary search in global memory instead.
 constexpr uint32_t kTcHash = 2048;  // set slots per warp (8 KiB)
+// longest v list a lane walks alone (longer ones: the whole warp strides)
+constexpr uint32_t kTcLaneWalk = 64;
 constexpr int kTcWarps = 8;         // warps per block
 
 // multiplicative hashing (Knuth): the top `bits` bits of x * 2^32/phi
@@ -1270,12 +1272,23 @@ k_tc_count(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
       __syncwarp();
     }
     unsigned long long cu = 0;
+    uint64_t mb0 = 0, mb1 = 0;  // this lane's v list, for a short N+(u)
+    uint32_t longest = ~0u;
     if (hashed && na <= 32) {
-      // a short N+(u): each lane walks one v's list alone (the lists are
-      // short too on such graphs), probing the set
       if ((uint64_t)lane < na) {
         const uint32_t v = A[lane];
-        const uint64_t b0 = off[v], b1 = off[v + 1];
+        mb0 = off[v];
+        mb1 = off[v + 1];
+      }
+      const uint64_t len = mb1 - mb0;
+      longest = __reduce_max_sync(0xffffffffu, len > 0xffffffffull ? 0xffffffffu : (uint32_t)len);
+    }
+    if (longest <= kTcLaneWalk) {
+      // a short N+(u) whose v lists are short too: each lane walks one v's
+      // list alone, probing the set
+      if ((uint64_t)lane < na) {
+        const uint32_t v = A[lane];
+        const uint64_t b0 = mb0, b1 = mb1;
         unsigned long long cv = 0;
         for (uint64_t j = b0; j < b1; j++) {
           const uint32_t w = adj[j];
