@@ -238,6 +238,13 @@ def ref():
                                    ctypes.POINTER(vp)]),
             "ref_free": (None, [vp]),
             "ref_tinyset_thresholds": (None, [u64, vp]),
+            "ref_wgraph_new": (vp, [u32]),
+            "ref_wgraph_free": (None, [vp]),
+            "ref_winsert_batch": (None, [vp, vp, vp, u64]),
+            "ref_wremove_each": (None, [vp, vp, u64]),
+            "ref_wM": (u64, [vp]),
+            "ref_wvalue": (u32, [vp, u32, u32]),
+            "ref_wto_csr": (None, [vp, vp, vp, vp]),
             "ref_tinyset_width": (u32, [u64, vp, u64]),
         }
         for name, (res, args) in sig.items():
@@ -301,6 +308,46 @@ class RefGraph:
         g.n = self.n
         g._h = ref().ref_rewrite_graph(self._h, _ptr(m))
         return g
+
+
+class RefWGraph:
+    """The reference SparseMatrixV<true, uint32_t> (compiled reference code):
+    insert_batch with a value per pair; removes one edge at a time (the
+    reference's weighted remove_batch does not compile)."""
+
+    def __init__(self, n: int):
+        self.n = int(n)
+        self._h = ref().ref_wgraph_new(self.n)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            ref().ref_wgraph_free(h)
+            self._h = None
+
+    def insert_batch(self, edges, values):
+        e = _pairs(edges)
+        v = np.ascontiguousarray(np.asarray(values, np.uint32).reshape(-1))
+        ref().ref_winsert_batch(self._h, _ptr(e), _ptr(v), e.shape[0])
+
+    def remove_each(self, edges):
+        e = _pairs(edges)
+        ref().ref_wremove_each(self._h, _ptr(e), e.shape[0])
+
+    def M(self) -> int:
+        return int(ref().ref_wM(self._h))
+
+    def value(self, r, c) -> int:
+        return int(ref().ref_wvalue(self._h, r, c))
+
+    def csr_values(self):
+        m = self.M()
+        off = np.empty(self.n + 1, np.uint64)
+        cols = np.empty(max(m, 1), np.uint32)
+        vals = np.empty(max(m, 1), np.uint32)
+        ref().ref_wto_csr(self._h, _ptr(off), _ptr(cols), _ptr(vals))
+        k = int(off[-1])
+        return off, cols[:k], vals[:k]
 
 
 def degree_order_map(degrees) -> np.ndarray:

@@ -13,6 +13,7 @@
 //   getDegree / M / common_neighbors      include/SSTGraph/SparseMatrix.hpp:57,518,61
 //   map_neighbors_no_early_exit           include/SSTGraph/SparseMatrix.hpp:243
 //   touch_all_sum                         include/SSTGraph/SparseMatrix.hpp:436
+//   SparseMatrixV<true, uint32_t>         include/SSTGraph/SparseMatrix.hpp:167,179-216,727
 //   TinySetV                              include/SSTGraph/TinySet.hpp:8-73
 //   TinySetV_small get_thresholds, get_b  include/SSTGraph/TinySet_small.hpp:129-135,227-263
 //   rMat / random_aspen / hash64 / hash32 include/SSTGraph/internal/rmat_util.h:29-131
@@ -108,6 +109,63 @@ void *ref_rewrite_graph(void *gp, const uint32_t *map) {
   Graph *g = static_cast<Graph *>(gp);
   std::vector<uint64_t> m(map, map + g->num_nodes());
   return new Graph(g->rewrite_graph(m));
+}
+
+// ---- weighted graph: SparseMatrixV<true, uint32_t>  (internal/test.hpp:714)
+// insert_batch takes (row, col, value) tuples (SparseMatrix.hpp:167,558);
+// a present edge takes the new value (PMA.hpp:1137-1145)
+using WGraph = SparseMatrixV<true, uint32_t>;
+void *ref_wgraph_new(uint32_t n) { return new WGraph(n, n); }
+void ref_wgraph_free(void *g) { delete static_cast<WGraph *>(g); }
+void ref_winsert_batch(void *g, const uint32_t *pairs, const uint32_t *vals,
+                       uint64_t b) {
+  std::vector<std::tuple<el_t, el_t, uint32_t>> es(b);
+  for (uint64_t i = 0; i < b; i++) es[i] = {pairs[2 * i], pairs[2 * i + 1], vals[i]};
+  static_cast<WGraph *>(g)->insert_batch(es.data(), b);
+}
+// The weighted remove_batch does not compile in the reference (its sort
+// comparator takes the (row, col, value) element while remove_batch passes
+// (row, col) pairs, SparseMatrix.hpp:489-494,647), so removes go through the
+// single-edge remove (SparseMatrix.hpp:537) one pair at a time.
+void ref_wremove_each(void *g, const uint32_t *pairs, uint64_t b) {
+  for (uint64_t i = 0; i < b; i++)
+    static_cast<WGraph *>(g)->remove(pairs[2 * i], pairs[2 * i + 1]);
+}
+uint64_t ref_wM(void *g) { return static_cast<WGraph *>(g)->M(); }
+// value(row, col)  SparseMatrix.hpp:727 (0 where absent)
+uint32_t ref_wvalue(void *g, uint32_t r, uint32_t c) {
+  return std::get<0>(static_cast<WGraph *>(g)->value(r, c));
+}
+
+struct collect_wf {
+  static constexpr bool no_early_exit = true;
+  std::vector<uint32_t> *out, *vout;
+  bool operator()(uint64_t, uint64_t dst, uint32_t val) {
+    out->push_back(static_cast<uint32_t>(dst));
+    vout->push_back(val);
+    return false;
+  }
+};
+
+// neighbour sets with their values in map order: offsets[n+1], cols[M],
+// vals[M]  (the value-carrying map_neighbors, SparseMatrix.hpp:179-216)
+void ref_wto_csr(void *gp, uint64_t *offsets, uint32_t *cols, uint32_t *vals) {
+  WGraph *g = static_cast<WGraph *>(gp);
+  uint64_t pos = 0;
+  std::vector<uint32_t> tmp, vtmp;
+  for (uint64_t v = 0; v < g->num_nodes(); v++) {
+    offsets[v] = pos;
+    tmp.clear();
+    vtmp.clear();
+    collect_wf f{&tmp, &vtmp};
+    g->map_neighbors(v, f, nullptr, false);
+    for (size_t k = 0; k < tmp.size(); k++) {
+      cols[pos] = tmp[k];
+      vals[pos] = vtmp[k];
+      pos++;
+    }
+  }
+  offsets[g->num_nodes()] = pos;
 }
 
 // ---- standalone set (TinySetV) ----

@@ -30,8 +30,20 @@ Fixtures (all small, npz):
                         column counts (TinySet_small.hpp:227-263), and the key
                         width get_b() of a reference set after inserting k
                         distinct ids, for k on both sides of each threshold
+  weighted_stream.npz   SparseMatrixV<true, uint32_t> (internal/test.hpp:714):
+                        a weighted RMAT scale-10 base graph, then 6 batches of
+                        weighted inserts (a fifth of each re-inserts present
+                        edges with new values: PMA.hpp:1137-1145) with removes
+                        of sampled edges after every second one; the batches
+                        and a sha256 of the CSR with its values after every
+                        batch (the last one in full).  No
+                        pair repeats inside a batch: the reference's batch
+                        sort (SparseMatrix.hpp:489-494) does not define which
+                        of equal pairs wins.  Removes go through the
+                        single-edge remove (the weighted remove_batch does not
+                        compile in the reference)
 
-`--only tinyset_widths` writes that fixture alone.
+`--only tinyset_widths` / `--only weighted_stream` writes that fixture alone.
 """
 import hashlib
 import os
@@ -85,6 +97,62 @@ def tinyset_widths():
     np.savez_compressed(os.path.join(HERE, "tinyset_widths.npz"),
                         max_el=np.array(TINYSET_MAX_ELS, np.uint64), thresholds=th,
                         width_max_el=w[:, 0], width_count=w[:, 1], width=w[:, 2])
+
+
+def wcsr_digest(off, cols, vals):
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(off, np.uint64).tobytes())
+    h.update(np.ascontiguousarray(cols, np.uint32).tobytes())
+    h.update(np.ascontiguousarray(vals, np.uint32).tobytes())
+    return h.hexdigest()
+
+
+def weighted_stream():
+    scale, n = 10, 1 << 10
+    rng = np.random.default_rng(12)
+    g = oracle.RefWGraph(n)
+
+    def unique_pairs(e):
+        _, idx = np.unique(e[:, 0].astype(np.int64) * n + e[:, 1], return_index=True)
+        return np.ascontiguousarray(e[np.sort(idx)])
+
+    base = unique_pairs(oracle.symmetrize(oracle.rmat(scale, 8 * n, seed=31)))
+    bval = rng.integers(1, 1 << 20, len(base)).astype(np.uint32)
+    g.insert_batch(base, bval)
+    out = {"scale": np.uint32(scale), "base": base, "base_val": bval}
+    steps, digests, ms = [], [], []
+
+    def snap(tag):
+        off, cols, vals = g.csr_values()
+        digests.append(wcsr_digest(off, cols, vals))
+        ms.append(len(cols))
+        steps.append(tag)
+        out["off_final"], out["cols_final"], out["vals_final"] = off, cols, vals
+        return off, cols
+
+    off, cols = snap("base")
+    for i in range(6):
+        new = oracle.rmat(scale, 600, seed=32, first=i * 600)
+        rows = np.repeat(np.arange(n), np.diff(off.astype(np.int64)))
+        pick = rng.choice(len(cols), 150, replace=False)
+        old = np.stack([rows[pick], cols[pick]], 1).astype(np.uint32)
+        ins = unique_pairs(np.concatenate([new, old]))
+        val = rng.integers(1, 1 << 20, len(ins)).astype(np.uint32)
+        g.insert_batch(ins, val)
+        out[f"ins_{i}"] = ins
+        out[f"insval_{i}"] = val
+        off, cols = snap(f"i{i}")
+        if i % 2 == 1:
+            rows = np.repeat(np.arange(n), np.diff(off.astype(np.int64)))
+            pick = rng.choice(len(cols), 120, replace=False)
+            rem = np.stack([rows[pick], cols[pick]], 1).astype(np.uint32)
+            g.remove_each(rem)
+            out[f"rem_{i}"] = rem
+            off, cols = snap(f"r{i}")
+    out["steps"] = np.array(steps)
+    out["digests"] = np.array(digests)
+    out["M"] = np.array(ms, np.uint64)
+    np.savez_compressed(os.path.join(HERE, "weighted_stream.npz"), **out)
 
 
 def main(ref_root):
@@ -179,6 +247,7 @@ def main(ref_root):
         ex[f"{key}_cols"] = cols
     np.savez_compressed(os.path.join(HERE, "examples_mtx.npz"), **ex)
     tinyset_widths()
+    weighted_stream()
     print("golden fixtures written to", HERE)
 
 
@@ -186,5 +255,7 @@ if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     if "--only" in sys.argv and sys.argv[-1] == "tinyset_widths":
         tinyset_widths()
+    elif "--only" in sys.argv and sys.argv[-1] == "weighted_stream":
+        weighted_stream()
     else:
         main(args[0] if args else "/root/reference")

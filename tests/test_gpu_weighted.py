@@ -129,3 +129,14 @@ def test_weighted_refusals(sg):
         sg.BF(g, 8)
     g.close()
     u.close()
+
+
+def test_device_matches_reference_weighted_stream(sg):
+    """The device replays the stream the reference's own
+    SparseMatrixV<true, uint32_t> wrote (tests/golden/weighted_stream.npz):
+    CSR and values equal to the reference's after every batch."""
+    from weighted_golden import replay
+    g = replay(lambda n: sg.SparseMatrixV(n, weighted=True),
+               lambda g, p, v: g.insert_batch_weighted(p, v),
+               lambda g, p: g.remove_batch(p))
+    g.close()

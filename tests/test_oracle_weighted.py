@@ -43,3 +43,12 @@ def test_bf_matches_dijkstra():
         got = o2.bf(src)
         exp32 = np.where(np.isinf(exp), INF32, exp).astype(np.int64)
         assert np.array_equal(got.astype(np.int64), exp32)
+
+
+def test_oracle_matches_reference_weighted_stream():
+    """The restatement replays the reference's weighted stream (values of
+    present edges overwritten, removes) with the reference's CSR and values
+    after every batch."""
+    from weighted_golden import replay
+    replay(WeightedOracle, lambda g, p, v: g.insert_batch(p, v),
+           lambda g, p: g.remove_batch(p))
