@@ -55,6 +55,8 @@ def args_parse():
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the oracle replay of the bench graph's batches")
     ap.add_argument("--pr-iters", type=int, default=10)
+    ap.add_argument("--profile-batch", type=int, default=1000000,
+                    help="--only insert-profile: pairs in the profiled insert")
     ap.add_argument("--batched-batches", type=int, default=512)
     ap.add_argument("--serve-requests", type=int, default=400)
     # offered load of the serving latency run (requests/s): below the
@@ -63,7 +65,7 @@ def args_parse():
     ap.add_argument("--serve-scale", type=int, default=25)
     ap.add_argument("--only", default="all",
                     choices=["all", "updates", "pagerank", "bfs", "batched", "serving",
-                             "multi", "compact", "extras", "static"],
+                             "multi", "compact", "extras", "static", "insert-profile"],
                     help="one part of the run (profiling cases): the update steps "
                          "alone, or one traversal on the base graph")
     return ap.parse_args()
@@ -284,10 +286,48 @@ def workload_config(a):
             "parallelism": "replicas" if a.gpus > 1 else "single GPU"}
 
 
+def insert_profile(a):
+    """One insert batch for a profiler: the scale-`scale` RMAT base graph
+    (seed 5, symmetrised), a warm-up batch of `profile_batch` RMAT pairs
+    (seed 6; it grows the scratch and captures the planning graph), then
+    one more such batch between cudaProfilerStart and cudaProfilerStop, so
+    `ncu --profile-from-start off` sees that batch's launches alone."""
+    import torch
+
+    import sstgraph_gb300 as sg
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    n = 1 << a.scale
+    g = sg.SparseMatrixV(n, initial_slots=int(3.2 * 16 * n))
+    g.set_stream(stream.cuda_stream)
+    b = a.profile_batch
+    with torch.cuda.stream(stream):
+        x = torch.empty((8 * n, 2), dtype=torch.int32, device="cuda")
+        sg.gen_rmat(a.scale, 8 * n, seed=5, out=x, **RMAT)
+        g.insert_batch(x)
+        g.insert_batch(x.flip(1).contiguous())
+        del x
+        ys = [torch.empty((b, 2), dtype=torch.int32, device="cuda") for _ in range(2)]
+        for i, y in enumerate(ys):
+            sg.gen_rmat(a.scale, b, seed=6, first=i * b, out=y, **RMAT)
+    torch.cuda.synchronize()
+    g.insert_batch(ys[0])
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    g.insert_batch(ys[1])
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"only": "insert-profile", "scale": a.scale, "batch": b,
+                      "edges": g.M()}))
+    g.close()
+
+
 def main():
     a = args_parse()
     if a.impl == "reference":
         return reference_arm(a)
+    if a.only == "insert-profile":
+        return insert_profile(a)
     import numpy as np
     import torch
 
@@ -1103,14 +1143,14 @@ def main():
     print(json.dumps(line))
 
 
-# DRAM bytes (read + write) per launch from one ncu capture of the kernel's
-# launches at the bench's batch sizes (dram__bytes_read.sum +
-# dram__bytes_write.sum; k_scan_lb: its 40 launches over whole 1e6-element
-# arrays in 1e6-pair batches, whose scan sizes do not depend on the graph's
-# scale; the scans' writes stay in L2 within the launch.  Scans over a
-# device-side count are profiled apart.  k_scatter: its 48 passes over 1e6
-# keys, 245 tiles of 4096; the scattered keys stay in L2 within the launch.)
-NCU_TRAFFIC = {"(k_scan_lb<T, Op, Epi>)": 6.43e6, "(k_scatter<false, 16>)": 8.46e6}
+# DRAM bytes (read + write) per launch from one ncu capture of one 1e6-pair
+# insert (profiles/scan_scatter_locate_1e6_insert_rmat21.md): the host-sized
+# single-pass scans read their input once and their writes stay in L2
+# (mean over the five of the planning sequence); a one-sweep scatter pass
+# over 1e6 keys reads the keys once; the leaf search reads ~5.6 random
+# sectors a key.
+NCU_TRAFFIC = {"(k_scan_lb<T, Op, Epi>)": 6.75e6, "(k_scatter_os<false, 16>)": 8.30e6,
+               "k_locate": 1.92e8}
 
 
 def update_roofline(prof, prof_all, hbm_peak, peak_kind):
@@ -1151,7 +1191,7 @@ def update_roofline(prof, prof_all, hbm_peak, peak_kind):
            "forms": grp["forms"],
            "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind,
            "traffic": traffic[0] if traffic else None,
-           "traffic_basis": "DRAM read + write per launch at 1e6-pair batches (ncu); "
+           "traffic_basis": "DRAM read + write per launch in one 1e6-pair insert (ncu); "
                             "the kernel pass's launches span all four batch sizes"}
     if decl:
         byts = sum(v["bytes"] for v in decl)

@@ -313,6 +313,13 @@ SST_API sst_status sst_compact_has_batch(sst_compact *c, const uint32_t *pairs,
 SST_API sst_status sst_compact_pagerank(sst_compact *c, uint32_t iters,
                                         double damping, double *out,
                                         uint32_t flags);
+/* BFS(g, src)  test.hpp:486 on the snapshot: depths (-1 unreached), equal
+ * to sst_bfs's on the graph it was taken from; the same push / pull switch */
+SST_API sst_status sst_compact_bfs(sst_compact *c, uint32_t src, int32_t *depths,
+                                   uint32_t flags);
+/* CC(g)  test.hpp:571 on the snapshot: each label the component's smallest
+ * vertex id, equal to sst_cc's */
+SST_API sst_status sst_compact_cc(sst_compact *c, uint32_t *labels, uint32_t flags);
 /* the stream the snapshot's work runs on (NULL: its own), as sst_set_stream */
 SST_API sst_status sst_compact_set_stream(sst_compact *c, void *stream);
 SST_API sst_status sst_compact_sync(sst_compact *c);

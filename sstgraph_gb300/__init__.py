@@ -152,6 +152,8 @@ SIGNATURES = {
     "sst_compact_to_csr": (_i32, [_vp, _vp, _vp, _u32]),
     "sst_compact_has_batch": (_i32, [_vp, _vp, _u64, _vp, _u32]),
     "sst_compact_pagerank": (_i32, [_vp, _u32, _dbl, _vp, _u32]),
+    "sst_compact_bfs": (_i32, [_vp, _u32, _vp, _u32]),
+    "sst_compact_cc": (_i32, [_vp, _vp, _u32]),
     "sst_compact_sync": (_i32, [_vp]),
     "sst_compact_set_stream": (_i32, [_vp, _vp]),
     "sst_profile_start": (_i32, [ctypes.c_char_p]),
@@ -721,6 +723,20 @@ class CompactGraph:
         buf = np.empty(self.rows, np.float64) if out is None else out
         p, flags = _ptr(buf)
         _check(lib().sst_compact_pagerank(self._h, iters, damping, p, flags))
+        return buf
+
+    def bfs(self, src: int, out=None):
+        """BFS depths from src (-1 unreached), as BFS(g, src, depths=True)."""
+        buf = np.empty(self.rows, np.int32) if out is None else out
+        p, flags = _ptr(buf)
+        _check(lib().sst_compact_bfs(self._h, int(src), p, flags))
+        return buf
+
+    def cc(self, out=None):
+        """Component labels (the component's smallest id), as CC(g)."""
+        buf = np.empty(self.rows, np.uint32) if out is None else out
+        p, flags = _ptr(buf)
+        _check(lib().sst_compact_cc(self._h, p, flags))
         return buf
 
     def sync(self):

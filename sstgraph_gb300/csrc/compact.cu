@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "ccshared.cuh"
 #include "graph.cuh"
 #include "prfixed.cuh"
 
@@ -530,6 +531,181 @@ __global__ void k_fill_d(double *__restrict__ out, uint32_t n, double x) {
   if (v < n) out[v] = x;
 }
 
+// ------------------------------------------------------ traversals
+// BFS and CC read the snapshot's rows through the PageRank work lists:
+// one-bucket rows of up to kSmallRow ids (a thread each) and chunks of
+// kElemsPerWarp ids of the other rows (a warp each).
+
+// id of element i of a one-bucket small row at byte offset o (B bytes)
+__device__ __forceinline__ uint32_t small_id(const uint8_t *bytes, uint64_t o,
+                                             uint32_t i, uint32_t B) {
+  return low_at(bytes + o + (uint64_t)i * B, B);
+}
+
+// ---- connected components (Afforest; the shared parts in ccshared.cuh)
+// round r: v links to its r-th smallest neighbour
+__global__ void k_ccc_sample(DCompact c, uint32_t r, uint32_t *__restrict__ par,
+                             unsigned long long *__restrict__ err) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= c.n) return;
+  const uint32_t d = c.deg[v];
+  if (r >= d) return;
+  const Row row = row_of(c, v);
+  cc_link(par, v, elem_at(row, r, row.nb > 1 ? bucket_of(row, r) : 0u), err);
+}
+
+__global__ void k_ccc_rest_small(DCompact c, const unsigned long long *__restrict__ sdesc,
+                                 const uint32_t *__restrict__ small, uint64_t nsmall,
+                                 const unsigned long long *__restrict__ giant,
+                                 uint32_t *__restrict__ par,
+                                 unsigned long long *__restrict__ err) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsmall) return;
+  const uint32_t v = small[i];
+  if (ld_par(par, v) == (uint32_t)*giant) return;
+  const unsigned long long dsc = sdesc[i];
+  const uint32_t d = (uint32_t)(dsc & 63);
+  const uint32_t B = width_of(d, c.t24, c.t16, c.t8);
+  for (uint32_t j = 0; j < d; j++) cc_link(par, v, small_id(c.bytes, dsc >> 6, j, B), err);
+}
+
+__global__ void k_ccc_rest_chunks(DCompact c, const uint32_t *__restrict__ cv,
+                                  const uint32_t *__restrict__ c0, uint64_t nchunks,
+                                  const unsigned long long *__restrict__ giant,
+                                  uint32_t *__restrict__ par,
+                                  unsigned long long *__restrict__ err) {
+  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= nchunks) return;
+  const uint32_t v = cv[w], e0 = c0[w];
+  if (ld_par(par, v) == (uint32_t)*giant) return;
+  const Row r = row_of(c, v);
+  const uint32_t e1 = min(e0 + kElemsPerWarp, r.d);
+  uint32_t b = (r.nb > 1 && e0 + lane < e1) ? bucket_of(r, e0 + lane) : 0u;
+  for (uint32_t i = e0 + lane; i < e1; i += 32) {
+    if (r.nb > 1)
+      while (r.dir[b + 1] <= i) b++;
+    cc_link(par, v, elem_at(r, i, b), err);
+  }
+}
+
+// ---- BFS (depths), push or pull per level as on the PMA graph
+__device__ __forceinline__ void cbfs_enqueue(uint32_t w, uint32_t d,
+                                             uint32_t *__restrict__ nq,
+                                             unsigned long long *__restrict__ cnt) {
+  const unsigned long long at = atomicAdd(&cnt[0], 1ull);
+  nq[at] = w;
+  atomicAdd(&cnt[1], (unsigned long long)d);
+  atomicAdd(&cnt[2], (unsigned long long)((d + kElemsPerWarp - 1) / kElemsPerWarp));
+}
+
+__global__ void k_cbfs_init(int32_t *__restrict__ depth, uint32_t n, uint32_t src) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n) depth[v] = v == src ? 0 : -1;
+}
+
+__global__ void k_cbfs_bits(const uint32_t *__restrict__ q, uint64_t qn,
+                            uint32_t *__restrict__ bits) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < qn) atomicOr(&bits[q[i] >> 5], 1u << (q[i] & 31));
+}
+
+__device__ __forceinline__ bool in_front(const uint32_t *bits, uint32_t x) {
+  return (__ldg(bits + (x >> 5)) >> (x & 31)) & 1u;
+}
+
+// pull, small rows: an unreached vertex looks for a neighbour in the
+// frontier and stops at the first
+__global__ void k_cbfs_pull_small(DCompact c, const unsigned long long *__restrict__ sdesc,
+                                  const uint32_t *__restrict__ small, uint64_t nsmall,
+                                  const uint32_t *__restrict__ bits,
+                                  int32_t *__restrict__ depth, uint32_t *__restrict__ nq,
+                                  unsigned long long *__restrict__ cnt, int32_t lvl) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsmall) return;
+  const uint32_t v = small[i];
+  if (depth[v] >= 0) return;
+  const unsigned long long dsc = sdesc[i];
+  const uint32_t d = (uint32_t)(dsc & 63);
+  const uint32_t B = width_of(d, c.t24, c.t16, c.t8);
+  for (uint32_t j = 0; j < d; j++)
+    if (in_front(bits, small_id(c.bytes, dsc >> 6, j, B))) {
+      depth[v] = lvl + 1;  // a small row is its vertex's only work item
+      cbfs_enqueue(v, d, nq, cnt);
+      return;
+    }
+}
+
+// pull, chunks: a warp per chunk, 32 ids a step, until one is in the
+// frontier; the chunks of one row claim their vertex with a
+// compare-and-swap
+__global__ void k_cbfs_pull_chunks(DCompact c, const uint32_t *__restrict__ cv,
+                                   const uint32_t *__restrict__ c0, uint64_t nchunks,
+                                   const uint32_t *__restrict__ bits,
+                                   int32_t *__restrict__ depth, uint32_t *__restrict__ nq,
+                                   unsigned long long *__restrict__ cnt, int32_t lvl) {
+  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= nchunks) return;
+  const uint32_t v = cv[w], e0 = c0[w];
+  if (__ldcg(depth + v) >= 0) return;
+  const Row r = row_of(c, v);
+  const uint32_t e1 = min(e0 + kElemsPerWarp, r.d);
+  uint32_t b = (r.nb > 1 && e0 + lane < e1) ? bucket_of(r, e0 + lane) : 0u;
+  for (uint32_t i0 = e0; i0 < e1; i0 += 32) {
+    const uint32_t i = i0 + lane;
+    bool hit = false;
+    if (i < e1) {
+      if (r.nb > 1)
+        while (r.dir[b + 1] <= i) b++;
+      hit = in_front(bits, elem_at(r, i, b));
+    }
+    if (__any_sync(0xffffffffu, hit)) {
+      if (lane == 0 && atomicCAS(depth + v, -1, lvl + 1) == -1) cbfs_enqueue(v, r.d, nq, cnt);
+      return;
+    }
+  }
+}
+
+// push: work items of kElemsPerWarp ids of the frontier's rows
+__global__ void k_cbfs_items(const uint32_t *__restrict__ q, uint64_t qn,
+                             const uint32_t *__restrict__ deg, uint32_t *__restrict__ k) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < qn) k[i] = (deg[q[i]] + kElemsPerWarp - 1) / kElemsPerWarp;
+}
+
+__global__ void k_cbfs_expand(const uint32_t *__restrict__ q, uint64_t qn,
+                              const uint32_t *__restrict__ k,
+                              const uint32_t *__restrict__ koff,
+                              uint32_t *__restrict__ iv, uint32_t *__restrict__ ie0) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= qn) return;
+  for (uint32_t j = 0; j < k[i]; j++) {
+    iv[koff[i] + j] = q[i];
+    ie0[koff[i] + j] = j * kElemsPerWarp;
+  }
+}
+
+__global__ void k_cbfs_push(DCompact c, const uint32_t *__restrict__ iv,
+                            const uint32_t *__restrict__ ie0, uint64_t nitems,
+                            int32_t *__restrict__ depth, uint32_t *__restrict__ nq,
+                            unsigned long long *__restrict__ cnt, int32_t lvl) {
+  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= nitems) return;
+  const uint32_t u = iv[w], e0 = ie0[w];
+  const Row r = row_of(c, u);
+  const uint32_t e1 = min(e0 + kElemsPerWarp, r.d);
+  uint32_t b = (r.nb > 1 && e0 + lane < e1) ? bucket_of(r, e0 + lane) : 0u;
+  for (uint32_t i = e0 + lane; i < e1; i += 32) {
+    if (r.nb > 1)
+      while (r.dir[b + 1] <= i) b++;
+    const uint32_t x = elem_at(r, i, b);
+    if (__ldcg(depth + x) < 0 && atomicCAS(depth + x, -1, lvl + 1) == -1)
+      cbfs_enqueue(x, c.deg[x], nq, cnt);
+  }
+}
+
 }  // namespace
 }  // namespace sst
 
@@ -556,6 +732,11 @@ struct sst_compact {
   uint64_t nmulti = 0;
   unsigned long long *d_rdeg = nullptr, *d_ca = nullptr, *d_cb = nullptr,
                      *d_partial = nullptr;
+  // traversal buffers (BFS queues, frontier bits, push items; counters)
+  uint32_t *d_qa = nullptr, *d_qb = nullptr, *d_bits = nullptr;
+  uint32_t *d_ik = nullptr, *d_ikoff = nullptr, *d_iv = nullptr, *d_ie0 = nullptr;
+  uint64_t items_cap = 0;
+  unsigned long long *d_cnt = nullptr, *h_cnt = nullptr;  // h_cnt pinned
   sst::Arena arena;  // scans and staging
 
   sst::DCompact view() const {
@@ -572,8 +753,11 @@ void compact_release(sst_compact *c) {
   for (void *p : {(void *)c->d_off, (void *)c->d_deg, (void *)c->d_bytes,
                   (void *)c->d_small, (void *)c->d_sdesc, (void *)c->d_cv, (void *)c->d_c0,
                   (void *)c->d_multi, (void *)c->d_first, (void *)c->d_rdeg,
-                  (void *)c->d_ca, (void *)c->d_cb, (void *)c->d_partial})
+                  (void *)c->d_ca, (void *)c->d_cb, (void *)c->d_partial,
+                  (void *)c->d_qa, (void *)c->d_qb, (void *)c->d_bits, (void *)c->d_ik,
+                  (void *)c->d_ikoff, (void *)c->d_iv, (void *)c->d_ie0, (void *)c->d_cnt})
     if (p) cudaFree(p);
+  if (c->h_cnt) cudaFreeHost(c->h_cnt);
   c->arena.release();
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   c->stream = c->own_stream = nullptr;
@@ -762,13 +946,127 @@ sst_status compact_pagerank(sst_compact *c, uint32_t iters, double damping,
   return SST_OK;
 }
 
+static sst_status compact_trav_buffers(sst_compact *c) {
+  if (c->d_cnt) return SST_OK;
+  const uint64_t n = std::max<uint32_t>(c->n, 1);
+  SST_CUDA_TRY(cudaMalloc(&c->d_cnt, 8 * sizeof(unsigned long long)));
+  SST_CUDA_TRY(cudaMallocHost(&c->h_cnt, 8 * sizeof(unsigned long long)));
+  SST_CUDA_TRY(cudaMalloc(&c->d_qa, n * 4));
+  SST_CUDA_TRY(cudaMalloc(&c->d_qb, n * 4));
+  SST_CUDA_TRY(cudaMalloc(&c->d_bits, (n / 32 + 2) * 4));
+  SST_CUDA_TRY(cudaMalloc(&c->d_ik, (n + 1) * 4));
+  SST_CUDA_TRY(cudaMalloc(&c->d_ikoff, (n + 1) * 4));
+  return SST_OK;
+}
+
+// BFS(g, src) on the snapshot: depths, -1 unreached (the same pull / push
+// switch as on the PMA graph: pull once (frontier + its edges) * 20 > m)
+sst_status compact_bfs(sst_compact *c, uint32_t src, int32_t *d_depth) {
+  SST_CUDA_TRY(cudaSetDevice(c->device));
+  sst_status st = compact_trav_buffers(c);
+  if (st != SST_OK) return st;
+  cudaStream_t s = c->stream;
+  const uint32_t n = c->n;
+  const DCompact dc = c->view();
+  SST_LAUNCH(k_cbfs_init, blocks_for(n), kTB, 0, s, d_depth, n, src);
+  uint32_t d0 = 0;
+  SST_CUDA_TRY(cudaMemcpyAsync(c->d_qa, &src, 4, cudaMemcpyHostToDevice, s));
+  SST_CUDA_TRY(cudaMemcpyAsync(&d0, c->d_deg + src, 4, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint64_t qn = 1, qdeg = d0, qitems = (d0 + kElemsPerWarp - 1) / kElemsPerWarp;
+  uint32_t *q = c->d_qa, *nq = c->d_qb;
+  const uint64_t m = c->m;
+  Arena &A = c->arena;
+  SST_CUDA_TRY(A.reserve(scan_scratch_bytes((uint64_t)n + 1, 4) + 4096));
+  for (int32_t lvl = 0; qn > 0; lvl++) {
+    if ((uint64_t)lvl > n) {
+      set_error_message("BFS exceeded n levels");
+      return SST_ETIMEDOUT;
+    }
+    SST_CUDA_TRY(cudaMemsetAsync(c->d_cnt, 0, 24, s));
+    if ((qn + qdeg) * 20 > m) {
+      SST_CUDA_TRY(cudaMemsetAsync(c->d_bits, 0, ((uint64_t)n / 32 + 1) * 4, s));
+      SST_LAUNCH(k_cbfs_bits, blocks_for(qn), kTB, 0, s, q, qn, c->d_bits);
+      if (c->nsmall)
+        SST_LAUNCH(k_cbfs_pull_small, blocks_for(c->nsmall), kTB, 0, s, dc, c->d_sdesc,
+                   c->d_small, c->nsmall, c->d_bits, d_depth, nq, c->d_cnt, lvl);
+      if (c->nchunks)
+        SST_LAUNCH(k_cbfs_pull_chunks, warp_blocks(c->nchunks), kTB, 0, s, dc, c->d_cv,
+                   c->d_c0, c->nchunks, c->d_bits, d_depth, nq, c->d_cnt, lvl);
+    } else if (qitems) {
+      if (qitems > c->items_cap) {
+        cudaFree(c->d_iv);
+        cudaFree(c->d_ie0);
+        c->d_iv = c->d_ie0 = nullptr;
+        c->items_cap = 0;
+        const uint64_t want = qitems + qitems / 4 + 64;
+        SST_CUDA_TRY(cudaMalloc(&c->d_iv, want * 4));
+        SST_CUDA_TRY(cudaMalloc(&c->d_ie0, want * 4));
+        c->items_cap = want;
+      }
+      SST_LAUNCH(k_cbfs_items, blocks_for(qn), kTB, 0, s, q, qn, c->d_deg, c->d_ik);
+      A.reset();
+      SST_CUDA_TRY((scan<uint32_t, OpAdd>(c->d_ik, c->d_ikoff, qn, 0u, OpAdd{}, true,
+                                          false, nullptr, A, s)));
+      SST_LAUNCH(k_cbfs_expand, blocks_for(qn), kTB, 0, s, q, qn, c->d_ik, c->d_ikoff,
+                 c->d_iv, c->d_ie0);
+      SST_LAUNCH(k_cbfs_push, warp_blocks(qitems), kTB, 0, s, dc, c->d_iv, c->d_ie0, qitems,
+                 d_depth, nq, c->d_cnt, lvl);
+    }
+    SST_CUDA_TRY(cudaMemcpyAsync(c->h_cnt, c->d_cnt, 24, cudaMemcpyDeviceToHost, s));
+    SST_CUDA_TRY(cudaStreamSynchronize(s));
+    qn = c->h_cnt[0];
+    qdeg = c->h_cnt[1];
+    qitems = c->h_cnt[2];
+    std::swap(q, nq);
+  }
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+// CC(g) on the snapshot: label = the component's smallest vertex id
+sst_status compact_cc(sst_compact *c, uint32_t *d_labels) {
+  SST_CUDA_TRY(cudaSetDevice(c->device));
+  sst_status st = compact_trav_buffers(c);
+  if (st != SST_OK) return st;
+  cudaStream_t s = c->stream;
+  const uint32_t n = c->n;
+  if (n == 0) return SST_OK;
+  const DCompact dc = c->view();
+  unsigned long long *giant = c->d_cnt, *err = c->d_cnt + 1;
+  SST_CUDA_TRY(cudaMemsetAsync(c->d_cnt, 0, 16, s));
+  SST_LAUNCH(k_iota, blocks_for(n), kTB, 0, s, d_labels, n);
+  for (uint32_t r = 0; r < 2; r++) {
+    SST_LAUNCH(k_ccc_sample, blocks_for(n), kTB, 0, s, dc, r, d_labels, err);
+    SST_LAUNCH(k_cc_compress, blocks_for(n), kTB, 0, s, d_labels, n);
+  }
+  SST_LAUNCH(k_cc_giant, 1, 1024, 0, s, d_labels, n, giant);
+  if (c->nsmall)
+    SST_LAUNCH(k_ccc_rest_small, blocks_for(c->nsmall), kTB, 0, s, dc, c->d_sdesc,
+               c->d_small, c->nsmall, giant, d_labels, err);
+  if (c->nchunks)
+    SST_LAUNCH(k_ccc_rest_chunks, warp_blocks(c->nchunks), kTB, 0, s, dc, c->d_cv, c->d_c0,
+               c->nchunks, giant, d_labels, err);
+  SST_LAUNCH(k_cc_compress, blocks_for(n), kTB, 0, s, d_labels, n);
+  SST_CUDA_TRY(cudaMemcpyAsync(c->h_cnt, c->d_cnt, 16, cudaMemcpyDeviceToHost, s));
+  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  SST_CUDA_TRY(cudaGetLastError());
+  if (c->h_cnt[1]) {
+    set_error_message("connected components: %llu links gave up",
+                      (unsigned long long)c->h_cnt[1]);
+    return SST_ETIMEDOUT;
+  }
+  return SST_OK;
+}
+
 // device bytes the snapshot holds: its rows and index, and (after a
-// PageRank) the work lists and iteration buffers
+// PageRank, BFS or CC) the work lists and iteration buffers
 void compact_bytes(const sst_compact *c, uint64_t *storage, uint64_t *total) {
   const uint64_t n = c->n;
   *storage = (n + 1) * 8 + n * 4 + c->nbytes;
   uint64_t t = *storage + c->nsmall * 12 + c->nchunks * 8 + n * 12 + c->arena.cap;
   if (c->d_ca) t += n * 24 + std::max<uint64_t>(c->nchunks, 1) * 8;
+  if (c->d_cnt) t += n * 16 + n / 8 + c->items_cap * 8 + 64;  // BFS / CC buffers
   *total = t;
 }
 
@@ -784,6 +1082,37 @@ sst_status compact_dev_check(sst_compact *c) {
   }
   return SST_OK;
 }
+
+// traversal output of n entries of T: written on the device directly, or
+// through a temporary for a host pointer
+template <typename T, typename Fn>
+sst_status compact_out(sst_compact *c, T *out, uint32_t flags, const char *what,
+                              Fn run) {
+  sst_status st = compact_dev_check(c);
+  if (st != SST_OK) return st;
+  if (!out) return SST_EINVAL;
+  if (c->n != c->width) {  // column ids index per-row arrays
+    sst::set_error_message("%s needs as many rows as columns (%u x %u)", what, c->n,
+                           c->width);
+    return SST_EINVAL;
+  }
+  SST_CUDA_TRY(cudaSetDevice(c->device));
+  if (flags & SST_DEVICE_PTR) {
+    st = run(out);
+    if (st == SST_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) st = SST_EDEVICE;
+    return st;
+  }
+  T *d = nullptr;
+  SST_CUDA_TRY(cudaMalloc(&d, std::max<uint64_t>(c->n, 1) * sizeof(T)));
+  st = run(d);
+  if (st == SST_OK) {
+    cudaMemcpyAsync(out, d, (uint64_t)c->n * sizeof(T), cudaMemcpyDeviceToHost, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) st = SST_EDEVICE;
+  }
+  cudaFree(d);
+  return st;
+}
+
 
 }  // namespace
 
@@ -924,6 +1253,20 @@ sst_status sst_compact_pagerank(sst_compact *c, uint32_t iters, double damping,
   }
   cudaFree(d);
   return st;
+}
+
+sst_status sst_compact_bfs(sst_compact *c, uint32_t src, int32_t *depths, uint32_t flags) {
+  if (c && src >= c->n) {
+    sst::set_error_message("source out of range");
+    return SST_EINVAL;
+  }
+  return compact_out(c, depths, flags, "sst_compact_bfs",
+                     [&](int32_t *d) { return sst::compact_bfs(c, src, d); });
+}
+
+sst_status sst_compact_cc(sst_compact *c, uint32_t *labels, uint32_t flags) {
+  return compact_out(c, labels, flags, "sst_compact_cc",
+                     [&](uint32_t *d) { return sst::compact_cc(c, d); });
 }
 
 sst_status sst_compact_set_stream(sst_compact *c, void *stream) {

@@ -175,6 +175,14 @@ constexpr int kTile = kThreads * kItems;  // 4096
 // quarter of the keys, so a pass's dependent chain is shorter.
 constexpr int kSmallItems = 4;
 constexpr uint64_t kSmallTileKeys = 256ull * kThreads * kSmallItems;  // 2^18
+// The one-sweep passes (sorts below 2^30 keys) keep 1024-key tiles up to
+// this many keys: a tile's look-back is linear in the tiles before it, and
+// shorter per-tile chains at three blocks an SM beat fewer, longer ones
+// (4096-key tiles of 127-register blocks fill under a fifth of an SM's warp
+// slots)
+constexpr uint64_t kOsSmallTileKeys = 1ull << 22;
+
+inline bool os_small_tiles(uint64_t n) { return n <= kOsSmallTileKeys && n < (1ull << 30); }
 constexpr int kRadix = 256;
 constexpr uint32_t kNoDigit = 0xffffffffu;  // an item past the end
 // Sorts of at most this many tiles run one launch per pass: every block
@@ -462,7 +470,7 @@ __device__ __forceinline__ uint32_t os_count_tile(const uint64_t *in, uint64_t n
 }
 
 template <bool KV, int IT>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, IT == kSmallItems ? 3 : 2)
 k_scatter_os(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
              uint64_t n, int shift, const uint32_t *__restrict__ totals,
              uint32_t *__restrict__ status, const uint32_t *__restrict__ vin,
@@ -636,7 +644,8 @@ constexpr int kSmallSortKV = 1024;
 }  // namespace
 
 size_t radix_sort_scratch_bytes(uint64_t n) {
-  const uint64_t tile = n <= kSmallTileKeys ? (uint64_t)kThreads * kSmallItems : kTile;
+  const uint64_t tile = (n <= kSmallTileKeys || os_small_tiles(n))
+                            ? (uint64_t)kThreads * kSmallItems : kTile;
   uint64_t nblocks = (n + tile - 1) / tile;
   uint64_t hn = nblocks * kRadix;
   // the one-sweep form: digit totals and up to eight passes' tile status;
@@ -782,7 +791,7 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
                n, bits, d_n);
     return cudaGetLastError();
   }
-  if (!vals && n <= kSmallTileKeys)
+  if ((!vals && n <= kSmallTileKeys) || os_small_tiles(n))
     return radix_sort_tiles<kSmallItems>(keys, tmp, vals, vtmp, n, bits, arena, s, result,
                                          vresult, d_n);
   return radix_sort_tiles<kItems>(keys, tmp, vals, vtmp, n, bits, arena, s, result, vresult,

@@ -1,8 +1,10 @@
 """Byte-width snapshot (sst_compact_*) against the graph it was taken from
 and the layout restatement (oracle/compact.py): the decoded CSR bit-exact,
 rows per key width and storage bytes as the restatement predicts,
-membership answers equal, and PageRank equal bit for bit to the PMA
-PageRank (the same fixed-point arithmetic over the same rows)."""
+membership answers equal, PageRank equal bit for bit to the PMA
+PageRank (the same fixed-point arithmetic over the same rows), and, on
+symmetric graphs, BFS depths and CC labels equal to the graph's and the
+oracle's."""
 import numpy as np
 import pytest
 
@@ -134,3 +136,74 @@ def test_weighted_graph_refused(sg):
     with pytest.raises(sg.SSTError):
         sg.CompactGraph(g)
     g.close()
+
+
+def check_traversals(sg, g, n, srcs):
+    """BFS and CC on the snapshot = on the live graph = the oracle."""
+    off, cols = g.csr()
+    o = oracle.OracleGraph(n)
+    rows = np.repeat(np.arange(n, dtype=np.uint32), np.diff(off).astype(np.int64))
+    o.insert_batch(np.stack([rows, cols], 1))
+    c = sg.CompactGraph(g)
+    try:
+        for s in srcs:
+            want = o.bfs(int(s))
+            assert np.array_equal(c.bfs(int(s)), want), s
+            assert np.array_equal(sg.BFS(g, int(s), depths=True), want), s
+        want = o.cc()
+        assert np.array_equal(c.cc(), want)
+        assert np.array_equal(sg.CC(g), want)
+    finally:
+        c.close()
+
+
+def test_traversals_rmat(sg):
+    n = 1 << 16
+    g = sg.SparseMatrixV(n)
+    g.insert_batch(oracle.symmetrize(oracle.rmat(16, 16 * n, seed=1)))
+    deg = g.degrees()
+    check_traversals(sg, g, n, [0, int(np.argmax(deg)), int(np.nonzero(deg)[0][-1]), 12345])
+    g.close()
+
+
+def test_traversals_every_width_symmetric(sg):
+    """Rows of every key width with bucket directories (2^20 columns), made
+    symmetric; several components."""
+    n = 1 << 20
+    rng = np.random.default_rng(3)
+    sizes = {1: 70000, 2: 65536, 3: 300, 4: 256, 5: 4, 6: 3, 9: 5000}
+    hubs = rows_at(rng, n, sizes)
+    rand = rng.integers(0, n, (200000, 2)).astype(np.uint32)
+    g = sg.SparseMatrixV(n)
+    g.insert_batch(oracle.symmetrize(np.concatenate([hubs, rand])))
+    info = check_snapshot(sg, g, n)
+    assert all(info["rows_per_width"][b] > 0 for b in (1, 2, 3, 4))
+    check_traversals(sg, g, n, [1, 2, 9, 5, int(rand[0, 0]), n - 1])
+    g.close()
+
+
+def test_traversals_device_arrays_and_refusal(sg):
+    torch = pytest.importorskip("torch")
+    n = 1 << 12
+    g = sg.SparseMatrixV(n)
+    g.insert_batch(oracle.symmetrize(oracle.rmat(12, 20000, seed=8)))
+    c = sg.CompactGraph(g)
+    d = torch.empty(n, dtype=torch.int32, device="cuda")
+    c.bfs(7, out=d)
+    assert np.array_equal(d.cpu().numpy(), sg.BFS(g, 7, depths=True))
+    lab = torch.empty(n, dtype=torch.int32, device="cuda")
+    c.cc(out=lab)
+    assert np.array_equal(lab.cpu().numpy().view(np.uint32), sg.CC(g))
+    with pytest.raises(sg.SSTError):
+        c.bfs(n)
+    c.close()
+    g.close()
+    w = sg.SparseMatrixV(8, 1 << 20)
+    w.insert_batch(np.array([[1, 5]], np.uint32))
+    cw = sg.CompactGraph(w)
+    for call in (lambda: cw.bfs(1), lambda: cw.cc()):
+        with pytest.raises(sg.SSTError) as e:
+            call()
+        assert "rows as columns" in str(e.value)
+    cw.close()
+    w.close()
