@@ -436,6 +436,40 @@ def main():
         sg.PR_S(g, a.pr_iters, out=ref)
         torch.cuda.synchronize()
         pprof = sg.profile_collect()
+        # the other traversals on the snapshot beside the live graph's
+        trav = {}
+
+        def timed(fn):
+            fn()
+            torch.cuda.synchronize()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            r = fn()
+            s1.record(stream)
+            s1.synchronize()
+            return s0.elapsed_time(s1), r
+
+        d1 = torch.empty(n, dtype=torch.int32, device="cuda")
+        d2 = torch.empty(n, dtype=torch.int32, device="cuda")
+        for name, on_snap, on_live, same in (
+                ("bfs", lambda: c.bfs(0, out=d1), lambda: sg.BFS(g, 0, depths=True, out=d2),
+                 lambda: bool(torch.equal(d1, d2))),
+                ("cc", lambda: c.cc(out=d1), lambda: sg.CC(g, out=d2),
+                 lambda: bool(torch.equal(d1, d2)))):
+            ms_s, _ = timed(on_snap)
+            ms_l, _ = timed(on_live)
+            trav[name] = {"snapshot_ms": ms_s, "graph_ms": ms_l, "equal": same()}
+        b1 = torch.empty(n, dtype=torch.float64, device="cuda")
+        b2 = torch.empty(n, dtype=torch.float64, device="cuda")
+        ms_s, _ = timed(lambda: c.bc(0, out=b1))
+        ms_l, _ = timed(lambda: sg.BC(g, 0, out=b2))
+        trav["bc"] = {"snapshot_ms": ms_s, "graph_ms": ms_l,
+                      "within_1e-9": bool((b1 - b2).abs().max().item()
+                                          <= 1e-9 * b2.abs().max().item())}
+        ms_s, t_s = timed(lambda: c.tc())
+        ms_l, t_l = timed(lambda: sg.TC(g))
+        trav["tc"] = {"snapshot_ms": ms_s, "graph_ms": ms_l, "equal": t_s == t_l}
+        del d1, d2, b1, b2
         # the live graph's storage: vertex table (base, cap, deg) and the
         # slab's used slots with their leaf counts
         nslots = ctypes.c_uint64()
@@ -452,6 +486,7 @@ def main():
                 "pagerank_ms_per_iter": t_iter * 1e3,
                 "pagerank_bytes_per_iter": info["storage_bytes"] + 24 * n,
                 "pagerank_equal_to_pma": equal,
+                "traversals": trav,
                 "kernels": cprof, "pma_kernels": pprof}
 
     def measure_bfs():

@@ -320,6 +320,16 @@ SST_API sst_status sst_compact_bfs(sst_compact *c, uint32_t src, int32_t *depths
 /* CC(g)  test.hpp:571 on the snapshot: each label the component's smallest
  * vertex id, equal to sst_cc's */
 SST_API sst_status sst_compact_cc(sst_compact *c, uint32_t *labels, uint32_t flags);
+/* BC(g, src)  test.hpp:547 on the snapshot: single-source dependency scores,
+ * within 1e-9 relative of sst_bc's (FP64 sums in another order); the rows
+ * are decoded into temporary device memory */
+SST_API sst_status sst_compact_bc(sst_compact *c, uint32_t src, double *out,
+                                  uint32_t flags);
+/* TC(g)  test.hpp:606 on the snapshot: triangles (each once), equal to
+ * sst_tc's; per_vertex may be NULL (the snapshot's rows are decoded and
+ * oriented into temporary device memory) */
+SST_API sst_status sst_compact_tc(sst_compact *c, uint64_t *total, uint64_t *per_vertex,
+                                  uint32_t flags);
 /* the stream the snapshot's work runs on (NULL: its own), as sst_set_stream */
 SST_API sst_status sst_compact_set_stream(sst_compact *c, void *stream);
 SST_API sst_status sst_compact_sync(sst_compact *c);

@@ -154,6 +154,8 @@ SIGNATURES = {
     "sst_compact_pagerank": (_i32, [_vp, _u32, _dbl, _vp, _u32]),
     "sst_compact_bfs": (_i32, [_vp, _u32, _vp, _u32]),
     "sst_compact_cc": (_i32, [_vp, _vp, _u32]),
+    "sst_compact_tc": (_i32, [_vp, ctypes.POINTER(_u64), _vp, _u32]),
+    "sst_compact_bc": (_i32, [_vp, _u32, _vp, _u32]),
     "sst_compact_sync": (_i32, [_vp]),
     "sst_compact_set_stream": (_i32, [_vp, _vp]),
     "sst_profile_start": (_i32, [ctypes.c_char_p]),
@@ -738,6 +740,24 @@ class CompactGraph:
         p, flags = _ptr(buf)
         _check(lib().sst_compact_cc(self._h, p, flags))
         return buf
+
+    def bc(self, src: int, out=None):
+        """Single-source dependency scores, as BC(g, src) (within 1e-9)."""
+        buf = np.empty(self.rows, np.float64) if out is None else out
+        p, flags = _ptr(buf)
+        _check(lib().sst_compact_bc(self._h, int(src), p, flags))
+        return buf
+
+    def tc(self, per_vertex: bool = False):
+        """Triangle count (and per-vertex counts), as TC(g)."""
+        total = ctypes.c_uint64()
+        if per_vertex:
+            pv = np.empty(self.rows, np.uint64)
+            _check(lib().sst_compact_tc(self._h, ctypes.byref(total),
+                                        ctypes.c_void_p(pv.ctypes.data), HOST_PTR))
+            return total.value, pv
+        _check(lib().sst_compact_tc(self._h, ctypes.byref(total), None, HOST_PTR))
+        return total.value
 
     def sync(self):
         _check(lib().sst_compact_sync(self._h))

@@ -27,10 +27,12 @@
 // bit for bit.
 #include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "ccshared.cuh"
 #include "graph.cuh"
 #include "prfixed.cuh"
+#include "tcshared.cuh"
 
 namespace sst {
 namespace {
@@ -667,6 +669,101 @@ __global__ void k_cbfs_pull_chunks(DCompact c, const uint32_t *__restrict__ cv,
   }
 }
 
+// ---- triangle counting: the decoded rows oriented towards the higher
+// (degree, id) rank, then the shared counting kernel (tcshared.cuh)
+// warp per row: keep[e] = 1 where the row's e-th id ranks above the row
+__global__ void k_ctc_keep(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+                           const uint32_t *__restrict__ deg, uint32_t n,
+                           uint32_t *__restrict__ keep) {
+  const uint64_t v = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (v >= n) return;
+  for (uint64_t e = off[v] + lane; e < off[v + 1]; e += 32)
+    keep[e] = ranks_above(deg, cols[e], (uint32_t)v) ? 1u : 0u;
+}
+
+__global__ void k_ctc_fill(const uint32_t *__restrict__ cols, const uint32_t *__restrict__ keep,
+                           const uint32_t *__restrict__ pos, uint64_t m,
+                           uint32_t *__restrict__ adj) {
+  const uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < m && keep[e]) adj[pos[e]] = cols[e];
+}
+
+// a row's oriented list starts where its first kept id lands
+__global__ void k_ctc_off(const uint64_t *__restrict__ off, const uint32_t *__restrict__ pos,
+                          uint32_t n, uint64_t m, uint64_t *__restrict__ doff) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v <= n) doff[v] = pos[off[v] < m ? off[v] : m];
+}
+
+// ---- betweenness (Brandes) over the decoded rows, level by level
+__global__ void k_cbc_maxdepth(const int32_t *__restrict__ depth, uint32_t n,
+                               unsigned long long *__restrict__ out) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n && depth[v] >= 0) atomicMax(out, (unsigned long long)depth[v]);
+}
+
+__global__ void k_cbc_count(const int32_t *__restrict__ depth, uint32_t n,
+                            uint32_t *__restrict__ cnt) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n && depth[v] >= 0) atomicAdd(&cnt[depth[v]], 1u);
+}
+
+__global__ void k_cbc_scatter(const int32_t *__restrict__ depth, uint32_t n,
+                              const uint32_t *__restrict__ off, uint32_t *__restrict__ ctr,
+                              uint32_t *__restrict__ list) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n && depth[v] >= 0) list[off[depth[v]] + atomicAdd(&ctr[depth[v]], 1u)] = v;
+}
+
+__global__ void k_cbc_init(double *__restrict__ sigma, double *__restrict__ dep, uint32_t n,
+                           uint32_t src) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  sigma[v] = v == src ? 1.0 : 0.0;
+  dep[v] = 0.0;
+}
+
+// warp per vertex w of level d: sigma(w) = sum of sigma over its neighbours
+// one level up
+__global__ void k_cbc_sigma(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+                            const int32_t *__restrict__ depth, const uint32_t *__restrict__ list,
+                            uint32_t count, int32_t d, double *__restrict__ sigma) {
+  const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= count) return;
+  const uint32_t w = list[i];
+  double acc = 0.0;
+  for (uint64_t e = off[w] + lane; e < off[w + 1]; e += 32) {
+    const uint32_t v = cols[e];
+    if (depth[v] == d - 1) acc += sigma[v];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) sigma[w] = acc;
+}
+
+// warp per vertex v of level d: dep(v) = sum over neighbours w one level
+// down of sigma(v) / sigma(w) * (1 + dep(w))
+__global__ void k_cbc_dep(const uint64_t *__restrict__ off, const uint32_t *__restrict__ cols,
+                          const int32_t *__restrict__ depth, const uint32_t *__restrict__ list,
+                          uint32_t count, int32_t d, const double *__restrict__ sigma,
+                          double *__restrict__ dep) {
+  const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= count) return;
+  const uint32_t v = list[i];
+  const double sv = sigma[v];
+  double acc = 0.0;
+  for (uint64_t e = off[v] + lane; e < off[v + 1]; e += 32) {
+    const uint32_t w = cols[e];
+    if (depth[w] == d + 1) acc += sv / sigma[w] * (1.0 + dep[w]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) dep[v] = acc;
+}
+
 // push: work items of kElemsPerWarp ids of the frontier's rows
 __global__ void k_cbfs_items(const uint32_t *__restrict__ q, uint64_t qn,
                              const uint32_t *__restrict__ deg, uint32_t *__restrict__ k) {
@@ -1024,6 +1121,130 @@ sst_status compact_bfs(sst_compact *c, uint32_t src, int32_t *d_depth) {
   return SST_OK;
 }
 
+// TC(g) on the snapshot: triangles (each once); d_pv (may be null) gets
+// the triangles containing each vertex
+sst_status compact_tc(sst_compact *c, uint64_t *total, uint64_t *d_pv, int sms) {
+  SST_CUDA_TRY(cudaSetDevice(c->device));
+  sst_status st = compact_trav_buffers(c);
+  if (st != SST_OK) return st;
+  cudaStream_t s = c->stream;
+  const uint32_t n = c->n;
+  const uint64_t m = c->m;
+  *total = 0;
+  if (d_pv) SST_CUDA_TRY(cudaMemsetAsync(d_pv, 0, (uint64_t)n * 8, s));
+  if (n == 0 || m == 0) return SST_OK;
+  if (m >= (1ull << 32)) {
+    set_error_message("sst_compact_tc: more than 2^32 stored edges");
+    return SST_EINVAL;
+  }
+  uint64_t *off = nullptr, *doff = nullptr;
+  uint32_t *cols = nullptr, *keep = nullptr, *pos = nullptr, *adj = nullptr;
+  cudaError_t e = cudaMalloc(&off, ((uint64_t)n + 1) * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&doff, ((uint64_t)n + 1) * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&cols, m * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&keep, m * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&pos, (m + 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&adj, m * 4);
+  if (e == cudaSuccess) {
+    st = compact_to_csr(c, off, cols);
+    if (st == SST_OK) {
+      Arena &A = c->arena;
+      e = A.reserve(scan_scratch_bytes(m, 4) + 4096);
+      if (e == cudaSuccess) {
+        A.reset();
+        const DCompact dc = c->view();
+        SST_LAUNCH(k_ctc_keep, warp_blocks(n), kTB, 0, s, off, cols, dc.deg, n, keep);
+        e = scan<uint32_t, OpAdd>(keep, pos, m, 0u, OpAdd{}, true, false, pos + m, A, s);
+        if (e == cudaSuccess) {
+          SST_LAUNCH(k_ctc_fill, blocks_for(m), kTB, 0, s, cols, keep, pos, m, adj);
+          SST_LAUNCH(k_ctc_off, blocks_for((uint64_t)n + 1), kTB, 0, s, off, pos, n, m, doff);
+          e = cudaMemsetAsync(c->d_cnt, 0, 8, s);
+          if (e == cudaSuccess)
+            e = tc_count_launch(doff, adj, n, c->d_cnt,
+                                reinterpret_cast<unsigned long long *>(d_pv), sms, s);
+          if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->h_cnt, c->d_cnt, 8, cudaMemcpyDeviceToHost, s);
+          if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+          if (e == cudaSuccess) *total = c->h_cnt[0];
+        }
+      }
+    }
+  }
+  for (void *p : {(void *)off, (void *)doff, (void *)cols, (void *)keep, (void *)pos,
+                  (void *)adj})
+    if (p) cudaFree(p);
+  if (st != SST_OK) return st;
+  SST_CUDA_TRY(e);
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
+// BC(g, src) on the snapshot: single-source dependencies (Brandes), FP64
+sst_status compact_bc(sst_compact *c, uint32_t src, double *d_dep) {
+  SST_CUDA_TRY(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  const uint32_t n = c->n;
+  const uint64_t m = c->m;
+  int32_t *depth = nullptr;
+  uint64_t *off = nullptr;
+  uint32_t *cols = nullptr, *list = nullptr, *lv = nullptr;
+  double *sigma = nullptr;
+  cudaError_t e = cudaMalloc(&depth, (uint64_t)n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&off, ((uint64_t)n + 1) * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&cols, std::max<uint64_t>(m, 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&list, (uint64_t)n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&sigma, (uint64_t)n * 8);
+  sst_status st = SST_OK;
+  std::vector<uint32_t> ho;
+  if (e == cudaSuccess) st = compact_bfs(c, src, depth);
+  if (e == cudaSuccess && st == SST_OK) st = compact_to_csr(c, off, cols);
+  if (e == cudaSuccess && st == SST_OK) {
+    SST_LAUNCH(k_cbc_init, blocks_for(n), kTB, 0, s, sigma, d_dep, n, src);
+    e = cudaMemsetAsync(c->d_cnt, 0, 8, s);
+    if (e == cudaSuccess)
+      SST_LAUNCH(k_cbc_maxdepth, blocks_for(n), kTB, 0, s, depth, n, c->d_cnt);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_cnt, c->d_cnt, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    const uint32_t D = (uint32_t)c->h_cnt[0];
+    // level counts, offsets and cursors
+    if (e == cudaSuccess) e = cudaMalloc(&lv, 3 * ((uint64_t)D + 2) * 4);
+    uint32_t *cnt = lv, *loff = lv + D + 2, *ctr = loff + D + 2;
+    if (e == cudaSuccess) e = cudaMemsetAsync(lv, 0, 3 * ((uint64_t)D + 2) * 4, s);
+    if (e == cudaSuccess) SST_LAUNCH(k_cbc_count, blocks_for(n), kTB, 0, s, depth, n, cnt);
+    std::vector<uint32_t> hc(D + 2);
+    ho.assign(D + 2, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hc.data(), cnt, (D + 1) * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    uint32_t acc = 0;
+    for (uint32_t d = 0; d <= D; d++) {
+      ho[d] = acc;
+      acc += hc[d];
+    }
+    ho[D + 1] = acc;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(loff, ho.data(), (D + 2) * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      SST_LAUNCH(k_cbc_scatter, blocks_for(n), kTB, 0, s, depth, n, loff, ctr, list);
+    for (uint32_t d = 1; e == cudaSuccess && d <= D; d++) {
+      const uint32_t k = ho[d + 1] - ho[d];
+      if (k) SST_LAUNCH(k_cbc_sigma, warp_blocks(k), kTB, 0, s, off, cols, depth, list + ho[d],
+                        k, (int32_t)d, sigma);
+    }
+    for (int64_t d = D; e == cudaSuccess && d >= 0; d--) {
+      const uint32_t k = ho[d + 1] - ho[d];
+      if (k) SST_LAUNCH(k_cbc_dep, warp_blocks(k), kTB, 0, s, off, cols, depth, list + ho[d],
+                        k, (int32_t)d, sigma, d_dep);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  for (void *p : {(void *)depth, (void *)off, (void *)cols, (void *)list, (void *)lv,
+                  (void *)sigma})
+    if (p) cudaFree(p);
+  if (st != SST_OK) return st;
+  SST_CUDA_TRY(e);
+  SST_CUDA_TRY(cudaGetLastError());
+  return SST_OK;
+}
+
 // CC(g) on the snapshot: label = the component's smallest vertex id
 sst_status compact_cc(sst_compact *c, uint32_t *d_labels) {
   SST_CUDA_TRY(cudaSetDevice(c->device));
@@ -1262,6 +1483,37 @@ sst_status sst_compact_bfs(sst_compact *c, uint32_t src, int32_t *depths, uint32
   }
   return compact_out(c, depths, flags, "sst_compact_bfs",
                      [&](int32_t *d) { return sst::compact_bfs(c, src, d); });
+}
+
+sst_status sst_compact_tc(sst_compact *c, uint64_t *total, uint64_t *per_vertex,
+                          uint32_t flags) {
+  if (!total) return SST_EINVAL;
+  if (!per_vertex) {
+    sst_status st = compact_dev_check(c);
+    if (st != SST_OK) return st;
+    if (c->n != c->width) {
+      sst::set_error_message("sst_compact_tc needs as many rows as columns (%u x %u)", c->n,
+                             c->width);
+      return SST_EINVAL;
+    }
+    int sms = 0;
+    SST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    return sst::compact_tc(c, total, nullptr, sms);
+  }
+  return compact_out(c, per_vertex, flags, "sst_compact_tc", [&](uint64_t *d) {
+    int sms = 0;
+    SST_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    return sst::compact_tc(c, total, d, sms);
+  });
+}
+
+sst_status sst_compact_bc(sst_compact *c, uint32_t src, double *out, uint32_t flags) {
+  if (c && src >= c->n) {
+    sst::set_error_message("source out of range");
+    return SST_EINVAL;
+  }
+  return compact_out(c, out, flags, "sst_compact_bc",
+                     [&](double *d) { return sst::compact_bc(c, src, d); });
 }
 
 sst_status sst_compact_cc(sst_compact *c, uint32_t *labels, uint32_t flags) {

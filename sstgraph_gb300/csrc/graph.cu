@@ -130,6 +130,7 @@ __global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
                             unsigned long long *__restrict__ invalid,
                             const uint32_t *__restrict__ w,
                             uint32_t *__restrict__ wv) {
+  pdl_wait();
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b) return;
   // weighted graphs: the pair's value (1 when the call gives none) rides
@@ -153,6 +154,7 @@ k_make_keys_packed(const uint32_t *__restrict__ pairs, uint64_t b, uint32_t n,
                    uint64_t *__restrict__ keys,
                    unsigned long long *__restrict__ invalid,
                    uint32_t *__restrict__ nkeys) {
+  pdl_wait();
   __shared__ uint32_t s_warp[8];
   __shared__ uint32_t s_base;
   const uint64_t t0 = (uint64_t)blockIdx.x * (256 * kPackItems);
@@ -210,6 +212,7 @@ __global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
                          const uint32_t *__restrict__ wv,
                          uint64_t *__restrict__ lS, uint32_t *__restrict__ lc,
                          const uint32_t *__restrict__ nkeys) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b) return;
   const uint64_t sent = (uint64_t)g.n << dbits;
@@ -254,6 +257,7 @@ __global__ void k_pack(const uint64_t *__restrict__ keys,
                        const uint32_t *__restrict__ wv, uint32_t *__restrict__ p_w,
                        const uint64_t *__restrict__ lS, const uint32_t *__restrict__ lc,
                        uint64_t *__restrict__ p_S, uint32_t *__restrict__ p_c) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b || !flag[i]) return;
   uint64_t k = keys[i];
@@ -269,6 +273,7 @@ __global__ void k_pack(const uint64_t *__restrict__ keys,
 __global__ void k_group_flags(const uint64_t *__restrict__ p_ul,
                               const uint32_t *__restrict__ d_nitems, uint64_t b,
                               uint32_t *__restrict__ gflag) {
+  pdl_wait();
   uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= b) return;
   uint32_t n = *d_nitems;
@@ -312,6 +317,7 @@ __global__ void k_classify_insert(DGraph g, const uint64_t *__restrict__ p_ul,
                                   uint32_t *__restrict__ gw1,
                                   uint32_t *__restrict__ climb,
                                   uint32_t *__restrict__ nclimb) {
+  pdl_wait();
   const uint32_t ng = *d_ngroups;
   GRID_STRIDE(gid, ng) {
     uint32_t j0 = g_start[gid], k = g_start[gid + 1] - j0;
@@ -373,6 +379,7 @@ k_leaf_delete(DGraph g, uint32_t lo_leaf, const uint64_t *__restrict__ p_ul,
               uint8_t *__restrict__ gtype, uint8_t *__restrict__ glev,
               uint32_t *__restrict__ gw0, uint32_t *__restrict__ gw1,
               uint32_t *__restrict__ climb, uint32_t *__restrict__ nclimb) {
+  pdl_wait();
   const int lane = threadIdx.x & 31;
   constexpr int Q = kGroupsPerWarp;
   const uint32_t ng = *d_ngroups;
@@ -464,6 +471,7 @@ __global__ void k_climb(DGraph g, PmaParams p, bool insert,
                         const uint32_t *__restrict__ nclimb,
                         uint8_t *__restrict__ gtype, uint8_t *__restrict__ glev,
                         uint32_t *__restrict__ gw0, uint32_t *__restrict__ gw1) {
+  pdl_wait();
   const int lane = threadIdx.x & 31;
   const uint32_t nc = *nclimb, nitems = *d_nitems;
   for (uint64_t ci = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -537,6 +545,7 @@ __global__ void k_dom_keys(const uint64_t *__restrict__ p_ul,
                            const uint32_t *__restrict__ d_ngroups, uint64_t gmax,
                            uint64_t *__restrict__ fkey,
                            uint64_t *__restrict__ bkey) {
+  pdl_wait();
   uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= gmax) return;
   uint64_t f = 0, bk = ~0ull;
@@ -561,6 +570,7 @@ __global__ void k_dom_classify(const uint64_t *__restrict__ p_ul,
                                const uint64_t *__restrict__ bscan,
                                const uint32_t *__restrict__ d_ngroups,
                                uint64_t gmax, uint64_t *__restrict__ mt) {
+  pdl_wait();
   uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= gmax) return;
   uint32_t mf = 0, tf = 0;
@@ -590,6 +600,7 @@ __global__ void k_emit(const uint64_t *__restrict__ mt,
                        const uint32_t *__restrict__ g_start,
                        uint64_t *__restrict__ merge_jk,
                        uint32_t *__restrict__ task_group) {
+  pdl_wait();
   uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= gmax) return;
   const uint64_t f = mt[gid], p = mtpos[gid];
@@ -635,6 +646,7 @@ __global__ void k_task_setup(DGraph g, uint64_t inv_fill, bool insert,
                              const uint32_t *__restrict__ d_nitems,
                              uint64_t gmax, Tasks t,
                              uint32_t *__restrict__ class_cnt) {
+  pdl_wait();
   const int lane = threadIdx.x & 31;
   const uint32_t ntasks = *d_ntasks, nitems = *d_nitems;
   for (uint64_t tid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -699,6 +711,7 @@ k_leaf_merge(DGraph g, const uint32_t *__restrict__ p_x,
              const uint64_t *__restrict__ p_S, const uint32_t *__restrict__ p_c,
              const uint64_t *__restrict__ merge_jk, const uint32_t *__restrict__ d_nmerge,
              const uint32_t *__restrict__ p_w) {
+  pdl_wait();
   const int lane = threadIdx.x & 31;
   constexpr int Q = kGroupsPerWarp;
   const uint32_t nmerge = *d_nmerge;
@@ -767,6 +780,7 @@ k_leaf_merge(DGraph g, const uint32_t *__restrict__ p_x,
 // all ones beforehand)
 __global__ void k_task_index(Tasks t, uint32_t ntasks, uint32_t *__restrict__ stask,
                              uint32_t *__restrict__ dtask, uint32_t *__restrict__ itask) {
+  pdl_wait();
   const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (w >= ntasks) return;
@@ -780,6 +794,7 @@ __global__ void k_task_index(Tasks t, uint32_t ntasks, uint32_t *__restrict__ st
 __global__ void k_src_counts(DGraph g, Tasks t, uint32_t ntasks,
                              uint64_t nsrc_total, uint64_t *__restrict__ scnt,
                              const uint32_t *__restrict__ stask) {
+  pdl_wait();
   uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsrc_total) return;
   uint64_t tau = stask[s];
@@ -795,6 +810,7 @@ __global__ void k_gather_old(DGraph g, Tasks t, uint32_t ntasks,
                              const uint32_t *__restrict__ p_x,
                              uint32_t *__restrict__ stage,
                              const uint32_t *__restrict__ stask) {
+  pdl_wait();
   uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (s >= nsrc_total) return;
@@ -823,6 +839,7 @@ __global__ void k_gather_new(DGraph g, Tasks t, uint32_t ntasks,
                              const uint32_t *__restrict__ p_x, uint32_t nitems,
                              uint32_t *__restrict__ stage,
                              const uint32_t *__restrict__ itask) {
+  pdl_wait();
   uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nitems || ntasks == 0) return;
   const uint32_t tau = itask[j];
@@ -872,6 +889,7 @@ __global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
                                const uint64_t *__restrict__ class_start,
                                const uint32_t *__restrict__ stage,
                                const uint32_t *__restrict__ dtask) {
+  pdl_wait();
   uint64_t d = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (d >= ndst_total) return;
@@ -908,6 +926,7 @@ __global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
 
 __global__ void k_finalize(DGraph g, Tasks t, uint32_t ntasks,
                            const uint64_t *__restrict__ class_start) {
+  pdl_wait();
   uint64_t tau = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (tau >= ntasks || t.type[tau] != kResize) return;
   uint32_t u = t.u[tau];
@@ -919,6 +938,7 @@ __global__ void k_finalize(DGraph g, Tasks t, uint32_t ntasks,
 __global__ void k_deg_add(DGraph g, const uint64_t *__restrict__ p_ul,
                           const uint32_t *__restrict__ g_start,
                           const uint32_t *__restrict__ d_ngroups, uint64_t gmax) {
+  pdl_wait();
   uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= gmax || gid >= *d_ngroups) return;
   uint32_t u = (uint32_t)(p_ul[g_start[gid]] >> 32);
@@ -928,6 +948,7 @@ __global__ void k_deg_add(DGraph g, const uint64_t *__restrict__ p_ul,
 // ---------------------------------------------------------------- repack
 __global__ void k_class_count(const uint32_t *__restrict__ cap, uint32_t n,
                               uint32_t *__restrict__ cnt) {
+  pdl_wait();
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n || cap[v] == 0) return;
   atomicAdd(&cnt[log2_floor(cap[v])], 1u);
@@ -937,6 +958,7 @@ __global__ void k_repack_assign(const uint32_t *__restrict__ cap, uint32_t n,
                                 const uint64_t *__restrict__ class_start,
                                 uint32_t *__restrict__ ctr,
                                 uint64_t *__restrict__ newbase) {
+  pdl_wait();
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   uint32_t c = cap[v];
@@ -957,6 +979,7 @@ __global__ void k_repack_copy(const uint32_t *__restrict__ cap, uint32_t n,
                               uint8_t *__restrict__ nlcnt,
                               const uint32_t *__restrict__ ovals,
                               uint32_t *__restrict__ nvals) {
+  pdl_wait();
   uint64_t v = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (v >= n) return;
@@ -1191,7 +1214,7 @@ sst_status repack(sst_graph *g, uint64_t extra) {
   uint64_t *cstart = reinterpret_cast<uint64_t *>(tmp + 256);
   uint64_t *newbase = reinterpret_cast<uint64_t *>(tmp + 512);
   SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, kNumClasses * 8, s));
-  if (n) SST_LAUNCH(k_class_count, blocks_for(n), kTB, 0, s, g->d_cap, n, cnt);
+  if (n) SST_LAUNCH_PDL(k_class_count, blocks_for(n), kTB, 0, s, g->d_cap, n, cnt);
   uint32_t hcnt[kNumClasses];
   SST_CUDA_TRY(cudaMemcpyAsync(hcnt, cnt, sizeof(hcnt), cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1221,9 +1244,9 @@ sst_status repack(sst_graph *g, uint64_t extra) {
   }
   SST_CUDA_TRY(cudaMemcpyAsync(cstart, hstart, sizeof(hstart), cudaMemcpyHostToDevice, s));
   if (n) {
-    SST_LAUNCH(k_repack_assign, blocks_for(n), kTB, 0, s, g->d_cap, n, cstart,
+    SST_LAUNCH_PDL(k_repack_assign, blocks_for(n), kTB, 0, s, g->d_cap, n, cstart,
                cnt + kNumClasses, newbase);
-    SST_LAUNCH(k_repack_copy, warp_blocks(n), kTB, 0, s, g->d_cap, n, g->d_base,
+    SST_LAUNCH_PDL(k_repack_copy, warp_blocks(n), kTB, 0, s, g->d_cap, n, g->d_base,
                newbase, g->d_slots, g->d_lcnt, nslots_, nlcnt, g->d_vals, nvals);
     SST_CUDA_TRY(cudaMemcpyAsync(g->d_base, newbase, (uint64_t)n * 8, cudaMemcpyDeviceToDevice, s));
   }
@@ -1466,11 +1489,11 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     // n, one bit fewer to sort when n is a power of two
     nkeys = wt ? nullptr : &P->n_keys;
     if (wt)
-      SST_LAUNCH_B(16 * b, k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n,
+      SST_LAUNCH_PDL_B(16 * b, k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n,
                    g->width, dbits, insert && !g->keep_loops, keys,
                    reinterpret_cast<unsigned long long *>(&P->invalid), d_w, wv);
     else
-      SST_LAUNCH_B(16 * npairs, k_make_keys_packed, blocks_for(npairs, kTB * kPackItems),
+      SST_LAUNCH_PDL_B(16 * npairs, k_make_keys_packed, blocks_for(npairs, kTB * kPackItems),
                    kTB, 0, s, d_pairs, npairs, g->n, g->width, dbits,
                    insert && !g->keep_loops, keys,
                    reinterpret_cast<unsigned long long *>(&P->invalid), nkeys);
@@ -1485,7 +1508,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   auto fork_merges = [&](cudaStream_t from) -> sst_status {
     SST_CUDA_TRY(cudaEventRecord(g->fork_ev, from));
     SST_CUDA_TRY(cudaStreamWaitEvent(g->side, g->fork_ev, 0));
-    SST_LAUNCH(k_leaf_merge, std::min(warp_blocks((b + 31) / 32), (unsigned)g->sms * 8),
+    SST_LAUNCH_PDL(k_leaf_merge, std::min(warp_blocks((b + 31) / 32), (unsigned)g->sms * 8),
                kTB, 0, g->side, dg, p_x, p_S, p_c, merge_jk, &P->n_merge, p_w);
     SST_CUDA_TRY(cudaEventRecord(g->merge_done, g->side));
     join.ev = g->merge_done;
@@ -1519,13 +1542,13 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     }
     // 3-5: locate, pack, group
     // sorted key in (8 B), flag and leaf out (8 B)
-    SST_LAUNCH_B(16 * b, k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg,
+    SST_LAUNCH_PDL_B(16 * b, k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg,
                  insert, flag, leaf, wt ? wv : nullptr, lS, lc, nkeys);
     SST_CUDA_TRY((scan<uint32_t, OpAdd>(flag, pos, b, 0u, OpAdd{}, true, false,
                                         &P->n_items, A, s)));
-    SST_LAUNCH(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,
+    SST_LAUNCH_PDL(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,
                p_ul, p_x, wv, p_w, lS, lc, p_S, p_c);
-    SST_LAUNCH(k_group_flags, blocks_for(b), kTB, 0, s, p_ul, &P->n_items, b, gflag);
+    SST_LAUNCH_PDL(k_group_flags, blocks_for(b), kTB, 0, s, p_ul, &P->n_items, b, gflag);
     SST_CUDA_TRY((scan_epi<uint32_t, OpAdd, GroupStartEpi>(
         gflag, b, 0u, OpAdd{}, true, false, &P->n_groups, A, s, nullptr,
         GroupStartEpi{gflag, &P->n_items, b, g_start}, false)));
@@ -1534,18 +1557,18 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     const unsigned tgrid = std::min(blocks_for(b), cap_blocks);
     const unsigned wgrid = std::min(warp_blocks(b), cap_blocks);
     if (insert) {
-      SST_LAUNCH(k_classify_insert, tgrid, kTB, 0, s, dg, p_ul, g_start,
+      SST_LAUNCH_PDL(k_classify_insert, tgrid, kTB, 0, s, dg, p_ul, g_start,
                  &P->n_groups, gtype, glev, gw0, gw1, climb, &P->n_climb);
     } else {
       // multi-leaf segments have H >= 1 (at least two leaves)
-      SST_LAUNCH(k_leaf_delete, wgrid, kTB, 0, s, dg,
+      SST_LAUNCH_PDL(k_leaf_delete, wgrid, kTB, 0, s, dg,
                  (uint32_t)window_lower(g->params, 0, 1), p_ul, p_x, p_S, p_c,
                  g_start, &P->n_groups, gtype, glev, gw0, gw1, climb, &P->n_climb);
     }
-    SST_LAUNCH(k_climb, wgrid, kTB, 0, s, dg, g->params, insert, p_ul, g_start,
+    SST_LAUNCH_PDL(k_climb, wgrid, kTB, 0, s, dg, g->params, insert, p_ul, g_start,
                &P->n_items, climb, &P->n_climb, gtype, glev, gw0, gw1);
     // 7: dominance
-    SST_LAUNCH(k_dom_keys, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
+    SST_LAUNCH_PDL(k_dom_keys, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
                gw0, gw1, &P->n_groups, b, fkey, bkey);
     // the scans run out of place into merge_jk and mtpos, which hold nothing
     // until the merge/task scan and k_emit below overwrite them
@@ -1554,7 +1577,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                                         nullptr, A, s)));
     SST_CUDA_TRY((scan<uint64_t, OpMin>(bkey, bscan, b, ~0ull, OpMin{}, true, true,
                                         nullptr, A, s)));
-    SST_LAUNCH(k_dom_classify, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
+    SST_LAUNCH_PDL(k_dom_classify, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
                fscan, bscan, &P->n_groups, b, mt);
     // totals land as one word on (n_merge, n_tasks), adjacent in the plan
     static_assert(offsetof(PlanSummary, n_tasks) == offsetof(PlanSummary, n_merge) + 4 &&
@@ -1562,14 +1585,14 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                   "n_merge and n_tasks share one aligned 64-bit word");
     SST_CUDA_TRY((scan<uint64_t, OpAdd>(mt, mtpos, b, 0ull, OpAdd{}, true, false,
                                         reinterpret_cast<uint64_t *>(&P->n_merge), A, s)));
-    SST_LAUNCH(k_emit, blocks_for(b), kTB, 0, s, mt, mtpos, b, g_start, merge_jk,
+    SST_LAUNCH_PDL(k_emit, blocks_for(b), kTB, 0, s, mt, mtpos, b, g_start, merge_jk,
                task_group);
     if (fork && insert) {
       sst_status st = fork_merges(s);
       if (st != SST_OK) return st;
     }
     // 8: plan
-    SST_LAUNCH(k_task_setup, wgrid, kTB, 0, s, dg, fill_inv_q24(g->params.grow_fill), insert,
+    SST_LAUNCH_PDL(k_task_setup, wgrid, kTB, 0, s, dg, fill_inv_q24(g->params.grow_fill), insert,
                p_ul, g_start, gtype, gw0, gw1, task_group, &P->n_tasks, &P->n_items, b, T,
                P->class_cnt);
     SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.total, T.out, b, 0ull, OpAdd{}, true,
@@ -1668,29 +1691,29 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   if (ps.n_tasks) {
     if (itask)
       SST_CUDA_TRY(cudaMemsetAsync(itask, 0xFF, (uint64_t)ps.n_items * 4, s));
-    SST_LAUNCH(k_task_index, warp_blocks(ps.n_tasks), kTB, 0, s, T, ps.n_tasks, stask,
+    SST_LAUNCH_PDL(k_task_index, warp_blocks(ps.n_tasks), kTB, 0, s, T, ps.n_tasks, stask,
                dtask, itask);
     if (ps.src_leaves) {
-      SST_LAUNCH(k_src_counts, blocks_for(ps.src_leaves), kTB, 0, s, dg, T,
+      SST_LAUNCH_PDL(k_src_counts, blocks_for(ps.src_leaves), kTB, 0, s, dg, T,
                  ps.n_tasks, ps.src_leaves, scnt, stask);
       SST_CUDA_TRY((scan<uint64_t, OpAdd>(scnt, spre, ps.src_leaves, 0ull,
                                           OpAdd{}, true, false, nullptr,
                                           g->work, s)));
-      SST_LAUNCH(k_gather_old, warp_blocks(ps.src_leaves), kTB, 0, s, dg, T,
+      SST_LAUNCH_PDL(k_gather_old, warp_blocks(ps.src_leaves), kTB, 0, s, dg, T,
                  ps.n_tasks, ps.src_leaves, spre, p_x, stage, stask);
     }
     if (insert && ps.n_items)
-      SST_LAUNCH(k_gather_new, blocks_for(ps.n_items), kTB, 0, s, dg, T,
+      SST_LAUNCH_PDL(k_gather_new, blocks_for(ps.n_items), kTB, 0, s, dg, T,
                  ps.n_tasks, spre, p_ul, p_x, ps.n_items, stage, itask);
     if (ps.dst_leaves)
-      SST_LAUNCH(k_task_scatter, warp_blocks(ps.dst_leaves), kTB, 0, s, dg, T,
+      SST_LAUNCH_PDL(k_task_scatter, warp_blocks(ps.dst_leaves), kTB, 0, s, dg, T,
                  ps.n_tasks, ps.dst_leaves, cstart, stage, dtask);
-    SST_LAUNCH(k_finalize, blocks_for(ps.n_tasks), kTB, 0, s, dg, T, ps.n_tasks,
+    SST_LAUNCH_PDL(k_finalize, blocks_for(ps.n_tasks), kTB, 0, s, dg, T, ps.n_tasks,
                cstart);
   }
   join.wait();
   if (insert)
-    SST_LAUNCH(k_deg_add, blocks_for(b), kTB, 0, s, dg, p_ul, g_start,
+    SST_LAUNCH_PDL(k_deg_add, blocks_for(b), kTB, 0, s, dg, p_ul, g_start,
                &P->n_groups, b);
   // the staging-rank check of this batch is read back with the next plan
   // (or by sst_sync), so a batch ends without a second host synchronisation
@@ -1719,6 +1742,7 @@ __global__ void k_make_keys_batched(const uint32_t *__restrict__ pairs,
                                     bool drop_loops, uint64_t *__restrict__ keys,
                                     uint32_t *__restrict__ vals,
                                     unsigned long long *__restrict__ invalid) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   uint32_t lo = 0, hi = nb;  // batch: last with boff[b] <= i
@@ -1741,6 +1765,7 @@ __global__ void k_last_op(const uint64_t *__restrict__ keys,
                           const uint32_t *__restrict__ vals, uint64_t N,
                           uint64_t sent, uint32_t *__restrict__ fins,
                           uint32_t *__restrict__ fdel) {
+  pdl_wait();
   uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= N) return;
   uint64_t k = keys[j];
@@ -1753,6 +1778,7 @@ __global__ void k_compact_keys(const uint64_t *__restrict__ keys,
                                const uint32_t *__restrict__ f,
                                const uint32_t *__restrict__ pos, uint64_t N,
                                uint64_t *__restrict__ out) {
+  pdl_wait();
   uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j < N && f[j]) out[pos[j]] = keys[j];
 }
@@ -1789,14 +1815,14 @@ sst_status update_batches(sst_graph *g, const uint32_t *d_pairs,
   }
   const int dbits = g->dbits;
   const uint64_t sent = (uint64_t)g->n << dbits;
-  SST_LAUNCH(k_make_keys_batched, blocks_for(N), kTB, 0, s, d_pairs, N, d_boff,
+  SST_LAUNCH_PDL(k_make_keys_batched, blocks_for(N), kTB, 0, s, d_pairs, N, d_boff,
              nb, d_ops, g->n, g->width, dbits, !g->keep_loops, keys, vals,
              reinterpret_cast<unsigned long long *>(&P->invalid));
   uint64_t *sk = keys;
   uint32_t *sv = vals;
   SST_CUDA_TRY(radix_sort_kv(keys, ktmp, vals, vtmp, N, g->rbits + dbits, A, s,
                              &sk, &sv));
-  SST_LAUNCH(k_last_op, blocks_for(N), kTB, 0, s, sk, sv, N, sent, fins, fdel);
+  SST_LAUNCH_PDL(k_last_op, blocks_for(N), kTB, 0, s, sk, sv, N, sent, fins, fdel);
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(fins, pins, N, 0u, OpAdd{}, true, false,
                                       &P->n_items, A, s)));
   SST_CUDA_TRY((scan<uint32_t, OpAdd>(fdel, pdel, N, 0u, OpAdd{}, true, false,
@@ -1809,8 +1835,8 @@ sst_status update_batches(sst_graph *g, const uint32_t *d_pairs,
   if (n_ins + n_del == 0) return SST_OK;
   uint64_t *net = nullptr;
   SST_CUDA_TRY(cudaMallocAsync(&net, (n_ins + n_del) * 8, s));
-  SST_LAUNCH(k_compact_keys, blocks_for(N), kTB, 0, s, sk, fins, pins, N, net);
-  SST_LAUNCH(k_compact_keys, blocks_for(N), kTB, 0, s, sk, fdel, pdel, N, net + n_ins);
+  SST_LAUNCH_PDL(k_compact_keys, blocks_for(N), kTB, 0, s, sk, fins, pins, N, net);
+  SST_LAUNCH_PDL(k_compact_keys, blocks_for(N), kTB, 0, s, sk, fdel, pdel, N, net + n_ins);
   sst_status st = run_pipeline(g, nullptr, net + n_ins, n_del, false, nullptr, nullptr);
   if (st == SST_OK) st = run_pipeline(g, nullptr, net, n_ins, true, nullptr, nullptr);
   cudaFreeAsync(net, s);
@@ -1825,11 +1851,13 @@ sst_status update_batches(sst_graph *g, const uint32_t *d_pairs,
 namespace {
 __global__ void k_degkey(const uint32_t *__restrict__ deg, uint32_t n,
                          uint64_t *__restrict__ keys) {
+  pdl_wait();
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v < n) keys[v] = ((uint64_t)(0xFFFFFFFFu - deg[v]) << 32) | (0xFFFFFFFFu - v);
 }
 __global__ void k_rank_to_map(const uint64_t *__restrict__ sorted, uint32_t n,
                               uint32_t *__restrict__ map) {
+  pdl_wait();
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < n) map[0xFFFFFFFFu - (uint32_t)sorted[r]] = r;
 }
@@ -1838,6 +1866,7 @@ __global__ void k_csr_to_pairs(const uint64_t *__restrict__ off,
                                uint32_t *__restrict__ pairs);
 __global__ void k_relabel_pairs(uint32_t *__restrict__ pairs, uint64_t m,
                                 const uint32_t *__restrict__ map) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   pairs[2 * i] = map[pairs[2 * i]];
@@ -1852,10 +1881,10 @@ sst_status degree_order_map(sst_graph *g, uint32_t *d_map) {
   g->arena.reset();
   SST_CUDA_TRY(g->arena.reserve((uint64_t)n * 16 + radix_sort_scratch_bytes(n) + 8192));
   uint64_t *keys = g->arena.take<uint64_t>(n), *tmp = g->arena.take<uint64_t>(n);
-  SST_LAUNCH(k_degkey, blocks_for(n), kTB, 0, s, g->d_deg, n, keys);
+  SST_LAUNCH_PDL(k_degkey, blocks_for(n), kTB, 0, s, g->d_deg, n, keys);
   uint64_t *sorted = keys;
   SST_CUDA_TRY(radix_sort_u64(keys, tmp, n, 64, g->arena, s, &sorted));
-  SST_LAUNCH(k_rank_to_map, blocks_for(n), kTB, 0, s, sorted, n, d_map);
+  SST_LAUNCH_PDL(k_rank_to_map, blocks_for(n), kTB, 0, s, sorted, n, d_map);
   SST_CUDA_TRY(cudaGetLastError());
   return SST_OK;
 }
@@ -1872,8 +1901,8 @@ sst_status rewrite_graph(sst_graph *g, const uint32_t *d_map, sst_graph *out) {
   SST_CUDA_TRY(cudaMallocAsync(&pairs, m * 8, s));
   sst_status st = to_csr(g, off, cols);
   if (st == SST_OK) {
-    SST_LAUNCH(k_csr_to_pairs, warp_blocks(n), kTB, 0, s, off, cols, n, pairs);
-    SST_LAUNCH(k_relabel_pairs, blocks_for(m), kTB, 0, s, pairs, m, d_map);
+    SST_LAUNCH_PDL(k_csr_to_pairs, warp_blocks(n), kTB, 0, s, off, cols, n, pairs);
+    SST_LAUNCH_PDL(k_relabel_pairs, blocks_for(m), kTB, 0, s, pairs, m, d_map);
     SST_CUDA_TRY(cudaStreamSynchronize(s));
     const uint64_t chunk = 1ull << 25;
     for (uint64_t first = 0; first < m && st == SST_OK; first += chunk)
@@ -1906,6 +1935,7 @@ namespace {
 __global__ void k_csr_to_pairs(const uint64_t *__restrict__ off,
                                const uint32_t *__restrict__ cols, uint32_t n,
                                uint32_t *__restrict__ pairs) {
+  pdl_wait();
   uint64_t v = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (v >= n) return;
@@ -1919,6 +1949,7 @@ __global__ void k_csr_to_pairs(const uint64_t *__restrict__ off,
 // value (0 where absent)
 __global__ void k_has(DGraph g, const uint32_t *__restrict__ pairs, uint64_t n,
                       uint8_t *__restrict__ out, uint32_t *__restrict__ vals) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t u = pairs[2 * i], x = pairs[2 * i + 1];
@@ -1942,6 +1973,7 @@ __global__ void k_has(DGraph g, const uint32_t *__restrict__ pairs, uint64_t n,
 
 __global__ void k_vertex_leaves(const uint32_t *__restrict__ cap, uint32_t n,
                                 uint64_t *__restrict__ nl) {
+  pdl_wait();
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   nl[v] = cap[v] ? nleaves_of(cap[v]) : 0;
@@ -1952,6 +1984,7 @@ __global__ void k_dir_fill(DGraph g, const uint64_t *__restrict__ vleaf,
                            uint32_t *__restrict__ owner,
                            uint64_t *__restrict__ slot,
                            uint32_t *__restrict__ cnt) {
+  pdl_wait();
   uint64_t v = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (v >= g.n) return;
@@ -1972,6 +2005,7 @@ __global__ void k_dir_copy(const uint32_t *__restrict__ slots,
                            const uint32_t *__restrict__ cnt,
                            const uint64_t *__restrict__ pre, uint64_t nleaves,
                            uint32_t *__restrict__ cols) {
+  pdl_wait();
   uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (k >= nleaves) return;
@@ -1980,6 +2014,7 @@ __global__ void k_dir_copy(const uint32_t *__restrict__ slots,
 
 __global__ void k_widen(const uint32_t *__restrict__ in, uint64_t n,
                         uint64_t *__restrict__ out) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = in[i];
 }
@@ -1990,6 +2025,7 @@ __global__ void k_sample(const uint32_t *__restrict__ slots,
                          const uint64_t *__restrict__ pre, uint64_t nleaves,
                          uint64_t m, uint64_t seed, uint64_t first,
                          uint64_t count, uint32_t *__restrict__ pairs) {
+  pdl_wait();
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   if (m == 0) {
@@ -2007,6 +2043,7 @@ __global__ void k_sum_leaves(const uint32_t *__restrict__ slots,
                              const uint64_t *__restrict__ slot,
                              const uint32_t *__restrict__ cnt, uint64_t nleaves,
                              unsigned long long *__restrict__ out) {
+  pdl_wait();
   uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (k >= nleaves) return;
@@ -2033,7 +2070,7 @@ sst_status build_from_csr(sst_graph *g, const uint64_t *d_off,
   if (m == 0) return SST_OK;
   uint32_t *pairs = nullptr;
   SST_CUDA_TRY(cudaMallocAsync(&pairs, m * 8, s));
-  SST_LAUNCH(k_csr_to_pairs, warp_blocks(g->n), kTB, 0, s, d_off, d_cols, g->n, pairs);
+  SST_LAUNCH_PDL(k_csr_to_pairs, warp_blocks(g->n), kTB, 0, s, d_off, d_cols, g->n, pairs);
   sst_status st = update_batch(g, pairs, m, true, nullptr);
   cudaFreeAsync(pairs, s);
   return st;
@@ -2042,7 +2079,7 @@ sst_status build_from_csr(sst_graph *g, const uint64_t *d_off,
 sst_status has_batch(sst_graph *g, const uint32_t *d_pairs, uint64_t n,
                      uint8_t *d_out, uint32_t *d_vals) {
   if (n == 0) return SST_OK;
-  SST_LAUNCH(k_has, blocks_for(n), kTB, 0, g->stream, g->view(), d_pairs, n, d_out,
+  SST_LAUNCH_PDL(k_has, blocks_for(n), kTB, 0, g->stream, g->view(), d_pairs, n, d_out,
              d_vals);
   SST_CUDA_TRY(cudaGetLastError());
   return SST_OK;
@@ -2057,7 +2094,7 @@ sst_status ensure_leaf_dir(sst_graph *g) {
   g->arena.reset();
   SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes((uint64_t)n + 1, 8) + 4096));
   uint64_t *total = g->arena.take<uint64_t>(1);
-  if (n) SST_LAUNCH(k_vertex_leaves, blocks_for(n), kTB, 0, s, g->d_cap, n, D.vleaf);
+  if (n) SST_LAUNCH_PDL(k_vertex_leaves, blocks_for(n), kTB, 0, s, g->d_cap, n, D.vleaf);
   SST_CUDA_TRY((scan<uint64_t, OpAdd>(D.vleaf, D.vleaf, n, 0ull, OpAdd{}, true,
                                       false, total, g->arena, s)));
   uint64_t nl = 0;
@@ -2085,12 +2122,12 @@ sst_status ensure_leaf_dir(sst_graph *g) {
     D.cap = want;
   }
   D.nleaves = nl;
-  if (n) SST_LAUNCH(k_dir_fill, warp_blocks(n), kTB, 0, s, g->view(), D.vleaf,
+  if (n) SST_LAUNCH_PDL(k_dir_fill, warp_blocks(n), kTB, 0, s, g->view(), D.vleaf,
                     D.owner, D.slot, D.cnt);
   g->arena.reset();
   SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes(nl + 1, 8) + (nl + 1) * 8 + 4096));
   uint64_t *wide = g->arena.take<uint64_t>(nl + 1);
-  if (nl) SST_LAUNCH(k_widen, blocks_for(nl), kTB, 0, s, D.cnt, nl, wide);
+  if (nl) SST_LAUNCH_PDL(k_widen, blocks_for(nl), kTB, 0, s, D.cnt, nl, wide);
   SST_CUDA_TRY((scan<uint64_t, OpAdd>(wide, D.pre, nl, 0ull, OpAdd{}, true,
                                       false, D.pre + nl, g->arena, s)));
   SST_CUDA_TRY(cudaGetLastError());
@@ -2109,14 +2146,14 @@ sst_status to_csr(sst_graph *g, uint64_t *d_off, uint32_t *d_cols,
   g->arena.reset();
   SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes((uint64_t)n + 1, 8) + ((uint64_t)n + 1) * 8 + 4096));
   uint64_t *wide = g->arena.take<uint64_t>((uint64_t)n + 1);
-  if (n) SST_LAUNCH(k_widen, blocks_for(n), kTB, 0, s, g->d_deg, n, wide);
+  if (n) SST_LAUNCH_PDL(k_widen, blocks_for(n), kTB, 0, s, g->d_deg, n, wide);
   SST_CUDA_TRY((scan<uint64_t, OpAdd>(wide, d_off, n, 0ull, OpAdd{}, true, false,
                                       d_off + n, g->arena, s)));
   if (D.nleaves)
-    SST_LAUNCH(k_dir_copy, warp_blocks(D.nleaves), kTB, 0, s, g->d_slots, D.slot,
+    SST_LAUNCH_PDL(k_dir_copy, warp_blocks(D.nleaves), kTB, 0, s, g->d_slots, D.slot,
                D.cnt, D.pre, D.nleaves, d_cols);
   if (D.nleaves && d_vals && g->d_vals)  // values in the same CSR order
-    SST_LAUNCH(k_dir_copy, warp_blocks(D.nleaves), kTB, 0, s, g->d_vals, D.slot,
+    SST_LAUNCH_PDL(k_dir_copy, warp_blocks(D.nleaves), kTB, 0, s, g->d_vals, D.slot,
                D.cnt, D.pre, D.nleaves, d_vals);
   SST_CUDA_TRY(cudaGetLastError());
   return SST_OK;
@@ -2140,13 +2177,13 @@ sst_status neighbors(sst_graph *g, uint32_t v, uint32_t *d_out, uint64_t cap,
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   if (cap >= d) {
     // copy leaves with positions rebased to the vertex's first element
-    SST_LAUNCH(k_dir_copy, warp_blocks(k[1] - k[0]), kTB, 0, s, g->d_slots,
+    SST_LAUNCH_PDL(k_dir_copy, warp_blocks(k[1] - k[0]), kTB, 0, s, g->d_slots,
                D.slot + k[0], D.cnt + k[0], D.pre + k[0], k[1] - k[0],
                d_out - p0);
   } else {
     uint32_t *tmp = nullptr;
     SST_CUDA_TRY(cudaMallocAsync(&tmp, (uint64_t)d * 4, s));
-    SST_LAUNCH(k_dir_copy, warp_blocks(k[1] - k[0]), kTB, 0, s, g->d_slots,
+    SST_LAUNCH_PDL(k_dir_copy, warp_blocks(k[1] - k[0]), kTB, 0, s, g->d_slots,
                D.slot + k[0], D.cnt + k[0], D.pre + k[0], k[1] - k[0], tmp - p0);
     SST_CUDA_TRY(cudaMemcpyAsync(d_out, tmp, cap * 4, cudaMemcpyDeviceToDevice, s));
     cudaFreeAsync(tmp, s);
@@ -2161,7 +2198,7 @@ sst_status sample_edges(sst_graph *g, uint64_t seed, uint64_t first,
   sst_status st = ensure_leaf_dir(g);
   if (st != SST_OK) return st;
   LeafDir &D = g->dir;
-  SST_LAUNCH(k_sample, blocks_for(count), kTB, 0, g->stream, g->d_slots, D.owner,
+  SST_LAUNCH_PDL(k_sample, blocks_for(count), kTB, 0, g->stream, g->d_slots, D.owner,
              D.slot, D.pre, D.nleaves, g->m, seed, first, count, d_pairs);
   SST_CUDA_TRY(cudaGetLastError());
   return SST_OK;
@@ -2177,7 +2214,7 @@ sst_status touch_all_sum(sst_graph *g, uint64_t *out) {
   unsigned long long *acc = g->arena.take<unsigned long long>(1);
   SST_CUDA_TRY(cudaMemsetAsync(acc, 0, 8, s));
   if (D.nleaves)
-    SST_LAUNCH(k_sum_leaves, warp_blocks(D.nleaves), kTB, 0, s, g->d_slots,
+    SST_LAUNCH_PDL(k_sum_leaves, warp_blocks(D.nleaves), kTB, 0, s, g->d_slots,
                D.slot, D.cnt, D.nleaves, acc);
   SST_CUDA_TRY(cudaMemcpyAsync(out, acc, 8, cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));

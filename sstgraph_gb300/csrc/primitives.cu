@@ -36,7 +36,8 @@ thread_local bool t_capture_forms = false;
 thread_local DeviceScanTags *t_scan_tags = nullptr;
 
 namespace {
-__global__ void k_scan_epoch_bump(unsigned long long *epoch) { *epoch += 1; }
+__global__ void k_scan_epoch_bump(unsigned long long *epoch) {
+  pdl_wait(); *epoch += 1; }
 }  // namespace
 
 DeviceScanTags::DeviceScanTags(unsigned long long *e) : epoch(e), prev(t_scan_tags) {
@@ -45,7 +46,7 @@ DeviceScanTags::DeviceScanTags(unsigned long long *e) : epoch(e), prev(t_scan_ta
 DeviceScanTags::~DeviceScanTags() { t_scan_tags = prev; }
 cudaError_t DeviceScanTags::bump(cudaStream_t s) {
   next = 0;
-  SST_LAUNCH(k_scan_epoch_bump, 1, 1, 0, s, epoch);
+  SST_LAUNCH_PDL(k_scan_epoch_bump, 1, 1, 0, s, epoch);
   return cudaGetLastError();
 }
 
@@ -175,14 +176,9 @@ constexpr int kTile = kThreads * kItems;  // 4096
 // quarter of the keys, so a pass's dependent chain is shorter.
 constexpr int kSmallItems = 4;
 constexpr uint64_t kSmallTileKeys = 256ull * kThreads * kSmallItems;  // 2^18
-// The one-sweep passes (sorts below 2^30 keys) keep 1024-key tiles up to
-// this many keys: a tile's look-back is linear in the tiles before it, and
-// shorter per-tile chains at three blocks an SM beat fewer, longer ones
-// (4096-key tiles of 127-register blocks fill under a fifth of an SM's warp
-// slots)
-constexpr uint64_t kOsSmallTileKeys = 1ull << 22;
-
-inline bool os_small_tiles(uint64_t n) { return n <= kOsSmallTileKeys && n < (1ull << 30); }
+// (1024-key tiles for larger one-sweep sorts were measured too: at 1e6 keys
+// 977 tiles made a pass 29 us against 19 us for 245 tiles of 4096 -- the
+// longer look-back walks cost more than the extra resident warps gain)
 constexpr int kRadix = 256;
 constexpr uint32_t kNoDigit = 0xffffffffu;  // an item past the end
 // Sorts of at most this many tiles run one launch per pass: every block
@@ -264,6 +260,7 @@ __global__ void __launch_bounds__(kThreads)
 k_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
        uint32_t *__restrict__ hist, uint32_t dstride, uint32_t bstride,
        uint32_t *__restrict__ zero, const uint32_t *__restrict__ d_n) {
+  pdl_wait();
   if (d_n && *d_n < n) n = *d_n;
   __shared__ uint32_t h[kRadix];
   h[threadIdx.x] = 0;
@@ -313,6 +310,7 @@ k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
           uint32_t *__restrict__ vout, uint32_t *__restrict__ hist_next,
           int next_shift, uint32_t *__restrict__ hist_zero,
           const uint32_t *__restrict__ d_n) {
+  pdl_wait();
   constexpr int TILE = kThreads * IT;
   if (d_n && *d_n < n) n = *d_n;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -437,6 +435,7 @@ __global__ void __launch_bounds__(kThreads)
 k_hist_all(const uint64_t *__restrict__ keys, uint64_t n, int passes,
            uint32_t *__restrict__ totals, uint32_t *__restrict__ status,
            uint64_t status_words, const uint32_t *__restrict__ d_n) {
+  pdl_wait();
   if (d_n && *d_n < n) n = *d_n;
   __shared__ uint32_t h[8][kRadix];
   for (int p = 0; p < passes; p++) h[p][threadIdx.x] = 0;
@@ -475,6 +474,7 @@ k_scatter_os(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
              uint64_t n, int shift, const uint32_t *__restrict__ totals,
              uint32_t *__restrict__ status, const uint32_t *__restrict__ vin,
              uint32_t *__restrict__ vout, const uint32_t *__restrict__ d_n) {
+  pdl_wait();
   constexpr int TILE = kThreads * IT;
   if (d_n && *d_n < n) n = *d_n;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -514,19 +514,33 @@ k_scatter_os(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
     atomicExch(mine, kOsIncl | tcount);
   } else {
     atomicExch(mine, kOsAgg | tcount);
-    for (int64_t t = (int64_t)tile - 1; t >= 0; t--) {
-      const volatile uint32_t *sp = status + (uint64_t)t * kRadix + d;
-      uint32_t v = *sp;
-      for (int p = 0; (v & ~kOsMask) == 0 && p < kOsPolls; p++) {
-        __nanosleep(p < 32 ? 20 : 200);
-        v = *sp;
+    // the walk loads kOsAhead earlier tiles' words at once, then takes them
+    // in order (a word not yet published is polled again on its own)
+    constexpr int kOsAhead = 8;
+    bool done = false;
+    for (int64_t t0 = (int64_t)tile - 1; t0 >= 0 && !done; t0 -= kOsAhead) {
+      uint32_t w[kOsAhead];
+#pragma unroll
+      for (int q = 0; q < kOsAhead; q++)
+        w[q] = t0 - q >= 0 ? *(const volatile uint32_t *)(status + (uint64_t)(t0 - q) * kRadix + d)
+                           : kOsIncl;
+#pragma unroll
+      for (int q = 0; q < kOsAhead; q++) {
+        const int64_t t = t0 - q;
+        if (done || t < 0) break;
+        uint32_t v = w[q];
+        const volatile uint32_t *sp = status + (uint64_t)t * kRadix + d;
+        for (int p = 0; (v & ~kOsMask) == 0 && p < kOsPolls; p++) {
+          __nanosleep(p < 32 ? 20 : 200);
+          v = *sp;
+        }
+        if ((v & ~kOsMask) == 0) {  // never published: count its keys
+          before += os_count_tile(in, n, (uint64_t)t, TILE, shift, d);
+          continue;
+        }
+        before += v & kOsMask;
+        if ((v & ~kOsMask) == kOsIncl) done = true;
       }
-      if ((v & ~kOsMask) == 0) {  // never published: count its keys
-        before += os_count_tile(in, n, (uint64_t)t, TILE, shift, d);
-        continue;
-      }
-      before += v & kOsMask;
-      if ((v & ~kOsMask) == kOsIncl) break;
     }
     atomicExch(mine, kOsIncl | (before + tcount));
   }
@@ -586,6 +600,7 @@ template <bool KV, int TILE>
 __global__ void __launch_bounds__(kThreads)
 k_sort_small(uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
              uint64_t n, int bits, const uint32_t *__restrict__ d_n) {
+  pdl_wait();
   if (d_n && *d_n < n) n = *d_n;
   constexpr int IT = TILE / kThreads;
   __shared__ uint64_t buf[2][TILE];
@@ -644,8 +659,7 @@ constexpr int kSmallSortKV = 1024;
 }  // namespace
 
 size_t radix_sort_scratch_bytes(uint64_t n) {
-  const uint64_t tile = (n <= kSmallTileKeys || os_small_tiles(n))
-                            ? (uint64_t)kThreads * kSmallItems : kTile;
+  const uint64_t tile = n <= kSmallTileKeys ? (uint64_t)kThreads * kSmallItems : kTile;
   uint64_t nblocks = (n + tile - 1) / tile;
   uint64_t hn = nblocks * kRadix;
   // the one-sweep form: digit totals and up to eight passes' tile status;
@@ -699,16 +713,16 @@ static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *val
     if (!totals || !status) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMemsetAsync(totals, 0, (size_t)passes * kRadix * 4, s);
     if (e != cudaSuccess) return e;
-    SST_LAUNCH_NB("(k_hist_all)", 8 * n, k_hist_all<IT>, nblocks, kThreads, 0, s, src, n,
+    SST_LAUNCH_PDL_NB("(k_hist_all)", 8 * n, k_hist_all<IT>, nblocks, kThreads, 0, s, src, n,
                   passes, totals, status, (uint64_t)passes * hn, d_n);
     for (int p = 0; p < passes; p++) {
       const uint64_t sb = (vals ? 24 : 16) * n + 8 * (uint64_t)kRadix * nblocks;
       if (vals)
-        SST_LAUNCH_NB((scatter_os_name<true, IT>()), sb, (k_scatter_os<true, IT>), nblocks,
+        SST_LAUNCH_PDL_NB((scatter_os_name<true, IT>()), sb, (k_scatter_os<true, IT>), nblocks,
                       kThreads, (scatter_smem_bytes<true, IT>()), s, src, dst, n, 8 * p,
                       totals + p * kRadix, status + (uint64_t)p * hn, vsrc, vdst, d_n);
       else
-        SST_LAUNCH_NB((scatter_os_name<false, IT>()), sb, (k_scatter_os<false, IT>), nblocks,
+        SST_LAUNCH_PDL_NB((scatter_os_name<false, IT>()), sb, (k_scatter_os<false, IT>), nblocks,
                       kThreads, (scatter_smem_bytes<false, IT>()), s, src, dst, n, 8 * p,
                       totals + p * kRadix, status + (uint64_t)p * hn, vsrc, vdst, d_n);
       std::swap(src, dst);
@@ -720,7 +734,7 @@ static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *val
     uint32_t *h[3];
     for (auto &t : h)
       if (!(t = arena.take<uint32_t>(hn))) return cudaErrorMemoryAllocation;
-    SST_LAUNCH_B(hist_bytes, k_hist<IT>, nblocks, kThreads, 0, s, src, n, 0, h[0],
+    SST_LAUNCH_PDL_B(hist_bytes, k_hist<IT>, nblocks, kThreads, 0, s, src, n, 0, h[0],
                  1u, (uint32_t)kRadix, h[1], d_n);
     int p = 0;
     for (int shift = 0; shift < bits; shift += 8, p++) {
@@ -728,12 +742,12 @@ static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *val
       uint32_t *nx = more ? h[(p + 1) % 3] : nullptr;
       uint32_t *zr = more ? h[(p + 2) % 3] : nullptr;
       if (vals)
-        SST_LAUNCH_NB((scatter_name<true, IT>()), scatter_bytes, (k_scatter<true, IT>), nblocks, kThreads,
+        SST_LAUNCH_PDL_NB((scatter_name<true, IT>()), scatter_bytes, (k_scatter<true, IT>), nblocks, kThreads,
                      (scatter_smem_bytes<true, IT>()), s, src,
                      dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
                      shift + 8, zr, d_n);
       else
-        SST_LAUNCH_NB((scatter_name<false, IT>()), scatter_bytes, (k_scatter<false, IT>), nblocks, kThreads,
+        SST_LAUNCH_PDL_NB((scatter_name<false, IT>()), scatter_bytes, (k_scatter<false, IT>), nblocks, kThreads,
                      (scatter_smem_bytes<false, IT>()), s, src,
                      dst, n, shift, h[p % 3], nblocks, true, vsrc, vdst, nx,
                      shift + 8, zr, d_n);
@@ -747,7 +761,7 @@ static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *val
     uint32_t *hist = arena.take<uint32_t>(hn);
     if (!cnts || !hist) return cudaErrorMemoryAllocation;
     for (int shift = 0; shift < bits; shift += 8) {
-      SST_LAUNCH_B(hist_bytes, k_hist<IT>, nblocks, kThreads, 0, s, src, n, shift,
+      SST_LAUNCH_PDL_B(hist_bytes, k_hist<IT>, nblocks, kThreads, 0, s, src, n, shift,
                    cnts, nblocks, 1u, (uint32_t *)nullptr, d_n);
       size_t mark = arena.used;
       cudaError_t e = scan<uint32_t, OpAdd>(cnts, hist, hn, 0u, OpAdd{}, true,
@@ -755,12 +769,12 @@ static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *val
       arena.used = mark;
       if (e != cudaSuccess) return e;
       if (vals)
-        SST_LAUNCH_NB((scatter_name<true, IT>()), scatter_bytes, (k_scatter<true, IT>), nblocks, kThreads,
+        SST_LAUNCH_PDL_NB((scatter_name<true, IT>()), scatter_bytes, (k_scatter<true, IT>), nblocks, kThreads,
                      (scatter_smem_bytes<true, IT>()), s, src,
                      dst, n, shift, hist, nblocks, false, vsrc, vdst,
                      (uint32_t *)nullptr, 0, (uint32_t *)nullptr, d_n);
       else
-        SST_LAUNCH_NB((scatter_name<false, IT>()), scatter_bytes, (k_scatter<false, IT>), nblocks, kThreads,
+        SST_LAUNCH_PDL_NB((scatter_name<false, IT>()), scatter_bytes, (k_scatter<false, IT>), nblocks, kThreads,
                      (scatter_smem_bytes<false, IT>()), s, src,
                      dst, n, shift, hist, nblocks, false, vsrc, vdst,
                      (uint32_t *)nullptr, 0, (uint32_t *)nullptr, d_n);
@@ -782,16 +796,16 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
   if (vresult) *vresult = vals;
   if (n < 2 || bits <= 0) return cudaSuccess;
   if (!vals && n <= (uint64_t)kSmallSort) {
-    SST_LAUNCH_B(16 * n, (k_sort_small<false, kSmallSort>), 1, kThreads, 0, s, keys,
+    SST_LAUNCH_PDL_B(16 * n, (k_sort_small<false, kSmallSort>), 1, kThreads, 0, s, keys,
                (uint32_t *)nullptr, n, bits, d_n);
     return cudaGetLastError();
   }
   if (vals && n <= (uint64_t)kSmallSortKV) {
-    SST_LAUNCH_B(24 * n, (k_sort_small<true, kSmallSortKV>), 1, kThreads, 0, s, keys, vals,
+    SST_LAUNCH_PDL_B(24 * n, (k_sort_small<true, kSmallSortKV>), 1, kThreads, 0, s, keys, vals,
                n, bits, d_n);
     return cudaGetLastError();
   }
-  if ((!vals && n <= kSmallTileKeys) || os_small_tiles(n))
+  if (!vals && n <= kSmallTileKeys)
     return radix_sort_tiles<kSmallItems>(keys, tmp, vals, vtmp, n, bits, arena, s, result,
                                          vresult, d_n);
   return radix_sort_tiles<kItems>(keys, tmp, vals, vtmp, n, bits, arena, s, result, vresult,

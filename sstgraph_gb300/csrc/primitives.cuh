@@ -4,6 +4,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <utility>
 
 #include "common.cuh"
 
@@ -51,6 +52,48 @@ void prof_end(const char *name, cudaEvent_t start, cudaStream_t s,
   SST_LAUNCH_NB(#kernel, bytes, kernel, grid, block, smem, stream, __VA_ARGS__)
 #define SST_LAUNCH(kernel, grid, block, smem, stream, ...)                    \
   SST_LAUNCH_B(0, kernel, grid, block, smem, stream, __VA_ARGS__)
+
+// Programmatic dependent launch: the kernel may be scheduled while the
+// kernel before it on the stream still runs (its launch and block set-up
+// overlap that kernel's tail); it must call pdl_wait() before touching
+// anything the earlier kernels read or write.  Used for the update
+// pipeline's chains of dependent kernels (graph.cu, the scans and sorts);
+// captured into a CUDA graph the dependency becomes a programmatic edge.
+#define SST_LAUNCH_PDL_NB(name, bytes, kernel, grid, block, smem, stream, ...) \
+  do {                                                                        \
+    cudaEvent_t _sst_ev =                                                     \
+        ::sst::profiling(name) ? ::sst::prof_begin(stream) : nullptr;         \
+    ::sst::launch_pdl(kernel, (grid), (block), (smem), (stream), __VA_ARGS__); \
+    ::sst::note_launch();                                                     \
+    if (_sst_ev) ::sst::prof_end(name, _sst_ev, stream, (bytes));             \
+  } while (0)
+#define SST_LAUNCH_PDL_B(bytes, kernel, grid, block, smem, stream, ...)       \
+  SST_LAUNCH_PDL_NB(#kernel, bytes, kernel, grid, block, smem, stream, __VA_ARGS__)
+#define SST_LAUNCH_PDL(kernel, grid, block, smem, stream, ...)                \
+  SST_LAUNCH_PDL_B(0, kernel, grid, block, smem, stream, __VA_ARGS__)
+
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t s, Args &&...args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  // an error is left for the caller's cudaGetLastError, as a <<<>>> launch
+  (void)cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// wait for the kernels this one was launched after (a no-op for a kernel
+// launched without programmatic serialization)
+__device__ __forceinline__ void pdl_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
 
 // ----------------------------------------------------------------- arena
 // Bump allocator over one device buffer; reset at the start of each
@@ -207,6 +250,7 @@ __global__ void k_scan_reduce(const T *__restrict__ in, uint64_t n, T identity,
                               Op op, bool reverse, uint64_t tiles_per_range,
                               T *__restrict__ range_sums,
                               const uint32_t *__restrict__ d_n) {
+  pdl_wait();
   if (d_n && *d_n < n) n = *d_n;
   const uint64_t t0 = (uint64_t)blockIdx.x * tiles_per_range;
   T acc = identity;
@@ -231,6 +275,7 @@ __global__ void k_scan_ranges(const T *__restrict__ in, Epi out,
                               const T *__restrict__ range_sums,
                               T *__restrict__ total_out,
                               const uint32_t *__restrict__ d_n) {
+  pdl_wait();
   if (d_n && *d_n < n) n = *d_n;
   __shared__ T s_carry;
   // carry into this range: the sums of the ranges before it
@@ -277,6 +322,7 @@ __global__ void k_scan_tile(const T *__restrict__ in, Epi out,
                             uint64_t n, T identity, Op op, bool reverse,
                             bool exclusive, T *__restrict__ total_out,
                             const uint32_t *__restrict__ d_n) {
+  pdl_wait();
   if (d_n && *d_n < n) n = *d_n;
   T vals[kScanItems];
   T acc = identity;
@@ -422,6 +468,7 @@ k_scan_lb(const T *__restrict__ in, Epi out, uint64_t n,
           T *__restrict__ total_out, const uint32_t *__restrict__ d_n,
           ScanStatus<T> *st, unsigned long long tag, int polls,
           const unsigned long long *__restrict__ d_epoch) {
+  pdl_wait();
   if (d_epoch)  // the epoch is written before this launch, in stream order
     tag = kScanTag |
           (((*d_epoch * kScanTagsPerEpoch + (tag & 0xFF)) & kScanEpochMask) << 2);
@@ -516,7 +563,7 @@ cudaError_t scan_epi(const T *in, uint64_t n, T identity, Op op, bool exclusive,
   }
   const uint64_t tiles = (n + kScanTile - 1) / kScanTile;
   if (tiles == 1) {
-    SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_tile<T, Op, Epi>), 1, kScanThreads, 0, s,
+    SST_LAUNCH_PDL_B(2 * sizeof(T) * n, (k_scan_tile<T, Op, Epi>), 1, kScanThreads, 0, s,
                  in, epi, n, identity, op, reverse, exclusive, total_out, d_n);
     return cudaGetLastError();
   }
@@ -533,7 +580,7 @@ cudaError_t scan_epi(const T *in, uint64_t n, T identity, Op op, bool exclusive,
       // a scan whose element count is on the device (d_n) is profiled
       // apart, with no declared bytes: its launch size overstates its work
       const unsigned long long tag = dev_tags ? (unsigned long long)dt->next++ : next_scan_tag();
-      SST_LAUNCH_NB(d_n ? "(k_scan_lb<T, Op, Epi>, device count)" : "(k_scan_lb<T, Op, Epi>)",
+      SST_LAUNCH_PDL_NB(d_n ? "(k_scan_lb<T, Op, Epi>, device count)" : "(k_scan_lb<T, Op, Epi>)",
                     d_n ? 0 : 2 * sizeof(T) * n, (k_scan_lb<T, Op, Epi>), (unsigned)tiles,
                     kScanThreads, 0, s, in, epi, n, identity, op, reverse,
                     exclusive, total_out, d_n, st, tag, lookback_polls(),
@@ -544,7 +591,7 @@ cudaError_t scan_epi(const T *in, uint64_t n, T identity, Op op, bool exclusive,
   if (tiles <= kScanOneBlockTiles) {
     // one block walks the tiles with a running carry: one launch, where the
     // two-launch form would pay a second launch's latency for little work
-    SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_ranges<T, Op, Epi>), 1, kScanThreads, 0,
+    SST_LAUNCH_PDL_B(2 * sizeof(T) * n, (k_scan_ranges<T, Op, Epi>), 1, kScanThreads, 0,
                  s, in, epi, n, identity, op, reverse, exclusive, tiles,
                  (const T *)nullptr, total_out, d_n);
     return cudaGetLastError();
@@ -555,9 +602,9 @@ cudaError_t scan_epi(const T *in, uint64_t n, T identity, Op op, bool exclusive,
   T *sums = arena.take<T>(used);
   if (!sums) return cudaErrorMemoryAllocation;
   // the reduce reads the input; the scan reads it again and writes the output
-  SST_LAUNCH_B(sizeof(T) * n, (k_scan_reduce<T, Op>), (unsigned)used, kScanThreads,
+  SST_LAUNCH_PDL_B(sizeof(T) * n, (k_scan_reduce<T, Op>), (unsigned)used, kScanThreads,
                0, s, in, n, identity, op, reverse, per, sums, d_n);
-  SST_LAUNCH_B(2 * sizeof(T) * n, (k_scan_ranges<T, Op, Epi>), (unsigned)used,
+  SST_LAUNCH_PDL_B(2 * sizeof(T) * n, (k_scan_ranges<T, Op, Epi>), (unsigned)used,
                kScanThreads, 0, s, in, epi, n, identity, op, reverse, exclusive,
                per, (const T *)sums, total_out, d_n);
   return cudaGetLastError();

@@ -3,8 +3,8 @@ and the layout restatement (oracle/compact.py): the decoded CSR bit-exact,
 rows per key width and storage bytes as the restatement predicts,
 membership answers equal, PageRank equal bit for bit to the PMA
 PageRank (the same fixed-point arithmetic over the same rows), and, on
-symmetric graphs, BFS depths and CC labels equal to the graph's and the
-oracle's."""
+symmetric graphs, BFS depths, CC labels and triangle counts equal to the
+graph's and the oracle's and BC within 1e-9 relative of the oracle's."""
 import numpy as np
 import pytest
 
@@ -139,7 +139,7 @@ def test_weighted_graph_refused(sg):
 
 
 def check_traversals(sg, g, n, srcs):
-    """BFS and CC on the snapshot = on the live graph = the oracle."""
+    """BFS, CC, BC and TC on the snapshot = on the live graph = the oracle."""
     off, cols = g.csr()
     o = oracle.OracleGraph(n)
     rows = np.repeat(np.arange(n, dtype=np.uint32), np.diff(off).astype(np.int64))
@@ -153,6 +153,14 @@ def check_traversals(sg, g, n, srcs):
         want = o.cc()
         assert np.array_equal(c.cc(), want)
         assert np.array_equal(sg.CC(g), want)
+        for src in srcs[:3]:
+            want = o.bc(int(src))
+            err = np.max(np.abs(c.bc(int(src)) - want)) / max(np.max(np.abs(want)), 1e-300)
+            assert err <= 1e-9, src
+        t, pv = o.tc(per_vertex=True)
+        ct, cpv = c.tc(per_vertex=True)
+        assert ct == t and c.tc() == t
+        assert np.array_equal(cpv, pv)
     finally:
         c.close()
 
@@ -201,7 +209,7 @@ def test_traversals_device_arrays_and_refusal(sg):
     w = sg.SparseMatrixV(8, 1 << 20)
     w.insert_batch(np.array([[1, 5]], np.uint32))
     cw = sg.CompactGraph(w)
-    for call in (lambda: cw.bfs(1), lambda: cw.cc()):
+    for call in (lambda: cw.bfs(1), lambda: cw.cc(), lambda: cw.bc(1), lambda: cw.tc()):
         with pytest.raises(sg.SSTError) as e:
             call()
         assert "rows as columns" in str(e.value)
