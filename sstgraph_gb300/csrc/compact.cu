@@ -601,6 +601,68 @@ __device__ __forceinline__ void cbfs_enqueue(uint32_t w, uint32_t d,
   atomicAdd(&cnt[2], (unsigned long long)((d + kElemsPerWarp - 1) / kElemsPerWarp));
 }
 
+__device__ __forceinline__ uint32_t cbfs_items(uint32_t d) {
+  return (d + kElemsPerWarp - 1) / kElemsPerWarp;
+}
+
+// every lane of the warp calls it: the lanes with `want` append w (degree
+// d) to the next queue with one set of counter atomics for the warp
+__device__ __forceinline__ void cbfs_enqueue_warp(bool want, uint32_t w, uint32_t d,
+                                                  uint32_t *__restrict__ nq,
+                                                  unsigned long long *__restrict__ cnt) {
+  const uint32_t m = __ballot_sync(0xffffffffu, want);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  const uint32_t dsum = __reduce_add_sync(0xffffffffu, want ? d : 0u);
+  const uint32_t isum = __reduce_add_sync(0xffffffffu, want ? cbfs_items(d) : 0u);
+  const int leader = __ffs(m) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) {
+    base = atomicAdd(&cnt[0], (unsigned long long)__popc(m));
+    atomicAdd(&cnt[1], (unsigned long long)dsum);
+    atomicAdd(&cnt[2], (unsigned long long)isum);
+  }
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (want) nq[base + __popc(m & ((1u << lane) - 1u))] = w;
+}
+
+// every thread of the block calls it: one set of counter atomics a block
+__device__ __forceinline__ void cbfs_enqueue_block(bool want, uint32_t w, uint32_t d,
+                                                   uint32_t *__restrict__ nq,
+                                                   unsigned long long *__restrict__ cnt) {
+  __shared__ uint32_t s_cnt[kTB / 32];
+  __shared__ unsigned long long s_base, s_deg, s_items;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t m = __ballot_sync(0xffffffffu, want);
+  const uint32_t dsum = __reduce_add_sync(0xffffffffu, want ? d : 0u);
+  const uint32_t isum = __reduce_add_sync(0xffffffffu, want ? cbfs_items(d) : 0u);
+  if (threadIdx.x == 0) {
+    s_deg = 0;
+    s_items = 0;
+  }
+  if (lane == 0) s_cnt[warp] = __popc(m);
+  __syncthreads();
+  if (lane == 0 && m) {
+    atomicAdd(&s_deg, (unsigned long long)dsum);
+    atomicAdd(&s_items, (unsigned long long)isum);
+  }
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (int k = 0; k < kTB / 32; k++) {
+      const uint32_t c = s_cnt[k];
+      s_cnt[k] = tot;
+      tot += c;
+    }
+    s_base = tot ? atomicAdd(&cnt[0], (unsigned long long)tot) : 0ull;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && (s_deg || s_items)) {
+    atomicAdd(&cnt[1], s_deg);
+    atomicAdd(&cnt[2], s_items);
+  }
+  if (want) nq[s_base + s_cnt[warp] + __popc(m & ((1u << lane) - 1u))] = w;
+}
+
 __global__ void k_cbfs_init(int32_t *__restrict__ depth, uint32_t n, uint32_t src) {
   const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v < n) depth[v] = v == src ? 0 : -1;
@@ -616,26 +678,50 @@ __device__ __forceinline__ bool in_front(const uint32_t *bits, uint32_t x) {
   return (__ldg(bits + (x >> 5)) >> (x & 31)) & 1u;
 }
 
-// pull, small rows: an unreached vertex looks for a neighbour in the
-// frontier and stops at the first
+// B-byte id at byte p: two aligned words and a funnel shift (the byte
+// array carries 16 bytes of tail padding)
+__device__ __forceinline__ uint32_t id_words(const uint8_t *bytes, uint64_t p, uint32_t B) {
+  const uint32_t *w = reinterpret_cast<const uint32_t *>(bytes + (p & ~uint64_t(3)));
+  const uint32_t x = __funnelshift_r(__ldg(w), __ldg(w + 1), (uint32_t)(p & 3) * 8);
+  return B == 4 ? x : x & ((1u << (8 * B)) - 1u);
+}
+
+// id of element i (bucket b) of a row, by word loads
+__device__ __forceinline__ uint32_t elem_words(const DCompact &c, const Row &r, uint32_t i,
+                                               uint32_t b) {
+  const uint32_t lo = id_words(c.bytes, (uint64_t)(r.lows - c.bytes) + (uint64_t)i * r.B, r.B);
+  return r.nb > 1 ? (b << (8 * r.B)) | lo : lo;
+}
+
+// pull, small rows: 8 lanes per row (four ids a lane), an unreached vertex
+// looks for a neighbour in the frontier
 __global__ void k_cbfs_pull_small(DCompact c, const unsigned long long *__restrict__ sdesc,
                                   const uint32_t *__restrict__ small, uint64_t nsmall,
                                   const uint32_t *__restrict__ bits,
                                   int32_t *__restrict__ depth, uint32_t *__restrict__ nq,
                                   unsigned long long *__restrict__ cnt, int32_t lvl) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nsmall) return;
-  const uint32_t v = small[i];
-  if (depth[v] >= 0) return;
-  const unsigned long long dsc = sdesc[i];
-  const uint32_t d = (uint32_t)(dsc & 63);
-  const uint32_t B = width_of(d, c.t24, c.t16, c.t8);
-  for (uint32_t j = 0; j < d; j++)
-    if (in_front(bits, small_id(c.bytes, dsc >> 6, j, B))) {
-      depth[v] = lvl + 1;  // a small row is its vertex's only work item
-      cbfs_enqueue(v, d, nq, cnt);
-      return;
+  const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const uint32_t sub = threadIdx.x & 7;
+  const int lane = threadIdx.x & 31;
+  const bool ok = i < nsmall;
+  const uint32_t v = ok ? small[i] : 0u;
+  bool hit = false;
+  uint32_t d = 0;
+  if (ok && depth[v] < 0) {
+    const unsigned long long dsc = sdesc[i];
+    d = (uint32_t)(dsc & 63);
+    const uint32_t B = width_of(d, c.t24, c.t16, c.t8);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const uint32_t j = sub + 8 * q;
+      if (j < d) hit |= in_front(bits, id_words(c.bytes, (dsc >> 6) + (uint64_t)j * B, B));
     }
+  }
+  const uint32_t group = (__ballot_sync(0xffffffffu, hit) >> (lane & ~7)) & 0xffu;
+  // a small row is its vertex's only work item: no claim race
+  const bool claim = group && sub == 0;
+  if (claim) depth[v] = lvl + 1;
+  cbfs_enqueue_block(claim, v, d, nq, cnt);
 }
 
 // pull, chunks: a warp per chunk, 32 ids a step, until one is in the
@@ -660,7 +746,7 @@ __global__ void k_cbfs_pull_chunks(DCompact c, const uint32_t *__restrict__ cv,
     if (i < e1) {
       if (r.nb > 1)
         while (r.dir[b + 1] <= i) b++;
-      hit = in_front(bits, elem_at(r, i, b));
+      hit = in_front(bits, elem_words(c, r, i, b));
     }
     if (__any_sync(0xffffffffu, hit)) {
       if (lane == 0 && atomicCAS(depth + v, -1, lvl + 1) == -1) cbfs_enqueue(v, r.d, nq, cnt);
@@ -794,12 +880,17 @@ __global__ void k_cbfs_push(DCompact c, const uint32_t *__restrict__ iv,
   const Row r = row_of(c, u);
   const uint32_t e1 = min(e0 + kElemsPerWarp, r.d);
   uint32_t b = (r.nb > 1 && e0 + lane < e1) ? bucket_of(r, e0 + lane) : 0u;
-  for (uint32_t i = e0 + lane; i < e1; i += 32) {
-    if (r.nb > 1)
-      while (r.dir[b + 1] <= i) b++;
-    const uint32_t x = elem_at(r, i, b);
-    if (__ldcg(depth + x) < 0 && atomicCAS(depth + x, -1, lvl + 1) == -1)
-      cbfs_enqueue(x, c.deg[x], nq, cnt);
+  for (uint32_t i0 = e0; i0 < e1; i0 += 32) {  // warp-uniform steps
+    const uint32_t i = i0 + lane;
+    bool won = false;
+    uint32_t x = 0;
+    if (i < e1) {
+      if (r.nb > 1)
+        while (r.dir[b + 1] <= i) b++;
+      x = elem_words(c, r, i, b);
+      won = __ldcg(depth + x) < 0 && atomicCAS(depth + x, -1, lvl + 1) == -1;
+    }
+    cbfs_enqueue_warp(won, x, won ? c.deg[x] : 0u, nq, cnt);
   }
 }
 
@@ -1085,7 +1176,7 @@ sst_status compact_bfs(sst_compact *c, uint32_t src, int32_t *d_depth) {
       SST_CUDA_TRY(cudaMemsetAsync(c->d_bits, 0, ((uint64_t)n / 32 + 1) * 4, s));
       SST_LAUNCH(k_cbfs_bits, blocks_for(qn), kTB, 0, s, q, qn, c->d_bits);
       if (c->nsmall)
-        SST_LAUNCH(k_cbfs_pull_small, blocks_for(c->nsmall), kTB, 0, s, dc, c->d_sdesc,
+        SST_LAUNCH(k_cbfs_pull_small, blocks_for(c->nsmall * 8), kTB, 0, s, dc, c->d_sdesc,
                    c->d_small, c->nsmall, c->d_bits, d_depth, nq, c->d_cnt, lvl);
       if (c->nchunks)
         SST_LAUNCH(k_cbfs_pull_chunks, warp_blocks(c->nchunks), kTB, 0, s, dc, c->d_cv,

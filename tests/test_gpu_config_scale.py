@@ -147,6 +147,23 @@ def test_multi_source_rows_64_bfs_16_bc(sg, base24):
         assert relerr(got[i], w) <= REL, (i, int(bsrc[i]))
 
 
+def test_hub_source_bc_and_snapshot(sg, base24):
+    """BC and BFS from vertex 0 (the largest RMAT hub) on the scale-24
+    graph and on its byte-width snapshot against the oracle; runs before
+    the update stream below, on the symmetric base graph."""
+    n, g, o = base24
+    want_bc, want_d = o.bc(0), o.bfs(0)
+    scale = max(np.max(np.abs(want_bc)), 1e-300)
+    assert np.max(np.abs(sg.BC(g, 0) - want_bc)) / scale <= REL
+    assert np.array_equal(sg.BFS(g, 0, depths=True), want_d)
+    c = sg.CompactGraph(g)
+    try:
+        assert np.array_equal(c.bfs(0), want_d)
+        assert np.max(np.abs(c.bc(0) - want_bc)) / scale <= REL
+    finally:
+        c.close()
+
+
 def test_update_stream_1e2_to_1e7(sg, base24):
     """Each insert batch: 95% new RMAT edges and 5% sampled existing edges;
     each delete batch: as many sampled existing edges; the CSR after every
