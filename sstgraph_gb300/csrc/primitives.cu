@@ -516,7 +516,7 @@ k_scatter_os(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
     atomicExch(mine, kOsAgg | tcount);
     // the walk loads kOsAhead earlier tiles' words at once, then takes them
     // in order (a word not yet published is polled again on its own)
-    constexpr int kOsAhead = 8;
+    constexpr int kOsAhead = 16;
     bool done = false;
     for (int64_t t0 = (int64_t)tile - 1; t0 >= 0 && !done; t0 -= kOsAhead) {
       uint32_t w[kOsAhead];
