@@ -56,7 +56,14 @@ def args_parse():
                     help="skip the oracle replay of the bench graph's batches")
     ap.add_argument("--pr-iters", type=int, default=10)
     ap.add_argument("--profile-batch", type=int, default=1000000,
-                    help="--only insert-profile: pairs in the profiled insert")
+                    help="--only insert-profile: pairs in the profiled batch")
+    ap.add_argument("--profile-op", default="insert", choices=["insert", "remove"],
+                    help="--only insert-profile: the profiled batch's operation")
+    ap.add_argument("--algo", default="tc", choices=["bfs", "pagerank", "cc", "bc", "tc"],
+                    help="--only algo-profile: the algorithm profiled")
+    ap.add_argument("--graph", default="rmat", choices=["rmat", "er"],
+                    help="--only algo-profile: RMAT (seed 3) or Erdos-Renyi (seed 4), "
+                         "8 * 2^scale generated edges, symmetrised")
     ap.add_argument("--batched-batches", type=int, default=512)
     ap.add_argument("--serve-requests", type=int, default=400)
     # offered load of the serving latency run (requests/s): below the
@@ -65,7 +72,8 @@ def args_parse():
     ap.add_argument("--serve-scale", type=int, default=25)
     ap.add_argument("--only", default="all",
                     choices=["all", "updates", "pagerank", "bfs", "batched", "serving",
-                             "multi", "compact", "extras", "static", "insert-profile"],
+                             "multi", "compact", "extras", "static", "insert-profile",
+                             "algo-profile"],
                     help="one part of the run (profiling cases): the update steps "
                          "alone, or one traversal on the base graph")
     return ap.parse_args()
@@ -287,11 +295,13 @@ def workload_config(a):
 
 
 def insert_profile(a):
-    """One insert batch for a profiler: the scale-`scale` RMAT base graph
-    (seed 5, symmetrised), a warm-up batch of `profile_batch` RMAT pairs
-    (seed 6; it grows the scratch and captures the planning graph), then
-    one more such batch between cudaProfilerStart and cudaProfilerStop, so
-    `ncu --profile-from-start off` sees that batch's launches alone."""
+    """One update batch for a profiler: the scale-`scale` RMAT base graph
+    (seed 5, symmetrised), a warm-up batch of `profile_batch` pairs (it
+    grows the scratch and captures the planning graph), then one more such
+    batch between cudaProfilerStart and cudaProfilerStop, so
+    `ncu --profile-from-start off` sees that batch's launches alone.
+    Inserts are RMAT pairs (seed 6); with --profile-op remove the batches
+    are existing edges sampled from the graph (seed 7)."""
     import torch
 
     import sstgraph_gb300 as sg
@@ -311,14 +321,75 @@ def insert_profile(a):
         for i, y in enumerate(ys):
             sg.gen_rmat(a.scale, b, seed=6, first=i * b, out=y, **RMAT)
     torch.cuda.synchronize()
-    g.insert_batch(ys[0])
+    op = g.insert_batch
+    if a.profile_op == "remove":
+        op = g.remove_batch
+        for i, y in enumerate(ys):
+            g.sample_edges(b, seed=7, first=i * b, out=y)
+        torch.cuda.synchronize()
+    op(ys[0])
     torch.cuda.synchronize()
+    e0, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
     torch.cuda.profiler.start()
-    g.insert_batch(ys[1])
+    e0.record(stream)
+    op(ys[1])
+    e1.record(stream)
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()
-    print(json.dumps({"only": "insert-profile", "scale": a.scale, "batch": b,
-                      "edges": g.M()}))
+    print(json.dumps({"only": "insert-profile", "op": a.profile_op, "scale": a.scale,
+                      "batch": b, "edges": g.M(), "batch_us": e0.elapsed_time(e1) * 1e3}))
+    g.close()
+
+
+def algo_profile(a):
+    """One call of one algorithm for a profiler: the static-analytics graph
+    (RMAT seed 3 or Erdos-Renyi seed 4, 8 * 2^scale generated edges,
+    symmetrised), one warm-up call, then one call between cudaProfilerStart
+    and cudaProfilerStop."""
+    import torch
+
+    import sstgraph_gb300 as sg
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    n = 1 << a.scale
+    g = sg.SparseMatrixV(n)
+    g.set_stream(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        x = torch.empty((8 * n, 2), dtype=torch.int32, device="cuda")
+        if a.graph == "rmat":
+            sg.gen_rmat(a.scale, 8 * n, seed=3, out=x, **RMAT)
+        else:
+            sg.gen_er(n, 8 * n, seed=4, out=x)
+        g.insert_batch(x)
+        g.insert_batch(x.flip(1).contiguous())
+        del x
+    torch.cuda.synchronize()
+    g.release_scratch()
+    sg.autotune(g)
+    out = {"pagerank": torch.empty(n, dtype=torch.float64, device="cuda"),
+           "bc": torch.empty(n, dtype=torch.float64, device="cuda")}
+    d = torch.empty(n, dtype=torch.int32, device="cuda")
+    run = {"bfs": lambda: sg.BFS(g, 0, depths=True, out=d),
+           "pagerank": lambda: sg.PR_S(g, 20, out=out["pagerank"]),
+           "cc": lambda: sg.CC(g, out=d),
+           "bc": lambda: sg.BC(g, 0, out=out["bc"]),
+           "tc": lambda: sg.TC(g)}[a.algo]
+    run()
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    torch.cuda.profiler.start()
+    run()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"only": "algo-profile", "algo": a.algo, "graph": a.graph,
+                      "scale": a.scale, "edges": g.M(), "best_ms": best}))
     g.close()
 
 
@@ -328,6 +399,8 @@ def main():
         return reference_arm(a)
     if a.only == "insert-profile":
         return insert_profile(a)
+    if a.only == "algo-profile":
+        return algo_profile(a)
     import numpy as np
     import torch
 

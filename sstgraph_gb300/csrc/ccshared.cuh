@@ -35,22 +35,44 @@ __device__ __forceinline__ uint32_t ld_par(const uint32_t *par, uint32_t x) {
   return __ldcg(par + x);
 }
 
-// link the trees of u and v; err counts links that gave up (they cannot
-// fail to progress; the bound only keeps every loop finite)
+// the root of x, halving the path on the way: a visited vertex is pointed
+// at its grandparent.  Only roots are ever linked (compare-and-swap on a
+// root's own entry), so a non-root's entry changes only here, and always to
+// one of its ancestors: still its tree, and a smaller id.  Every step moves
+// to a smaller id, so the walk ends.
+__device__ __forceinline__ uint32_t cc_find(uint32_t *par, uint32_t x) {
+  for (;;) {
+    const uint32_t p = ld_par(par, x);
+    if (p == x) return x;
+    const uint32_t gp = ld_par(par, p);
+    if (gp == p) return p;
+    par[x] = gp;
+    x = gp;
+  }
+}
+
+// link the trees of u and v: find both roots, link the larger below the
+// smaller; a failed compare-and-swap means that root was linked meanwhile,
+// so the roots are looked up again.  err counts links that gave up (every
+// failed attempt is another link's progress; the bound only keeps every
+// loop finite).  Without halving, concurrent links build long chains of
+// roots that later links walk again and again.
 __device__ __forceinline__ void cc_link(uint32_t *par, uint32_t u, uint32_t v,
                                         unsigned long long *err) {
+  // the finds start at the parents (usually the roots themselves)
   uint32_t p1 = ld_par(par, u), p2 = ld_par(par, v);
-  for (int it = 0; p1 != p2; it++) {
+  if (p1 == p2) return;
+  for (int it = 0;; it++) {
     if (it == (1 << 20)) {
       atomicAdd(err, 1ull);
       return;
     }
-    const uint32_t hi = max(p1, p2), lo = min(p1, p2);
-    const uint32_t ph = ld_par(par, hi);
-    if (ph == lo) return;
-    if (ph == hi && atomicCAS(&par[hi], hi, lo) == hi) return;
-    p1 = ld_par(par, ld_par(par, hi));
-    p2 = ld_par(par, lo);
+    const uint32_t r1 = cc_find(par, p1), r2 = cc_find(par, p2);
+    if (r1 == r2) return;
+    const uint32_t hi = max(r1, r2), lo = min(r1, r2);
+    if (atomicCAS(&par[hi], hi, lo) == hi) return;
+    p1 = hi;
+    p2 = lo;
   }
 }
 

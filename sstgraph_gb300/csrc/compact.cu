@@ -1230,17 +1230,24 @@ sst_status compact_tc(sst_compact *c, uint64_t *total, uint64_t *d_pv, int sms) 
   }
   uint64_t *off = nullptr, *doff = nullptr;
   uint32_t *cols = nullptr, *keep = nullptr, *pos = nullptr, *adj = nullptr;
+  uint32_t *icnt = nullptr, *ioff = nullptr;
+  uint64_t *items = nullptr;
   cudaError_t e = cudaMalloc(&off, ((uint64_t)n + 1) * 8);
   if (e == cudaSuccess) e = cudaMalloc(&doff, ((uint64_t)n + 1) * 8);
   if (e == cudaSuccess) e = cudaMalloc(&cols, m * 4);
   if (e == cudaSuccess) e = cudaMalloc(&keep, m * 4);
   if (e == cudaSuccess) e = cudaMalloc(&pos, (m + 1) * 4);
   if (e == cudaSuccess) e = cudaMalloc(&adj, m * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&icnt, ((uint64_t)n + 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&ioff, ((uint64_t)n + 1) * 4);
+  // m bounds the oriented entries
+  if (e == cudaSuccess) e = cudaMalloc(&items, tc_items_bound(n, m) * 8);
   if (e == cudaSuccess) {
     st = compact_to_csr(c, off, cols);
     if (st == SST_OK) {
       Arena &A = c->arena;
-      e = A.reserve(scan_scratch_bytes(m, 4) + 4096);
+      e = A.reserve(std::max(scan_scratch_bytes(m, 4), scan_scratch_bytes((uint64_t)n + 1, 4)) +
+                    4096);
       if (e == cudaSuccess) {
         A.reset();
         const DCompact dc = c->view();
@@ -1249,9 +1256,10 @@ sst_status compact_tc(sst_compact *c, uint64_t *total, uint64_t *d_pv, int sms) 
         if (e == cudaSuccess) {
           SST_LAUNCH(k_ctc_fill, blocks_for(m), kTB, 0, s, cols, keep, pos, m, adj);
           SST_LAUNCH(k_ctc_off, blocks_for((uint64_t)n + 1), kTB, 0, s, off, pos, n, m, doff);
-          e = cudaMemsetAsync(c->d_cnt, 0, 8, s);
+          e = cudaMemsetAsync(c->d_cnt, 0, 16, s);  // count, work cursor
+          A.reset();
           if (e == cudaSuccess)
-            e = tc_count_launch(doff, adj, n, c->d_cnt,
+            e = tc_count_launch(doff, adj, n, m, TcScratch{icnt, ioff, items}, A, c->d_cnt,
                                 reinterpret_cast<unsigned long long *>(d_pv), sms, s);
           if (e == cudaSuccess)
             e = cudaMemcpyAsync(c->h_cnt, c->d_cnt, 8, cudaMemcpyDeviceToHost, s);
@@ -1262,7 +1270,7 @@ sst_status compact_tc(sst_compact *c, uint64_t *total, uint64_t *d_pv, int sms) 
     }
   }
   for (void *p : {(void *)off, (void *)doff, (void *)cols, (void *)keep, (void *)pos,
-                  (void *)adj})
+                  (void *)adj, (void *)icnt, (void *)ioff, (void *)items})
     if (p) cudaFree(p);
   if (st != SST_OK) return st;
   SST_CUDA_TRY(e);

@@ -1170,6 +1170,14 @@ void graph_release(sst_graph *g) {
   if (g->merge_done) cudaEventDestroy(g->merge_done);
   g->side = nullptr;
   g->fork_ev = g->merge_done = nullptr;
+  for (int k = 0; k < 2; k++) {
+    if (g->aux[k]) cudaStreamDestroy(g->aux[k]);
+    if (g->aux_join[k]) cudaEventDestroy(g->aux_join[k]);
+    g->aux[k] = nullptr;
+    g->aux_join[k] = nullptr;
+  }
+  if (g->aux_fork) cudaEventDestroy(g->aux_fork);
+  g->aux_fork = nullptr;
   g->stream = nullptr;
 }
 
@@ -1519,6 +1527,28 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     SST_CUDA_TRY(cudaEventCreateWithFlags(&g->fork_ev, cudaEventDisableTiming));
     SST_CUDA_TRY(cudaEventCreateWithFlags(&g->merge_done, cudaEventDisableTiming));
   }
+  if (!g->aux_fork) {
+    for (int k = 0; k < 2; k++) {
+      SST_CUDA_TRY(cudaStreamCreateWithFlags(&g->aux[k], cudaStreamNonBlocking));
+      SST_CUDA_TRY(cudaEventCreateWithFlags(&g->aux_join[k], cudaEventDisableTiming));
+    }
+    SST_CUDA_TRY(cudaEventCreateWithFlags(&g->aux_fork, cudaEventDisableTiming));
+  }
+  // run k independent pieces of work on aux[0..k-1] beside the stream
+  auto fork_aux = [&](cudaStream_t from, int k) -> cudaError_t {
+    cudaError_t e = cudaEventRecord(g->aux_fork, from);
+    for (int i = 0; i < k && e == cudaSuccess; i++)
+      e = cudaStreamWaitEvent(g->aux[i], g->aux_fork, 0);
+    return e;
+  };
+  auto join_aux = [&](cudaStream_t to, int k) -> cudaError_t {
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < k && e == cudaSuccess; i++) {
+      e = cudaEventRecord(g->aux_join[i], g->aux[i]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(to, g->aux_join[i], 0);
+    }
+    return e;
+  };
 
   // 2-8: sort to plan.  For a given batch size and graph layout this is a
   // fixed sequence of launches over device-resident counts; `fork` starts
@@ -1573,10 +1603,13 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     // the scans run out of place into merge_jk and mtpos, which hold nothing
     // until the merge/task scan and k_emit below overwrite them
     uint64_t *fscan = merge_jk, *bscan = mtpos;
+    // the two are independent: the backward one runs beside the forward one
+    SST_CUDA_TRY(fork_aux(s, 1));
     SST_CUDA_TRY((scan<uint64_t, OpMax>(fkey, fscan, b, 0ull, OpMax{}, true, false,
                                         nullptr, A, s)));
     SST_CUDA_TRY((scan<uint64_t, OpMin>(bkey, bscan, b, ~0ull, OpMin{}, true, true,
-                                        nullptr, A, s)));
+                                        nullptr, A, g->aux[0])));
+    SST_CUDA_TRY(join_aux(s, 1));
     SST_LAUNCH_PDL(k_dom_classify, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
                fscan, bscan, &P->n_groups, b, mt);
     // totals land as one word on (n_merge, n_tasks), adjacent in the plan
@@ -1595,12 +1628,15 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     SST_LAUNCH_PDL(k_task_setup, wgrid, kTB, 0, s, dg, fill_inv_q24(g->params.grow_fill), insert,
                p_ul, g_start, gtype, gw0, gw1, task_group, &P->n_tasks, &P->n_items, b, T,
                P->class_cnt);
+    // three independent scans, two of them beside the stream
+    SST_CUDA_TRY(fork_aux(s, 2));
     SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.total, T.out, b, 0ull, OpAdd{}, true,
                                         false, &P->task_elems, A, s, &P->n_tasks)));
     SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.nsrc, T.soff, b, 0ull, OpAdd{}, true,
-                                        false, &P->src_leaves, A, s, &P->n_tasks)));
+                                        false, &P->src_leaves, A, g->aux[0], &P->n_tasks)));
     SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.ndst, T.doff, b, 0ull, OpAdd{}, true,
-                                        false, &P->dst_leaves, A, s, &P->n_tasks)));
+                                        false, &P->dst_leaves, A, g->aux[1], &P->n_tasks)));
+    SST_CUDA_TRY(join_aux(s, 2));
     SST_CUDA_TRY(cudaMemcpyAsync(g->h_plan, P, sizeof(PlanSummary),
                                  cudaMemcpyDeviceToHost, s));
     SST_CUDA_TRY(cudaMemcpyAsync(&g->h_plan->apply_err, g->d_err, 8,

@@ -56,6 +56,11 @@ struct sst_graph {
   cudaStream_t side = nullptr;  // an update's leaf merges, beside its tasks;
                                 // its planning launches are captured here
   cudaEvent_t fork_ev = nullptr, merge_done = nullptr;
+  // independent scans of an update's planning sequence run here, forked
+  // from its stream and joined back (inside a captured plan: parallel
+  // branches of the graph)
+  cudaStream_t aux[2] = {nullptr, nullptr};
+  cudaEvent_t aux_fork = nullptr, aux_join[2] = {nullptr, nullptr};
   sst::PlanCache *plans = nullptr;  // captured planning launches
   bool plan_graphs = true;  // replay planning launches (off: launch directly)
   bool plan_direct = false; // with plan_graphs: launch them directly, in the

@@ -90,8 +90,8 @@ struct TravState {
   // cc
   DevBuf<uint32_t> par;
   // tc
-  DevBuf<uint64_t> toff, tlpre, tlcnt;
-  DevBuf<uint32_t> tadj;
+  DevBuf<uint64_t> toff, tlpre, tlcnt, titems;
+  DevBuf<uint32_t> tadj, tmask;
   // multi-source bfs: per-vertex source masks (visited, frontier, next)
   DevBuf<unsigned long long> mvis, mfr, mfr2, mnx, msrc;
   DevBuf<int32_t> mdepth;
@@ -146,6 +146,8 @@ static void trav_buffers_release(TravState *t) {
   t->tlpre.release();
   t->tlcnt.release();
   t->tadj.release();
+  t->titems.release();
+  t->tmask.release();
   t->mvis.release();
   t->mfr.release();
   t->mfr2.release();
@@ -195,7 +197,8 @@ uint64_t trav_device_bytes(const sst_graph *g) {
   add(t->il0.cap, 4); add(t->depth_tmp.cap, 4); add(t->parent_tmp.cap, 4);
   add(t->sigma.cap, 8); add(t->ratio.cap, 8); add(t->lvl_list.cap, 4);
   add(t->lvl_cnt.cap, 4); add(t->par.cap, 4); add(t->toff.cap, 8); add(t->tlpre.cap, 8);
-  add(t->tlcnt.cap, 8); add(t->tadj.cap, 4); add(t->mvis.cap, 8); add(t->mfr.cap, 8);
+  add(t->tlcnt.cap, 8); add(t->tadj.cap, 4); add(t->titems.cap, 8); add(t->tmask.cap, 4);
+  add(t->mvis.cap, 8); add(t->mfr.cap, 8);
   add(t->mfr2.cap, 8); add(t->mnx.cap, 8); add(t->msrc.cap, 8); add(t->mdepth.cap, 4);
   add(t->msig.cap, 8); add(t->mrat.cap, 8); add(t->mpart.cap, 8); add(t->mlist.cap, 4);
   add(t->micnt.cap, 4); add(t->mioff.cap, 4); add(t->miv.cap, 4); add(t->mil0.cap, 4);
@@ -1075,41 +1078,75 @@ __global__ void k_delta_small(DGraph g, const uint32_t *__restrict__ list,
 // ------------------------------------------------------------- tc
 // orientation and counting in tcshared.cuh
 
+// The orientation passes take kTcLeaves leaves a warp, all their loads
+// issued before any is used (a leaf alone is three dependent round trips:
+// its directory entry, its line, its ids' degrees).  The count pass also
+// records each leaf's keep mask, so the fill pass needs no degree lookups.
+constexpr int kTcLeaves = 4;
+
 __global__ void k_tc_leafcount(const uint32_t *__restrict__ slots,
                                const uint32_t *__restrict__ owner,
                                const uint64_t *__restrict__ slot,
                                const uint32_t *__restrict__ cnt,
                                uint64_t nleaves, const uint32_t *__restrict__ deg,
-                               uint64_t *__restrict__ out) {
-  uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+                               uint64_t *__restrict__ out, uint32_t *__restrict__ kmask) {
+  const uint64_t k0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kTcLeaves;
   const int lane = threadIdx.x & 31;
-  if (k >= nleaves) return;
-  uint32_t u = owner[k];
-  bool keep = false;
-  if ((uint32_t)lane < cnt[k]) keep = ranks_above(deg, slots[slot[k] + lane], u);
-  uint32_t m = __ballot_sync(0xffffffffu, keep);
-  if (lane == 0) out[k] = __popc(m);
+  if (k0 >= nleaves) return;
+  uint32_t u[kTcLeaves], c[kTcLeaves], x[kTcLeaves];
+  uint64_t sl[kTcLeaves];
+#pragma unroll
+  for (int j = 0; j < kTcLeaves; j++) {
+    const uint64_t k = k0 + j;
+    u[j] = 0;
+    c[j] = 0;
+    sl[j] = 0;
+    if (k < nleaves) {
+      u[j] = owner[k];
+      sl[j] = slot[k];
+      c[j] = cnt[k];
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kTcLeaves; j++) x[j] = (uint32_t)lane < c[j] ? slots[sl[j] + lane] : 0u;
+#pragma unroll
+  for (int j = 0; j < kTcLeaves; j++) {
+    const bool keep = (uint32_t)lane < c[j] && ranks_above(deg, x[j], u[j]);
+    const uint32_t m = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0 && k0 + j < nleaves) {
+      out[k0 + j] = __popc(m);
+      kmask[k0 + j] = m;
+    }
+  }
 }
 
 __global__ void k_tc_fill(const uint32_t *__restrict__ slots,
-                          const uint32_t *__restrict__ owner,
-                          const uint64_t *__restrict__ slot,
-                          const uint32_t *__restrict__ cnt, uint64_t nleaves,
-                          const uint32_t *__restrict__ deg,
+                          const uint64_t *__restrict__ slot, uint64_t nleaves,
+                          const uint32_t *__restrict__ kmask,
                           const uint64_t *__restrict__ lpre,
                           uint32_t *__restrict__ adj) {
-  uint64_t k = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t k0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kTcLeaves;
   const int lane = threadIdx.x & 31;
-  if (k >= nleaves) return;
-  uint32_t u = owner[k];
-  uint32_t w = 0;
-  bool keep = false;
-  if ((uint32_t)lane < cnt[k]) {
-    w = slots[slot[k] + lane];
-    keep = ranks_above(deg, w, u);
+  if (k0 >= nleaves) return;
+  uint32_t m[kTcLeaves], x[kTcLeaves];
+  uint64_t sl[kTcLeaves], at[kTcLeaves];
+#pragma unroll
+  for (int j = 0; j < kTcLeaves; j++) {
+    const uint64_t k = k0 + j;
+    m[j] = 0;
+    sl[j] = 0;
+    at[j] = 0;
+    if (k < nleaves) {
+      m[j] = kmask[k];
+      sl[j] = slot[k];
+      at[j] = lpre[k];
+    }
   }
-  uint32_t m = __ballot_sync(0xffffffffu, keep);
-  if (keep) adj[lpre[k] + __popc(m & ((1u << lane) - 1u))] = w;
+#pragma unroll
+  for (int j = 0; j < kTcLeaves; j++) x[j] = (m[j] >> lane) & 1u ? slots[sl[j] + lane] : 0u;
+#pragma unroll
+  for (int j = 0; j < kTcLeaves; j++)
+    if ((m[j] >> lane) & 1u) adj[at[j] + __popc(m[j] & ((1u << lane) - 1u))] = x[j];
 }
 
 __global__ void k_tc_off(const uint64_t *__restrict__ vleaf,
@@ -1588,27 +1625,36 @@ sst_status tc(sst_graph *g, uint64_t *total, uint64_t *d_pv) {
   uint64_t nl = D.nleaves;
   SST_CUDA_TRY(t->tlcnt.ensure(nl + 1));
   SST_CUDA_TRY(t->tlpre.ensure(nl + 1));
+  SST_CUDA_TRY(t->tmask.ensure(nl + 1));
   SST_CUDA_TRY(t->toff.ensure((uint64_t)n + 1));
   g->arena.reset();
   SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes(nl + 1, 8) + 4096));
+  const uint64_t tc_warps = (nl + kTcLeaves - 1) / kTcLeaves;
   if (nl)
-    SST_LAUNCH(k_tc_leafcount, warp_blocks(nl), kTB, 0, s, g->d_slots, D.owner,
-               D.slot, D.cnt, nl, g->d_deg, t->tlcnt.p);
+    SST_LAUNCH(k_tc_leafcount, warp_blocks(tc_warps), kTB, 0, s, g->d_slots, D.owner,
+               D.slot, D.cnt, nl, g->d_deg, t->tlcnt.p, t->tmask.p);
   SST_CUDA_TRY((scan<uint64_t, OpAdd>(t->tlcnt.p, t->tlpre.p, nl, 0ull, OpAdd{},
                                       true, false, t->tlpre.p + nl, g->arena, s)));
   uint64_t madj = 0;
   SST_CUDA_TRY(cudaMemcpyAsync(&madj, t->tlpre.p + nl, 8, cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));
   SST_CUDA_TRY(t->tadj.ensure(madj + 1));
+  SST_CUDA_TRY(t->icnt.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->ioff.ensure((uint64_t)n + 1));
+  SST_CUDA_TRY(t->titems.ensure(tc_items_bound(n, madj)));
+  g->arena.reset();
+  SST_CUDA_TRY(g->arena.reserve(scan_scratch_bytes((uint64_t)n + 1, 4) + 4096));
   if (nl)
-    SST_LAUNCH(k_tc_fill, warp_blocks(nl), kTB, 0, s, g->d_slots, D.owner, D.slot,
-               D.cnt, nl, g->d_deg, t->tlpre.p, t->tadj.p);
+    SST_LAUNCH(k_tc_fill, warp_blocks(tc_warps), kTB, 0, s, g->d_slots, D.slot, nl,
+               t->tmask.p, t->tlpre.p, t->tadj.p);
   SST_LAUNCH(k_tc_off, blocks_for((uint64_t)n + 1), kTB, 0, s, D.vleaf,
              t->tlpre.p, n, t->toff.p);
-  SST_CUDA_TRY(cudaMemsetAsync(t->d_small, 0, 8, s));
+  SST_CUDA_TRY(cudaMemsetAsync(t->d_small, 0, 16, s));  // count, work cursor
   if (d_pv) SST_CUDA_TRY(cudaMemsetAsync(d_pv, 0, (uint64_t)n * 8, s));
   if (n)
-    SST_CUDA_TRY(tc_count_launch(t->toff.p, t->tadj.p, n, t->d_small,
+    SST_CUDA_TRY(tc_count_launch(t->toff.p, t->tadj.p, n, madj,
+                                 TcScratch{t->icnt.p, t->ioff.p, t->titems.p}, g->arena,
+                                 t->d_small,
                                  reinterpret_cast<unsigned long long *>(d_pv), g->sms, s));
   SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, t->d_small, 8, cudaMemcpyDeviceToHost, s));
   SST_CUDA_TRY(cudaStreamSynchronize(s));

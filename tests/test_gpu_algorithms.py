@@ -77,6 +77,30 @@ def test_tc(sg, pair):
     te, pve = o.tc(per_vertex=True)
     assert t == te
     assert np.array_equal(pv, pve)
+    assert sg.TC(g) == te  # the count-only kernel
+
+
+def test_tc_lists_longer_than_the_set(sg):
+    """A vertex whose list of higher-ranked neighbours outgrows the
+    shared-memory set (more than 1024 entries) is counted by binary search:
+    a clique of 1030 vertices, each also tied to a hub of larger degree, so
+    clique vertex i keeps the 1029 - i clique vertices above it and the
+    hub."""
+    k, n = 1030, 1030 + 1 + 1200
+    hub = k
+    rows, cols = np.triu_indices(k, 1)
+    e = [np.stack([rows, cols], 1), np.stack([np.full(k, hub), np.arange(k)], 1),
+         np.stack([np.full(1200, hub), np.arange(k + 1, n)], 1)]
+    pairs = oracle.symmetrize(np.concatenate(e).astype(np.uint32))
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    g.insert_batch(pairs)
+    o.insert_batch(pairs)
+    t, pv = sg.TC(g, per_vertex=True)
+    te, pve = o.tc(per_vertex=True)
+    assert t == te and sg.TC(g) == te
+    assert np.array_equal(pv, pve)
+    g.close()
 
 
 def test_traversals_refuse_non_square_graph(sg):

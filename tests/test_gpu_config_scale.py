@@ -106,6 +106,7 @@ def test_static_tc(sg, static_pair):
     te, pve = o.tc(per_vertex=True)
     assert t == te
     assert np.array_equal(pv, pve)
+    assert sg.TC(g) == te  # the count-only kernel
 
 
 def test_static_pagerank_20(sg, static_pair):
