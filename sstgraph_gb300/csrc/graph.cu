@@ -114,9 +114,12 @@ __device__ __forceinline__ uint32_t warp_sum_lcnt(const uint8_t *lc,
   return __reduce_add_sync(0xffffffffu, s);
 }
 
-// count word of an item's leaf: the leaf's element count, plus this bit
-// when the row is a multi-leaf segment (its leaves keep counts in lcnt)
+// count word of an item's leaf: the leaf's element count (bits 0-7), plus
+// this bit when the row is a multi-leaf segment (its leaves keep counts in
+// lcnt), else the one-leaf row's capacity (0..32) from bit kCapShift
 constexpr uint32_t kMultiLeaf = 1u << 8;
+constexpr int kCapShift = 16;
+__device__ __forceinline__ uint32_t one_leaf_cap(uint32_t cw) { return cw >> kCapShift; }
 
 // ---------------------------------------------------------------- steps 1-5
 // Keys of a batch, in one of two forms.
@@ -241,7 +244,7 @@ __global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
     if (present && insert && wv && g.vals)
       g.vals[base + ((uint64_t)l << kLeafLog) + pos] = wv[i];
     S = base + ((uint64_t)l << kLeafLog);
-    cw = c | (cap > kLeaf ? kMultiLeaf : 0u);
+    cw = c | (cap > kLeaf ? kMultiLeaf : cap << kCapShift);
   }
   flag[i] = insert ? !present : present;
   leaf_out[i] = l;
@@ -308,7 +311,12 @@ struct GroupStartEpi {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); \
        i += (uint64_t)gridDim.x * blockDim.x)
 
-__global__ void k_classify_insert(DGraph g, const uint64_t *__restrict__ p_ul,
+// The count word of the group's first item (its leaf's count and, for a
+// one-leaf row, the row's capacity, as k_locate read them; nothing has
+// changed either since) decides, so no vertex record or leaf count is read
+// again.
+__global__ void k_classify_insert(const uint64_t *__restrict__ p_ul,
+                                  const uint32_t *__restrict__ p_c,
                                   const uint32_t *__restrict__ g_start,
                                   const uint32_t *__restrict__ d_ngroups,
                                   uint8_t *__restrict__ gtype,
@@ -320,20 +328,19 @@ __global__ void k_classify_insert(DGraph g, const uint64_t *__restrict__ p_ul,
   pdl_wait();
   const uint32_t ng = *d_ngroups;
   GRID_STRIDE(gid, ng) {
-    uint32_t j0 = g_start[gid], k = g_start[gid + 1] - j0;
-    uint64_t key = p_ul[j0];
-    uint32_t u = (uint32_t)(key >> 32), leaf = (uint32_t)key;
-    uint32_t cap = g.cap[u];
+    const uint32_t j0 = g_start[gid], k = g_start[gid + 1] - j0;
+    const uint32_t leaf = (uint32_t)p_ul[j0];
+    const uint32_t cw = p_c[j0], c = cw & 0xff;
     uint8_t type = kMerge;
     uint32_t lev = 0, w0 = leaf, w1 = leaf + 1;
-    if (cap <= kLeaf) {
-      if (g.deg[u] + k > cap) {
+    if (!(cw & kMultiLeaf)) {
+      if (c + k > one_leaf_cap(cw)) {  // a one-leaf row's count is its degree
         type = kResize;
         lev = 31;
         w0 = 0;
         w1 = 1;
       }
-    } else if (g.lcnt[(g.base[u] >> kLeafLog) + leaf] + k > kLeaf) {
+    } else if (c + k > kLeaf) {
       type = kNone;  // decided by the climb
       climb[atomicAdd(nclimb, 1u)] = (uint32_t)gid;
     }
@@ -365,11 +372,12 @@ __device__ __forceinline__ uint32_t leaf_slot(uint32_t linev, uint64_t S,
 // window's lower bound in a multi-leaf segment, window_lower(p, 0, H), the
 // same for every H >= 1 (computed once on the host: no per-group FP64).
 // A warp takes 32 groups at a time: lane l first loads group l's item
-// range, its first item's leaf
-// start, count word and key, and its row's capacity (three dependent loads
-// for all 32 groups at once), then the groups go kGroupsPerWarp at a time
-// with their items and leaf lines loaded together, one dependent load per
-// batch.
+// range, its first item's leaf start, count word and key (two dependent
+// loads for all 32 groups at once), then the
+// groups' leaves go kGroupsPerWarp at a time with their items and leaf
+// lines loaded together, one dependent load per batch; the bookkeeping
+// (leaf count, degree, classification) runs once for all 32 groups, lane l
+// for group l.
 __global__ void __launch_bounds__(256, 4)
 k_leaf_delete(DGraph g, uint32_t lo_leaf, const uint64_t *__restrict__ p_ul,
               const uint32_t *__restrict__ p_x,
@@ -394,10 +402,13 @@ k_leaf_delete(DGraph g, uint32_t lo_leaf, const uint64_t *__restrict__ p_ul,
     const uint32_t cwl = okl ? p_c[j0l] : 0;
     const uint64_t keyl = okl ? p_ul[j0l] : 0;
     const uint32_t ul = (uint32_t)(keyl >> 32), leafl = (uint32_t)keyl;
-    const uint32_t capl = okl ? g.cap[ul] : 0;
+    // a one-leaf row's capacity is in its count word; a multi-leaf row
+    // only needs to be told apart
+    const uint32_t capl = (cwl & kMultiLeaf) ? kLeaf + 1 : one_leaf_cap(cwl);
     const uint32_t cnt = ng - w * 32 < 32 ? (uint32_t)(ng - w * 32) : 32u;
+    uint32_t my_nc = 0;  // lane l: group l's count after the deletes
     for (uint32_t q0 = 0; q0 < cnt; q0 += Q) {
-      uint32_t j0[Q], k[Q], d[Q], linev[Q], cw[Q], u[Q], cp[Q], lf[Q];
+      uint32_t j0[Q], k[Q], d[Q], linev[Q], cw[Q];
       uint64_t S[Q];
       bool ok[Q];
 #pragma unroll
@@ -408,9 +419,6 @@ k_leaf_delete(DGraph g, uint32_t lo_leaf, const uint64_t *__restrict__ p_ul,
         k[q] = ok[q] ? __shfl_sync(0xffffffffu, kl, src) : 0;
         S[q] = __shfl_sync(0xffffffffu, Sl, src);
         cw[q] = __shfl_sync(0xffffffffu, cwl, src);
-        u[q] = __shfl_sync(0xffffffffu, ul, src);
-        cp[q] = __shfl_sync(0xffffffffu, capl, src);
-        lf[q] = __shfl_sync(0xffffffffu, leafl, src);
       }
 #pragma unroll
       for (int q = 0; q < Q; q++) {
@@ -424,38 +432,51 @@ k_leaf_delete(DGraph g, uint32_t lo_leaf, const uint64_t *__restrict__ p_ul,
         const uint32_t a = leaf_slot(linev[q], S[q], c, lane);
         bool del = false;
         for (uint32_t j = 0; j < k[q]; j++) del |= (__shfl_sync(0xffffffffu, d[q], j) == a);
-        bool keep = (uint32_t)lane < c && !del;
-        uint32_t mask = __ballot_sync(0xffffffffu, keep);
-        uint32_t pos = __popc(mask & ((1u << lane) - 1u));
-        const uint32_t av = (g.vals && (uint32_t)lane < c) ? g.vals[S[q] + lane] : 0u;
-        __syncwarp();
-        if (keep) g.slots[S[q] + pos] = a;
-        if (keep && g.vals) g.vals[S[q] + pos] = av;
-        if ((uint32_t)lane >= c - k[q] && (uint32_t)lane < c) g.slots[S[q] + lane] = kEmpty;
-        if (lane == 0) {
-          const uint32_t nc = c - k[q];
-          if (cw[q] & kMultiLeaf) g.lcnt[S[q] >> kLeafLog] = (uint8_t)nc;
-          atomicSub(&g.deg[u[q]], k[q]);
-          const uint32_t gid = (uint32_t)(w * 32) + q0 + q;
-          uint8_t type = kNone;
-          uint32_t lev = 0, w0 = lf[q], w1 = lf[q] + 1;
-          if (cp[q] <= kLeaf) {
-            if (nc == 0 || (cp[q] > 1 && 4 * nc <= cp[q])) {
-              type = kResize;
-              lev = 31;
-              w0 = 0;
-              w1 = 1;
-            }
-          } else if (nc < lo_leaf) {
-            climb[atomicAdd(nclimb, 1u)] = gid;
-          }
-          gtype[gid] = type;
-          glev[gid] = (uint8_t)lev;
-          gw0[gid] = w0;
-          gw1[gid] = w1;
+        const bool keep = (uint32_t)lane < c && !del;
+        const uint32_t mask = __ballot_sync(0xffffffffu, keep);
+        const uint32_t pos = __popc(mask & ((1u << lane) - 1u));
+        if (g.vals) {
+          const uint32_t av = (uint32_t)lane < c ? g.vals[S[q] + lane] : 0u;
+          __syncwarp();  // every value read before any is moved
+          if (keep) g.vals[S[q] + pos] = av;
         }
-        __syncwarp();
+        // the ids come from registers: no lane reads the line again
+        if (keep) g.slots[S[q] + pos] = a;
+        if ((uint32_t)lane >= c - k[q] && (uint32_t)lane < c) g.slots[S[q] + lane] = kEmpty;
+        if (lane == (int)((q0 + q) & 31)) my_nc = c - k[q];
       }
+    }
+    // the chunk's bookkeeping, lane l for group l
+    const uint32_t gid = (uint32_t)(w * 32) + lane;
+    bool to_climb = false;
+    if (okl) {
+      const uint32_t nc = my_nc;
+      if (cwl & kMultiLeaf) g.lcnt[Sl >> kLeafLog] = (uint8_t)nc;
+      atomicSub(&g.deg[ul], kl);
+      uint8_t type = kNone;
+      uint32_t lev = 0, w0 = leafl, w1 = leafl + 1;
+      if (capl <= kLeaf) {
+        if (nc == 0 || (capl > 1 && 4 * nc <= capl)) {
+          type = kResize;
+          lev = 31;
+          w0 = 0;
+          w1 = 1;
+        }
+      } else if (nc < lo_leaf) {
+        to_climb = true;
+      }
+      gtype[gid] = type;
+      glev[gid] = (uint8_t)lev;
+      gw0[gid] = w0;
+      gw1[gid] = w1;
+    }
+    // one reservation in the climb list for the warp's climbing groups
+    const uint32_t cm = __ballot_sync(0xffffffffu, to_climb);
+    if (cm) {
+      uint32_t at = 0;
+      if (lane == __ffs(cm) - 1) at = atomicAdd(nclimb, (uint32_t)__popc(cm));
+      at = __shfl_sync(0xffffffffu, at, __ffs(cm) - 1);
+      if (to_climb) climb[at + __popc(cm & ((1u << lane) - 1u))] = gid;
     }
   }
 }
@@ -633,70 +654,140 @@ struct Tasks {
   const uint32_t *p_w;      // weighted graphs: values of the packed items
 };
 
-// warp per task slot (all gmax slots, so the prefix scans see zeros beyond
-// the task count)
+// Task setup in two passes.  The first takes the task slots a lane each: a
+// resize of a one-leaf row -- the common task -- is set up right there (the
+// row has one group, so its new items are that group's: no search; the
+// lanes' capacity-class ranks come from one atomic per class and warp);
+// every other task (windows, resizes of multi-leaf rows) goes to a list
+// that the second pass works through a warp per task (a window's leaf
+// counts and the row's item range by warp searches).
+__device__ __forceinline__ void task_store(Tasks &t, uint64_t tid, uint32_t u, uint32_t w0,
+                                           uint64_t nsrc, uint64_t ndst, uint32_t nb,
+                                           uint32_t ne, uint64_t old, uint64_t capn,
+                                           uint32_t rank, uint8_t type) {
+  t.u[tid] = u;
+  t.w0[tid] = w0;
+  t.key[tid] = ((uint64_t)u << 32) | w0;
+  t.nsrc[tid] = nsrc;
+  t.ndst[tid] = ndst;
+  t.newbeg[tid] = nb;
+  t.newend[tid] = ne;
+  t.total[tid] = old + (ne - nb);
+  t.capn[tid] = capn;
+  t.rank[tid] = rank;
+  t.type[tid] = type;
+}
+
 __global__ void k_task_setup(DGraph g, uint64_t inv_fill, bool insert,
                              const uint64_t *__restrict__ p_ul,
                              const uint32_t *__restrict__ g_start,
                              const uint8_t *__restrict__ gtype,
-                             const uint32_t *__restrict__ gw0,
-                             const uint32_t *__restrict__ gw1,
                              const uint32_t *__restrict__ task_group,
-                             const uint32_t *__restrict__ d_ntasks,
-                             const uint32_t *__restrict__ d_nitems,
-                             uint64_t gmax, Tasks t,
-                             uint32_t *__restrict__ class_cnt) {
+                             const uint32_t *__restrict__ d_ntasks, Tasks t,
+                             uint32_t *__restrict__ class_cnt,
+                             uint32_t *__restrict__ hard, uint32_t *__restrict__ nhard) {
   pdl_wait();
   const int lane = threadIdx.x & 31;
-  const uint32_t ntasks = *d_ntasks, nitems = *d_nitems;
-  for (uint64_t tid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-       tid < ntasks; tid += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
-  uint32_t gid = task_group[tid];
-  const uint32_t j0 = g_start[gid];
-  uint32_t u = (uint32_t)(p_ul[j0] >> 32);
-  uint8_t type = gtype[gid];
-  uint64_t base = g.base[u];
-  uint32_t cap = g.cap[u], deg = g.deg[u];
-  uint64_t kk = (uint64_t)u << 32;
-  uint32_t w0, nsrc, nb = 0, ne = 0;
-  uint64_t old, capn = 0, ndst;
-  uint32_t rank = 0;
-  if (type == kWindow) {
-    w0 = gw0[gid];
-    uint32_t w1 = gw1[gid];
-    nsrc = w1 - w0;
-    old = warp_sum_lcnt(g.lcnt, (base >> kLeafLog) + w0, (base >> kLeafLog) + w1);
-    if (insert) {  // the group's first item lies between the two bounds
-      nb = warp_lb_u64(p_ul, 0, j0 + 1, kk | w0);
-      ne = warp_lb_u64(p_ul, j0, nitems, kk | w1);
+  const uint32_t full = 0xffffffffu;
+  const uint32_t ntasks = *d_ntasks;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       w * 32 < ntasks; w += nwarps) {
+    const uint64_t tid = w * 32 + lane;
+    const bool ok = tid < ntasks;
+    const uint32_t gid = ok ? task_group[tid] : 0u;
+    const uint32_t j0 = ok ? g_start[gid] : 0u;
+    const uint32_t j1 = ok ? g_start[gid + 1] : 0u;
+    const uint32_t u = ok ? (uint32_t)(p_ul[j0] >> 32) : 0u;
+    const uint8_t type = ok ? gtype[gid] : (uint8_t)kNone;
+    const uint32_t cap = ok ? g.cap[u] : 0u;
+    // a resize of a one-leaf (or empty) row, set up by this lane
+    const bool simple = ok && type != kWindow && cap <= kLeaf;
+    uint32_t cls = kEmpty;  // capacity class taking a rank, else none
+    uint64_t capn = 0;
+    uint32_t nb = 0, ne = 0, deg = 0;
+    if (simple) {
+      deg = g.deg[u];
+      if (insert) {
+        nb = j0;
+        ne = j1;
+      }
+      capn = cap_for((uint64_t)deg + (ne - nb), inv_fill);
+      if (capn > 0) cls = log2_floor(capn);
     }
-    ndst = nsrc;
-  } else {
-    w0 = 0;
-    nsrc = cap == 0 ? 0 : nleaves_of(cap);
-    old = deg;
-    if (insert) {
-      nb = warp_lb_u64(p_ul, 0, j0 + 1, kk);
-      ne = warp_lb_u64(p_ul, j0, nitems, kk + (1ull << 32));
+    // one rank reservation per class among the warp's simple lanes
+    const uint32_t peers = __match_any_sync(full, cls);
+    const int leader = __ffs(peers) - 1;
+    uint32_t rbase = 0;
+    if (cls != kEmpty && lane == leader) rbase = atomicAdd(&class_cnt[cls], (uint32_t)__popc(peers));
+    rbase = __shfl_sync(full, rbase, leader);
+    if (simple) {
+      const uint32_t rank = cls != kEmpty ? rbase + __popc(peers & ((1u << lane) - 1u)) : 0u;
+      const uint64_t ndst = capn == 0 ? 0 : nleaves_of((uint32_t)capn);
+      task_store(t, tid, u, 0, cap == 0 ? 0 : nleaves_of(cap), ndst, nb, ne, deg, capn,
+                 rank, type);
     }
-    capn = cap_for(old + (ne - nb), inv_fill);
-    ndst = capn == 0 ? 0 : nleaves_of((uint32_t)capn);
-    if (lane == 0 && capn > 0) rank = atomicAdd(&class_cnt[log2_floor(capn)], 1u);
+    // the rest to the second pass, one reservation for the warp
+    const uint32_t hm = __ballot_sync(full, ok && !simple);
+    if (hm) {
+      uint32_t at = 0;
+      if (lane == __ffs(hm) - 1) at = atomicAdd(nhard, (uint32_t)__popc(hm));
+      at = __shfl_sync(full, at, __ffs(hm) - 1);
+      if (ok && !simple) hard[at + __popc(hm & ((1u << lane) - 1u))] = (uint32_t)tid;
+    }
   }
-  if (lane == 0) {
-    t.u[tid] = u;
-    t.w0[tid] = w0;
-    t.key[tid] = kk | w0;
-    t.nsrc[tid] = nsrc;
-    t.ndst[tid] = ndst;
-    t.newbeg[tid] = nb;
-    t.newend[tid] = ne;
-    t.total[tid] = old + (ne - nb);
-    t.capn[tid] = capn;
-    t.rank[tid] = rank;
-    t.type[tid] = type;
-  }
-  __syncwarp();
+}
+
+__global__ void k_task_setup_hard(DGraph g, uint64_t inv_fill, bool insert,
+                                  const uint64_t *__restrict__ p_ul,
+                                  const uint32_t *__restrict__ g_start,
+                                  const uint8_t *__restrict__ gtype,
+                                  const uint32_t *__restrict__ gw0,
+                                  const uint32_t *__restrict__ gw1,
+                                  const uint32_t *__restrict__ task_group,
+                                  const uint32_t *__restrict__ hard,
+                                  const uint32_t *__restrict__ nhard,
+                                  const uint32_t *__restrict__ d_nitems, Tasks t,
+                                  uint32_t *__restrict__ class_cnt) {
+  pdl_wait();
+  const int lane = threadIdx.x & 31;
+  const uint32_t nh = *nhard, nitems = *d_nitems;
+  for (uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nh;
+       i += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+    const uint32_t tid = hard[i];
+    const uint32_t gid = task_group[tid];
+    const uint32_t j0 = g_start[gid];
+    const uint32_t u = (uint32_t)(p_ul[j0] >> 32);
+    const uint8_t type = gtype[gid];
+    const uint64_t base = g.base[u];
+    const uint32_t cap = g.cap[u];
+    const uint64_t kk = (uint64_t)u << 32;
+    uint32_t w0, b = 0, e = 0, rank = 0;
+    uint64_t nsrc, ndst, old, capn = 0;
+    if (type == kWindow) {
+      w0 = gw0[gid];
+      const uint32_t w1 = gw1[gid];
+      nsrc = w1 - w0;
+      old = warp_sum_lcnt(g.lcnt, (base >> kLeafLog) + w0, (base >> kLeafLog) + w1);
+      if (insert) {  // the group's first item lies between the two bounds
+        b = warp_lb_u64(p_ul, 0, j0 + 1, kk | w0);
+        e = warp_lb_u64(p_ul, j0, nitems, kk | w1);
+      }
+      ndst = nsrc;
+    } else {
+      w0 = 0;
+      nsrc = cap == 0 ? 0 : nleaves_of(cap);
+      old = g.deg[u];
+      if (insert) {
+        b = warp_lb_u64(p_ul, 0, j0 + 1, kk);
+        e = warp_lb_u64(p_ul, j0, nitems, kk + (1ull << 32));
+      }
+      capn = cap_for(old + (e - b), inv_fill);
+      ndst = capn == 0 ? 0 : nleaves_of((uint32_t)capn);
+      if (lane == 0 && capn > 0) rank = atomicAdd(&class_cnt[log2_floor(capn)], 1u);
+    }
+    if (lane == 0) task_store(t, tid, u, w0, nsrc, ndst, b, e, old, capn, rank, type);
+    __syncwarp();
   }
 }
 
@@ -707,7 +798,7 @@ __global__ void k_task_setup(DGraph g, uint64_t inv_fill, bool insert,
 // groups at once), then the groups go kGroupsPerWarp at a time with their
 // items and leaf lines loaded together, one dependent load per batch.
 __global__ void __launch_bounds__(256, 4)
-k_leaf_merge(DGraph g, const uint32_t *__restrict__ p_x,
+k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul, const uint32_t *__restrict__ p_x,
              const uint64_t *__restrict__ p_S, const uint32_t *__restrict__ p_c,
              const uint64_t *__restrict__ merge_jk, const uint32_t *__restrict__ d_nmerge,
              const uint32_t *__restrict__ p_w) {
@@ -724,6 +815,7 @@ k_leaf_merge(DGraph g, const uint32_t *__restrict__ p_x,
     const uint32_t j0l = (uint32_t)(jkl >> 32), kl = (uint32_t)jkl;
     const uint64_t Sl = okl ? p_S[j0l] : 0;
     const uint32_t cwl = okl ? p_c[j0l] : 0;
+    const uint32_t ul = okl ? (uint32_t)(p_ul[j0l] >> 32) : 0u;
     const uint32_t cnt = nmerge - w * 32 < 32 ? (uint32_t)(nmerge - w * 32) : 32u;
     for (uint32_t q0 = 0; q0 < cnt; q0 += Q) {
       uint32_t j0[Q], k[Q], x[Q], linev[Q], cw[Q];
@@ -759,16 +851,24 @@ k_leaf_merge(DGraph g, const uint32_t *__restrict__ p_x,
           if ((uint32_t)lane == j) px = j + below;
         }
         // values move with their ids (weighted graphs)
-        const uint32_t av = (g.vals && (uint32_t)lane < c) ? g.vals[S[q] + lane] : 0u;
-        const uint32_t xv = (g.vals && (uint32_t)lane < k[q]) ? (p_w ? p_w[j0[q] + lane] : 1u) : 0u;
-        __syncwarp();
+        if (g.vals) {
+          const uint32_t av = (uint32_t)lane < c ? g.vals[S[q] + lane] : 0u;
+          const uint32_t xv = (uint32_t)lane < k[q] ? (p_w ? p_w[j0[q] + lane] : 1u) : 0u;
+          __syncwarp();  // every value read before any is moved
+          if ((uint32_t)lane < c) g.vals[S[q] + pa] = av;
+          if ((uint32_t)lane < k[q]) g.vals[S[q] + px] = xv;
+        }
+        // the ids come from registers: no lane reads the line again
         if ((uint32_t)lane < c) g.slots[S[q] + pa] = a;
         if ((uint32_t)lane < k[q]) g.slots[S[q] + px] = x[q];
-        if (g.vals && (uint32_t)lane < c) g.vals[S[q] + pa] = av;
-        if (g.vals && (uint32_t)lane < k[q]) g.vals[S[q] + px] = xv;
-        if (lane == 0 && (cw[q] & kMultiLeaf)) g.lcnt[S[q] >> kLeafLog] = (uint8_t)(c + k[q]);
-        __syncwarp();
       }
+    }
+    // the chunk's leaf counts and degrees, lane l for group l.  No task
+    // reads these rows' degrees: a one-leaf row is one group (a merge or a
+    // resize), and a row with a resize task has no merge group.
+    if (okl) {
+      if (cwl & kMultiLeaf) g.lcnt[Sl >> kLeafLog] = (uint8_t)((cwl & 0xff) + kl);
+      atomicAdd(&g.deg[ul], kl);
     }
   }
 }
@@ -924,25 +1024,21 @@ __global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
   if (lane == 0 && multi) g.lcnt[S >> kLeafLog] = (uint8_t)cnt;
 }
 
+// resized rows get their new segment; every task's row gets the new items
+// the task took (an insert's items are each taken by one merge group or one
+// task, and the merge kernel counts its own)
 __global__ void k_finalize(DGraph g, Tasks t, uint32_t ntasks,
                            const uint64_t *__restrict__ class_start) {
   pdl_wait();
   uint64_t tau = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (tau >= ntasks || t.type[tau] != kResize) return;
+  if (tau >= ntasks) return;
   uint32_t u = t.u[tau];
+  const uint32_t added = t.newend[tau] - t.newbeg[tau];
+  if (added) atomicAdd(&g.deg[u], added);
+  if (t.type[tau] != kResize) return;
   uint64_t capn = t.capn[tau];
   g.base[u] = capn ? task_new_base(t, tau, class_start) : 0;
   g.cap[u] = (uint32_t)capn;
-}
-
-__global__ void k_deg_add(DGraph g, const uint64_t *__restrict__ p_ul,
-                          const uint32_t *__restrict__ g_start,
-                          const uint32_t *__restrict__ d_ngroups, uint64_t gmax) {
-  pdl_wait();
-  uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= gmax || gid >= *d_ngroups) return;
-  uint32_t u = (uint32_t)(p_ul[g_start[gid]] >> 32);
-  atomicAdd(&g.deg[u], g_start[gid + 1] - g_start[gid]);
 }
 
 // ---------------------------------------------------------------- repack
@@ -1511,13 +1607,14 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   // (on the device), so they run on a second stream from there, beside the
   // task planning, the plan readback and the window / resize tasks.  They
   // touch disjoint leaves: a group inside a task's window (or a resized row)
-  // is that task's, not a merge.  Every later step that could meet them -- a
-  // repack of the slab, the degree update, the end of the batch -- waits.
+  // is that task's, not a merge, and the merges add their rows' degrees
+  // themselves (no task reads those).  Every later step that could meet
+  // them -- a repack of the slab, the end of the batch -- waits.
   auto fork_merges = [&](cudaStream_t from) -> sst_status {
     SST_CUDA_TRY(cudaEventRecord(g->fork_ev, from));
     SST_CUDA_TRY(cudaStreamWaitEvent(g->side, g->fork_ev, 0));
     SST_LAUNCH_PDL(k_leaf_merge, std::min(warp_blocks((b + 31) / 32), (unsigned)g->sms * 8),
-               kTB, 0, g->side, dg, p_x, p_S, p_c, merge_jk, &P->n_merge, p_w);
+               kTB, 0, g->side, dg, p_ul, p_x, p_S, p_c, merge_jk, &P->n_merge, p_w);
     SST_CUDA_TRY(cudaEventRecord(g->merge_done, g->side));
     join.ev = g->merge_done;
     return SST_OK;
@@ -1587,7 +1684,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     const unsigned tgrid = std::min(blocks_for(b), cap_blocks);
     const unsigned wgrid = std::min(warp_blocks(b), cap_blocks);
     if (insert) {
-      SST_LAUNCH_PDL(k_classify_insert, tgrid, kTB, 0, s, dg, p_ul, g_start,
+      SST_LAUNCH_PDL(k_classify_insert, tgrid, kTB, 0, s, p_ul, p_c, g_start,
                  &P->n_groups, gtype, glev, gw0, gw1, climb, &P->n_climb);
     } else {
       // multi-leaf segments have H >= 1 (at least two leaves)
@@ -1625,9 +1722,13 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
       if (st != SST_OK) return st;
     }
     // 8: plan
-    SST_LAUNCH_PDL(k_task_setup, wgrid, kTB, 0, s, dg, fill_inv_q24(g->params.grow_fill), insert,
-               p_ul, g_start, gtype, gw0, gw1, task_group, &P->n_tasks, &P->n_items, b, T,
-               P->class_cnt);
+    SST_LAUNCH_PDL(k_task_setup, tgrid, kTB, 0, s, dg, fill_inv_q24(g->params.grow_fill),
+               insert, p_ul, g_start, gtype, task_group, &P->n_tasks, T, P->class_cnt,
+               climb, &P->n_hard);
+    // the climb list is free again: it holds the second pass's tasks
+    SST_LAUNCH_PDL(k_task_setup_hard, wgrid, kTB, 0, s, dg, fill_inv_q24(g->params.grow_fill),
+               insert, p_ul, g_start, gtype, gw0, gw1, task_group, climb, &P->n_hard,
+               &P->n_items, T, P->class_cnt);
     // three independent scans, two of them beside the stream
     SST_CUDA_TRY(fork_aux(s, 2));
     SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.total, T.out, b, 0ull, OpAdd{}, true,
@@ -1748,9 +1849,6 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                cstart);
   }
   join.wait();
-  if (insert)
-    SST_LAUNCH_PDL(k_deg_add, blocks_for(b), kTB, 0, s, dg, p_ul, g_start,
-               &P->n_groups, b);
   // the staging-rank check of this batch is read back with the next plan
   // (or by sst_sync), so a batch ends without a second host synchronisation
   SST_CUDA_TRY(cudaGetLastError());

@@ -26,6 +26,7 @@ struct PlanSummary {
   uint32_t class_cnt[kNumClasses];  // new segments per capacity class
   unsigned long long apply_err;     // staged ranks out of range (must be 0)
   uint32_t n_keys;                  // keys kept by a compacting key build
+  uint32_t n_hard;                  // tasks set up a warp each (k_task_setup_hard)
 };
 
 // Flattened list of all leaves in vertex order: the iteration space of the

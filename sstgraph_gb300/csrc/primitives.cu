@@ -178,7 +178,9 @@ constexpr int kSmallItems = 4;
 constexpr uint64_t kSmallTileKeys = 256ull * kThreads * kSmallItems;  // 2^18
 // (1024-key tiles for larger one-sweep sorts were measured too: at 1e6 keys
 // 977 tiles made a pass 29 us against 19 us for 245 tiles of 4096 -- the
-// longer look-back walks cost more than the extra resident warps gain)
+// longer look-back walks cost more than the extra resident warps gain; and
+// 2048-key tiles, three blocks an SM, made a 1e6-pair insert 567 us against
+// 553 us)
 constexpr int kRadix = 256;
 constexpr uint32_t kNoDigit = 0xffffffffu;  // an item past the end
 // Sorts of at most this many tiles run one launch per pass: every block
