@@ -616,22 +616,6 @@ __global__ void k_dom_classify(const uint64_t *__restrict__ p_ul,
   mt[gid] = ((uint64_t)tf << 32) | mf;
 }
 
-__global__ void k_emit(const uint64_t *__restrict__ mt,
-                       const uint64_t *__restrict__ mtpos, uint64_t gmax,
-                       const uint32_t *__restrict__ g_start,
-                       uint64_t *__restrict__ merge_jk,
-                       uint32_t *__restrict__ task_group) {
-  pdl_wait();
-  uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= gmax) return;
-  const uint64_t f = mt[gid], p = mtpos[gid];
-  const uint32_t mpos = (uint32_t)p, tpos = (uint32_t)(p >> 32);
-  if ((uint32_t)f && mpos < gmax) {
-    const uint32_t j0 = g_start[gid];
-    merge_jk[mpos] = ((uint64_t)j0 << 32) | (g_start[gid + 1] - j0);
-  }
-  if ((f >> 32) && tpos < gmax) task_group[tpos] = (uint32_t)gid;
-}
 
 // ---------------------------------------------------------------- step 8
 struct Tasks {
@@ -654,13 +638,7 @@ struct Tasks {
   const uint32_t *p_w;      // weighted graphs: values of the packed items
 };
 
-// Task setup in two passes.  The first takes the task slots a lane each: a
-// resize of a one-leaf row -- the common task -- is set up right there (the
-// row has one group, so its new items are that group's: no search; the
-// lanes' capacity-class ranks come from one atomic per class and warp);
-// every other task (windows, resizes of multi-leaf rows) goes to a list
-// that the second pass works through a warp per task (a window's leaf
-// counts and the row's item range by warp searches).
+// A task's record (the setup kernels below write it).
 __device__ __forceinline__ void task_store(Tasks &t, uint64_t tid, uint32_t u, uint32_t w0,
                                            uint64_t nsrc, uint64_t ndst, uint32_t nb,
                                            uint32_t ne, uint64_t old, uint64_t capn,
@@ -678,63 +656,79 @@ __device__ __forceinline__ void task_store(Tasks &t, uint64_t tid, uint32_t u, u
   t.type[tid] = type;
 }
 
-__global__ void k_task_setup(DGraph g, uint64_t inv_fill, bool insert,
-                             const uint64_t *__restrict__ p_ul,
-                             const uint32_t *__restrict__ g_start,
-                             const uint8_t *__restrict__ gtype,
-                             const uint32_t *__restrict__ task_group,
-                             const uint32_t *__restrict__ d_ntasks, Tasks t,
-                             uint32_t *__restrict__ class_cnt,
-                             uint32_t *__restrict__ hard, uint32_t *__restrict__ nhard) {
+// Each group's outputs from the merge/task scan: a merge group's item range
+// (and, on an insert, "no task" for its items in itask), a task group's
+// slot.  The lane of a task group then sets the task up when it is a
+// resize of a one-leaf row -- the common task: the row has one group, so
+// its new items are that group's (no search), and the lanes'
+// capacity-class ranks come from one atomic per class and warp -- and
+// lists every other task (windows, resizes of multi-leaf rows) for
+// k_task_setup_hard, which takes them a warp each (a window's leaf counts
+// and the row's item range by warp searches).
+__global__ void k_emit(const uint64_t *__restrict__ mt,
+                       const uint64_t *__restrict__ mtpos, uint64_t gmax,
+                       const uint32_t *__restrict__ g_start,
+                       uint64_t *__restrict__ merge_jk,
+                       uint32_t *__restrict__ task_group, DGraph g, uint64_t inv_fill,
+                       bool insert, const uint64_t *__restrict__ p_ul,
+                       const uint8_t *__restrict__ gtype, Tasks t,
+                       uint32_t *__restrict__ class_cnt, uint32_t *__restrict__ hard,
+                       uint32_t *__restrict__ nhard, uint32_t *__restrict__ itask) {
   pdl_wait();
+  const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const uint32_t full = 0xffffffffu;
-  const uint32_t ntasks = *d_ntasks;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-       w * 32 < ntasks; w += nwarps) {
-    const uint64_t tid = w * 32 + lane;
-    const bool ok = tid < ntasks;
-    const uint32_t gid = ok ? task_group[tid] : 0u;
-    const uint32_t j0 = ok ? g_start[gid] : 0u;
-    const uint32_t j1 = ok ? g_start[gid + 1] : 0u;
-    const uint32_t u = ok ? (uint32_t)(p_ul[j0] >> 32) : 0u;
-    const uint8_t type = ok ? gtype[gid] : (uint8_t)kNone;
-    const uint32_t cap = ok ? g.cap[u] : 0u;
-    // a resize of a one-leaf (or empty) row, set up by this lane
-    const bool simple = ok && type != kWindow && cap <= kLeaf;
-    uint32_t cls = kEmpty;  // capacity class taking a rank, else none
-    uint64_t capn = 0;
-    uint32_t nb = 0, ne = 0, deg = 0;
+  const bool in = gid < gmax;  // no early return: the warp votes below
+  const uint64_t f = in ? mt[gid] : 0, p = in ? mtpos[gid] : 0;
+  const uint32_t mpos = (uint32_t)p, tpos = (uint32_t)(p >> 32);
+  if ((uint32_t)f && mpos < gmax) {
+    const uint32_t j0 = g_start[gid], j1 = g_start[gid + 1];
+    merge_jk[mpos] = ((uint64_t)j0 << 32) | (j1 - j0);
+    if (itask)
+      for (uint32_t j = j0; j < j1; j++) itask[j] = kEmpty;
+  }
+  const bool task = (f >> 32) && tpos < gmax;
+  bool simple = false;
+  uint32_t cls = kEmpty;  // capacity class taking a rank, else none
+  uint32_t u = 0, cap = 0, deg = 0, nb = 0, ne = 0;
+  uint64_t capn = 0;
+  uint8_t type = kNone;
+  if (task) {
+    task_group[tpos] = (uint32_t)gid;
+    const uint32_t j0 = g_start[gid];
+    type = gtype[gid];
+    u = (uint32_t)(p_ul[j0] >> 32);
+    cap = g.cap[u];
+    simple = type != kWindow && cap <= kLeaf;  // a resize of a one-leaf (or empty) row
     if (simple) {
       deg = g.deg[u];
       if (insert) {
         nb = j0;
-        ne = j1;
+        ne = g_start[gid + 1];
       }
       capn = cap_for((uint64_t)deg + (ne - nb), inv_fill);
       if (capn > 0) cls = log2_floor(capn);
     }
-    // one rank reservation per class among the warp's simple lanes
-    const uint32_t peers = __match_any_sync(full, cls);
-    const int leader = __ffs(peers) - 1;
-    uint32_t rbase = 0;
-    if (cls != kEmpty && lane == leader) rbase = atomicAdd(&class_cnt[cls], (uint32_t)__popc(peers));
-    rbase = __shfl_sync(full, rbase, leader);
-    if (simple) {
-      const uint32_t rank = cls != kEmpty ? rbase + __popc(peers & ((1u << lane) - 1u)) : 0u;
-      const uint64_t ndst = capn == 0 ? 0 : nleaves_of((uint32_t)capn);
-      task_store(t, tid, u, 0, cap == 0 ? 0 : nleaves_of(cap), ndst, nb, ne, deg, capn,
-                 rank, type);
-    }
-    // the rest to the second pass, one reservation for the warp
-    const uint32_t hm = __ballot_sync(full, ok && !simple);
-    if (hm) {
-      uint32_t at = 0;
-      if (lane == __ffs(hm) - 1) at = atomicAdd(nhard, (uint32_t)__popc(hm));
-      at = __shfl_sync(full, at, __ffs(hm) - 1);
-      if (ok && !simple) hard[at + __popc(hm & ((1u << lane) - 1u))] = (uint32_t)tid;
-    }
+  }
+  // one rank reservation per class among the warp's simple lanes
+  const uint32_t peers = __match_any_sync(full, cls);
+  const int leader = __ffs(peers) - 1;
+  uint32_t rbase = 0;
+  if (cls != kEmpty && lane == leader) rbase = atomicAdd(&class_cnt[cls], (uint32_t)__popc(peers));
+  rbase = __shfl_sync(full, rbase, leader);
+  if (simple) {
+    const uint32_t rank = cls != kEmpty ? rbase + __popc(peers & ((1u << lane) - 1u)) : 0u;
+    const uint64_t ndst = capn == 0 ? 0 : nleaves_of((uint32_t)capn);
+    task_store(t, tpos, u, 0, cap == 0 ? 0 : nleaves_of(cap), ndst, nb, ne, deg, capn, rank,
+               type);
+  }
+  // the rest to k_task_setup_hard, one reservation for the warp
+  const uint32_t hm = __ballot_sync(full, task && !simple);
+  if (hm) {
+    uint32_t at = 0;
+    if (lane == __ffs(hm) - 1) at = atomicAdd(nhard, (uint32_t)__popc(hm));
+    at = __shfl_sync(full, at, __ffs(hm) - 1);
+    if (task && !simple) hard[at + __popc(hm & ((1u << lane) - 1u))] = tpos;
   }
 }
 
@@ -875,33 +869,31 @@ k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul, const uint32_t *__rest
 
 // the task of every source and destination leaf of the window / resize
 // tasks (a warp per task fills its two ranges), so the apply kernels find a
-// leaf's task with one load, not a binary search over the offsets
-// (and, on an insert, the task of each new item that a task takes; itask is
-// all ones beforehand)
-__global__ void k_task_index(Tasks t, uint32_t ntasks, uint32_t *__restrict__ stask,
-                             uint32_t *__restrict__ dtask, uint32_t *__restrict__ itask) {
+// leaf's task with one load, not a binary search over the offsets; the
+// source leaves' element counts beside (scnt); and, on an insert, the task
+// of each new item that a task takes (k_emit marked the merged items)
+__global__ void k_task_index(DGraph g, Tasks t, uint32_t ntasks, uint32_t *__restrict__ stask,
+                             uint32_t *__restrict__ dtask, uint32_t *__restrict__ itask,
+                             uint64_t *__restrict__ scnt) {
   pdl_wait();
   const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (w >= ntasks) return;
   const uint64_t s0 = t.soff[w], ns = t.nsrc[w], d0 = t.doff[w], nd = t.ndst[w];
-  for (uint64_t j = lane; j < ns; j += 32) stask[s0 + j] = (uint32_t)w;
+  if (ns) {
+    const uint32_t u = t.u[w], l0 = t.w0[w];
+    const uint64_t base = g.base[u];
+    const uint32_t cap = g.cap[u], deg = g.deg[u];
+    for (uint64_t j = lane; j < ns; j += 32) {
+      stask[s0 + j] = (uint32_t)w;
+      scnt[s0 + j] = leaf_count(g, base, cap, deg, l0 + (uint32_t)j);
+    }
+  }
   for (uint64_t j = lane; j < nd; j += 32) dtask[d0 + j] = (uint32_t)w;
   if (itask)
     for (uint32_t j = t.newbeg[w] + lane; j < t.newend[w]; j += 32) itask[j] = (uint32_t)w;
 }
 
-__global__ void k_src_counts(DGraph g, Tasks t, uint32_t ntasks,
-                             uint64_t nsrc_total, uint64_t *__restrict__ scnt,
-                             const uint32_t *__restrict__ stask) {
-  pdl_wait();
-  uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsrc_total) return;
-  uint64_t tau = stask[s];
-  uint32_t u = t.u[tau];
-  uint32_t l = t.w0[tau] + (uint32_t)(s - t.soff[tau]);
-  scnt[s] = leaf_count(g, g.base[u], g.cap[u], g.deg[u], l);
-}
 
 // warp per source leaf: old elements to their merged rank
 __global__ void k_gather_old(DGraph g, Tasks t, uint32_t ntasks,
@@ -943,7 +935,7 @@ __global__ void k_gather_new(DGraph g, Tasks t, uint32_t ntasks,
   uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nitems || ntasks == 0) return;
   const uint32_t tau = itask[j];
-  if (tau == kEmpty) return;  // a leaf merge takes this item
+  if (tau >= ntasks) return;  // a leaf merge takes this item (kEmpty)
   const uint32_t u = (uint32_t)(p_ul[j] >> 32);
   uint32_t x = p_x[j];
   uint64_t base = g.base[u];
@@ -1483,7 +1475,7 @@ static sst_status plan_graph_launch(sst_graph *g, uint64_t b, bool insert,
 
 // bytes of arena scratch an update batch of b pairs takes
 static size_t update_scratch_bytes(uint64_t b) {
-  size_t per = 8 * 2 + 4 * 4 + 8 + 4 + 4 * 3 + 1 * 2 + 4 * 2 + 8 * 4 + 4 * 6 +
+  size_t per = 8 * 2 + 4 * 5 + 8 + 4 + 4 * 3 + 1 * 2 + 4 * 2 + 8 * 4 + 4 * 6 +
                8 * 8 + 4 * 4 + 1 + 64 + 4 * 3 /* values */ +
                8 + 4 + 8 + 4 + 4 /* leaf starts and counts, merge ranges */;
   return b * per + radix_sort_scratch_bytes(b) + 8 * scan_scratch_bytes(b, 8) +
@@ -1555,6 +1547,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   uint64_t *lS = A.take<uint64_t>(b), *p_S = A.take<uint64_t>(b);
   uint32_t *lc = A.take<uint32_t>(b), *p_c = A.take<uint32_t>(b);
   uint32_t *climb = A.take<uint32_t>(b);
+  uint32_t *itask = A.take<uint32_t>(b);  // inserts: each item's task, or none
   Tasks T;
   T.u = A.take<uint32_t>(b);
   T.w0 = A.take<uint32_t>(b);
@@ -1715,17 +1708,15 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                   "n_merge and n_tasks share one aligned 64-bit word");
     SST_CUDA_TRY((scan<uint64_t, OpAdd>(mt, mtpos, b, 0ull, OpAdd{}, true, false,
                                         reinterpret_cast<uint64_t *>(&P->n_merge), A, s)));
+    // 8: plan.  The climb list is free again: it holds the tasks that
+    // k_task_setup_hard sets up
     SST_LAUNCH_PDL(k_emit, blocks_for(b), kTB, 0, s, mt, mtpos, b, g_start, merge_jk,
-               task_group);
+               task_group, dg, fill_inv_q24(g->params.grow_fill), insert, p_ul, gtype, T,
+               P->class_cnt, climb, &P->n_hard, insert ? itask : nullptr);
     if (fork && insert) {
       sst_status st = fork_merges(s);
       if (st != SST_OK) return st;
     }
-    // 8: plan
-    SST_LAUNCH_PDL(k_task_setup, tgrid, kTB, 0, s, dg, fill_inv_q24(g->params.grow_fill),
-               insert, p_ul, g_start, gtype, task_group, &P->n_tasks, T, P->class_cnt,
-               climb, &P->n_hard);
-    // the climb list is free again: it holds the second pass's tasks
     SST_LAUNCH_PDL(k_task_setup_hard, wgrid, kTB, 0, s, dg, fill_inv_q24(g->params.grow_fill),
                insert, p_ul, g_start, gtype, gw0, gw1, task_group, climb, &P->n_hard,
                &P->n_items, T, P->class_cnt);
@@ -1807,8 +1798,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
 
   // staging for window / resize tasks
   size_t wneed = ps.task_elems * (g->weighted ? 8 : 4) + ps.src_leaves * 20 +
-                 ps.dst_leaves * 4 + (uint64_t)ps.n_items * 4 +
-                 scan_scratch_bytes(ps.src_leaves, 8) + 4096;
+                 ps.dst_leaves * 4 + scan_scratch_bytes(ps.src_leaves, 8) + 4096;
   if (wneed > g->work.cap) {
     sst_status st = budget_check(g, wneed - g->work.cap);
     if (st != SST_OK) return st;
@@ -1821,18 +1811,13 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   uint64_t *spre = g->work.take<uint64_t>(ps.src_leaves);
   uint32_t *stask = g->work.take<uint32_t>(ps.src_leaves);
   uint32_t *dtask = g->work.take<uint32_t>(ps.dst_leaves);
-  uint32_t *itask = insert && ps.n_tasks && ps.n_items ? g->work.take<uint32_t>(ps.n_items)
-                                                       : nullptr;
+  uint32_t *const titem = insert && ps.n_tasks && ps.n_items ? itask : nullptr;
 
   // 9b: apply the window / resize tasks
   if (ps.n_tasks) {
-    if (itask)
-      SST_CUDA_TRY(cudaMemsetAsync(itask, 0xFF, (uint64_t)ps.n_items * 4, s));
-    SST_LAUNCH_PDL(k_task_index, warp_blocks(ps.n_tasks), kTB, 0, s, T, ps.n_tasks, stask,
-               dtask, itask);
+    SST_LAUNCH_PDL(k_task_index, warp_blocks(ps.n_tasks), kTB, 0, s, dg, T, ps.n_tasks,
+               stask, dtask, titem, scnt);
     if (ps.src_leaves) {
-      SST_LAUNCH_PDL(k_src_counts, blocks_for(ps.src_leaves), kTB, 0, s, dg, T,
-                 ps.n_tasks, ps.src_leaves, scnt, stask);
       SST_CUDA_TRY((scan<uint64_t, OpAdd>(scnt, spre, ps.src_leaves, 0ull,
                                           OpAdd{}, true, false, nullptr,
                                           g->work, s)));
@@ -1841,7 +1826,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     }
     if (insert && ps.n_items)
       SST_LAUNCH_PDL(k_gather_new, blocks_for(ps.n_items), kTB, 0, s, dg, T,
-                 ps.n_tasks, spre, p_ul, p_x, ps.n_items, stage, itask);
+                 ps.n_tasks, spre, p_ul, p_x, ps.n_items, stage, titem);
     if (ps.dst_leaves)
       SST_LAUNCH_PDL(k_task_scatter, warp_blocks(ps.dst_leaves), kTB, 0, s, dg, T,
                  ps.n_tasks, ps.dst_leaves, cstart, stage, dtask);
