@@ -658,6 +658,39 @@ k_sort_small(uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
 
 constexpr int kSmallSortKV = 1024;
 
+// Keys alone (no payload: equal keys are indistinguishable, so the order
+// need not be stable) of at most kSmallSort: a bitonic sort in one CTA of
+// kBitonicThreads, each thread taking the compare-exchanges of its pairs
+// at every stage (55 stages for 1024 keys, 66 for 2048), against the six
+// rank-and-scatter passes of the radix form.
+constexpr int kBitonicThreads = 1024;
+static_assert(kSmallSort <= 2 * kBitonicThreads, "one pair per thread and stage");
+__global__ void __launch_bounds__(kBitonicThreads)
+k_sort_bitonic(uint64_t *__restrict__ keys, uint64_t n, const uint32_t *__restrict__ d_n) {
+  pdl_wait();
+  __shared__ uint64_t sk[kSmallSort];
+  if (d_n && *d_n < n) n = *d_n;
+  uint32_t N = 2;
+  while (N < n) N <<= 1;
+  const uint32_t t = threadIdx.x;
+  for (uint32_t i = t; i < N; i += kBitonicThreads) sk[i] = i < n ? keys[i] : ~0ull;
+  __syncthreads();
+  for (uint32_t k = 2; k <= N; k <<= 1)
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      // thread t takes the pair (i, i ^ j) whose lower index i is its t-th
+      const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+      if (i + j < N) {
+        const uint64_t a = sk[i], b = sk[i + j];
+        if ((a > b) == ((i & k) == 0)) {
+          sk[i] = b;
+          sk[i + j] = a;
+        }
+      }
+      __syncthreads();
+    }
+  for (uint32_t i = t; i < n; i += kBitonicThreads) keys[i] = sk[i];
+}
+
 }  // namespace
 
 size_t radix_sort_scratch_bytes(uint64_t n) {
@@ -798,8 +831,7 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
   if (vresult) *vresult = vals;
   if (n < 2 || bits <= 0) return cudaSuccess;
   if (!vals && n <= (uint64_t)kSmallSort) {
-    SST_LAUNCH_PDL_B(16 * n, (k_sort_small<false, kSmallSort>), 1, kThreads, 0, s, keys,
-               (uint32_t *)nullptr, n, bits, d_n);
+    SST_LAUNCH_PDL_B(16 * n, k_sort_bitonic, 1, kBitonicThreads, 0, s, keys, n, d_n);
     return cudaGetLastError();
   }
   if (vals && n <= (uint64_t)kSmallSortKV) {
