@@ -22,6 +22,7 @@ from __future__ import annotations
 import argparse
 import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -34,6 +35,18 @@ sys.path.insert(0, ROOT)
 
 SIZES = [1000, 10000, 100000, 1000000]
 RMAT = dict(a=0.57, b=0.19, c=0.19)
+
+
+def strict(x):
+    """The value with every non-finite float replaced by None (the printed
+    lines are strict JSON)."""
+    if isinstance(x, float) and not math.isfinite(x):
+        return None
+    if isinstance(x, dict):
+        return {k: strict(v) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [strict(v) for v in x]
+    return x
 
 
 def peaks():
@@ -279,7 +292,7 @@ def reference_arm(a):
         "note": "reference storage code cannot be built on the GPU host (its "
                 "sources are not shipped there); the C restatement in oracle/ is timed",
     }
-    print(json.dumps(line))
+    print(json.dumps(strict(line), allow_nan=False))
 
 
 def workload_config(a):
@@ -539,9 +552,18 @@ def main():
         # after the update stream the graph is directed (inserts are not
         # symmetrised), where BC is not defined: the difference is reported,
         # not judged (BC parity is tested on symmetric graphs)
+        # (a directed graph can leave vertices with no shortest-path count
+        # under the symmetric formulation: their values are not finite, and
+        # are counted, not compared)
+        fin = torch.isfinite(b1) & torch.isfinite(b2)
+        nfin = int((~fin).sum().item())
+        diff = (b1 - b2)[fin].abs().max().item() if nfin < n else 0.0
+        scale = b2[fin].abs().max().item() if nfin < n else 0.0
         trav["bc"] = {"snapshot_ms": ms_s, "graph_ms": ms_l,
-                      "max_rel_diff_on_directed_graph":
-                          (b1 - b2).abs().max().item() / max(b2.abs().max().item(), 1e-300)}
+                      "max_rel_diff_on_directed_graph": diff / max(scale, 1e-300),
+                      "nonfinite_entries": nfin,
+                      "nonfinite_in_same_places":
+                          bool(torch.equal(torch.isfinite(b1), torch.isfinite(b2)))}
         ms_s, t_s = timed(lambda: c.tc())
         ms_l, t_l = timed(lambda: sg.TC(g))
         trav["tc"] = {"snapshot_ms": ms_s, "graph_ms": ms_l, "equal": t_s == t_l}
@@ -1039,7 +1061,7 @@ def main():
         else:
             res["bfs"] = measure_bfs()
         g.close()
-        print(json.dumps(res))
+        print(json.dumps(strict(res), allow_nan=False))
         return
 
     # ---- batches: inserts are 95% new RMAT edges and 5% sampled existing
@@ -1251,7 +1273,7 @@ def main():
         "serving": serving,
         "update_kernels": upd_kernels,
     }
-    print(json.dumps(line))
+    print(json.dumps(strict(line), allow_nan=False))
 
 
 # DRAM bytes (read + write) per launch from one ncu capture of one 1e6-pair

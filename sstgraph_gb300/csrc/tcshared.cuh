@@ -154,13 +154,42 @@ k_tc_count(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
       my_na = off[uu + 1] - my_a0;
     }
     const int ng = (int)((Q - q0) < (unsigned long long)kTcGrab ? (Q - q0) : kTcGrab);
+    // The item's v (stage 1) and its list bounds (stage 2) load ahead: v two
+    // items before the item's turn, the bounds one item before (they need
+    // v), so a small item's three dependent loads overlap earlier items.
+    auto load_v = [&](int g, bool &okv) -> uint32_t {
+      const uint64_t itg = __shfl_sync(full, my_it, g & 31);
+      const uint64_t a0g = __shfl_sync(full, my_a0, g & 31);
+      const uint64_t nag = __shfl_sync(full, my_na, g & 31);
+      const uint64_t e = (itg >> 32) * kTcBatch + lane;
+      okv = g < ng && e < nag;
+      return okv ? adj[a0g + e] : 0u;
+    };
+    bool ok_n1 = false, ok_n2 = false;
+    uint32_t v_n1 = load_v(0, ok_n1);  // item gi's v
+    uint32_t v_n2 = load_v(1, ok_n2);  // item gi + 1's v
+    uint64_t b_n1 = ok_n1 ? off[v_n1] : 0, e_n1 = ok_n1 ? off[v_n1 + 1] : 0;
     for (int gi = 0; gi < ng; gi++) {
       const uint64_t it = __shfl_sync(full, my_it, gi);
       const uint64_t a0 = __shfl_sync(full, my_a0, gi);
       const uint64_t na = __shfl_sync(full, my_na, gi);
       const uint32_t u = (uint32_t)it;
-      const uint64_t i0 = (it >> 32) * kTcBatch;
       const uint32_t *A = adj + a0;
+      // this lane's v and the bounds of N+(v), loaded ahead
+      const bool okv = ok_n1;
+      const uint32_t v = okv ? v_n1 : 0u;
+      const uint64_t b0 = okv ? b_n1 : 0;
+      const uint64_t l = okv ? e_n1 - b_n1 : 0;
+      const uint32_t len = l > 0xffffffffull ? 0xffffffffu : (uint32_t)l;
+      // the next items' loads go out before this item's work
+      bool ok_n3 = false;
+      const uint32_t v_n3 = load_v(gi + 2, ok_n3);
+      ok_n1 = ok_n2;
+      v_n1 = v_n2;
+      b_n1 = ok_n2 ? off[v_n2] : 0;
+      e_n1 = ok_n2 ? off[v_n2 + 1] : 0;
+      ok_n2 = ok_n3;
+      v_n2 = v_n3;
       const bool hashed = na <= kTcSlots / 2;
       int bits = 3;
       while (bits < kTcBucketBits && (1ull << bits) < 2 * na) bits++;
@@ -172,15 +201,6 @@ k_tc_count(const uint64_t *__restrict__ off, const uint32_t *__restrict__ adj,
         for (uint64_t i = lane; i < na; i += 32) tc_set_insert(tab, A[i], bits);
         __syncwarp();
         set_u = u;
-      }
-      // this lane's v and the bounds of N+(v)
-      uint32_t v = 0, len = 0;
-      uint64_t b0 = 0;
-      if (i0 + lane < na) {
-        v = A[i0 + lane];
-        b0 = off[v];
-        const uint64_t l = off[v + 1] - b0;
-        len = l > 0xffffffffull ? 0xffffffffu : (uint32_t)l;
       }
       // inclusive prefix of the lengths.  It fits 32 bits: every w in N+(v)
       // has degree >= deg(v) >= |N+(v)|, so |N+(v)|^2 <= m and 32 lists
