@@ -718,10 +718,19 @@ def main():
             off, cols = gg.csr()
             deg = np.diff(off.astype(np.int64))
             rows = np.repeat(np.arange(nn, dtype=np.int64), deg)
-            low = cols.astype(np.int64) < rows
-            dl = np.bincount(rows[low], minlength=nn).astype(np.int64)
-            tc_bytes = 4 * int((dl[rows[low]] + dl[cols[low].astype(np.int64)]).sum()) + 4 * m
-            del off, cols, rows, low
+            # TC reads: every stored id once (orientation), the oriented
+            # lists N+ written and read back into the per-u sets, and every
+            # entry of N+(v) for each oriented edge (u, v) probed once;
+            # the orientation keeps an edge at its lower (degree, id) rank
+            c64 = cols.astype(np.int64)
+            rank_r = deg[rows] * nn + rows
+            rank_c = deg[c64] * nn + c64
+            up = rank_c > rank_r
+            dplus = np.bincount(rows[up], minlength=nn).astype(np.int64)
+            m_plus = int(up.sum())
+            probes = int(dplus[c64[up]].sum())
+            tc_bytes = 4 * m + 8 * m_plus + 4 * probes
+            del off, cols, rows, c64, rank_r, rank_c, up, dplus
             dep = torch.empty(nn, dtype=torch.int32, device="cuda")
             pr = torch.empty(nn, dtype=torch.float64, device="cuda")
             lab = torch.empty(nn, dtype=torch.int32, device="cuda")

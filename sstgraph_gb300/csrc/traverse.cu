@@ -954,6 +954,9 @@ __global__ void k_bc_init(double *__restrict__ sigma, double *__restrict__ ratio
   dep[v] = 0.0;
 }
 
+// neighbours (or leaves) whose loads the BC kernels keep in flight together
+constexpr int kBcAhead = 8;
+
 // sigma(v) = sum of sigma over neighbours one level up (thread per vertex)
 __global__ void k_sigma_small(DGraph g, const uint32_t *__restrict__ list,
                               uint32_t cnt, const int32_t *__restrict__ depth,
@@ -965,9 +968,21 @@ __global__ void k_sigma_small(DGraph g, const uint32_t *__restrict__ list,
   const uint32_t *p = g.slots + g.base[v];
   uint32_t dg = g.deg[v];
   double s = 0.0;
-  for (uint32_t k = 0; k < dg; k++) {
-    uint32_t u = p[k];
-    if (depth[u] == d - 1) s += sigma[u];
+  // kBcAhead neighbours at a time, each load stage issued for all of them
+  // before any is used; the sum keeps neighbour order
+  for (uint32_t k0 = 0; k0 < dg; k0 += kBcAhead) {
+    uint32_t u[kBcAhead];
+    bool on[kBcAhead];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) u[q] = k0 + q < dg ? p[k0 + q] : 0u;
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) on[q] = k0 + q < dg && depth[u[q]] == d - 1;
+    double x[kBcAhead];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) x[q] = on[q] ? sigma[u[q]] : 0.0;
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++)
+      if (on[q]) s += x[q];
   }
   sigma[v] = s;
 }
@@ -1019,11 +1034,24 @@ __global__ void k_bc_chunks(DGraph g, const uint32_t *__restrict__ iv,
   uint64_t base = g.base[v];
   const uint8_t *lc = g.lcnt + (base >> kLeafLog);
   double acc = 0.0;
-  for (uint32_t l = l0; l < l1; l++) {
-    if ((uint32_t)lane < lc[l]) {
-      uint32_t u = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
-      if (depth[u] == want) acc += val[u];
-    }
+  // kBcAhead leaves at a time, each load stage issued for all of them before
+  // any is used; the sum keeps leaf order
+  for (uint32_t l = l0; l < l1; l += kBcAhead) {
+    uint32_t u[kBcAhead];
+    bool on[kBcAhead];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) on[q] = l + q < l1 && (uint32_t)lane < lc[l + q];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++)
+      u[q] = on[q] ? g.slots[base + ((uint64_t)(l + q) << kLeafLog) + lane] : 0u;
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) on[q] = on[q] && depth[u[q]] == want;
+    double x[kBcAhead];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) x[q] = on[q] ? val[u[q]] : 0.0;
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++)
+      if (on[q]) acc += x[q];
   }
   double s = warp_sum_d(acc);
   if (lane == 0) partial[i] = s;
@@ -1066,9 +1094,19 @@ __global__ void k_delta_small(DGraph g, const uint32_t *__restrict__ list,
   const uint32_t *p = g.slots + g.base[v];
   uint32_t dg = g.deg[v];
   double s = 0.0;
-  for (uint32_t k = 0; k < dg; k++) {
-    uint32_t w = p[k];
-    if (depth[w] == d + 1) s += ratio[w];
+  for (uint32_t k0 = 0; k0 < dg; k0 += kBcAhead) {  // as in k_sigma_small
+    uint32_t w[kBcAhead];
+    bool on[kBcAhead];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) w[q] = k0 + q < dg ? p[k0 + q] : 0u;
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) on[q] = k0 + q < dg && depth[w[q]] == d + 1;
+    double x[kBcAhead];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) x[q] = on[q] ? ratio[w[q]] : 0.0;
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++)
+      if (on[q]) s += x[q];
   }
   double dv = sigma[v] * s;
   dep[v] = dv;
