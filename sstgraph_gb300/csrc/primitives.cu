@@ -662,7 +662,10 @@ constexpr int kSmallSortKV = 1024;
 // need not be stable) of at most kSmallSort: a bitonic sort in one CTA of
 // kBitonicThreads, each thread taking the compare-exchanges of its pairs
 // at every stage (55 stages for 1024 keys, 66 for 2048), against the six
-// rank-and-scatter passes of the radix form.
+// rank-and-scatter passes of the radix form.  (Holding two keys a thread in
+// registers, with warp shuffles for the stages within a warp and the
+// shared array only for the rest, measured slower: 15.7 against 13.0 us
+// at 1e3 keys.)
 constexpr int kBitonicThreads = 1024;
 static_assert(kSmallSort <= 2 * kBitonicThreads, "one pair per thread and stage");
 __global__ void __launch_bounds__(kBitonicThreads)
