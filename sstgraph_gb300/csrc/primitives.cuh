@@ -204,7 +204,8 @@ constexpr uint64_t kScanOneBlockTiles = 8;
 // single-pass (look-back) scans up to this many tiles (4M elements)
 constexpr uint64_t kScanLookbackTiles = 1024;
 
-// A tile's results leave through shared memory: each thread holds items
+// A tile's results leave through shared memory (its inputs arrive the same
+// way, load_tile below): each thread holds items
 // t*kScanItems .. +kScanItems-1 of the tile, which it writes to a padded
 // buffer (stride kScanItems+1, no bank conflicts for 4-byte elements), and
 // the block then stores the tile striped, so each store instruction writes
@@ -219,10 +220,43 @@ struct StoreOut {
   __device__ __forceinline__ void operator()(uint64_t i, T r) const { out[i] = r; }
 };
 
+// tile t of the scan order: element i of the array (forward or reversed)
+template <typename T>
+__device__ __forceinline__ T scan_load(const T *in, uint64_t i, uint64_t n,
+                                       bool reverse, T identity) {
+  return i < n ? in[reverse ? n - 1 - i : i] : identity;
+}
+
+// The tile's padded staging buffer (shared by its load and its store).
+template <typename T>
+__device__ __forceinline__ T *tile_sbuf() {
+  __shared__ T sbuf[kScanThreads * (kScanItems + 1)];
+  return sbuf;
+}
+
+// A tile's inputs arrive the same way in reverse: the block loads the tile
+// striped (each load instruction reads whole sectors), into the padded
+// buffer, and each thread then takes its kScanItems consecutive items.
+template <typename T>
+__device__ __forceinline__ void load_tile(const T *in, uint64_t base, uint64_t n,
+                                          bool reverse, T identity, T *vals) {
+  T *sbuf = tile_sbuf<T>();
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    const uint32_t e = (uint32_t)k * kScanThreads + threadIdx.x;
+    sbuf[(e / kScanItems) * (kScanItems + 1) + e % kScanItems] =
+        scan_load(in, base + e, n, reverse, identity);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) vals[k] = sbuf[threadIdx.x * (kScanItems + 1) + k];
+  __syncthreads();  // the buffer is free again
+}
+
 template <typename T, typename Epi>
 __device__ __forceinline__ void store_tile(const Epi &epi, uint64_t base, uint64_t n,
                                            bool reverse, const T *vals) {
-  __shared__ T sbuf[kScanThreads * (kScanItems + 1)];
+  T *sbuf = tile_sbuf<T>();
 #pragma unroll
   for (int k = 0; k < kScanItems; k++)
     sbuf[threadIdx.x * (kScanItems + 1) + k] = vals[k];
@@ -238,12 +272,6 @@ __device__ __forceinline__ void store_tile(const Epi &epi, uint64_t base, uint64
   __syncthreads();
 }
 
-// tile t of the scan order: element i of the array (forward or reversed)
-template <typename T>
-__device__ __forceinline__ T scan_load(const T *in, uint64_t i, uint64_t n,
-                                       bool reverse, T identity) {
-  return i < n ? in[reverse ? n - 1 - i : i] : identity;
-}
 
 template <typename T, typename Op>
 __global__ void k_scan_reduce(const T *__restrict__ in, uint64_t n, T identity,
@@ -294,13 +322,10 @@ __global__ void k_scan_ranges(const T *__restrict__ in, Epi out,
     const uint64_t base = t * kScanTile;
     if (base >= n) break;
     T vals[kScanItems];
+    load_tile(in, base, n, reverse, identity, vals);
     T acc = identity;
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-      vals[k] = scan_load(in, base + (uint64_t)threadIdx.x * kScanItems + k, n,
-                          reverse, identity);
-      acc = op(acc, vals[k]);
-    }
+    for (int k = 0; k < kScanItems; k++) acc = op(acc, vals[k]);
     T total;
     T run = op(carry, block_exclusive(acc, identity, op, &total));
 #pragma unroll
@@ -325,13 +350,10 @@ __global__ void k_scan_tile(const T *__restrict__ in, Epi out,
   pdl_wait();
   if (d_n && *d_n < n) n = *d_n;
   T vals[kScanItems];
+  load_tile(in, 0, n, reverse, identity, vals);
   T acc = identity;
 #pragma unroll
-  for (int k = 0; k < kScanItems; k++) {
-    vals[k] = scan_load(in, (uint64_t)threadIdx.x * kScanItems + k, n, reverse,
-                        identity);
-    acc = op(acc, vals[k]);
-  }
+  for (int k = 0; k < kScanItems; k++) acc = op(acc, vals[k]);
   T total;
   T run = block_exclusive(acc, identity, op, &total);
 #pragma unroll
@@ -479,13 +501,10 @@ k_scan_lb(const T *__restrict__ in, Epi out, uint64_t n,
     return;
   }
   T vals[kScanItems];
+  load_tile(in, base, n, reverse, identity, vals);
   T acc = identity;
 #pragma unroll
-  for (int k = 0; k < kScanItems; k++) {
-    vals[k] = scan_load(in, base + (uint64_t)threadIdx.x * kScanItems + k, n,
-                        reverse, identity);
-    acc = op(acc, vals[k]);
-  }
+  for (int k = 0; k < kScanItems; k++) acc = op(acc, vals[k]);
   T total;
   T run = block_exclusive(acc, identity, op, &total);
   T carry = identity;
