@@ -922,29 +922,6 @@ __device__ __forceinline__ void block_max_to(int32_t d, unsigned long long *out)
   if (threadIdx.x == 0 && s_max >= 0) atomicMax(out, (unsigned long long)s_max);
 }
 
-__global__ void k_max_depth(const int32_t *__restrict__ depth, uint32_t n,
-                            unsigned long long *__restrict__ out) {
-  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  block_max_to(v < n ? depth[v] : -1, out);
-}
-
-__global__ void k_level_count(const int32_t *__restrict__ depth, uint32_t n,
-                              uint32_t *__restrict__ cnt) {
-  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  const int32_t d = v < n ? depth[v] : -1;
-  level_add(cnt + (d >= 0 ? d : 0), d, d >= 0);
-}
-
-__global__ void k_level_scatter(const int32_t *__restrict__ depth, uint32_t n,
-                                const uint32_t *__restrict__ off,
-                                uint32_t *__restrict__ ctr,
-                                uint32_t *__restrict__ list) {
-  uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  const int32_t d = v < n ? depth[v] : -1;
-  const uint32_t at = level_add(ctr + (d >= 0 ? d : 0), d, d >= 0);
-  if (d >= 0) list[off[d] + at] = v;
-}
-
 __global__ void k_bc_init(double *__restrict__ sigma, double *__restrict__ ratio,
                           double *__restrict__ dep, uint32_t n, uint32_t src) {
   uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1459,7 +1436,11 @@ sst_status pagerank(sst_graph *g, uint32_t iters, double damping, double *d_rank
   return SST_OK;
 }
 
-sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths) {
+// BFS from src; with d_levels (n entries, device) it also lists the vertices
+// level by level, as the level queues come (each level's new queue is
+// copied after the level), their counts in *level_counts.
+static sst_status bfs_run(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths,
+                          uint32_t *d_levels, std::vector<uint32_t> *level_counts) {
   sst_status st = ensure_lists(g);
   if (st != SST_OK) return st;
   TravState *t = g->trav;
@@ -1489,6 +1470,12 @@ sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths
   uint32_t *q = t->qa.p, *nq = t->qb.p;
   unsigned long long *cnt = t->d_small;
   const uint64_t m = g->m;
+  uint64_t listed = 0;  // vertices listed in d_levels so far
+  if (d_levels) {
+    level_counts->assign(1, 1u);  // level 0: the source
+    SST_CUDA_TRY(cudaMemcpyAsync(d_levels, &src, 4, cudaMemcpyHostToDevice, s));
+    listed = 1;
+  }
   SST_CUDA_TRY(t->icnt.ensure((uint64_t)n + 1));
   SST_CUDA_TRY(t->ioff.ensure((uint64_t)n + 1));
   g->arena.reset();
@@ -1528,10 +1515,23 @@ sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths
     qn = t->h_small[0];
     qdeg = t->h_small[1];
     qitems = t->h_small[2];
+    if (d_levels && qn) {
+      if (listed + qn > n) {
+        set_error_message("BFS listed more than n vertices");
+        return SST_EDEVICE;
+      }
+      SST_CUDA_TRY(cudaMemcpyAsync(d_levels + listed, nq, qn * 4, cudaMemcpyDeviceToDevice, s));
+      level_counts->push_back((uint32_t)qn);
+      listed += qn;
+    }
     std::swap(q, nq);
   }
   SST_CUDA_TRY(cudaGetLastError());
   return SST_OK;
+}
+
+sst_status bfs(sst_graph *g, uint32_t src, int32_t *d_parents, int32_t *d_depths) {
+  return bfs_run(g, src, d_parents, d_depths, nullptr, nullptr);
 }
 
 sst_status cc(sst_graph *g, uint32_t *d_labels) {
@@ -1573,26 +1573,21 @@ sst_status bc(sst_graph *g, uint32_t src, double *d_dep) {
   TravState *t = state(g);
   uint32_t n = g->n;
   SST_CUDA_TRY(t->depth_tmp.ensure(n));
-  sst_status st = bfs(g, src, nullptr, t->depth_tmp.p);
+  SST_CUDA_TRY(t->lvl_list.ensure(n + 1));
+  // the BFS lists the vertices level by level as its queues come (their
+  // order within a level does not enter any per-vertex sum below)
+  std::vector<uint32_t> hc;
+  sst_status st = bfs_run(g, src, nullptr, t->depth_tmp.p, t->lvl_list.p, &hc);
   if (st != SST_OK) return st;
   cudaStream_t s = g->stream;
   const int32_t *depth = t->depth_tmp.p;
-  SST_CUDA_TRY(cudaMemsetAsync(t->d_small, 0, 8, s));
-  SST_LAUNCH(k_max_depth, blocks_for(n), kTB, 0, s, depth, n, t->d_small);
-  SST_CUDA_TRY(cudaMemcpyAsync(t->h_small, t->d_small, 8, cudaMemcpyDeviceToHost, s));
-  SST_CUDA_TRY(cudaStreamSynchronize(s));
-  uint32_t D = (uint32_t)t->h_small[0];
-  SST_CUDA_TRY(t->lvl_cnt.ensure(4 * ((uint64_t)D + 2)));
-  SST_CUDA_TRY(t->lvl_list.ensure(n + 1));
+  const uint32_t D = (uint32_t)hc.size() - 1;  // deepest level
+  hc.resize(D + 2, 0u);
+  SST_CUDA_TRY(t->lvl_cnt.ensure(2 * ((uint64_t)D + 2)));
   SST_CUDA_TRY(t->sigma.ensure(n));
   SST_CUDA_TRY(t->ratio.ensure(n));
-  uint32_t *cnt = t->lvl_cnt.p, *off = cnt + D + 2, *ctr = off + D + 2,
-           *ibound = ctr + D + 2;
-  SST_CUDA_TRY(cudaMemsetAsync(cnt, 0, 3 * ((uint64_t)D + 2) * 4, s));
-  SST_LAUNCH(k_level_count, blocks_for(n), kTB, 0, s, depth, n, cnt);
-  std::vector<uint32_t> hc(D + 2), ho(D + 2), hib(D + 2);
-  SST_CUDA_TRY(cudaMemcpyAsync(hc.data(), cnt, (D + 1) * 4, cudaMemcpyDeviceToHost, s));
-  SST_CUDA_TRY(cudaStreamSynchronize(s));
+  uint32_t *off = t->lvl_cnt.p, *ibound = off + D + 2;
+  std::vector<uint32_t> ho(D + 2), hib(D + 2);
   uint32_t acc = 0;
   for (uint32_t d = 0; d <= D; d++) {
     ho[d] = acc;
@@ -1601,8 +1596,6 @@ sst_status bc(sst_graph *g, uint32_t src, double *d_dep) {
   ho[D + 1] = acc;
   const uint32_t R = acc;  // reached vertices
   SST_CUDA_TRY(cudaMemcpyAsync(off, ho.data(), (D + 2) * 4, cudaMemcpyHostToDevice, s));
-  SST_LAUNCH(k_level_scatter, blocks_for(n), kTB, 0, s, depth, n, off, ctr,
-             t->lvl_list.p);
   // chunk items of the big vertices, in level-list order
   SST_CUDA_TRY(t->icnt.ensure((uint64_t)R + 1));
   SST_CUDA_TRY(t->ioff.ensure((uint64_t)R + 1));
