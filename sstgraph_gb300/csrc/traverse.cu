@@ -1928,9 +1928,19 @@ __global__ void k_msbc_sigma_small(DGraph g, const uint32_t *__restrict__ list,
   const uint32_t *p = g.slots + g.base[v];
   uint32_t dg = g.deg[v];
   double acc = 0.0;
-  for (uint32_t k = 0; k < dg; k++) {
-    uint32_t u = p[k];
-    if (depth[so + u] == d - 1) acc += sigma[so + u];
+  for (uint32_t k0 = 0; k0 < dg; k0 += kBcAhead) {  // as in k_sigma_small
+    uint32_t u[kBcAhead];
+    bool on[kBcAhead];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) u[q] = k0 + q < dg ? p[k0 + q] : 0u;
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) on[q] = k0 + q < dg && depth[so + u[q]] == d - 1;
+    double x[kBcAhead];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) x[q] = on[q] ? sigma[so + u[q]] : 0.0;
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++)
+      if (on[q]) acc += x[q];
   }
   sigma[so + v] = acc;
 }
@@ -2015,9 +2025,19 @@ __global__ void k_msbc_delta_small(DGraph g, const uint32_t *__restrict__ list,
   const uint32_t *p = g.slots + g.base[v];
   uint32_t dg = g.deg[v];
   double acc = 0.0;
-  for (uint32_t k = 0; k < dg; k++) {
-    uint32_t w = p[k];
-    if (depth[so + w] == d + 1) acc += ratio[so + w];
+  for (uint32_t k0 = 0; k0 < dg; k0 += kBcAhead) {  // as in k_sigma_small
+    uint32_t w[kBcAhead];
+    bool on[kBcAhead];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) w[q] = k0 + q < dg ? p[k0 + q] : 0u;
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) on[q] = k0 + q < dg && depth[so + w[q]] == d + 1;
+    double x[kBcAhead];
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++) x[q] = on[q] ? ratio[so + w[q]] : 0.0;
+#pragma unroll
+    for (int q = 0; q < kBcAhead; q++)
+      if (on[q]) acc += x[q];
   }
   double dv = sigma[so + v] * acc;
   dep[so + v] = dv;
