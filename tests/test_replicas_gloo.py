@@ -58,3 +58,13 @@ def test_reference_arm_under_torchrun_prints_once():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port"
+
+
+def test_printed_lines_are_strict_json():
+    """Every line bench.py prints is strict JSON: non-finite floats (a
+    comparison on a graph where a quantity is undefined) become null."""
+    sys.path.insert(0, ROOT)
+    import bench
+    line = {"a": float("nan"), "b": [1.5, float("inf"), {"c": -float("inf")}], "d": "x"}
+    text = json.dumps(bench.strict(line), allow_nan=False)
+    assert json.loads(text) == {"a": None, "b": [1.5, None, {"c": None}], "d": "x"}
