@@ -754,208 +754,6 @@ __global__ void k_emit(const uint64_t *__restrict__ mt, const uint64_t *__restri
   emit_group(a, gid, in ? mt[gid] : 0, in ? mtpos[gid] : 0);
 }
 
-// Exclusive scan of one value per thread over a block of kPlanThreads
-// (forward: over the threads before; reverse: over the threads after),
-// through sh[kPlanThreads]: warp 0 walks 32 positions a lane, then scans
-// the 32 lane totals.
-constexpr uint32_t kPlanThreads = 1024;
-template <typename T, typename Op>
-__device__ __forceinline__ T plan_block_excl(T x, T ident, Op op, bool reverse, T *sh) {
-  const uint32_t t = threadIdx.x;
-  sh[t] = x;
-  __syncthreads();
-  if (t < 32) {
-    T agg = ident;
-    for (uint32_t k = 0; k < 32; k++) {
-      const uint32_t q = 32 * t + k, i = reverse ? kPlanThreads - 1 - q : q;
-      agg = op(agg, sh[i]);
-    }
-    T inc = agg;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const T y = __shfl_up_sync(0xffffffffu, inc, d);
-      if ((int)t >= d) inc = op(inc, y);
-    }
-    T run = __shfl_up_sync(0xffffffffu, inc, 1);
-    if (t == 0) run = ident;
-    for (uint32_t k = 0; k < 32; k++) {
-      const uint32_t q = 32 * t + k, i = reverse ? kPlanThreads - 1 - q : q;
-      const T v = sh[i];
-      sh[i] = run;
-      run = op(run, v);
-    }
-  }
-  __syncthreads();
-  const T r = sh[t];
-  __syncthreads();
-  return r;
-}
-
-// fkey / bkey of group gid (see k_dom_keys)
-__device__ __forceinline__ void dom_keys_of(const uint64_t *p_ul, const uint32_t *g_start,
-                                            const uint8_t *gtype, const uint8_t *glev,
-                                            const uint32_t *gw0, const uint32_t *gw1,
-                                            uint64_t gid, uint64_t &f, uint64_t &bk) {
-  f = 0;
-  bk = ~0ull;
-  if (gtype[gid] >= kWindow) {
-    const uint64_t u = p_ul[g_start[gid]] >> 32, lev = glev[gid];
-    f = (u << 32) | ((uint64_t)gw1[gid] << 5) | lev;
-    bk = (u << 32) | ((uint64_t)gw0[gid] << 5) | (31 - lev);
-  }
-}
-
-// the merge / task flags of group gid from its exclusive window scans
-// (see k_dom_classify)
-__device__ __forceinline__ uint64_t dom_flags_of(const uint64_t *p_ul, const uint32_t *g_start,
-                                                 const uint8_t *gtype, const uint8_t *glev,
-                                                 uint64_t gid, uint64_t L, uint64_t R) {
-  uint32_t mf = 0, tf = 0;
-  if (gtype[gid] != kNone) {
-    const uint64_t key = p_ul[g_start[gid]];
-    const uint64_t u = key >> 32;
-    const uint32_t leaf = (uint32_t)key;
-    const bool lcov = L != 0 && (L >> 32) == u && ((L >> 5) & kWinMask) > leaf;
-    const bool rcov = R != ~0ull && (R >> 32) == u && ((R >> 5) & kWinMask) <= leaf;
-    const uint32_t lt = (uint32_t)(L & 31), rt = 31u - (uint32_t)(R & 31);
-    if (gtype[gid] == kMerge) {
-      mf = !(lcov || rcov);
-    } else {
-      const uint32_t lev = glev[gid];
-      tf = !((lcov && lt >= lev) || (rcov && rt > lev));
-    }
-  }
-  return ((uint64_t)tf << 32) | mf;
-}
-
-struct OpMaxU64 {
-  __device__ uint64_t operator()(uint64_t a, uint64_t b) const { return a > b ? a : b; }
-};
-struct OpMinU64 {
-  __device__ uint64_t operator()(uint64_t a, uint64_t b) const { return a < b ? a : b; }
-};
-struct OpAddU64 {
-  __device__ uint64_t operator()(uint64_t a, uint64_t b) const { return a + b; }
-};
-
-// Steps 7-8 for a batch of at most kPlanGroups groups in one block: the
-// window keys, both dominance scans, the classification, the merge/task
-// scan (its totals to *nmt, as the scan's would be) and the emit -- the six
-// launches of the general form, with the same results.  Thread t takes a
-// contiguous run of groups; fscan (global) holds each group's forward
-// window scan between the two walks.  Each group is a chain of dependent
-// loads per walk, so the block only wins while the runs stay short: at
-// 1e3 pairs it saves 6-7 us a batch, at 1e4 (runs of ~9 groups) it lost
-// 20 us to the six launches.
-constexpr uint32_t kPlanGroups = 2 * kPlanThreads;
-__global__ void __launch_bounds__(kPlanThreads, 1)
-k_plan_small(const uint64_t *__restrict__ p_ul, const uint32_t *__restrict__ g_start,
-             const uint8_t *__restrict__ gtype, const uint8_t *__restrict__ glev,
-             const uint32_t *__restrict__ gw0, const uint32_t *__restrict__ gw1,
-             const uint32_t *__restrict__ d_ngroups, uint64_t *__restrict__ fscan,
-             uint64_t *__restrict__ mt, uint64_t *__restrict__ nmt, EmitArgs a) {
-  pdl_wait();
-  __shared__ uint64_t sh[kPlanThreads];
-  const uint32_t t = threadIdx.x;
-  const uint32_t ng = min(*d_ngroups, kPlanGroups);
-  const uint32_t per = (ng + kPlanThreads - 1) / kPlanThreads;  // <= 16
-  const uint32_t c0 = min(t * per, ng), c1 = min(c0 + per, ng);
-  // the run's window keys
-  uint64_t fa = 0, ba = ~0ull;
-  for (uint32_t gid = c0; gid < c1; gid++) {
-    uint64_t f, bk;
-    dom_keys_of(p_ul, g_start, gtype, glev, gw0, gw1, gid, f, bk);
-    fa = f > fa ? f : fa;
-    ba = bk < ba ? bk : ba;
-  }
-  uint64_t L = plan_block_excl(fa, (uint64_t)0, OpMaxU64{}, false, sh);
-  uint64_t R = plan_block_excl(ba, ~(uint64_t)0, OpMinU64{}, true, sh);
-  // forward walk: each group's forward scan
-  for (uint32_t gid = c0; gid < c1; gid++) {
-    uint64_t f, bk;
-    dom_keys_of(p_ul, g_start, gtype, glev, gw0, gw1, gid, f, bk);
-    fscan[gid] = L;
-    L = f > L ? f : L;
-  }
-  // backward walk: the flags
-  uint64_t ma = 0;
-  for (uint32_t gid = c1; gid-- > c0;) {
-    uint64_t f, bk;
-    dom_keys_of(p_ul, g_start, gtype, glev, gw0, gw1, gid, f, bk);
-    const uint64_t m = dom_flags_of(p_ul, g_start, gtype, glev, gid, fscan[gid], R);
-    mt[gid] = m;
-    ma += m;
-    R = bk < R ? bk : R;
-  }
-  uint64_t pos = plan_block_excl(ma, (uint64_t)0, OpAddU64{}, false, sh);
-  if (t == kPlanThreads - 1) *nmt = pos + ma;  // (merges, tasks) in one word
-  // the emit, the warp's lanes in step (their q-th groups together)
-  for (uint32_t q = 0; q < per; q++) {
-    const uint32_t gid = c0 + q;
-    const bool in = gid < c1;
-    const uint64_t m = in ? mt[gid] : 0;
-    emit_group(a, gid, m, pos);
-    pos += m;
-  }
-}
-
-struct OpAddU32 {
-  __device__ uint32_t operator()(uint32_t a, uint32_t b) const { return a + b; }
-};
-
-// Steps 4-5 for a batch of at most kPlanGroups pairs in one block: the
-// kept keys' positions (a block scan of k_locate's flags, the count to
-// *n_items), the packing (as k_pack), the group flags and the group starts
-// (as k_group_flags and the group-start scan, the count to *n_groups) --
-// four launches of the general form, with the same results.
-__global__ void __launch_bounds__(kPlanThreads, 1)
-k_pack_small(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ flag,
-             const uint32_t *__restrict__ leaf, uint64_t b, int dbits,
-             uint64_t *__restrict__ p_ul, uint32_t *__restrict__ p_x,
-             const uint32_t *__restrict__ wv, uint32_t *__restrict__ p_w,
-             const uint64_t *__restrict__ lS, const uint32_t *__restrict__ lc,
-             uint64_t *__restrict__ p_S, uint32_t *__restrict__ p_c,
-             uint32_t *__restrict__ n_items, uint32_t *__restrict__ n_groups,
-             uint32_t *__restrict__ g_start) {
-  pdl_wait();
-  __shared__ uint32_t sh[kPlanThreads];
-  const uint32_t t = threadIdx.x;
-  const uint32_t nb = b < kPlanGroups ? (uint32_t)b : kPlanGroups;
-  const uint32_t per = (nb + kPlanThreads - 1) / kPlanThreads;
-  const uint32_t c0 = min(t * per, nb), c1 = min(c0 + per, nb);
-  uint32_t fa = 0;
-  for (uint32_t i = c0; i < c1; i++) fa += flag[i];
-  uint32_t pos = plan_block_excl(fa, 0u, OpAddU32{}, false, sh);
-  if (t == kPlanThreads - 1) {
-    *n_items = pos + fa;
-    sh[0] = pos + fa;
-  }
-  for (uint32_t i = c0; i < c1; i++) {
-    if (!flag[i]) continue;
-    const uint64_t k = keys[i];
-    const uint32_t j = pos++;
-    p_ul[j] = ((k >> dbits) << 32) | leaf[i];
-    p_x[j] = (uint32_t)(k & ((1ull << dbits) - 1));
-    if (p_w) p_w[j] = wv[i];
-    p_S[j] = lS[i];
-    p_c[j] = lc[i];
-  }
-  __syncthreads();  // the packed items and the count are visible to the block
-  const uint32_t items = sh[0];
-  __syncthreads();
-  const uint32_t per2 = (items + kPlanThreads - 1) / kPlanThreads;
-  const uint32_t d0 = min(t * per2, items), d1 = min(d0 + per2, items);
-  uint32_t ga = 0;
-  for (uint32_t j = d0; j < d1; j++) ga += (j == 0 || p_ul[j] != p_ul[j - 1]) ? 1u : 0u;
-  uint32_t gp = plan_block_excl(ga, 0u, OpAddU32{}, false, sh);
-  if (t == kPlanThreads - 1) {
-    *n_groups = gp + ga;
-    g_start[gp + ga] = items;  // the list's end (g_start[0] = 0 when empty)
-  }
-  for (uint32_t j = d0; j < d1; j++)
-    if (j == 0 || p_ul[j] != p_ul[j - 1]) g_start[gp++] = j;
-}
-
 __global__ void k_task_setup_hard(DGraph g, uint64_t inv_fill, bool insert,
                                   const uint64_t *__restrict__ p_ul,
                                   const uint32_t *__restrict__ g_start,
@@ -1888,19 +1686,14 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     // sorted key in (8 B), flag and leaf out (8 B)
     SST_LAUNCH_PDL_B(16 * b, k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg,
                  insert, flag, leaf, wt ? wv : nullptr, lS, lc, nkeys);
-    if (b <= kPlanGroups) {
-      SST_LAUNCH_PDL(k_pack_small, 1, kPlanThreads, 0, s, sorted, flag, leaf, b, dbits, p_ul,
-                     p_x, wv, p_w, lS, lc, p_S, p_c, &P->n_items, &P->n_groups, g_start);
-    } else {
-      SST_CUDA_TRY((scan<uint32_t, OpAdd>(flag, pos, b, 0u, OpAdd{}, true, false,
-                                          &P->n_items, A, s)));
-      SST_LAUNCH_PDL(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,
-                     p_ul, p_x, wv, p_w, lS, lc, p_S, p_c);
-      SST_LAUNCH_PDL(k_group_flags, blocks_for(b), kTB, 0, s, p_ul, &P->n_items, b, gflag);
-      SST_CUDA_TRY((scan_epi<uint32_t, OpAdd, GroupStartEpi>(
-          gflag, b, 0u, OpAdd{}, true, false, &P->n_groups, A, s, nullptr,
-          GroupStartEpi{gflag, &P->n_items, b, g_start}, false)));
-    }
+    SST_CUDA_TRY((scan<uint32_t, OpAdd>(flag, pos, b, 0u, OpAdd{}, true, false,
+                                        &P->n_items, A, s)));
+    SST_LAUNCH_PDL(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,
+                   p_ul, p_x, wv, p_w, lS, lc, p_S, p_c);
+    SST_LAUNCH_PDL(k_group_flags, blocks_for(b), kTB, 0, s, p_ul, &P->n_items, b, gflag);
+    SST_CUDA_TRY((scan_epi<uint32_t, OpAdd, GroupStartEpi>(
+        gflag, b, 0u, OpAdd{}, true, false, &P->n_groups, A, s, nullptr,
+        GroupStartEpi{gflag, &P->n_items, b, g_start}, false)));
     // 6: classify (grids capped: the kernels stride over the device count)
     const unsigned cap_blocks = (unsigned)g->sms * 8;
     const unsigned tgrid = std::min(blocks_for(b), cap_blocks);
@@ -1925,31 +1718,23 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     static_assert(offsetof(PlanSummary, n_tasks) == offsetof(PlanSummary, n_merge) + 4 &&
                       offsetof(PlanSummary, n_merge) % 8 == 0,
                   "n_merge and n_tasks share one aligned 64-bit word");
-    if (b <= kPlanGroups) {
-      // at most kPlanGroups groups: all of it in one block (fscan in merge_jk,
-      // which the emit overwrites after the last scan)
-      SST_LAUNCH_PDL(k_plan_small, 1, kPlanThreads, 0, s, p_ul, g_start, gtype, glev, gw0,
-                     gw1, &P->n_groups, merge_jk, mt,
-                     reinterpret_cast<uint64_t *>(&P->n_merge), ea);
-    } else {
-      SST_LAUNCH_PDL(k_dom_keys, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
-                     gw0, gw1, &P->n_groups, b, fkey, bkey);
-      // the scans run out of place into merge_jk and mtpos, which hold
-      // nothing until the merge/task scan and k_emit below overwrite them
-      uint64_t *fscan = merge_jk, *bscan = mtpos;
-      // the two are independent: the backward one runs beside the forward one
-      SST_CUDA_TRY(fork_aux(s, 1));
-      SST_CUDA_TRY((scan<uint64_t, OpMax>(fkey, fscan, b, 0ull, OpMax{}, true, false,
-                                          nullptr, A, s)));
-      SST_CUDA_TRY((scan<uint64_t, OpMin>(bkey, bscan, b, ~0ull, OpMin{}, true, true,
-                                          nullptr, A, g->aux[0])));
-      SST_CUDA_TRY(join_aux(s, 1));
-      SST_LAUNCH_PDL(k_dom_classify, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
-                     fscan, bscan, &P->n_groups, b, mt);
-      SST_CUDA_TRY((scan<uint64_t, OpAdd>(mt, mtpos, b, 0ull, OpAdd{}, true, false,
-                                          reinterpret_cast<uint64_t *>(&P->n_merge), A, s)));
-      SST_LAUNCH_PDL(k_emit, blocks_for(b), kTB, 0, s, mt, mtpos, ea);
-    }
+    SST_LAUNCH_PDL(k_dom_keys, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
+                   gw0, gw1, &P->n_groups, b, fkey, bkey);
+    // the scans run out of place into merge_jk and mtpos, which hold
+    // nothing until the merge/task scan and k_emit below overwrite them
+    uint64_t *fscan = merge_jk, *bscan = mtpos;
+    // the two are independent: the backward one runs beside the forward one
+    SST_CUDA_TRY(fork_aux(s, 1));
+    SST_CUDA_TRY((scan<uint64_t, OpMax>(fkey, fscan, b, 0ull, OpMax{}, true, false,
+                                        nullptr, A, s)));
+    SST_CUDA_TRY((scan<uint64_t, OpMin>(bkey, bscan, b, ~0ull, OpMin{}, true, true,
+                                        nullptr, A, g->aux[0])));
+    SST_CUDA_TRY(join_aux(s, 1));
+    SST_LAUNCH_PDL(k_dom_classify, blocks_for(b), kTB, 0, s, p_ul, g_start, gtype, glev,
+                   fscan, bscan, &P->n_groups, b, mt);
+    SST_CUDA_TRY((scan<uint64_t, OpAdd>(mt, mtpos, b, 0ull, OpAdd{}, true, false,
+                                        reinterpret_cast<uint64_t *>(&P->n_merge), A, s)));
+    SST_LAUNCH_PDL(k_emit, blocks_for(b), kTB, 0, s, mt, mtpos, ea);
     if (fork && insert) {
       sst_status st = fork_merges(s);
       if (st != SST_OK) return st;

@@ -49,8 +49,7 @@ def test_empty_and_tiny(sg):
 def test_batch_sizes_across_sort_forms(sg, b):
     """Batch sizes on both sides of each form of the key sort: one CTA
     (up to 2048 keys), one launch a pass over tiles of 1024 keys (up to 2^18
-    keys) or of 4096 keys (up to 256 tiles), and the scanned form -- and on
-    both sides of the one-block planning kernels (up to 2048 pairs); each
+    keys) or of 4096 keys (up to 256 tiles), and the scanned form; each
     batch holds a hub row (skewed high digits) and repeated pairs, and half
     of it is removed again."""
     n = 1 << 14
