@@ -364,6 +364,42 @@ __device__ __forceinline__ uint32_t leaf_slot(uint32_t linev, uint64_t S,
   return (uint32_t)lane < c ? a : kEmpty;
 }
 
+// Groups of one item (nearly all of them: a batch rarely puts two ids in
+// one leaf) take eight lanes, four at a time in a warp: lane `sub` of the
+// eight holds the leaf's slots 4 sub .. 4 sub + 3 from S (kEmpty from c on),
+// and the one id's place is the count of the slots below it.  The lists of
+// a warp's one-item groups and of its other groups are built per chunk of
+// 32 groups in shared memory (one byte per group).
+constexpr int kLeafWarps = kTB / 32;  // warps of the leaf kernels' blocks
+__device__ __forceinline__ void load_quarter(const uint32_t *slots, uint64_t S,
+                                             uint32_t c, int sub, uint32_t (&a)[4]) {
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const uint32_t p = 4 * sub + r;
+    a[r] = p < c ? slots[S + p] : kEmpty;
+  }
+}
+// slots below x in the group's eight lanes (aligned lane octets)
+__device__ __forceinline__ uint32_t below_in_octet(const uint32_t (&a)[4], uint32_t x) {
+  uint32_t b = (uint32_t)(a[0] < x) + (a[1] < x) + (a[2] < x) + (a[3] < x);
+  b += __shfl_xor_sync(0xffffffffu, b, 1);
+  b += __shfl_xor_sync(0xffffffffu, b, 2);
+  b += __shfl_xor_sync(0xffffffffu, b, 4);
+  return b;
+}
+// list the chunk's groups, one-item groups first: list[0, n1) their lanes
+// in order, list[n1, cnt) the others'; returns n1
+__device__ __forceinline__ uint32_t list_groups(uint8_t *list, bool ok, bool one, int lane) {
+  const uint32_t okm = __ballot_sync(0xffffffffu, ok);
+  const uint32_t om = __ballot_sync(0xffffffffu, ok && one);
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t n1 = __popc(om);
+  __syncwarp();  // the previous chunk's lists are read
+  if (ok) list[one ? __popc(om & lt) : n1 + __popc(okm & ~om & lt)] = (uint8_t)lane;
+  __syncwarp();
+  return n1;
+}
+
 // remove: delete inside each touched leaf, take the count off the row's
 // degree and classify the group: a leaf of a multi-leaf segment under the
 // lower bound goes to the climb list; a one-leaf segment that emptied or
@@ -388,7 +424,9 @@ k_leaf_delete(DGraph g, uint32_t lo_leaf, const uint64_t *__restrict__ p_ul,
               uint32_t *__restrict__ gw0, uint32_t *__restrict__ gw1,
               uint32_t *__restrict__ climb, uint32_t *__restrict__ nclimb) {
   pdl_wait();
-  const int lane = threadIdx.x & 31;
+  __shared__ uint8_t glist[kLeafWarps][32];
+  const int lane = threadIdx.x & 31, sub = lane & 7;
+  uint8_t *list = glist[threadIdx.x >> 5];
   constexpr int Q = kGroupsPerWarp;
   const uint32_t ng = *d_ngroups;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -406,15 +444,38 @@ k_leaf_delete(DGraph g, uint32_t lo_leaf, const uint64_t *__restrict__ p_ul,
     // only needs to be told apart
     const uint32_t capl = (cwl & kMultiLeaf) ? kLeaf + 1 : one_leaf_cap(cwl);
     const uint32_t cnt = ng - w * 32 < 32 ? (uint32_t)(ng - w * 32) : 32u;
-    uint32_t my_nc = 0;  // lane l: group l's count after the deletes
-    for (uint32_t q0 = 0; q0 < cnt; q0 += Q) {
+    // one-item groups: the slots from the deleted id's place on take their
+    // right neighbour (kEmpty past the count)
+    const uint32_t n1 = list_groups(list, okl, kl == 1 && !g.vals, lane);
+    for (uint32_t f0 = 0; f0 < n1; f0 += 4) {
+      const uint32_t f = f0 + (lane >> 3);
+      const bool on = f < n1;
+      const int src = list[on ? f : 0];
+      const uint32_t j0 = __shfl_sync(0xffffffffu, j0l, src);
+      const uint64_t S = __shfl_sync(0xffffffffu, Sl, src);
+      const uint32_t cw = __shfl_sync(0xffffffffu, cwl, src);
+      const uint32_t c = on ? (cw & 0xff) : 0u;
+      const uint32_t d = on ? p_x[j0] : kEmpty;
+      uint32_t a[4];
+      load_quarter(g.slots, S, c, sub, a);
+      const uint32_t pos = below_in_octet(a, d);
+      const uint32_t nxt = __shfl_down_sync(0xffffffffu, a[0], 1, 8);
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const uint32_t p = 4 * sub + r;
+        if (p >= pos && p < c) g.slots[S + p] = r < 3 ? a[r + 1] : (sub == 7 ? kEmpty : nxt);
+      }
+    }
+    // the other groups: a warp each, kGroupsPerWarp at a time
+    const uint32_t nrest = cnt - n1;
+    for (uint32_t q0 = 0; q0 < nrest; q0 += Q) {
       uint32_t j0[Q], k[Q], d[Q], linev[Q], cw[Q];
       uint64_t S[Q];
       bool ok[Q];
 #pragma unroll
       for (int q = 0; q < Q; q++) {
-        const int src = (int)((q0 + q) & 31);
-        ok[q] = q0 + q < cnt;
+        ok[q] = q0 + q < nrest;
+        const int src = list[n1 + (ok[q] ? q0 + q : 0)];
         j0[q] = __shfl_sync(0xffffffffu, j0l, src);
         k[q] = ok[q] ? __shfl_sync(0xffffffffu, kl, src) : 0;
         S[q] = __shfl_sync(0xffffffffu, Sl, src);
@@ -443,14 +504,13 @@ k_leaf_delete(DGraph g, uint32_t lo_leaf, const uint64_t *__restrict__ p_ul,
         // the ids come from registers: no lane reads the line again
         if (keep) g.slots[S[q] + pos] = a;
         if ((uint32_t)lane >= c - k[q] && (uint32_t)lane < c) g.slots[S[q] + lane] = kEmpty;
-        if (lane == (int)((q0 + q) & 31)) my_nc = c - k[q];
       }
     }
     // the chunk's bookkeeping, lane l for group l
     const uint32_t gid = (uint32_t)(w * 32) + lane;
     bool to_climb = false;
     if (okl) {
-      const uint32_t nc = my_nc;
+      const uint32_t nc = (cwl & 0xff) - kl;  // every item of a group is present
       if (cwl & kMultiLeaf) g.lcnt[Sl >> kLeafLog] = (uint8_t)nc;
       atomicSub(&g.deg[ul], kl);
       uint8_t type = kNone;
@@ -819,7 +879,9 @@ k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul, const uint32_t *__rest
              const uint64_t *__restrict__ merge_jk, const uint32_t *__restrict__ d_nmerge,
              const uint32_t *__restrict__ p_w) {
   pdl_wait();
-  const int lane = threadIdx.x & 31;
+  __shared__ uint8_t glist[kLeafWarps][32];
+  const int lane = threadIdx.x & 31, sub = lane & 7;
+  uint8_t *list = glist[threadIdx.x >> 5];
   constexpr int Q = kGroupsPerWarp;
   const uint32_t nmerge = *d_nmerge;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -833,14 +895,38 @@ k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul, const uint32_t *__rest
     const uint32_t cwl = okl ? p_c[j0l] : 0;
     const uint32_t ul = okl ? (uint32_t)(p_ul[j0l] >> 32) : 0u;
     const uint32_t cnt = nmerge - w * 32 < 32 ? (uint32_t)(nmerge - w * 32) : 32u;
-    for (uint32_t q0 = 0; q0 < cnt; q0 += Q) {
+    // one-item groups: the new id goes to the count of the slots below it,
+    // the slots from there up move one place right
+    const uint32_t n1 = list_groups(list, okl, kl == 1 && !g.vals, lane);
+    for (uint32_t f0 = 0; f0 < n1; f0 += 4) {
+      const uint32_t f = f0 + (lane >> 3);
+      const bool on = f < n1;
+      const int src = list[on ? f : 0];
+      const uint32_t j0 = __shfl_sync(0xffffffffu, j0l, src);
+      const uint64_t S = __shfl_sync(0xffffffffu, Sl, src);
+      const uint32_t cw = __shfl_sync(0xffffffffu, cwl, src);
+      const uint32_t c = on ? (cw & 0xff) : 0u;
+      const uint32_t x = on ? p_x[j0] : kEmpty;
+      uint32_t a[4];
+      load_quarter(g.slots, S, c, sub, a);
+      const uint32_t pos = below_in_octet(a, x);
+      const uint32_t prev = __shfl_up_sync(0xffffffffu, a[3], 1, 8);
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const uint32_t p = 4 * sub + r;
+        if (on && p >= pos && p <= c) g.slots[S + p] = p == pos ? x : (r ? a[r - 1] : prev);
+      }
+    }
+    // the other groups: a warp each, kGroupsPerWarp at a time
+    const uint32_t nrest = cnt - n1;
+    for (uint32_t q0 = 0; q0 < nrest; q0 += Q) {
       uint32_t j0[Q], k[Q], x[Q], linev[Q], cw[Q];
       uint64_t S[Q];
       bool ok[Q];
 #pragma unroll
       for (int q = 0; q < Q; q++) {
-        const int src = (int)((q0 + q) & 31);
-        ok[q] = q0 + q < cnt;
+        ok[q] = q0 + q < nrest;
+        const int src = list[n1 + (ok[q] ? q0 + q : 0)];
         j0[q] = __shfl_sync(0xffffffffu, j0l, src);
         k[q] = ok[q] ? __shfl_sync(0xffffffffu, kl, src) : 0;
         S[q] = __shfl_sync(0xffffffffu, Sl, src);
