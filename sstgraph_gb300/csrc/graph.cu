@@ -106,6 +106,28 @@ __device__ __forceinline__ uint32_t count_less(const uint32_t *a, uint32_t lo,
   return lo - b;
 }
 
+// count_less for four keys over the same range at once (the branchless
+// lower bound: each step halves the range for all four searches, so their
+// loads are in flight together)
+__device__ __forceinline__ void count_less4(const uint32_t *a, uint32_t lo, uint32_t hi,
+                                            const uint32_t (&x)[4], uint32_t (&out)[4]) {
+  uint32_t b[4] = {lo, lo, lo, lo};
+  uint32_t n = hi - lo;
+  if (n == 0) {
+#pragma unroll
+    for (int r = 0; r < 4; r++) out[r] = 0;
+    return;
+  }
+  while (n > 1) {
+    const uint32_t half = n >> 1;
+#pragma unroll
+    for (int r = 0; r < 4; r++) b[r] = a[b[r] + half] < x[r] ? b[r] + half : b[r];
+    n -= half;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; r++) out[r] = (b[r] - lo) + (a[b[r]] < x[r] ? 1u : 0u);
+}
+
 __device__ __forceinline__ uint32_t warp_sum_lcnt(const uint8_t *lc,
                                                   uint64_t lo, uint64_t hi) {
   const int lane = threadIdx.x & 31;
@@ -980,30 +1002,34 @@ k_leaf_merge(DGraph g, const uint64_t *__restrict__ p_ul, const uint32_t *__rest
 // leaf's task with one load, not a binary search over the offsets; the
 // source leaves' element counts beside (scnt); and, on an insert, the task
 // of each new item that a task takes (k_emit marked the merged items)
+// (eight lanes a task: most tasks resize a one-leaf row, one leaf each way)
 __global__ void k_task_index(DGraph g, Tasks t, uint32_t ntasks, uint32_t *__restrict__ stask,
                              uint32_t *__restrict__ dtask, uint32_t *__restrict__ itask,
                              uint64_t *__restrict__ scnt) {
   pdl_wait();
-  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const uint32_t sub = threadIdx.x & 7;
   if (w >= ntasks) return;
   const uint64_t s0 = t.soff[w], ns = t.nsrc[w], d0 = t.doff[w], nd = t.ndst[w];
   if (ns) {
     const uint32_t u = t.u[w], l0 = t.w0[w];
     const uint64_t base = g.base[u];
     const uint32_t cap = g.cap[u], deg = g.deg[u];
-    for (uint64_t j = lane; j < ns; j += 32) {
+    for (uint64_t j = sub; j < ns; j += 8) {
       stask[s0 + j] = (uint32_t)w;
       scnt[s0 + j] = leaf_count(g, base, cap, deg, l0 + (uint32_t)j);
     }
   }
-  for (uint64_t j = lane; j < nd; j += 32) dtask[d0 + j] = (uint32_t)w;
+  for (uint64_t j = sub; j < nd; j += 8) dtask[d0 + j] = (uint32_t)w;
   if (itask)
-    for (uint32_t j = t.newbeg[w] + lane; j < t.newend[w]; j += 32) itask[j] = (uint32_t)w;
+    for (uint32_t j = t.newbeg[w] + sub; j < t.newend[w]; j += 8) itask[j] = (uint32_t)w;
 }
 
 
-// warp per source leaf: old elements to their merged rank
+// old elements to their merged rank: eight lanes per source leaf, lane
+// `sub` taking slots sub, sub + 8, sub + 16, sub + 24, four leaves a warp
+// (the chain of dependent loads -- task, row, count, ids, rank among the
+// task's new ids -- is paid once per four leaves, not once per leaf)
 __global__ void k_gather_old(DGraph g, Tasks t, uint32_t ntasks,
                              uint64_t nsrc_total,
                              const uint64_t *__restrict__ spre,
@@ -1011,25 +1037,34 @@ __global__ void k_gather_old(DGraph g, Tasks t, uint32_t ntasks,
                              uint32_t *__restrict__ stage,
                              const uint32_t *__restrict__ stask) {
   pdl_wait();
-  uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  const uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const uint32_t sub = threadIdx.x & 7;
   if (s >= nsrc_total) return;
   const uint64_t tau = stask[s];
-  uint32_t u = t.u[tau];
-  uint32_t l = t.w0[tau] + (uint32_t)(s - t.soff[tau]);
-  uint64_t base = g.base[u];
-  uint32_t c = leaf_count(g, base, g.cap[u], g.deg[u], l);
-  if ((uint32_t)lane >= c) return;
-  uint32_t a = g.slots[base + ((uint64_t)l << kLeafLog) + lane];
-  uint64_t rank = (spre[s] - spre[t.soff[tau]]) + lane +
-                  count_less(p_x, t.newbeg[tau], t.newend[tau], a);
-  if (rank >= t.total[tau]) {
-    atomicAdd(t.err, 1ull);
-    return;
+  const uint32_t u = t.u[tau];
+  const uint64_t soff = t.soff[tau];
+  const uint32_t l = t.w0[tau] + (uint32_t)(s - soff);
+  const uint64_t base = g.base[u];
+  const uint32_t c = leaf_count(g, base, g.cap[u], g.deg[u], l);
+  if (sub >= c) return;
+  const uint64_t at = base + ((uint64_t)l << kLeafLog);
+  uint32_t a[4], below[4];
+#pragma unroll
+  for (int r = 0; r < 4; r++) a[r] = sub + 8 * r < c ? g.slots[at + sub + 8 * r] : kEmpty;
+  count_less4(p_x, t.newbeg[tau], t.newend[tau], a, below);
+  const uint64_t r0 = spre[s] - spre[soff], total = t.total[tau], out = t.out[tau];
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const uint32_t p = sub + 8 * r;
+    if (p >= c) break;
+    const uint64_t rank = r0 + p + below[r];
+    if (rank >= total) {
+      atomicAdd(t.err, 1ull);
+      continue;
+    }
+    stage[out + rank] = a[r];
+    if (t.stage_v) t.stage_v[out + rank] = g.vals[at + p];
   }
-  stage[t.out[tau] + rank] = a;
-  if (t.stage_v)
-    t.stage_v[t.out[tau] + rank] = g.vals[base + ((uint64_t)l << kLeafLog) + lane];
 }
 
 // thread per packed item owned by a task: new elements to their merged rank
@@ -1081,47 +1116,46 @@ __device__ __forceinline__ uint64_t task_new_base(const Tasks &t, uint64_t tau,
   return class_start[log2_floor(capn)] + (uint64_t)t.rank[tau] * capn;
 }
 
-// warp per destination leaf: even redistribution of the staged elements.
-// Lane 0 finds the leaf's task and its share of the task's elements (32-bit
-// arithmetic: a task holds fewer than 2^32 elements) and broadcasts them.
+// even redistribution of the staged elements: eight lanes per destination
+// leaf (slots sub, sub + 8, sub + 16, sub + 24), four leaves a warp.  Each
+// lane finds the leaf's task and its share of the task's elements itself
+// (the loads are the same address across the eight; 32-bit arithmetic: a
+// task holds fewer than 2^32 elements).
 __global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
                                uint64_t ndst_total,
                                const uint64_t *__restrict__ class_start,
                                const uint32_t *__restrict__ stage,
                                const uint32_t *__restrict__ dtask) {
   pdl_wait();
-  uint64_t d = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  const uint64_t d = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const uint32_t sub = threadIdx.x & 7;
   if (d >= ndst_total) return;
-  uint64_t S = 0, src = 0;
-  uint32_t cnt = 0, leafsize = kLeaf, multi = 1;
-  if (lane == 0) {
-    const uint64_t tau = dtask[d];
-    uint32_t i = (uint32_t)(d - t.doff[tau]);
-    uint32_t NL = (uint32_t)t.ndst[tau], T = (uint32_t)t.total[tau];
-    uint32_t per = T / NL, ext = T - per * NL;
-    cnt = per + (i < ext);
-    src = t.out[tau] + (uint64_t)i * per + (i < ext ? i : ext);
-    if (t.type[tau] == kResize) {
-      uint64_t capn = t.capn[tau];
-      S = task_new_base(t, tau, class_start) + ((uint64_t)i << kLeafLog);
-      if (capn <= kLeaf) {
-        leafsize = (uint32_t)capn;
-        multi = 0;
-      }
-    } else {
-      S = g.base[t.u[tau]] + ((uint64_t)(t.w0[tau] + i) << kLeafLog);
+  const uint64_t tau = dtask[d];
+  const uint32_t i = (uint32_t)(d - t.doff[tau]);
+  const uint32_t NL = (uint32_t)t.ndst[tau], T = (uint32_t)t.total[tau];
+  const uint32_t per = T / NL, ext = T - per * NL;
+  const uint32_t cnt = per + (i < ext);
+  const uint64_t src = t.out[tau] + (uint64_t)i * per + (i < ext ? i : ext);
+  uint64_t S;
+  uint32_t leafsize = kLeaf;
+  bool multi = true;
+  if (t.type[tau] == kResize) {
+    const uint64_t capn = t.capn[tau];
+    S = task_new_base(t, tau, class_start) + ((uint64_t)i << kLeafLog);
+    if (capn <= kLeaf) {
+      leafsize = (uint32_t)capn;
+      multi = false;
     }
+  } else {
+    S = g.base[t.u[tau]] + ((uint64_t)(t.w0[tau] + i) << kLeafLog);
   }
-  S = __shfl_sync(0xffffffffu, S, 0);
-  src = __shfl_sync(0xffffffffu, src, 0);
-  cnt = __shfl_sync(0xffffffffu, cnt, 0);
-  leafsize = __shfl_sync(0xffffffffu, leafsize, 0);
-  multi = __shfl_sync(0xffffffffu, multi, 0);
-  if ((uint32_t)lane < leafsize)
-    g.slots[S + lane] = (uint32_t)lane < cnt ? stage[src + lane] : kEmpty;
-  if (g.vals && (uint32_t)lane < cnt) g.vals[S + lane] = t.stage_v[src + lane];
-  if (lane == 0 && multi) g.lcnt[S >> kLeafLog] = (uint8_t)cnt;
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const uint32_t p = sub + 8 * r;
+    if (p < leafsize) g.slots[S + p] = p < cnt ? stage[src + p] : kEmpty;
+    if (g.vals && p < cnt) g.vals[S + p] = t.stage_v[src + p];
+  }
+  if (sub == 0 && multi) g.lcnt[S >> kLeafLog] = (uint8_t)cnt;
 }
 
 // resized rows get their new segment; every task's row gets the new items
@@ -1923,20 +1957,30 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
 
   // 9b: apply the window / resize tasks
   if (ps.n_tasks) {
-    SST_LAUNCH_PDL(k_task_index, warp_blocks(ps.n_tasks), kTB, 0, s, dg, T, ps.n_tasks,
-               stask, dtask, titem, scnt);
-    if (ps.src_leaves) {
+    // eight lanes a task (k_task_index) and a leaf (k_gather_old,
+    // k_task_scatter); the new ids' gather writes other staging slots than
+    // the old ids', so it runs beside it on an aux stream
+    SST_LAUNCH_PDL(k_task_index, blocks_for(8 * (uint64_t)ps.n_tasks), kTB, 0, s, dg, T,
+               ps.n_tasks, stask, dtask, titem, scnt);
+    if (ps.src_leaves)
       SST_CUDA_TRY((scan<uint64_t, OpAdd>(scnt, spre, ps.src_leaves, 0ull,
                                           OpAdd{}, true, false, nullptr,
                                           g->work, s)));
-      SST_LAUNCH_PDL(k_gather_old, warp_blocks(ps.src_leaves), kTB, 0, s, dg, T,
-                 ps.n_tasks, ps.src_leaves, spre, p_x, stage, stask);
-    }
-    if (insert && ps.n_items)
+    const bool gnew = insert && ps.n_items;
+    if (gnew && ps.src_leaves) {
+      SST_CUDA_TRY(fork_aux(s, 1));
+      SST_LAUNCH_PDL(k_gather_new, blocks_for(ps.n_items), kTB, 0, g->aux[0], dg, T,
+                 ps.n_tasks, spre, p_ul, p_x, ps.n_items, stage, titem);
+    } else if (gnew) {
       SST_LAUNCH_PDL(k_gather_new, blocks_for(ps.n_items), kTB, 0, s, dg, T,
                  ps.n_tasks, spre, p_ul, p_x, ps.n_items, stage, titem);
+    }
+    if (ps.src_leaves)
+      SST_LAUNCH_PDL(k_gather_old, blocks_for(8 * ps.src_leaves), kTB, 0, s, dg, T,
+                 ps.n_tasks, ps.src_leaves, spre, p_x, stage, stask);
+    if (gnew && ps.src_leaves) SST_CUDA_TRY(join_aux(s, 1));
     if (ps.dst_leaves)
-      SST_LAUNCH_PDL(k_task_scatter, warp_blocks(ps.dst_leaves), kTB, 0, s, dg, T,
+      SST_LAUNCH_PDL(k_task_scatter, blocks_for(8 * ps.dst_leaves), kTB, 0, s, dg, T,
                  ps.n_tasks, ps.dst_leaves, cstart, stage, dtask);
     SST_LAUNCH_PDL(k_finalize, blocks_for(ps.n_tasks), kTB, 0, s, dg, T, ps.n_tasks,
                cstart);
