@@ -93,22 +93,9 @@ __device__ __forceinline__ uint64_t last_le_u64(const uint64_t *a, uint64_t n,
   return lo;
 }
 
-__device__ __forceinline__ uint32_t count_less(const uint32_t *a, uint32_t lo,
-                                               uint32_t hi, uint32_t x) {
-  uint32_t b = lo;
-  while (lo < hi) {
-    uint32_t mid = (lo + hi) >> 1;
-    if (a[mid] < x)
-      lo = mid + 1;
-    else
-      hi = mid;
-  }
-  return lo - b;
-}
-
-// count_less for four keys over the same range at once (the branchless
-// lower bound: each step halves the range for all four searches, so their
-// loads are in flight together)
+// elements of a[lo, hi) below each of four keys, found at once (the
+// branchless lower bound: each step halves the range for all four searches,
+// so their loads are in flight together)
 __device__ __forceinline__ void count_less4(const uint32_t *a, uint32_t lo, uint32_t hi,
                                             const uint32_t (&x)[4], uint32_t (&out)[4]) {
   uint32_t b[4] = {lo, lo, lo, lo};
@@ -889,6 +876,29 @@ __global__ void k_task_setup_hard(DGraph g, uint64_t inv_fill, bool insert,
   }
 }
 
+// The plan summary to the host, written by one block straight into the
+// pinned host copy (mapped), with the staging-rank error count of the batches
+// before it; a kernel follows the planning kernels at once (programmatic
+// launch), where a copy-engine transfer would start only after they finish.
+static_assert(sizeof(PlanSummary) % 8 == 0 && offsetof(PlanSummary, apply_err) % 8 == 0,
+              "the plan summary is copied as 8-byte words");
+__global__ void k_plan_out(const PlanSummary *__restrict__ P,
+                           const unsigned long long *__restrict__ err,
+                           PlanSummary *__restrict__ host) {
+  pdl_wait();
+  constexpr int kWords = (int)(sizeof(PlanSummary) / 8);
+  constexpr int kErrWord = (int)(offsetof(PlanSummary, apply_err) / 8);
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(P);
+  unsigned long long *dst = reinterpret_cast<unsigned long long *>(host);
+  for (int i = threadIdx.x; i < kWords; i += blockDim.x) dst[i] = i == kErrWord ? *err : src[i];
+}
+// the staging-rank error count alone (the end of a host-pointer call)
+__global__ void k_err_out(const unsigned long long *__restrict__ err,
+                          unsigned long long *__restrict__ host) {
+  pdl_wait();
+  if (threadIdx.x == 0) *host = *err;
+}
+
 // ---------------------------------------------------------------- step 9
 // merge_jk[t] = (first item << 32) | item count of merge group t.  A warp
 // takes 32 groups at a time: lane l first loads group l's item range and its
@@ -1110,8 +1120,15 @@ __global__ void k_gather_new(DGraph g, Tasks t, uint32_t ntasks,
   if (t.stage_v) t.stage_v[t.out[tau] + rank] = t.p_w ? t.p_w[j] : 1u;
 }
 
+// first slab slot of each capacity class's new segments (largest class
+// first), passed by value: the apply kernels need no copy of it on the device
+struct ClassStarts {
+  uint64_t s[kNumClasses];
+};
+
 __device__ __forceinline__ uint64_t task_new_base(const Tasks &t, uint64_t tau,
-                                                  const uint64_t *class_start) {
+                                                  const ClassStarts &cs) {
+  const uint64_t *class_start = cs.s;
   uint64_t capn = t.capn[tau];
   return class_start[log2_floor(capn)] + (uint64_t)t.rank[tau] * capn;
 }
@@ -1123,7 +1140,7 @@ __device__ __forceinline__ uint64_t task_new_base(const Tasks &t, uint64_t tau,
 // task holds fewer than 2^32 elements).
 __global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
                                uint64_t ndst_total,
-                               const uint64_t *__restrict__ class_start,
+                               const ClassStarts class_start,
                                const uint32_t *__restrict__ stage,
                                const uint32_t *__restrict__ dtask) {
   pdl_wait();
@@ -1162,7 +1179,7 @@ __global__ void k_task_scatter(DGraph g, Tasks t, uint32_t ntasks,
 // the task took (an insert's items are each taken by one merge group or one
 // task, and the merge kernel counts its own)
 __global__ void k_finalize(DGraph g, Tasks t, uint32_t ntasks,
-                           const uint64_t *__restrict__ class_start) {
+                           const ClassStarts class_start) {
   pdl_wait();
   uint64_t tau = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (tau >= ntasks) return;
@@ -1363,6 +1380,7 @@ sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
   g->nslots = slots;
   g->bump = 0;
   SST_CUDA_TRY(cudaMallocHost(&g->h_plan, sizeof(PlanSummary)));
+  SST_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void **>(&g->h_plan_dev), g->h_plan, 0));
   SST_CUDA_TRY(cudaMalloc(&g->d_plan, sizeof(PlanSummary)));
   SST_CUDA_TRY(cudaMalloc(&g->d_err, sizeof(unsigned long long)));
   SST_CUDA_TRY(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned long long), g->stream));
@@ -1713,11 +1731,6 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   uint32_t *p_w = wt ? A.take<uint32_t>(b) : nullptr;
   T.stage_v = nullptr;  // set with the staging below
   T.p_w = p_w;
-  uint64_t *cstart = A.take<uint64_t>(kNumClasses);
-  if (!cstart) {
-    set_error_message("update scratch sizing error");
-    return SST_ENOMEM;
-  }
 
   // 1: keys
   const uint64_t *sorted = presorted;
@@ -1871,10 +1884,7 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     SST_CUDA_TRY((scan<uint64_t, OpAdd>(T.ndst, T.doff, b, 0ull, OpAdd{}, true,
                                         false, &P->dst_leaves, A, g->aux[1], &P->n_tasks)));
     SST_CUDA_TRY(join_aux(s, 2));
-    SST_CUDA_TRY(cudaMemcpyAsync(g->h_plan, P, sizeof(PlanSummary),
-                                 cudaMemcpyDeviceToHost, s));
-    SST_CUDA_TRY(cudaMemcpyAsync(&g->h_plan->apply_err, g->d_err, 8,
-                                 cudaMemcpyDeviceToHost, s));
+    SST_LAUNCH_PDL(k_plan_out, 1, 64, 0, s, P, g->d_err, g->h_plan_dev);
     return SST_OK;
   };
 
@@ -1926,17 +1936,13 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     // the items' leaf starts (p_S) point into the old slab now, but the leaf
     // merges and deletes that read them have run already
   }
-  uint64_t hstart[kNumClasses];
+  ClassStarts cstart;
   uint64_t off = start;
   for (int c = kNumClasses - 1; c >= 0; c--) {
-    hstart[c] = off;
+    cstart.s[c] = off;
     off += (uint64_t)ps.class_cnt[c] << c;
   }
   if (grow > 0) g->bump = off;
-  uint64_t *hs = static_cast<uint64_t *>(pinned(g, sizeof(hstart)));
-  if (!hs) return SST_ENOMEM;
-  memcpy(hs, hstart, sizeof(hstart));
-  SST_CUDA_TRY(cudaMemcpyAsync(cstart, hs, sizeof(hstart), cudaMemcpyHostToDevice, s));
 
   // staging for window / resize tasks
   size_t wneed = ps.task_elems * (g->weighted ? 8 : 4) + ps.src_leaves * 20 +
@@ -2190,8 +2196,7 @@ sst_status rewrite_graph(sst_graph *g, const uint32_t *d_map, sst_graph *out) {
 // Complete the graph's stream and report a staging-rank error left by an
 // earlier batch (device-pointer updates do not wait for it).
 sst_status sync_checked(sst_graph *g) {
-  SST_CUDA_TRY(cudaMemcpyAsync(&g->h_plan->apply_err, g->d_err, 8,
-                               cudaMemcpyDeviceToHost, g->stream));
+  SST_LAUNCH_PDL(k_err_out, 1, 32, 0, g->stream, g->d_err, &g->h_plan_dev->apply_err);
   SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
   if (g->h_plan->apply_err) {
     set_error_message("internal error: %llu failed device checks (staging rank out of range)",

@@ -88,6 +88,7 @@ struct sst_graph {
   sst::Arena work;   // window / resize staging
   sst::Arena io;     // device copies of host-pointer arguments
   sst::PlanSummary *h_plan = nullptr;  // pinned
+  sst::PlanSummary *h_plan_dev = nullptr;  // h_plan's address for kernels (mapped)
   sst::PlanSummary *d_plan = nullptr;
   unsigned long long *d_err = nullptr;  // staging-rank check, read lazily
   unsigned long long *d_scan_epoch = nullptr;  // tags of captured scans
