@@ -261,6 +261,75 @@ __global__ void k_locate(const uint64_t *__restrict__ keys, uint64_t b,
   lc[i] = cw;
 }
 
+// k_locate for small batches, a warp per key (a batch of up to
+// kLocateWarpKeys keys fills about one wave of warps): the leaf search
+// probes 32 leaf heads at once, so a row of L leaves takes about log32(L)
+// dependent steps where a thread takes log2(L), and the leaf's 32 slots come
+// in with one coalesced load.  Same outputs as k_locate (the heads of a
+// segment's leaves ascend, so the leaves whose head is <= x are a prefix).
+constexpr uint64_t kLocateWarpKeys = 16384;
+__global__ void k_locate_warp(const uint64_t *__restrict__ keys, uint64_t b,
+                              int dbits, DGraph g, bool insert,
+                              uint32_t *__restrict__ flag,
+                              uint32_t *__restrict__ leaf_out,
+                              const uint32_t *__restrict__ wv,
+                              uint64_t *__restrict__ lS, uint32_t *__restrict__ lc,
+                              const uint32_t *__restrict__ nkeys) {
+  pdl_wait();
+  const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= b) return;  // whole warps
+  const uint64_t sent = (uint64_t)g.n << dbits;
+  const uint64_t nk = nkeys ? *nkeys : b;
+  const uint64_t k = i < nk ? keys[i] : sent;
+  if (k >= sent || (i + 1 < nk && keys[i + 1] == k)) {
+    if (lane == 0) {
+      flag[i] = 0;
+      leaf_out[i] = 0;
+    }
+    return;
+  }
+  const uint32_t u = (uint32_t)(k >> dbits);
+  const uint32_t x = (uint32_t)(k & ((1ull << dbits) - 1));
+  const uint64_t base = g.base[u];
+  const uint32_t cap = g.cap[u], deg = g.deg[u];
+  bool present = false;
+  uint32_t l = 0, c = 0, pos = 0;
+  uint64_t S = 0;
+  uint32_t cw = 0;
+  if (cap > 0) {
+    if (cap > kLeaf) {
+      // the answer lies in leaves [lo, lo + n); lane j probes leaf lo + j*step
+      uint32_t lo = 0, n = cap >> kLeafLog;
+      for (;;) {
+        const uint32_t step = n > 32 ? (n + 31) / 32 : 1u;
+        const uint32_t j = (uint32_t)lane * step;
+        const bool le = lane > 0 && j < n && g.slots[base + ((uint64_t)(lo + j) << kLeafLog)] <= x;
+        const uint32_t m = __ballot_sync(0xffffffffu, le);
+        const uint32_t jj = m ? 31u - __clz(m) : 0u;
+        lo += jj * step;
+        if (step == 1) break;
+        n = n - jj * step < step ? n - jj * step : step;
+      }
+      l = lo;
+    }
+    c = leaf_count(g, base, cap, deg, l);
+    S = base + ((uint64_t)l << kLeafLog);
+    const uint32_t a = (uint32_t)lane < c ? g.slots[S + lane] : kEmpty;
+    pos = __popc(__ballot_sync(0xffffffffu, a < x));
+    const uint32_t at = __shfl_sync(0xffffffffu, a, pos & 31);
+    present = pos < c && at == x;
+    cw = c | (cap > kLeaf ? kMultiLeaf : cap << kCapShift);
+  }
+  if (lane == 0) {
+    if (present && insert && wv && g.vals) g.vals[S + pos] = wv[i];
+    flag[i] = insert ? !present : present;
+    leaf_out[i] = l;
+    lS[i] = S;
+    lc[i] = cw;
+  }
+}
+
 __global__ void k_pack(const uint64_t *__restrict__ keys,
                        const uint32_t *__restrict__ flag,
                        const uint32_t *__restrict__ pos,
@@ -1817,8 +1886,12 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
     }
     // 3-5: locate, pack, group
     // sorted key in (8 B), flag and leaf out (8 B)
-    SST_LAUNCH_PDL_B(16 * b, k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg,
-                 insert, flag, leaf, wt ? wv : nullptr, lS, lc, nkeys);
+    if (b <= kLocateWarpKeys)
+      SST_LAUNCH_PDL_B(16 * b, k_locate_warp, warp_blocks(b), kTB, 0, s, sorted, b, dbits, dg,
+                   insert, flag, leaf, wt ? wv : nullptr, lS, lc, nkeys);
+    else
+      SST_LAUNCH_PDL_B(16 * b, k_locate, blocks_for(b), kTB, 0, s, sorted, b, dbits, dg,
+                   insert, flag, leaf, wt ? wv : nullptr, lS, lc, nkeys);
     SST_CUDA_TRY((scan<uint32_t, OpAdd>(flag, pos, b, 0u, OpAdd{}, true, false,
                                         &P->n_items, A, s)));
     SST_LAUNCH_PDL(k_pack, blocks_for(b), kTB, 0, s, sorted, flag, pos, leaf, b, dbits,
