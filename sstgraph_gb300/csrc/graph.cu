@@ -619,10 +619,16 @@ k_leaf_delete(DGraph g, uint32_t lo_leaf, const uint64_t *__restrict__ p_ul,
   }
 }
 
+// window density bounds by segment height H (2^H leaves, H < kBoundsH: a
+// segment holds at most 2^33 slots) and window level t <= H: entry
+// [H * kBoundsH + t] of the table, window_upper for inserts, window_lower
+// (the second table) for removes
+constexpr uint32_t kBoundsH = 32;
+
 // warp per climbing group: the smallest aligned window of 2^t leaves that
 // meets the density bound (insert: upper bound with the batch's new ids in
 // the window counted; remove: lower bound), else a resize of the segment
-__global__ void k_climb(DGraph g, PmaParams p, bool insert,
+__global__ void k_climb(DGraph g, const uint64_t *__restrict__ bound, bool insert,
                         const uint64_t *__restrict__ p_ul,
                         const uint32_t *__restrict__ g_start,
                         const uint32_t *__restrict__ d_nitems,
@@ -668,9 +674,9 @@ __global__ void k_climb(DGraph g, PmaParams p, bool insert,
       if (insert) {
         ib = warp_lb_u64(p_ul, rb, ib + 1 < re ? ib + 1 : re, kk | w0);
         ie = warp_lb_u64(p_ul, ie, re, kk | w1);
-        ok = cur + (ie - ib) <= window_upper(p, t, H);
+        ok = cur + (ie - ib) <= bound[H * kBoundsH + t];
       } else {
-        ok = cur >= window_lower(p, t, H);
+        ok = cur >= bound[H * kBoundsH + t];
       }
       if (ok) {
         type = kWindow;
@@ -1455,6 +1461,16 @@ sst_status graph_init(sst_graph *g, uint32_t height, uint32_t width,
   SST_CUDA_TRY(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned long long), g->stream));
   SST_CUDA_TRY(cudaMalloc(&g->d_scan_epoch, sizeof(unsigned long long)));
   SST_CUDA_TRY(cudaMemsetAsync(g->d_scan_epoch, 0, sizeof(unsigned long long), g->stream));
+  // the climb's density bounds per (segment height, window level), computed
+  // once here with the graph's parameters: no FP64 on the device
+  std::vector<uint64_t> wb(2 * kBoundsH * kBoundsH, 0);
+  for (uint32_t H = 0; H < kBoundsH; H++)
+    for (uint32_t t = 0; t <= H; t++) {
+      wb[H * kBoundsH + t] = window_upper(g->params, t, H);
+      wb[kBoundsH * kBoundsH + H * kBoundsH + t] = window_lower(g->params, t, H);
+    }
+  SST_CUDA_TRY(cudaMalloc(&g->d_bounds, wb.size() * 8));
+  SST_CUDA_TRY(cudaMemcpy(g->d_bounds, wb.data(), wb.size() * 8, cudaMemcpyHostToDevice));
   SST_CUDA_TRY(cudaStreamSynchronize(g->stream));
   return SST_OK;
 }
@@ -1470,6 +1486,7 @@ void graph_release(sst_graph *g) {
   cudaFree(g->d_lcnt);
   cudaFree(g->d_plan);
   cudaFree(g->d_err);
+  cudaFree(g->d_bounds);
   cudaFree(g->d_scan_epoch);
   if (g->h_plan) cudaFreeHost(g->h_plan);
   if (g->h_pinned) cudaFreeHost(g->h_pinned);
@@ -1913,7 +1930,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                  (uint32_t)window_lower(g->params, 0, 1), p_ul, p_x, p_S, p_c,
                  g_start, &P->n_groups, gtype, glev, gw0, gw1, climb, &P->n_climb);
     }
-    SST_LAUNCH_PDL(k_climb, wgrid, kTB, 0, s, dg, g->params, insert, p_ul, g_start,
+    SST_LAUNCH_PDL(k_climb, wgrid, kTB, 0, s, dg,
+               g->d_bounds + (insert ? 0 : kBoundsH * kBoundsH), insert, p_ul, g_start,
                &P->n_items, climb, &P->n_climb, gtype, glev, gw0, gw1);
     // 7-8: dominance, classification and emit.  The climb list is free
     // again: it holds the tasks that k_task_setup_hard sets up

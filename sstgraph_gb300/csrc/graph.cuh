@@ -91,6 +91,7 @@ struct sst_graph {
   sst::PlanSummary *h_plan_dev = nullptr;  // h_plan's address for kernels (mapped)
   sst::PlanSummary *d_plan = nullptr;
   unsigned long long *d_err = nullptr;  // staging-rank check, read lazily
+  uint64_t *d_bounds = nullptr;  // window density bounds (sst::window_bounds_table)
   unsigned long long *d_scan_epoch = nullptr;  // tags of captured scans
   sst::LeafDir dir;
   sst::TravState *trav = nullptr;  // traversal work lists and buffers
