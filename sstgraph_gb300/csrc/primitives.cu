@@ -199,40 +199,44 @@ __device__ __forceinline__ uint32_t tile_offset(int it) {
   return (threadIdx.x >> 5) * (ITEMS * 32) + it * 32 + (threadIdx.x & 31);
 }
 
-// Lanes of the warp holding the same 8-bit digit as this lane (valid lanes
-// only): one ballot per digit bit, each lane keeping the lanes that agree
-// with it on every bit.  Eight ballots issue far faster than one
-// __match_any_sync.
-__device__ __forceinline__ uint32_t same_digit_lanes(uint32_t d, bool valid) {
-  uint32_t m = __ballot_sync(0xffffffffu, valid);
-#pragma unroll
-  for (int b = 0; b < 8; b++) {
-    const bool on = (d >> b) & 1u;
-    const uint32_t bb = __ballot_sync(0xffffffffu, on);
-    m &= on ? bb : ~bb;
-  }
-  return m;
-}
-
 // Stable rank of each of the warp's items among the warp's earlier items of
-// the same digit.  wc (the warp's 256 counters, zero and visible to the
-// warp on entry) ends as the warp's count of each digit.  Items past the
-// end carry kNoDigit.
+// the same digit.  The lanes holding one digit find each other through a
+// warp-private word per digit in shared memory: each sets its bit with an
+// atomic OR and reads the word back (far fewer instructions than eight
+// ballots, one per digit bit, or __match_any_sync); the lowest of them then
+// advances the digit's counter and clears the word.  wc (the warp's 256
+// counters) and wm (its 256 match words) are zero and visible to the warp
+// on entry; wc ends as the warp's count of each digit, wm zero again.  Items
+// past the end carry kNoDigit.
 template <int ITEMS>
 __device__ __forceinline__ void warp_rank(const uint32_t (&dg)[ITEMS],
-                                          uint32_t (&lr)[ITEMS], uint32_t *wc) {
-  const uint32_t below = (1u << (threadIdx.x & 31)) - 1u;
+                                          uint32_t (&lr)[ITEMS], uint32_t *wc,
+                                          uint32_t *wm) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t below = (1u << lane) - 1u;
 #pragma unroll
   for (int it = 0; it < ITEMS; it++) {
     const uint32_t d = dg[it];
     const bool valid = d != kNoDigit;
-    const uint32_t peers = same_digit_lanes(d, valid);
+    if (valid) atomicOr(&wm[d], 1u << lane);
+    __syncwarp();
+    const uint32_t peers = valid ? wm[d] : 0u;
     const uint32_t c = valid ? wc[d] : 0u;
     lr[it] = c + __popc(peers & below);
     __syncwarp();
-    if (valid && (peers & below) == 0) wc[d] = c + __popc(peers);
+    if (valid && (peers & below) == 0) {
+      wc[d] = c + __popc(peers);
+      wm[d] = 0;
+    }
     __syncwarp();
   }
+}
+// a warp clears its 256 match words (then visible to the warp)
+__device__ __forceinline__ void clear_match_words(uint32_t *wm) {
+  const uint32_t lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < kRadix / 32; k++) wm[lane + 32 * k] = 0;
+  __syncwarp();
 }
 
 // Exclusive scan of one value per thread over the block, in thread order
@@ -379,8 +383,12 @@ k_scatter(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
     gbase = hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x];
     __syncthreads();
   }
+  // the match words sit in the staging area, free until the reorder (the
+  // raw form's partial-sum tables there are read: barrier above)
+  uint32_t *wm = reinterpret_cast<uint32_t *>(smem) + warp * kRadix;
+  clear_match_words(wm);
   uint32_t lr[IT];
-  warp_rank<IT>(dg, lr, wcnt[warp]);
+  warp_rank<IT>(dg, lr, wcnt[warp], wm);
   __syncthreads();
   // tile-local start of each digit, then of each warp's share of it
   uint32_t tcount = 0;
@@ -502,9 +510,12 @@ k_scatter_os(const uint64_t *__restrict__ in, uint64_t *__restrict__ out,
     if (KV) vv[it] = i < n ? vin[i] : 0u;
     dg[it] = i < n ? (uint32_t)(kk[it] >> shift) & 0xff : kNoDigit;
   }
+  // the match words sit in the staging area, free until the reorder
+  uint32_t *wm = reinterpret_cast<uint32_t *>(smem) + warp * kRadix;
+  clear_match_words(wm);
   __syncthreads();
   uint32_t lr[IT];
-  warp_rank<IT>(dg, lr, wcnt[warp]);
+  warp_rank<IT>(dg, lr, wcnt[warp], wm);
   __syncthreads();
   uint32_t tcount = 0;
 #pragma unroll
@@ -608,8 +619,10 @@ k_sort_small(uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
   __shared__ uint64_t buf[2][TILE];
   __shared__ uint32_t vbuf[KV ? 2 : 1][KV ? TILE : 1];
   __shared__ uint32_t wcnt[kWarps][kRadix];
+  __shared__ uint32_t wmatch[kWarps][kRadix];
   __shared__ uint32_t wsum[kWarps];
   const int warp = threadIdx.x >> 5;
+  clear_match_words(wmatch[warp]);  // warp_rank leaves them clear again
   for (uint64_t i = threadIdx.x; i < n; i += kThreads) {
     buf[0][i] = keys[i];
     if (KV) vbuf[0][i] = vals[i];
@@ -627,7 +640,7 @@ k_sort_small(uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
       kk[it] = o < n ? buf[cur][o] : 0;
       dg[it] = o < n ? (uint32_t)(kk[it] >> shift) & 0xff : kNoDigit;
     }
-    warp_rank<IT>(dg, lr, wcnt[warp]);
+    warp_rank<IT>(dg, lr, wcnt[warp], wmatch[warp]);
     __syncthreads();
     uint32_t tot = 0;
 #pragma unroll
