@@ -672,13 +672,15 @@ k_sort_small(uint64_t *__restrict__ keys, uint32_t *__restrict__ vals,
 constexpr int kSmallSortKV = 1024;
 
 // Keys alone (no payload: equal keys are indistinguishable, so the order
-// need not be stable) of at most kSmallSort: a bitonic sort in one CTA of
+// need not be stable) of 1025 .. kSmallSort: a bitonic sort in one CTA of
 // kBitonicThreads, each thread taking the compare-exchanges of its pairs
-// at every stage (55 stages for 1024 keys, 66 for 2048), against the six
-// rank-and-scatter passes of the radix form.  (Holding two keys a thread in
-// registers, with warp shuffles for the stages within a warp and the
-// shared array only for the rest, measured slower: 15.7 against 13.0 us
-// at 1e3 keys.)
+// at every stage (66 stages for 2048 keys).  Up to 1024 keys the one-CTA
+// radix form (k_sort_small, whose ranking by shared-memory match words is
+// cheap) is faster: 10.5 against 12.9 us at 1e3 keys (serialised); its
+// buffers for 2048 keys would pass the 48 KB of static shared memory.
+// (Holding two keys a thread in registers, with warp shuffles for the
+// stages within a warp and the shared array only for the rest, measured
+// slower than this bitonic form: 15.7 against 13.0 us at 1e3 keys.)
 constexpr int kBitonicThreads = 1024;
 static_assert(kSmallSort <= 2 * kBitonicThreads, "one pair per thread and stage");
 __global__ void __launch_bounds__(kBitonicThreads)
@@ -846,6 +848,11 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
   *result = keys;
   if (vresult) *vresult = vals;
   if (n < 2 || bits <= 0) return cudaSuccess;
+  if (!vals && n <= (uint64_t)kSmallSortKV) {
+    SST_LAUNCH_PDL_B(16 * n, (k_sort_small<false, kSmallSortKV>), 1, kThreads, 0, s, keys,
+                     (uint32_t *)nullptr, n, bits, d_n);
+    return cudaGetLastError();
+  }
   if (!vals && n <= (uint64_t)kSmallSort) {
     SST_LAUNCH_PDL_B(16 * n, k_sort_bitonic, 1, kBitonicThreads, 0, s, keys, n, d_n);
     return cudaGetLastError();

@@ -651,7 +651,8 @@ inline size_t scan_scratch_bytes(uint64_t n, size_t elem) {
 // ----------------------------------------------------------- radix sort
 // Stable LSD radix sort of 64-bit keys on their low `bits` bits, 8-bit
 // digits.  keys and tmp are both n long; *result points at whichever holds
-// the sorted keys.  Batches up to kSmallSort keys sort in one CTA.
+// the sorted keys.  Batches up to kSmallSort keys sort in one CTA (up to
+// 1024 keys by radix passes, more by a bitonic network).
 constexpr int kSmallSort = 2048;
 // the same with a 32-bit payload per key moved along (stable)
 cudaError_t radix_sort_kv(uint64_t *keys, uint64_t *tmp, uint32_t *vals,
