@@ -158,8 +158,12 @@ __global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
 // k_make_keys_packed: only the kept keys, packed to the front in any order
 // (*nkeys of them; one reservation per block of kPackItems x 256 pairs).
 // Equal keys are equal, so their order does not matter (unweighted
-// graphs), and the sort needs no bit for the sentinel row.
+// graphs), and the sort needs no bit for the sentinel row.  With V2 (the
+// pairs 8-byte aligned) a pair comes in with one 8-byte load: the warp's
+// load covers 256 contiguous bytes once, where two 4-byte loads a pair read
+// each line twice (pinned host pairs are read across the host link).
 constexpr int kPackItems = 8;
+template <bool V2>
 __global__ void __launch_bounds__(256)
 k_make_keys_packed(const uint32_t *__restrict__ pairs, uint64_t b, uint32_t n,
                    uint32_t width, int dbits, bool drop_loops,
@@ -177,8 +181,14 @@ k_make_keys_packed(const uint32_t *__restrict__ pairs, uint64_t b, uint32_t n,
     const uint64_t i = t0 + (uint64_t)k * 256 + threadIdx.x;
     uint32_t r = 0, c = 0;
     if (i < b) {
-      r = pairs[2 * i];
-      c = pairs[2 * i + 1];
+      if (V2) {
+        const uint2 rc = reinterpret_cast<const uint2 *>(pairs)[i];
+        r = rc.x;
+        c = rc.y;
+      } else {
+        r = pairs[2 * i];
+        c = pairs[2 * i + 1];
+      }
     }
     const bool ok = i < b && r < n && c < width && c != kEmpty;
     bad += i < b && !ok;
@@ -1830,10 +1840,15 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
       SST_LAUNCH_PDL_B(16 * b, k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n,
                    g->width, dbits, insert && !g->keep_loops, keys,
                    reinterpret_cast<unsigned long long *>(&P->invalid), d_w, wv);
+    else if ((reinterpret_cast<uintptr_t>(d_pairs) & 7) == 0)
+      SST_LAUNCH_PDL_NB("k_make_keys_packed", 16 * npairs, k_make_keys_packed<true>,
+                   blocks_for(npairs, kTB * kPackItems), kTB, 0, s, d_pairs, npairs, g->n,
+                   g->width, dbits, insert && !g->keep_loops, keys,
+                   reinterpret_cast<unsigned long long *>(&P->invalid), nkeys);
     else
-      SST_LAUNCH_PDL_B(16 * npairs, k_make_keys_packed, blocks_for(npairs, kTB * kPackItems),
-                   kTB, 0, s, d_pairs, npairs, g->n, g->width, dbits,
-                   insert && !g->keep_loops, keys,
+      SST_LAUNCH_PDL_NB("k_make_keys_packed", 16 * npairs, k_make_keys_packed<false>,
+                   blocks_for(npairs, kTB * kPackItems), kTB, 0, s, d_pairs, npairs, g->n,
+                   g->width, dbits, insert && !g->keep_loops, keys,
                    reinterpret_cast<unsigned long long *>(&P->invalid), nkeys);
   }
   MergeJoin join{s, nullptr};

@@ -204,6 +204,38 @@ def test_pinned_host_inputs(sg):
     w.close()
 
 
+def test_pairs_only_4_byte_aligned(sg):
+    """Pair arrays at a 4-byte (not 8-byte) aligned address, device and
+    pinned host, take the key build's two-loads-a-pair form: same graph as
+    the oracle, and the same invalid-pair counts."""
+    torch = pytest.importorskip("torch")
+    n = 1 << 12
+    rng = np.random.default_rng(33)
+    g = sg.SparseMatrixV(n)
+    o = oracle.OracleGraph(n)
+    for i, b in enumerate([3, 2000, 150000]):
+        e = rng.integers(0, n, (b, 2)).astype(np.uint32)
+        e[:5, 1] = n + 7  # out of range: counted, skipped
+        buf = torch.empty(2 * b + 1, dtype=torch.int32, device="cuda")
+        buf[1:].copy_(torch.from_numpy(e.view(np.int32).reshape(-1)))
+        dev = buf[1:]
+        assert dev.data_ptr() % 8 == 4
+        hbuf = torch.empty(2 * b + 1, dtype=torch.int32).pin_memory()
+        hbuf[1:].copy_(torch.from_numpy(e.view(np.int32).reshape(-1)))
+        host = hbuf[1:]
+        assert host.data_ptr() % 8 == 4
+        assert g.insert_batch(dev if i % 2 == 0 else host) == min(5, b)
+        o.insert_batch(e[e[:, 1] < n])  # the oracle gets the valid pairs
+        same(g, o, structure=False)
+        half = np.ascontiguousarray(e[: b // 2])
+        hb = torch.empty(2 * len(half) + 1, dtype=torch.int32, device="cuda")
+        hb[1:].copy_(torch.from_numpy(half.view(np.int32).reshape(-1)))
+        g.remove_batch(hb[1:])
+        o.remove_batch(half[half[:, 1] < n])
+        same(g, o, structure=False)
+    g.close()
+
+
 @pytest.mark.parametrize("polls", [0, 1])
 def test_scan_lookback_fallback(sg, polls):
     """The single-pass scans' bounded wait: with a poll limit of 0 every
