@@ -162,6 +162,9 @@ __global__ void k_make_keys(const uint32_t *__restrict__ pairs, uint64_t b,
 // pairs 8-byte aligned) a pair comes in with one 8-byte load: the warp's
 // load covers 256 contiguous bytes once, where two 4-byte loads a pair read
 // each line twice (pinned host pairs are read across the host link).
+// With sd.passes > 0 it also counts every radix pass's 8-bit digits of the
+// keys it keeps into sd.totals (zero on entry) and clears the sort's tile
+// status words (SortDigits): the sort then skips its own counting read.
 constexpr int kPackItems = 8;
 template <bool V2>
 __global__ void __launch_bounds__(256)
@@ -169,10 +172,12 @@ k_make_keys_packed(const uint32_t *__restrict__ pairs, uint64_t b, uint32_t n,
                    uint32_t width, int dbits, bool drop_loops,
                    uint64_t *__restrict__ keys,
                    unsigned long long *__restrict__ invalid,
-                   uint32_t *__restrict__ nkeys) {
+                   uint32_t *__restrict__ nkeys, SortDigits sd) {
   pdl_wait();
   __shared__ uint32_t s_warp[8];
   __shared__ uint32_t s_base;
+  __shared__ uint32_t s_hist[8][256];
+  for (int p = 0; p < sd.passes; p++) s_hist[p][threadIdx.x] = 0;
   const uint64_t t0 = (uint64_t)blockIdx.x * (256 * kPackItems);
   uint64_t key[kPackItems];
   uint32_t kept = 0, bad = 0;  // bit k: item k is kept
@@ -216,11 +221,23 @@ k_make_keys_packed(const uint32_t *__restrict__ pairs, uint64_t b, uint32_t n,
     }
     s_base = tot ? atomicAdd(nkeys, tot) : 0u;
   }
+  if (sd.passes) {
+#pragma unroll
+    for (int k = 0; k < kPackItems; k++)
+      if ((kept >> k) & 1u)
+        for (int p = 0; p < sd.passes; p++)
+          atomicAdd(&s_hist[p][(key[k] >> (8 * p)) & 0xff], 1u);
+    for (uint64_t i = (uint64_t)blockIdx.x * 256 + threadIdx.x; i < sd.status_words;
+         i += (uint64_t)gridDim.x * 256)
+      sd.status[i] = 0;
+  }
   __syncthreads();
   const uint64_t at = (uint64_t)s_base + s_warp[warp] + inc - keep;
 #pragma unroll
   for (int k = 0; k < kPackItems; k++)
     if ((kept >> k) & 1u) keys[at + __popc(kept & ((1u << k) - 1u))] = key[k];
+  for (int p = 0; p < sd.passes; p++)
+    if (s_hist[p][threadIdx.x]) atomicAdd(&sd.totals[p * 256 + threadIdx.x], s_hist[p][threadIdx.x]);
 }
 
 // Of a run of equal keys the last (in input order: the sort is stable) is
@@ -1831,6 +1848,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
   // 1: keys
   const uint64_t *sorted = presorted;
   uint32_t *nkeys = nullptr;
+  const int sort_bits = bits_for(g->n ? g->n - 1 : 0) + dbits;  // unweighted keys
+  SortDigits sdig;
   if (!presorted) {
     // pair in (8 B), key out (8 B)
     // unweighted keys are compacted (see k_make_keys): their rows are below
@@ -1840,16 +1859,25 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
       SST_LAUNCH_PDL_B(16 * b, k_make_keys, blocks_for(b), kTB, 0, s, d_pairs, b, g->n,
                    g->width, dbits, insert && !g->keep_loops, keys,
                    reinterpret_cast<unsigned long long *>(&P->invalid), d_w, wv);
-    else if ((reinterpret_cast<uintptr_t>(d_pairs) & 7) == 0)
-      SST_LAUNCH_PDL_NB("k_make_keys_packed", 16 * npairs, k_make_keys_packed<true>,
-                   blocks_for(npairs, kTB * kPackItems), kTB, 0, s, d_pairs, npairs, g->n,
-                   g->width, dbits, insert && !g->keep_loops, keys,
-                   reinterpret_cast<unsigned long long *>(&P->invalid), nkeys);
-    else
-      SST_LAUNCH_PDL_NB("k_make_keys_packed", 16 * npairs, k_make_keys_packed<false>,
-                   blocks_for(npairs, kTB * kPackItems), kTB, 0, s, d_pairs, npairs, g->n,
-                   g->width, dbits, insert && !g->keep_loops, keys,
-                   reinterpret_cast<unsigned long long *>(&P->invalid), nkeys);
+    else {
+      // the sort's digit counts come from the key build when the sort takes
+      // the one-sweep form (its tables taken here, before the sort's scratch)
+      if (radix_sort_digits(b, sort_bits, A, &sdig)) {
+        SST_CUDA_TRY(cudaMemsetAsync(sdig.totals, 0, (size_t)sdig.passes * 256 * 4, s));
+      } else {
+        sdig = SortDigits{};
+      }
+      if ((reinterpret_cast<uintptr_t>(d_pairs) & 7) == 0)
+        SST_LAUNCH_PDL_NB("k_make_keys_packed", 16 * npairs, k_make_keys_packed<true>,
+                     blocks_for(npairs, kTB * kPackItems), kTB, 0, s, d_pairs, npairs, g->n,
+                     g->width, dbits, insert && !g->keep_loops, keys,
+                     reinterpret_cast<unsigned long long *>(&P->invalid), nkeys, sdig);
+      else
+        SST_LAUNCH_PDL_NB("k_make_keys_packed", 16 * npairs, k_make_keys_packed<false>,
+                     blocks_for(npairs, kTB * kPackItems), kTB, 0, s, d_pairs, npairs, g->n,
+                     g->width, dbits, insert && !g->keep_loops, keys,
+                     reinterpret_cast<unsigned long long *>(&P->invalid), nkeys, sdig);
+    }
   }
   MergeJoin join{s, nullptr};
   // 9a (inserts): the leaf merges need only k_emit's output and their count
@@ -1911,8 +1939,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                                    &out, &wout));
         wv = wout;
       } else {
-        SST_CUDA_TRY(radix_sort_u64(keys, ktmp, b, bits_for(g->n ? g->n - 1 : 0) + dbits,
-                                    A, s, &out, nkeys));
+        SST_CUDA_TRY(radix_sort_u64(keys, ktmp, b, sort_bits, A, s, &out, nkeys,
+                                    sdig.passes ? &sdig : nullptr));
       }
       sorted = out;
     }

@@ -745,7 +745,8 @@ template <int IT>
 static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *vals,
                                     uint32_t *vtmp, uint64_t n, int bits, Arena &arena,
                                     cudaStream_t s, uint64_t **result,
-                                    uint32_t **vresult, const uint32_t *d_n) {
+                                    uint32_t **vresult, const uint32_t *d_n,
+                                    const SortDigits *pre) {
   constexpr int TILE = kThreads * IT;
   const uint32_t nblocks = (uint32_t)((n + TILE - 1) / TILE);
   const uint64_t hn = (uint64_t)nblocks * kRadix;
@@ -762,13 +763,21 @@ static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *val
   if (n < (1ull << 30) && passes <= 8) {
     // one sweep: all passes' digit totals in one read, then one launch a
     // pass whose tiles find their offsets by looking back
-    uint32_t *totals = arena.take<uint32_t>(8 * kRadix);
-    uint32_t *status = arena.take<uint32_t>((uint64_t)passes * hn);
-    if (!totals || !status) return cudaErrorMemoryAllocation;
-    cudaError_t e = cudaMemsetAsync(totals, 0, (size_t)passes * kRadix * 4, s);
-    if (e != cudaSuccess) return e;
-    SST_LAUNCH_PDL_NB("(k_hist_all)", 8 * n, k_hist_all<IT>, nblocks, kThreads, 0, s, src, n,
-                  passes, totals, status, (uint64_t)passes * hn, d_n);
+    uint32_t *totals, *status;
+    if (pre) {  // counted by the caller, status words cleared
+      if (pre->passes != passes || pre->status_words != (uint64_t)passes * hn)
+        return cudaErrorInvalidValue;
+      totals = pre->totals;
+      status = pre->status;
+    } else {
+      totals = arena.take<uint32_t>(8 * kRadix);
+      status = arena.take<uint32_t>((uint64_t)passes * hn);
+      if (!totals || !status) return cudaErrorMemoryAllocation;
+      cudaError_t e = cudaMemsetAsync(totals, 0, (size_t)passes * kRadix * 4, s);
+      if (e != cudaSuccess) return e;
+      SST_LAUNCH_PDL_NB("(k_hist_all)", 8 * n, k_hist_all<IT>, nblocks, kThreads, 0, s, src, n,
+                    passes, totals, status, (uint64_t)passes * hn, d_n);
+    }
     for (int p = 0; p < passes; p++) {
       const uint64_t sb = (vals ? 24 : 16) * n + 8 * (uint64_t)kRadix * nblocks;
       if (vals)
@@ -841,14 +850,38 @@ static cudaError_t radix_sort_tiles(uint64_t *keys, uint64_t *tmp, uint32_t *val
   return cudaGetLastError();
 }
 
+// the form radix_sort_impl takes: 0 none (n < 2), 1 one CTA, 2 tiles of
+// kSmallItems a thread, 3 tiles of kItems
+static int sort_form(uint64_t n, int bits, bool vals) {
+  if (n < 2 || bits <= 0) return 0;
+  if (!vals && n <= (uint64_t)kSmallSort) return 1;
+  if (vals && n <= (uint64_t)kSmallSortKV) return 1;
+  if (!vals && n <= kSmallTileKeys) return 2;
+  return 3;
+}
+
+bool radix_sort_digits(uint64_t n, int bits, Arena &arena, SortDigits *d) {
+  const int form = sort_form(n, bits, false);
+  const int passes = (bits + 7) / 8;
+  if (form < 2 || n >= (1ull << 30) || passes > 8) return false;
+  const uint64_t tile = (uint64_t)kThreads * (form == 2 ? kSmallItems : kItems);
+  const uint64_t hn = (n + tile - 1) / tile * kRadix;
+  d->totals = arena.take<uint32_t>(8 * kRadix);
+  d->status = arena.take<uint32_t>((uint64_t)passes * hn);
+  d->status_words = (uint64_t)passes * hn;
+  d->passes = passes;
+  return d->totals && d->status;
+}
+
 static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
                                    uint32_t *vals, uint32_t *vtmp, uint64_t n,
                                    int bits, Arena &arena, cudaStream_t s,
                                    uint64_t **result, uint32_t **vresult,
-                                   const uint32_t *d_n) {
+                                   const uint32_t *d_n, const SortDigits *pre = nullptr) {
   *result = keys;
   if (vresult) *vresult = vals;
   if (n < 2 || bits <= 0) return cudaSuccess;
+  if (pre && (vals || sort_form(n, bits, false) < 2)) return cudaErrorInvalidValue;
   if (!vals && n <= (uint64_t)kSmallSortKV) {
     SST_LAUNCH_PDL_B(16 * n, (k_sort_small<false, kSmallSortKV>), 1, kThreads, 0, s, keys,
                      (uint32_t *)nullptr, n, bits, d_n);
@@ -865,16 +898,16 @@ static cudaError_t radix_sort_impl(uint64_t *keys, uint64_t *tmp,
   }
   if (!vals && n <= kSmallTileKeys)
     return radix_sort_tiles<kSmallItems>(keys, tmp, vals, vtmp, n, bits, arena, s, result,
-                                         vresult, d_n);
+                                         vresult, d_n, pre);
   return radix_sort_tiles<kItems>(keys, tmp, vals, vtmp, n, bits, arena, s, result, vresult,
-                                  d_n);
+                                  d_n, pre);
 }
 
 cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
                            Arena &arena, cudaStream_t s, uint64_t **result,
-                           const uint32_t *d_n) {
+                           const uint32_t *d_n, const SortDigits *pre) {
   return radix_sort_impl(keys, tmp, nullptr, nullptr, n, bits, arena, s, result,
-                         nullptr, d_n);
+                         nullptr, d_n, pre);
 }
 
 cudaError_t radix_sort_kv(uint64_t *keys, uint64_t *tmp, uint32_t *vals,

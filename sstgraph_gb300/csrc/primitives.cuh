@@ -660,9 +660,25 @@ cudaError_t radix_sort_kv(uint64_t *keys, uint64_t *tmp, uint32_t *vals,
                           cudaStream_t s, uint64_t **result, uint32_t **vresult);
 // d_n (device, may be null): sort only the first min(n, *d_n) keys; n sizes
 // the launches, the rest of the arrays is left as it was
+// The digit counts of the one-sweep form (key-only sorts of more than
+// kSmallSort keys), when the caller produces them: every pass's 256 digit
+// totals of the keys (zero before the keys are counted) and the passes'
+// tile status words (cleared).  The update pipeline's key build counts the
+// digits of the keys it writes, so the sort skips its own counting read.
+struct SortDigits {
+  uint32_t *totals = nullptr;  // passes x 256
+  uint32_t *status = nullptr;  // status_words
+  uint64_t status_words = 0;
+  int passes = 0;
+};
+// whether radix_sort_u64 of n keys on `bits` bits takes the one-sweep form;
+// if so, its digit tables are taken from the arena into *d (call it where
+// the sort would take them: before the sort's other scratch)
+bool radix_sort_digits(uint64_t n, int bits, Arena &arena, SortDigits *d);
 cudaError_t radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
                            Arena &arena, cudaStream_t s, uint64_t **result,
-                           const uint32_t *d_n = nullptr);
+                           const uint32_t *d_n = nullptr,
+                           const SortDigits *pre = nullptr);
 size_t radix_sort_scratch_bytes(uint64_t n);
 
 }  // namespace sst
