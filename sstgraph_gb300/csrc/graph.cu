@@ -844,10 +844,10 @@ struct EmitArgs {
   const uint32_t *g_start;
   uint64_t *merge_jk;
   uint32_t *task_group;
-  DGraph g;
   uint64_t inv_fill;
   bool insert;
   const uint64_t *p_ul;
+  const uint32_t *p_c;  // items' count words (k_locate)
   const uint8_t *gtype;
   Tasks t;
   uint32_t *class_cnt, *hard, *nhard, *itask;
@@ -859,7 +859,6 @@ __device__ __forceinline__ void emit_group(const EmitArgs &a, uint64_t gid, uint
   const uint32_t *__restrict__ g_start = a.g_start;
   const uint64_t *__restrict__ p_ul = a.p_ul;
   const uint8_t *__restrict__ gtype = a.gtype;
-  const DGraph &g = a.g;
   const bool insert = a.insert;
   uint32_t *itask = a.itask;
   const int lane = threadIdx.x & 31;
@@ -882,13 +881,19 @@ __device__ __forceinline__ void emit_group(const EmitArgs &a, uint64_t gid, uint
     const uint32_t j0 = g_start[gid];
     type = gtype[gid];
     u = (uint32_t)(p_ul[j0] >> 32);
-    cap = g.cap[u];
-    simple = type != kWindow && cap <= kLeaf;  // a resize of a one-leaf (or empty) row
+    // the count word of the group's first item holds a one-leaf row's
+    // capacity and count as the batch found them (no vertex record read):
+    // an insert has not changed the row yet; a remove's one group of the
+    // row has taken its items off (all present)
+    const uint32_t cw = a.p_c[j0];
+    simple = type != kWindow && !(cw & kMultiLeaf);  // a resize of a one-leaf (or empty) row
     if (simple) {
-      deg = g.deg[u];
+      cap = one_leaf_cap(cw);
+      const uint32_t j1 = g_start[gid + 1];
+      deg = insert ? (cw & 0xff) : (cw & 0xff) - (j1 - j0);
       if (insert) {
         nb = j0;
-        ne = g_start[gid + 1];
+        ne = j1;
       }
       capn = cap_for((uint64_t)deg + (ne - nb), a.inv_fill);
       if (capn > 0) cls = log2_floor(capn);
@@ -1978,8 +1983,8 @@ static sst_status run_pipeline(sst_graph *g, const uint32_t *d_pairs,
                &P->n_items, climb, &P->n_climb, gtype, glev, gw0, gw1);
     // 7-8: dominance, classification and emit.  The climb list is free
     // again: it holds the tasks that k_task_setup_hard sets up
-    const EmitArgs ea{b, g_start, merge_jk, task_group, dg,
-                      fill_inv_q24(g->params.grow_fill), insert, p_ul, gtype, T,
+    const EmitArgs ea{b, g_start, merge_jk, task_group,
+                      fill_inv_q24(g->params.grow_fill), insert, p_ul, p_c, gtype, T,
                       P->class_cnt, climb, &P->n_hard, insert ? itask : nullptr};
     // totals land as one word on (n_merge, n_tasks), adjacent in the plan
     static_assert(offsetof(PlanSummary, n_tasks) == offsetof(PlanSummary, n_merge) + 4 &&
